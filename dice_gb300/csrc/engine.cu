@@ -1,0 +1,979 @@
+// Engine context, device Davidson solver, the variational driver and the
+// C-ABI entry points of libshci_gpu (include/shci_gpu.h).
+//
+// Davidson (replaces davidson / davidsonDirect, SHCI/Davidson.cpp:111-590):
+// the basis V and its sigma W live on the device in FP64 (column-major). Each
+// iteration forms G = V^T W (one fused Gram pass), solves the small symmetric
+// eigenproblem on the host in FP64, forms Ritz vectors X = V Q, HX = W Q and
+// residuals R = HX - lambda X on the device, and appends preconditioned,
+// orthogonalised corrections. The basis is only rotated on collapse; the
+// subspace sequence is the reference's (same maxCopies, same collapse to the
+// lowest nroots+2 Ritz vectors, corrections orthogonalised against the whole
+// basis before the collapse). Block mode adds one correction per unconverged
+// root and applies sigma to all of them in one k-vector launch.
+//
+// Mixed precision: sigma runs in FP32 (FP32 CSR values and vectors, FP32
+// accumulation, FP64 diagonal term) until the residual tolerance is met; the
+// solve then restarts from the converged Ritz vectors with sigma in FP64
+// (FP32 head + FP32 tail of every element), which refines the Ritz pairs and
+// yields FP64 Rayleigh quotients.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <numeric>
+
+#include "../../include/shci_gpu.h"
+#include "ham.h"
+#include "host_io.h"
+
+namespace shci {
+
+std::atomic<int64_t> g_launch_count{0};
+
+static inline unsigned grid_for(size_t n, int threads, size_t max_blocks = 152 * 32) {
+  size_t b = (n + threads - 1) / threads;
+  if (b < 1) b = 1;
+  if (b > max_blocks) b = max_blocks;
+  return (unsigned)b;
+}
+
+static double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// Dense symmetric eigensolver (cyclic Jacobi), ascending eigenvalues; A is
+// m x m row-major, evecs column-major (column c = eigenvector c).
+static void sym_eig(int m, std::vector<double> A, std::vector<double>& evals, std::vector<double>& evecs) {
+  std::vector<double> V((size_t)m * m, 0.0);
+  for (int i = 0; i < m; ++i) V[(size_t)i * m + i] = 1.0;
+  for (int sweep = 0; sweep < 100; ++sweep) {
+    double off = 0.0, diag = 0.0;
+    for (int p = 0; p < m; ++p) {
+      diag += A[(size_t)p * m + p] * A[(size_t)p * m + p];
+      for (int q = p + 1; q < m; ++q) off += A[(size_t)p * m + q] * A[(size_t)p * m + q];
+    }
+    if (off <= 1e-32 * diag || off < 1e-300) break;
+    for (int p = 0; p < m; ++p)
+      for (int q = p + 1; q < m; ++q) {
+        const double apq = A[(size_t)p * m + q];
+        if (apq == 0.0) continue;
+        const double app = A[(size_t)p * m + p], aqq = A[(size_t)q * m + q];
+        const double theta = (aqq - app) / (2.0 * apq);
+        const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+        for (int k = 0; k < m; ++k) {
+          double akp = A[(size_t)k * m + p], akq = A[(size_t)k * m + q];
+          A[(size_t)k * m + p] = c * akp - s * akq;
+          A[(size_t)k * m + q] = s * akp + c * akq;
+        }
+        for (int k = 0; k < m; ++k) {
+          double apk = A[(size_t)p * m + k], aqk = A[(size_t)q * m + k];
+          A[(size_t)p * m + k] = c * apk - s * aqk;
+          A[(size_t)q * m + k] = s * apk + c * aqk;
+        }
+        for (int k = 0; k < m; ++k) {
+          double vkp = V[(size_t)k * m + p], vkq = V[(size_t)k * m + q];
+          V[(size_t)k * m + p] = c * vkp - s * vkq;
+          V[(size_t)k * m + q] = s * vkp + c * vkq;
+        }
+      }
+  }
+  std::vector<int> ord(m);
+  std::iota(ord.begin(), ord.end(), 0);
+  std::stable_sort(ord.begin(), ord.end(),
+                   [&](int x, int y) { return A[(size_t)x * m + x] < A[(size_t)y * m + y]; });
+  evals.resize(m);
+  evecs.assign((size_t)m * m, 0.0);
+  for (int c = 0; c < m; ++c) {
+    evals[c] = A[(size_t)ord[c] * m + ord[c]];
+    for (int i = 0; i < m; ++i) evecs[(size_t)c * m + i] = V[(size_t)i * m + ord[c]];
+  }
+}
+
+__global__ void k_cmax(const double* __restrict__ ci, size_t ld, int nroots, size_t n, double* __restrict__ out) {
+  for (size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int r = 0; r < nroots; ++r) {
+      double c = fabs(ci[(size_t)r * ld + j]);
+      s = __dadd_rn(s, __dmul_rn(c, c));
+    }
+    out[j] = sqrt(s);
+  }
+}
+
+__global__ void k_append(const Det2* __restrict__ src, size_t n, Det2* __restrict__ dst) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+
+struct IterLog {
+  int64_t ndets;
+  double energy;
+  int dav_iters;
+  double seconds;
+};
+
+struct Context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+
+  HostInts hints;
+  HostHeatBath hhb;
+  bool have_ints = false;
+  DevBuf<double> dI1, dI2, dDirect, dExchange, dSingles;
+  DevBuf<float> dSameVal, dOppVal;
+  DevBuf<int16_t> dSamePairs, dOppPairs;
+  DevBuf<int64_t> dSameStart, dOppStart;
+  SelectParams sp;
+
+  DevBuf<Det2> dets;
+  size_t ndet = 0;
+  DetHash hash;
+  Helpers helpers;
+  bool helpers_ok = false;
+  Csr H;
+  int ham_mode = -1;
+  bool ham_ok = false;
+  DevBuf<double> diag;
+  size_t ndiag = 0;
+  Prims prims;
+  DevBuf<int64_t> counter;
+  DevBuf<Det2> cand;
+
+  // Davidson workspace
+  DevBuf<double> V, W, Vt, Wt, X, Y, R, D, xb64, yb64, gpart, dG, dQ, dlam, dsmall;
+  DevBuf<float> xb32;
+
+  // run state
+  DevBuf<double> ci, cmax;
+  int nroots_run = 0;
+  std::vector<IterLog> log;
+  double t_select = 0, t_ham = 0, t_dav = 0, t_total = 0, t_sigma = 0;
+  int64_t n_sigma = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+  ~Context() {
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  IntsView ints() const { return IntsView{dI1.p, dI2.p, dDirect.p, dExchange.p, hints.norb}; }
+  HeatBathView hb() const {
+    return HeatBathView{dSameVal.p, dSamePairs.p, dSameStart.p, dOppVal.p, dOppPairs.p, dOppStart.p, dSingles.p};
+  }
+  void require_ints() const {
+    if (!have_ints) throw Error(kErrState, "no integrals loaded (call shci_read_fcidump first)");
+  }
+  void require_dets() const {
+    if (ndet == 0) throw Error(kErrState, "determinant space is empty");
+  }
+
+  template <class T>
+  void upload(DevBuf<T>& b, const std::vector<T>& h) {
+    b.resize(h.size() ? h.size() : 1);
+    if (!h.empty())
+      SHCI_CUDA(cudaMemcpyAsync(b.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, stream));
+  }
+
+  void load_fcidump(const std::string& path) {
+    HostInts hi;
+    read_fcidump(path, hi);
+    HostHeatBath hb;
+    build_heatbath(hi, hb);
+    hints = std::move(hi);
+    hhb = std::move(hb);
+    upload(dI1, hints.I1);
+    upload(dI2, hints.I2);
+    upload(dDirect, hints.Direct);
+    upload(dExchange, hints.Exchange);
+    upload(dSingles, hhb.singles);
+    upload(dSameVal, hhb.sameVal);
+    upload(dOppVal, hhb.oppVal);
+    upload(dSamePairs, hhb.samePairs);
+    upload(dOppPairs, hhb.oppPairs);
+    upload(dSameStart, hhb.sameStart);
+    upload(dOppStart, hhb.oppStart);
+    SHCI_CUDA(cudaStreamSynchronize(stream));
+    have_ints = true;
+    ndet = 0;
+    helpers_ok = ham_ok = false;
+    ndiag = 0;
+  }
+
+  void invalidate_space() {
+    helpers_ok = false;
+    ham_ok = false;
+  }
+
+  void set_dets(const uint64_t* h, int64_t n) {
+    require_ints();
+    if (n < 0) throw Error(kErrInvalid, "negative determinant count");
+    const int n2 = 2 * hints.norb;
+    for (int64_t i = 0; i < n; ++i) {
+      uint64_t w0 = h[2 * i], w1 = h[2 * i + 1];
+      int ne = __builtin_popcountll(w0) + __builtin_popcountll(w1);
+      if (ne != hints.nelec) throw Error(kErrInvalid, "determinant " + std::to_string(i) + " has wrong electron count");
+      if (n2 < 128) {
+        uint64_t lim0 = n2 >= 64 ? ~0ull : ((1ull << n2) - 1ull);
+        uint64_t lim1 = n2 > 64 ? ((1ull << (n2 - 64)) - 1ull) : 0ull;
+        if ((w0 & ~lim0) || (w1 & ~lim1))
+          throw Error(kErrInvalid, "determinant " + std::to_string(i) + " occupies orbitals beyond NORB");
+      }
+    }
+    dets.resize(n > 0 ? (size_t)n : 1);
+    if (n) SHCI_CUDA(cudaMemcpyAsync(dets.p, h, (size_t)n * sizeof(Det2), cudaMemcpyHostToDevice, stream));
+    ndet = (size_t)n;
+    ndiag = 0;
+    invalidate_space();
+    SHCI_CUDA(cudaStreamSynchronize(stream));
+  }
+
+  // Heat-bath selection from every current determinant; appends new ones.
+  int64_t select(const double* cmax_dev, double eps1) {
+    require_ints();
+    require_dets();
+    hash.build(dets.p, ndet, stream);
+    counter.resize(1);
+    int64_t cap = (int64_t)std::max<size_t>(cand.cap, std::max<size_t>((size_t)1 << 20, 4 * ndet));
+    cand.reserve((size_t)cap);
+    cap = (int64_t)cand.cap;
+    int64_t total = select_candidates(dets.p, cmax_dev, ndet, eps1, ints(), hb(), hints.maxEntry, sp, hash, cand.p,
+                                      cap, counter.p, stream);
+    if (total > cap) {
+      cand.release();
+      cand.reserve((size_t)total + total / 8);
+      cap = (int64_t)cand.cap;
+      total = select_candidates(dets.p, cmax_dev, ndet, eps1, ints(), hb(), hints.maxEntry, sp, hash, cand.p, cap,
+                                counter.p, stream);
+      if (total > cap) throw Error(kErrState, "candidate count changed between passes");
+    }
+    size_t nnew = 0;
+    if (total > 0) {
+      sort_dets(cand.p, nullptr, (size_t)total, prims, stream);
+      nnew = unique_dets(cand.p, (size_t)total, prims, stream);
+    }
+    if (nnew) {
+      if (ndet + nnew >= (size_t)0x7fffffff) throw Error(kErrInvalid, "determinant space exceeds 2^31 entries");
+      dets.grow_keep(ndet + nnew, stream);
+      k_append<<<grid_for(nnew, 256), 256, 0, stream>>>(cand.p, nnew, dets.p + ndet);
+      SHCI_LAUNCH_CHECK();
+      ndet += nnew;
+      invalidate_space();
+    }
+    SHCI_CUDA(cudaStreamSynchronize(stream));
+    return (int64_t)nnew;
+  }
+
+  void ensure_diag() {
+    require_dets();
+    if (ndiag >= ndet) return;
+    diag.grow_keep(ndet, stream);
+    compute_diag(dets.p + ndiag, ndet - ndiag, ints(), diag.p + ndiag, stream);
+    ndiag = ndet;
+  }
+
+  void build_ham(int mode) {
+    require_ints();
+    require_dets();
+    if (mode < 0 || mode > 2) throw Error(kErrInvalid, "unknown Hamiltonian mode");
+    if (!helpers_ok) {
+      helpers.build(dets.p, ndet, hints.norb, prims, stream);
+      helpers_ok = true;
+    }
+    ensure_diag();
+    if (mode == SHCI_MODE_DIRECT) {
+      H.col.release();
+      H.v64.release();
+      H.vhi.release();
+      H.vlo.release();
+      H.rowptr.release();
+      H.N = ndet;
+      H.nnz = 0;
+    } else {
+      build_ham_csr(helpers, dets.p, ints(), H, mode == SHCI_MODE_FP64, mode == SHCI_MODE_MIXED,
+                    mode == SHCI_MODE_MIXED, prims, stream);
+    }
+    ham_mode = mode;
+    ham_ok = true;
+    SHCI_CUDA(cudaStreamSynchronize(stream));
+  }
+
+  // Y[:, yc0 + c] = H A[:, c0 + c], c < k, in the given sigma mode.
+  void apply_sigma(int mode, const double* A, size_t lda, int c0, int k, double* Yp, size_t ldy, int yc0) {
+    if (!ham_ok) throw Error(kErrState, "Hamiltonian not built for the current space (call shci_ham_build)");
+    if (mode == SHCI_MODE_DIRECT && !helpers_ok) throw Error(kErrState, "string tables missing");
+    if (mode != SHCI_MODE_DIRECT && ham_mode == SHCI_MODE_DIRECT)
+      throw Error(kErrState, "Hamiltonian was built matrix-free; stored sigma unavailable");
+    if (mode == SHCI_MODE_MIXED && ham_mode != SHCI_MODE_MIXED)
+      throw Error(kErrState, "mixed sigma needs a Hamiltonian built in mixed mode");
+    const size_t N = ndet;
+    SHCI_CUDA(cudaEventRecord(ev0, stream));
+    for (int done = 0; done < k;) {
+      const int kk = std::min(4, k - done);
+      const int kp = kk == 3 ? 4 : kk;
+      if (mode == SHCI_MODE_MIXED) {
+        xb32.reserve(N * kp);
+        pack_f32(A, lda, c0 + done, kk, kp, N, xb32.p, stream);
+        sigma_csr_mixed(H, diag.p, xb32.p, kp, kk, Yp + (size_t)(yc0 + done) * ldy, ldy, stream);
+      } else if (mode == SHCI_MODE_FP64) {
+        xb64.reserve(N * kp);
+        pack_f64(A, lda, c0 + done, kk, kp, N, xb64.p, stream);
+        sigma_csr_f64(H, diag.p, xb64.p, kp, kk, Yp + (size_t)(yc0 + done) * ldy, ldy, H.v64.p == nullptr, stream);
+      } else {
+        xb64.reserve(N * kp);
+        yb64.reserve(N * kp);
+        pack_f64(A, lda, c0 + done, kk, kp, N, xb64.p, stream);
+        sigma_direct(helpers, dets.p, ints(), diag.p, xb64.p, yb64.p, kp, stream);
+        unpack_f64(yb64.p, kp, kk, N, Yp, ldy, yc0 + done, stream);
+      }
+      done += kk;
+    }
+    SHCI_CUDA(cudaEventRecord(ev1, stream));
+    SHCI_CUDA(cudaEventSynchronize(ev1));
+    float ms = 0.f;
+    SHCI_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+    t_sigma += ms * 1e-3;
+    n_sigma += 1;
+  }
+
+  // ---- Davidson -----------------------------------------------------------
+  std::vector<double> gram_host(const double* A, size_t lda, int ma, const double* B, size_t ldb, int mb) {
+    dG.reserve((size_t)ma * mb);
+    ts_gram(A, lda, ma, B, ldb, mb, ndet, dG.p, gpart, stream);
+    std::vector<double> g((size_t)ma * mb);
+    SHCI_CUDA(cudaMemcpyAsync(g.data(), dG.p, g.size() * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    SHCI_CUDA(cudaStreamSynchronize(stream));
+    return g;
+  }
+  void to_dev(DevBuf<double>& b, const std::vector<double>& h) {
+    b.reserve(h.size());
+    SHCI_CUDA(cudaMemcpyAsync(b.p, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
+  }
+  void fill_random(double* col, uint64_t seed) {
+    std::vector<double> h(ndet);
+    uint64_t s = seed * 0x9E3779B97F4A7C15ull + 1;
+    for (auto& v : h) {
+      s ^= s << 13;
+      s ^= s >> 7;
+      s ^= s << 17;
+      v = ((s >> 11) * (1.0 / 9007199254740992.0)) * 2.0 - 1.0;
+    }
+    SHCI_CUDA(cudaMemcpyAsync(col, h.data(), ndet * sizeof(double), cudaMemcpyHostToDevice, stream));
+    SHCI_CUDA(cudaStreamSynchronize(stream));
+  }
+  // col_j -= (col_i . col_j) col_i  (device-only)
+  void project_out(const double* ci_, double* cj) {
+    dsmall.reserve(4);
+    ts_gram(ci_, ndet, 1, cj, ndet, 1, ndet, dsmall.p, gpart, stream);
+    ts_gemm(ci_, ndet, 1, dsmall.p, 1, ndet, -1.0, 1.0, cj, ndet, stream);
+  }
+  double norm_host(const double* c) {
+    auto g = gram_host(c, ndet, 1, c, ndet, 1);
+    return std::sqrt(g[0]);
+  }
+  void scale_col(double* c, double s) {
+    to_dev(dsmall, std::vector<double>{s});
+    scale_cols(c, ndet, dsmall.p, 1, ndet, stream);
+  }
+
+  // One Davidson solve in a fixed sigma mode. x: device N x nroots (ld N).
+  void davidson_core(int mode, bool block, int nroots, double* x, int maxCopies, double tol, bool direct_rules,
+                     std::vector<double>& E, int& numIter) {
+    const size_t N = ndet;
+    if (nroots < 1) throw Error(kErrInvalid, "nroots must be >= 1");
+    if ((size_t)nroots > N) throw Error(kErrInvalid, "more roots than determinants");
+    int mmax = std::max(maxCopies, nroots + 1);
+    if (mmax > 16) mmax = 16;
+    if ((size_t)mmax > N) mmax = (int)N;
+    if (nroots > 16) throw Error(kErrInvalid, "at most 16 roots");
+    V.reserve(N * mmax);
+    W.reserve(N * mmax);
+    Vt.reserve(N * mmax);
+    Wt.reserve(N * mmax);
+    X.reserve(N * nroots);
+    Y.reserve(N * nroots);
+    R.reserve(N * nroots);
+    D.reserve(N * nroots);
+    // initial block (SHCI/Davidson.cpp:156-180)
+    SHCI_CUDA(cudaMemcpyAsync(V.p, x, N * nroots * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+    for (int i = 0; i < nroots; ++i) {
+      double* bi = V.p + (size_t)i * N;
+      if (norm_host(bi) < 1.e-10) {
+        fill_random(bi, 1000 + i);
+        scale_col(bi, 1.0 / norm_host(bi));
+      }
+    }
+    for (int i = 0; i < nroots; ++i) {
+      double* bi = V.p + (size_t)i * N;
+      for (int j = 0; j < i; ++j) project_out(V.p + (size_t)j * N, bi);
+      if (norm_host(bi) < 1e-8) fill_random(bi, 2000 + i);
+      for (int j = 0; j < i; ++j) project_out(V.p + (size_t)j * N, bi);
+      scale_col(bi, 1.0 / norm_host(bi));
+    }
+    apply_sigma(mode, V.p, N, 0, nroots, W.p, N, 0);
+    int m = nroots;
+    numIter = 0;
+    int cR = 0;
+    const int soft_cap = (direct_rules ? 400 : 800) * nroots;
+    const int hard_cap = (direct_rules ? 400 : 2000) * nroots;
+    std::vector<double> lam, Q;
+    while (true) {
+      // Rayleigh-Ritz (SHCI/Davidson.cpp:250-269)
+      std::vector<double> G = gram_host(V.p, N, m, W.p, N, m);
+      std::vector<double> hs((size_t)m * m);
+      for (int i = 0; i < m; ++i)
+        for (int j = i; j < m; ++j) hs[(size_t)i * m + j] = hs[(size_t)j * m + i] = G[(size_t)i + (size_t)j * m];
+      sym_eig(m, hs, lam, Q);
+      to_dev(dQ, Q);
+      std::vector<double> lr(lam.begin(), lam.begin() + nroots);
+      to_dev(dlam, lr);
+      ts_gemm(V.p, N, m, dQ.p, nroots, N, 1.0, 0.0, X.p, N, stream);
+      ts_gemm(W.p, N, m, dQ.p, nroots, N, 1.0, 0.0, Y.p, N, stream);
+      residual(X.p, Y.p, dlam.p, nroots, N, N, R.p, stream);
+      std::vector<double> RR = gram_host(R.p, N, nroots, R.p, N, nroots);
+      std::vector<double> rn(nroots);
+      for (int c = 0; c < nroots; ++c) rn[c] = std::sqrt(std::max(0.0, RR[(size_t)c * nroots + c]));
+      numIter++;
+      auto finish = [&]() {
+        E.assign(lam.begin(), lam.begin() + nroots);
+        SHCI_CUDA(cudaMemcpyAsync(x, X.p, N * nroots * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+        SHCI_CUDA(cudaStreamSynchronize(stream));
+      };
+      if ((size_t)m == N) {
+        finish();
+        return;
+      }
+      std::vector<int> act;
+      std::vector<double> act_lam;
+      if (!block) {
+        // root-by-root scheme of the reference (SHCI/Davidson.cpp:271-323)
+        const double ei = lam[cR];
+        bool back = false;
+        for (int i = 0; i < cR; ++i)
+          if (rn[i] > tol) {
+            cR = i;
+            back = true;
+            break;
+          }
+        double error = rn[cR];
+        if (back) {
+          // the reference keeps the old eigenvalue for the residual here
+          to_dev(dsmall, std::vector<double>{ei});
+          residual(X.p + (size_t)cR * N, Y.p + (size_t)cR * N, dsmall.p, 1, N, N, R.p + (size_t)cR * N, stream);
+          error = norm_host(R.p + (size_t)cR * N);
+        }
+        const int rootForR = cR;
+        if (error < tol || numIter > soft_cap) {
+          if (numIter > hard_cap)
+            throw Error(kErrNoConv, "Davidson calculation did not converge for root " + std::to_string(cR + 1));
+          cR++;
+          if (cR == nroots) {
+            finish();
+            return;
+          }
+        }
+        act.push_back(rootForR);
+        act_lam.push_back(ei);
+      } else {
+        for (int c = 0; c < nroots; ++c)
+          if (!(rn[c] < tol)) {
+            act.push_back(c);
+            act_lam.push_back(lam[c]);
+          }
+        if (act.empty() || numIter > soft_cap) {
+          if (!act.empty() && numIter > hard_cap) throw Error(kErrNoConv, "block Davidson did not converge");
+          finish();
+          return;
+        }
+      }
+      const int nact = (int)act.size();
+      for (int a = 0; a < nact; ++a)
+        SHCI_CUDA(cudaMemcpyAsync(D.p + (size_t)a * N, R.p + (size_t)act[a] * N, N * sizeof(double),
+                                  cudaMemcpyDeviceToDevice, stream));
+      to_dev(dlam, act_lam);
+      precondition(diag.p, dlam.p, nact, N, D.p, N, stream);
+      // orthogonalise against the whole basis (two classical Gram-Schmidt passes)
+      dG.reserve((size_t)m * nact);
+      for (int pass = 0; pass < 2; ++pass) {
+        ts_gram(V.p, N, m, D.p, N, nact, N, dG.p, gpart, stream);
+        ts_gemm(V.p, N, m, dG.p, nact, N, -1.0, 1.0, D.p, N, stream);
+      }
+      int kept = 0;
+      for (int a = 0; a < nact; ++a) {
+        double* da = D.p + (size_t)a * N;
+        for (int b = 0; b < kept; ++b) project_out(D.p + (size_t)b * N, da);
+        double nrm = norm_host(da);
+        if (!(nrm > 1e-14)) continue;  // linearly dependent correction
+        scale_col(da, 1.0 / nrm);
+        if (kept != a)
+          SHCI_CUDA(cudaMemcpyAsync(D.p + (size_t)kept * N, da, N * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+        ++kept;
+      }
+      if (kept == 0) {  // nothing new to add: the subspace is exhausted
+        finish();
+        return;
+      }
+      if (m + kept > mmax) {
+        int keep = block ? mmax - kept : std::min(nroots + 2, mmax - kept);
+        if (keep < nroots) keep = nroots;
+        ts_gemm(V.p, N, m, dQ.p, keep, N, 1.0, 0.0, Vt.p, N, stream);
+        ts_gemm(W.p, N, m, dQ.p, keep, N, 1.0, 0.0, Wt.p, N, stream);
+        V.swap(Vt);
+        W.swap(Wt);
+        m = keep;
+      }
+      SHCI_CUDA(cudaMemcpyAsync(V.p + (size_t)m * N, D.p, (size_t)kept * N * sizeof(double),
+                                cudaMemcpyDeviceToDevice, stream));
+      apply_sigma(mode, V.p, N, m, kept, W.p, N, m);
+      m += kept;
+    }
+  }
+
+  void davidson(int mode, bool block, int nroots, double* x, int maxCopies, double tol, bool direct_rules,
+                std::vector<double>& E, int& iters) {
+    if (!ham_ok) throw Error(kErrState, "Hamiltonian not built for the current space (call shci_ham_build)");
+    ensure_diag();
+    if (mode == SHCI_MODE_MIXED) {
+      int it1 = 0, it2 = 0;
+      davidson_core(SHCI_MODE_MIXED, block, nroots, x, maxCopies, tol, direct_rules, E, it1);
+      davidson_core(SHCI_MODE_FP64, block, nroots, x, maxCopies, tol, direct_rules, E, it2);
+      iters = it1 + it2;
+    } else {
+      davidson_core(mode, block, nroots, x, maxCopies, tol, direct_rules, E, iters);
+    }
+  }
+
+  // ---- variational driver (SHCIbasics::DoVariational) -----------------------
+  void run(const Schedule& s, int mode, bool block, std::vector<double>& Eout) {
+    require_ints();
+    const double t0 = now_s();
+    t_select = t_ham = t_dav = t_sigma = 0;
+    n_sigma = 0;
+    log.clear();
+    if (s.direct) mode = SHCI_MODE_DIRECT;
+    // selection parameters
+    sp.ncore = s.ncore;
+    sp.nact = s.nact;
+    sp.nrestrict = (int)s.restrictions.size();
+    for (int r = 0; r < sp.nrestrict; ++r) {
+      sp.rmin[r] = s.restrictions[r].minElec;
+      sp.rmax[r] = s.restrictions[r].maxElec;
+      uint64_t m0 = 0, m1 = 0;
+      for (int k = 0; k < 64; ++k)
+        if ((s.restrictions[r].mask >> k) & 1ull) {
+          for (int spn = 0; spn < 2; ++spn) {
+            int p = 2 * k + spn;
+            if (p < 64)
+              m0 |= 1ull << p;
+            else
+              m1 |= 1ull << (p - 64);
+          }
+        }
+      sp.rmask0[r] = m0;
+      sp.rmask1[r] = m1;
+    }
+    // reference determinants and initial ci (SHCI/SHCI.cpp:289-399)
+    std::vector<uint64_t> hd;
+    int lowest = 0;
+    double lowestE = 1e300;
+    for (size_t d = 0; d < s.occupied.size(); ++d) {
+      uint64_t w[2] = {0, 0};
+      if ((int)s.occupied[d].size() != hints.nelec)
+        throw Error(kErrInvalid, "The number of electrons given in the FCIDUMP should be equal to the nocc given in the shci input file.");
+      for (int p : s.occupied[d]) {
+        if (p < 0 || p >= 2 * hints.norb) throw Error(kErrInvalid, "orbital index out of range in nocc");
+        if ((w[p >> 6] >> (p & 63)) & 1ull)
+          throw Error(kErrInvalid, "orbital " + std::to_string(p) + " appears twice in input determinant number " +
+                                       std::to_string(d));
+        w[p >> 6] |= 1ull << (p & 63);
+      }
+      for (size_t e = 0; e < d; ++e)
+        if (hd[2 * e] == w[0] && hd[2 * e + 1] == w[1])
+          throw Error(kErrInvalid, "Determinant appears twice in the input determinant list.");
+      hd.push_back(w[0]);
+      hd.push_back(w[1]);
+      double E = 0.0;
+      {
+        std::vector<int> cl;
+        for (int p = 0; p < 2 * hints.norb; ++p)
+          if ((w[p >> 6] >> (p & 63)) & 1ull) cl.push_back(p);
+        const int n2 = 2 * hints.norb;
+        for (size_t i = 0; i < cl.size(); ++i) {
+          E += hints.I1[(size_t)cl[i] * n2 + cl[i]];
+          for (size_t j = i + 1; j < cl.size(); ++j) {
+            E += hints.Direct[(size_t)(cl[i] / 2) * hints.norb + cl[j] / 2];
+            if ((cl[i] % 2) == (cl[j] % 2)) E -= hints.Exchange[(size_t)(cl[i] / 2) * hints.norb + cl[j] / 2];
+          }
+        }
+      }
+      if (E < lowestE) {
+        lowestE = E;
+        lowest = (int)d;
+      }
+    }
+    if (s.occupied.empty()) throw Error(kErrInvalid, "nocc keyword has to be included.");
+    set_dets(hd.data(), (int64_t)s.occupied.size());
+    const int nroots = s.nroots;
+    if (nroots < 1 || nroots > 16) throw Error(kErrInvalid, "nroots must be in 1..16");
+    nroots_run = nroots;
+    {
+      const size_t n0 = ndet;
+      std::vector<double> c0(n0 * nroots, 0.0);
+      for (size_t j = 0; j < n0; ++j) c0[j] = 1.0;
+      c0[lowest] += (double)n0;
+      double nn = 0.0;
+      for (size_t j = 0; j < n0; ++j) nn += c0[j] * c0[j];
+      nn = std::sqrt(nn);
+      for (size_t j = 0; j < n0; ++j) c0[j] /= nn;
+      ci.resize(n0 * nroots);
+      SHCI_CUDA(cudaMemcpyAsync(ci.p, c0.data(), c0.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
+    }
+    std::vector<double> E0(nroots, 0.0);
+    DevBuf<double> X0;
+    for (size_t iter = 0; iter < s.epsilon1.size(); ++iter) {
+      const double eps1 = s.epsilon1[iter];
+      const size_t N0 = ndet;
+      double ta = now_s();
+      cmax.resize(N0);
+      k_cmax<<<grid_for(N0, 256), 256, 0, stream>>>(ci.p, N0, nroots, N0, cmax.p);
+      SHCI_LAUNCH_CHECK();
+      select(cmax.p, eps1);
+      const size_t N = ndet;
+      // X0 = [ci; 0]
+      X0.resize(N * nroots);
+      SHCI_CUDA(cudaMemsetAsync(X0.p, 0, N * nroots * sizeof(double), stream));
+      for (int r = 0; r < nroots; ++r)
+        SHCI_CUDA(cudaMemcpyAsync(X0.p + (size_t)r * N, ci.p + (size_t)r * N0, N0 * sizeof(double),
+                                  cudaMemcpyDeviceToDevice, stream));
+      double tb = now_s();
+      t_select += tb - ta;
+      build_ham(mode);
+      double tc = now_s();
+      t_ham += tc - tb;
+      const double prevE0 = (iter == 0) ? -10.0 : E0[0];
+      int numIter = 0;
+      const int maxCopies = block ? std::max(nroots + 4, 3 * nroots) : (s.direct ? nroots + 2 : nroots + 4);
+      davidson(mode, block, nroots, X0.p, maxCopies, s.davidsonTolLoose, s.direct, E0, numIter);
+      ci.swap(X0);
+      double td = now_s();
+      t_dav += td - tc;
+      log.push_back({(int64_t)N, E0[0] + hints.coreE, numIter, td - t0});
+      if (std::fabs(E0[0] - prevE0) < s.dE || iter == s.epsilon1.size() - 1) {
+        davidson(mode, block, nroots, ci.p, block ? std::max(nroots + 4, 3 * nroots) : nroots + 4, s.davidsonTol,
+                 s.direct, E0, numIter);
+        t_dav += now_s() - td;
+        break;
+      }
+    }
+    Eout.resize(nroots);
+    for (int r = 0; r < nroots; ++r) Eout[r] = E0[r] + hints.coreE;
+    t_total = now_s() - t0;
+  }
+};
+
+}  // namespace shci
+
+// ===========================================================================
+// C-ABI
+// ===========================================================================
+using shci::Context;
+using shci::Error;
+
+struct shci_ctx {
+  Context c;
+};
+
+namespace {
+thread_local std::string g_create_error;
+
+template <class F>
+int guarded(shci_ctx* ctx, F&& f) {
+  if (!ctx) return SHCI_ERR_INVALID;
+  try {
+    ctx->c.err.clear();
+    cudaSetDevice(ctx->c.device);
+    f(ctx->c);
+    return SHCI_OK;
+  } catch (const Error& e) {
+    ctx->c.err = e.what();
+    return e.code;
+  } catch (const std::exception& e) {
+    ctx->c.err = e.what();
+    return SHCI_ERR_INVALID;
+  }
+}
+}  // namespace
+
+extern "C" {
+
+int shci_ctx_create(int device, shci_ctx** out) {
+  if (!out) return SHCI_ERR_INVALID;
+  *out = nullptr;
+  try {
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) {
+      cudaGetLastError();
+      g_create_error = "no CUDA device available";
+      return SHCI_ERR_CUDA;
+    }
+    if (device < 0 || device >= ndev) {
+      g_create_error = "device index out of range";
+      return SHCI_ERR_INVALID;
+    }
+    std::unique_ptr<shci_ctx> ctx(new shci_ctx());
+    ctx->c.device = device;
+    SHCI_CUDA(cudaSetDevice(device));
+    SHCI_CUDA(cudaStreamCreateWithFlags(&ctx->c.stream, cudaStreamNonBlocking));
+    SHCI_CUDA(cudaEventCreate(&ctx->c.ev0));
+    SHCI_CUDA(cudaEventCreate(&ctx->c.ev1));
+    *out = ctx.release();
+    return SHCI_OK;
+  } catch (const Error& e) {
+    g_create_error = e.what();
+    return e.code;
+  }
+}
+
+int shci_ctx_destroy(shci_ctx* ctx) {
+  if (!ctx) return SHCI_ERR_INVALID;
+  cudaSetDevice(ctx->c.device);
+  cudaStreamSynchronize(ctx->c.stream);
+  delete ctx;
+  return SHCI_OK;
+}
+
+const char* shci_last_error(shci_ctx* ctx) { return ctx ? ctx->c.err.c_str() : g_create_error.c_str(); }
+
+void* shci_ctx_stream(shci_ctx* ctx) { return ctx ? (void*)ctx->c.stream : nullptr; }
+
+int shci_set_alloc_cap(shci_ctx* ctx, uint64_t bytes) {
+  return guarded(ctx, [&](Context&) { shci::g_alloc_cap = (size_t)bytes; });
+}
+
+int shci_read_fcidump(shci_ctx* ctx, const char* path, int* norb, int* nelec, double* coreE) {
+  return guarded(ctx, [&](Context& c) {
+    if (!path) throw Error(SHCI_ERR_INVALID, "null path");
+    c.load_fcidump(path);
+    if (norb) *norb = c.hints.norb;
+    if (nelec) *nelec = c.hints.nelec;
+    if (coreE) *coreE = c.hints.coreE;
+  });
+}
+
+int shci_heatbath_export(shci_ctx* ctx, int which, int64_t* count, float* vals, int16_t* pairs, int64_t* starts,
+                         double* singles) {
+  return guarded(ctx, [&](Context& c) {
+    c.require_ints();
+    const auto& V = which ? c.hhb.sameVal : c.hhb.oppVal;
+    const auto& P = which ? c.hhb.samePairs : c.hhb.oppPairs;
+    const auto& S = which ? c.hhb.sameStart : c.hhb.oppStart;
+    if (count) *count = (int64_t)V.size();
+    if (vals) std::memcpy(vals, V.data(), V.size() * sizeof(float));
+    if (pairs) std::memcpy(pairs, P.data(), P.size() * sizeof(int16_t));
+    if (starts) std::memcpy(starts, S.data(), S.size() * sizeof(int64_t));
+    if (singles) std::memcpy(singles, c.hhb.singles.data(), c.hhb.singles.size() * sizeof(double));
+  });
+}
+
+int shci_set_selection_params(shci_ctx* ctx, int ncore, int nact, int nrestrict, const int* rmin, const int* rmax,
+                              const uint64_t* spatial_masks) {
+  return guarded(ctx, [&](Context& c) {
+    if (nrestrict < 0 || nrestrict > shci::kMaxRestrict) throw Error(SHCI_ERR_INVALID, "at most 4 restrictions");
+    if (ncore < 0 || nact < 0) throw Error(SHCI_ERR_INVALID, "ncore/nact must be >= 0");
+    c.sp.ncore = ncore;
+    c.sp.nact = nact;
+    c.sp.nrestrict = nrestrict;
+    for (int r = 0; r < nrestrict; ++r) {
+      c.sp.rmin[r] = rmin[r];
+      c.sp.rmax[r] = rmax[r];
+      uint64_t m0 = 0, m1 = 0;
+      for (int k = 0; k < 64; ++k)
+        if ((spatial_masks[r] >> k) & 1ull)
+          for (int s = 0; s < 2; ++s) {
+            int p = 2 * k + s;
+            if (p < 64) m0 |= 1ull << p; else m1 |= 1ull << (p - 64);
+          }
+      c.sp.rmask0[r] = m0;
+      c.sp.rmask1[r] = m1;
+    }
+  });
+}
+
+int shci_dets_set(shci_ctx* ctx, const uint64_t* dets, int64_t n) {
+  return guarded(ctx, [&](Context& c) {
+    if (n > 0 && !dets) throw Error(SHCI_ERR_INVALID, "null determinant array");
+    c.set_dets(dets, n);
+  });
+}
+
+int shci_dets_count(shci_ctx* ctx, int64_t* n) {
+  return guarded(ctx, [&](Context& c) { *n = (int64_t)c.ndet; });
+}
+
+int shci_dets_get(shci_ctx* ctx, uint64_t* out, int64_t cap) {
+  return guarded(ctx, [&](Context& c) {
+    if (cap < (int64_t)c.ndet) throw Error(SHCI_ERR_INVALID, "output buffer too small");
+    if (c.ndet)
+      SHCI_CUDA(cudaMemcpyAsync(out, c.dets.p, c.ndet * sizeof(shci::Det2), cudaMemcpyDeviceToHost, c.stream));
+    SHCI_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+
+int shci_select(shci_ctx* ctx, const double* cmax, double eps1, int64_t* n_new) {
+  return guarded(ctx, [&](Context& c) {
+    c.require_dets();
+    if (!cmax) throw Error(SHCI_ERR_INVALID, "null cmax");
+    c.cmax.resize(c.ndet);
+    SHCI_CUDA(cudaMemcpyAsync(c.cmax.p, cmax, c.ndet * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    int64_t k = c.select(c.cmax.p, eps1);
+    if (n_new) *n_new = k;
+  });
+}
+
+int shci_ham_build(shci_ctx* ctx, int mode, int64_t* nnz) {
+  return guarded(ctx, [&](Context& c) {
+    c.build_ham(mode);
+    if (nnz) *nnz = c.H.nnz;
+  });
+}
+
+int shci_ham_export(shci_ctx* ctx, int64_t* rowptr, int32_t* col, double* val) {
+  return guarded(ctx, [&](Context& c) {
+    if (!c.ham_ok || c.ham_mode == SHCI_MODE_DIRECT) throw Error(SHCI_ERR_STATE, "no stored Hamiltonian");
+    const size_t N = c.H.N, nnz = (size_t)c.H.nnz;
+    SHCI_CUDA(cudaMemcpyAsync(rowptr, c.H.rowptr.p, (N + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, c.stream));
+    if (nnz) {
+      SHCI_CUDA(cudaMemcpyAsync(col, c.H.col.p, nnz * sizeof(int32_t), cudaMemcpyDeviceToHost, c.stream));
+      if (c.H.v64.p) {
+        SHCI_CUDA(cudaMemcpyAsync(val, c.H.v64.p, nnz * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        SHCI_CUDA(cudaStreamSynchronize(c.stream));
+      } else {
+        std::vector<float> hi(nnz), lo(nnz);
+        SHCI_CUDA(cudaMemcpyAsync(hi.data(), c.H.vhi.p, nnz * sizeof(float), cudaMemcpyDeviceToHost, c.stream));
+        SHCI_CUDA(cudaMemcpyAsync(lo.data(), c.H.vlo.p, nnz * sizeof(float), cudaMemcpyDeviceToHost, c.stream));
+        SHCI_CUDA(cudaStreamSynchronize(c.stream));
+        for (size_t i = 0; i < nnz; ++i) val[i] = (double)hi[i] + (double)lo[i];
+      }
+    }
+    SHCI_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+
+int shci_diag(shci_ctx* ctx, double* out) {
+  return guarded(ctx, [&](Context& c) {
+    c.require_ints();
+    c.ensure_diag();
+    if (out)
+      SHCI_CUDA(cudaMemcpyAsync(out, c.diag.p, c.ndet * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    SHCI_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+
+int shci_sigma(shci_ctx* ctx, int mode, const double* x, double* y, int k) {
+  return guarded(ctx, [&](Context& c) {
+    if (k < 1 || k > 4) throw Error(SHCI_ERR_INVALID, "k must be in 1..4");
+    if (!x || !y) throw Error(SHCI_ERR_INVALID, "null vector");
+    const size_t N = c.ndet;
+    c.X.reserve(N * k);
+    c.Y.reserve(N * k);
+    SHCI_CUDA(cudaMemcpyAsync(c.X.p, x, N * k * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    c.ensure_diag();
+    c.apply_sigma(mode, c.X.p, N, 0, k, c.Y.p, N, 0);
+    SHCI_CUDA(cudaMemcpyAsync(y, c.Y.p, N * k * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    SHCI_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+
+int shci_sigma_device(shci_ctx* ctx, int mode, const double* x_dev, double* y_dev, int k, int64_t ld) {
+  return guarded(ctx, [&](Context& c) {
+    if (k < 1 || k > 4) throw Error(SHCI_ERR_INVALID, "k must be in 1..4");
+    if (ld < (int64_t)c.ndet) throw Error(SHCI_ERR_INVALID, "leading dimension smaller than N");
+    c.ensure_diag();
+    c.apply_sigma(mode, x_dev, (size_t)ld, 0, k, y_dev, (size_t)ld, 0);
+  });
+}
+
+int shci_davidson(shci_ctx* ctx, int mode, int block, int nroots, double* x0, int max_copies, double tol, double* E,
+                  int* iters) {
+  return guarded(ctx, [&](Context& c) {
+    if (!x0 || !E) throw Error(SHCI_ERR_INVALID, "null argument");
+    const size_t N = c.ndet;
+    shci::DevBuf<double> x;
+    x.resize(N * nroots);
+    SHCI_CUDA(cudaMemcpyAsync(x.p, x0, N * nroots * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    std::vector<double> ev;
+    int it = 0;
+    c.davidson(mode, block != 0, nroots, x.p, max_copies, tol, false, ev, it);
+    SHCI_CUDA(cudaMemcpyAsync(x0, x.p, N * nroots * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    SHCI_CUDA(cudaStreamSynchronize(c.stream));
+    for (int r = 0; r < nroots; ++r) E[r] = ev[r];
+    if (iters) *iters = it;
+  });
+}
+
+int shci_run_input(shci_ctx* ctx, const char* input_path, const char* fcidump, int mode, int block, double* E,
+                   int cap_roots, int* nroots) {
+  return guarded(ctx, [&](Context& c) {
+    if (!input_path) throw Error(SHCI_ERR_INVALID, "null input path");
+    shci::Schedule s;
+    shci::read_input(input_path, s);
+    std::string dir = input_path;
+    size_t slash = dir.find_last_of('/');
+    dir = slash == std::string::npos ? std::string(".") : dir.substr(0, slash);
+    std::string fd = fcidump ? std::string(fcidump)
+                             : (s.integralFile.size() && s.integralFile[0] == '/' ? s.integralFile
+                                                                                   : dir + "/" + s.integralFile);
+    c.load_fcidump(fd);
+    if (mode < 0) mode = s.mode >= 0 ? s.mode : SHCI_MODE_FP64;
+    if (block < 0) block = s.block ? 1 : 0;
+    std::vector<double> ev;
+    c.run(s, mode, block != 0, ev);
+    if (nroots) *nroots = (int)ev.size();
+    for (int r = 0; r < (int)ev.size() && r < cap_roots; ++r) E[r] = ev[r];
+  });
+}
+
+int shci_run_log(shci_ctx* ctx, int cap, int* niter, int64_t* ndets, double* energy, int* dav_iters,
+                 double* seconds) {
+  return guarded(ctx, [&](Context& c) {
+    if (niter) *niter = (int)c.log.size();
+    for (int i = 0; i < (int)c.log.size() && i < cap; ++i) {
+      if (ndets) ndets[i] = c.log[i].ndets;
+      if (energy) energy[i] = c.log[i].energy;
+      if (dav_iters) dav_iters[i] = c.log[i].dav_iters;
+      if (seconds) seconds[i] = c.log[i].seconds;
+    }
+  });
+}
+
+int shci_run_ci(shci_ctx* ctx, double* out, int64_t cap) {
+  return guarded(ctx, [&](Context& c) {
+    const size_t n = c.ndet * (size_t)c.nroots_run;
+    if (cap < (int64_t)n) throw Error(SHCI_ERR_INVALID, "output buffer too small");
+    SHCI_CUDA(cudaMemcpyAsync(out, c.ci.p, n * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    SHCI_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+
+int shci_run_timings(shci_ctx* ctx, double* t_select, double* t_ham, double* t_davidson, double* t_total,
+                     int64_t* n_sigma, double* t_sigma) {
+  return guarded(ctx, [&](Context& c) {
+    if (t_select) *t_select = c.t_select;
+    if (t_ham) *t_ham = c.t_ham;
+    if (t_davidson) *t_davidson = c.t_dav;
+    if (t_total) *t_total = c.t_total;
+    if (n_sigma) *n_sigma = c.n_sigma;
+    if (t_sigma) *t_sigma = c.t_sigma;
+  });
+}
+
+int shci_launch_count(shci_ctx* ctx, int64_t* n) {
+  return guarded(ctx, [&](Context&) { *n = shci::g_launch_count.load(); });
+}
+
+}  // extern "C"

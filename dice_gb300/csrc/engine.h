@@ -1,0 +1,123 @@
+// Host-side declarations shared by the CUDA translation units of libshci_gpu.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "shci_common.cuh"
+#include "status.h"
+
+namespace shci {
+
+#define SHCI_CUDA(call)                                                                         \
+  do {                                                                                          \
+    cudaError_t e_ = (call);                                                                    \
+    if (e_ != cudaSuccess) {                                                                    \
+      throw ::shci::Error(e_ == cudaErrorMemoryAllocation ? ::shci::kErrOOM : ::shci::kErrCuda, \
+                          std::string(#call) + ": " + cudaGetErrorString(e_));                  \
+    }                                                                                           \
+  } while (0)
+
+// Number of kernel launches issued by the library (every launch site ends with
+// SHCI_LAUNCH_CHECK()).
+extern std::atomic<int64_t> g_launch_count;
+#define SHCI_LAUNCH_CHECK()                                                   \
+  do {                                                                        \
+    ::shci::g_launch_count.fetch_add(1, std::memory_order_relaxed);           \
+    SHCI_CUDA(cudaGetLastError());                                            \
+  } while (0)
+
+// Device allocation cap (bytes) for out-of-memory emulation in tests; 0 = off.
+extern size_t g_alloc_cap;
+extern size_t g_alloc_live;
+void* dev_alloc(size_t bytes);
+void dev_free(void* p, size_t bytes);
+
+// Owning device buffer.
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;    // elements in use
+  size_t cap = 0;  // elements allocated
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) dev_free(p, cap * sizeof(T));
+    p = nullptr;
+    n = cap = 0;
+  }
+  // Ensure room for `count` elements; contents are not preserved.
+  void reserve(size_t count) {
+    if (count <= cap) return;
+    release();
+    size_t c = count < 16 ? 16 : count;
+    p = static_cast<T*>(dev_alloc(c * sizeof(T)));
+    cap = c;
+  }
+  void resize(size_t count) {
+    reserve(count);
+    n = count;
+  }
+  // Grow keeping the first `n` elements.
+  void grow_keep(size_t count, cudaStream_t s) {
+    if (count <= cap) {
+      n = count;
+      return;
+    }
+    size_t c = count + count / 2;
+    T* q = static_cast<T*>(dev_alloc(c * sizeof(T)));
+    if (p && n) SHCI_CUDA(cudaMemcpyAsync(q, p, n * sizeof(T), cudaMemcpyDeviceToDevice, s));
+    SHCI_CUDA(cudaStreamSynchronize(s));
+    if (p) dev_free(p, cap * sizeof(T));
+    p = q;
+    cap = c;
+    n = count;
+  }
+  size_t bytes() const { return n * sizeof(T); }
+  void swap(DevBuf& o) {
+    std::swap(p, o.p);
+    std::swap(n, o.n);
+    std::swap(cap, o.cap);
+  }
+};
+
+// Temporaries of the device primitives, owned by one context (calls on one
+// context are serialised on its stream). Each primitive has its own buffers so
+// that nested calls (sort -> scan) never share storage.
+struct Prims {
+  DevBuf<unsigned char> scan_lvl[4];  // block sums per recursion level
+  DevBuf<uint64_t> sort_k0, sort_k1;  // alternate key words
+  DevBuf<uint32_t> sort_v;            // alternate payload
+  DevBuf<uint32_t> sort_hist;         // per-tile digit counts
+  DevBuf<uint32_t> sort_glob;         // 16 x 256 global digit histogram
+  DevBuf<int64_t> uniq_flag, uniq_pos;
+  DevBuf<unsigned char> small;        // small host<->device transfers
+};
+
+// ---- primitives (kernels_core.cu) -----------------------------------------
+void scan_exclusive_i64(const int64_t* in, int64_t* out, size_t n, int64_t* total_host, Prims& pr,
+                        cudaStream_t s);
+void scan_exclusive_u32(const uint32_t* in, uint32_t* out, size_t n, Prims& pr, cudaStream_t s);
+// Stable sort of determinants in Dice's order (signed words, top word first),
+// optionally carrying a uint32 payload (vals may be null). Sorted in place.
+void sort_dets(Det2* keys, uint32_t* vals, size_t n, Prims& pr, cudaStream_t s);
+// Stable sort of uint64 keys (unsigned order) with a uint32 payload, in place.
+void sort_u64(uint64_t* keys, uint32_t* vals, size_t n, Prims& pr, cudaStream_t s);
+// Remove adjacent duplicates of sorted determinants; returns the new count.
+size_t unique_dets(Det2* keys, size_t n, Prims& pr, cudaStream_t s);
+
+// Determinant hash set over indices into a determinant array.
+struct DetHash {
+  DevBuf<uint32_t> slots;
+  uint64_t mask = 0;
+  void build(const Det2* dets, size_t n, cudaStream_t s);
+};
+
+}  // namespace shci

@@ -1,0 +1,120 @@
+// Device data structures of the determinant space and the Hamiltonian.
+#pragma once
+#include "engine.h"
+
+namespace shci {
+
+// Plain-pointer view passed to kernels.
+struct HelperView {
+  size_t N;
+  const uint64_t* astr;  // alpha string of each determinant
+  const uint64_t* bstr;  // beta string of each determinant
+  const uint32_t* aidx;  // determinant -> alpha group
+  const uint32_t* bidx;  // determinant -> beta group
+  const int64_t* aStart;  // alpha group g spans [aStart[g], aStart[g+1])
+  const uint32_t* aDets;  // determinant indices grouped by alpha string (AlphaMajorToDet)
+  const uint64_t* aGroupB;  // beta string of aDets[p] (AlphaMajorToBeta)
+  const int64_t* bStart;
+  const uint32_t* bDets;    // BetaMajorToDet
+  const uint64_t* bGroupA;  // BetaMajorToAlpha
+  const int64_t* aSingStart;  // SinglesFromAlpha as CSR over alpha groups
+  const uint32_t* aSing;
+};
+
+// Alpha/beta string tables of one determinant space
+// (HamHelpers2, SHCI/SHCImakeHamiltonian.h:44-82).
+struct Helpers {
+  size_t N = 0;
+  int64_t NA = 0, NB = 0, nsing = 0;
+  DevBuf<uint64_t> astr, bstr, ua, ub, aGroupB, bGroupA;
+  DevBuf<uint32_t> aidx, bidx, aDets, bDets, aSing;
+  DevBuf<int64_t> aStart, bStart, aSingStart;
+  void build(const Det2* dets, size_t n, int norb, Prims& pr, cudaStream_t s);
+  HelperView view() const {
+    return HelperView{N, astr.p, bstr.p, aidx.p, bidx.p, aStart.p, aDets.p, aGroupB.p,
+                      bStart.p, bDets.p, bGroupA.p, aSingStart.p, aSing.p};
+  }
+  size_t bytes() const {
+    return astr.bytes() + bstr.bytes() + ua.bytes() + ub.bytes() + aGroupB.bytes() + bGroupA.bytes() +
+           aidx.bytes() + bidx.bytes() + aDets.bytes() + bDets.bytes() + aSing.bytes() + aStart.bytes() +
+           bStart.bytes() + aSingStart.bytes();
+  }
+};
+
+// Off-diagonal Hamiltonian as full-row CSR (both triangles); the diagonal is
+// kept separately in FP64. Values are FP64 (v64) for the plain path, or an
+// FP32 head (vhi) plus an FP32 tail (vlo = h - (double)vhi) for the mixed path,
+// so that vhi + vlo reproduces the FP64 element to about 2^-48 relative.
+struct Csr {
+  size_t N = 0;
+  int64_t nnz = 0;
+  DevBuf<int64_t> rowptr;
+  DevBuf<int32_t> col;
+  DevBuf<double> v64;
+  DevBuf<float> vhi, vlo;
+  size_t bytes() const { return rowptr.bytes() + col.bytes() + v64.bytes() + vhi.bytes() + vlo.bytes(); }
+};
+
+void build_ham_csr(const Helpers& hp, const Det2* dets, const IntsView& ints, Csr& H, bool want64, bool want32,
+                   bool want_lo, Prims& pr, cudaStream_t s);
+void compute_diag(const Det2* dets, size_t n, const IntsView& ints, double* diag, cudaStream_t s);
+void sigma_direct(const Helpers& hp, const Det2* dets, const IntsView& ints, const double* diag, const double* x,
+                  double* y, int k, cudaStream_t s);
+
+// ---- selection (kernels_select.cu) -----------------------------------------
+struct HeatBathView {
+  const float* sameVal;
+  const int16_t* samePairs;
+  const int64_t* sameStart;
+  const float* oppVal;
+  const int16_t* oppPairs;
+  const int64_t* oppStart;
+  const double* singles;  // (2n)x(2n)
+};
+
+constexpr int kMaxRestrict = 4;
+struct SelectParams {
+  int ncore = 0;
+  int nact = 1000000;
+  int nrestrict = 0;
+  int rmin[kMaxRestrict];
+  int rmax[kMaxRestrict];
+  uint64_t rmask0[kMaxRestrict];  // spin-orbital masks, bits 0..63
+  uint64_t rmask1[kMaxRestrict];  // bits 64..127
+};
+
+// Candidates from every parent, dropping those already present (hash set);
+// returns the number of candidates written (may exceed cap: then nothing past
+// cap is written and the caller retries with a larger buffer).
+int64_t select_candidates(const Det2* dets, const double* cmax, size_t n, double eps1, const IntsView& ints,
+                          const HeatBathView& hb, double maxEntry, const SelectParams& sp, const DetHash& present,
+                          Det2* out, int64_t cap, int64_t* d_counter, cudaStream_t s);
+
+// ---- sigma and Davidson vector kernels (kernels_sigma.cu) -------------------
+// Y[:, c] (column-major, leading dimension ldy) = diag .* X[:, c] + Hoff X[:, c]
+// for c < k, where X is row-interleaved [N][kp] in the path's precision.
+void sigma_csr_mixed(const Csr& H, const double* diag, const float* x32, int kp, int k, double* y, size_t ldy,
+                     cudaStream_t s);
+void sigma_csr_f64(const Csr& H, const double* diag, const double* x64, int kp, int k, double* y, size_t ldy,
+                   bool use_hilo, cudaStream_t s);
+// Pack columns [c0, c0+k) of column-major A (lda) into row-interleaved [N][kp]
+// (zero padded) in FP32 or FP64.
+void pack_f32(const double* A, size_t lda, int c0, int k, int kp, size_t N, float* out, cudaStream_t s);
+void pack_f64(const double* A, size_t lda, int c0, int k, int kp, size_t N, double* out, cudaStream_t s);
+void unpack_f64(const double* in, int kp, int k, size_t N, double* A, size_t lda, int c0, cudaStream_t s);
+// Tall-skinny products over column-major N x m blocks (deterministic order):
+// G (ma x mb, column-major) = A^T B.
+void ts_gram(const double* A, size_t lda, int ma, const double* B, size_t ldb, int mb, size_t N, double* G,
+             DevBuf<double>& part, cudaStream_t s);
+// Y = alpha * A Q + beta * Y, Q (m x k column-major, device).
+void ts_gemm(const double* A, size_t lda, int m, const double* Q, int k, size_t N, double alpha, double beta,
+             double* Y, size_t ldy, cudaStream_t s);
+// R[:, c] = Y[:, c] - lam[c] X[:, c]
+void residual(const double* X, const double* Y, const double* lam, int k, size_t N, size_t ld, double* R,
+              cudaStream_t s);
+// R[:, c] /= (lam[c] - diag) with the reference's 1e-12 guard
+void precondition(const double* diag, const double* lam, int k, size_t N, double* R, size_t ld, cudaStream_t s);
+// A[:, c] *= scale[c]
+void scale_cols(double* A, size_t ld, const double* scale, int k, size_t N, cudaStream_t s);
+
+}  // namespace shci

@@ -1,0 +1,52 @@
+// Host-side integrals, heat-bath tables and input schedule.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "status.h"
+
+namespace shci {
+
+struct HostInts {
+  int norb = 0, nelec = 0;
+  double coreE = 0.0, maxEntry = 0.0;
+  std::vector<double> I1;  // (2n)x(2n) spin-orbital
+  std::vector<double> I2;  // 8-fold packed spatial
+  std::vector<double> Direct, Exchange;
+  double i2(int i, int j, int k, int l) const;  // spin-orbital accessor
+};
+
+struct HostHeatBath {
+  std::vector<float> sameVal, oppVal;
+  std::vector<int16_t> samePairs, oppPairs;
+  std::vector<int64_t> sameStart, oppStart;
+  std::vector<double> singles;
+};
+
+struct Restriction {
+  int minElec = 0, maxElec = 10000;
+  uint64_t mask = 0;  // spatial orbitals
+};
+
+// Variational subset of the reference's schedule (SHCI/input.h:35-194).
+struct Schedule {
+  std::vector<std::vector<int>> occupied;
+  std::vector<double> epsilon1;
+  int nroots = 1;
+  double davidsonTol = 5e-5, davidsonTolLoose = 5e-5, dE = 1e-8;
+  bool direct = false;
+  int ncore = 0, nact = 1000000;
+  std::vector<Restriction> restrictions;
+  std::string integralFile = "FCIDUMP";
+  int mode = -1;       // precision keyword: -1 unset, 0 fp64, 1 mixed
+  bool block = false;  // blockdavidson keyword
+};
+
+void split_tokens(const std::string& in, const char* delims, std::vector<std::string>& tok);
+bool iequal(const std::string& a, const std::string& b);
+void read_fcidump(const std::string& path, HostInts& H);
+void build_heatbath(const HostInts& H, HostHeatBath& hb);
+void read_input(const std::string& path, Schedule& s);
+
+}  // namespace shci

@@ -1,0 +1,227 @@
+// Heat-bath selection of new determinants, one warp per parent determinant.
+// Restates SHCIgetdeterminants::getDeterminantsVariationalApprox
+// (SHCI/SHCIgetdeterminants.cpp:586-739) as called from the parent loop of
+// DoVariational (SHCI/SHCIbasics.cpp:969-982) with threshold eps1/|cMax_i|:
+//   singles: for occupied i, empty a (ncore/nact and restriction filters):
+//            bound Singles(a,i) > eps, then the exact FP64 Hij_1Excite > eps;
+//   doubles: for occupied pairs i > j, the heat-bath list of the pair is
+//            scanned while |v| >= eps (list sorted by |float| descending).
+// The prefix length of each pair list is found by binary search, and the
+// (pair, entry) work is flattened across the 32 lanes.
+// Candidates already in the variational space are dropped by a hash lookup
+// (the reference's binary_search over SortedDets); sort + unique follow.
+#include <cmath>
+
+#include "ham.h"
+
+namespace shci {
+
+struct SelArgs {
+  const Det2* dets;
+  const double* cmax;
+  size_t n;
+  double eps1;
+  IntsView ints;
+  HeatBathView hb;
+  double maxEntry;
+  SelectParams sp;
+  const uint32_t* hslots;
+  uint64_t hmask;
+  Det2* out;
+  int64_t cap;
+  int64_t* counter;
+};
+
+constexpr int kSelThreads = 256;
+constexpr int kSelWarps = kSelThreads / 32;
+
+__device__ __forceinline__ bool hash_contains(const uint32_t* __restrict__ slots, uint64_t mask,
+                                              const Det2* __restrict__ dets, const Det2& x) {
+  uint64_t h = det_hash(x) & mask;
+  for (uint64_t probe = 0; probe <= mask; ++probe) {
+    uint32_t s = slots[h];
+    if (s == 0xffffffffu) return false;
+    Det2 y = dets[s];
+    if (det_eq(x, y)) return true;
+    h = (h + 1) & mask;
+  }
+  return false;
+}
+
+__device__ __forceinline__ int in_mask(const SelectParams& sp, int r, int p) {
+  return p < 64 ? (int)((sp.rmask0[r] >> p) & 1ull) : (int)((sp.rmask1[r] >> (p - 64)) & 1ull);
+}
+
+// Warp-aggregated append of one candidate per lane with `emit` set.
+__device__ __forceinline__ void append(const SelArgs& a, bool emit, const Det2& cand) {
+  const int lane = threadIdx.x & 31;
+  unsigned m = __ballot_sync(kFull, emit);
+  if (!m) return;
+  int leader = __ffs(m) - 1;
+  int64_t base = 0;
+  if (lane == leader) base = atomicAdd((unsigned long long*)a.counter, (unsigned long long)__popc(m));
+  base = __shfl_sync(kFull, base, leader);
+  if (emit) {
+    int64_t q = base + __popc(m & ((1u << lane) - 1u));
+    if (q < a.cap) a.out[q] = cand;
+  }
+}
+
+__global__ void __launch_bounds__(kSelThreads) k_select(SelArgs a) {
+  __shared__ unsigned char s_closed[kSelWarps][kMaxSpin];
+  __shared__ unsigned char s_open[kSelWarps][kMaxSpin];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  unsigned char* closed = s_closed[wib];
+  unsigned char* open = s_open[wib];
+  const int n2 = 2 * a.ints.norb;
+  const int64_t warps = (int64_t)gridDim.x * kSelWarps;
+  const SelectParams& sp = a.sp;
+  for (int64_t p = (int64_t)blockIdx.x * kSelWarps + wib; p < (int64_t)a.n; p += warps) {
+    const Det2 d = a.dets[p];
+    const double eps = a.eps1 / fabs(a.cmax[p]);
+    if (!(eps < INFINITY)) continue;  // |c| = 0: nothing passes any threshold
+    __syncwarp();
+    if (lane == 0) {
+      int nc = 0, no = 0;
+      for (int q = 0; q < n2; ++q) {
+        if (det_getocc(d, q))
+          closed[nc++] = (unsigned char)q;
+        else
+          open[no++] = (unsigned char)q;
+      }
+    }
+    __syncwarp();
+    const int nclosed = __popcll(d.w0) + __popcll(d.w1);
+    const int nopen = n2 - nclosed;
+    int cur[kMaxRestrict];
+    for (int r = 0; r < sp.nrestrict; ++r) cur[r] = __popcll(d.w0 & sp.rmask0[r]) + __popcll(d.w1 & sp.rmask1[r]);
+
+    // ---- singles
+    const int ns = nclosed * nopen;
+    for (int base = 0; base < ns; base += 32) {
+      const int q = base + lane;
+      bool emit = false;
+      Det2 cand = d;
+      if (q < ns) {
+        const int ci = closed[q / nopen], oa = open[q % nopen];
+        bool ok = (ci >> 1) >= sp.ncore && (oa >> 1) < sp.ncore + sp.nact;
+        for (int r = 0; ok && r < sp.nrestrict; ++r) {
+          int e = cur[r] - in_mask(sp, r, ci) + in_mask(sp, r, oa);
+          ok = e >= sp.rmin[r] && e <= sp.rmax[r];
+        }
+        if (ok) {
+          double integral = a.hb.singles[(size_t)oa * n2 + ci];
+          if (fabs(integral) > eps)
+            if ((ci & 1) == (oa & 1)) integral = hij_single(a.ints, d, oa, ci);
+          if (fabs(integral) > eps) {
+            det_flip(cand, oa);
+            det_flip(cand, ci);
+            emit = !hash_contains(a.hslots, a.hmask, a.dets, cand);
+          }
+        }
+      }
+      append(a, emit, cand);
+    }
+
+    // ---- doubles
+    if (fabs(a.maxEntry) < eps) continue;
+    const int npairs = nclosed * (nclosed - 1) / 2;
+    for (int pb = 0; pb < npairs; pb += 32) {
+      const int q = pb + lane;
+      int ci = 0, cj = 0;
+      int64_t lstart = 0, len = 0;
+      bool same = false;
+      if (q < npairs) {
+        // q -> (i, j), i > j, q = i(i-1)/2 + j
+        int i = (int)((1.0 + sqrt(1.0 + 8.0 * (double)q)) * 0.5);
+        while (i * (i - 1) / 2 > q) --i;
+        while ((i + 1) * i / 2 <= q) ++i;
+        int j = q - i * (i - 1) / 2;
+        ci = closed[i];
+        cj = closed[j];
+        if ((ci >> 1) >= sp.ncore && (cj >> 1) >= sp.ncore) {
+          int I = ci >> 1, J = cj >> 1;
+          int X = I > J ? I : J, Y = I > J ? J : I;
+          int pair = X * (X + 1) / 2 + Y;
+          same = (ci & 1) == (cj & 1);
+          const int64_t* st = same ? a.hb.sameStart : a.hb.oppStart;
+          const float* vals = same ? a.hb.sameVal : a.hb.oppVal;
+          int64_t s0 = st[pair], s1 = st[pair + 1];
+          // first index with |v| < eps
+          int64_t lo = s0, hi = s1;
+          while (lo < hi) {
+            int64_t mid = (lo + hi) >> 1;
+            if ((double)fabsf(vals[mid]) < eps)
+              hi = mid;
+            else
+              lo = mid + 1;
+          }
+          lstart = s0;
+          len = lo - s0;
+        }
+      }
+      int64_t incl = len;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        int64_t y = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += y;
+      }
+      const int64_t total = __shfl_sync(kFull, incl, 31);
+      const int64_t excl = incl - len;
+      for (int64_t f0 = 0; f0 < total; f0 += 32) {
+        const int64_t f = f0 + lane;
+        int lo = 0;
+#pragma unroll
+        for (int st = 16; st >= 1; st >>= 1) {
+          int c = lo + st;
+          int64_t e = __shfl_sync(kFull, excl, c < 32 ? c : 31);
+          if (c < 32 && e <= f) lo = c;
+        }
+        const int64_t ls = __shfl_sync(kFull, lstart, lo);
+        const int64_t eo = __shfl_sync(kFull, excl, lo);
+        const int oci = __shfl_sync(kFull, ci, lo);
+        const int ocj = __shfl_sync(kFull, cj, lo);
+        const bool osame = __shfl_sync(kFull, (int)same, lo) != 0;
+        bool emit = false;
+        Det2 cand = d;
+        if (f < total) {
+          const int64_t index = ls + (f - eo);
+          const int16_t* pr = osame ? a.hb.samePairs : a.hb.oppPairs;
+          const int av = 2 * pr[2 * index] + (oci & 1);
+          const int bv = 2 * pr[2 * index + 1] + (ocj & 1);
+          bool ok = (av >> 1) < sp.ncore + sp.nact && (bv >> 1) < sp.ncore + sp.nact;
+          for (int r = 0; ok && r < sp.nrestrict; ++r) {
+            int e = cur[r] - in_mask(sp, r, oci) - in_mask(sp, r, ocj) + in_mask(sp, r, av) + in_mask(sp, r, bv);
+            ok = e >= sp.rmin[r] && e <= sp.rmax[r];
+          }
+          if (ok && !(det_getocc(d, av) || det_getocc(d, bv))) {
+            det_flip(cand, av);
+            det_flip(cand, bv);
+            det_flip(cand, oci);
+            det_flip(cand, ocj);
+            emit = !hash_contains(a.hslots, a.hmask, a.dets, cand);
+          }
+        }
+        append(a, emit, cand);
+      }
+    }
+  }
+}
+
+int64_t select_candidates(const Det2* dets, const double* cmax, size_t n, double eps1, const IntsView& ints,
+                          const HeatBathView& hb, double maxEntry, const SelectParams& sp, const DetHash& present,
+                          Det2* out, int64_t cap, int64_t* d_counter, cudaStream_t s) {
+  SHCI_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(int64_t), s));
+  SelArgs a{dets, cmax, n, eps1, ints, hb, maxEntry, sp, present.slots.p, present.mask, out, cap, d_counter};
+  size_t blocks = (n + kSelWarps - 1) / kSelWarps;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  if (blocks < 1) blocks = 1;
+  k_select<<<(unsigned)blocks, kSelThreads, 0, s>>>(a);
+  SHCI_LAUNCH_CHECK();
+  int64_t total = 0;
+  SHCI_CUDA(cudaMemcpyAsync(&total, d_counter, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  return total;
+}
+
+}  // namespace shci

@@ -1,0 +1,356 @@
+// Sigma (y = H x) on the stored Hamiltonian and the tall-skinny vector
+// kernels of the block Davidson solver.
+//
+// Sigma replaces Hmult2::operator() (SHCI/Hmult.h:52-150). The reference
+// stores the lower triangle and scatters symmetrically into a private
+// temporary; here every row is complete (both triangles), so each row is
+// owned by VW lanes of one warp and written once, without atomics:
+//   y[I] = diag[I] x[I] (FP64) + sum_J h_IJ x[J]
+// Mixed path: h in FP32, x in FP32, FP32 accumulation, the FP64 diagonal term
+// added in FP64. Plain path: FP64 throughout. k vectors share one pass over
+// the matrix (x is row-interleaved, one 4/8/16-byte gather per column index).
+//
+// The Davidson kernels (Gram products, Ritz combinations, residuals and the
+// diagonal preconditioner of SHCI/Davidson.cpp:85-106) reduce in a fixed
+// order, so results do not depend on scheduling.
+#include "ham.h"
+
+namespace shci {
+
+static inline unsigned grid_for(size_t n, int threads, size_t max_blocks = 152 * 32) {
+  size_t b = (n + threads - 1) / threads;
+  if (b < 1) b = 1;
+  if (b > max_blocks) b = max_blocks;
+  return (unsigned)b;
+}
+
+template <int KP>
+struct VecF;
+template <>
+struct VecF<1> {
+  using T = float;
+  __device__ static void fma(float* acc, float h, const float* x, int j) { acc[0] += h * __ldg(x + j); }
+};
+template <>
+struct VecF<2> {
+  __device__ static void fma(float* acc, float h, const float* x, int j) {
+    float2 v = __ldg(reinterpret_cast<const float2*>(x) + j);
+    acc[0] += h * v.x;
+    acc[1] += h * v.y;
+  }
+};
+template <>
+struct VecF<4> {
+  __device__ static void fma(float* acc, float h, const float* x, int j) {
+    float4 v = __ldg(reinterpret_cast<const float4*>(x) + j);
+    acc[0] += h * v.x;
+    acc[1] += h * v.y;
+    acc[2] += h * v.z;
+    acc[3] += h * v.w;
+  }
+};
+
+template <int VW, int KP>
+__global__ void __launch_bounds__(256) k_sigma_mixed(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                                                     const float* __restrict__ val, const double* __restrict__ diag,
+                                                     const float* __restrict__ x, size_t N, int k,
+                                                     double* __restrict__ y, size_t ldy) {
+  // The row loop is uniform per warp (rows past N run empty) so that the
+  // width-VW shuffles below always see all 32 lanes.
+  const int sub = threadIdx.x & (VW - 1);
+  const size_t rows_per_warp = 32 / VW;
+  const size_t stride = ((size_t)gridDim.x * blockDim.x / 32) * rows_per_warp;
+  for (size_t wr = (((size_t)blockIdx.x * blockDim.x + threadIdx.x) / 32) * rows_per_warp; wr < N; wr += stride) {
+    const size_t r = wr + (threadIdx.x & 31) / VW;
+    const bool live = r < N;
+    float acc[KP];
+#pragma unroll
+    for (int c = 0; c < KP; ++c) acc[c] = 0.f;
+    const int64_t p1 = live ? __ldg(rowptr + r + 1) : 0;
+    for (int64_t p = (live ? __ldg(rowptr + r) : 0) + sub; p < p1; p += VW) {
+      const int j = __ldcs(col + p);
+      const float h = __ldcs(val + p);
+      VecF<KP>::fma(acc, h, x, j);
+    }
+#pragma unroll
+    for (int c = 0; c < KP; ++c) {
+#pragma unroll
+      for (int o = VW / 2; o; o >>= 1) acc[c] += __shfl_xor_sync(kFull, acc[c], o, VW);
+    }
+    if (sub == 0 && live) {
+      const double dg = diag[r];
+#pragma unroll
+      for (int c = 0; c < KP; ++c)
+        if (c < k) y[(size_t)c * ldy + r] = dg * (double)x[r * KP + c] + (double)acc[c];
+    }
+  }
+}
+
+template <int VW, int KP, bool HILO>
+__global__ void __launch_bounds__(256) k_sigma_f64(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                                                   const double* __restrict__ v64, const float* __restrict__ vhi,
+                                                   const float* __restrict__ vlo, const double* __restrict__ diag,
+                                                   const double* __restrict__ x, size_t N, int k,
+                                                   double* __restrict__ y, size_t ldy) {
+  const int sub = threadIdx.x & (VW - 1);
+  const size_t rows_per_warp = 32 / VW;
+  const size_t stride = ((size_t)gridDim.x * blockDim.x / 32) * rows_per_warp;
+  for (size_t wr = (((size_t)blockIdx.x * blockDim.x + threadIdx.x) / 32) * rows_per_warp; wr < N; wr += stride) {
+    const size_t r = wr + (threadIdx.x & 31) / VW;
+    const bool live = r < N;
+    double acc[KP];
+#pragma unroll
+    for (int c = 0; c < KP; ++c) acc[c] = 0.0;
+    const int64_t p1 = live ? __ldg(rowptr + r + 1) : 0;
+    for (int64_t p = (live ? __ldg(rowptr + r) : 0) + sub; p < p1; p += VW) {
+      const int j = __ldcs(col + p);
+      double h;
+      if (HILO)
+        h = (double)__ldcs(vhi + p) + (double)__ldcs(vlo + p);
+      else
+        h = __ldcs(v64 + p);
+#pragma unroll
+      for (int c = 0; c < KP; ++c) acc[c] += h * __ldg(x + (size_t)j * KP + c);
+    }
+#pragma unroll
+    for (int c = 0; c < KP; ++c) {
+#pragma unroll
+      for (int o = VW / 2; o; o >>= 1) acc[c] += __shfl_xor_sync(kFull, acc[c], o, VW);
+    }
+    if (sub == 0 && live) {
+      const double dg = diag[r];
+#pragma unroll
+      for (int c = 0; c < KP; ++c)
+        if (c < k) y[(size_t)c * ldy + r] = dg * x[r * KP + c] + acc[c];
+    }
+  }
+}
+
+static int pick_vw(const Csr& H) {
+  double avg = H.N ? (double)H.nnz / (double)H.N : 0.0;
+  if (avg >= 96) return 32;
+  if (avg >= 40) return 16;
+  if (avg >= 14) return 8;
+  return 4;
+}
+
+template <int KP>
+static void launch_mixed(int vw, const Csr& H, const double* diag, const float* x, int k, double* y, size_t ldy,
+                         cudaStream_t s) {
+  const size_t threads = H.N * (size_t)vw;
+  const unsigned blocks = grid_for(threads, 256, 152 * 16);
+  switch (vw) {
+    case 32: k_sigma_mixed<32, KP><<<blocks, 256, 0, s>>>(H.rowptr.p, H.col.p, H.vhi.p, diag, x, H.N, k, y, ldy); break;
+    case 16: k_sigma_mixed<16, KP><<<blocks, 256, 0, s>>>(H.rowptr.p, H.col.p, H.vhi.p, diag, x, H.N, k, y, ldy); break;
+    case 8: k_sigma_mixed<8, KP><<<blocks, 256, 0, s>>>(H.rowptr.p, H.col.p, H.vhi.p, diag, x, H.N, k, y, ldy); break;
+    default: k_sigma_mixed<4, KP><<<blocks, 256, 0, s>>>(H.rowptr.p, H.col.p, H.vhi.p, diag, x, H.N, k, y, ldy); break;
+  }
+  SHCI_LAUNCH_CHECK();
+}
+
+void sigma_csr_mixed(const Csr& H, const double* diag, const float* x32, int kp, int k, double* y, size_t ldy,
+                     cudaStream_t s) {
+  if (!H.vhi.p) throw Error(kErrState, "Hamiltonian has no FP32 values (built for the FP64 path)");
+  if (H.N == 0) return;
+  int vw = pick_vw(H);
+  switch (kp) {
+    case 1: launch_mixed<1>(vw, H, diag, x32, k, y, ldy, s); break;
+    case 2: launch_mixed<2>(vw, H, diag, x32, k, y, ldy, s); break;
+    case 4: launch_mixed<4>(vw, H, diag, x32, k, y, ldy, s); break;
+    default: throw Error(kErrInvalid, "sigma block width must be 1, 2 or 4");
+  }
+}
+
+template <int KP, bool HILO>
+static void launch_f64(int vw, const Csr& H, const double* diag, const double* x, int k, double* y, size_t ldy,
+                       cudaStream_t s) {
+  const size_t threads = H.N * (size_t)vw;
+  const unsigned blocks = grid_for(threads, 256, 152 * 16);
+  const double* v64 = H.v64.p;
+  const float *vhi = H.vhi.p, *vlo = H.vlo.p;
+  switch (vw) {
+    case 32: k_sigma_f64<32, KP, HILO><<<blocks, 256, 0, s>>>(H.rowptr.p, H.col.p, v64, vhi, vlo, diag, x, H.N, k, y, ldy); break;
+    case 16: k_sigma_f64<16, KP, HILO><<<blocks, 256, 0, s>>>(H.rowptr.p, H.col.p, v64, vhi, vlo, diag, x, H.N, k, y, ldy); break;
+    case 8: k_sigma_f64<8, KP, HILO><<<blocks, 256, 0, s>>>(H.rowptr.p, H.col.p, v64, vhi, vlo, diag, x, H.N, k, y, ldy); break;
+    default: k_sigma_f64<4, KP, HILO><<<blocks, 256, 0, s>>>(H.rowptr.p, H.col.p, v64, vhi, vlo, diag, x, H.N, k, y, ldy); break;
+  }
+  SHCI_LAUNCH_CHECK();
+}
+
+void sigma_csr_f64(const Csr& H, const double* diag, const double* x64, int kp, int k, double* y, size_t ldy,
+                   bool use_hilo, cudaStream_t s) {
+  if (H.N == 0) return;
+  if (use_hilo && !(H.vhi.p && H.vlo.p)) throw Error(kErrState, "Hamiltonian has no FP32 head/tail values");
+  if (!use_hilo && !H.v64.p) throw Error(kErrState, "Hamiltonian has no FP64 values");
+  int vw = pick_vw(H);
+  if (use_hilo) {
+    switch (kp) {
+      case 1: launch_f64<1, true>(vw, H, diag, x64, k, y, ldy, s); break;
+      case 2: launch_f64<2, true>(vw, H, diag, x64, k, y, ldy, s); break;
+      case 4: launch_f64<4, true>(vw, H, diag, x64, k, y, ldy, s); break;
+      default: throw Error(kErrInvalid, "sigma block width must be 1, 2 or 4");
+    }
+  } else {
+    switch (kp) {
+      case 1: launch_f64<1, false>(vw, H, diag, x64, k, y, ldy, s); break;
+      case 2: launch_f64<2, false>(vw, H, diag, x64, k, y, ldy, s); break;
+      case 4: launch_f64<4, false>(vw, H, diag, x64, k, y, ldy, s); break;
+      default: throw Error(kErrInvalid, "sigma block width must be 1, 2 or 4");
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Packing between column-major FP64 blocks and row-interleaved vectors
+// ---------------------------------------------------------------------------
+__global__ void k_pack_f32(const double* __restrict__ A, size_t lda, int c0, int k, int kp, size_t N,
+                           float* __restrict__ out) {
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < N; r += (size_t)gridDim.x * blockDim.x)
+    for (int c = 0; c < kp; ++c) out[r * kp + c] = c < k ? (float)A[(size_t)(c0 + c) * lda + r] : 0.f;
+}
+__global__ void k_pack_f64(const double* __restrict__ A, size_t lda, int c0, int k, int kp, size_t N,
+                           double* __restrict__ out) {
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < N; r += (size_t)gridDim.x * blockDim.x)
+    for (int c = 0; c < kp; ++c) out[r * kp + c] = c < k ? A[(size_t)(c0 + c) * lda + r] : 0.0;
+}
+__global__ void k_unpack_f64(const double* __restrict__ in, int kp, int k, size_t N, double* __restrict__ A,
+                             size_t lda, int c0) {
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < N; r += (size_t)gridDim.x * blockDim.x)
+    for (int c = 0; c < k; ++c) A[(size_t)(c0 + c) * lda + r] = in[r * kp + c];
+}
+void pack_f32(const double* A, size_t lda, int c0, int k, int kp, size_t N, float* out, cudaStream_t s) {
+  k_pack_f32<<<grid_for(N, 256), 256, 0, s>>>(A, lda, c0, k, kp, N, out);
+  SHCI_LAUNCH_CHECK();
+}
+void pack_f64(const double* A, size_t lda, int c0, int k, int kp, size_t N, double* out, cudaStream_t s) {
+  k_pack_f64<<<grid_for(N, 256), 256, 0, s>>>(A, lda, c0, k, kp, N, out);
+  SHCI_LAUNCH_CHECK();
+}
+void unpack_f64(const double* in, int kp, int k, size_t N, double* A, size_t lda, int c0, cudaStream_t s) {
+  k_unpack_f64<<<grid_for(N, 256), 256, 0, s>>>(in, kp, k, N, A, lda, c0);
+  SHCI_LAUNCH_CHECK();
+}
+
+// ---------------------------------------------------------------------------
+// Tall-skinny Gram: G = A^T B. Blocks own contiguous row ranges; each block
+// stages 32-row tiles in shared memory and thread t accumulates pair t.
+// A second kernel adds the per-block partials in block order.
+// ---------------------------------------------------------------------------
+constexpr int kGramMax = 16;
+constexpr int kGramRows = 32;
+constexpr unsigned kGramBlocks = 152 * 2;
+
+__global__ void __launch_bounds__(256) k_gram_part(const double* __restrict__ A, size_t lda, int ma,
+                                                   const double* __restrict__ B, size_t ldb, int mb, size_t N,
+                                                   double* __restrict__ part) {
+  __shared__ double sA[kGramMax][kGramRows + 1];
+  __shared__ double sB[kGramMax][kGramRows + 1];
+  const int t = threadIdx.x;
+  const int P = ma * mb;
+  const int pi = t % ma, pj = t / ma;
+  double acc = 0.0;
+  const size_t per = (N + gridDim.x - 1) / gridDim.x;
+  const size_t r0 = (size_t)blockIdx.x * per;
+  const size_t r1 = r0 + per < N ? r0 + per : N;
+  for (size_t base = r0; base < r1; base += kGramRows) {
+    for (int e = t; e < kGramMax * kGramRows; e += blockDim.x) {
+      int c = e / kGramRows, rr = e % kGramRows;
+      size_t row = base + rr;
+      sA[c][rr] = (c < ma && row < r1) ? A[(size_t)c * lda + row] : 0.0;
+      sB[c][rr] = (c < mb && row < r1) ? B[(size_t)c * ldb + row] : 0.0;
+    }
+    __syncthreads();
+    if (t < P) {
+#pragma unroll 8
+      for (int rr = 0; rr < kGramRows; ++rr) acc += sA[pi][rr] * sB[pj][rr];
+    }
+    __syncthreads();
+  }
+  if (t < P) part[(size_t)blockIdx.x * P + t] = acc;
+}
+
+__global__ void k_gram_sum(const double* __restrict__ part, int nblocks, int P, double* __restrict__ G) {
+  int t = threadIdx.x;
+  if (t < P) {
+    double s = 0.0;
+    for (int b = 0; b < nblocks; ++b) s += part[(size_t)b * P + t];
+    G[t] = s;
+  }
+}
+
+void ts_gram(const double* A, size_t lda, int ma, const double* B, size_t ldb, int mb, size_t N, double* G,
+             DevBuf<double>& part, cudaStream_t s) {
+  if (ma > kGramMax || mb > kGramMax || ma * mb > 256) throw Error(kErrInvalid, "Gram block too wide");
+  unsigned nb = kGramBlocks;
+  if ((size_t)nb * kGramRows > N) nb = (unsigned)((N + kGramRows - 1) / kGramRows);
+  if (nb < 1) nb = 1;
+  part.reserve((size_t)nb * ma * mb);
+  k_gram_part<<<nb, 256, 0, s>>>(A, lda, ma, B, ldb, mb, N, part.p);
+  SHCI_LAUNCH_CHECK();
+  k_gram_sum<<<1, 256, 0, s>>>(part.p, (int)nb, ma * mb, G);
+  SHCI_LAUNCH_CHECK();
+}
+
+// Y = alpha * A Q + beta * Y
+__global__ void k_ts_gemm(const double* __restrict__ A, size_t lda, int m, const double* __restrict__ Q, int k,
+                          size_t N, double alpha, double beta, double* __restrict__ Y, size_t ldy) {
+  __shared__ double sQ[kGramMax * kGramMax];
+  for (int e = threadIdx.x; e < m * k; e += blockDim.x) sQ[e] = Q[e];
+  __syncthreads();
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < N; r += (size_t)gridDim.x * blockDim.x) {
+    double a[kGramMax];
+    for (int i = 0; i < m; ++i) a[i] = A[(size_t)i * lda + r];
+    for (int c = 0; c < k; ++c) {
+      double s = 0.0;
+      for (int i = 0; i < m; ++i) s += a[i] * sQ[c * m + i];
+      double* yp = Y + (size_t)c * ldy + r;
+      *yp = (beta == 0.0) ? alpha * s : alpha * s + beta * (*yp);
+    }
+  }
+}
+void ts_gemm(const double* A, size_t lda, int m, const double* Q, int k, size_t N, double alpha, double beta,
+             double* Y, size_t ldy, cudaStream_t s) {
+  if (m > kGramMax || k > kGramMax) throw Error(kErrInvalid, "tall-skinny product too wide");
+  k_ts_gemm<<<grid_for(N, 256), 256, 0, s>>>(A, lda, m, Q, k, N, alpha, beta, Y, ldy);
+  SHCI_LAUNCH_CHECK();
+}
+
+__global__ void k_residual(const double* __restrict__ X, const double* __restrict__ Y, const double* __restrict__ lam,
+                           int k, size_t N, size_t ld, double* __restrict__ R) {
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < N; r += (size_t)gridDim.x * blockDim.x)
+    for (int c = 0; c < k; ++c) R[(size_t)c * ld + r] = Y[(size_t)c * ld + r] - lam[c] * X[(size_t)c * ld + r];
+}
+void residual(const double* X, const double* Y, const double* lam, int k, size_t N, size_t ld, double* R,
+              cudaStream_t s) {
+  k_residual<<<grid_for(N, 256), 256, 0, s>>>(X, Y, lam, k, N, ld, R);
+  SHCI_LAUNCH_CHECK();
+}
+
+// precondition (SHCI/Davidson.cpp:85-106)
+__global__ void k_precondition(const double* __restrict__ diag, const double* __restrict__ lam, int k, size_t N,
+                               double* __restrict__ R, size_t ld) {
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < N; r += (size_t)gridDim.x * blockDim.x)
+    for (int c = 0; c < k; ++c) {
+      double e = lam[c], d = diag[r];
+      double* p = R + (size_t)c * ld + r;
+      if (fabs(e - d) > 1e-12)
+        *p = *p / (e - d);
+      else
+        *p = *p / (e - d - 1.e-12);
+    }
+}
+void precondition(const double* diag, const double* lam, int k, size_t N, double* R, size_t ld, cudaStream_t s) {
+  k_precondition<<<grid_for(N, 256), 256, 0, s>>>(diag, lam, k, N, R, ld);
+  SHCI_LAUNCH_CHECK();
+}
+
+__global__ void k_scale_cols(double* __restrict__ A, size_t ld, const double* __restrict__ sc, int k, size_t N) {
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < N; r += (size_t)gridDim.x * blockDim.x)
+    for (int c = 0; c < k; ++c) A[(size_t)c * ld + r] *= sc[c];
+}
+void scale_cols(double* A, size_t ld, const double* scale, int k, size_t N, cudaStream_t s) {
+  k_scale_cols<<<grid_for(N, 256), 256, 0, s>>>(A, ld, scale, k, N);
+  SHCI_LAUNCH_CHECK();
+}
+
+}  // namespace shci

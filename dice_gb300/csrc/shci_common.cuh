@@ -1,0 +1,197 @@
+// Shared device code: determinant bit operations, integral accessors and the
+// Slater-Condon rules, written for sm_103a.
+//
+// Determinant layout (same bit convention as Dice, SHCI/Determinants.h:247-602):
+// two 64-bit words per determinant, spin-orbital p at bit p%64 of word p/64,
+// alpha orbital k = spin-orbital 2k, beta orbital k = spin-orbital 2k+1.
+// Alpha/beta strings are single 64-bit words with orbital k at bit k.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace shci {
+
+constexpr int kMaxOrb = 64;      // spatial orbitals
+constexpr int kMaxSpin = 128;    // spin orbitals
+constexpr unsigned kFull = 0xffffffffu;
+
+struct Det2 {
+  uint64_t w0, w1;
+};
+
+__host__ __device__ inline bool det_getocc(const Det2& d, int p) {
+  return p < 64 ? ((d.w0 >> p) & 1ull) : ((d.w1 >> (p - 64)) & 1ull);
+}
+__host__ __device__ inline void det_flip(Det2& d, int p) {
+  if (p < 64)
+    d.w0 ^= (1ull << p);
+  else
+    d.w1 ^= (1ull << (p - 64));
+}
+
+// Determinant::operator< (SHCI/Determinants.h:490-498): signed words, top down.
+__host__ __device__ inline bool det_less(const Det2& a, const Det2& b) {
+  if ((int64_t)a.w1 != (int64_t)b.w1) return (int64_t)a.w1 < (int64_t)b.w1;
+  return (int64_t)a.w0 < (int64_t)b.w0;
+}
+__host__ __device__ inline bool det_eq(const Det2& a, const Det2& b) { return a.w0 == b.w0 && a.w1 == b.w1; }
+
+// Even-bit extraction: bits 0,2,4,... of x packed into the low 32 bits.
+__host__ __device__ inline uint32_t compact_even(uint64_t x) {
+  x &= 0x5555555555555555ull;
+  x = (x | (x >> 1)) & 0x3333333333333333ull;
+  x = (x | (x >> 2)) & 0x0f0f0f0f0f0f0f0full;
+  x = (x | (x >> 4)) & 0x00ff00ff00ff00ffull;
+  x = (x | (x >> 8)) & 0x0000ffff0000ffffull;
+  x = (x | (x >> 16)) & 0x00000000ffffffffull;
+  return (uint32_t)x;
+}
+__host__ __device__ inline uint64_t spread_even(uint32_t v) {
+  uint64_t x = v;
+  x = (x | (x << 16)) & 0x0000ffff0000ffffull;
+  x = (x | (x << 8)) & 0x00ff00ff00ff00ffull;
+  x = (x | (x << 4)) & 0x0f0f0f0f0f0f0f0full;
+  x = (x | (x << 2)) & 0x3333333333333333ull;
+  x = (x | (x << 1)) & 0x5555555555555555ull;
+  return x;
+}
+// getAlpha / getBeta (SHCI/Determinants.h:471-487)
+__host__ __device__ inline uint64_t det_alpha(const Det2& d) {
+  return (uint64_t)compact_even(d.w0) | ((uint64_t)compact_even(d.w1) << 32);
+}
+__host__ __device__ inline uint64_t det_beta(const Det2& d) {
+  return (uint64_t)compact_even(d.w0 >> 1) | ((uint64_t)compact_even(d.w1 >> 1) << 32);
+}
+__host__ __device__ inline Det2 det_from_strings(uint64_t a, uint64_t b) {
+  Det2 d;
+  d.w0 = spread_even((uint32_t)a) | (spread_even((uint32_t)b) << 1);
+  d.w1 = spread_even((uint32_t)(a >> 32)) | (spread_even((uint32_t)(b >> 32)) << 1);
+  return d;
+}
+
+// Number of occupied spin orbitals strictly between lo and hi (lo < hi).
+__device__ inline int occ_between(const Det2& d, int lo, int hi) {
+  // bits (lo, hi): mask of bits < hi minus bits <= lo
+  auto below = [](uint64_t w, int k) -> uint64_t {  // bits of w below position k (0..64)
+    return k >= 64 ? w : (k <= 0 ? 0ull : (w & ((1ull << k) - 1ull)));
+  };
+  int c = __popcll(below(d.w0, hi)) + __popcll(below(d.w1, hi - 64));
+  c -= __popcll(below(d.w0, lo + 1)) + __popcll(below(d.w1, lo + 1 - 64));
+  return c;
+}
+
+// Device view of the integrals (SHCI/integral.h:47-101).
+struct IntsView {
+  const double* I1;        // (2n)x(2n) spin-orbital matrix
+  const double* I2;        // 8-fold packed spatial (ij|kl)
+  const double* Direct;    // n x n, (ii|jj)
+  const double* Exchange;  // n x n, (ij|ji)
+  int norb;
+};
+
+__device__ __forceinline__ int pair_index(int i, int j) {
+  int a = i > j ? i : j, b = i > j ? j : i;
+  return a * (a + 1) / 2 + b;
+}
+// twoInt::operator() on spatial indices
+__device__ __forceinline__ double i2_spatial(const double* __restrict__ I2, int i, int j, int k, int l) {
+  int ij = pair_index(i, j), kl = pair_index(k, l);
+  size_t A = ij > kl ? ij : kl, B = ij > kl ? kl : ij;
+  return __ldg(I2 + A * (A + 1) / 2 + B);
+}
+// twoInt::operator() on spin orbitals: zero unless both pairs are same-spin
+__device__ __forceinline__ double i2_spin(const double* __restrict__ I2, int i, int j, int k, int l) {
+  if (((i ^ j) & 1) || ((k ^ l) & 1)) return 0.0;
+  return i2_spatial(I2, i >> 1, j >> 1, k >> 1, l >> 1);
+}
+
+// Hij_1Excite (SHCI/Determinants.cpp:437-505): `a` created, `i` destroyed,
+// the sum running over the ket's occupied spin orbitals in ascending order.
+// Adds are kept un-fused and in the reference's order so the FP64 result is
+// bit-identical to it.
+__device__ inline double hij_single(const IntsView& I, const Det2& ket, int a, int i) {
+  const int n2 = 2 * I.norb;
+  double energy = __ldg(I.I1 + (size_t)a * n2 + i);
+  const int sa = a & 1;
+  const int ai = pair_index(a >> 1, i >> 1);
+#pragma unroll 1
+  for (int w = 0; w < 2; ++w) {
+    uint64_t bits = w ? ket.w1 : ket.w0;
+    while (bits) {
+      int j = __ffsll((long long)bits) - 1 + 64 * w;
+      bits &= bits - 1;
+      // (ai|jj) - (aj|ji); the exchange term vanishes for opposite spins
+      int jj = pair_index(j >> 1, j >> 1);
+      size_t A = ai > jj ? ai : jj, B = ai > jj ? jj : ai;
+      double d = __ldg(I.I2 + A * (A + 1) / 2 + B);
+      double x = 0.0;
+      if ((j & 1) == sa) x = i2_spatial(I.I2, a >> 1, j >> 1, j >> 1, i >> 1);
+      energy = __dadd_rn(energy, __dsub_rn(d, x));
+    }
+  }
+  int lo = a < i ? a : i, hi = a < i ? i : a;
+  return (occ_between(ket, lo, hi) & 1) ? -energy : energy;
+}
+
+// Hij_2Excite (SHCI/Determinants.cpp:406-434): i<j destroyed, a<b created.
+__device__ inline double hij_double(const IntsView& I, const Det2& ket, int i, int j, int a, int b) {
+  int c = occ_between(ket, i < a ? i : a, i < a ? a : i) + occ_between(ket, j < b ? j : b, j < b ? b : j);
+  double sgn = (c & 1) ? -1.0 : 1.0;
+  if (a > j || b < i) sgn = -sgn;
+  double v = __dsub_rn(i2_spin(I.I2, a, i, b, j), i2_spin(I.I2, a, j, b, i));
+  return sgn * v;
+}
+
+// Hij(bra, ket) for determinants at excitation distance 1 or 2
+// (SHCI/Determinants.cpp:564-631).
+__device__ inline double hij_any(const IntsView& I, const Det2& bra, const Det2& ket) {
+  uint64_t u0 = bra.w0 ^ ket.w0, u1 = bra.w1 ^ ket.w1;
+  uint64_t c0 = u0 & bra.w0, c1 = u1 & bra.w1;  // created
+  uint64_t d0 = u0 & ket.w0, d1 = u1 & ket.w1;  // destroyed
+  int ncre = __popcll(c0) + __popcll(c1);
+  int cre[2], des[2];
+  int k = 0;
+  while (c0 && k < 2) { cre[k++] = __ffsll((long long)c0) - 1; c0 &= c0 - 1; }
+  while (c1 && k < 2) { cre[k++] = __ffsll((long long)c1) - 1 + 64; c1 &= c1 - 1; }
+  k = 0;
+  while (d0 && k < 2) { des[k++] = __ffsll((long long)d0) - 1; d0 &= d0 - 1; }
+  while (d1 && k < 2) { des[k++] = __ffsll((long long)d1) - 1 + 64; d1 &= d1 - 1; }
+  if (ncre == 1) return hij_single(I, ket, cre[0], des[0]);
+  if (ncre == 2) return hij_double(I, ket, des[0], des[1], cre[0], cre[1]);
+  return 0.0;
+}
+
+// Determinant::Energy without the core energy (SHCI/Determinants.cpp:252-300).
+__device__ inline double det_energy(const IntsView& I, const Det2& d, const double* sDirect,
+                                    const double* sExchange) {
+  const int n = I.norb, n2 = 2 * n;
+  int closed[kMaxSpin];
+  int nc = 0;
+  uint64_t b0 = d.w0, b1 = d.w1;
+  while (b0) { closed[nc++] = __ffsll((long long)b0) - 1; b0 &= b0 - 1; }
+  while (b1) { closed[nc++] = __ffsll((long long)b1) - 1 + 64; b1 &= b1 - 1; }
+  double energy = 0.0;
+  for (int i = 0; i < nc; i++) {
+    int P = closed[i];
+    energy = __dadd_rn(energy, __ldg(I.I1 + (size_t)P * n2 + P));
+    for (int j = i + 1; j < nc; j++) {
+      int Q = closed[j];
+      energy = __dadd_rn(energy, sDirect[(P >> 1) * n + (Q >> 1)]);
+      if (((P ^ Q) & 1) == 0) energy = __dsub_rn(energy, sExchange[(P >> 1) * n + (Q >> 1)]);
+    }
+  }
+  return energy;
+}
+
+// 64-bit mixing hash for determinant keys (splitmix64 finaliser).
+__host__ __device__ inline uint64_t mix64(uint64_t x) {
+  x ^= x >> 30;
+  x *= 0xbf58476d1ce4e5b9ull;
+  x ^= x >> 27;
+  x *= 0x94d049bb133111ebull;
+  x ^= x >> 31;
+  return x;
+}
+__host__ __device__ inline uint64_t det_hash(const Det2& d) { return mix64(d.w0 ^ mix64(d.w1 + 0x9e3779b97f4a7c15ull)); }
+
+}  // namespace shci

@@ -1,0 +1,250 @@
+"""ctypes binding of libshci_gpu (include/shci_gpu.h).
+
+The Python layer only marshals arrays; every computation runs in the CUDA
+library. If the library is missing this module raises instead of falling
+back to anything else.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libshci_gpu.so")
+
+MODE_FP64, MODE_MIXED, MODE_DIRECT = 0, 1, 2
+MODES = {"fp64": MODE_FP64, "mixed": MODE_MIXED, "direct": MODE_DIRECT}
+
+_ERR = {1: "invalid argument", 2: "I/O error", 3: "CUDA error", 4: "out of device memory",
+        5: "Davidson did not converge", 6: "device wait timed out", 7: "call out of order"}
+
+# (name, restype, argtypes) of every exported entry point
+_vp, _i32, _i64, _dbl, _u64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_double, ctypes.c_uint64
+_P = ctypes.POINTER
+SIGNATURES = [
+    ("shci_ctx_create", _i32, [_i32, _P(_vp)]),
+    ("shci_ctx_destroy", _i32, [_vp]),
+    ("shci_last_error", ctypes.c_char_p, [_vp]),
+    ("shci_ctx_stream", _vp, [_vp]),
+    ("shci_set_alloc_cap", _i32, [_vp, _u64]),
+    ("shci_read_fcidump", _i32, [_vp, ctypes.c_char_p, _P(_i32), _P(_i32), _P(_dbl)]),
+    ("shci_heatbath_export", _i32, [_vp, _i32, _P(_i64), _vp, _vp, _vp, _vp]),
+    ("shci_set_selection_params", _i32, [_vp, _i32, _i32, _i32, _vp, _vp, _vp]),
+    ("shci_dets_set", _i32, [_vp, _vp, _i64]),
+    ("shci_dets_count", _i32, [_vp, _P(_i64)]),
+    ("shci_dets_get", _i32, [_vp, _vp, _i64]),
+    ("shci_select", _i32, [_vp, _vp, _dbl, _P(_i64)]),
+    ("shci_ham_build", _i32, [_vp, _i32, _P(_i64)]),
+    ("shci_ham_export", _i32, [_vp, _vp, _vp, _vp]),
+    ("shci_diag", _i32, [_vp, _vp]),
+    ("shci_sigma", _i32, [_vp, _i32, _vp, _vp, _i32]),
+    ("shci_sigma_device", _i32, [_vp, _i32, _vp, _vp, _i32, _i64]),
+    ("shci_davidson", _i32, [_vp, _i32, _i32, _i32, _vp, _i32, _dbl, _vp, _P(_i32)]),
+    ("shci_run_input", _i32, [_vp, ctypes.c_char_p, ctypes.c_char_p, _i32, _i32, _vp, _i32, _P(_i32)]),
+    ("shci_run_log", _i32, [_vp, _i32, _P(_i32), _vp, _vp, _vp, _vp]),
+    ("shci_run_ci", _i32, [_vp, _vp, _i64]),
+    ("shci_run_timings", _i32, [_vp, _P(_dbl), _P(_dbl), _P(_dbl), _P(_dbl), _P(_i64), _P(_dbl)]),
+    ("shci_launch_count", _i32, [_vp, _P(_i64)]),
+]
+
+_lib = None
+
+
+def load_library(path=LIB_PATH):
+    """Load libshci_gpu.so; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise RuntimeError("libshci_gpu.so not built: run `python -m dice_gb300.build` "
+                               "(or __graft_entry__.build())")
+        L = ctypes.CDLL(path)
+        for name, res, args in SIGNATURES:
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+class ShciError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (status %d): %s" % (_ERR.get(code, "error"), code, msg))
+        self.code = code
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Engine:
+    """One context of the GPU engine (one CUDA stream, device-resident state)."""
+
+    def __init__(self, device=0):
+        L = load_library()
+        self.h = ctypes.c_void_p()
+        rc = L.shci_ctx_create(device, ctypes.byref(self.h))
+        if rc:
+            raise ShciError(rc, L.shci_last_error(None).decode())
+        self.norb = self.nelec = 0
+        self.coreE = 0.0
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            load_library().shci_ctx_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc:
+            raise ShciError(rc, load_library().shci_last_error(self.h).decode())
+
+    @property
+    def stream(self):
+        return load_library().shci_ctx_stream(self.h)
+
+    def set_alloc_cap(self, nbytes):
+        self._check(load_library().shci_set_alloc_cap(self.h, int(nbytes)))
+
+    def read_fcidump(self, path):
+        n, e, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        self._check(load_library().shci_read_fcidump(self.h, os.fspath(path).encode(), ctypes.byref(n),
+                                                     ctypes.byref(e), ctypes.byref(c)))
+        self.norb, self.nelec, self.coreE = n.value, e.value, c.value
+        return self.norb, self.nelec, self.coreE
+
+    def heatbath(self, same):
+        L = load_library()
+        cnt = ctypes.c_int64()
+        self._check(L.shci_heatbath_export(self.h, int(same), ctypes.byref(cnt), None, None, None, None))
+        n = self.norb
+        vals = np.zeros(cnt.value, np.float32)
+        pairs = np.zeros(2 * cnt.value, np.int16)
+        starts = np.zeros(n * (n + 1) // 2 + 1, np.int64)
+        singles = np.zeros((2 * n) ** 2, np.float64)
+        self._check(L.shci_heatbath_export(self.h, int(same), ctypes.byref(cnt), _p(vals), _p(pairs), _p(starts),
+                                           _p(singles)))
+        return vals, pairs, starts, singles
+
+    def set_selection_params(self, ncore=0, nact=1000000, restrictions=()):
+        """restrictions: iterable of (min, max, spatial_orbital_list)."""
+        nr = len(restrictions)
+        rmin = np.array([r[0] for r in restrictions] or [0], np.int32)
+        rmax = np.array([r[1] for r in restrictions] or [0], np.int32)
+        masks = np.zeros(max(1, nr), np.uint64)
+        for i, (_, _, orbs) in enumerate(restrictions):
+            m = 0
+            for o in orbs:
+                m |= 1 << int(o)
+            masks[i] = np.uint64(m)
+        self._check(load_library().shci_set_selection_params(self.h, ncore, nact, nr, _p(rmin), _p(rmax),
+                                                             _p(masks)))
+
+    def set_dets(self, dets):
+        d = np.ascontiguousarray(dets, dtype=np.uint64).reshape(-1, 2)
+        self._check(load_library().shci_dets_set(self.h, _p(d), len(d)))
+
+    def ndets(self):
+        n = ctypes.c_int64()
+        self._check(load_library().shci_dets_count(self.h, ctypes.byref(n)))
+        return n.value
+
+    def dets(self):
+        n = self.ndets()
+        out = np.zeros((n, 2), np.uint64)
+        self._check(load_library().shci_dets_get(self.h, _p(out), n))
+        return out
+
+    def select(self, cmax, eps1):
+        c = np.ascontiguousarray(cmax, dtype=np.float64)
+        k = ctypes.c_int64()
+        self._check(load_library().shci_select(self.h, _p(c), float(eps1), ctypes.byref(k)))
+        return k.value
+
+    def ham_build(self, mode="fp64"):
+        nnz = ctypes.c_int64()
+        self._check(load_library().shci_ham_build(self.h, MODES.get(mode, mode), ctypes.byref(nnz)))
+        return nnz.value
+
+    def ham_export(self, nnz):
+        n = self.ndets()
+        rowptr = np.zeros(n + 1, np.int64)
+        col = np.zeros(max(1, nnz), np.int32)
+        val = np.zeros(max(1, nnz), np.float64)
+        self._check(load_library().shci_ham_export(self.h, _p(rowptr), _p(col), _p(val)))
+        return rowptr, col[:nnz], val[:nnz]
+
+    def diag(self):
+        out = np.zeros(self.ndets(), np.float64)
+        self._check(load_library().shci_diag(self.h, _p(out)))
+        return out
+
+    def sigma(self, x, mode="fp64"):
+        """x: (N,) or (k, N) -> H x with the same shape."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        one = x.ndim == 1
+        xx = x.reshape(1, -1) if one else x
+        y = np.zeros_like(xx)
+        self._check(load_library().shci_sigma(self.h, MODES.get(mode, mode), _p(xx), _p(y), xx.shape[0]))
+        return y[0] if one else y
+
+    def davidson(self, x0, mode="fp64", block=False, max_copies=None, tol=5e-5):
+        x = np.ascontiguousarray(x0, dtype=np.float64).reshape(-1, self.ndets()).copy()
+        nroots = x.shape[0]
+        E = np.zeros(nroots)
+        it = ctypes.c_int()
+        mc = max_copies if max_copies is not None else nroots + 4
+        self._check(load_library().shci_davidson(self.h, MODES.get(mode, mode), int(block), nroots, _p(x), mc,
+                                                 float(tol), _p(E), ctypes.byref(it)))
+        return E, x, it.value
+
+    def run_input(self, path, mode=None, block=None, fcidump=None):
+        """Whole variational stage of a Dice input file; returns E_var per root
+        (core energy included). mode/block None: from the input file."""
+        E = np.zeros(16)
+        nr = ctypes.c_int()
+        m = -1 if mode is None else MODES.get(mode, mode)
+        b = -1 if block is None else int(block)
+        self._check(load_library().shci_run_input(self.h, os.fspath(path).encode(),
+                                                  fcidump.encode() if fcidump else None, m, b, _p(E), 16,
+                                                  ctypes.byref(nr)))
+        return E[: nr.value].copy()
+
+    def run_log(self):
+        L = load_library()
+        ni = ctypes.c_int()
+        self._check(L.shci_run_log(self.h, 0, ctypes.byref(ni), None, None, None, None))
+        n = ni.value
+        nd = np.zeros(n, np.int64)
+        en = np.zeros(n)
+        di = np.zeros(n, np.int32)
+        sec = np.zeros(n)
+        self._check(L.shci_run_log(self.h, n, ctypes.byref(ni), _p(nd), _p(en), _p(di), _p(sec)))
+        return {"ndets": nd, "energy": en, "davidson": di, "seconds": sec}
+
+    def run_ci(self, nroots):
+        n = self.ndets()
+        out = np.zeros((nroots, n))
+        self._check(load_library().shci_run_ci(self.h, _p(out), out.size))
+        return out
+
+    def timings(self):
+        vals = [ctypes.c_double() for _ in range(4)]
+        ns = ctypes.c_int64()
+        ts = ctypes.c_double()
+        self._check(load_library().shci_run_timings(self.h, *[ctypes.byref(v) for v in vals], ctypes.byref(ns),
+                                                    ctypes.byref(ts)))
+        keys = ["select", "ham", "davidson", "total"]
+        out = {k: v.value for k, v in zip(keys, vals)}
+        out["n_sigma"] = ns.value
+        out["sigma"] = ts.value
+        return out
+
+    def launch_count(self):
+        n = ctypes.c_int64()
+        self._check(load_library().shci_launch_count(self.h, ctypes.byref(n)))
+        return n.value

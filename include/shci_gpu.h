@@ -1,0 +1,152 @@
+/*
+ * libshci_gpu: C-ABI of the GB300 engine for the variational stage of
+ * semistochastic heat-bath CI (the drop-in for Dice's SHCI variational loop).
+ *
+ * Conventions
+ *   - Every entry point returns an int status (SHCI_OK = 0). On failure the
+ *     message is available from shci_last_error(ctx). The reference has no
+ *     error codes: it calls exit(0)/abort() (SHCI/integral.cpp:71-74,
+ *     SHCI/Davidson.cpp:262-266, :305-308, SHCI/input.cpp:373-375).
+ *   - Determinants are two uint64 words each (up to 64 spatial orbitals):
+ *     spin-orbital p is bit p%64 of word p/64, alpha orbital k = spin-orbital
+ *     2k, beta orbital k = 2k+1 (Dice's Determinant, SHCI/Determinants.h:247-602).
+ *   - Vectors on the host are column-major: vector c of length N starts at
+ *     x + c*N (Eigen MatrixXx columns in the reference).
+ *   - Energies exclude the core energy unless stated (the reference zeroes
+ *     coreE during the variational loop, SHCI/SHCIbasics.cpp:815-818).
+ *   - A context owns one CUDA stream and all device buffers; calls on one
+ *     context must not overlap (not thread-safe per context).
+ */
+#ifndef SHCI_GPU_H
+#define SHCI_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct shci_ctx shci_ctx;
+
+enum {
+  SHCI_OK = 0,
+  SHCI_ERR_INVALID = 1, /* bad argument or input file */
+  SHCI_ERR_IO = 2,      /* file missing or unreadable */
+  SHCI_ERR_CUDA = 3,    /* CUDA runtime error */
+  SHCI_ERR_OOM = 4,     /* device allocation failed or exceeded the cap */
+  SHCI_ERR_NOCONV = 5,  /* Davidson did not converge */
+  SHCI_ERR_TIMEOUT = 6, /* a bounded device wait gave up */
+  SHCI_ERR_STATE = 7    /* call out of order (e.g. sigma before ham_build) */
+};
+
+/* Sigma / Hamiltonian storage modes. */
+enum {
+  SHCI_MODE_FP64 = 0,   /* plain path: FP64 CSR values, FP64 sigma */
+  SHCI_MODE_MIXED = 1,  /* FP32 CSR head + FP32 tail, FP32 sigma, FP64 refinement */
+  SHCI_MODE_DIRECT = 2  /* matrix-free: H_ij recomputed in every sigma (HmultDirect) */
+};
+
+/* Context. */
+int shci_ctx_create(int device, shci_ctx** out);
+int shci_ctx_destroy(shci_ctx* ctx);
+const char* shci_last_error(shci_ctx* ctx);
+/* The context's cudaStream_t, for callers that time or order work on it. */
+void* shci_ctx_stream(shci_ctx* ctx);
+/* Cap on the context's device allocations in bytes (0 = no cap). */
+int shci_set_alloc_cap(shci_ctx* ctx, uint64_t bytes);
+
+/* Integrals. Replaces readIntegrals (SHCI/integral.cpp:43-225) and the
+ * heat-bath construction twoIntHeatBath::constructClass +
+ * twoIntHeatBathSHM::constructClass (SHCI/integral.h:125-153,
+ * SHCI/integral.cpp:228-389). Builds the heat-bath tables as well. */
+int shci_read_fcidump(shci_ctx* ctx, const char* path, int* norb, int* nelec, double* coreE);
+/* Heat-bath table sizes and contents (for parity checks). which: 1 = same
+ * spin, 0 = opposite spin. Arrays may be NULL. starts has n(n+1)/2+1 entries,
+ * pairs 2 per entry, singles (2n)^2. */
+int shci_heatbath_export(shci_ctx* ctx, int which, int64_t* count, float* vals, int16_t* pairs, int64_t* starts,
+                         double* singles);
+
+/* Selection parameters (schedule fields ncore, nact, restrict/restrictv;
+ * SHCI/input.h:35-194, SHCI/OccRestrictions.h:37-78). Each restriction is
+ * (min, max, 64-bit mask of spatial orbitals). At most 4 restrictions. */
+int shci_set_selection_params(shci_ctx* ctx, int ncore, int nact, int nrestrict, const int* rmin, const int* rmax,
+                              const uint64_t* spatial_masks);
+
+/* Determinant space. set replaces the space; get copies it out in index
+ * order (new determinants are appended in sorted order, as the reference
+ * does at SHCI/SHCIbasics.cpp:1059-1077). */
+int shci_dets_set(shci_ctx* ctx, const uint64_t* dets, int64_t n);
+int shci_dets_count(shci_ctx* ctx, int64_t* n);
+int shci_dets_get(shci_ctx* ctx, uint64_t* out, int64_t cap);
+
+/* Heat-bath selection. Replaces the parent loop over
+ * SHCIgetdeterminants::getDeterminantsVariationalApprox
+ * (SHCI/SHCIgetdeterminants.cpp:586-739, called at SHCI/SHCIbasics.cpp:969-982)
+ * plus sort/unique and the append at SHCI/SHCIbasics.cpp:992-1077.
+ * cmax: host array of |c| per current determinant (cMax,
+ * SHCI/SHCIbasics.cpp:954-965). The new determinants are appended to the
+ * space; *n_new returns how many. */
+int shci_select(shci_ctx* ctx, const double* cmax, double eps1, int64_t* n_new);
+
+/* Hamiltonian. Replaces HamHelpers2::PopulateHelpers/MakeSHMHelpers and
+ * SparseHam::makeFromHelper (SHCI/SHCImakeHamiltonian.cpp:290-408, :959-1147,
+ * :486-715). mode: SHCI_MODE_*; MIXED also keeps the FP32 tail for FP64
+ * refinement, DIRECT builds only the string tables. *nnz = off-diagonal
+ * nonzeros, both triangles. */
+int shci_ham_build(shci_ctx* ctx, int mode, int64_t* nnz);
+/* The stored off-diagonal CSR (full rows) in FP64; rowptr N+1, col/val nnz.
+ * For MIXED, val = head + tail. */
+int shci_ham_export(shci_ctx* ctx, int64_t* rowptr, int32_t* col, double* val);
+
+/* Diagonal energies Determinant::Energy (SHCI/Determinants.cpp:252-300),
+ * coreE excluded, into host out[N] (may be NULL to only compute them). */
+int shci_diag(shci_ctx* ctx, double* out);
+
+/* Sigma y = H x for k vectors (1 <= k <= 4), host buffers (column-major N x k).
+ * Replaces Hmult2::operator() / HmultDirect::operator() (SHCI/Hmult.h:52,
+ * :241). The reference's Hmult2 writes y (zero-initialised) and HmultDirect
+ * accumulates into y; this call always overwrites y.
+ * mode SHCI_MODE_MIXED computes in FP32; SHCI_MODE_FP64 in FP64 (FP64 values,
+ * or head+tail when the matrix was built MIXED); SHCI_MODE_DIRECT matrix-free. */
+int shci_sigma(shci_ctx* ctx, int mode, const double* x, double* y, int k);
+/* Same on device buffers of this context's device (column-major, leading
+ * dimension ld), enqueued on the context stream without host synchronisation. */
+int shci_sigma_device(shci_ctx* ctx, int mode, const double* x_dev, double* y_dev, int k, int64_t ld);
+
+/* Davidson. Replaces davidson / davidsonDirect (SHCI/Davidson.cpp:111-348,
+ * :353-590) with the diagonal preconditioner (:85-106).
+ * x0: host nroots x N column-major, initial guesses in, eigenvectors out.
+ * mode: SHCI_MODE_FP64 (plain), SHCI_MODE_MIXED (FP32 sigma, then FP64
+ * refinement of the Ritz pairs), SHCI_MODE_DIRECT.
+ * block: 0 = one correction vector per iteration for the lowest unconverged
+ * root (the reference's scheme), 1 = one per unconverged root in a single
+ * k-vector sigma launch. max_copies: subspace size (reference: nroots+4).
+ * E[nroots] receives eigenvalues (coreE excluded); *iters the iteration count. */
+int shci_davidson(shci_ctx* ctx, int mode, int block, int nroots, double* x0, int max_copies, double tol, double* E,
+                  int* iters);
+
+/* Whole variational stage from a Dice input file (replaces
+ * SHCIbasics::DoVariational, SHCI/SHCIbasics.cpp:783-1378, driven as in
+ * SHCI/SHCI.cpp:157-446). Reads input.dat and its FCIDUMP (relative paths
+ * resolve against the input file's directory unless fcidump is given).
+ * E[cap_roots] receives E_var per root with coreE added; *nroots the count. */
+int shci_run_input(shci_ctx* ctx, const char* input_path, const char* fcidump, int mode, int block, double* E,
+                   int cap_roots, int* nroots);
+/* Per-iteration log of the last run: ndets, E (root 0, coreE added),
+ * Davidson iterations and seconds since the start of the run. */
+int shci_run_log(shci_ctx* ctx, int cap, int* niter, int64_t* ndets, double* energy, int* dav_iters, double* seconds);
+/* Coefficient vectors of the last run's final space, host out (nroots x N). */
+int shci_run_ci(shci_ctx* ctx, double* out, int64_t cap);
+
+/* Stage timings of the last run in seconds: selection, Hamiltonian build,
+ * Davidson, total; and the sigma calls/time spent inside Davidson. */
+int shci_run_timings(shci_ctx* ctx, double* t_select, double* t_ham, double* t_davidson, double* t_total,
+                     int64_t* n_sigma, double* t_sigma);
+
+/* Kernel launches issued by this context since creation (own kernels only). */
+int shci_launch_count(shci_ctx* ctx, int64_t* n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,230 @@
+"""ctypes binding of the CPU oracle (shci_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: the checker the GPU library is compared against.
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this module; the product (dice_gb300) never does.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liborc.so")
+CLI = os.path.join(HERE, "_build", "shci_oracle")
+
+_c_double_p = ctypes.POINTER(ctypes.c_double)
+
+
+def build(force=False):
+    """Compile the oracle library and CLI with the Makefile beside this file."""
+    if force or not (os.path.exists(LIB) and os.path.exists(CLI)) or \
+            os.path.getmtime(LIB) < os.path.getmtime(os.path.join(HERE, "shci_oracle.cpp")):
+        subprocess.run(["make", "-s", "-C", HERE, "-B" if force else "all"], check=True)
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        vp, i64, i32, dbl = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_double
+        L.orc_load.restype = vp
+        L.orc_load.argtypes = [ctypes.c_char_p, ctypes.c_char_p, i32]
+        L.orc_free.argtypes = [vp]
+        L.orc_info.argtypes = [vp, ctypes.POINTER(i32), ctypes.POINTER(i32), _c_double_p, _c_double_p]
+        L.orc_i2_size.restype = i64
+        L.orc_i2_size.argtypes = [vp]
+        L.orc_i2_export.argtypes = [vp, vp]
+        L.orc_i1_export.argtypes = [vp, vp]
+        L.orc_hb_size.restype = i64
+        L.orc_hb_size.argtypes = [vp, i32]
+        L.orc_hb_export.argtypes = [vp, i32, vp, vp, vp, vp]
+        L.orc_energy.restype = dbl
+        L.orc_energy.argtypes = [vp, vp]
+        L.orc_hij.restype = dbl
+        L.orc_hij.argtypes = [vp, vp, vp]
+        L.orc_select.restype = i64
+        L.orc_select.argtypes = [vp, vp, i64, vp, dbl, vp, i64, i32, i32, vp, i32, vp, i64]
+        L.orc_ham_build.restype = i64
+        L.orc_ham_build.argtypes = [vp, vp, i64]
+        L.orc_ham_export.argtypes = [vp, vp, vp, vp]
+        L.orc_sigma.argtypes = [vp, vp, vp]
+        L.orc_davidson.restype = i32
+        L.orc_davidson.argtypes = [vp, vp, i32, vp, i32, dbl, i32, vp, ctypes.POINTER(i32)]
+        L.orc_run_input.restype = i32
+        L.orc_run_input.argtypes = [ctypes.POINTER(vp), ctypes.c_char_p, ctypes.c_char_p, i32,
+                                    ctypes.c_char_p, i32]
+        L.orc_var_nroots.restype = i32
+        L.orc_var_nroots.argtypes = [vp]
+        L.orc_var_ndets.restype = i64
+        L.orc_var_ndets.argtypes = [vp]
+        L.orc_var_niters.restype = i32
+        L.orc_var_niters.argtypes = [vp]
+        L.orc_var_seconds.restype = dbl
+        L.orc_var_seconds.argtypes = [vp]
+        L.orc_var_nnz_lower.restype = i64
+        L.orc_var_nnz_lower.argtypes = [vp]
+        L.orc_var_energies.argtypes = [vp, vp]
+        L.orc_var_log.argtypes = [vp, vp, vp, vp, vp, vp]
+        L.orc_var_dets.argtypes = [vp, vp]
+        L.orc_var_ci.argtypes = [vp, i32, vp]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Oracle:
+    """Integrals + heat-bath tables read from one FCIDUMP."""
+
+    def __init__(self, fcidump=None, _handle=None):
+        L = lib()
+        if _handle is not None:
+            self.h = _handle
+        else:
+            err = ctypes.create_string_buffer(512)
+            self.h = L.orc_load(fcidump.encode(), err, 512)
+            if not self.h:
+                raise RuntimeError(err.value.decode())
+        n, e = ctypes.c_int(), ctypes.c_int()
+        c, m = ctypes.c_double(), ctypes.c_double()
+        L.orc_info(self.h, ctypes.byref(n), ctypes.byref(e), ctypes.byref(c), ctypes.byref(m))
+        self.norb, self.nelec, self.coreE, self.maxEntry = n.value, e.value, c.value, m.value
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_free(self.h)
+            self.h = None
+
+    def i2(self):
+        out = np.zeros(lib().orc_i2_size(self.h), np.float64)
+        lib().orc_i2_export(self.h, _p(out))
+        return out
+
+    def i1(self):
+        out = np.zeros((2 * self.norb) ** 2, np.float64)
+        lib().orc_i1_export(self.h, _p(out))
+        return out
+
+    def heatbath(self, same):
+        L = lib()
+        m = L.orc_hb_size(self.h, int(same))
+        n = self.norb
+        vals = np.zeros(m, np.float32)
+        pairs = np.zeros(2 * m, np.int16)
+        starts = np.zeros(n * (n + 1) // 2 + 1, np.uint64)
+        singles = np.zeros((2 * n) ** 2, np.float64)
+        L.orc_hb_export(self.h, int(same), _p(vals), _p(pairs), _p(starts), _p(singles))
+        return vals, pairs, starts, singles
+
+    def energy(self, det):
+        d = np.ascontiguousarray(det, dtype=np.uint64)
+        return lib().orc_energy(self.h, _p(d))
+
+    def hij(self, bra, ket):
+        b = np.ascontiguousarray(bra, dtype=np.uint64)
+        k = np.ascontiguousarray(ket, dtype=np.uint64)
+        return lib().orc_hij(self.h, _p(b), _p(k))
+
+    def select(self, dets, cmax, eps1, existing_sorted, ncore=0, nact=1000000, restrictions=()):
+        """restrictions: iterable of (min, max, spatial_orbital_list)."""
+        dets = np.ascontiguousarray(dets, dtype=np.uint64)
+        cmax = np.ascontiguousarray(cmax, dtype=np.float64)
+        ex = np.ascontiguousarray(existing_sorted, dtype=np.uint64)
+        r = np.zeros((max(1, len(restrictions)), 4), np.int64)
+        for i, (lo, hi, orbs) in enumerate(restrictions):
+            m = 0
+            for o in orbs:
+                m |= 1 << o
+            r[i] = (lo, hi, np.int64(np.uint64(m).view(np.int64)) if m >= 2**63 else m, 0)
+        cap = 1 << 16
+        while True:
+            out = np.zeros((cap, 2), np.uint64)
+            n = lib().orc_select(self.h, _p(dets), len(dets), _p(cmax), eps1, _p(ex), len(ex), ncore, nact,
+                                 _p(r), len(restrictions), _p(out), cap)
+            if n <= cap:
+                return out[:n]
+            cap = n
+
+    def ham(self, dets):
+        """Lower-triangle CSR as the reference's SparseHam holds it: row I is
+        [I (diagonal), then every J < I connected to I], values in FP64."""
+        dets = np.ascontiguousarray(dets, dtype=np.uint64)
+        nnz = lib().orc_ham_build(self.h, _p(dets), len(dets))
+        rowptr = np.zeros(len(dets) + 1, np.int64)
+        col = np.zeros(nnz, np.int32)
+        val = np.zeros(nnz, np.float64)
+        lib().orc_ham_export(self.h, _p(rowptr), _p(col), _p(val))
+        self._n = len(dets)
+        return rowptr, col, val
+
+    def sigma(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.zeros_like(x)
+        lib().orc_sigma(self.h, _p(x), _p(y))
+        return y
+
+    def davidson(self, x0, diag, max_copies, tol, direct=False):
+        x0 = np.ascontiguousarray(x0, dtype=np.float64).copy()
+        nroots = x0.shape[0]
+        d = np.ascontiguousarray(diag, dtype=np.float64)
+        e = np.zeros(nroots)
+        it = ctypes.c_int()
+        rc = lib().orc_davidson(self.h, _p(x0), nroots, _p(d), max_copies, tol, int(direct), _p(e),
+                                ctypes.byref(it))
+        if rc:
+            raise RuntimeError("Davidson did not converge")
+        return e, x0, it.value
+
+
+class VarRun:
+    """Result of a whole variational stage run by the oracle on an input file."""
+
+    def __init__(self, h):
+        self.h = h
+        L = lib()
+        nr = L.orc_var_nroots(h)
+        self.E = np.zeros(nr)
+        L.orc_var_energies(h, _p(self.E))
+        nd = L.orc_var_ndets(h)
+        self.dets = np.zeros((nd, 2), np.uint64)
+        L.orc_var_dets(h, _p(self.dets))
+        self.ci = np.zeros((nr, nd))
+        for r in range(nr):
+            row = np.zeros(nd)
+            L.orc_var_ci(h, r, _p(row))
+            self.ci[r] = row
+        ni = L.orc_var_niters(h)
+        self.ndets_log = np.zeros(ni, np.int64)
+        self.energy_log = np.zeros(ni)
+        self.davidson_log = np.zeros(ni, np.int32)
+        self.eps1_log = np.zeros(ni)
+        self.seconds_log = np.zeros(ni)
+        L.orc_var_log(h, _p(self.ndets_log), _p(self.energy_log), _p(self.davidson_log), _p(self.eps1_log),
+                      _p(self.seconds_log))
+        self.seconds = L.orc_var_seconds(h)
+        self.nnz_lower = L.orc_var_nnz_lower(h)
+        self.oracle = Oracle(_handle=h)
+
+
+def run_input(input_path, fcidump=None, verbose=False):
+    """Run the whole variational stage of a Dice input file on the CPU."""
+    h = ctypes.c_void_p()
+    err = ctypes.create_string_buffer(512)
+    cwd = os.getcwd()
+    os.chdir(os.path.dirname(os.path.abspath(input_path)))
+    try:
+        rc = lib().orc_run_input(ctypes.byref(h), os.path.basename(input_path).encode(),
+                                 fcidump.encode() if fcidump else None, int(verbose), err, 512)
+    finally:
+        os.chdir(cwd)
+    if rc:
+        raise RuntimeError(err.value.decode())
+    return VarRun(h.value)

@@ -1,0 +1,1202 @@
+// SHCI variational oracle: a CPU restatement of Dice's variational path.
+//
+// TEST INFRASTRUCTURE ONLY. This file is the checker for the GPU library in
+// dice_gb300/: only tests/, __graft_entry__.smoke() and bench.py's CPU
+// baseline leg may load it. Nothing in the product links or calls it.
+//
+// Every function below restates one piece of the reference (sanshar/Dice,
+// directory SHCI/) and cites the file:line it follows. Arithmetic order is
+// kept where it decides bits: the FP32 cast and ordering of the heat-bath
+// lists, the threshold comparisons of the selection, the summation order of
+// the single-excitation matrix element and of the diagonal energy.
+//
+// Parity pins (checked by tests/test_oracle_golden.py against data copied
+// from the reference's own tests/examples): examples/h8_631g (per-iteration
+// determinant counts, the final determinant set, E_var), tests/SHCI/restart
+// (E_var), tests/SHCI/n2_RAS (E_var with an occupation restriction).
+//
+// Determinants are two 64-bit words (up to 64 spatial orbitals), spin-orbital
+// p at bit p%64 of word p/64, alpha = even p, beta = odd p, as in
+// SHCI/Determinants.h:247-602.
+
+#include <algorithm>
+#include <cassert>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <numeric>
+#include <sstream>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+namespace orc {
+
+static const int W = 2;
+struct Det {
+  uint64_t w[W];
+};
+
+static inline bool det_less(const Det& a, const Det& b) {
+  // Determinant::operator< (SHCI/Determinants.h:490-498): words compared as
+  // signed long from the top word down.
+  for (int i = W - 1; i >= 0; --i) {
+    int64_t x = (int64_t)a.w[i], y = (int64_t)b.w[i];
+    if (x < y) return true;
+    if (x > y) return false;
+  }
+  return false;
+}
+static inline bool det_eq(const Det& a, const Det& b) {
+  for (int i = 0; i < W; ++i)
+    if (a.w[i] != b.w[i]) return false;
+  return true;
+}
+static inline bool getocc(const Det& d, int p) { return (d.w[p >> 6] >> (p & 63)) & 1ull; }
+static inline void setocc(Det& d, int p, bool v) {
+  if (v)
+    d.w[p >> 6] |= (1ull << (p & 63));
+  else
+    d.w[p >> 6] &= ~(1ull << (p & 63));
+}
+static inline int popc(uint64_t x) { return __builtin_popcountll(x); }
+
+// ---------------------------------------------------------------------------
+// Integrals (SHCI/integral.h:47-102, SHCI/integral.cpp:43-225)
+// ---------------------------------------------------------------------------
+struct Ints {
+  int norb = 0;   // spatial orbitals
+  int nelec = 0;
+  double coreE = 0.0;
+  std::vector<double> I1;  // (2n)x(2n) spin-orbital one-electron matrix
+  std::vector<double> I2;  // 8-fold packed (ij|kl), spatial
+  std::vector<double> Direct, Exchange;  // n x n
+  double maxEntry = 100.0;
+  std::vector<int> irrep;
+
+  // twoInt::operator() (SHCI/integral.h:86-101), non-ksym branch
+  inline double i2(int i, int j, int k, int l) const {
+    if (!((i % 2 == j % 2) && (k % 2 == l % 2))) return 0.0;
+    int I = i / 2, J = j / 2, K = k / 2, L = l / 2;
+    int IJ = std::max(I, J) * (std::max(I, J) + 1) / 2 + std::min(I, J);
+    int KL = std::max(K, L) * (std::max(K, L) + 1) / 2 + std::min(K, L);
+    size_t A = std::max(IJ, KL), B = std::min(IJ, KL);
+    return I2[A * (A + 1) / 2 + B];
+  }
+  inline double& i2ref_spatial(int I, int J, int K, int L) {
+    int IJ = std::max(I, J) * (std::max(I, J) + 1) / 2 + std::min(I, J);
+    int KL = std::max(K, L) * (std::max(K, L) + 1) / 2 + std::min(K, L);
+    size_t A = std::max(IJ, KL), B = std::min(IJ, KL);
+    return I2[A * (A + 1) / 2 + B];
+  }
+  inline double i1(int i, int j) const { return I1[(size_t)i * (2 * norb) + j]; }
+  inline double direct(int i, int j) const { return Direct[(size_t)i * norb + j]; }
+  inline double exchange(int i, int j) const { return Exchange[(size_t)i * norb + j]; }
+};
+
+// boost::trim + boost::split(tok, line, is_any_of(delims), token_compress_on)
+static void split_compress(const std::string& in, const char* delims, std::vector<std::string>& tok) {
+  size_t b = 0, e = in.size();
+  while (b < e && isspace((unsigned char)in[b])) ++b;
+  while (e > b && isspace((unsigned char)in[e - 1])) --e;
+  std::string s = in.substr(b, e - b);
+  tok.clear();
+  std::string cur;
+  bool last_delim = false;
+  for (size_t i = 0; i < s.size(); ++i) {
+    if (strchr(delims, s[i])) {
+      if (!last_delim) {
+        tok.push_back(cur);
+        cur.clear();
+      }
+      last_delim = true;
+    } else {
+      cur.push_back(s[i]);
+      last_delim = false;
+    }
+  }
+  tok.push_back(cur);
+}
+static bool iequals(const std::string& a, const std::string& b) {
+  if (a.size() != b.size()) return false;
+  for (size_t i = 0; i < a.size(); ++i)
+    if (tolower((unsigned char)a[i]) != tolower((unsigned char)b[i])) return false;
+  return true;
+}
+
+// readIntegrals (SHCI/integral.cpp:43-225), serial branch.
+static int read_fcidump(const char* path, Ints& I, std::string& err) {
+  std::ifstream dump(path);
+  if (!dump.good()) {
+    err = std::string("Integral file ") + path + " does not exist!";
+    return 1;
+  }
+  int norbs = -1, nelec = -1;
+  std::vector<std::string> tok;
+  std::string msg;
+  while (!dump.eof()) {
+    std::getline(dump, msg);
+    split_compress(msg, ", \t=", tok);
+    if (tok.size() == 1 && (iequals(tok[0], "&END") || iequals(tok[0], "/"))) break;
+    if (iequals(tok[0].substr(0, 4), "&FCI")) {
+      if (tok.size() > 2 && iequals(tok[1].substr(0, 4), "NORB")) norbs = atoi(tok[2].c_str());
+      if (tok.size() > 4 && iequals(tok[3].substr(0, 5), "NELEC")) nelec = atoi(tok[4].c_str());
+    } else if (iequals(tok[0].substr(0, 4), "ISYM")) {
+      continue;
+    } else if (iequals(tok[0].substr(0, 4), "KSYM")) {
+      err = "KSYM integrals are not supported";
+      return 2;
+    } else if (iequals(tok[0].substr(0, 6), "ORBSYM")) {
+      for (size_t i = 1; i < tok.size(); i++) I.irrep.push_back(atoi(tok[i].c_str()));
+    } else {
+      for (size_t i = 0; i < tok.size(); i++) I.irrep.push_back(atoi(tok[i].c_str()));
+    }
+  }
+  if (norbs == -1 || nelec == -1) {
+    err = "could not read the norbs or nelec";
+    return 3;
+  }
+  if (norbs > 64) {
+    err = "more than 64 spatial orbitals";
+    return 4;
+  }
+  I.irrep.resize(norbs);
+  I.norb = norbs;
+  I.nelec = nelec;
+  size_t npair = (size_t)norbs * (norbs + 1) / 2;
+  I.I2.assign(npair * (npair + 1) / 2, 0.0);
+  I.I1.assign((size_t)(2 * norbs) * (2 * norbs), 0.0);
+  I.coreE = 0.0;
+  const int n2 = 2 * norbs;
+  while (!dump.eof()) {
+    std::getline(dump, msg);
+    split_compress(msg, ", \t", tok);
+    if (tok.size() != 5) continue;
+    double integral = atof(tok[0].c_str());
+    int a = atoi(tok[1].c_str()), b = atoi(tok[2].c_str()), c = atoi(tok[3].c_str()),
+        d = atoi(tok[4].c_str());
+    if (a == b && b == c && c == d && d == 0) {
+      I.coreE = integral;
+    } else if (b == c && c == d && d == 0) {
+      continue;
+    } else if (c == d && d == 0) {
+      if (a < 1 || b < 1 || a > norbs || b > norbs) continue;
+      I.I1[(size_t)(2 * (a - 1)) * n2 + 2 * (b - 1)] = integral;
+      I.I1[(size_t)(2 * (a - 1) + 1) * n2 + 2 * (b - 1) + 1] = integral;
+      I.I1[(size_t)(2 * (b - 1)) * n2 + 2 * (a - 1)] = integral;
+      I.I1[(size_t)(2 * (b - 1) + 1) * n2 + 2 * (a - 1) + 1] = integral;
+    } else {
+      if (a < 1 || b < 1 || c < 1 || d < 1 || a > norbs || b > norbs || c > norbs || d > norbs) continue;
+      I.i2ref_spatial(a - 1, b - 1, c - 1, d - 1) = integral;
+    }
+  }
+  // maxEntry: element of largest magnitude (SHCI/integral.cpp:38, :170-171)
+  double best = I.I2.empty() ? 0.0 : I.I2[0];
+  for (double v : I.I2)
+    if (fabs(best) < fabs(v)) best = v;
+  I.maxEntry = best;
+  I.Direct.assign((size_t)norbs * norbs, 0.0);
+  I.Exchange.assign((size_t)norbs * norbs, 0.0);
+  for (int i = 0; i < norbs; i++)
+    for (int j = 0; j < norbs; j++) {
+      I.Direct[(size_t)i * norbs + j] = I.i2(2 * i, 2 * i, 2 * j, 2 * j);
+      I.Exchange[(size_t)i * norbs + j] = I.i2(2 * i, 2 * j, 2 * j, 2 * i);
+    }
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Heat-bath tables (SHCI/integral.h:125-153, SHCI/integral.cpp:228-389)
+// ---------------------------------------------------------------------------
+struct HeatBath {
+  std::vector<float> sameVal, oppVal;
+  std::vector<int16_t> samePairs, oppPairs;  // (a,b) per entry
+  std::vector<uint64_t> sameStart, oppStart;  // n(n+1)/2 + 1
+  std::vector<double> Singles;               // (2n)x(2n)
+};
+
+// One pair list: entries inserted in (a,b) order into a multimap keyed by
+// |float| (compAbs), read back by reverse iteration. That is: |v| descending,
+// equal |v| in reverse insertion order.
+struct HBEntry {
+  float v;
+  int16_t a, b;
+  int seq;
+};
+static void hb_emit(std::vector<HBEntry>& e, std::vector<float>& vals, std::vector<int16_t>& pairs) {
+  std::sort(e.begin(), e.end(), [](const HBEntry& x, const HBEntry& y) {
+    float ax = fabsf(x.v), ay = fabsf(y.v);
+    if (ax != ay) return ax > ay;
+    return x.seq > y.seq;
+  });
+  for (auto& x : e) {
+    vals.push_back(x.v);
+    pairs.push_back(x.a);
+    pairs.push_back(x.b);
+  }
+}
+
+static void build_heatbath(const Ints& I, HeatBath& hb) {
+  const int n = I.norb;
+  const double eps = 1.e-10;  // twoIntHeatBath(1.e-10) at SHCI/SHCI.cpp:247
+  hb.sameStart.assign(1, 0);
+  hb.oppStart.assign(1, 0);
+  std::vector<HBEntry> same, opp;
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j <= i; j++) {
+      same.clear();
+      opp.clear();
+      int seqs = 0, seqo = 0;
+      for (int a = 0; a < n; a++)
+        for (int b = 0; b < n; b++) {
+          double v = I.i2(2 * i, 2 * a, 2 * j, 2 * b);
+          if (fabs(v) > eps) opp.push_back({(float)v, (int16_t)a, (int16_t)b, seqo++});
+          if (a >= b) {
+            double s = I.i2(2 * i, 2 * a, 2 * j, 2 * b) - I.i2(2 * i, 2 * b, 2 * j, 2 * a);
+            if (fabs(s) > eps) same.push_back({(float)s, (int16_t)a, (int16_t)b, seqs++});
+          }
+        }
+      hb_emit(same, hb.sameVal, hb.samePairs);
+      hb_emit(opp, hb.oppVal, hb.oppPairs);
+      hb.sameStart.push_back(hb.sameVal.size());
+      hb.oppStart.push_back(hb.oppVal.size());
+    }
+  const int n2 = 2 * n;
+  hb.Singles.assign((size_t)n2 * n2, 0.0);
+  for (int i = 0; i < n2; i++)
+    for (int a = 0; a < n2; a++) {
+      double s = fabs(I.i1(i, a));
+      for (int j = 0; j < n2; j++) {
+        double t = I.i2(i, a, j, j) - I.i2(i, j, j, a);
+        if (fabs(s) < fabs(t)) s = fabs(t);
+      }
+      hb.Singles[(size_t)i * n2 + a] = s;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Slater-Condon rules (SHCI/Determinants.cpp:252-300, :406-505, :564-631)
+// ---------------------------------------------------------------------------
+static int closed_list(const Det& d, int nspin, int* closed) {
+  int c = 0;
+  for (int p = 0; p < nspin; ++p)
+    if (getocc(d, p)) closed[c++] = p;
+  return c;
+}
+
+// Determinant::Energy, coreE excluded (SHCI/Determinants.cpp:252-300)
+static double det_energy(const Ints& I, const Det& d) {
+  int closed[128];
+  int nc = closed_list(d, 2 * I.norb, closed);
+  double energy = 0.0;
+  for (int i = 0; i < nc; i++) {
+    int P = closed[i];
+    energy += I.i1(P, P);
+    for (int j = i + 1; j < nc; j++) {
+      int Q = closed[j];
+      energy += I.direct(P / 2, Q / 2);
+      if ((P % 2) == (Q % 2)) energy -= I.exchange(P / 2, Q / 2);
+    }
+  }
+  return energy;
+}
+
+// Determinant::parity(start,end) (SHCI/Determinants.h:283-301): sign of the
+// number of occupied spin orbitals strictly between start and end.
+static double parity_between(const Det& d, int lo, int hi) {
+  int cnt = 0;
+  for (int p = lo + 1; p < hi; ++p) cnt += getocc(d, p);
+  return (cnt & 1) ? -1.0 : 1.0;
+}
+
+// Hij_1Excite(a, i, ..., closed, nclosed) (SHCI/Determinants.cpp:437-469):
+// a created, i destroyed; sum runs over the ket's occupied list in order.
+static double hij_1excite(const Ints& I, int a, int i, const int* closed, int nclosed) {
+  double sgn = 1.0;
+  double energy = I.i1(a, i);
+  int lo = std::min(i, a), hi = std::max(i, a);
+  for (int j = 0; j < nclosed; j++) {
+    if (closed[j] > lo && closed[j] < hi) sgn *= -1.;
+    energy += (I.i2(a, i, closed[j], closed[j]) - I.i2(a, closed[j], closed[j], i));
+  }
+  return energy * sgn;
+}
+
+// Determinant::Hij_2Excite(i, j, a, b) (SHCI/Determinants.cpp:406-434)
+static double hij_2excite(const Ints& I, const Det& ket, int i, int j, int a, int b) {
+  double sgn = 1.0;
+  int II = std::min(i, j), JJ = std::max(i, j), A = std::min(a, b), B = std::max(a, b);
+  sgn *= parity_between(ket, std::min(II, A), std::max(II, A));
+  sgn *= parity_between(ket, std::min(JJ, B), std::max(JJ, B));
+  if (A > JJ || B < II) sgn *= -1.;
+  return sgn * (I.i2(A, II, B, JJ) - I.i2(A, JJ, B, II));
+}
+
+// Hij(bra, ket) (SHCI/Determinants.cpp:564-631)
+static double hij(const Ints& I, const Det& bra, const Det& ket) {
+  int cre[4], des[4], ncre = 0, ndes = 0;
+  for (int w = 0; w < W; ++w) {
+    uint64_t u = bra.w[w] ^ ket.w[w];
+    uint64_t b = u & bra.w[w], k = u & ket.w[w];
+    while (b) {
+      int pos = __builtin_ctzll(b);
+      if (ncre < 4) cre[ncre] = pos + 64 * w;
+      ncre++;
+      b &= b - 1;
+    }
+    while (k) {
+      int pos = __builtin_ctzll(k);
+      if (ndes < 4) des[ndes] = pos + 64 * w;
+      ndes++;
+      k &= k - 1;
+    }
+  }
+  if (ncre == 1) {
+    int closed[128];
+    int nc = closed_list(ket, 2 * I.norb, closed);
+    // ket.Hij_1Excite(cre, des) sums over the ket's occupied orbitals
+    // (SHCI/Determinants.cpp:472-505); same arithmetic as the free function.
+    return hij_1excite(I, cre[0], des[0], closed, nc);
+  } else if (ncre == 2) {
+    return hij_2excite(I, ket, des[0], des[1], cre[0], cre[1]);
+  }
+  return 0.0;
+}
+
+static inline int excitation_distance(const Det& a, const Det& b) {
+  int n = 0;
+  for (int w = 0; w < W; ++w) n += popc(a.w[w] ^ b.w[w]);
+  return n / 2;
+}
+
+// ---------------------------------------------------------------------------
+// Occupation restrictions (SHCI/OccRestrictions.cpp)
+// ---------------------------------------------------------------------------
+struct Restriction {
+  int minElec, maxElec;
+  std::vector<int> orbs;  // spin orbitals
+  int currentElec = 0;
+};
+static void restrictions_init(std::vector<Restriction>& rs, const int* closed, int nc) {
+  for (auto& r : rs) {
+    r.currentElec = 0;
+    for (int i = 0; i < nc; i++)
+      for (int o : r.orbs)
+        if (o == closed[i]) r.currentElec++;
+  }
+}
+static bool restr_one(const std::vector<Restriction>& rs, int i, int a) {
+  for (auto& r : rs) {
+    int e = r.currentElec;
+    for (int o : r.orbs) {
+      if (o == i) e--;
+      if (o == a) e++;
+    }
+    if (e < r.minElec || e > r.maxElec) return false;
+  }
+  return true;
+}
+static bool restr_two(const std::vector<Restriction>& rs, int i, int j, int a, int b) {
+  for (auto& r : rs) {
+    int e = r.currentElec;
+    for (int o : r.orbs) {
+      if (o == i || o == j) e--;
+      if (o == a || o == b) e++;
+    }
+    if (e < r.minElec || e > r.maxElec) return false;
+  }
+  return true;
+}
+
+struct SelParams {
+  int ncore = 0;
+  int nact = 1000000;
+  std::vector<Restriction> restrictions;
+};
+
+// SHCIgetdeterminants::getDeterminantsVariationalApprox
+// (SHCI/SHCIgetdeterminants.cpp:586-739)
+static void select_from_parent(const Ints& I, const HeatBath& hb, const Det& d, double epsilon,
+                               SelParams& sp, const Det* sorted, size_t nsorted,
+                               std::vector<Det>& out) {
+  const int nspin = 2 * I.norb;
+  int closed[128], open[128];
+  int nclosed = 0, nopen = 0;
+  for (int p = 0; p < nspin; ++p) {
+    if (getocc(d, p))
+      closed[nclosed++] = p;
+    else
+      open[nopen++] = p;
+  }
+  restrictions_init(sp.restrictions, closed, nclosed);
+  auto present = [&](const Det& x) {
+    return std::binary_search(sorted, sorted + nsorted, x, det_less);
+  };
+  const int n2 = nspin;
+  for (int ia = 0; ia < nopen * nclosed; ia++) {
+    int i = ia / nopen, a = ia % nopen;
+    if (closed[i] / 2 < sp.ncore || open[a] / 2 >= sp.ncore + sp.nact) continue;
+    if (!restr_one(sp.restrictions, closed[i], open[a])) continue;
+    double integral = hb.Singles[(size_t)open[a] * n2 + closed[i]];
+    if (fabs(integral) > epsilon)
+      if (closed[i] % 2 == open[a] % 2)
+        integral = hij_1excite(I, open[a], closed[i], closed, nclosed);
+    if (fabs(integral) > epsilon) {
+      Det di = d;
+      setocc(di, open[a], true);
+      setocc(di, closed[i], false);
+      if (!present(di)) out.push_back(di);
+    }
+  }
+  if (fabs(I.maxEntry) < epsilon) return;
+  for (int ij = 0; ij < nclosed * nclosed; ij++) {
+    int i = ij / nclosed, j = ij % nclosed;
+    if (i <= j) continue;
+    int Ii = closed[i] / 2, Jj = closed[j] / 2;
+    int X = std::max(Ii, Jj), Y = std::min(Ii, Jj);
+    if (closed[i] / 2 < sp.ncore || closed[j] / 2 < sp.ncore) continue;
+    int pairIndex = X * (X + 1) / 2 + Y;
+    bool same = closed[i] % 2 == closed[j] % 2;
+    size_t start = same ? hb.sameStart[pairIndex] : hb.oppStart[pairIndex];
+    size_t end = same ? hb.sameStart[pairIndex + 1] : hb.oppStart[pairIndex + 1];
+    const float* integrals = same ? hb.sameVal.data() : hb.oppVal.data();
+    const int16_t* orbIndices = same ? hb.samePairs.data() : hb.oppPairs.data();
+    for (size_t index = start; index < end; index++) {
+      if (fabsf(integrals[index]) < epsilon) break;
+      int a = 2 * orbIndices[2 * index] + closed[i] % 2;
+      int b = 2 * orbIndices[2 * index + 1] + closed[j] % 2;
+      if (a / 2 >= sp.ncore + sp.nact || b / 2 >= sp.ncore + sp.nact) continue;
+      if (!restr_two(sp.restrictions, closed[i], closed[j], a, b)) continue;
+      if (!(getocc(d, a) || getocc(d, b))) {
+        Det di = d;
+        setocc(di, a, true);
+        setocc(di, b, true);
+        setocc(di, closed[i], false);
+        setocc(di, closed[j], false);
+        if (!present(di)) out.push_back(di);
+      }
+    }
+  }
+}
+
+// Selection over all parents + sort/unique (SHCI/SHCIbasics.cpp:954-994)
+static void select_all(const Ints& I, const HeatBath& hb, const Det* dets, size_t n, const double* cmax,
+                       double eps1, SelParams& sp, const Det* sorted, size_t nsorted,
+                       std::vector<Det>& newdets) {
+  newdets.clear();
+  for (size_t i = 0; i < n; i++)
+    select_from_parent(I, hb, dets[i], eps1 / fabs(cmax[i]), sp, sorted, nsorted, newdets);
+  std::sort(newdets.begin(), newdets.end(), det_less);
+  newdets.erase(std::unique(newdets.begin(), newdets.end(), det_eq), newdets.end());
+}
+
+// ---------------------------------------------------------------------------
+// Sparse Hamiltonian: lower triangle with diagonal first, as SparseHam holds it
+// (SHCI/SHCImakeHamiltonian.cpp:486-715). Connections are every J < I at
+// excitation distance 1 or 2; values Hij(Dets[J], Dets[I]).
+// The reference finds them through alpha/beta string helper lists
+// (:184-408); the oracle finds the same set by grouping on strings too.
+// ---------------------------------------------------------------------------
+struct SparseHam {
+  std::vector<int64_t> rowptr;  // N+1
+  std::vector<int32_t> col;
+  std::vector<double> val;
+};
+
+static inline uint64_t spin_string(const Det& d, int s) {
+  // getAlpha/getBeta (SHCI/Determinants.h:471-487): orbital k of spin s is
+  // spin-orbital 2k+s.
+  uint64_t out = 0;
+  for (int w = 0; w < W; ++w) {
+    uint64_t x = d.w[w] >> s;
+    for (int k = 0; k < 32; ++k)
+      if ((x >> (2 * k)) & 1ull) out |= 1ull << (32 * w + k);
+  }
+  return out;
+}
+
+static void build_ham(const Ints& I, const Det* dets, size_t N, SparseHam& H) {
+  std::unordered_map<uint64_t, int> amap, bmap;
+  std::vector<uint64_t> astr, bstr;
+  std::vector<int> aidx(N), bidx(N);
+  for (size_t k = 0; k < N; ++k) {
+    uint64_t a = spin_string(dets[k], 0), b = spin_string(dets[k], 1);
+    auto ia = amap.emplace(a, (int)astr.size());
+    if (ia.second) astr.push_back(a);
+    auto ib = bmap.emplace(b, (int)bstr.size());
+    if (ib.second) bstr.push_back(b);
+    aidx[k] = ia.first->second;
+    bidx[k] = ib.first->second;
+  }
+  std::vector<std::vector<int>> byA(astr.size()), byB(bstr.size());
+  for (size_t k = 0; k < N; ++k) {
+    byA[aidx[k]].push_back((int)k);
+    byB[bidx[k]].push_back((int)k);
+  }
+  // single-excitation neighbours among the present alpha strings
+  const int n = I.norb;
+  std::vector<std::vector<int>> singA(astr.size());
+  for (size_t s = 0; s < astr.size(); ++s) {
+    uint64_t x = astr[s];
+    for (int i = 0; i < n; ++i) {
+      if (!((x >> i) & 1)) continue;
+      for (int a = 0; a < n; ++a) {
+        if ((x >> a) & 1) continue;
+        uint64_t y = (x & ~(1ull << i)) | (1ull << a);
+        auto it = amap.find(y);
+        if (it != amap.end()) singA[s].push_back(it->second);
+      }
+    }
+  }
+  H.rowptr.assign(N + 1, 0);
+  H.col.clear();
+  H.val.clear();
+  std::vector<int> row;
+  for (size_t I_ = 0; I_ < N; ++I_) {
+    row.clear();
+    const uint64_t A = astr[aidx[I_]], B = bstr[bidx[I_]];
+    // same alpha string: beta single or double
+    for (int J : byA[aidx[I_]]) {
+      if ((size_t)J >= I_) continue;
+      int d = popc(bstr[bidx[J]] ^ B);
+      if (d == 2 || d == 4) row.push_back(J);
+    }
+    // alpha single: beta equal (single alpha) or beta single (alpha-beta double)
+    for (int As : singA[aidx[I_]])
+      for (int J : byA[As]) {
+        if ((size_t)J >= I_) continue;
+        int d = popc(bstr[bidx[J]] ^ B);
+        if (d == 0 || d == 2) row.push_back(J);
+      }
+    // same beta string: alpha double
+    for (int J : byB[bidx[I_]]) {
+      if ((size_t)J >= I_) continue;
+      int d = popc(astr[aidx[J]] ^ A);
+      if (d == 4) row.push_back(J);
+    }
+    std::sort(row.begin(), row.end());
+    H.col.push_back((int32_t)I_);
+    H.val.push_back(det_energy(I, dets[I_]));
+    for (int J : row) {
+      H.col.push_back(J);
+      H.val.push_back(hij(I, dets[J], dets[I_]));
+    }
+    H.rowptr[I_ + 1] = H.col.size();
+  }
+}
+
+// Hmult2::operator() (SHCI/Hmult.h:52-150), serial branch: symmetric
+// scatter from the lower triangle.
+static void sigma(const SparseHam& H, size_t N, const double* x, double* y) {
+  std::vector<double> yt(N, 0.0);
+  for (size_t i = 0; i < N; i++) {
+    for (int64_t p = H.rowptr[i]; p < H.rowptr[i + 1]; ++p) {
+      double h = H.val[p];
+      int J = H.col[p];
+      yt[i] += h * x[J];
+      if ((size_t)J != i) yt[J] += h * x[i];
+    }
+  }
+  for (size_t j = 0; j < N; j++) y[j] = yt[j];
+}
+
+// ---------------------------------------------------------------------------
+// Dense symmetric eigensolver (cyclic Jacobi) for the Davidson subspace. The
+// reference uses Eigen::SelfAdjointEigenSolver (SHCI/Davidson.cpp:262); both
+// return ascending eigenvalues with orthonormal eigenvectors.
+// ---------------------------------------------------------------------------
+static void jacobi_eig(int m, std::vector<double> A, std::vector<double>& evals, std::vector<double>& evecs) {
+  // A row-major m x m symmetric; evecs column-major m x m (column k = vector k)
+  std::vector<double> V((size_t)m * m, 0.0);
+  for (int i = 0; i < m; ++i) V[(size_t)i * m + i] = 1.0;
+  for (int sweep = 0; sweep < 100; ++sweep) {
+    double off = 0.0;
+    for (int p = 0; p < m; ++p)
+      for (int q = p + 1; q < m; ++q) off += A[(size_t)p * m + q] * A[(size_t)p * m + q];
+    if (off < 1e-300) break;
+    for (int p = 0; p < m; ++p)
+      for (int q = p + 1; q < m; ++q) {
+        double apq = A[(size_t)p * m + q];
+        if (fabs(apq) < 1e-300) continue;
+        double app = A[(size_t)p * m + p], aqq = A[(size_t)q * m + q];
+        double theta = (aqq - app) / (2.0 * apq);
+        double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+        double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+        for (int k = 0; k < m; ++k) {
+          double akp = A[(size_t)k * m + p], akq = A[(size_t)k * m + q];
+          A[(size_t)k * m + p] = c * akp - s * akq;
+          A[(size_t)k * m + q] = s * akp + c * akq;
+        }
+        for (int k = 0; k < m; ++k) {
+          double apk = A[(size_t)p * m + k], aqk = A[(size_t)q * m + k];
+          A[(size_t)p * m + k] = c * apk - s * aqk;
+          A[(size_t)q * m + k] = s * apk + c * aqk;
+        }
+        for (int k = 0; k < m; ++k) {
+          double vkp = V[(size_t)k * m + p], vkq = V[(size_t)k * m + q];
+          V[(size_t)k * m + p] = c * vkp - s * vkq;
+          V[(size_t)k * m + q] = s * vkp + c * vkq;
+        }
+      }
+  }
+  std::vector<int> ord(m);
+  std::iota(ord.begin(), ord.end(), 0);
+  std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return A[(size_t)x * m + x] < A[(size_t)y * m + y]; });
+  evals.resize(m);
+  evecs.assign((size_t)m * m, 0.0);
+  for (int k = 0; k < m; ++k) {
+    evals[k] = A[(size_t)ord[k] * m + ord[k]];
+    for (int i = 0; i < m; ++i) evecs[(size_t)k * m + i] = V[(size_t)i * m + ord[k]];
+  }
+}
+
+static double dot(const double* a, const double* b, size_t n) {
+  double s = 0.0;
+  for (size_t i = 0; i < n; ++i) s += a[i] * b[i];
+  return s;
+}
+
+// Deterministic stand-in for Eigen's setRandom (uniform in [-1,1]); the
+// reference seeds it from the clock unless `seed` is given.
+static uint64_t g_rng = 0x9E3779B97F4A7C15ull;
+static double rnd_pm1() {
+  g_rng ^= g_rng << 13;
+  g_rng ^= g_rng >> 7;
+  g_rng ^= g_rng << 17;
+  return ((g_rng >> 11) * (1.0 / 9007199254740992.0)) * 2.0 - 1.0;
+}
+
+// davidson / davidsonDirect (SHCI/Davidson.cpp:111-348, :353-590) and
+// precondition (:85-106). `direct` selects davidsonDirect's collapse rule and
+// iteration cap. Returns 0 on success, 1 on non-convergence.
+static int davidson(const SparseHam& H, size_t N, std::vector<std::vector<double>>& x0,
+                    const std::vector<double>& diag, int maxCopies, double tol, bool direct,
+                    std::vector<double>& eroots, int& numIter) {
+  const int nroots = (int)x0.size();
+  eroots.clear();
+  std::vector<std::vector<double>> b(maxCopies, std::vector<double>(N, 0.0));
+  std::vector<std::vector<double>> sig(maxCopies, std::vector<double>(N, 0.0));
+  for (int i = 0; i < nroots; i++) {
+    b[i] = x0[i];
+    if (sqrt(dot(x0[i].data(), x0[i].data(), N)) < 1.e-10) {
+      for (size_t k = 0; k < N; ++k) b[i][k] = rnd_pm1();
+      double nn = sqrt(dot(b[i].data(), b[i].data(), N));
+      for (size_t k = 0; k < N; ++k) b[i][k] /= nn;
+    }
+  }
+  for (int i = 0; i < nroots; i++) {
+    for (int j = 0; j < i; j++) {
+      double ov = dot(b[j].data(), b[i].data(), N);
+      for (size_t k = 0; k < N; ++k) b[i][k] -= ov * b[j][k];
+    }
+    if (sqrt(dot(b[i].data(), b[i].data(), N)) < 1e-8)
+      for (size_t k = 0; k < N; ++k) b[i][k] = rnd_pm1();
+    for (int j = 0; j < i; j++) {
+      double ov = dot(b[j].data(), b[i].data(), N);
+      for (size_t k = 0; k < N; ++k) b[i][k] -= ov * b[j][k];
+    }
+    double nn = sqrt(dot(b[i].data(), b[i].data(), N));
+    for (size_t k = 0; k < N; ++k) b[i][k] /= nn;
+  }
+  int sigmaSize = 0, bsize = nroots;
+  std::vector<double> r(N);
+  int convergedRoot = 0;
+  numIter = 0;
+  double ei = 0.0;
+  std::vector<double> tmp;
+  while (true) {
+    for (int i = sigmaSize; i < bsize; i++) {
+      sigma(H, N, b[i].data(), sig[i].data());
+      sigmaSize++;
+    }
+    std::vector<double> hs((size_t)bsize * bsize);
+    for (int i = 0; i < bsize; i++)
+      for (int j = i; j < bsize; j++) {
+        hs[(size_t)i * bsize + j] = dot(b[i].data(), sig[j].data(), N);
+        hs[(size_t)j * bsize + i] = hs[(size_t)i * bsize + j];
+      }
+    std::vector<double> ev, evec;
+    jacobi_eig(bsize, hs, ev, evec);
+    // b <- b * V ; sigma <- sigma * V
+    tmp.assign((size_t)bsize * N, 0.0);
+    for (int kcol = 0; kcol < bsize; ++kcol)
+      for (int i = 0; i < bsize; ++i) {
+        double c = evec[(size_t)kcol * bsize + i];
+        const double* src = b[i].data();
+        double* dst = &tmp[(size_t)kcol * N];
+        for (size_t k = 0; k < N; ++k) dst[k] += c * src[k];
+      }
+    for (int kcol = 0; kcol < bsize; ++kcol) std::copy(&tmp[(size_t)kcol * N], &tmp[(size_t)kcol * N] + N, b[kcol].begin());
+    tmp.assign((size_t)bsize * N, 0.0);
+    for (int kcol = 0; kcol < bsize; ++kcol)
+      for (int i = 0; i < bsize; ++i) {
+        double c = evec[(size_t)kcol * bsize + i];
+        const double* src = sig[i].data();
+        double* dst = &tmp[(size_t)kcol * N];
+        for (size_t k = 0; k < N; ++k) dst[k] += c * src[k];
+      }
+    for (int kcol = 0; kcol < bsize; ++kcol) std::copy(&tmp[(size_t)kcol * N], &tmp[(size_t)kcol * N] + N, sig[kcol].begin());
+
+    ei = ev[convergedRoot];
+    for (int i = 0; i < convergedRoot; i++) {
+      for (size_t k = 0; k < N; ++k) r[k] = sig[i][k] - ev[i] * b[i][k];
+      double error = sqrt(dot(r.data(), r.data(), N));
+      if (error > tol) convergedRoot = i;
+    }
+    for (size_t k = 0; k < N; ++k) r[k] = sig[convergedRoot][k] - ei * b[convergedRoot][k];
+    double error = sqrt(dot(r.data(), r.data(), N));
+    numIter++;
+    if ((size_t)bsize == N) {
+      for (int i = 0; i < nroots; i++) {
+        x0[i] = b[i];
+        eroots.push_back(ev[i]);
+      }
+      return 0;
+    }
+    const int cap = direct ? 400 * nroots : 800 * nroots;
+    if (error < tol || numIter > cap) {
+      if (numIter > (direct ? 400 * nroots : 2000 * nroots)) return 1;
+      convergedRoot++;
+      if (convergedRoot == nroots) {
+        for (int i = 0; i < convergedRoot; i++) {
+          x0[i] = b[i];
+          eroots.push_back(ev[i]);
+        }
+        return 0;
+      }
+    }
+    for (size_t k = 0; k < N; ++k) {
+      if (fabs(ei - diag[k]) > 1e-12)
+        r[k] = r[k] / (ei - diag[k]);
+      else
+        r[k] = r[k] / (ei - diag[k] - 1.e-12);
+    }
+    for (int i = 0; i < bsize; i++) {
+      double ov = dot(b[i].data(), r.data(), N) / dot(b[i].data(), b[i].data(), N);
+      for (size_t k = 0; k < N; ++k) r[k] -= ov * b[i][k];
+    }
+    double rn = sqrt(dot(r.data(), r.data(), N));
+    if (bsize < maxCopies) {
+      for (size_t k = 0; k < N; ++k) b[bsize][k] = r[k] / rn;
+      bsize++;
+    } else {
+      if (direct) {
+        bsize = std::min(nroots + 3, maxCopies);
+        sigmaSize = bsize - 1;
+      } else {
+        bsize = nroots + 3;
+        sigmaSize = nroots + 2;
+      }
+      for (size_t k = 0; k < N; ++k) b[bsize - 1][k] = r[k] / rn;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// input.dat (SHCI/input.cpp:35-404), variational subset.
+// ---------------------------------------------------------------------------
+struct Schedule {
+  std::vector<std::vector<int>> occupied;
+  std::vector<double> epsilon1;
+  int nroots = 1;
+  double davidsonTol = 5e-5, davidsonTolLoose = 5e-5, dE = 1e-8;
+  bool direct = false;
+  SelParams sel;
+  std::string integralFile = "FCIDUMP";
+};
+
+static int read_input(const char* path, Schedule& s, std::string& err) {
+  std::ifstream ifs(path);
+  if (!ifs.good()) {
+    err = std::string("cannot open ") + path;
+    return 1;
+  }
+  std::stringstream dump;
+  dump << ifs.rdbuf();
+  int maxiter = -1, nocc = -1;
+  std::vector<int> sweep_iter;
+  std::vector<double> sweep_eps;
+  std::vector<std::string> tok;
+  while (dump.good()) {
+    std::string Line;
+    std::getline(dump, Line);
+    split_compress(Line, ", \t\n", tok);
+    std::string arg = tok[0];
+    if (arg.empty() || arg[0] == '#') continue;
+    if (iequals(arg, "nocc")) {
+      nocc = atoi(tok[1].c_str());
+      std::getline(dump, Line);
+      split_compress(Line, ", \t", tok);
+      while (!iequals(tok[0], "end")) {
+        if ((int)tok.size() != nocc) {
+          err = "nocc count mismatch";
+          return 2;
+        }
+        std::vector<int> occ;
+        for (auto& t : tok) occ.push_back(atoi(t.c_str()));
+        s.occupied.push_back(occ);
+        std::getline(dump, Line);
+        split_compress(Line, ", \t", tok);
+      }
+    } else if (iequals(arg, "nact")) s.sel.nact = atoi(tok[1].c_str());
+    else if (iequals(arg, "ncore")) s.sel.ncore = atoi(tok[1].c_str());
+    else if (iequals(arg, "directdavidson")) s.direct = true;
+    else if (iequals(arg, "nroots")) s.nroots = (int)atof(tok[1].c_str());
+    else if (iequals(arg, "orbitals")) s.integralFile = tok[1];
+    else if (iequals(arg, "davidsonTol")) s.davidsonTol = atof(tok[1].c_str());
+    else if (iequals(arg, "davidsonTolLoose")) s.davidsonTolLoose = atof(tok[1].c_str());
+    else if (iequals(arg, "dE")) s.dE = atof(tok[1].c_str());
+    else if (iequals(arg, "maxiter")) maxiter = atoi(tok[1].c_str());
+    else if (iequals(arg, "restrict") || iequals(arg, "restrictv")) {
+      Restriction r;
+      r.minElec = atoi(tok[1].c_str());
+      r.maxElec = atoi(tok[2].c_str());
+      for (size_t i = 3; i < tok.size(); i++) {
+        r.orbs.push_back(2 * atoi(tok[i].c_str()));
+        r.orbs.push_back(2 * atoi(tok[i].c_str()) + 1);
+      }
+      s.sel.restrictions.push_back(r);
+    } else if (iequals(arg, "schedule")) {
+      std::getline(dump, Line);
+      std::vector<std::string> st;
+      split_compress(Line, " \t", st);
+      while (!iequals(st[0], "END")) {
+        if (st[0].empty() || st[0][0] != '#') {
+          sweep_iter.push_back(atoi(st[0].c_str()));
+          sweep_eps.push_back(atof(st.size() > 1 ? st[1].c_str() : "0"));
+        }
+        if (!dump.good()) break;
+        std::getline(dump, Line);
+        split_compress(Line, " \t", st);
+      }
+    }
+    // every other keyword belongs to stages outside the variational path
+  }
+  if (sweep_iter.empty() || maxiter < sweep_iter.back()) {
+    err = "maxiter should be greater than last entry of sweep_iter";
+    return 3;
+  }
+  if (nocc == -1) {
+    err = "nocc keyword has to be included.";
+    return 4;
+  }
+  if (s.direct) s.davidsonTolLoose = 3.e-2;
+  for (size_t i = 1; i < sweep_iter.size(); i++)
+    for (int j = sweep_iter[i - 1]; j < sweep_iter[i]; j++) s.epsilon1.push_back(sweep_eps[i - 1]);
+  for (int j = sweep_iter.back(); j < maxiter; j++) s.epsilon1.push_back(sweep_eps.back());
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Variational driver: SHCI/SHCI.cpp:289-427 (reference dets, initial ci) and
+// SHCIbasics::DoVariational (SHCI/SHCIbasics.cpp:783-1378), serial, no Trev,
+// no restart files.
+// ---------------------------------------------------------------------------
+struct IterLog {
+  int iter;
+  double eps1;
+  int64_t ndets;
+  double energy;  // root 0, coreE added
+  int davidson_iters;
+  double seconds;
+};
+struct VarResult {
+  std::vector<double> E;  // per root, coreE added
+  std::vector<Det> dets;  // final variational space, in index order
+  std::vector<std::vector<double>> ci;
+  std::vector<IterLog> log;
+  int64_t nnz_lower = 0;
+  double seconds = 0.0;
+};
+
+static double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+static int do_variational(const Ints& I, const HeatBath& hb, Schedule& s, VarResult& res, std::string& err,
+                          int verbose) {
+  double t0 = now_s();
+  // reference dets and initial ci (SHCI/SHCI.cpp:289-399)
+  std::vector<Det> Dets(s.occupied.size());
+  int lowest = 0;
+  double lowestE = 1e12;
+  for (size_t d = 0; d < s.occupied.size(); ++d) {
+    memset(&Dets[d], 0, sizeof(Det));
+    for (int p : s.occupied[d]) {
+      if (p < 0 || p >= 2 * I.norb || getocc(Dets[d], p)) {
+        err = "bad or repeated orbital in nocc";
+        return 1;
+      }
+      setocc(Dets[d], p, true);
+    }
+    if ((int)s.occupied[d].size() != I.nelec) {
+      err = "nocc differs from NELEC";
+      return 2;
+    }
+    double E = det_energy(I, Dets[d]) + I.coreE;
+    if (E < lowestE) {
+      lowestE = E;
+      lowest = (int)d;
+    }
+  }
+  const int nroots = s.nroots;
+  std::vector<std::vector<double>> ci(nroots, std::vector<double>(Dets.size(), 0.0));
+  for (size_t j = 0; j < Dets.size(); ++j) ci[0][j] = 1.0;
+  ci[0][lowest] += Dets.size();
+  double nn = sqrt(dot(ci[0].data(), ci[0].data(), Dets.size()));
+  for (auto& v : ci[0]) v /= nn;
+
+  std::vector<Det> sorted = Dets;
+  std::sort(sorted.begin(), sorted.end(), det_less);
+  std::vector<double> diag;
+  std::vector<double> E0(nroots, fabs(det_energy(I, Dets[0])));
+  SparseHam H;
+  for (size_t iter = 0; iter < s.epsilon1.size(); ++iter) {
+    double eps1 = s.epsilon1[iter];
+    size_t N0 = Dets.size();
+    std::vector<double> cMax(N0, 0.0);
+    for (size_t j = 0; j < N0; j++) {
+      for (int i = 0; i < nroots; i++) cMax[j] += pow(fabs(ci[i][j]), 2);
+      cMax[j] = pow(cMax[j], 0.5);
+    }
+    std::vector<Det> newDets;
+    select_all(I, hb, Dets.data(), N0, cMax.data(), eps1, s.sel, sorted.data(), sorted.size(), newDets);
+    std::vector<std::vector<double>> X0(nroots, std::vector<double>(N0 + newDets.size(), 0.0));
+    for (int i = 0; i < nroots; i++) std::copy(ci[i].begin(), ci[i].end(), X0[i].begin());
+    Dets.insert(Dets.end(), newDets.begin(), newDets.end());
+    size_t N = Dets.size();
+    build_ham(I, Dets.data(), N, H);
+    sorted = Dets;
+    std::sort(sorted.begin(), sorted.end(), det_less);
+    size_t old = diag.size();
+    diag.resize(N);
+    for (size_t k = old; k < N; ++k) diag[k] = det_energy(I, Dets[k]);
+    double prevE0 = (iter == 0) ? -10.0 : E0[0];
+    int numIter = 0;
+    std::vector<double> ev;
+    int rc = davidson(H, N, X0, diag, s.direct ? nroots + 2 : nroots + 4, s.davidsonTolLoose, s.direct, ev,
+                      numIter);
+    if (rc) {
+      err = "Davidson calculation did not converge";
+      return 3;
+    }
+    E0 = ev;
+    ci = X0;
+    res.log.push_back({(int)iter, eps1, (int64_t)N, E0[0] + I.coreE, numIter, now_s() - t0});
+    if (verbose)
+      printf("%4d %4d  %10.2e  %10zu   %18.10f  %9d  %10.2f\n", (int)iter, 0, eps1, N, E0[0] + I.coreE, numIter,
+             now_s() - t0);
+    if (fabs(E0[0] - prevE0) < s.dE || iter == s.epsilon1.size() - 1) {
+      rc = davidson(H, N, ci, diag, nroots + 4, s.davidsonTol, s.direct, ev, numIter);
+      if (rc) {
+        err = "Davidson calculation did not converge";
+        return 3;
+      }
+      E0 = ev;
+      break;
+    }
+  }
+  res.E.resize(nroots);
+  for (int i = 0; i < nroots; ++i) res.E[i] = E0[i] + I.coreE;
+  res.dets = Dets;
+  res.ci = ci;
+  res.nnz_lower = H.col.size();
+  res.seconds = now_s() - t0;
+  return 0;
+}
+
+}  // namespace orc
+
+// ===========================================================================
+// C interface used by the Python test harness (oracle/oracle.py).
+// ===========================================================================
+using namespace orc;
+
+struct orc_ctx {
+  Ints ints;
+  HeatBath hb;
+  SparseHam ham;
+  size_t ham_n = 0;
+  VarResult var;
+  std::string err;
+};
+
+extern "C" {
+
+const char* orc_last_error(orc_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+orc_ctx* orc_load(const char* fcidump, char* errbuf, int errlen) {
+  orc_ctx* c = new orc_ctx();
+  std::string err;
+  if (read_fcidump(fcidump, c->ints, err)) {
+    if (errbuf && errlen > 0) snprintf(errbuf, errlen, "%s", err.c_str());
+    delete c;
+    return nullptr;
+  }
+  build_heatbath(c->ints, c->hb);
+  return c;
+}
+
+void orc_free(orc_ctx* c) { delete c; }
+
+void orc_info(orc_ctx* c, int* norb, int* nelec, double* coreE, double* maxEntry) {
+  *norb = c->ints.norb;
+  *nelec = c->ints.nelec;
+  *coreE = c->ints.coreE;
+  *maxEntry = c->ints.maxEntry;
+}
+
+// packed integrals, for cross-checking the GPU library's reader
+int64_t orc_i2_size(orc_ctx* c) { return (int64_t)c->ints.I2.size(); }
+void orc_i2_export(orc_ctx* c, double* out) { std::copy(c->ints.I2.begin(), c->ints.I2.end(), out); }
+void orc_i1_export(orc_ctx* c, double* out) { std::copy(c->ints.I1.begin(), c->ints.I1.end(), out); }
+
+int64_t orc_hb_size(orc_ctx* c, int same) { return same ? c->hb.sameVal.size() : c->hb.oppVal.size(); }
+void orc_hb_export(orc_ctx* c, int same, float* vals, int16_t* pairs, uint64_t* starts, double* singles) {
+  auto& V = same ? c->hb.sameVal : c->hb.oppVal;
+  auto& P = same ? c->hb.samePairs : c->hb.oppPairs;
+  auto& S = same ? c->hb.sameStart : c->hb.oppStart;
+  if (vals) std::copy(V.begin(), V.end(), vals);
+  if (pairs) std::copy(P.begin(), P.end(), pairs);
+  if (starts) std::copy(S.begin(), S.end(), starts);
+  if (singles) std::copy(c->hb.Singles.begin(), c->hb.Singles.end(), singles);
+}
+
+double orc_energy(orc_ctx* c, const uint64_t* det) {
+  Det d;
+  memcpy(&d, det, sizeof(Det));
+  return det_energy(c->ints, d);
+}
+
+double orc_hij(orc_ctx* c, const uint64_t* bra, const uint64_t* ket) {
+  Det b, k;
+  memcpy(&b, bra, sizeof(Det));
+  memcpy(&k, ket, sizeof(Det));
+  return hij(c->ints, b, k);
+}
+
+// Selection from every parent with threshold eps1/|cmax_i|; candidates present
+// in `existing` are dropped; result sorted and unique. restr: nrestr triples
+// (min, max, spatial-orbital mask lo, hi) packed as int64[4].
+int64_t orc_select(orc_ctx* c, const uint64_t* dets, int64_t n, const double* cmax, double eps1,
+                   const uint64_t* existing_sorted, int64_t nexisting, int ncore, int nact,
+                   const int64_t* restr, int nrestr, uint64_t* out, int64_t cap) {
+  SelParams sp;
+  sp.ncore = ncore;
+  sp.nact = nact;
+  for (int r = 0; r < nrestr; ++r) {
+    Restriction R;
+    R.minElec = (int)restr[4 * r];
+    R.maxElec = (int)restr[4 * r + 1];
+    uint64_t m0 = (uint64_t)restr[4 * r + 2];
+    for (int k = 0; k < 64; ++k)
+      if ((m0 >> k) & 1) {
+        R.orbs.push_back(2 * k);
+        R.orbs.push_back(2 * k + 1);
+      }
+    sp.restrictions.push_back(R);
+  }
+  std::vector<Det> nd;
+  select_all(c->ints, c->hb, (const Det*)dets, (size_t)n, cmax, eps1, sp, (const Det*)existing_sorted,
+             (size_t)nexisting, nd);
+  if ((int64_t)nd.size() <= cap) memcpy(out, nd.data(), nd.size() * sizeof(Det));
+  return (int64_t)nd.size();
+}
+
+// Lower-triangle Hamiltonian with the diagonal first in every row (SparseHam).
+int64_t orc_ham_build(orc_ctx* c, const uint64_t* dets, int64_t n) {
+  build_ham(c->ints, (const Det*)dets, (size_t)n, c->ham);
+  c->ham_n = (size_t)n;
+  return (int64_t)c->ham.col.size();
+}
+void orc_ham_export(orc_ctx* c, int64_t* rowptr, int32_t* col, double* val) {
+  std::copy(c->ham.rowptr.begin(), c->ham.rowptr.end(), rowptr);
+  std::copy(c->ham.col.begin(), c->ham.col.end(), col);
+  std::copy(c->ham.val.begin(), c->ham.val.end(), val);
+}
+void orc_sigma(orc_ctx* c, const double* x, double* y) { sigma(c->ham, c->ham_n, x, y); }
+
+// Dice's Davidson on the last built Hamiltonian. x0: nroots x n (row major);
+// overwritten by the eigenvectors. Returns 0 or 1 (no convergence).
+int orc_davidson(orc_ctx* c, double* x0, int nroots, const double* diag, int maxCopies, double tol, int direct,
+                 double* eroots, int* numIter) {
+  size_t n = c->ham_n;
+  std::vector<std::vector<double>> X(nroots, std::vector<double>(n));
+  for (int r = 0; r < nroots; ++r) std::copy(x0 + r * n, x0 + (r + 1) * n, X[r].begin());
+  std::vector<double> d(diag, diag + n), ev;
+  int rc = davidson(c->ham, n, X, d, maxCopies, tol, direct != 0, ev, *numIter);
+  if (rc) return rc;
+  for (int r = 0; r < nroots; ++r) {
+    std::copy(X[r].begin(), X[r].end(), x0 + r * n);
+    eroots[r] = ev[r];
+  }
+  return 0;
+}
+
+// Whole variational stage from a Dice input file. The FCIDUMP named in the
+// input (or `fcidump_override`) is read relative to the current directory.
+int orc_run_input(orc_ctx** out_ctx, const char* input, const char* fcidump_override, int verbose, char* errbuf,
+                  int errlen) {
+  Schedule s;
+  std::string err;
+  if (read_input(input, s, err)) {
+    snprintf(errbuf, errlen, "%s", err.c_str());
+    return 1;
+  }
+  const char* path = fcidump_override ? fcidump_override : s.integralFile.c_str();
+  orc_ctx* c = orc_load(path, errbuf, errlen);
+  if (!c) return 2;
+  if (do_variational(c->ints, c->hb, s, c->var, err, verbose)) {
+    snprintf(errbuf, errlen, "%s", err.c_str());
+    delete c;
+    return 3;
+  }
+  *out_ctx = c;
+  return 0;
+}
+
+int orc_var_nroots(orc_ctx* c) { return (int)c->var.E.size(); }
+int64_t orc_var_ndets(orc_ctx* c) { return (int64_t)c->var.dets.size(); }
+int orc_var_niters(orc_ctx* c) { return (int)c->var.log.size(); }
+double orc_var_seconds(orc_ctx* c) { return c->var.seconds; }
+int64_t orc_var_nnz_lower(orc_ctx* c) { return c->var.nnz_lower; }
+void orc_var_energies(orc_ctx* c, double* E) { std::copy(c->var.E.begin(), c->var.E.end(), E); }
+void orc_var_log(orc_ctx* c, int64_t* ndets, double* energy, int* dav_iters, double* eps1, double* secs) {
+  for (size_t i = 0; i < c->var.log.size(); ++i) {
+    ndets[i] = c->var.log[i].ndets;
+    energy[i] = c->var.log[i].energy;
+    dav_iters[i] = c->var.log[i].davidson_iters;
+    eps1[i] = c->var.log[i].eps1;
+    secs[i] = c->var.log[i].seconds;
+  }
+}
+void orc_var_dets(orc_ctx* c, uint64_t* out) { memcpy(out, c->var.dets.data(), c->var.dets.size() * sizeof(Det)); }
+void orc_var_ci(orc_ctx* c, int root, double* out) {
+  std::copy(c->var.ci[root].begin(), c->var.ci[root].end(), out);
+}
+
+}  // extern "C"
+
+#ifdef ORACLE_MAIN
+int main(int argc, char** argv) {
+  if (argc < 2) {
+    fprintf(stderr, "usage: %s input.dat [FCIDUMP]\n", argv[0]);
+    return 1;
+  }
+  orc_ctx* c = nullptr;
+  char err[512];
+  int rc = orc_run_input(&c, argv[1], argc > 2 ? argv[2] : nullptr, 1, err, sizeof(err));
+  if (rc) {
+    fprintf(stderr, "error: %s\n", err);
+    return rc;
+  }
+  for (size_t i = 0; i < c->var.E.size(); ++i) printf("root %zu  E_var %.12f\n", i, c->var.E[i]);
+  printf("ndets %zu  seconds %.3f\n", c->var.dets.size(), c->var.seconds);
+  orc_free(c);
+  return 0;
+}
+#endif

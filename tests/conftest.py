@@ -1,0 +1,45 @@
+import gzip
+import os
+import shutil
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs the sm_103a library)")
+    config.addinivalue_line("markers", "slow: long CPU oracle run")
+
+
+def golden_case(tmp_path, name, input_name):
+    """Unpack a golden fixture (FCIDUMP + input file) into tmp_path; returns
+    the input path."""
+    d = tmp_path / name
+    d.mkdir(parents=True, exist_ok=True)
+    with gzip.open(os.path.join(GOLDEN, name + ".FCIDUMP.gz"), "rb") as f, open(d / "FCIDUMP", "wb") as g:
+        shutil.copyfileobj(f, g)
+    src = os.path.join(GOLDEN, name + "." + input_name)
+    text = open(src).read()
+    # inputs name their integral file relative to their own directory
+    text = text.replace("orbitals ./FCIDUMP", "orbitals FCIDUMP")
+    with open(d / "input.dat", "w") as f:
+        f.write(text)
+    return str(d / "input.dat")
+
+
+@pytest.fixture
+def golden(tmp_path):
+    return lambda name, inp: golden_case(tmp_path, name, inp)
+
+
+def gpu_available():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False

@@ -1,0 +1,107 @@
+"""Regenerate the golden fixtures in this directory from a checkout of the
+reference (sanshar/Dice).
+
+Usage: python tests/golden/make_golden.py /path/to/Dice
+
+What is copied, and what it pins:
+  * examples/h8_631g: FCIDUMP, dice.dat, the per-iteration table of dice.out
+    (determinant counts, energies, Davidson iterations) and the final
+    determinant set from the `dets` listing (2470 determinants with weights).
+  * tests/SHCI/restart: FCIDUMP and input3.dat; trusted_hci.e holds E_var of
+    the eps1 schedule 5e-3 -> 1e-3 -> 5e-5.
+  * tests/SHCI/n2_RAS: FCIDUMP, input.dat (with an occupation restriction),
+    trusted_hci.e (E_var).
+  * tests/SHCI/o2_det: FCIDUMP and input.dat (used as an extra parity case;
+    its trusted energy includes perturbation theory, which is not pinned).
+FCIDUMPs are stored gzip-compressed. Energies and tables go to golden.json.
+"""
+import gzip
+import json
+import os
+import re
+import shutil
+import struct
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def gz(src, dst):
+    with open(src, "rb") as f, open(dst, "wb") as raw:
+        with gzip.GzipFile(fileobj=raw, mode="wb", compresslevel=9, mtime=0) as g:
+            shutil.copyfileobj(f, g)
+
+
+def read_e(path):
+    with open(path, "rb") as f:
+        return struct.unpack("d", f.read(8))[0]
+
+
+def det_from_string(fields):
+    """Spatial-orbital occupation string ('2','a','b','0') -> two uint64 words
+    in the interleaved spin-orbital layout (alpha 2k, beta 2k+1)."""
+    w = [0, 0]
+    for k, c in enumerate(fields):
+        for s, on in ((0, c in ("2", "a")), (1, c in ("2", "b"))):
+            if on:
+                p = 2 * k + s
+                w[p // 64] |= 1 << (p % 64)
+    return w
+
+
+def main(ref):
+    out = {}
+    # h8 / 6-31G example
+    ex = os.path.join(ref, "examples", "h8_631g")
+    gz(os.path.join(ex, "FCIDUMP"), os.path.join(HERE, "h8_631g.FCIDUMP.gz"))
+    shutil.copy(os.path.join(ex, "dice.dat"), os.path.join(HERE, "h8_631g.dice.dat"))
+    table = []
+    result = None
+    lines = open(os.path.join(ex, "dice.out")).read().splitlines()
+    for i, ln in enumerate(lines):
+        m = re.match(r"\s*(\d+)\s+(\d+)\s+([0-9.eE+-]+)\s+(\d+)\s+(-?[0-9.]+)\s+(\d+)\s+([0-9.]+)\s*$", ln)
+        if m and result is None:
+            table.append({"iter": int(m.group(1)), "eps1": float(m.group(3)), "ndets": int(m.group(4)),
+                          "energy": float(m.group(5)), "davidson": int(m.group(6))})
+        if ln.strip().startswith("Root") and "Energy" in ln:
+            result = float(lines[i + 1].split()[1])
+    dets, weights = [], []
+    for ln in open(os.path.join(ex, "dets")):
+        f = ln.split()
+        if len(f) < 2:
+            continue
+        weights.append(float(f[0]))
+        dets.append(det_from_string(f[1:]))
+    np.savez_compressed(os.path.join(HERE, "h8_631g_dets.npz"),
+                        dets=np.array(dets, dtype=np.uint64), weights=np.array(weights))
+    out["h8_631g"] = {"table": table, "E_var": result, "ndets": len(dets),
+                      "source": "examples/h8_631g/dice.out, examples/h8_631g/dets"}
+
+    # restart fixture
+    rs = os.path.join(ref, "tests", "SHCI", "restart")
+    gz(os.path.join(rs, "FCIDUMP"), os.path.join(HERE, "restart.FCIDUMP.gz"))
+    shutil.copy(os.path.join(rs, "input3.dat"), os.path.join(HERE, "restart.input3.dat"))
+    out["restart"] = {"E_var": read_e(os.path.join(rs, "trusted_hci.e")), "tol": 5e-5,
+                      "source": "tests/SHCI/restart/trusted_hci.e (runTests.sh tolerance 5e-5)"}
+
+    # n2 with RAS restriction
+    n2 = os.path.join(ref, "tests", "SHCI", "n2_RAS")
+    gz(os.path.join(n2, "FCIDUMP"), os.path.join(HERE, "n2_RAS.FCIDUMP.gz"))
+    shutil.copy(os.path.join(n2, "input.dat"), os.path.join(HERE, "n2_RAS.input.dat"))
+    out["n2_RAS"] = {"E_var": read_e(os.path.join(n2, "trusted_hci.e")),
+                     "source": "tests/SHCI/n2_RAS/trusted_hci.e"}
+
+    # o2 (variational part only is used)
+    o2 = os.path.join(ref, "tests", "SHCI", "o2_det")
+    gz(os.path.join(o2, "FCIDUMP"), os.path.join(HERE, "o2.FCIDUMP.gz"))
+    shutil.copy(os.path.join(o2, "input.dat"), os.path.join(HERE, "o2.input.dat"))
+
+    with open(os.path.join(HERE, "golden.json"), "w") as f:
+        json.dump(out, f, indent=1)
+    print(json.dumps(out)[:400])
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

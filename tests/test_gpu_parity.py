@@ -1,0 +1,248 @@
+"""GPU parity: every stage of the CUDA path against the CPU oracle, through
+the C-ABI (dice_gb300.engine wraps include/shci_gpu.h with ctypes).
+
+Tolerances: integer/bit work (heat-bath tables, selection, connection sets,
+determinant order) is compared exactly; FP64 Slater-Condon values and
+diagonal energies bit-exactly (same summation order as the reference);
+FP64 sigma to 1e-12 relative (different summation order); mixed FP32 sigma
+to 2e-5 of the row scale; E_var to 1 uHa for the mixed path and 1e-9 Ha for
+the FP64 path."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from dice_gb300 import engine as eng
+from dice_gb300 import synthetic
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+G = json.load(open(os.path.join(GOLDEN, "golden.json")))
+
+
+def _fcidump(path_to_input):
+    return os.path.join(os.path.dirname(path_to_input), "FCIDUMP")
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    e = eng.Engine(0)
+    yield e
+    e.close()
+
+
+def _sorted_rows(rowptr, col, val):
+    """Full-row CSR -> dict {(i, j): v}"""
+    out = {}
+    for i in range(len(rowptr) - 1):
+        for p in range(rowptr[i], rowptr[i + 1]):
+            out[(i, int(col[p]))] = val[p]
+    return out
+
+
+def test_integrals_and_heatbath_bit_exact(gpu, golden):
+    inp = golden("h8_631g", "dice.dat")
+    o = orc.Oracle(_fcidump(inp))
+    n, ne, core = gpu.read_fcidump(_fcidump(inp))
+    assert (n, ne) == (o.norb, o.nelec) and core == o.coreE
+    for same in (0, 1):
+        v, p, s, sing = gpu.heatbath(same)
+        ov, op, os_, osing = o.heatbath(same)
+        assert np.array_equal(v, ov)
+        assert np.array_equal(p, op)
+        assert np.array_equal(s.astype(np.uint64), os_)
+        assert np.array_equal(sing, osing)
+
+
+def test_diag_and_hamiltonian_bit_exact(gpu, golden):
+    inp = golden("h8_631g", "dice.dat")
+    dets = np.load(os.path.join(GOLDEN, "h8_631g_dets.npz"))["dets"]
+    o = orc.Oracle(_fcidump(inp))
+    gpu.read_fcidump(_fcidump(inp))
+    gpu.set_dets(dets)
+    d = gpu.diag()
+    od = np.array([o.energy(x) for x in dets])
+    assert np.array_equal(d, od)
+    nnz = gpu.ham_build("fp64")
+    rowptr, col, val = gpu.ham_export(nnz)
+    orp, ocol, oval = o.ham(dets)
+    # oracle: lower triangle with the diagonal first in each row
+    ref = {}
+    for i in range(len(dets)):
+        for p in range(orp[i], orp[i + 1]):
+            j = int(ocol[p])
+            if j != i:
+                ref[(i, j)] = oval[p]
+                ref[(j, i)] = oval[p]
+    got = _sorted_rows(rowptr, col, val)
+    assert set(got) == set(ref)
+    assert all(got[k] == ref[k] for k in ref)
+    assert nnz == 2 * (len(ocol) - len(dets))
+
+
+def test_sigma_paths_against_oracle(gpu, golden):
+    inp = golden("h8_631g", "dice.dat")
+    dets = np.load(os.path.join(GOLDEN, "h8_631g_dets.npz"))["dets"]
+    o = orc.Oracle(_fcidump(inp))
+    gpu.read_fcidump(_fcidump(inp))
+    gpu.set_dets(dets)
+    o.ham(dets)
+    rng = np.random.default_rng(3)
+    X = rng.standard_normal((4, len(dets)))
+    ref = np.stack([o.sigma(x) for x in X])
+    gpu.ham_build("fp64")
+    for k in (1, 2, 3, 4):
+        y = gpu.sigma(X[:k], "fp64")
+        assert np.allclose(y, ref[:k], rtol=1e-12, atol=1e-12 * np.abs(ref).max())
+    y = gpu.sigma(X, "direct")
+    assert np.allclose(y, ref, rtol=1e-12, atol=1e-12 * np.abs(ref).max())
+    gpu.ham_build("mixed")
+    y32 = gpu.sigma(X, "mixed")
+    scale = np.abs(ref).max()
+    assert np.max(np.abs(y32 - ref)) < 2e-5 * scale
+    y64 = gpu.sigma(X, "fp64")  # head + tail refinement sigma
+    assert np.allclose(y64, ref, rtol=1e-11, atol=1e-11 * scale)
+
+
+def test_selection_bit_exact_given_same_c(gpu, golden):
+    inp = golden("h8_631g", "dice.dat")
+    run = orc.run_input(inp)
+    o = run.oracle
+    gpu.read_fcidump(_fcidump(inp))
+    gpu.set_selection_params(0, 8)  # the input's nact 8
+    # parents: the first 187 determinants of the final space with the final c
+    for npar, eps1 in ((187, 1e-6), (1693, 1e-6), (2470, 1e-5), (2470, 1e-7)):
+        parents = run.dets[:npar]
+        c = np.abs(run.ci[0][:npar])
+        existing = np.array(sorted(map(tuple, parents.tolist()), key=lambda t: (np.int64(np.uint64(t[1])),
+                                                                                 np.int64(np.uint64(t[0])))),
+                            dtype=np.uint64)
+        ref = o.select(parents, c, eps1, existing, ncore=0, nact=8)
+        gpu.set_dets(parents)
+        nnew = gpu.select(c, eps1)
+        got = gpu.dets()[npar:]
+        assert nnew == len(ref)
+        assert np.array_equal(got, ref)  # same set, same (reference) order
+
+
+def test_selection_with_restriction(gpu, golden):
+    inp = golden("n2_RAS", "input.dat")
+    run = orc.run_input(inp)
+    o = run.oracle
+    gpu.read_fcidump(_fcidump(inp))
+    restr = [(0, 3, [0, 1])]
+    gpu.set_selection_params(0, 1000000, restr)
+    parents = run.dets[:300]
+    c = np.abs(run.ci[0][:300])
+    existing = np.array(sorted(map(tuple, parents.tolist()), key=lambda t: (np.int64(np.uint64(t[1])),
+                                                                             np.int64(np.uint64(t[0])))),
+                        dtype=np.uint64)
+    ref = o.select(parents, c, 1e-5, existing, restrictions=restr)
+    gpu.set_dets(parents)
+    gpu.select(c, 1e-5)
+    assert np.array_equal(gpu.dets()[300:], ref)
+
+
+@pytest.mark.parametrize("mode", ["fp64", "mixed", "direct"])
+def test_davidson_against_oracle(gpu, golden, mode):
+    inp = golden("h8_631g", "dice.dat")
+    dets = np.load(os.path.join(GOLDEN, "h8_631g_dets.npz"))["dets"]
+    o = orc.Oracle(_fcidump(inp))
+    o.ham(dets)
+    diag = np.array([o.energy(x) for x in dets])
+    x0 = np.zeros((1, len(dets)))
+    x0[0, np.argmin(diag)] = 1.0
+    e_ref, v_ref, it_ref = o.davidson(x0, diag, 5, 1e-8)
+    gpu.read_fcidump(_fcidump(inp))
+    gpu.set_dets(dets)
+    gpu.ham_build("mixed" if mode == "mixed" else ("direct" if mode == "direct" else "fp64"))
+    e, v, it = gpu.davidson(x0, mode=mode, tol=1e-8)
+    assert abs(e[0] - e_ref[0]) < 1e-9
+    if mode == "fp64":
+        assert it == it_ref
+    assert abs(abs(v[0] @ v_ref[0]) - 1.0) < 1e-10
+
+
+def test_h8_end_to_end_fp64_matches_reference(gpu, golden):
+    inp = golden("h8_631g", "dice.dat")
+    E = gpu.run_input(inp, mode="fp64")
+    log = gpu.run_log()
+    table = G["h8_631g"]["table"]
+    assert list(log["ndets"]) == [r["ndets"] for r in table]
+    assert list(log["davidson"]) == [r["davidson"] for r in table]
+    for got, r in zip(log["energy"], table):
+        assert abs(got - r["energy"]) < 1e-9
+    assert abs(E[0] - G["h8_631g"]["E_var"]) < 1e-9
+    ref = np.load(os.path.join(GOLDEN, "h8_631g_dets.npz"))["dets"]
+    assert set(map(tuple, gpu.dets().tolist())) == set(map(tuple, ref.tolist()))
+
+
+def test_h8_end_to_end_mixed_within_1uha(gpu, golden):
+    inp = golden("h8_631g", "dice.dat")
+    E = gpu.run_input(inp, mode="mixed")
+    assert abs(E[0] - G["h8_631g"]["E_var"]) < 1e-6
+
+
+def test_n2_ras_end_to_end(gpu, golden):
+    inp = golden("n2_RAS", "input.dat")
+    E = gpu.run_input(inp, mode="fp64")
+    assert abs(E[0] - G["n2_RAS"]["E_var"]) < 1e-9
+    E = gpu.run_input(inp, mode="mixed")
+    assert abs(E[0] - G["n2_RAS"]["E_var"]) < 1e-6
+
+
+def test_restart_fixture_end_to_end(gpu, golden):
+    inp = golden("restart", "input3.dat")
+    E = gpu.run_input(inp, mode="fp64")
+    assert abs(E[0] - G["restart"]["E_var"]) < 1e-8
+    assert gpu.ndets() == 524307
+    E = gpu.run_input(inp, mode="mixed")
+    assert abs(E[0] - G["restart"]["E_var"]) < 1e-6
+
+
+def test_hubbard_ring_against_oracle(gpu, tmp_path):
+    inp = synthetic.make_workload("hubbard12", str(tmp_path / "hub"), schedule=[(0, 1e-3), (2, 3e-4)], maxiter=4)
+    run = orc.run_input(inp)
+    E = gpu.run_input(inp, mode="fp64")
+    log = gpu.run_log()
+    assert list(log["ndets"]) == list(run.ndets_log)
+    assert abs(E[0] - run.E[0]) < 1e-9
+    assert set(map(tuple, gpu.dets().tolist())) == set(map(tuple, run.dets.tolist()))
+
+
+def test_multiroot_block_davidson(gpu, golden):
+    inp = golden("h8_631g", "dice.dat")
+    dets = np.load(os.path.join(GOLDEN, "h8_631g_dets.npz"))["dets"]
+    o = orc.Oracle(_fcidump(inp))
+    o.ham(dets)
+    diag = np.array([o.energy(x) for x in dets])
+    order = np.argsort(diag)
+    x0 = np.zeros((4, len(dets)))
+    for r in range(4):
+        x0[r, order[r]] = 1.0
+    e_ref, _, _ = o.davidson(x0, diag, 8, 1e-7)
+    gpu.read_fcidump(_fcidump(inp))
+    gpu.set_dets(dets)
+    gpu.ham_build("mixed")
+    for block in (False, True):
+        for mode in ("fp64", "mixed"):
+            e, v, it = gpu.davidson(x0, mode=mode, block=block, max_copies=12, tol=1e-7)
+            assert np.allclose(e, e_ref, atol=1e-9), (block, mode, e, e_ref)
+
+
+def test_errors_are_status_codes(gpu, tmp_path):
+    with pytest.raises(eng.ShciError) as ei:
+        gpu.read_fcidump(str(tmp_path / "missing"))
+    assert ei.value.code == 2
+    bad = tmp_path / "bad"
+    bad.write_text(" &FCI NORB=2,NELEC=2,\n &END\n")
+    with pytest.raises(eng.ShciError):
+        gpu.read_fcidump(str(bad))
+    e2 = eng.Engine(0)
+    with pytest.raises(eng.ShciError) as ei:
+        e2.ham_build("fp64")
+    assert ei.value.code == 7
+    e2.close()
