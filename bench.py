@@ -1,0 +1,321 @@
+"""Benchmark of the SHCI variational engine on one GB300 (or N replicas).
+
+Workload: the synthetic molecular Hamiltonian with 24 spatial orbitals,
+12 alpha + 12 beta electrons, 72 Cholesky vectors (seeded), eps1 schedule
+1e-3 -> 3e-4 -> 1e-4, one root. The whole variational stage is run in the
+mixed path (FP32 sigma + FP64 refinement) and in the plain FP64 path; the
+timed "step" is then one sigma (y = H x) over the final variational space
+with the Hamiltonian resident in HBM.
+
+value: sigma Mdets/s (N / t_sigma / 1e6), kernel-only, device-resident
+vectors. e2e: the same through the C-ABI call with host buffers
+(shci_sigma: host->device copy of x and device->host copy of y inside the
+timed region). Extra keys report the variational wall time and E_var of
+both paths.
+
+--impl reference: the CPU oracle (a restatement of Dice's serial C++; Dice
+itself needs Boost and MPI, absent here) timed on a bounded sample of the
+same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "mol24"
+CPU_SAMPLE_DETS = 100000
+
+
+def dist_info():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, gpu):
+        self.path = tempfile.mktemp(suffix=".csv")
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(gpu), "--query-gpu=" + q, "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_gbs():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        return json.load(open(p))["hbm_gbs"], "measured"
+    return 6800.0, "fallback"
+
+
+def make_inputs(d, case="full"):
+    """case "small": the same Hamiltonian stopped after two eps1 = 1e-3
+    iterations (about 8e4 determinants, a ~0.8 GB Hamiltonian: larger than L2,
+    small enough for a full ncu capture)."""
+    from dice_gb300 import synthetic
+    if case == "small":
+        return synthetic.make_workload(WORKLOAD, d, schedule=[(0, 1e-3)], maxiter=2)
+    return synthetic.make_workload(WORKLOAD, d)
+
+
+def cpu_sample(work_dir, max_dets=CPU_SAMPLE_DETS):
+    """Determinants for the CPU baseline: the first `max_dets` of the space the
+    oracle selects with the first two eps1 = 1e-3 iterations of the workload."""
+    from dice_gb300 import synthetic
+    from oracle import oracle as orc
+    d = os.path.join(work_dir, "cpu_sample")
+    w = dict(synthetic.WORKLOADS[WORKLOAD])
+    inp = synthetic.make_workload(WORKLOAD, d, schedule=[(0, 1e-3)], maxiter=2)
+    run = orc.run_input(inp)
+    dets = run.dets[:max_dets]
+    o = orc.Oracle(os.path.join(d, "FCIDUMP"))
+    t0 = time.perf_counter()
+    rowptr, col, val = o.ham(dets)
+    t_build = time.perf_counter() - t0
+    return o, dets, len(col), t_build, w
+
+
+def time_cpu_sigma(o, n, seconds=10.0, max_reps=50):
+    x = np.random.default_rng(1).standard_normal(n)
+    times = []
+    t_start = time.perf_counter()
+    while len(times) < max_reps and (time.perf_counter() - t_start) < seconds:
+        t0 = time.perf_counter()
+        o.sigma(x)
+        times.append(time.perf_counter() - t0)
+    return times
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    from oracle import oracle as orc
+    orc.build()
+    with tempfile.TemporaryDirectory() as d:
+        o, dets, nnz_lower, t_build, w = cpu_sample(d)
+        n = len(dets)
+        x = np.random.default_rng(1).standard_normal(n)
+        for _ in range(args.warmup):
+            o.sigma(x)
+        times = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            o.sigma(x)
+            times.append(time.perf_counter() - t0)
+    t = statistics.mean(times)
+    val = n / t / 1e6
+    sample = ("first %d determinants of the eps1=1e-3 space of the workload (oracle selection), "
+              "lower-triangle nnz %d; serial Hmult2-style symmetric scatter in FP64" % (n, nnz_lower))
+    line = {"metric": "sigma Mdets/s (SHCI variational, stored H)", "value": val, "unit": "Mdets/s",
+            "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "mol24: synthetic molecular FCIDUMP n=24, 12a+12b, rank-72 Cholesky ERIs, seed 20260001",
+                       "sample": sample},
+            "cpu_baseline": {"value": val, "unit": "Mdets/s", "cores": 1, "kind": "port", "sample": sample},
+            "e2e": {"value": val, "unit": "Mdets/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "Dice cannot be built here (needs Boost and MPI); the CPU oracle restating its serial path is timed"}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    rank, world, local = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    from dice_gb300 import engine as eng
+
+    work = tempfile.mkdtemp()
+    inp = make_inputs(work, args.case)
+    e = eng.Engine(local)
+
+    # whole variational stage, plain FP64 path then mixed path
+    E64 = e.run_input(inp, mode="fp64")
+    t64 = e.timings()
+    log64 = e.run_log()
+    E32 = e.run_input(inp, mode="mixed")
+    t32 = e.timings()
+    log32 = e.run_log()
+    N = e.ndets()
+    dets_mixed = e.dets()
+
+    stream = torch.cuda.ExternalStream(e.stream, device=torch.device("cuda", local))
+    k = 1
+    rng = np.random.default_rng(5)
+    x_host = rng.standard_normal(N)
+
+    def timed_sigma(mode, packed, nsteps, nwarm):
+        nnz = e.ham_build(mode)
+        y = torch.zeros(N, dtype=torch.float64, device="cuda")
+        for _ in range(nwarm):
+            e.sigma_packed_device(packed.data_ptr(), 1, k, y.data_ptr(), N, mode=mode)
+        torch.cuda.synchronize()
+        csr_bytes, _ = e.ham_bytes()
+        flush = None
+        if csr_bytes < 2 * 129 * 2 ** 20:
+            flush = torch.empty(256 * 2 ** 20 // 4, dtype=torch.float32, device="cuda")
+        ts = []
+        l0 = e.launch_count()
+        # NVTX range so that a profiler can select exactly these launches
+        torch.cuda.nvtx.range_push("bench_sigma_" + mode)
+        for _ in range(nsteps):
+            if flush is not None:
+                with torch.cuda.stream(stream):
+                    flush.fill_(1.0)
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            e.sigma_packed_device(packed.data_ptr(), 1, k, y.data_ptr(), N, mode=mode)
+            b.record(stream)
+            b.synchronize()
+            ts.append(a.elapsed_time(b) * 1e-3)
+        torch.cuda.nvtx.range_pop()
+        launches = e.launch_count() - l0
+        return nnz, ts, launches, flush is not None, y
+
+    x_dev = torch.tensor(x_host, device="cuda")
+    # plain FP64 sigma on the final space of the mixed run
+    nnz64, ts64, _, _, y64 = timed_sigma("fp64", x_dev, max(3, args.steps // 2), args.warmup)
+    # mixed FP32 sigma (the timed region of `value`)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    wall0 = time.perf_counter()
+    nnz, ts32, launches, flushed, y32 = timed_sigma("mixed", x_dev.float(), args.steps, args.warmup)
+    wall = time.perf_counter() - wall0
+    clk = clocks.stop()
+    torch.cuda.synchronize()
+    t_max = statistics.mean(ts32)
+    if world > 1:
+        tt = torch.tensor([t_max], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_max = tt.item()
+    value = world * k * N / t_max / 1e6
+    sig_err = float((y32 - y64).abs().max() / y64.abs().max())
+
+    # end to end through the C-ABI with host buffers
+    for _ in range(2):
+        e.sigma(x_host, "mixed")
+    te = []
+    for _ in range(max(3, args.steps // 2)):
+        t0 = time.perf_counter()
+        e.sigma(x_host, "mixed")
+        te.append(time.perf_counter() - t0)
+    e2e = world * k * N / statistics.mean(te) / 1e6
+
+    peak, peak_kind = measured_peak_gbs()
+    alg_bytes = nnz * 8 + 8 * (N + 1) + 8 * N + k * N * 4 + k * N * 8
+    achieved = alg_bytes / t_max / 1e9
+    alg64 = nnz64 * 12 + 8 * (N + 1) + 8 * N + k * N * 8 + k * N * 8
+    ach64 = alg64 / statistics.mean(ts64) / 1e9
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        from oracle import oracle as orc
+        orc.build()
+        o, dets, nnz_lower, t_build, _ = cpu_sample(work)
+        tc = time_cpu_sigma(o, len(dets))
+        cpu = {"value": len(dets) / statistics.mean(tc) / 1e6, "unit": "Mdets/s", "cores": 1, "kind": "port",
+               "sample": "first %d determinants of the eps1=1e-3 space of the workload; serial FP64 symmetric-"
+                         "scatter sigma of the oracle, %d reps" % (len(dets), len(tc))}
+
+    line = {
+        "metric": "sigma Mdets/s (SHCI variational, stored H)", "value": value, "unit": "Mdets/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 diagonal, FP64 refinement)",
+        "data": "synthetic",
+        "config": {"workload": "mol24: synthetic molecular FCIDUMP n=24, 12a+12b, rank-72 Cholesky ERIs, "
+                               "seed 20260001, eps1 1e-3 -> 3e-4 -> 1e-4, 1 root",
+                   "n_dets": N, "nnz_offdiag": nnz, "k_vectors": k,
+                   "l2": "L2 flushed between steps (256 MiB write)" if flushed else
+                         "Hamiltonian (%.1f GB) larger than L2; no flush" % (nnz * 8 / 1e9),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "e2e": {"value": e2e, "unit": "Mdets/s", "h2d_bytes_per_step": N * k * 8, "d2h_bytes_per_step": N * k * 8},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "peak_kind": peak_kind, "alg_bytes_per_launch": alg_bytes},
+        "plain_fp64_sigma": {"mdets_s": k * N / statistics.mean(ts64) / 1e6, "achieved_gbs": ach64,
+                             "frac": ach64 / peak, "nnz": nnz64},
+        "mixed_vs_fp64_sigma_speedup": statistics.mean(ts64) / t_max,
+        "sigma_rel_err_fp32_vs_fp64": sig_err,
+        "var": {"mixed": {"wall_s": t32["total"], "E_var": float(E32[0]), "stages_s": t32,
+                          "ndets": [int(v) for v in log32["ndets"]], "davidson_iters": [int(v) for v in log32["davidson"]]},
+                "fp64": {"wall_s": t64["total"], "E_var": float(E64[0]), "stages_s": t64,
+                         "ndets": [int(v) for v in log64["ndets"]], "davidson_iters": [int(v) for v in log64["davidson"]]},
+                "dE_mixed_minus_fp64": float(E32[0] - E64[0]),
+                "wall_speedup_mixed_vs_fp64": t64["total"] / t32["total"]},
+        "clocks": clk, "timed_wall_s": wall,
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    e.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--case", default="full", choices=["full", "small"],
+                    help="small: the profiling case (two eps1 = 1e-3 iterations)")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

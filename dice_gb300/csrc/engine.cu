@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <numeric>
@@ -31,6 +32,18 @@
 namespace shci {
 
 std::atomic<int64_t> g_launch_count{0};
+
+// Residual norm below which the FP32 stage of the mixed solver may stop on
+// stagnation and hand over to the FP64 stage.
+constexpr double kStallWindow = 2e-5;
+// |<x|F|x>| above which a vector counts as having a definite flip parity.
+constexpr double kParityDefinite = 0.999;
+
+// SHCI_TRACE=1 prints one line per Davidson iteration to stderr.
+static const int trace_level = [] {
+  const char* v = std::getenv("SHCI_TRACE");
+  return v ? std::atoi(v) : 0;
+}();
 
 static inline unsigned grid_for(size_t n, int threads, size_t max_blocks = 152 * 32) {
   size_t b = (n + threads - 1) / threads;
@@ -144,8 +157,13 @@ struct Context {
   DevBuf<Det2> cand;
 
   // Davidson workspace
-  DevBuf<double> V, W, Vt, Wt, X, Y, R, D, xb64, yb64, gpart, dG, dQ, dlam, dsmall;
+  DevBuf<double> V, W, Vt, Wt, X, Y, R, D, xb64, yb64, gpart, dG, dQ, dlam, dsmall, ftmp;
   DevBuf<float> xb32;
+
+  // alpha <-> beta flip map of the current space (-1 unknown, 0 not closed, 1 closed)
+  DevBuf<int32_t> flipidx;
+  DevBuf<int8_t> flipsgn;
+  int flip_state = -1;
 
   // run state
   DevBuf<double> ci, cmax;
@@ -207,6 +225,30 @@ struct Context {
   void invalidate_space() {
     helpers_ok = false;
     ham_ok = false;
+    flip_state = -1;
+  }
+
+  // True when the space is closed under the alpha <-> beta flip (equal alpha
+  // and beta electron counts and every flipped determinant present).
+  bool ensure_flip() {
+    if (flip_state >= 0) return flip_state == 1;
+    flip_state = 0;
+    if (ndet == 0) return false;
+    Det2 d0;
+    SHCI_CUDA(cudaMemcpyAsync(&d0, dets.p, sizeof(Det2), cudaMemcpyDeviceToHost, stream));
+    SHCI_CUDA(cudaStreamSynchronize(stream));
+    if (__builtin_popcountll(det_alpha(d0)) != __builtin_popcountll(det_beta(d0))) return false;
+    hash.build(dets.p, ndet, stream);
+    flipidx.resize(ndet);
+    flipsgn.resize(ndet);
+    counter.resize(1);
+    if (build_flip_map(dets.p, ndet, hash, flipidx.p, flipsgn.p, counter.p, stream)) flip_state = 1;
+    return flip_state == 1;
+  }
+  // Project column c (length ndet) onto the flip sector of sign p.
+  void project_parity(double* c, double p) {
+    ftmp.reserve(ndet);
+    flip_project(c, ndet, flipidx.p, flipsgn.p, p, ftmp.p, stream);
   }
 
   void set_dets(const uint64_t* h, int64_t n) {
@@ -381,9 +423,22 @@ struct Context {
   }
 
   // One Davidson solve in a fixed sigma mode. x: device N x nroots (ld N).
+  // stall_exit: stop early (returning the current Ritz vectors) once the
+  // residual stops decreasing -- the FP32 stage of the mixed path, whose
+  // residual floor is set by FP32 rounding in sigma, hands over to the FP64
+  // stage there.
+  //
+  // resume_m > 0: continue on the basis V[:, :resume_m] left by a previous
+  // stage (W is recomputed in this stage's sigma mode); x is then ignored on
+  // entry. On return basis_m holds the size of the basis left in V.
   void davidson_core(int mode, bool block, int nroots, double* x, int maxCopies, double tol, bool direct_rules,
-                     std::vector<double>& E, int& numIter) {
+                     std::vector<double>& E, int& numIter, bool stall_exit = false, int resume_m = 0,
+                     int* basis_m = nullptr) {
     const size_t N = ndet;
+    // FP32 stage: hold the iterates in the alpha <-> beta flip sector that exact
+    // arithmetic would keep them in (see the note on compensated accumulation
+    // in kernels_sigma.cu); FP64 sigma keeps it to rounding by itself.
+    const bool sym = stall_exit && ensure_flip();
     if (nroots < 1) throw Error(kErrInvalid, "nroots must be >= 1");
     if ((size_t)nroots > N) throw Error(kErrInvalid, "more roots than determinants");
     int mmax = std::max(maxCopies, nroots + 1);
@@ -398,29 +453,46 @@ struct Context {
     Y.reserve(N * nroots);
     R.reserve(N * nroots);
     D.reserve(N * nroots);
-    // initial block (SHCI/Davidson.cpp:156-180)
-    SHCI_CUDA(cudaMemcpyAsync(V.p, x, N * nroots * sizeof(double), cudaMemcpyDeviceToDevice, stream));
-    for (int i = 0; i < nroots; ++i) {
-      double* bi = V.p + (size_t)i * N;
-      if (norm_host(bi) < 1.e-10) {
-        fill_random(bi, 1000 + i);
+    int m = nroots;
+    if (resume_m > 0) {
+      m = std::min(resume_m, mmax);
+      apply_sigma(mode, V.p, N, 0, m, W.p, N, 0);
+    } else {
+      // initial block (SHCI/Davidson.cpp:156-180)
+      SHCI_CUDA(cudaMemcpyAsync(V.p, x, N * nroots * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+      for (int i = 0; i < nroots; ++i) {
+        double* bi = V.p + (size_t)i * N;
+        if (norm_host(bi) < 1.e-10) {
+          fill_random(bi, 1000 + i);
+          scale_col(bi, 1.0 / norm_host(bi));
+        }
+      }
+      for (int i = 0; i < nroots; ++i) {
+        double* bi = V.p + (size_t)i * N;
+        for (int j = 0; j < i; ++j) project_out(V.p + (size_t)j * N, bi);
+        if (norm_host(bi) < 1e-8) fill_random(bi, 2000 + i);
+        for (int j = 0; j < i; ++j) project_out(V.p + (size_t)j * N, bi);
         scale_col(bi, 1.0 / norm_host(bi));
       }
+      if (sym) {
+        for (int i = 0; i < nroots; ++i) {
+          double* bi = V.p + (size_t)i * N;
+          const double p = flip_parity(bi, N, flipidx.p, flipsgn.p, gpart, stream);
+          if (std::fabs(p) > kParityDefinite) {
+            project_parity(bi, p > 0 ? 1.0 : -1.0);
+            scale_col(bi, 1.0 / norm_host(bi));
+          }
+        }
+      }
+      apply_sigma(mode, V.p, N, 0, nroots, W.p, N, 0);
     }
-    for (int i = 0; i < nroots; ++i) {
-      double* bi = V.p + (size_t)i * N;
-      for (int j = 0; j < i; ++j) project_out(V.p + (size_t)j * N, bi);
-      if (norm_host(bi) < 1e-8) fill_random(bi, 2000 + i);
-      for (int j = 0; j < i; ++j) project_out(V.p + (size_t)j * N, bi);
-      scale_col(bi, 1.0 / norm_host(bi));
-    }
-    apply_sigma(mode, V.p, N, 0, nroots, W.p, N, 0);
-    int m = nroots;
     numIter = 0;
     int cR = 0;
     const int soft_cap = (direct_rules ? 400 : 800) * nroots;
     const int hard_cap = (direct_rules ? 400 : 2000) * nroots;
     std::vector<double> lam, Q;
+    double best_resid = 1e300;
+    int stall = 0, stall_root = 0;
     while (true) {
       // Rayleigh-Ritz (SHCI/Davidson.cpp:250-269)
       std::vector<double> G = gram_host(V.p, N, m, W.p, N, m);
@@ -438,7 +510,11 @@ struct Context {
       std::vector<double> rn(nroots);
       for (int c = 0; c < nroots; ++c) rn[c] = std::sqrt(std::max(0.0, RR[(size_t)c * nroots + c]));
       numIter++;
+      if (trace_level > 0)
+        std::fprintf(stderr, "[davidson mode=%d it=%d m=%d] lam0=%.12f res0=%.3e G00=%.12f\n", mode, numIter, m,
+                     lam[0], rn[0], G[0]);
       auto finish = [&]() {
+        if (basis_m) *basis_m = m;
         E.assign(lam.begin(), lam.begin() + nroots);
         SHCI_CUDA(cudaMemcpyAsync(x, X.p, N * nroots * sizeof(double), cudaMemcpyDeviceToDevice, stream));
         SHCI_CUDA(cudaStreamSynchronize(stream));
@@ -446,6 +522,29 @@ struct Context {
       if ((size_t)m == N) {
         finish();
         return;
+      }
+      if (stall_exit) {
+        // progress measure: the worked-on root (root-by-root) or the worst root (block)
+        double worst = 0.0;
+        if (block) {
+          for (int c = 0; c < nroots; ++c) worst = std::max(worst, rn[c]);
+        } else {
+          worst = rn[cR];
+          if (cR != stall_root) {
+            stall_root = cR;
+            best_resid = 1e300;
+            stall = 0;
+          }
+        }
+        // Only near the FP32 rounding floor (~1e-6): a plateau higher up is
+        // ordinary Davidson behaviour and the FP32 stage keeps going.
+        if (worst < 0.8 * best_resid) {
+          best_resid = worst;
+          stall = 0;
+        } else if (worst < kStallWindow && ++stall >= 8) {
+          finish();
+          return;
+        }
       }
       std::vector<int> act;
       std::vector<double> act_lam;
@@ -496,6 +595,13 @@ struct Context {
                                   cudaMemcpyDeviceToDevice, stream));
       to_dev(dlam, act_lam);
       precondition(diag.p, dlam.p, nact, N, D.p, N, stream);
+      if (sym) {
+        // keep each correction in the flip sector of the root it corrects
+        for (int a = 0; a < nact; ++a) {
+          const double p = flip_parity(X.p + (size_t)act[a] * N, N, flipidx.p, flipsgn.p, gpart, stream);
+          if (std::fabs(p) > kParityDefinite) project_parity(D.p + (size_t)a * N, p > 0 ? 1.0 : -1.0);
+        }
+      }
       // orthogonalise against the whole basis (two classical Gram-Schmidt passes)
       dG.reserve((size_t)m * nact);
       for (int pass = 0; pass < 2; ++pass) {
@@ -538,9 +644,11 @@ struct Context {
     if (!ham_ok) throw Error(kErrState, "Hamiltonian not built for the current space (call shci_ham_build)");
     ensure_diag();
     if (mode == SHCI_MODE_MIXED) {
-      int it1 = 0, it2 = 0;
-      davidson_core(SHCI_MODE_MIXED, block, nroots, x, maxCopies, tol, direct_rules, E, it1);
-      davidson_core(SHCI_MODE_FP64, block, nroots, x, maxCopies, tol, direct_rules, E, it2);
+      // FP32 stage, then the FP64 stage continues on the same basis with W
+      // recomputed in FP64 (head + tail values)
+      int it1 = 0, it2 = 0, m = 0;
+      davidson_core(SHCI_MODE_MIXED, block, nroots, x, maxCopies, tol, direct_rules, E, it1, true, 0, &m);
+      davidson_core(SHCI_MODE_FP64, block, nroots, x, maxCopies, tol, direct_rules, E, it2, false, m);
       iters = it1 + it2;
     } else {
       davidson_core(mode, block, nroots, x, maxCopies, tol, direct_rules, E, iters);
@@ -895,6 +1003,30 @@ int shci_sigma_device(shci_ctx* ctx, int mode, const double* x_dev, double* y_de
     if (ld < (int64_t)c.ndet) throw Error(SHCI_ERR_INVALID, "leading dimension smaller than N");
     c.ensure_diag();
     c.apply_sigma(mode, x_dev, (size_t)ld, 0, k, y_dev, (size_t)ld, 0);
+  });
+}
+
+int shci_sigma_packed_device(shci_ctx* ctx, int mode, const void* x_packed, int kp, int k, double* y_dev,
+                             int64_t ld) {
+  return guarded(ctx, [&](Context& c) {
+    if (!(kp == 1 || kp == 2 || kp == 4) || k < 1 || k > kp) throw Error(SHCI_ERR_INVALID, "need k <= kp in {1,2,4}");
+    if (!c.ham_ok || c.ham_mode == SHCI_MODE_DIRECT) throw Error(SHCI_ERR_STATE, "no stored Hamiltonian");
+    if (ld < (int64_t)c.ndet) throw Error(SHCI_ERR_INVALID, "leading dimension smaller than N");
+    c.ensure_diag();
+    if (mode == SHCI_MODE_MIXED)
+      shci::sigma_csr_mixed(c.H, c.diag.p, static_cast<const float*>(x_packed), kp, k, y_dev, (size_t)ld, c.stream);
+    else if (mode == SHCI_MODE_FP64)
+      shci::sigma_csr_f64(c.H, c.diag.p, static_cast<const double*>(x_packed), kp, k, y_dev, (size_t)ld,
+                          c.H.v64.p == nullptr, c.stream);
+    else
+      throw Error(SHCI_ERR_INVALID, "packed sigma supports the stored modes only");
+  });
+}
+
+int shci_ham_bytes(shci_ctx* ctx, int64_t* csr_bytes, int64_t* helper_bytes) {
+  return guarded(ctx, [&](Context& c) {
+    if (csr_bytes) *csr_bytes = (int64_t)c.H.bytes();
+    if (helper_bytes) *helper_bytes = (int64_t)c.helpers.bytes();
   });
 }
 

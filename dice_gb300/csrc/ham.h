@@ -90,6 +90,20 @@ int64_t select_candidates(const Det2* dets, const double* cmax, size_t n, double
                           const HeatBathView& hb, double maxEntry, const SelectParams& sp, const DetHash& present,
                           Det2* out, int64_t cap, int64_t* d_counter, cudaStream_t s);
 
+// ---- alpha <-> beta flip of the space (kernels_select.cu) -------------------
+// flip[i] = index of the determinant with alpha and beta strings exchanged,
+// sign[i] = (-1)^(number of doubly occupied orbitals of det i), the phase of
+// the relabelling in the interleaved spin-orbital order. Returns false (and
+// leaves the map unusable) when some flipped determinant is not in the space.
+bool build_flip_map(const Det2* dets, size_t n, const DetHash& hash, int32_t* flip, int8_t* sign,
+                    int64_t* d_missing, cudaStream_t s);
+// parity p = <x|F|x> / <x|x> of one column (host result)
+double flip_parity(const double* x, size_t n, const int32_t* flip, const int8_t* sign, DevBuf<double>& part,
+                   cudaStream_t s);
+// x <- (x + p F x) / 2 in place (p = +1 or -1), using tmp (n doubles)
+void flip_project(double* x, size_t n, const int32_t* flip, const int8_t* sign, double p, double* tmp,
+                  cudaStream_t s);
+
 // ---- sigma and Davidson vector kernels (kernels_sigma.cu) -------------------
 // Y[:, c] (column-major, leading dimension ldy) = diag .* X[:, c] + Hoff X[:, c]
 // for c < k, where X is row-interleaved [N][kp] in the path's precision.

@@ -207,7 +207,10 @@ static const char* kIgnored[] = {
     "dosocqdpt", "dogtensor", "socmultiplier", "doresponse", "onlyperturbative", "algorithm", "dolcc",
     "pointGroup", "spin", "irrep", "searchForLowestEnergyDet", "cdfciTol", "cdfciIter", "cdfciOn",
     "reportInterval", "z_threshold", "cdfciSample", "eps", "maxseniority", "maxexcitation", "SenioAndExc",
-    "diskdavidson", "Treversal"};
+    "diskdavidson", "Treversal",
+    // no checkpoint files are kept: a restart runs the whole schedule, which
+    // reaches the same variational space as the reference's resumed run
+    "restart", "fullrestart"};
 
 void read_input(const std::string& path, Schedule& s) {
   std::ifstream ifs(path.c_str());

@@ -208,6 +208,121 @@ __global__ void __launch_bounds__(kSelThreads) k_select(SelArgs a) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// alpha <-> beta flip map. The relabelling a+_{2k} <-> a+_{2k+1} maps the
+// ordered creation string of a determinant onto that of its flipped partner
+// up to one transposition per doubly occupied orbital, hence the sign.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int64_t hash_find(const uint32_t* __restrict__ slots, uint64_t mask,
+                                             const Det2* __restrict__ dets, const Det2& x) {
+  uint64_t h = det_hash(x) & mask;
+  for (uint64_t probe = 0; probe <= mask; ++probe) {
+    uint32_t s = slots[h];
+    if (s == 0xffffffffu) return -1;
+    if (det_eq(x, dets[s])) return (int64_t)s;
+    h = (h + 1) & mask;
+  }
+  return -1;
+}
+
+__global__ void k_flip_map(const Det2* __restrict__ dets, size_t n, const uint32_t* __restrict__ slots, uint64_t mask,
+                           int32_t* __restrict__ flip, int8_t* __restrict__ sign,
+                           unsigned long long* __restrict__ missing) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const Det2 d = dets[i];
+    const uint64_t a = det_alpha(d), b = det_beta(d);
+    const Det2 f = det_from_strings(b, a);
+    const int64_t j = hash_find(slots, mask, dets, f);
+    if (j < 0) {
+      atomicAdd(missing, 1ull);
+      flip[i] = (int32_t)i;
+    } else {
+      flip[i] = (int32_t)j;
+    }
+    sign[i] = (__popcll(a & b) & 1) ? -1 : 1;
+  }
+}
+
+bool build_flip_map(const Det2* dets, size_t n, const DetHash& hash, int32_t* flip, int8_t* sign,
+                    int64_t* d_missing, cudaStream_t s) {
+  SHCI_CUDA(cudaMemsetAsync(d_missing, 0, sizeof(int64_t), s));
+  size_t blocks = (n + 255) / 256;
+  if (blocks > 152 * 32) blocks = 152 * 32;
+  if (blocks < 1) blocks = 1;
+  k_flip_map<<<(unsigned)blocks, 256, 0, s>>>(dets, n, hash.slots.p, hash.mask, flip, sign,
+                                              reinterpret_cast<unsigned long long*>(d_missing));
+  SHCI_LAUNCH_CHECK();
+  int64_t missing = 0;
+  SHCI_CUDA(cudaMemcpyAsync(&missing, d_missing, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  return missing == 0;
+}
+
+constexpr unsigned kParBlocks = 152 * 2;
+
+__global__ void k_flip_parity(const double* __restrict__ x, size_t n, const int32_t* __restrict__ flip,
+                              const int8_t* __restrict__ sign, double* __restrict__ part) {
+  __shared__ double sxy[8], sxx[8];
+  double xy = 0.0, xx = 0.0;
+  const size_t per = (n + gridDim.x - 1) / gridDim.x;
+  const size_t r0 = (size_t)blockIdx.x * per, r1 = r0 + per < n ? r0 + per : n;
+  for (size_t i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+    const double v = x[i];
+    xy += v * (double)sign[i] * x[flip[i]];
+    xx += v * v;
+  }
+  for (int o = 16; o; o >>= 1) {
+    xy += __shfl_xor_sync(kFull, xy, o);
+    xx += __shfl_xor_sync(kFull, xx, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    sxy[threadIdx.x >> 5] = xy;
+    sxx[threadIdx.x >> 5] = xx;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      a += sxy[w];
+      b += sxx[w];
+    }
+    part[2 * blockIdx.x] = a;
+    part[2 * blockIdx.x + 1] = b;
+  }
+}
+
+double flip_parity(const double* x, size_t n, const int32_t* flip, const int8_t* sign, DevBuf<double>& part,
+                   cudaStream_t s) {
+  part.reserve(2 * kParBlocks);
+  k_flip_parity<<<kParBlocks, 256, 0, s>>>(x, n, flip, sign, part.p);
+  SHCI_LAUNCH_CHECK();
+  std::vector<double> h(2 * kParBlocks);
+  SHCI_CUDA(cudaMemcpyAsync(h.data(), part.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  double a = 0.0, b = 0.0;
+  for (unsigned k = 0; k < kParBlocks; ++k) {
+    a += h[2 * k];
+    b += h[2 * k + 1];
+  }
+  return b > 0.0 ? a / b : 0.0;
+}
+
+__global__ void k_flip_apply(const double* __restrict__ x, size_t n, const int32_t* __restrict__ flip,
+                             const int8_t* __restrict__ sign, double p, double* __restrict__ out) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = 0.5 * (x[i] + p * (double)sign[i] * x[flip[i]]);
+}
+
+void flip_project(double* x, size_t n, const int32_t* flip, const int8_t* sign, double p, double* tmp,
+                  cudaStream_t s) {
+  size_t blocks = (n + 255) / 256;
+  if (blocks > 152 * 32) blocks = 152 * 32;
+  if (blocks < 1) blocks = 1;
+  k_flip_apply<<<(unsigned)blocks, 256, 0, s>>>(x, n, flip, sign, p, tmp);
+  SHCI_LAUNCH_CHECK();
+  SHCI_CUDA(cudaMemcpyAsync(x, tmp, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+}
+
 int64_t select_candidates(const Det2* dets, const double* cmax, size_t n, double eps1, const IntsView& ints,
                           const HeatBathView& hb, double maxEntry, const SelectParams& sp, const DetHash& present,
                           Det2* out, int64_t cap, int64_t* d_counter, cudaStream_t s) {

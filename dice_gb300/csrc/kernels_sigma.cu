@@ -24,29 +24,60 @@ static inline unsigned grid_for(size_t n, int threads, size_t max_blocks = 152 *
   return (unsigned)b;
 }
 
+// Compensated FP32 accumulation: the running sum s carries an FP32 error term
+// c that collects the rounding error of every product (FMA residual) and of
+// every addition (TwoSum), so s + c equals the exact sum of the FP32 products
+// to about 2^-44 relative, whatever the summation order.
+//
+// Why it matters: the selected space is closed under the alpha <-> beta flip
+// and H commutes with it, so a Davidson run seeded with a flip-even vector
+// stays flip-even in exact arithmetic -- and in FP64, which is how the
+// reference converges to the state of its reference determinant. A row and
+// its flipped partner hold the same products in a different order; plain FP32
+// accumulation rounds them differently, breaking the symmetry at 1e-7, and a
+// lower flip-odd state (present in some spaces) can then take over the solve.
+struct Acc {
+  float s, c;
+};
+__device__ __forceinline__ void acc_add(Acc& a, float h, float x) {
+  const float p = __fmul_rn(h, x);
+  const float pe = __fmaf_rn(h, x, -p);  // exact product residual
+  const float t = __fadd_rn(a.s, p);
+  const float bp = __fsub_rn(t, a.s);
+  const float e = __fadd_rn(__fsub_rn(a.s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+  a.s = t;
+  a.c = __fadd_rn(a.c, __fadd_rn(e, pe));
+}
+__device__ __forceinline__ void acc_merge(Acc& a, const Acc& b) {
+  const float t = __fadd_rn(a.s, b.s);
+  const float bp = __fsub_rn(t, a.s);
+  const float e = __fadd_rn(__fsub_rn(a.s, __fsub_rn(t, bp)), __fsub_rn(b.s, bp));
+  a.s = t;
+  a.c = __fadd_rn(a.c, __fadd_rn(e, b.c));
+}
+
 template <int KP>
 struct VecF;
 template <>
 struct VecF<1> {
-  using T = float;
-  __device__ static void fma(float* acc, float h, const float* x, int j) { acc[0] += h * __ldg(x + j); }
+  __device__ static void fma(Acc* acc, float h, const float* x, int j) { acc_add(acc[0], h, __ldg(x + j)); }
 };
 template <>
 struct VecF<2> {
-  __device__ static void fma(float* acc, float h, const float* x, int j) {
+  __device__ static void fma(Acc* acc, float h, const float* x, int j) {
     float2 v = __ldg(reinterpret_cast<const float2*>(x) + j);
-    acc[0] += h * v.x;
-    acc[1] += h * v.y;
+    acc_add(acc[0], h, v.x);
+    acc_add(acc[1], h, v.y);
   }
 };
 template <>
 struct VecF<4> {
-  __device__ static void fma(float* acc, float h, const float* x, int j) {
+  __device__ static void fma(Acc* acc, float h, const float* x, int j) {
     float4 v = __ldg(reinterpret_cast<const float4*>(x) + j);
-    acc[0] += h * v.x;
-    acc[1] += h * v.y;
-    acc[2] += h * v.z;
-    acc[3] += h * v.w;
+    acc_add(acc[0], h, v.x);
+    acc_add(acc[1], h, v.y);
+    acc_add(acc[2], h, v.z);
+    acc_add(acc[3], h, v.w);
   }
 };
 
@@ -63,25 +94,46 @@ __global__ void __launch_bounds__(256) k_sigma_mixed(const int64_t* __restrict__
   for (size_t wr = (((size_t)blockIdx.x * blockDim.x + threadIdx.x) / 32) * rows_per_warp; wr < N; wr += stride) {
     const size_t r = wr + (threadIdx.x & 31) / VW;
     const bool live = r < N;
-    float acc[KP];
+    Acc acc[KP];
 #pragma unroll
-    for (int c = 0; c < KP; ++c) acc[c] = 0.f;
+    for (int c = 0; c < KP; ++c) acc[c] = Acc{0.f, 0.f};
+    const int64_t p0 = live ? __ldg(rowptr + r) : 0;
     const int64_t p1 = live ? __ldg(rowptr + r + 1) : 0;
-    for (int64_t p = (live ? __ldg(rowptr + r) : 0) + sub; p < p1; p += VW) {
-      const int j = __ldcs(col + p);
-      const float h = __ldcs(val + p);
-      VecF<KP>::fma(acc, h, x, j);
+    // head up to a 16-byte boundary, then 4 nonzeros per lane per step with
+    // 16-byte streaming loads (four independent gathers in flight), then tail
+    const int64_t pa = min(p1, (p0 + 3) & ~(int64_t)3);
+    for (int64_t p = p0 + sub; p < pa; p += VW) VecF<KP>::fma(acc, __ldcs(val + p), x, __ldcs(col + p));
+    const int64_t nv = (p1 - pa) >> 2;
+    const int4* c4 = reinterpret_cast<const int4*>(col + pa);
+    const float4* v4 = reinterpret_cast<const float4*>(val + pa);
+    for (int64_t q = sub; q < nv; q += VW) {
+      const int4 j = __ldcs(c4 + q);
+      const float4 h = __ldcs(v4 + q);
+      VecF<KP>::fma(acc, h.x, x, j.x);
+      VecF<KP>::fma(acc, h.y, x, j.y);
+      VecF<KP>::fma(acc, h.z, x, j.z);
+      VecF<KP>::fma(acc, h.w, x, j.w);
     }
+    for (int64_t p = pa + (nv << 2) + sub; p < p1; p += VW) VecF<KP>::fma(acc, __ldcs(val + p), x, __ldcs(col + p));
 #pragma unroll
     for (int c = 0; c < KP; ++c) {
 #pragma unroll
-      for (int o = VW / 2; o; o >>= 1) acc[c] += __shfl_xor_sync(kFull, acc[c], o, VW);
+      for (int o = VW / 2; o; o >>= 1) {
+        Acc other{__shfl_xor_sync(kFull, acc[c].s, o, VW), __shfl_xor_sync(kFull, acc[c].c, o, VW)};
+        // merge in lane order so that both partners of a pair compute the same value
+        if ((threadIdx.x & o) == 0) {
+          acc_merge(acc[c], other);
+        } else {
+          acc_merge(other, acc[c]);
+          acc[c] = other;
+        }
+      }
     }
     if (sub == 0 && live) {
       const double dg = diag[r];
 #pragma unroll
       for (int c = 0; c < KP; ++c)
-        if (c < k) y[(size_t)c * ldy + r] = dg * (double)x[r * KP + c] + (double)acc[c];
+        if (c < k) y[(size_t)c * ldy + r] = dg * (double)x[r * KP + c] + ((double)acc[c].s + (double)acc[c].c);
     }
   }
 }
@@ -101,9 +153,9 @@ __global__ void __launch_bounds__(256) k_sigma_f64(const int64_t* __restrict__ r
     double acc[KP];
 #pragma unroll
     for (int c = 0; c < KP; ++c) acc[c] = 0.0;
+    const int64_t p0 = live ? __ldg(rowptr + r) : 0;
     const int64_t p1 = live ? __ldg(rowptr + r + 1) : 0;
-    for (int64_t p = (live ? __ldg(rowptr + r) : 0) + sub; p < p1; p += VW) {
-      const int j = __ldcs(col + p);
+    auto elem = [&](int64_t p, int j) {
       double h;
       if (HILO)
         h = (double)__ldcs(vhi + p) + (double)__ldcs(vlo + p);
@@ -111,7 +163,20 @@ __global__ void __launch_bounds__(256) k_sigma_f64(const int64_t* __restrict__ r
         h = __ldcs(v64 + p);
 #pragma unroll
       for (int c = 0; c < KP; ++c) acc[c] += h * __ldg(x + (size_t)j * KP + c);
+    };
+    const int64_t pa = min(p1, (p0 + 3) & ~(int64_t)3);
+    for (int64_t p = p0 + sub; p < pa; p += VW) elem(p, __ldcs(col + p));
+    const int64_t nv = (p1 - pa) >> 2;
+    const int4* c4 = reinterpret_cast<const int4*>(col + pa);
+    for (int64_t q = sub; q < nv; q += VW) {
+      const int4 j = __ldcs(c4 + q);
+      const int64_t p = pa + 4 * q;
+      elem(p, j.x);
+      elem(p + 1, j.y);
+      elem(p + 2, j.z);
+      elem(p + 3, j.w);
     }
+    for (int64_t p = pa + (nv << 2) + sub; p < p1; p += VW) elem(p, __ldcs(col + p));
 #pragma unroll
     for (int c = 0; c < KP; ++c) {
 #pragma unroll

@@ -39,6 +39,8 @@ SIGNATURES = [
     ("shci_diag", _i32, [_vp, _vp]),
     ("shci_sigma", _i32, [_vp, _i32, _vp, _vp, _i32]),
     ("shci_sigma_device", _i32, [_vp, _i32, _vp, _vp, _i32, _i64]),
+    ("shci_sigma_packed_device", _i32, [_vp, _i32, _vp, _i32, _i32, _vp, _i64]),
+    ("shci_ham_bytes", _i32, [_vp, _P(_i64), _P(_i64)]),
     ("shci_davidson", _i32, [_vp, _i32, _i32, _i32, _vp, _i32, _dbl, _vp, _P(_i32)]),
     ("shci_run_input", _i32, [_vp, ctypes.c_char_p, ctypes.c_char_p, _i32, _i32, _vp, _i32, _P(_i32)]),
     ("shci_run_log", _i32, [_vp, _i32, _P(_i32), _vp, _vp, _vp, _vp]),
@@ -191,6 +193,20 @@ class Engine:
         y = np.zeros_like(xx)
         self._check(load_library().shci_sigma(self.h, MODES.get(mode, mode), _p(xx), _p(y), xx.shape[0]))
         return y[0] if one else y
+
+    def sigma_device(self, x_ptr, y_ptr, k, ld, mode="fp64"):
+        """Device pointers (ints): column-major x, y with leading dimension ld."""
+        self._check(load_library().shci_sigma_device(self.h, MODES.get(mode, mode), ctypes.c_void_p(x_ptr),
+                                                     ctypes.c_void_p(y_ptr), k, ld))
+
+    def sigma_packed_device(self, xp_ptr, kp, k, y_ptr, ld, mode="mixed"):
+        self._check(load_library().shci_sigma_packed_device(self.h, MODES.get(mode, mode), ctypes.c_void_p(xp_ptr),
+                                                            kp, k, ctypes.c_void_p(y_ptr), ld))
+
+    def ham_bytes(self):
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        self._check(load_library().shci_ham_bytes(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
 
     def davidson(self, x0, mode="fp64", block=False, max_copies=None, tol=5e-5):
         x = np.ascontiguousarray(x0, dtype=np.float64).reshape(-1, self.ndets()).copy()

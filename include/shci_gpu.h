@@ -113,6 +113,17 @@ int shci_sigma(shci_ctx* ctx, int mode, const double* x, double* y, int k);
  * dimension ld), enqueued on the context stream without host synchronisation. */
 int shci_sigma_device(shci_ctx* ctx, int mode, const double* x_dev, double* y_dev, int k, int64_t ld);
 
+/* Sigma on vectors already in the engine's gather layout: x_packed is
+ * row-interleaved N x kp (kp = 1, 2 or 4; k <= kp columns used), FP32 for
+ * SHCI_MODE_MIXED and FP64 for SHCI_MODE_FP64; y_dev column-major (ld).
+ * Exactly one kernel launch on the context stream, no synchronisation.
+ * Replaces the inner product loop of Hmult2::operator() (SHCI/Hmult.h:108-123). */
+int shci_sigma_packed_device(shci_ctx* ctx, int mode, const void* x_packed, int kp, int k, double* y_dev,
+                             int64_t ld);
+/* Bytes of the stored Hamiltonian (row pointers, columns, values) and of the
+ * string tables, for memory and roofline accounting. */
+int shci_ham_bytes(shci_ctx* ctx, int64_t* csr_bytes, int64_t* helper_bytes);
+
 /* Davidson. Replaces davidson / davidsonDirect (SHCI/Davidson.cpp:111-348,
  * :353-590) with the diagonal preconditioner (:85-106).
  * x0: host nroots x N column-major, initial guesses in, eigenvectors out.
