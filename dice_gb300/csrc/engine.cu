@@ -1023,6 +1023,25 @@ int shci_sigma_packed_device(shci_ctx* ctx, int mode, const void* x_packed, int 
   });
 }
 
+int shci_sigma_device_noalloc(shci_ctx* ctx, int mode, const double* x_dev, double* y_dev, int k, int64_t ld) {
+  return guarded(ctx, [&](Context& c) {
+    if (k < 1 || k > 4) throw Error(SHCI_ERR_INVALID, "k must be in 1..4");
+    if (mode != SHCI_MODE_MIXED && mode != SHCI_MODE_FP64)
+      throw Error(SHCI_ERR_INVALID, "the allocation-free sigma supports the stored modes (MIXED, FP64) only");
+    const size_t need = c.ndet * (size_t)(k == 3 ? 4 : k) * (mode == SHCI_MODE_MIXED ? sizeof(float) : sizeof(double));
+    if (need > shci::kNoAllocPackBytes)
+      throw Error(SHCI_ERR_INVALID, "allocation-free sigma: N x k needs " + std::to_string(need) +
+                                        " bytes of scratch, more than its fixed " +
+                                        std::to_string(shci::kNoAllocPackBytes) + " bytes");
+    if (!c.ham_ok || c.ham_mode == SHCI_MODE_DIRECT) throw Error(SHCI_ERR_STATE, "no stored Hamiltonian");
+    if (mode == SHCI_MODE_MIXED && c.ham_mode != SHCI_MODE_MIXED)
+      throw Error(SHCI_ERR_STATE, "mixed sigma needs a Hamiltonian built in mixed mode");
+    if (c.ndiag < c.ndet) throw Error(SHCI_ERR_STATE, "diagonal not computed (call shci_ham_build first)");
+    if (ld < (int64_t)c.ndet) throw Error(SHCI_ERR_INVALID, "leading dimension smaller than N");
+    shci::sigma_noalloc(c.H, c.diag.p, mode == SHCI_MODE_MIXED, x_dev, (size_t)ld, k, y_dev, (size_t)ld, c.stream);
+  });
+}
+
 int shci_ham_bytes(shci_ctx* ctx, int64_t* csr_bytes, int64_t* helper_bytes) {
   return guarded(ctx, [&](Context& c) {
     if (csr_bytes) *csr_bytes = (int64_t)c.H.bytes();

@@ -111,6 +111,13 @@ void sigma_csr_mixed(const Csr& H, const double* diag, const float* x32, int kp,
                      cudaStream_t s);
 void sigma_csr_f64(const Csr& H, const double* diag, const double* x64, int kp, int k, double* y, size_t ldy,
                    bool use_hilo, cudaStream_t s);
+// Sigma that allocates nothing: x (column-major, ldx) is packed into a fixed
+// device array of kNoAllocPackBytes (16 MiB: N x k up to 4,194,304 in the
+// mixed path, 2,097,152 in the FP64 path; k = 3 counts as 4) and the stored
+// Hamiltonian's sigma kernel runs on it. Larger sizes are rejected.
+constexpr size_t kNoAllocPackBytes = (size_t)16 << 20;
+void sigma_noalloc(const Csr& H, const double* diag, int mode_mixed, const double* x, size_t ldx, int k, double* y,
+                   size_t ldy, cudaStream_t s);
 // Pack columns [c0, c0+k) of column-major A (lda) into row-interleaved [N][kp]
 // (zero padded) in FP32 or FP64.
 void pack_f32(const double* A, size_t lda, int c0, int k, int kp, size_t N, float* out, cudaStream_t s);

@@ -13,6 +13,8 @@
 // The Davidson kernels (Gram products, Ritz combinations, residuals and the
 // diagonal preconditioner of SHCI/Davidson.cpp:85-106) reduce in a fixed
 // order, so results do not depend on scheduling.
+#include <mutex>
+
 #include "ham.h"
 
 namespace shci {
@@ -416,6 +418,61 @@ __global__ void k_scale_cols(double* __restrict__ A, size_t ld, const double* __
 void scale_cols(double* A, size_t ld, const double* scale, int k, size_t N, cudaStream_t s) {
   k_scale_cols<<<grid_for(N, 256), 256, 0, s>>>(A, ld, scale, k, N);
   SHCI_LAUNCH_CHECK();
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free sigma (shci_sigma_device_noalloc). The row-interleaved copy
+// of x that the sigma kernels gather from lives in this fixed device array
+// instead of a context buffer, so a call never allocates. Every GPU that loads
+// the library holds the array until the process exits. All calls share it and
+// each call overwrites the part it uses (including the zero padding), so
+// nothing has to be cleared between calls; calls that overlap on the GPU
+// (different streams or contexts at the same time) race on it.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) unsigned char g_sigma_pack_scratch[kNoAllocPackBytes];
+
+namespace {
+std::mutex g_scratch_mu;
+void* g_scratch_addr[64] = {nullptr};
+}  // namespace
+
+// Device address of the array on the current device, looked up once per
+// device (host code cannot use the symbol itself: on the host it names a
+// stand-in, not device memory).
+static void* noalloc_scratch() {
+  int dev = 0;
+  SHCI_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) throw Error(kErrInvalid, "device index beyond 63");
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  if (!g_scratch_addr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_sigma_pack_scratch);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      throw Error(kErrCuda, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+    }
+    g_scratch_addr[dev] = p;
+  }
+  return g_scratch_addr[dev];
+}
+
+void sigma_noalloc(const Csr& H, const double* diag, int mode_mixed, const double* x, size_t ldx, int k, double* y,
+                   size_t ldy, cudaStream_t s) {
+  const size_t N = H.N;
+  const int kp = k == 3 ? 4 : k;
+  const size_t need = N * (size_t)kp * (mode_mixed ? sizeof(float) : sizeof(double));
+  if (need > kNoAllocPackBytes)
+    throw Error(kErrInvalid, "allocation-free sigma: N x k = " + std::to_string(N) + " x " + std::to_string(kp) +
+                                 " needs " + std::to_string(need) + " bytes of scratch, the fixed maximum is " +
+                                 std::to_string(kNoAllocPackBytes));
+  void* scratch = noalloc_scratch();
+  if (mode_mixed) {
+    pack_f32(x, ldx, 0, k, kp, N, static_cast<float*>(scratch), s);
+    sigma_csr_mixed(H, diag, static_cast<const float*>(scratch), kp, k, y, ldy, s);
+  } else {
+    pack_f64(x, ldx, 0, k, kp, N, static_cast<double*>(scratch), s);
+    sigma_csr_f64(H, diag, static_cast<const double*>(scratch), kp, k, y, ldy, H.v64.p == nullptr, s);
+  }
 }
 
 }  // namespace shci

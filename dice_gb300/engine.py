@@ -40,6 +40,7 @@ SIGNATURES = [
     ("shci_sigma", _i32, [_vp, _i32, _vp, _vp, _i32]),
     ("shci_sigma_device", _i32, [_vp, _i32, _vp, _vp, _i32, _i64]),
     ("shci_sigma_packed_device", _i32, [_vp, _i32, _vp, _i32, _i32, _vp, _i64]),
+    ("shci_sigma_device_noalloc", _i32, [_vp, _i32, _vp, _vp, _i32, _i64]),
     ("shci_ham_bytes", _i32, [_vp, _P(_i64), _P(_i64)]),
     ("shci_davidson", _i32, [_vp, _i32, _i32, _i32, _vp, _i32, _dbl, _vp, _P(_i32)]),
     ("shci_run_input", _i32, [_vp, ctypes.c_char_p, ctypes.c_char_p, _i32, _i32, _vp, _i32, _P(_i32)]),
@@ -198,6 +199,11 @@ class Engine:
         """Device pointers (ints): column-major x, y with leading dimension ld."""
         self._check(load_library().shci_sigma_device(self.h, MODES.get(mode, mode), ctypes.c_void_p(x_ptr),
                                                      ctypes.c_void_p(y_ptr), k, ld))
+
+    def sigma_device_noalloc(self, x_ptr, y_ptr, k, ld, mode="mixed"):
+        """Allocation-free sigma on device pointers (see include/shci_gpu.h)."""
+        self._check(load_library().shci_sigma_device_noalloc(self.h, MODES.get(mode, mode), ctypes.c_void_p(x_ptr),
+                                                             ctypes.c_void_p(y_ptr), k, ld))
 
     def sigma_packed_device(self, xp_ptr, kp, k, y_ptr, ld, mode="mixed"):
         self._check(load_library().shci_sigma_packed_device(self.h, MODES.get(mode, mode), ctypes.c_void_p(xp_ptr),

@@ -120,6 +120,24 @@ int shci_sigma_device(shci_ctx* ctx, int mode, const double* x_dev, double* y_de
  * Replaces the inner product loop of Hmult2::operator() (SHCI/Hmult.h:108-123). */
 int shci_sigma_packed_device(shci_ctx* ctx, int mode, const void* x_packed, int kp, int k, double* y_dev,
                              int64_t ld);
+/* Allocation-free variant of shci_sigma_device. It has no counterpart in the
+ * reference. It is for callers that cannot allocate device memory while they
+ * run: for example a host program whose own memory pool owns all of the GPU's
+ * memory, or a time-critical loop that must not trigger the implicit device
+ * synchronisation that cudaMalloc/cudaFree can cause. The context must have
+ * been set up beforehand (shci_ham_build, which does allocate); this call
+ * itself calls no cudaMalloc, cudaFree or allocating library routine.
+ * The row-interleaved copy of x goes to one fixed 16 MiB device array
+ * compiled into the library instead of a context buffer, which limits N x k
+ * (k = 3 counts as 4) to 4,194,304 for SHCI_MODE_MIXED and 2,097,152 for
+ * SHCI_MODE_FP64; larger sizes return SHCI_ERR_INVALID. The array is held by
+ * every GPU that loads the library until the process exits. The first call on
+ * each device looks up the array's device address (cudaGetSymbolAddress), so
+ * make that first call before any stream capture on that device. All calls
+ * share the array: calls that overlap on the GPU (other streams or contexts
+ * at the same time) race on it. Enqueued on the context stream, no host
+ * synchronisation. SHCI_MODE_DIRECT is not supported. */
+int shci_sigma_device_noalloc(shci_ctx* ctx, int mode, const double* x_dev, double* y_dev, int k, int64_t ld);
 /* Bytes of the stored Hamiltonian (row pointers, columns, values) and of the
  * string tables, for memory and roofline accounting. */
 int shci_ham_bytes(shci_ctx* ctx, int64_t* csr_bytes, int64_t* helper_bytes);
