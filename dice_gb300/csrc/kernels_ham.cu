@@ -191,12 +191,13 @@ __device__ void visit_row(const HelperView& h, uint32_t I, V& v) {
       int64_t p = base + lane;
       bool hit = false;
       uint32_t J = 0;
+      int d = -1;
       if (p < p1) {
-        int d = __popcll(h.aGroupB[p] ^ B);
+        d = __popcll(h.aGroupB[p] ^ B);
         hit = (d == 2 || d == 4);
         J = h.aDets[p];
       }
-      v.step(hit, J);
+      v.step(hit, J, d == 2);
     }
   }
   // 2. alpha single excitation: beta equal (single alpha) or beta single (alpha-beta double)
@@ -231,13 +232,14 @@ __device__ void visit_row(const HelperView& h, uint32_t I, V& v) {
         int64_t eo = __shfl_sync(kFull, excl, lo);
         bool hit = false;
         uint32_t J = 0;
+        int d = -1;
         if (f < total) {
           int64_t p = gb + (f - eo);
-          int d = __popcll(h.aGroupB[p] ^ B);
+          d = __popcll(h.aGroupB[p] ^ B);
           hit = (d == 0 || d == 2);
           J = h.aDets[p];
         }
-        v.step(hit, J);
+        v.step(hit, J, d == 0);
       }
     }
   }
@@ -253,14 +255,14 @@ __device__ void visit_row(const HelperView& h, uint32_t I, V& v) {
         hit = (d == 4);
         J = h.bDets[p];
       }
-      v.step(hit, J);
+      v.step(hit, J, false);
     }
   }
 }
 
 struct CountVisitor {
   int64_t c = 0;
-  __device__ void step(bool hit, uint32_t) { c += hit; }
+  __device__ void step(bool hit, uint32_t, bool) { c += hit; }
 };
 
 __global__ void k_ham_count(HelperView h, int64_t* __restrict__ counts) {
@@ -279,6 +281,11 @@ __global__ void k_ham_count(HelperView h, int64_t* __restrict__ counts) {
 // Emits (col, value) for one row; H_IJ is evaluated with the higher-index
 // determinant as the ket, the element the reference stores in row max(I,J)
 // (SHCI/SHCImakeHamiltonian.cpp:565-580).
+//
+// Connections found by the scans are queued per warp in shared memory, one
+// queue for single and one for double excitations; whenever a queue holds 32
+// entries all lanes evaluate one Slater-Condon element each, so the FP64 work
+// runs on full warps and singles (an O(n_elec) sum) do not wait on doubles.
 struct EmitVisitor {
   const Det2* dets;
   IntsView ints;
@@ -289,32 +296,64 @@ struct EmitVisitor {
   double* v64;
   float* vhi;
   float* vlo;
-  __device__ void step(bool hit, uint32_t J) {
-    const int lane = threadIdx.x & 31;
-    unsigned m = __ballot_sync(kFull, hit);
-    if (hit) {
-      int64_t q = pos + __popc(m & ((1u << lane) - 1u));
-      Det2 dJ = dets[J];
-      double hv = (J < I) ? hij_any(ints, dJ, dI) : hij_any(ints, dI, dJ);
-      col[q] = (int32_t)J;
-      if (v64) v64[q] = hv;
-      if (vhi) {
-        float hi = (float)hv;
-        vhi[q] = hi;
-        if (vlo) vlo[q] = (float)(hv - (double)hi);
-      }
+  uint32_t* qs;  // 64 entries: single excitations
+  uint32_t* qd;  // 64 entries: double excitations
+  int ns, nd;
+
+  __device__ void store(int64_t q, uint32_t J) {
+    const Det2 dJ = dets[J];
+    const double hv = (J < I) ? hij_any(ints, dJ, dI) : hij_any(ints, dI, dJ);
+    col[q] = (int32_t)J;
+    if (v64) v64[q] = hv;
+    if (vhi) {
+      const float hi = (float)hv;
+      vhi[q] = hi;
+      if (vlo) vlo[q] = (float)(hv - (double)hi);
     }
-    pos += __popc(m);
+  }
+  // evaluate the first `cnt` (<= 32) entries of queue q, then shift the rest down
+  __device__ int drain(uint32_t* q, int n, int cnt) {
+    const int lane = threadIdx.x & 31;
+    if (lane < cnt) store(pos + lane, q[lane]);
+    pos += cnt;
+    __syncwarp();
+    const int rest = n - cnt;
+    uint32_t v = lane < rest ? q[cnt + lane] : 0u;
+    __syncwarp();
+    if (lane < rest) q[lane] = v;
+    __syncwarp();
+    return rest;
+  }
+  __device__ void step(bool hit, uint32_t J, bool single) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const unsigned ms = __ballot_sync(kFull, hit && single);
+    const unsigned md = __ballot_sync(kFull, hit && !single);
+    if (hit && single) qs[ns + __popc(ms & lt)] = J;
+    if (hit && !single) qd[nd + __popc(md & lt)] = J;
+    ns += __popc(ms);
+    nd += __popc(md);
+    __syncwarp();
+    if (ns >= 32) ns = drain(qs, ns, 32);
+    if (nd >= 32) nd = drain(qd, nd, 32);
+  }
+  __device__ void flush() {
+    if (ns) ns = drain(qs, ns, ns);
+    if (nd) nd = drain(qd, nd, nd);
   }
 };
 
-__global__ void k_ham_emit(HelperView h, const Det2* __restrict__ dets, IntsView ints,
-                           const int64_t* __restrict__ rowptr, int32_t* __restrict__ col, double* __restrict__ v64,
-                           float* __restrict__ vhi, float* __restrict__ vlo) {
+__global__ void __launch_bounds__(256) k_ham_emit(HelperView h, const Det2* __restrict__ dets, IntsView ints,
+                                                  const int64_t* __restrict__ rowptr, int32_t* __restrict__ col,
+                                                  double* __restrict__ v64, float* __restrict__ vhi,
+                                                  float* __restrict__ vlo) {
+  __shared__ uint32_t s_q[8][2][64];
+  const int wib = threadIdx.x >> 5;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   for (int64_t I = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; I < (int64_t)h.N; I += warps) {
-    EmitVisitor v{dets, ints, dets[I], (uint32_t)I, rowptr[I], col, v64, vhi, vlo};
+    EmitVisitor v{dets, ints, dets[I], (uint32_t)I, rowptr[I], col, v64, vhi, vlo, s_q[wib][0], s_q[wib][1], 0, 0};
     visit_row(h, (uint32_t)I, v);
+    v.flush();
   }
 }
 
@@ -384,7 +423,7 @@ struct DirectVisitor {
   uint32_t I;
   const double* x;
   double acc[K];
-  __device__ void step(bool hit, uint32_t J) {
+  __device__ void step(bool hit, uint32_t J, bool) {
     if (hit) {
       Det2 dJ = dets[J];
       double hv = (J < I) ? hij_any(ints, dJ, dI) : hij_any(ints, dI, dJ);
