@@ -95,6 +95,8 @@ def make_inputs(d, case="full"):
     from dice_gb300 import synthetic
     if case == "small":
         return synthetic.make_workload(WORKLOAD, d, schedule=[(0, 1e-3)], maxiter=2)
+    if case == "medium":  # ~5.7e5 determinants: x no longer fits L1, a few GB on the device
+        return synthetic.make_workload(WORKLOAD, d, schedule=[(0, 1e-3), (2, 3e-4)], maxiter=3)
     return synthetic.make_workload(WORKLOAD, d)
 
 
@@ -306,7 +308,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--case", default="full", choices=["full", "small"],
+    ap.add_argument("--case", default="full", choices=["full", "medium", "small"],
                     help="small: the profiling case (two eps1 = 1e-3 iterations)")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -39,11 +39,26 @@ constexpr double kStallWindow = 2e-5;
 // |<x|F|x>| above which a vector counts as having a definite flip parity.
 constexpr double kParityDefinite = 0.999;
 
-// SHCI_TRACE=1 prints one line per Davidson iteration to stderr.
-static const int trace_level = [] {
-  const char* v = std::getenv("SHCI_TRACE");
-  return v ? std::atoi(v) : 0;
-}();
+// SHCI_TRACE=1 prints one line per Davidson iteration to stderr, 2 also the
+// phases of the Hamiltonian build.
+int trace_level() {
+  static const int level = [] {
+    const char* v = std::getenv("SHCI_TRACE");
+    return v ? std::atoi(v) : 0;
+  }();
+  return level;
+}
+static double wall_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+PhaseTimer::PhaseTimer(cudaStream_t st) : s(st), t0(trace_level() >= 2 ? wall_s() : 0.0) {}
+void PhaseTimer::mark(const char* what) {
+  if (trace_level() < 2) return;
+  cudaStreamSynchronize(s);
+  const double t = wall_s();
+  std::fprintf(stderr, "[phase] %-16s %9.3f ms\n", what, (t - t0) * 1e3);
+  t0 = t;
+}
 
 static inline unsigned grid_for(size_t n, int threads, size_t max_blocks = 152 * 32) {
   size_t b = (n + threads - 1) / threads;
@@ -253,6 +268,8 @@ struct Context {
 
   void set_dets(const uint64_t* h, int64_t n) {
     require_ints();
+    H.N = 0;  // the stored Hamiltonian no longer describes a prefix of the space
+    H.nnz = 0;
     if (n < 0) throw Error(kErrInvalid, "negative determinant count");
     const int n2 = 2 * hints.norb;
     for (int64_t i = 0; i < n; ++i) {
@@ -322,10 +339,12 @@ struct Context {
     require_ints();
     require_dets();
     if (mode < 0 || mode > 2) throw Error(kErrInvalid, "unknown Hamiltonian mode");
+    PhaseTimer pt(stream);
     if (!helpers_ok) {
       helpers.build(dets.p, ndet, hints.norb, prims, stream);
       helpers_ok = true;
     }
+    pt.mark("string tables");
     ensure_diag();
     if (mode == SHCI_MODE_DIRECT) {
       H.col.release();
@@ -333,11 +352,14 @@ struct Context {
       H.vhi.release();
       H.vlo.release();
       H.rowptr.release();
-      H.N = ndet;
+      H.N = 0;
       H.nnz = 0;
     } else {
+      // the stored rows stay valid for the unchanged prefix of the space
+      // (selection only appends), so only new rows and columns are built
+      const size_t n_old = (ham_mode == mode) ? H.N : 0;
       build_ham_csr(helpers, dets.p, ints(), H, mode == SHCI_MODE_FP64, mode == SHCI_MODE_MIXED,
-                    mode == SHCI_MODE_MIXED, prims, stream);
+                    mode == SHCI_MODE_MIXED, n_old, prims, stream);
     }
     ham_mode = mode;
     ham_ok = true;
@@ -510,7 +532,7 @@ struct Context {
       std::vector<double> rn(nroots);
       for (int c = 0; c < nroots; ++c) rn[c] = std::sqrt(std::max(0.0, RR[(size_t)c * nroots + c]));
       numIter++;
-      if (trace_level > 0)
+      if (trace_level() > 0)
         std::fprintf(stderr, "[davidson mode=%d it=%d m=%d] lam0=%.12f res0=%.3e G00=%.12f\n", mode, numIter, m,
                      lam[0], rn[0], G[0]);
       auto finish = [&]() {

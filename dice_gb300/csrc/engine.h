@@ -32,6 +32,16 @@ extern std::atomic<int64_t> g_launch_count;
     SHCI_CUDA(cudaGetLastError());                                            \
   } while (0)
 
+// SHCI_TRACE >= 2 prints the duration of each build phase to stderr (the
+// stream is synchronised at every mark only when tracing is on).
+int trace_level();
+struct PhaseTimer {
+  cudaStream_t s;
+  double t0;
+  explicit PhaseTimer(cudaStream_t st);
+  void mark(const char* what);
+};
+
 // Device allocation cap (bytes) for out-of-memory emulation in tests; 0 = off.
 extern size_t g_alloc_cap;
 extern size_t g_alloc_live;

@@ -55,8 +55,11 @@ struct Csr {
   size_t bytes() const { return rowptr.bytes() + col.bytes() + v64.bytes() + vhi.bytes() + vlo.bytes(); }
 };
 
+// Builds H for the space described by hp. When H already holds rows for the
+// first n_old determinants (same value arrays), only the rows >= n_old and the
+// new columns of the old rows are computed and merged in; otherwise all rows.
 void build_ham_csr(const Helpers& hp, const Det2* dets, const IntsView& ints, Csr& H, bool want64, bool want32,
-                   bool want_lo, Prims& pr, cudaStream_t s);
+                   bool want_lo, size_t n_old, Prims& pr, cudaStream_t s);
 void compute_diag(const Det2* dets, size_t n, const IntsView& ints, double* diag, cudaStream_t s);
 void sigma_direct(const Helpers& hp, const Det2* dets, const IntsView& ints, const double* diag, const double* x,
                   double* y, int k, cudaStream_t s);

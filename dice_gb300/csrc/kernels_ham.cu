@@ -14,6 +14,8 @@
 //   3. determinants sharing I's beta string: alpha distance 2.
 // This visits the same (I, J) set as the reference's five helper-list classes
 // (single alpha, alpha-beta, single beta, double beta, double alpha).
+#include <algorithm>
+
 #include "engine.h"
 #include "ham.h"
 
@@ -265,16 +267,17 @@ struct CountVisitor {
   __device__ void step(bool hit, uint32_t, bool) { c += hit; }
 };
 
-__global__ void k_ham_count(HelperView h, int64_t* __restrict__ counts) {
+// Rows [row0, N); counts[I - row0] = number of off-diagonal connections.
+__global__ void k_ham_count(HelperView h, int64_t row0, int64_t* __restrict__ counts) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t I = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; I < (int64_t)h.N; I += warps) {
+  for (int64_t I = row0 + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); I < (int64_t)h.N; I += warps) {
     CountVisitor v;
     visit_row(h, (uint32_t)I, v);
     int64_t c = v.c;
 #pragma unroll
     for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(kFull, c, o);
-    if (lane == 0) counts[I] = c;
+    if (lane == 0) counts[I - row0] = c;
   }
 }
 
@@ -343,15 +346,17 @@ struct EmitVisitor {
   }
 };
 
-__global__ void __launch_bounds__(256) k_ham_emit(HelperView h, const Det2* __restrict__ dets, IntsView ints,
-                                                  const int64_t* __restrict__ rowptr, int32_t* __restrict__ col,
-                                                  double* __restrict__ v64, float* __restrict__ vhi,
-                                                  float* __restrict__ vlo) {
+// Rows [row0, N) into a CSR whose row pointers start at row row0.
+__global__ void __launch_bounds__(256) k_ham_emit(HelperView h, int64_t row0, const Det2* __restrict__ dets,
+                                                  IntsView ints, const int64_t* __restrict__ rowptr,
+                                                  int32_t* __restrict__ col, double* __restrict__ v64,
+                                                  float* __restrict__ vhi, float* __restrict__ vlo) {
   __shared__ uint32_t s_q[8][2][64];
   const int wib = threadIdx.x >> 5;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t I = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; I < (int64_t)h.N; I += warps) {
-    EmitVisitor v{dets, ints, dets[I], (uint32_t)I, rowptr[I], col, v64, vhi, vlo, s_q[wib][0], s_q[wib][1], 0, 0};
+  for (int64_t I = row0 + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); I < (int64_t)h.N; I += warps) {
+    EmitVisitor v{dets, ints, dets[I], (uint32_t)I, rowptr[I - row0], col, v64, vhi, vlo, s_q[wib][0], s_q[wib][1],
+                  0, 0};
     visit_row(h, (uint32_t)I, v);
     v.flush();
   }
@@ -359,31 +364,259 @@ __global__ void __launch_bounds__(256) k_ham_emit(HelperView h, const Det2* __re
 
 __global__ void k_set_last(int64_t* rowptr, int64_t n, int64_t total) { rowptr[n] = total; }
 
-void build_ham_csr(const Helpers& hp, const Det2* dets, const IntsView& ints, Csr& H, bool want64, bool want32,
-                   bool want_lo, Prims& pr, cudaStream_t s) {
-  const size_t N = hp.N;
+// Bitonic sort of one row (columns with their values) in shared memory, one
+// block per row. Rows longer than kRowSortCap are left in emission order
+// (still correct, only with less gather locality in sigma).
+constexpr int kRowSortCap = 4096;
+
+__global__ void __launch_bounds__(256) k_row_sort(const int64_t* __restrict__ rowptr, size_t N, int32_t* __restrict__ col,
+                                                  double* __restrict__ v64, float* __restrict__ vhi,
+                                                  float* __restrict__ vlo) {
+  extern __shared__ unsigned char sm_raw[];
+  uint32_t* key = reinterpret_cast<uint32_t*>(sm_raw);
+  uint64_t* pay = reinterpret_cast<uint64_t*>(sm_raw + (size_t)kRowSortCap * sizeof(uint32_t));
+  for (size_t r = blockIdx.x; r < N; r += gridDim.x) {
+    const int64_t p0 = rowptr[r], len = rowptr[r + 1] - p0;
+    if (len <= 1 || len > kRowSortCap) continue;  // uniform across the block
+    int P = 2;
+    while (P < len) P <<= 1;
+    for (int i = threadIdx.x; i < P; i += blockDim.x) {
+      if (i < len) {
+        key[i] = (uint32_t)col[p0 + i];
+        uint64_t v;
+        if (v64) {
+          v = (uint64_t)__double_as_longlong(v64[p0 + i]);
+        } else {
+          v = (uint64_t)__float_as_uint(vhi[p0 + i]);
+          if (vlo) v |= (uint64_t)__float_as_uint(vlo[p0 + i]) << 32;
+        }
+        pay[i] = v;
+      } else {
+        key[i] = 0xffffffffu;
+        pay[i] = 0;
+      }
+    }
+    __syncthreads();
+    for (int k = 2; k <= P; k <<= 1)
+      for (int j = k >> 1; j > 0; j >>= 1) {
+        for (int i = threadIdx.x; i < P; i += blockDim.x) {
+          const int ixj = i ^ j;
+          if (ixj > i) {
+            const bool up = (i & k) == 0;
+            const uint32_t a = key[i], b = key[ixj];
+            if ((a > b) == up) {
+              key[i] = b;
+              key[ixj] = a;
+              const uint64_t t = pay[i];
+              pay[i] = pay[ixj];
+              pay[ixj] = t;
+            }
+          }
+        }
+        __syncthreads();
+      }
+    for (int i = threadIdx.x; i < len; i += blockDim.x) {
+      col[p0 + i] = (int32_t)key[i];
+      const uint64_t v = pay[i];
+      if (v64) {
+        v64[p0 + i] = __longlong_as_double((long long)v);
+      } else {
+        vhi[p0 + i] = __uint_as_float((uint32_t)v);
+        if (vlo) vlo[p0 + i] = __uint_as_float((uint32_t)(v >> 32));
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Value arrays of a CSR as raw pointers.
+struct CsrVals {
+  int32_t* col;
+  double* v64;
+  float* vhi;
+  float* vlo;
+};
+
+static void sort_rows(const int64_t* rowptr, size_t n, const CsrVals& v, cudaStream_t s) {
+  if (n == 0) return;
+  const size_t smem = (size_t)kRowSortCap * (sizeof(uint32_t) + sizeof(uint64_t));
+  SHCI_CUDA(cudaFuncSetAttribute(k_row_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const unsigned sblocks = (unsigned)std::min<size_t>(n, 152 * 8);
+  k_row_sort<<<sblocks, 256, smem, s>>>(rowptr, n, v.col, v.v64, v.vhi, v.vlo);
+  SHCI_LAUNCH_CHECK();
+}
+
+// Count, emit and sort the full rows [row0, N) into (rowptr, vals); returns nnz.
+static int64_t emit_rows(const Helpers& hp, size_t row0, const Det2* dets, const IntsView& ints, DevBuf<int64_t>& rowptr,
+                         DevBuf<int32_t>& col, DevBuf<double>& v64, DevBuf<float>& vhi, DevBuf<float>& vlo,
+                         bool want64, bool want32, bool want_lo, Prims& pr, cudaStream_t s, PhaseTimer& pt) {
+  const size_t N = hp.N, nr = N - row0;
   HelperView hv = hp.view();
   DevBuf<int64_t> counts;
-  counts.resize(N);
-  const unsigned blocks = grid_for(N * 32, 256, 152 * 16);
-  k_ham_count<<<blocks, 256, 0, s>>>(hv, counts.p);
-  SHCI_LAUNCH_CHECK();
-  H.rowptr.resize(N + 1);
+  counts.resize(nr > 0 ? nr : 1);
+  const unsigned blocks = grid_for(nr * 32, 256, 152 * 16);
+  if (nr) {
+    k_ham_count<<<blocks, 256, 0, s>>>(hv, (int64_t)row0, counts.p);
+    SHCI_LAUNCH_CHECK();
+  }
+  pt.mark("ham count");
+  rowptr.resize(nr + 1);
   int64_t total = 0;
-  scan_exclusive_i64(counts.p, H.rowptr.p, N, &total, pr, s);
-  k_set_last<<<1, 1, 0, s>>>(H.rowptr.p, (int64_t)N, total);
+  scan_exclusive_i64(counts.p, rowptr.p, nr, &total, pr, s);
+  k_set_last<<<1, 1, 0, s>>>(rowptr.p, (int64_t)nr, total);
   SHCI_LAUNCH_CHECK();
-  H.N = N;
-  H.nnz = total;
-  size_t cap = total > 0 ? (size_t)total : 1;
-  H.col.resize(cap);
-  if (want64) H.v64.resize(cap); else H.v64.release();
-  if (want32) H.vhi.resize(cap); else H.vhi.release();
-  if (want32 && want_lo) H.vlo.resize(cap); else H.vlo.release();
-  k_ham_emit<<<blocks, 256, 0, s>>>(hv, dets, ints, H.rowptr.p, H.col.p, want64 ? H.v64.p : nullptr,
-                                    want32 ? H.vhi.p : nullptr, (want32 && want_lo) ? H.vlo.p : nullptr);
+  const size_t cap = total > 0 ? (size_t)total : 1;
+  col.resize(cap);
+  if (want64) v64.resize(cap); else v64.release();
+  if (want32) vhi.resize(cap); else vhi.release();
+  if (want32 && want_lo) vlo.resize(cap); else vlo.release();
+  CsrVals v{col.p, want64 ? v64.p : nullptr, want32 ? vhi.p : nullptr, (want32 && want_lo) ? vlo.p : nullptr};
+  if (nr) {
+    k_ham_emit<<<blocks, 256, 0, s>>>(hv, (int64_t)row0, dets, ints, rowptr.p, v.col, v.v64, v.vhi, v.vlo);
+    SHCI_LAUNCH_CHECK();
+  }
+  pt.mark("ham emit");
+  // sort every row by column so that the 32 gathers of one warp instruction in
+  // sigma fall on fewer 32-byte sectors of x
+  sort_rows(rowptr.p, nr, v, s);
+  pt.mark("ham row sort");
+  return total;
+}
+
+// Incremental build helpers. New rows R >= n_old are emitted in full; their
+// entries with column C < n_old are the new columns of old row C (same value:
+// H_CR is evaluated with R, the higher index, as the ket in both places).
+__global__ void k_delta_count(const int64_t* __restrict__ rp_new, size_t nr, const int32_t* __restrict__ col_new,
+                              int64_t n_old, unsigned long long* __restrict__ dcnt) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < (int64_t)nr; r += warps)
+    for (int64_t p = rp_new[r] + lane; p < rp_new[r + 1]; p += 32) {
+      const int32_t c = col_new[p];
+      if (c < n_old) atomicAdd(&dcnt[c], 1ull);
+    }
+}
+__global__ void k_delta_fill(const int64_t* __restrict__ rp_new, size_t nr, CsrVals nv, int64_t n_old,
+                             const int64_t* __restrict__ dptr, unsigned long long* __restrict__ dfill, CsrVals dv) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < (int64_t)nr; r += warps)
+    for (int64_t p = rp_new[r] + lane; p < rp_new[r + 1]; p += 32) {
+      const int32_t c = nv.col[p];
+      if (c >= n_old) continue;
+      const int64_t q = dptr[c] + (int64_t)atomicAdd(&dfill[c], 1ull);
+      dv.col[q] = (int32_t)(n_old + r);
+      if (dv.v64) dv.v64[q] = nv.v64[p];
+      if (dv.vhi) dv.vhi[q] = nv.vhi[p];
+      if (dv.vlo) dv.vlo[q] = nv.vlo[p];
+    }
+}
+__global__ void k_merged_len(const int64_t* __restrict__ rp_old, const int64_t* __restrict__ dptr, int64_t n_old,
+                             const int64_t* __restrict__ rp_new, int64_t nr, int64_t* __restrict__ len) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_old + nr;
+       i += (int64_t)gridDim.x * blockDim.x)
+    len[i] = i < n_old ? (rp_old[i + 1] - rp_old[i]) + (dptr[i + 1] - dptr[i]) : rp_new[i - n_old + 1] - rp_new[i - n_old];
+}
+// Merged row I: old row I followed by its new columns (all larger than the
+// old ones, so the row stays sorted); rows >= n_old are copied from the new rows.
+__global__ void k_merge_rows(const int64_t* __restrict__ rp_old, CsrVals ov, const int64_t* __restrict__ dptr,
+                             CsrVals dv, const int64_t* __restrict__ rp_new, CsrVals nv, int64_t n_old, int64_t nr,
+                             const int64_t* __restrict__ rp, CsrVals out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  auto copy = [&](const CsrVals& src, int64_t s0, int64_t s1, int64_t d0) {
+    for (int64_t p = s0 + lane; p < s1; p += 32) {
+      const int64_t q = d0 + (p - s0);
+      out.col[q] = src.col[p];
+      if (out.v64) out.v64[q] = src.v64[p];
+      if (out.vhi) out.vhi[q] = src.vhi[p];
+      if (out.vlo) out.vlo[q] = src.vlo[p];
+    }
+  };
+  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n_old + nr; i += warps) {
+    const int64_t d = rp[i];
+    if (i < n_old) {
+      copy(ov, rp_old[i], rp_old[i + 1], d);
+      copy(dv, dptr[i], dptr[i + 1], d + (rp_old[i + 1] - rp_old[i]));
+    } else {
+      copy(nv, rp_new[i - n_old], rp_new[i - n_old + 1], d);
+    }
+  }
+}
+
+void build_ham_csr(const Helpers& hp, const Det2* dets, const IntsView& ints, Csr& H, bool want64, bool want32,
+                   bool want_lo, size_t n_old, Prims& pr, cudaStream_t s) {
+  const size_t N = hp.N;
+  PhaseTimer pt(s);
+  const bool incremental = n_old > 0 && n_old < N && H.N == n_old && (H.v64.p != nullptr) == want64 &&
+                           (H.vhi.p != nullptr) == want32 && (H.vlo.p != nullptr) == (want32 && want_lo);
+  if (!incremental) {
+    if (n_old == N && H.N == N) return;  // nothing new
+    H.nnz = emit_rows(hp, 0, dets, ints, H.rowptr, H.col, H.v64, H.vhi, H.vlo, want64, want32, want_lo, pr, s, pt);
+    H.N = N;
+    SHCI_CUDA(cudaStreamSynchronize(s));
+    return;
+  }
+  const size_t nr = N - n_old;
+  Csr Hn;  // rows n_old .. N-1
+  Hn.nnz = emit_rows(hp, n_old, dets, ints, Hn.rowptr, Hn.col, Hn.v64, Hn.vhi, Hn.vlo, want64, want32, want_lo, pr, s,
+                     pt);
+  CsrVals nv{Hn.col.p, Hn.v64.p, Hn.vhi.p, Hn.vlo.p};
+  // new columns of the old rows
+  DevBuf<unsigned long long> dcnt, dfill;
+  dcnt.resize(n_old);
+  dfill.resize(n_old);
+  SHCI_CUDA(cudaMemsetAsync(dcnt.p, 0, n_old * sizeof(unsigned long long), s));
+  SHCI_CUDA(cudaMemsetAsync(dfill.p, 0, n_old * sizeof(unsigned long long), s));
+  const unsigned wblocks = grid_for(nr * 32, 256, 152 * 16);
+  k_delta_count<<<wblocks, 256, 0, s>>>(Hn.rowptr.p, nr, Hn.col.p, (int64_t)n_old, dcnt.p);
+  SHCI_LAUNCH_CHECK();
+  DevBuf<int64_t> dptr;
+  dptr.resize(n_old + 1);
+  int64_t dtotal = 0;
+  scan_exclusive_i64(reinterpret_cast<const int64_t*>(dcnt.p), dptr.p, n_old, &dtotal, pr, s);
+  k_set_last<<<1, 1, 0, s>>>(dptr.p, (int64_t)n_old, dtotal);
+  SHCI_LAUNCH_CHECK();
+  Csr Hd;
+  const size_t dcap = dtotal > 0 ? (size_t)dtotal : 1;
+  Hd.col.resize(dcap);
+  if (want64) Hd.v64.resize(dcap);
+  if (want32) Hd.vhi.resize(dcap);
+  if (want32 && want_lo) Hd.vlo.resize(dcap);
+  CsrVals dv{Hd.col.p, Hd.v64.p, Hd.vhi.p, Hd.vlo.p};
+  k_delta_fill<<<wblocks, 256, 0, s>>>(Hn.rowptr.p, nr, nv, (int64_t)n_old, dptr.p, dfill.p, dv);
+  SHCI_LAUNCH_CHECK();
+  sort_rows(dptr.p, n_old, dv, s);
+  pt.mark("ham new columns");
+  // merge
+  DevBuf<int64_t> len, rp;
+  len.resize(N);
+  rp.resize(N + 1);
+  k_merged_len<<<grid_for(N, 256), 256, 0, s>>>(H.rowptr.p, dptr.p, (int64_t)n_old, Hn.rowptr.p, (int64_t)nr, len.p);
+  SHCI_LAUNCH_CHECK();
+  int64_t total = 0;
+  scan_exclusive_i64(len.p, rp.p, N, &total, pr, s);
+  k_set_last<<<1, 1, 0, s>>>(rp.p, (int64_t)N, total);
+  SHCI_LAUNCH_CHECK();
+  Csr M;
+  const size_t cap = total > 0 ? (size_t)total : 1;
+  M.col.resize(cap);
+  if (want64) M.v64.resize(cap);
+  if (want32) M.vhi.resize(cap);
+  if (want32 && want_lo) M.vlo.resize(cap);
+  CsrVals ov{H.col.p, H.v64.p, H.vhi.p, H.vlo.p}, mv{M.col.p, M.v64.p, M.vhi.p, M.vlo.p};
+  k_merge_rows<<<grid_for(N * 32, 256, 152 * 16), 256, 0, s>>>(H.rowptr.p, ov, dptr.p, dv, Hn.rowptr.p, nv,
+                                                               (int64_t)n_old, (int64_t)nr, rp.p, mv);
   SHCI_LAUNCH_CHECK();
   SHCI_CUDA(cudaStreamSynchronize(s));
+  H.rowptr.swap(rp);
+  H.col.swap(M.col);
+  H.v64.swap(M.v64);
+  H.vhi.swap(M.vhi);
+  H.vlo.swap(M.vlo);
+  H.N = N;
+  H.nnz = total;
+  pt.mark("ham merge");
 }
 
 // ---------------------------------------------------------------------------

@@ -101,22 +101,22 @@ __global__ void __launch_bounds__(256) k_sigma_mixed(const int64_t* __restrict__
     for (int c = 0; c < KP; ++c) acc[c] = Acc{0.f, 0.f};
     const int64_t p0 = live ? __ldg(rowptr + r) : 0;
     const int64_t p1 = live ? __ldg(rowptr + r + 1) : 0;
-    // head up to a 16-byte boundary, then 4 nonzeros per lane per step with
-    // 16-byte streaming loads (four independent gathers in flight), then tail
-    const int64_t pa = min(p1, (p0 + 3) & ~(int64_t)3);
-    for (int64_t p = p0 + sub; p < pa; p += VW) VecF<KP>::fma(acc, __ldcs(val + p), x, __ldcs(col + p));
-    const int64_t nv = (p1 - pa) >> 2;
-    const int4* c4 = reinterpret_cast<const int4*>(col + pa);
-    const float4* v4 = reinterpret_cast<const float4*>(val + pa);
-    for (int64_t q = sub; q < nv; q += VW) {
-      const int4 j = __ldcs(c4 + q);
-      const float4 h = __ldcs(v4 + q);
-      VecF<KP>::fma(acc, h.x, x, j.x);
-      VecF<KP>::fma(acc, h.y, x, j.y);
-      VecF<KP>::fma(acc, h.z, x, j.z);
-      VecF<KP>::fma(acc, h.w, x, j.w);
+    // Consecutive lanes take consecutive nonzeros: the column and value loads
+    // are coalesced, and on a column-sorted row the 32 gathers of one
+    // instruction land on as few 32-byte sectors of x as the row allows.
+    // Four nonzeros per lane per step keep four gathers in flight.
+    int64_t p = p0 + sub;
+    for (; p + 3 * VW < p1; p += 4 * VW) {
+      const int j0 = __ldcs(col + p), j1 = __ldcs(col + p + VW);
+      const int j2 = __ldcs(col + p + 2 * VW), j3 = __ldcs(col + p + 3 * VW);
+      const float h0 = __ldcs(val + p), h1 = __ldcs(val + p + VW);
+      const float h2 = __ldcs(val + p + 2 * VW), h3 = __ldcs(val + p + 3 * VW);
+      VecF<KP>::fma(acc, h0, x, j0);
+      VecF<KP>::fma(acc, h1, x, j1);
+      VecF<KP>::fma(acc, h2, x, j2);
+      VecF<KP>::fma(acc, h3, x, j3);
     }
-    for (int64_t p = pa + (nv << 2) + sub; p < p1; p += VW) VecF<KP>::fma(acc, __ldcs(val + p), x, __ldcs(col + p));
+    for (; p < p1; p += VW) VecF<KP>::fma(acc, __ldcs(val + p), x, __ldcs(col + p));
 #pragma unroll
     for (int c = 0; c < KP; ++c) {
 #pragma unroll
@@ -166,19 +166,17 @@ __global__ void __launch_bounds__(256) k_sigma_f64(const int64_t* __restrict__ r
 #pragma unroll
       for (int c = 0; c < KP; ++c) acc[c] += h * __ldg(x + (size_t)j * KP + c);
     };
-    const int64_t pa = min(p1, (p0 + 3) & ~(int64_t)3);
-    for (int64_t p = p0 + sub; p < pa; p += VW) elem(p, __ldcs(col + p));
-    const int64_t nv = (p1 - pa) >> 2;
-    const int4* c4 = reinterpret_cast<const int4*>(col + pa);
-    for (int64_t q = sub; q < nv; q += VW) {
-      const int4 j = __ldcs(c4 + q);
-      const int64_t p = pa + 4 * q;
-      elem(p, j.x);
-      elem(p + 1, j.y);
-      elem(p + 2, j.z);
-      elem(p + 3, j.w);
+    // consecutive lanes on consecutive nonzeros (see k_sigma_mixed)
+    int64_t p = p0 + sub;
+    for (; p + 3 * VW < p1; p += 4 * VW) {
+      const int j0 = __ldcs(col + p), j1 = __ldcs(col + p + VW);
+      const int j2 = __ldcs(col + p + 2 * VW), j3 = __ldcs(col + p + 3 * VW);
+      elem(p, j0);
+      elem(p + VW, j1);
+      elem(p + 2 * VW, j2);
+      elem(p + 3 * VW, j3);
     }
-    for (int64_t p = pa + (nv << 2) + sub; p < p1; p += VW) elem(p, __ldcs(col + p));
+    for (; p < p1; p += VW) elem(p, __ldcs(col + p));
 #pragma unroll
     for (int c = 0; c < KP; ++c) {
 #pragma unroll
