@@ -28,6 +28,7 @@
 #include "../../include/shci_gpu.h"
 #include "ham.h"
 #include "host_io.h"
+#include "mlp.h"
 
 namespace shci {
 
@@ -180,11 +181,25 @@ struct Context {
   DevBuf<int8_t> flipsgn;
   int flip_state = -1;
 
+  // preconditioner: 0 the reference's diagonal, 1 diagonal + second-order
+  // level shift from the stored H, 2 diagonal + shift predicted by the MLP
+  int precond = 0;
+  Mlp mlp;
+  DevBuf<double> shift, teacher;
+  bool shift_ready = false;
+  DevBuf<int32_t> tr_idx;
+  DevBuf<float> tr_tgt;
+  int mlp_steps = 200, mlp_batch = 4096;
+  float mlp_lr = 1e-3f;
+  int64_t mlp_sample = 200000;
+  double last_loss = 0.0;
+
   // run state
   DevBuf<double> ci, cmax;
   int nroots_run = 0;
   std::vector<IterLog> log;
-  double t_select = 0, t_ham = 0, t_dav = 0, t_total = 0, t_sigma = 0;
+  double t_select = 0, t_ham = 0, t_dav = 0, t_total = 0, t_sigma = 0, t_mlp = 0;
+  int64_t total_dav_iters = 0;
   int64_t n_sigma = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
@@ -616,7 +631,10 @@ struct Context {
         SHCI_CUDA(cudaMemcpyAsync(D.p + (size_t)a * N, R.p + (size_t)act[a] * N, N * sizeof(double),
                                   cudaMemcpyDeviceToDevice, stream));
       to_dev(dlam, act_lam);
-      precondition(diag.p, dlam.p, nact, N, D.p, N, stream);
+      if (shift_ready && shift.n >= N)
+        precondition_shift(diag.p, shift.p, dlam.p, nact, N, D.p, N, stream);
+      else
+        precondition(diag.p, dlam.p, nact, N, D.p, N, stream);
       if (sym) {
         // keep each correction in the flip sector of the root it corrects
         for (int a = 0; a < nact; ++a) {
@@ -661,10 +679,74 @@ struct Context {
     }
   }
 
+  // Shift of the preconditioner for the current space at energy estimate E
+  // (NaN: unknown, plain preconditioner).
+  void prepare_shift(double E) {
+    shift_ready = false;
+    if (precond == 0 || !(E == E) || ndet == 0) return;
+    shift.resize(ndet);
+    if (precond == 1) {
+      if (!ham_ok || ham_mode == SHCI_MODE_DIRECT) return;
+      pt2_shift(H, diag.p, E, shift.p, stream);
+      shift_ready = true;
+    } else if (precond == 2 && mlp.trained && mlp.nspin == 2 * hints.norb) {
+      mlp.infer(dets.p, diag.p, ndet, E, shift.p, stream);
+      shift_ready = true;
+    }
+  }
+
+  // Trains the MLP on the second-order shifts of (a sample of) the current
+  // space at energy E, the pairs the Davidson run itself produced. Returns the
+  // final minibatch loss.
+  double train_mlp(double E) {
+    if (!ham_ok || ham_mode == SHCI_MODE_DIRECT) throw Error(kErrState, "training needs a stored Hamiltonian");
+    ensure_diag();
+    if (mlp.nspin != 2 * hints.norb) mlp.init(2 * hints.norb, 7, stream);
+    teacher.resize(ndet);
+    pt2_shift(H, diag.p, E, teacher.p, stream);
+    const int64_t ns = std::min<int64_t>(mlp_sample, (int64_t)ndet);
+    std::vector<int32_t> idx(ndet);
+    std::iota(idx.begin(), idx.end(), 0);
+    uint64_t st = 0x2545F4914F6CDD1Dull ^ (uint64_t)ndet;
+    for (int64_t i = (int64_t)ndet - 1; i > 0; --i) {  // Fisher-Yates with xorshift
+      st ^= st << 13;
+      st ^= st >> 7;
+      st ^= st << 17;
+      std::swap(idx[i], idx[st % (uint64_t)(i + 1)]);
+    }
+    idx.resize(ns);
+    std::vector<double> t(ndet);
+    SHCI_CUDA(cudaMemcpyAsync(t.data(), teacher.p, ndet * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    SHCI_CUDA(cudaStreamSynchronize(stream));
+    double rms = 0.0;
+    for (int32_t i : idx) rms += t[i] * t[i];
+    rms = std::sqrt(rms / std::max<int64_t>(1, ns));
+    if (!(rms > 0.0)) rms = 1.0;
+    mlp.sigma = rms;
+    std::vector<float> tg(ns);
+    for (int64_t k = 0; k < ns; ++k) tg[k] = (float)(t[idx[k]] / rms);
+    tr_idx.resize(ns);
+    tr_tgt.resize(ns);
+    SHCI_CUDA(cudaMemcpyAsync(tr_idx.p, idx.data(), ns * sizeof(int32_t), cudaMemcpyHostToDevice, stream));
+    SHCI_CUDA(cudaMemcpyAsync(tr_tgt.p, tg.data(), ns * sizeof(float), cudaMemcpyHostToDevice, stream));
+    const int B = (int)std::min<int64_t>(mlp_batch, ns);
+    double loss = 0.0;
+    for (int s = 0; s < mlp_steps; ++s) {
+      const int64_t off = ((int64_t)s * B) % std::max<int64_t>(1, ns - B + 1);
+      loss = mlp.gradient(dets.p, diag.p, tr_idx.p + off, tr_tgt.p + off, B, E, stream);
+      mlp.adam(mlp_lr, stream);
+    }
+    SHCI_CUDA(cudaStreamSynchronize(stream));
+    mlp.trained = true;
+    last_loss = loss;
+    return loss;
+  }
+
   void davidson(int mode, bool block, int nroots, double* x, int maxCopies, double tol, bool direct_rules,
-                std::vector<double>& E, int& iters) {
+                std::vector<double>& E, int& iters, double E_est = std::nan("")) {
     if (!ham_ok) throw Error(kErrState, "Hamiltonian not built for the current space (call shci_ham_build)");
     ensure_diag();
+    prepare_shift(E_est);
     if (mode == SHCI_MODE_MIXED) {
       // FP32 stage, then the FP64 stage continues on the same basis with W
       // recomputed in FP64 (head + tail values)
@@ -681,8 +763,11 @@ struct Context {
   void run(const Schedule& s, int mode, bool block, std::vector<double>& Eout) {
     require_ints();
     const double t0 = now_s();
-    t_select = t_ham = t_dav = t_sigma = 0;
+    t_select = t_ham = t_dav = t_sigma = t_mlp = 0;
     n_sigma = 0;
+    total_dav_iters = 0;
+    shift_ready = false;
+    mlp.trained = false;
     log.clear();
     if (s.direct) mode = SHCI_MODE_DIRECT;
     // selection parameters
@@ -787,15 +872,24 @@ struct Context {
       const double prevE0 = (iter == 0) ? -10.0 : E0[0];
       int numIter = 0;
       const int maxCopies = block ? std::max(nroots + 4, 3 * nroots) : (s.direct ? nroots + 2 : nroots + 4);
-      davidson(mode, block, nroots, X0.p, maxCopies, s.davidsonTolLoose, s.direct, E0, numIter);
+      // the shifted preconditioners need an energy: the previous iteration's
+      const double E_est = iter == 0 ? std::nan("") : E0[0];
+      davidson(mode, block, nroots, X0.p, maxCopies, s.davidsonTolLoose, s.direct, E0, numIter, E_est);
       ci.swap(X0);
       double td = now_s();
       t_dav += td - tc;
       log.push_back({(int64_t)N, E0[0] + hints.coreE, numIter, td - t0});
+      total_dav_iters += numIter;
+      if (precond == 2 && mode != SHCI_MODE_DIRECT) {
+        train_mlp(E0[0]);  // pairs from this solve, used from the next solve on
+        t_mlp += now_s() - td;
+      }
       if (std::fabs(E0[0] - prevE0) < s.dE || iter == s.epsilon1.size() - 1) {
+        const double t1 = now_s();
         davidson(mode, block, nroots, ci.p, block ? std::max(nroots + 4, 3 * nroots) : nroots + 4, s.davidsonTol,
-                 s.direct, E0, numIter);
-        t_dav += now_s() - td;
+                 s.direct, E0, numIter, E0[0]);
+        total_dav_iters += numIter;
+        t_dav += now_s() - t1;
         break;
       }
     }
@@ -1081,7 +1175,8 @@ int shci_davidson(shci_ctx* ctx, int mode, int block, int nroots, double* x0, in
     SHCI_CUDA(cudaMemcpyAsync(x.p, x0, N * nroots * sizeof(double), cudaMemcpyHostToDevice, c.stream));
     std::vector<double> ev;
     int it = 0;
-    c.davidson(mode, block != 0, nroots, x.p, max_copies, tol, false, ev, it);
+    const double E_est = E[0];  // energy estimate for the shifted preconditioners (NaN: none)
+    c.davidson(mode, block != 0, nroots, x.p, max_copies, tol, false, ev, it, E_est);
     SHCI_CUDA(cudaMemcpyAsync(x0, x.p, N * nroots * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     SHCI_CUDA(cudaStreamSynchronize(c.stream));
     for (int r = 0; r < nroots; ++r) E[r] = ev[r];
@@ -1104,6 +1199,7 @@ int shci_run_input(shci_ctx* ctx, const char* input_path, const char* fcidump, i
     c.load_fcidump(fd);
     if (mode < 0) mode = s.mode >= 0 ? s.mode : SHCI_MODE_FP64;
     if (block < 0) block = s.block ? 1 : 0;
+    if (s.precond >= 0) c.precond = s.precond;
     std::vector<double> ev;
     c.run(s, mode, block != 0, ev);
     if (nroots) *nroots = (int)ev.size();
@@ -1142,6 +1238,105 @@ int shci_run_timings(shci_ctx* ctx, double* t_select, double* t_ham, double* t_d
     if (t_total) *t_total = c.t_total;
     if (n_sigma) *n_sigma = c.n_sigma;
     if (t_sigma) *t_sigma = c.t_sigma;
+  });
+}
+
+int shci_set_preconditioner(shci_ctx* ctx, int mode) {
+  return guarded(ctx, [&](Context& c) {
+    if (mode < 0 || mode > 2) throw Error(SHCI_ERR_INVALID, "preconditioner must be 0 (diagonal), 1 (PT2) or 2 (MLP)");
+    c.precond = mode;
+    c.shift_ready = false;
+  });
+}
+
+int shci_pt2_shift(shci_ctx* ctx, double E, double* out) {
+  return guarded(ctx, [&](Context& c) {
+    if (!c.ham_ok || c.ham_mode == SHCI_MODE_DIRECT) throw Error(SHCI_ERR_STATE, "no stored Hamiltonian");
+    c.ensure_diag();
+    c.teacher.resize(c.ndet);
+    shci::pt2_shift(c.H, c.diag.p, E, c.teacher.p, c.stream);
+    SHCI_CUDA(cudaMemcpyAsync(out, c.teacher.p, c.ndet * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    SHCI_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+
+int shci_mlp_configure(shci_ctx* ctx, int steps, int batch, float lr, int64_t sample_rows) {
+  return guarded(ctx, [&](Context& c) {
+    if (steps < 0 || batch < 1 || !(lr > 0.f) || sample_rows < 1) throw Error(SHCI_ERR_INVALID, "bad MLP settings");
+    c.mlp_steps = steps;
+    c.mlp_batch = batch;
+    c.mlp_lr = lr;
+    c.mlp_sample = sample_rows;
+  });
+}
+
+int shci_mlp_train(shci_ctx* ctx, double E, float* loss) {
+  return guarded(ctx, [&](Context& c) {
+    const double l = c.train_mlp(E);
+    if (loss) *loss = (float)l;
+  });
+}
+
+int shci_mlp_predict(shci_ctx* ctx, double E, double* out) {
+  return guarded(ctx, [&](Context& c) {
+    if (!c.mlp.trained && c.mlp.nparam == 0) throw Error(SHCI_ERR_STATE, "MLP not trained or loaded");
+    c.ensure_diag();
+    c.shift.resize(c.ndet);
+    c.mlp.infer(c.dets.p, c.diag.p, c.ndet, E, c.shift.p, c.stream);
+    SHCI_CUDA(cudaMemcpyAsync(out, c.shift.p, c.ndet * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    SHCI_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+
+int shci_mlp_params(shci_ctx* ctx, float* out, int cap, int* n, double* sigma) {
+  return guarded(ctx, [&](Context& c) {
+    c.require_ints();
+    if (c.mlp.nspin != 2 * c.hints.norb) c.mlp.init(2 * c.hints.norb, 7, c.stream);
+    if (n) *n = c.mlp.nparam;
+    if (sigma) *sigma = c.mlp.sigma;
+    if (out) {
+      if (cap < c.mlp.nparam) throw Error(SHCI_ERR_INVALID, "output buffer too small");
+      auto h = c.mlp.get_params(c.stream);
+      std::memcpy(out, h.data(), h.size() * sizeof(float));
+    }
+  });
+}
+
+int shci_mlp_set_params(shci_ctx* ctx, const float* in, int n, double sigma) {
+  return guarded(ctx, [&](Context& c) {
+    c.require_ints();
+    if (c.mlp.nspin != 2 * c.hints.norb) c.mlp.init(2 * c.hints.norb, 7, c.stream);
+    c.mlp.set_params(std::vector<float>(in, in + n), c.stream);
+    c.mlp.sigma = sigma;
+    c.mlp.trained = true;
+  });
+}
+
+int shci_mlp_gradient(shci_ctx* ctx, const int32_t* rows, const float* target, int B, double E, float* grad,
+                      float* loss) {
+  return guarded(ctx, [&](Context& c) {
+    c.require_dets();
+    c.ensure_diag();
+    if (c.mlp.nspin != 2 * c.hints.norb) c.mlp.init(2 * c.hints.norb, 7, c.stream);
+    for (int i = 0; i < B; ++i)
+      if (rows[i] < 0 || (size_t)rows[i] >= c.ndet) throw Error(SHCI_ERR_INVALID, "row index out of range");
+    c.tr_idx.resize(B);
+    c.tr_tgt.resize(B);
+    SHCI_CUDA(cudaMemcpyAsync(c.tr_idx.p, rows, B * sizeof(int32_t), cudaMemcpyHostToDevice, c.stream));
+    SHCI_CUDA(cudaMemcpyAsync(c.tr_tgt.p, target, B * sizeof(float), cudaMemcpyHostToDevice, c.stream));
+    const float l = c.mlp.gradient(c.dets.p, c.diag.p, c.tr_idx.p, c.tr_tgt.p, B, E, c.stream);
+    if (loss) *loss = l;
+    if (grad)
+      SHCI_CUDA(cudaMemcpyAsync(grad, c.mlp.grad.p, c.mlp.nparam * sizeof(float), cudaMemcpyDeviceToHost, c.stream));
+    SHCI_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+
+int shci_run_stats(shci_ctx* ctx, int64_t* davidson_iters, double* t_mlp, float* mlp_loss) {
+  return guarded(ctx, [&](Context& c) {
+    if (davidson_iters) *davidson_iters = c.total_dav_iters;
+    if (t_mlp) *t_mlp = c.t_mlp;
+    if (mlp_loss) *mlp_loss = (float)c.last_loss;
   });
 }
 

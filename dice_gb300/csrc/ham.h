@@ -138,6 +138,9 @@ void residual(const double* X, const double* Y, const double* lam, int k, size_t
               cudaStream_t s);
 // R[:, c] /= (lam[c] - diag) with the reference's 1e-12 guard
 void precondition(const double* diag, const double* lam, int k, size_t N, double* R, size_t ld, cudaStream_t s);
+// R[:, c] /= (lam[c] - diag - shift) where that is safe, else the plain denominator
+void precondition_shift(const double* diag, const double* shift, const double* lam, int k, size_t N, double* R,
+                        size_t ld, cudaStream_t s);
 // A[:, c] *= scale[c]
 void scale_cols(double* A, size_t ld, const double* scale, int k, size_t N, cudaStream_t s);
 

@@ -302,6 +302,16 @@ void read_input(const std::string& path, Schedule& s) {
         throw Error(kErrInvalid, "precision must be fp64 or mixed");
     } else if (iequal(arg, "blockdavidson")) {
       s.block = true;
+    } else if (iequal(arg, "precond")) {
+      need(1);
+      if (iequal(tok[1], "plain") || iequal(tok[1], "diagonal"))
+        s.precond = 0;
+      else if (iequal(tok[1], "pt2"))
+        s.precond = 1;
+      else if (iequal(tok[1], "mlp"))
+        s.precond = 2;
+      else
+        throw Error(kErrInvalid, "precond must be plain, pt2 or mlp");
     } else {
       bool ok = false;
       for (const char* k : kIgnored)

@@ -41,6 +41,7 @@ struct Schedule {
   std::string integralFile = "FCIDUMP";
   int mode = -1;       // precision keyword: -1 unset, 0 fp64, 1 mixed
   bool block = false;  // blockdavidson keyword
+  int precond = -1;    // precond keyword: -1 unset, 0 plain, 1 pt2, 2 mlp
 };
 
 void split_tokens(const std::string& in, const char* delims, std::vector<std::string>& tok);

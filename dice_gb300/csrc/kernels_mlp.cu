@@ -1,0 +1,344 @@
+// Learned correction of the Davidson preconditioner (no counterpart in the
+// reference, whose preconditioner is r_i / (theta - H_ii), SHCI/Davidson.cpp:85-106).
+//
+// The correction is a per-determinant shift s_i of the denominator,
+//   t_i = r_i / (theta - H_ii - s_i),
+// whose teacher is the second-order level shift of determinant i inside the
+// variational space, s_i = sum_j H_ij^2 / (E - H_jj) (computed from the stored
+// Hamiltonian at the Davidson energy E). A small MLP learns s_i from the
+// determinant itself:
+//   features: per spatial orbital "doubly occupied" and "singly occupied"
+//             (2n values, spin-free), (H_ii - E) / 10, and 1;
+//   net:      F -> 128 -> 128 -> 1, ReLU, weights stored in BF16,
+//             FP32 master weights and Adam moments;
+//   target:   s_i / sigma (sigma = RMS of the teacher shifts).
+// The forward, backward and Adam kernels below are the project's own; the
+// hidden activations are kept in FP32 inside the kernels.
+#include <cuda_bf16.h>
+
+#include "ham.h"
+#include "mlp.h"
+
+namespace shci {
+
+// ---------------------------------------------------------------------------
+// teacher: s_i = sum_j h_ij^2 / (E - d_j) over stored row i
+// ---------------------------------------------------------------------------
+template <bool F64>
+__global__ void k_pt2_shift(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                            const double* __restrict__ v64, const float* __restrict__ vhi,
+                            const double* __restrict__ diag, size_t N, double E, double* __restrict__ s) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < (int64_t)N; r += warps) {
+    double acc = 0.0;
+    for (int64_t p = rowptr[r] + lane; p < rowptr[r + 1]; p += 32) {
+      const int j = col[p];
+      const double h = F64 ? v64[p] : (double)vhi[p];
+      const double den = E - diag[j];
+      if (fabs(den) > 1e-8) acc += h * h / den;
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
+    if (lane == 0) s[r] = acc;
+  }
+}
+
+void pt2_shift(const Csr& H, const double* diag, double E, double* s, cudaStream_t st) {
+  if (H.N == 0) return;
+  size_t blocks = (H.N * 32 + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  if (H.v64.p)
+    k_pt2_shift<true><<<(unsigned)blocks, 256, 0, st>>>(H.rowptr.p, H.col.p, H.v64.p, nullptr, diag, H.N, E, s);
+  else
+    k_pt2_shift<false><<<(unsigned)blocks, 256, 0, st>>>(H.rowptr.p, H.col.p, nullptr, H.vhi.p, diag, H.N, E, s);
+  SHCI_LAUNCH_CHECK();
+}
+
+// ---------------------------------------------------------------------------
+// network
+// ---------------------------------------------------------------------------
+// Spin-free occupation features: f < n is "orbital f doubly occupied",
+// n <= f < 2n is "orbital f-n singly occupied". They are invariant under the
+// alpha <-> beta flip, so the predicted shift is too -- a flip-asymmetric
+// preconditioner would let a Davidson run leave the flip sector of its start
+// vector (see the note on compensated accumulation in kernels_sigma.cu).
+__device__ __forceinline__ float feature(const Det2& d, int f, int nspin, float dscaled) {
+  const int n = nspin >> 1;
+  if (f < n) return (det_getocc(d, 2 * f) && det_getocc(d, 2 * f + 1)) ? 1.f : 0.f;
+  if (f < nspin) return (det_getocc(d, 2 * (f - n)) != det_getocc(d, 2 * (f - n) + 1)) ? 1.f : 0.f;
+  if (f == nspin) return dscaled;
+  if (f == nspin + 1) return 1.f;
+  return 0.f;
+}
+
+// Shared-memory layout of one block (kHidden threads, one per hidden unit).
+struct MlpSmem {
+  __nv_bfloat16* W1;  // kHidden x F (row j = unit j)
+  __nv_bfloat16* W2;  // kHidden x kHidden
+  float* x;           // F
+  float* h1;          // kHidden
+  float* h2;          // kHidden
+  float* red;         // kHidden / 32 partial sums
+};
+
+__device__ __forceinline__ MlpSmem carve(unsigned char* base, int F) {
+  MlpSmem m;
+  m.W1 = reinterpret_cast<__nv_bfloat16*>(base);
+  m.W2 = m.W1 + (size_t)kHidden * F;
+  float* f = reinterpret_cast<float*>(m.W2 + (size_t)kHidden * kHidden);
+  m.x = f;
+  m.h1 = m.x + F;
+  m.h2 = m.h1 + kHidden;
+  m.red = m.h2 + kHidden;
+  return m;
+}
+size_t mlp_fwd_smem(int F) {
+  return (size_t)kHidden * F * 2 + (size_t)kHidden * kHidden * 2 + ((size_t)F + 2 * kHidden + kHidden / 32) * 4;
+}
+
+__device__ __forceinline__ void load_weights(const MlpView& w, MlpSmem& m, int F) {
+  for (int i = threadIdx.x; i < kHidden * F; i += blockDim.x) m.W1[i] = w.W1b[i];
+  for (int i = threadIdx.x; i < kHidden * kHidden; i += blockDim.x) m.W2[i] = w.W2b[i];
+  __syncthreads();
+}
+
+// forward of one sample by the block; returns the output in every thread
+__device__ __forceinline__ float forward_one(const MlpView& w, MlpSmem& m, int F) {
+  const int j = threadIdx.x;
+  float a = w.b1[j];
+  for (int f = 0; f < F; ++f) a += __bfloat162float(m.W1[(size_t)j * F + f]) * m.x[f];
+  m.h1[j] = fmaxf(a, 0.f);
+  __syncthreads();
+  float b = w.b2[j];
+  for (int k = 0; k < kHidden; ++k) b += __bfloat162float(m.W2[(size_t)j * kHidden + k]) * m.h1[k];
+  const float h2 = fmaxf(b, 0.f);
+  m.h2[j] = h2;
+  float o = w.w3[j] * h2;
+#pragma unroll
+  for (int s = 16; s; s >>= 1) o += __shfl_xor_sync(kFull, o, s);
+  if ((j & 31) == 0) m.red[j >> 5] = o;
+  __syncthreads();
+  float out = w.b3[0];
+  for (int q = 0; q < kHidden / 32; ++q) out += m.red[q];
+  __syncthreads();
+  return out;
+}
+
+__global__ void __launch_bounds__(kHidden) k_mlp_infer(MlpView w, const Det2* __restrict__ dets,
+                                                       const double* __restrict__ diag, size_t N, double E,
+                                                       double sigma, double* __restrict__ out) {
+  extern __shared__ unsigned char sm_raw[];
+  const int F = w.F, nspin = w.nspin;
+  MlpSmem m = carve(sm_raw, F);
+  load_weights(w, m, F);
+  for (size_t i = blockIdx.x; i < N; i += gridDim.x) {
+    const Det2 d = dets[i];
+    const float ds = (float)((diag[i] - E) * 0.1);
+    for (int f = threadIdx.x; f < F; f += blockDim.x) m.x[f] = feature(d, f, nspin, ds);
+    __syncthreads();
+    const float o = forward_one(w, m, F);
+    if (threadIdx.x == 0) out[i] = (double)o * sigma;
+  }
+}
+
+// Gradients of the mean squared error over a batch. Every block keeps its own
+// FP32 gradient in shared memory (thread j owns row j of dW1 and dW2) and
+// writes it to its slice of `part`; k_mlp_grad_sum adds the slices in block
+// order, so the result does not depend on scheduling.
+__global__ void __launch_bounds__(kHidden) k_mlp_grad(MlpView w, const Det2* __restrict__ dets,
+                                                      const double* __restrict__ diag, const int32_t* __restrict__ idx,
+                                                      const float* __restrict__ target, int B, double E,
+                                                      float* __restrict__ part, float* __restrict__ loss_part) {
+  extern __shared__ unsigned char sm_raw[];
+  const int F = w.F, nspin = w.nspin, j = threadIdx.x;
+  MlpSmem m = carve(sm_raw, F);
+  float* gW1 = reinterpret_cast<float*>(m.red + kHidden / 32);  // kHidden x F
+  float* gW2 = gW1 + (size_t)kHidden * F;                        // kHidden x kHidden
+  float* dh2 = gW2 + (size_t)kHidden * kHidden;                  // kHidden
+  load_weights(w, m, F);
+  for (int f = 0; f < F; ++f) gW1[(size_t)j * F + f] = 0.f;
+  for (int k = 0; k < kHidden; ++k) gW2[(size_t)j * kHidden + k] = 0.f;
+  float gb1 = 0.f, gb2 = 0.f, gw3 = 0.f, gb3 = 0.f, loss = 0.f;
+  __syncthreads();
+  const float inv = 2.f / (float)B;
+  for (int s = blockIdx.x; s < B; s += gridDim.x) {
+    const int i = idx[s];
+    const Det2 d = dets[i];
+    const float ds = (float)((diag[i] - E) * 0.1);
+    for (int f = threadIdx.x; f < F; f += blockDim.x) m.x[f] = feature(d, f, nspin, ds);
+    __syncthreads();
+    const float o = forward_one(w, m, F);
+    const float err = o - target[s];
+    loss += (j == 0) ? err * err / (float)B : 0.f;
+    const float dout = inv * err;
+    gb3 += (j == 0) ? dout : 0.f;
+    const float h2 = m.h2[j];
+    gw3 += dout * h2;
+    const float g2 = (h2 > 0.f) ? dout * w.w3[j] : 0.f;
+    dh2[j] = g2;
+    gb2 += g2;
+    for (int k = 0; k < kHidden; ++k) gW2[(size_t)j * kHidden + k] += g2 * m.h1[k];
+    __syncthreads();
+    // dh1[j] = sum_k dh2[k] W2[k][j]
+    float g1 = 0.f;
+    for (int k = 0; k < kHidden; ++k) g1 += dh2[k] * __bfloat162float(m.W2[(size_t)k * kHidden + j]);
+    g1 = (m.h1[j] > 0.f) ? g1 : 0.f;
+    gb1 += g1;
+    for (int f = 0; f < F; ++f) gW1[(size_t)j * F + f] += g1 * m.x[f];
+    __syncthreads();
+  }
+  float* mypart = part + (size_t)blockIdx.x * w.nparam;
+  for (int f = 0; f < F; ++f) mypart[w.offW1 + (size_t)j * F + f] = gW1[(size_t)j * F + f];
+  for (int k = 0; k < kHidden; ++k) mypart[w.offW2 + (size_t)j * kHidden + k] = gW2[(size_t)j * kHidden + k];
+  mypart[w.offb1 + j] = gb1;
+  mypart[w.offb2 + j] = gb2;
+  mypart[w.offw3 + j] = gw3;
+  if (j == 0) {
+    mypart[w.offb3] = gb3;
+    loss_part[blockIdx.x] = loss;
+  }
+}
+size_t mlp_grad_smem(int F) {
+  return mlp_fwd_smem(F) + ((size_t)kHidden * F + (size_t)kHidden * kHidden + kHidden) * 4;
+}
+
+__global__ void k_mlp_grad_sum(const float* __restrict__ part, int nblocks, int nparam, float* __restrict__ g) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nparam; i += gridDim.x * blockDim.x) {
+    float s = 0.f;
+    for (int b = 0; b < nblocks; ++b) s += part[(size_t)b * nparam + i];
+    g[i] = s;
+  }
+}
+
+// Adam on the FP32 master weights; refreshes the BF16 copies used by the kernels.
+__global__ void k_adam(float* __restrict__ p, float* __restrict__ mo, float* __restrict__ ve,
+                       const float* __restrict__ g, int n, float lr, float b1, float b2, float eps, float c1, float c2,
+                       __nv_bfloat16* __restrict__ pb, int nb) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float m = b1 * mo[i] + (1.f - b1) * gi;
+    const float v = b2 * ve[i] + (1.f - b2) * gi * gi;
+    mo[i] = m;
+    ve[i] = v;
+    const float np = p[i] - lr * (m / c1) / (sqrtf(v / c2) + eps);
+    p[i] = np;
+    if (i < nb) pb[i] = __float2bfloat16_rn(np);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+void Mlp::init(int nspin_, uint64_t seed, cudaStream_t s) {
+  nspin = nspin_;
+  F = nspin + 2;
+  offW1 = 0;
+  offW2 = offW1 + kHidden * F;
+  offb1 = offW2 + kHidden * kHidden;
+  offb2 = offb1 + kHidden;
+  offw3 = offb2 + kHidden;
+  offb3 = offw3 + kHidden;
+  nparam = offb3 + 1;
+  std::vector<float> h(nparam, 0.f);
+  uint64_t st = seed * 0x9E3779B97F4A7C15ull + 12345;
+  auto rnd = [&]() {
+    st ^= st << 13;
+    st ^= st >> 7;
+    st ^= st << 17;
+    return (float)(((st >> 11) * (1.0 / 9007199254740992.0)) * 2.0 - 1.0);
+  };
+  const float a1 = std::sqrt(6.f / (float)(F + kHidden)), a2 = std::sqrt(6.f / (2.f * kHidden));
+  for (int i = 0; i < kHidden * F; ++i) h[offW1 + i] = a1 * rnd();
+  for (int i = 0; i < kHidden * kHidden; ++i) h[offW2 + i] = a2 * rnd();
+  for (int i = 0; i < kHidden; ++i) h[offw3 + i] = a2 * rnd();
+  set_params(h, s);
+  step = 0;
+  sigma = 1.0;
+  trained = false;
+}
+
+void Mlp::set_params(const std::vector<float>& h, cudaStream_t s) {
+  if ((int)h.size() != nparam) throw Error(kErrInvalid, "MLP parameter count mismatch");
+  params.resize(nparam);
+  mom.resize(nparam);
+  var.resize(nparam);
+  grad.resize(nparam);
+  wb.resize((size_t)offb1);  // BF16 copies of W1 and W2 (contiguous at the start)
+  SHCI_CUDA(cudaMemcpyAsync(params.p, h.data(), nparam * sizeof(float), cudaMemcpyHostToDevice, s));
+  SHCI_CUDA(cudaMemsetAsync(mom.p, 0, nparam * sizeof(float), s));
+  SHCI_CUDA(cudaMemsetAsync(var.p, 0, nparam * sizeof(float), s));
+  std::vector<__nv_bfloat16> b(offb1);
+  for (int i = 0; i < offb1; ++i) b[i] = __float2bfloat16_rn(h[i]);
+  SHCI_CUDA(cudaMemcpyAsync(wb.p, b.data(), offb1 * sizeof(__nv_bfloat16), cudaMemcpyHostToDevice, s));
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  step = 0;
+}
+
+std::vector<float> Mlp::get_params(cudaStream_t s) const {
+  std::vector<float> h(nparam);
+  SHCI_CUDA(cudaMemcpyAsync(h.data(), params.p, nparam * sizeof(float), cudaMemcpyDeviceToHost, s));
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  return h;
+}
+
+MlpView Mlp::view() const {
+  MlpView v;
+  v.F = F;
+  v.nspin = nspin;
+  v.W1b = wb.p + offW1;
+  v.W2b = wb.p + offW2;
+  v.b1 = params.p + offb1;
+  v.b2 = params.p + offb2;
+  v.w3 = params.p + offw3;
+  v.b3 = params.p + offb3;
+  v.nparam = nparam;
+  v.offW1 = offW1;
+  v.offW2 = offW2;
+  v.offb1 = offb1;
+  v.offb2 = offb2;
+  v.offw3 = offw3;
+  v.offb3 = offb3;
+  return v;
+}
+
+constexpr int kGradBlocks = 64;
+
+float Mlp::gradient(const Det2* dets, const double* diag, const int32_t* idx, const float* target, int B, double E,
+                    cudaStream_t s) {
+  const size_t smem = mlp_grad_smem(F);
+  SHCI_CUDA(cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int nb = std::min(kGradBlocks, std::max(1, B));
+  part.reserve((size_t)nb * nparam);
+  lpart.reserve(nb);
+  k_mlp_grad<<<nb, kHidden, smem, s>>>(view(), dets, diag, idx, target, B, E, part.p, lpart.p);
+  SHCI_LAUNCH_CHECK();
+  k_mlp_grad_sum<<<(nparam + 255) / 256, 256, 0, s>>>(part.p, nb, nparam, grad.p);
+  SHCI_LAUNCH_CHECK();
+  std::vector<float> lp(nb);
+  SHCI_CUDA(cudaMemcpyAsync(lp.data(), lpart.p, nb * sizeof(float), cudaMemcpyDeviceToHost, s));
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  float loss = 0.f;
+  for (float v : lp) loss += v;
+  return loss;
+}
+
+void Mlp::adam(float lr, cudaStream_t s) {
+  ++step;
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float c1 = 1.f - std::pow(b1, (float)step), c2 = 1.f - std::pow(b2, (float)step);
+  k_adam<<<(nparam + 255) / 256, 256, 0, s>>>(params.p, mom.p, var.p, grad.p, nparam, lr, b1, b2, 1e-8f, c1, c2,
+                                             wb.p, offb1);
+  SHCI_LAUNCH_CHECK();
+}
+
+void Mlp::infer(const Det2* dets, const double* diag, size_t N, double E, double* out, cudaStream_t s) const {
+  if (N == 0) return;
+  const size_t smem = mlp_fwd_smem(F);
+  SHCI_CUDA(cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const unsigned blocks = (unsigned)std::min<size_t>(N, 152 * 8);
+  k_mlp_infer<<<blocks, kHidden, smem, s>>>(view(), dets, diag, N, E, sigma, out);
+  SHCI_LAUNCH_CHECK();
+}
+
+}  // namespace shci

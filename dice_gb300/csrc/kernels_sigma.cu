@@ -409,6 +409,32 @@ void precondition(const double* diag, const double* lam, int k, size_t N, double
   SHCI_LAUNCH_CHECK();
 }
 
+// Shifted preconditioner r_i / (lam - diag_i - shift_i). The plain denominator
+// is kept wherever the shifted one changes sign or shrinks below a fifth of it
+// (a shift that would blow the correction up), so the learned or second-order
+// shift can only refine the reference's denominator, never replace it wholesale.
+__global__ void k_precondition_shift(const double* __restrict__ diag, const double* __restrict__ shift,
+                                     const double* __restrict__ lam, int k, size_t N, double* __restrict__ R,
+                                     size_t ld) {
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < N; r += (size_t)gridDim.x * blockDim.x)
+    for (int c = 0; c < k; ++c) {
+      const double e = lam[c], d = diag[r];
+      double den = e - d;
+      const double d2 = den - shift[r];
+      if ((d2 > 0) == (den > 0) && fabs(d2) > 0.2 * fabs(den)) den = d2;
+      double* p = R + (size_t)c * ld + r;
+      if (fabs(den) > 1e-12)
+        *p = *p / den;
+      else
+        *p = *p / (den - 1.e-12);
+    }
+}
+void precondition_shift(const double* diag, const double* shift, const double* lam, int k, size_t N, double* R,
+                        size_t ld, cudaStream_t s) {
+  k_precondition_shift<<<grid_for(N, 256), 256, 0, s>>>(diag, shift, lam, k, N, R, ld);
+  SHCI_LAUNCH_CHECK();
+}
+
 __global__ void k_scale_cols(double* __restrict__ A, size_t ld, const double* __restrict__ sc, int k, size_t N) {
   for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < N; r += (size_t)gridDim.x * blockDim.x)
     for (int c = 0; c < k; ++c) A[(size_t)c * ld + r] *= sc[c];

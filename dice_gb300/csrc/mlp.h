@@ -1,0 +1,45 @@
+// Learned preconditioner correction (kernels_mlp.cu).
+#pragma once
+#include <cuda_bf16.h>
+
+#include "ham.h"
+
+namespace shci {
+
+constexpr int kHidden = 128;
+
+struct MlpView {
+  int F, nspin;
+  const __nv_bfloat16* W1b;  // kHidden x F
+  const __nv_bfloat16* W2b;  // kHidden x kHidden
+  const float *b1, *b2, *w3, *b3;
+  int nparam, offW1, offW2, offb1, offb2, offw3, offb3;
+};
+
+// Second-order level shift of every row of the stored Hamiltonian at energy E:
+// s_i = sum_j H_ij^2 / (E - diag_j).
+void pt2_shift(const Csr& H, const double* diag, double E, double* s, cudaStream_t st);
+
+struct Mlp {
+  int nspin = 0, F = 0, nparam = 0;
+  int offW1 = 0, offW2 = 0, offb1 = 0, offb2 = 0, offw3 = 0, offb3 = 0;
+  int step = 0;
+  double sigma = 1.0;  // target scale: prediction = output * sigma
+  bool trained = false;
+  DevBuf<float> params, mom, var, grad, part, lpart;
+  DevBuf<__nv_bfloat16> wb;
+
+  void init(int nspin, uint64_t seed, cudaStream_t s);
+  void set_params(const std::vector<float>& h, cudaStream_t s);
+  std::vector<float> get_params(cudaStream_t s) const;
+  MlpView view() const;
+  // mean squared error of the batch (rows idx, targets already divided by
+  // sigma) and its gradient into `grad`
+  float gradient(const Det2* dets, const double* diag, const int32_t* idx, const float* target, int B, double E,
+                 cudaStream_t s);
+  void adam(float lr, cudaStream_t s);
+  // out[i] = sigma * net(features of det i)
+  void infer(const Det2* dets, const double* diag, size_t N, double E, double* out, cudaStream_t s) const;
+};
+
+}  // namespace shci

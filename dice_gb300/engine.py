@@ -47,6 +47,15 @@ SIGNATURES = [
     ("shci_run_log", _i32, [_vp, _i32, _P(_i32), _vp, _vp, _vp, _vp]),
     ("shci_run_ci", _i32, [_vp, _vp, _i64]),
     ("shci_run_timings", _i32, [_vp, _P(_dbl), _P(_dbl), _P(_dbl), _P(_dbl), _P(_i64), _P(_dbl)]),
+    ("shci_set_preconditioner", _i32, [_vp, _i32]),
+    ("shci_pt2_shift", _i32, [_vp, _dbl, _vp]),
+    ("shci_mlp_configure", _i32, [_vp, _i32, _i32, ctypes.c_float, _i64]),
+    ("shci_mlp_train", _i32, [_vp, _dbl, _P(ctypes.c_float)]),
+    ("shci_mlp_predict", _i32, [_vp, _dbl, _vp]),
+    ("shci_mlp_params", _i32, [_vp, _vp, _i32, _P(_i32), _P(_dbl)]),
+    ("shci_mlp_set_params", _i32, [_vp, _vp, _i32, _dbl]),
+    ("shci_mlp_gradient", _i32, [_vp, _vp, _vp, _i32, _dbl, _vp, _P(ctypes.c_float)]),
+    ("shci_run_stats", _i32, [_vp, _P(_i64), _P(_dbl), _P(ctypes.c_float)]),
     ("shci_launch_count", _i32, [_vp, _P(_i64)]),
 ]
 
@@ -214,10 +223,11 @@ class Engine:
         self._check(load_library().shci_ham_bytes(self.h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
 
-    def davidson(self, x0, mode="fp64", block=False, max_copies=None, tol=5e-5):
+    def davidson(self, x0, mode="fp64", block=False, max_copies=None, tol=5e-5, e_est=float("nan")):
+        """e_est: energy estimate for the shifted preconditioners (NaN: none)."""
         x = np.ascontiguousarray(x0, dtype=np.float64).reshape(-1, self.ndets()).copy()
         nroots = x.shape[0]
-        E = np.zeros(nroots)
+        E = np.full(nroots, float(e_est))
         it = ctypes.c_int()
         mc = max_copies if max_copies is not None else nroots + 4
         self._check(load_library().shci_davidson(self.h, MODES.get(mode, mode), int(block), nroots, _p(x), mc,
@@ -265,6 +275,56 @@ class Engine:
         out["n_sigma"] = ns.value
         out["sigma"] = ts.value
         return out
+
+    PRECOND = {"plain": 0, "pt2": 1, "mlp": 2}
+
+    def set_preconditioner(self, mode):
+        self._check(load_library().shci_set_preconditioner(self.h, self.PRECOND.get(mode, mode)))
+
+    def pt2_shift(self, E):
+        out = np.zeros(self.ndets())
+        self._check(load_library().shci_pt2_shift(self.h, float(E), _p(out)))
+        return out
+
+    def mlp_configure(self, steps=200, batch=4096, lr=1e-3, sample_rows=200000):
+        self._check(load_library().shci_mlp_configure(self.h, steps, batch, lr, sample_rows))
+
+    def mlp_train(self, E):
+        loss = ctypes.c_float()
+        self._check(load_library().shci_mlp_train(self.h, float(E), ctypes.byref(loss)))
+        return loss.value
+
+    def mlp_predict(self, E):
+        out = np.zeros(self.ndets())
+        self._check(load_library().shci_mlp_predict(self.h, float(E), _p(out)))
+        return out
+
+    def mlp_params(self):
+        L = load_library()
+        n, sig = ctypes.c_int(), ctypes.c_double()
+        self._check(L.shci_mlp_params(self.h, None, 0, ctypes.byref(n), ctypes.byref(sig)))
+        out = np.zeros(n.value, np.float32)
+        self._check(L.shci_mlp_params(self.h, _p(out), n.value, ctypes.byref(n), ctypes.byref(sig)))
+        return out, sig.value
+
+    def mlp_set_params(self, params, sigma=1.0):
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        self._check(load_library().shci_mlp_set_params(self.h, _p(p), len(p), float(sigma)))
+
+    def mlp_gradient(self, rows, target, E):
+        rows = np.ascontiguousarray(rows, dtype=np.int32)
+        target = np.ascontiguousarray(target, dtype=np.float32)
+        n = len(self.mlp_params()[0])
+        grad = np.zeros(n, np.float32)
+        loss = ctypes.c_float()
+        self._check(load_library().shci_mlp_gradient(self.h, _p(rows), _p(target), len(rows), float(E), _p(grad),
+                                                     ctypes.byref(loss)))
+        return loss.value, grad
+
+    def run_stats(self):
+        it, tm, loss = ctypes.c_int64(), ctypes.c_double(), ctypes.c_float()
+        self._check(load_library().shci_run_stats(self.h, ctypes.byref(it), ctypes.byref(tm), ctypes.byref(loss)))
+        return {"davidson_iters": it.value, "t_mlp": tm.value, "mlp_loss": loss.value}
 
     def launch_count(self):
         n = ctypes.c_int64()

@@ -150,7 +150,9 @@ int shci_ham_bytes(shci_ctx* ctx, int64_t* csr_bytes, int64_t* helper_bytes);
  * block: 0 = one correction vector per iteration for the lowest unconverged
  * root (the reference's scheme), 1 = one per unconverged root in a single
  * k-vector sigma launch. max_copies: subspace size (reference: nroots+4).
- * E[nroots] receives eigenvalues (coreE excluded); *iters the iteration count. */
+ * E[nroots] receives eigenvalues (coreE excluded); *iters the iteration count.
+ * On entry E[0] is an energy estimate used by the shifted preconditioners
+ * (shci_set_preconditioner 1 or 2); NaN means none (diagonal preconditioner). */
 int shci_davidson(shci_ctx* ctx, int mode, int block, int nroots, double* x0, int max_copies, double tol, double* E,
                   int* iters);
 
@@ -171,6 +173,38 @@ int shci_run_ci(shci_ctx* ctx, double* out, int64_t cap);
  * Davidson, total; and the sigma calls/time spent inside Davidson. */
 int shci_run_timings(shci_ctx* ctx, double* t_select, double* t_ham, double* t_davidson, double* t_total,
                      int64_t* n_sigma, double* t_sigma);
+
+/* Davidson preconditioner (replaces precondition, SHCI/Davidson.cpp:85-106):
+ * 0 = the reference's r_i / (theta - H_ii) (default);
+ * 1 = denominator shifted by the second-order level shift
+ *     s_i = sum_j H_ij^2 / (E - H_jj) of the stored Hamiltonian;
+ * 2 = shift predicted by the learned MLP (no counterpart in the reference):
+ *     in shci_run_input the network is trained after every loose Davidson
+ *     solve on the (determinant, s_i) pairs of that solve and used from the
+ *     next solve on. The plain denominator is kept wherever a shift would flip
+ *     its sign or shrink it below a fifth, and convergence is still judged on
+ *     the unpreconditioned residual, so eigenvalues do not change. */
+int shci_set_preconditioner(shci_ctx* ctx, int mode);
+/* Second-order level shifts of the current space at energy E (host out[N]). */
+int shci_pt2_shift(shci_ctx* ctx, double E, double* out);
+/* MLP training settings: Adam steps per training call, minibatch, learning
+ * rate, rows sampled from the space. */
+int shci_mlp_configure(shci_ctx* ctx, int steps, int batch, float lr, int64_t sample_rows);
+/* Train on the current space's level shifts at energy E; final minibatch loss. */
+int shci_mlp_train(shci_ctx* ctx, double E, float* loss);
+/* Predicted shifts for every determinant of the current space (host out[N]). */
+int shci_mlp_predict(shci_ctx* ctx, double E, double* out);
+/* FP32 master parameters (W1 128xF row-major, W2 128x128, b1, b2, w3, b3;
+ * F = 2 NORB + 2) and the target scale; out may be NULL to query *n. */
+int shci_mlp_params(shci_ctx* ctx, float* out, int cap, int* n, double* sigma);
+int shci_mlp_set_params(shci_ctx* ctx, const float* in, int n, double sigma);
+/* Mean squared error and its gradient (FP32, same layout as the parameters)
+ * for the given rows of the current space and scaled targets. */
+int shci_mlp_gradient(shci_ctx* ctx, const int32_t* rows, const float* target, int B, double E, float* grad,
+                      float* loss);
+/* Totals of the last shci_run_input: Davidson iterations, seconds spent
+ * training the MLP, last training loss. */
+int shci_run_stats(shci_ctx* ctx, int64_t* davidson_iters, double* t_mlp, float* mlp_loss);
 
 /* Kernel launches issued by this context since creation (own kernels only). */
 int shci_launch_count(shci_ctx* ctx, int64_t* n);
