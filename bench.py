@@ -33,6 +33,11 @@ sys.path.insert(0, ROOT)
 
 WORKLOAD = "mol24"
 CPU_SAMPLE_DETS = 100000
+# DRAM bytes per mixed-sigma launch divided by its algorithmic bytes, from one
+# ncu capture of the medium case (6.007 GB measured / 5.915 GB algorithmic);
+# the full-size launch is too large to capture, and its traffic scales with
+# the nonzeros it streams.
+TRAFFIC_RATIO = 6.007 / 5.915
 
 
 def dist_info():
@@ -174,12 +179,22 @@ def run_ours(args):
     inp = make_inputs(work, args.case)
     e = eng.Engine(local)
 
-    # whole variational stage, plain FP64 path then mixed path
+    # whole variational stage: mixed + learned preconditioner, plain FP64 path
+    # (the reference's algorithm), then the mixed path whose final space the
+    # sigma steps below run on
+    e.set_preconditioner("mlp")
+    Eml = e.run_input(inp, mode="mixed")
+    tml = e.timings()
+    sml = e.run_stats()
+    logml = e.run_log()
+    e.set_preconditioner("plain")
     E64 = e.run_input(inp, mode="fp64")
     t64 = e.timings()
+    s64 = e.run_stats()
     log64 = e.run_log()
     E32 = e.run_input(inp, mode="mixed")
     t32 = e.timings()
+    s32 = e.run_stats()
     log32 = e.run_log()
     N = e.ndets()
     dets_mixed = e.dets()
@@ -189,11 +204,11 @@ def run_ours(args):
     rng = np.random.default_rng(5)
     x_host = rng.standard_normal(N)
 
-    def timed_sigma(mode, packed, nsteps, nwarm):
+    def timed_sigma(mode, packed, nsteps, nwarm, kp=1):
         nnz = e.ham_build(mode)
-        y = torch.zeros(N, dtype=torch.float64, device="cuda")
+        y = torch.zeros(kp * N, dtype=torch.float64, device="cuda")
         for _ in range(nwarm):
-            e.sigma_packed_device(packed.data_ptr(), 1, k, y.data_ptr(), N, mode=mode)
+            e.sigma_packed_device(packed.data_ptr(), kp, kp, y.data_ptr(), N, mode=mode)
         torch.cuda.synchronize()
         csr_bytes, _ = e.ham_bytes()
         flush = None
@@ -210,7 +225,7 @@ def run_ours(args):
             a = torch.cuda.Event(enable_timing=True)
             b = torch.cuda.Event(enable_timing=True)
             a.record(stream)
-            e.sigma_packed_device(packed.data_ptr(), 1, k, y.data_ptr(), N, mode=mode)
+            e.sigma_packed_device(packed.data_ptr(), kp, kp, y.data_ptr(), N, mode=mode)
             b.record(stream)
             b.synchronize()
             ts.append(a.elapsed_time(b) * 1e-3)
@@ -238,6 +253,11 @@ def run_ours(args):
         t_max = tt.item()
     value = world * k * N / t_max / 1e6
     sig_err = float((y32 - y64).abs().max() / y64.abs().max())
+    # block sigma: k = 4 vectors per pass (the block-Davidson launch)
+    x4 = torch.tensor(rng.standard_normal((N, 4)), device="cuda").float().contiguous()
+    _, ts4, _, _, _ = timed_sigma("mixed", x4, max(3, args.steps // 2), args.warmup, kp=4)
+    t4 = statistics.mean(ts4)
+    alg4 = nnz * 8 + 8 * (N + 1) + 8 * N + 4 * N * 4 + 4 * N * 8
 
     # end to end through the C-ABI with host buffers
     for _ in range(2):
@@ -279,17 +299,27 @@ def run_ours(args):
         "e2e": {"value": e2e, "unit": "Mdets/s", "h2d_bytes_per_step": N * k * 8, "d2h_bytes_per_step": N * k * 8},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "peak_kind": peak_kind, "alg_bytes_per_launch": alg_bytes},
+                     "traffic": alg_bytes * TRAFFIC_RATIO, "traffic_note": "scaled from the medium-case ncu capture",
+                     "peak_kind": peak_kind, "alg_bytes_per_launch": alg_bytes},
         "plain_fp64_sigma": {"mdets_s": k * N / statistics.mean(ts64) / 1e6, "achieved_gbs": ach64,
                              "frac": ach64 / peak, "nnz": nnz64},
         "mixed_vs_fp64_sigma_speedup": statistics.mean(ts64) / t_max,
+        "block_k4_sigma": {"mdets_s": 4 * N / t4 / 1e6, "ms": t4 * 1e3, "achieved_gbs": alg4 / t4 / 1e9,
+                           "frac": alg4 / t4 / 1e9 / peak},
         "sigma_rel_err_fp32_vs_fp64": sig_err,
-        "var": {"mixed": {"wall_s": t32["total"], "E_var": float(E32[0]), "stages_s": t32,
+        "var": {"mixed_mlp": {"wall_s": tml["total"], "E_var": float(Eml[0]), "stages_s": tml,
+                              "davidson_iters_total": sml["davidson_iters"], "mlp_train_s": sml["t_mlp"],
+                              "ndets": [int(v) for v in logml["ndets"]]},
+                "mixed": {"wall_s": t32["total"], "E_var": float(E32[0]), "stages_s": t32,
+                          "davidson_iters_total": s32["davidson_iters"],
                           "ndets": [int(v) for v in log32["ndets"]], "davidson_iters": [int(v) for v in log32["davidson"]]},
                 "fp64": {"wall_s": t64["total"], "E_var": float(E64[0]), "stages_s": t64,
+                         "davidson_iters_total": s64["davidson_iters"],
                          "ndets": [int(v) for v in log64["ndets"]], "davidson_iters": [int(v) for v in log64["davidson"]]},
                 "dE_mixed_minus_fp64": float(E32[0] - E64[0]),
-                "wall_speedup_mixed_vs_fp64": t64["total"] / t32["total"]},
+                "wall_speedup_mixed_vs_fp64": t64["total"] / t32["total"],
+                "dE_mixed_mlp_minus_fp64": float(Eml[0] - E64[0]),
+                "wall_speedup_mixed_mlp_vs_fp64": t64["total"] / tml["total"]},
         "clocks": clk, "timed_wall_s": wall,
     }
     if cpu:

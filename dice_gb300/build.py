@@ -41,9 +41,11 @@ def _headers_mtime():
 def _compile(src):
     path = os.path.join(CSRC, src)
     obj = os.path.join(OBJ, src + ".o")
-    if os.path.exists(obj) and os.path.getmtime(obj) > max(os.path.getmtime(path), _headers_mtime()):
+    if os.path.exists(obj) and os.path.getmtime(obj) > max(os.path.getmtime(path), _headers_mtime()) \
+            and not os.environ.get("SHCI_NVCC_FLAGS"):
         return obj
     common = ["-O3", "-std=c++17", "-I", os.path.join(ROOT, "include"), "-I", CSRC]
+    common += os.environ.get("SHCI_NVCC_FLAGS", "").split()  # extra flags for experiments
     if src.endswith(".cu"):
         cmd = [nvcc()] + ARCH + common + ["-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
                                           "-Xptxas", "-O3", "-c", path, "-o", obj]

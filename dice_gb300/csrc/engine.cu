@@ -180,6 +180,7 @@ struct Context {
   DevBuf<int32_t> flipidx;
   DevBuf<int8_t> flipsgn;
   int flip_state = -1;
+  bool last_stalled = false;  // the last FP32 Davidson stage stopped at its rounding floor
 
   // preconditioner: 0 the reference's diagonal, 1 diagonal + second-order
   // level shift from the stored H, 2 diagonal + shift predicted by the MLP
@@ -189,8 +190,8 @@ struct Context {
   bool shift_ready = false;
   DevBuf<int32_t> tr_idx;
   DevBuf<float> tr_tgt;
-  int mlp_steps = 200, mlp_batch = 4096;
-  float mlp_lr = 1e-3f;
+  int mlp_steps = 60, mlp_batch = 4096;
+  float mlp_lr = 2e-3f;
   int64_t mlp_sample = 200000;
   double last_loss = 0.0;
 
@@ -476,6 +477,7 @@ struct Context {
     // arithmetic would keep them in (see the note on compensated accumulation
     // in kernels_sigma.cu); FP64 sigma keeps it to rounding by itself.
     const bool sym = stall_exit && ensure_flip();
+    last_stalled = false;
     if (nroots < 1) throw Error(kErrInvalid, "nroots must be >= 1");
     if ((size_t)nroots > N) throw Error(kErrInvalid, "more roots than determinants");
     int mmax = std::max(maxCopies, nroots + 1);
@@ -579,6 +581,7 @@ struct Context {
           best_resid = worst;
           stall = 0;
         } else if (worst < kStallWindow && ++stall >= 8) {
+          last_stalled = true;
           finish();
           return;
         }
@@ -752,7 +755,10 @@ struct Context {
       // recomputed in FP64 (head + tail values)
       int it1 = 0, it2 = 0, m = 0;
       davidson_core(SHCI_MODE_MIXED, block, nroots, x, maxCopies, tol, direct_rules, E, it1, true, 0, &m);
-      davidson_core(SHCI_MODE_FP64, block, nroots, x, maxCopies, tol, direct_rules, E, it2, false, m);
+      // converged in FP32: one FP64 sigma of the Ritz vectors usually confirms
+      // it; stopped at the FP32 floor: keep the whole basis for the FP64 stage
+      davidson_core(SHCI_MODE_FP64, block, nroots, x, maxCopies, tol, direct_rules, E, it2, false,
+                    last_stalled ? m : 0);
       iters = it1 + it2;
     } else {
       davidson_core(mode, block, nroots, x, maxCopies, tol, direct_rules, E, iters);

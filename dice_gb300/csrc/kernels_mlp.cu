@@ -302,7 +302,7 @@ MlpView Mlp::view() const {
   return v;
 }
 
-constexpr int kGradBlocks = 64;
+constexpr int kGradBlocks = 152 * 2;
 
 float Mlp::gradient(const Det2* dets, const double* diag, const int32_t* idx, const float* target, int B, double E,
                     cudaStream_t s) {
