@@ -185,6 +185,10 @@ struct Context {
   // preconditioner: 0 the reference's diagonal, 1 diagonal + second-order
   // level shift from the stored H, 2 diagonal + shift predicted by the MLP
   int precond = 0;
+  // Davidson subspace: 0 = the reference's (nroots+4 vectors, collapsed to
+  // nroots+2 Ritz vectors); otherwise at most basis_max vectors, collapsed to
+  // basis_keep (shci_set_davidson_basis)
+  int basis_max = 0, basis_keep = 0;
   Mlp mlp;
   DevBuf<double> shift, teacher;
   bool shift_ready = false;
@@ -667,7 +671,8 @@ struct Context {
         return;
       }
       if (m + kept > mmax) {
-        int keep = block ? mmax - kept : std::min(nroots + 2, mmax - kept);
+        int keep = basis_keep > 0 ? std::min(basis_keep, mmax - kept)
+                   : (block ? mmax - kept : std::min(nroots + 2, mmax - kept));
         if (keep < nroots) keep = nroots;
         ts_gemm(V.p, N, m, dQ.p, keep, N, 1.0, 0.0, Vt.p, N, stream);
         ts_gemm(W.p, N, m, dQ.p, keep, N, 1.0, 0.0, Wt.p, N, stream);
@@ -877,7 +882,8 @@ struct Context {
       t_ham += tc - tb;
       const double prevE0 = (iter == 0) ? -10.0 : E0[0];
       int numIter = 0;
-      const int maxCopies = block ? std::max(nroots + 4, 3 * nroots) : (s.direct ? nroots + 2 : nroots + 4);
+      const int maxCopies = basis_max > 0 ? basis_max
+                            : (block ? std::max(nroots + 4, 3 * nroots) : (s.direct ? nroots + 2 : nroots + 4));
       // the shifted preconditioners need an energy: the previous iteration's
       const double E_est = iter == 0 ? std::nan("") : E0[0];
       davidson(mode, block, nroots, X0.p, maxCopies, s.davidsonTolLoose, s.direct, E0, numIter, E_est);
@@ -892,7 +898,8 @@ struct Context {
       }
       if (std::fabs(E0[0] - prevE0) < s.dE || iter == s.epsilon1.size() - 1) {
         const double t1 = now_s();
-        davidson(mode, block, nroots, ci.p, block ? std::max(nroots + 4, 3 * nroots) : nroots + 4, s.davidsonTol,
+        davidson(mode, block, nroots, ci.p,
+                 basis_max > 0 ? basis_max : (block ? std::max(nroots + 4, 3 * nroots) : nroots + 4), s.davidsonTol,
                  s.direct, E0, numIter, E0[0]);
         total_dav_iters += numIter;
         t_dav += now_s() - t1;
@@ -993,6 +1000,63 @@ int shci_read_fcidump(shci_ctx* ctx, const char* path, int* norb, int* nelec, do
     if (nelec) *nelec = c.hints.nelec;
     if (coreE) *coreE = c.hints.coreE;
   });
+}
+
+int shci_fcidump_info(const char* path, int* norb, int* nelec, double* coreE, int64_t* nnz_i2) {
+  try {
+    g_create_error.clear();
+    if (!path) throw Error(SHCI_ERR_INVALID, "null path");
+    shci::HostInts H;
+    shci::read_fcidump(path, H);
+    if (norb) *norb = H.norb;
+    if (nelec) *nelec = H.nelec;
+    if (coreE) *coreE = H.coreE;
+    if (nnz_i2) {
+      int64_t n = 0;
+      for (double v : H.I2) n += v != 0.0;
+      *nnz_i2 = n;
+    }
+    return SHCI_OK;
+  } catch (const Error& e) {
+    g_create_error = e.what();
+    return e.code;
+  } catch (const std::exception& e) {
+    g_create_error = e.what();
+    return SHCI_ERR_INVALID;
+  }
+}
+
+int shci_input_info(const char* path, double* eps1, int cap_eps, int* n_eps, double* tols, int* ints) {
+  try {
+    g_create_error.clear();
+    if (!path) throw Error(SHCI_ERR_INVALID, "null path");
+    shci::Schedule s;
+    shci::read_input(path, s);
+    if (n_eps) *n_eps = (int)s.epsilon1.size();
+    for (int i = 0; eps1 && i < cap_eps && i < (int)s.epsilon1.size(); ++i) eps1[i] = s.epsilon1[i];
+    if (tols) {
+      tols[0] = s.davidsonTol;
+      tols[1] = s.davidsonTolLoose;
+      tols[2] = s.dE;
+    }
+    if (ints) {
+      ints[0] = s.nroots;
+      ints[1] = (int)s.occupied.size();
+      ints[2] = s.ncore;
+      ints[3] = s.nact;
+      ints[4] = s.mode;
+      ints[5] = s.block ? 1 : 0;
+      ints[6] = s.precond;
+      ints[7] = s.basis_max;
+    }
+    return SHCI_OK;
+  } catch (const Error& e) {
+    g_create_error = e.what();
+    return e.code;
+  } catch (const std::exception& e) {
+    g_create_error = e.what();
+    return SHCI_ERR_INVALID;
+  }
 }
 
 int shci_heatbath_export(shci_ctx* ctx, int which, int64_t* count, float* vals, int16_t* pairs, int64_t* starts,
@@ -1206,6 +1270,10 @@ int shci_run_input(shci_ctx* ctx, const char* input_path, const char* fcidump, i
     if (mode < 0) mode = s.mode >= 0 ? s.mode : SHCI_MODE_FP64;
     if (block < 0) block = s.block ? 1 : 0;
     if (s.precond >= 0) c.precond = s.precond;
+    if (s.basis_max > 0) {
+      c.basis_max = s.basis_max;
+      c.basis_keep = s.basis_keep;
+    }
     std::vector<double> ev;
     c.run(s, mode, block != 0, ev);
     if (nroots) *nroots = (int)ev.size();
@@ -1252,6 +1320,19 @@ int shci_set_preconditioner(shci_ctx* ctx, int mode) {
     if (mode < 0 || mode > 2) throw Error(SHCI_ERR_INVALID, "preconditioner must be 0 (diagonal), 1 (PT2) or 2 (MLP)");
     c.precond = mode;
     c.shift_ready = false;
+  });
+}
+
+int shci_set_davidson_basis(shci_ctx* ctx, int max_basis, int keep) {
+  return guarded(ctx, [&](Context& c) {
+    if (max_basis == 0 && keep == 0) {
+      c.basis_max = c.basis_keep = 0;
+      return;
+    }
+    if (max_basis < 3 || max_basis > 16) throw Error(SHCI_ERR_INVALID, "max_basis must be 0 or in 3..16");
+    if (keep < 1 || keep >= max_basis) throw Error(SHCI_ERR_INVALID, "keep must be in 1..max_basis-1");
+    c.basis_max = max_basis;
+    c.basis_keep = keep;
   });
 }
 

@@ -312,6 +312,12 @@ void read_input(const std::string& path, Schedule& s) {
         s.precond = 2;
       else
         throw Error(kErrInvalid, "precond must be plain, pt2 or mlp");
+    } else if (iequal(arg, "davidsonBasis")) {
+      need(2);
+      s.basis_max = std::atoi(tok[1].c_str());
+      s.basis_keep = std::atoi(tok[2].c_str());
+      if (s.basis_max < 3 || s.basis_max > 16 || s.basis_keep < 1 || s.basis_keep >= s.basis_max)
+        throw Error(kErrInvalid, "davidsonBasis needs max in 3..16 and keep in 1..max-1");
     } else {
       bool ok = false;
       for (const char* k : kIgnored)

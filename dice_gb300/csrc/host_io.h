@@ -42,6 +42,7 @@ struct Schedule {
   int mode = -1;       // precision keyword: -1 unset, 0 fp64, 1 mixed
   bool block = false;  // blockdavidson keyword
   int precond = -1;    // precond keyword: -1 unset, 0 plain, 1 pt2, 2 mlp
+  int basis_max = 0, basis_keep = 0;  // davidsonBasis keyword: 0 = the reference's subspace
 };
 
 void split_tokens(const std::string& in, const char* delims, std::vector<std::string>& tok);

@@ -6,12 +6,18 @@
 //     (replaces MakeHfromSMHelpers2, SHCI/SHCImakeHamiltonian.cpp:486-715);
 //   * the matrix-free sigma (replaces HmultDirect::operator(), SHCI/Hmult.h:241-381).
 //
-// One warp owns one row I. The connected determinants J are found in three
-// scans over string groups:
-//   1. determinants sharing I's alpha string: beta distance 1 or 2;
-//   2. determinants whose alpha string is a single excitation of I's and whose
-//      beta string equals I's or is one excitation away;
-//   3. determinants sharing I's beta string: alpha distance 2.
+// One warp owns one row I = (A, B). The connected determinants J are found in
+// three parts:
+//   1. determinants sharing I's alpha string: beta distance 1 or 2 (scan of
+//      the alpha group);
+//   2. determinants whose alpha string As is a single excitation of A and
+//      whose beta string equals B or is one excitation away. Every such J
+//      contains the partial string B - b for some occupied b of B, so it is
+//      found by looking up the keys (As, B - b) in the partial-string index:
+//      |singles(A)| x |B| probes that return (nearly) only connections,
+//      instead of a scan over every determinant of every group As;
+//   3. determinants sharing I's beta string: alpha distance 2 (scan of the
+//      beta group).
 // This visits the same (I, J) set as the reference's five helper-list classes
 // (single alpha, alpha-beta, single beta, double beta, double alpha).
 #include <algorithm>
@@ -146,6 +152,57 @@ static void build_groups(const uint64_t* str_of_det, const uint64_t* partner_of_
   (void)str_of_det;
 }
 
+// Key of a partial string: alpha group g with the beta string bpart (one
+// electron removed). A splitmix64-style mix; lookups verify every candidate,
+// so a collision costs a wasted probe, never a wrong connection.
+__device__ __forceinline__ uint64_t partial_key(uint32_t g, uint64_t bpart) {
+  uint64_t z = bpart + 0x9E3779B97F4A7C15ull * ((uint64_t)g + 1ull);
+  z ^= z >> 30;
+  z *= 0xBF58476D1CE4E5B9ull;
+  z ^= z >> 27;
+  z *= 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return z;
+}
+
+__global__ void k_m1_count(const uint64_t* __restrict__ bstr, size_t n, int64_t* __restrict__ cnt) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    cnt[i] = __popcll(bstr[i]);
+}
+__global__ void k_m1_fill(const uint64_t* __restrict__ bstr, const uint32_t* __restrict__ aidx, size_t n,
+                          const int64_t* __restrict__ off, uint64_t* __restrict__ key, uint32_t* __restrict__ det) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const uint64_t B = bstr[i];
+    const uint32_t g = aidx[i];
+    int64_t q = off[i];
+    for (uint64_t r = B; r; r &= r - 1) {
+      const uint64_t bit = r & (~r + 1ull);
+      key[q] = partial_key(g, B ^ bit);
+      det[q] = (uint32_t)i;
+      ++q;
+    }
+  }
+}
+// dir[p] = first entry whose key's top `bits` bits are >= p, p in [0, 2^bits]
+__global__ void k_m1_dir(const uint64_t* __restrict__ key, int64_t n, int bits, uint32_t* __restrict__ dir) {
+  const int64_t nb = (int64_t)1 << bits;
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p <= nb; p += (int64_t)gridDim.x * blockDim.x) {
+    int64_t lo = 0, hi = n;
+    if (p == nb) {
+      lo = n;
+    } else {
+      while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if ((int64_t)(key[mid] >> (64 - bits)) < p)
+          lo = mid + 1;
+        else
+          hi = mid;
+      }
+    }
+    dir[p] = (uint32_t)lo;
+  }
+}
+
 void Helpers::build(const Det2* dets, size_t n, int norb, Prims& pr, cudaStream_t s) {
   N = n;
   astr.resize(n);
@@ -174,6 +231,31 @@ void Helpers::build(const Det2* dets, size_t n, int norb, Prims& pr, cudaStream_
                                                                          aSing.p);
   SHCI_LAUNCH_CHECK();
   nsing = total;
+  // partial-string index (one entry per determinant and occupied beta orbital)
+  {
+    DevBuf<int64_t> c1, o1;
+    c1.resize(n);
+    o1.resize(n + 1);
+    k_m1_count<<<grid_for(n, 256), 256, 0, s>>>(bstr.p, n, c1.p);
+    SHCI_LAUNCH_CHECK();
+    int64_t ne = 0;
+    scan_exclusive_i64(c1.p, o1.p, n, &ne, pr, s);
+    if (ne >= ((int64_t)1 << 32)) throw Error(kErrInvalid, "partial-string index too large");
+    nm1 = ne;
+    if (ne > 0) {
+      m1key.resize(ne);
+      m1det.resize(ne);
+      k_m1_fill<<<grid_for(n, 256), 256, 0, s>>>(bstr.p, aidx.p, n, o1.p, m1key.p, m1det.p);
+      SHCI_LAUNCH_CHECK();
+      sort_u64(m1key.p, m1det.p, (size_t)ne, pr, s);
+      int bits = 4;
+      while (bits < 28 && ((int64_t)1 << bits) < ne) ++bits;  // about one entry per bucket
+      m1bits = bits;
+      m1dir.resize(((size_t)1 << bits) + 1);
+      k_m1_dir<<<grid_for(((size_t)1 << bits) + 1, 256), 256, 0, s>>>(m1key.p, ne, bits, m1dir.p);
+      SHCI_LAUNCH_CHECK();
+    }
+  }
   SHCI_CUDA(cudaStreamSynchronize(s));
 }
 
@@ -202,8 +284,78 @@ __device__ void visit_row(const HelperView& h, uint32_t I, V& v) {
       v.step(hit, J, d == 2);
     }
   }
-  // 2. alpha single excitation: beta equal (single alpha) or beta single (alpha-beta double)
-  {
+  // 2. alpha single excitation: beta equal (single alpha) or beta single
+  // (alpha-beta double), from the partial-string index
+  if (h.m1key != nullptr && B != 0) {
+    const int64_t s0 = h.aSingStart[ia], s1 = h.aSingStart[ia + 1];
+    const int nb = __popcll(B);
+    const int64_t nprobe = (s1 - s0) * nb;
+    const int shift = 64 - h.m1bits;
+    for (int64_t base = 0; base < nprobe; base += 32) {
+      const int64_t t = base + lane;
+      // each lane locates the entries of its key (As, B - b)
+      int64_t lo = 0, len = 0;
+      uint32_t As = 0;
+      uint64_t Bm = 0;
+      bool first_b = false;
+      if (t < nprobe) {
+        As = h.aSing[s0 + t / nb];
+        const int which = (int)(t % nb);
+        uint64_t r = B;
+        for (int k = 0; k < which; ++k) r &= r - 1;
+        Bm = B ^ (r & (~r + 1ull));
+        first_b = which == 0;
+        const uint64_t key = partial_key(As, Bm);
+        const uint32_t p = (uint32_t)(key >> shift);
+        uint32_t e = h.m1dir[p];
+        const uint32_t e1 = h.m1dir[p + 1];
+        while (e < e1 && h.m1key[e] < key) ++e;
+        uint32_t f = e;
+        while (f < e1 && h.m1key[f] == key) ++f;
+        lo = e;
+        len = f - e;
+      }
+      // flatten the lanes' matches and verify them 32 at a time
+      int64_t incl = len;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        int64_t y = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += y;
+      }
+      const int64_t total = __shfl_sync(kFull, incl, 31);
+      const int64_t excl = incl - len;
+      for (int64_t f0 = 0; f0 < total; f0 += 32) {
+        const int64_t f = f0 + lane;
+        int src = 0;
+#pragma unroll
+        for (int st = 16; st >= 1; st >>= 1) {
+          const int c = src + st;
+          const int64_t e = __shfl_sync(kFull, excl, c < 32 ? c : 31);
+          if (c < 32 && e <= f) src = c;
+        }
+        const int64_t elo = __shfl_sync(kFull, lo, src);
+        const int64_t eo = __shfl_sync(kFull, excl, src);
+        const uint32_t as = __shfl_sync(kFull, As, src);
+        const uint64_t bm = __shfl_sync(kFull, Bm, src);
+        const bool fb = __shfl_sync(kFull, first_b, src);
+        bool hit = false, single = false;
+        uint32_t J = 0;
+        if (f < total) {
+          J = h.m1det[elo + (f - eo)];
+          if (h.aidx[J] == as) {
+            const uint64_t BJ = h.bstr[J];
+            if ((BJ & bm) == bm) {
+              const int d = __popcll(BJ ^ B);
+              // beta equal: found once per occupied b, kept for the first
+              single = d == 0;
+              hit = single ? fb : d == 2;
+            }
+          }
+        }
+        v.step(hit, J, single);
+      }
+    }
+  } else {  // no index (or no beta electrons): scan every group As
     const int64_t s0 = h.aSingStart[ia], s1 = h.aSingStart[ia + 1];
     for (int64_t base = s0; base < s1; base += 32) {
       int64_t q = base + lane;

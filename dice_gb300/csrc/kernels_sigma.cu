@@ -297,41 +297,96 @@ void unpack_f64(const double* in, int kp, int k, size_t N, double* A, size_t lda
 }
 
 // ---------------------------------------------------------------------------
-// Tall-skinny Gram: G = A^T B. Blocks own contiguous row ranges; each block
-// stages 32-row tiles in shared memory and thread t accumulates pair t.
-// A second kernel adds the per-block partials in block order.
+// Tall-skinny Gram: G = A^T B. Blocks own contiguous row ranges and write
+// one partial per block; a second kernel adds the partials in block order, so
+// the result does not depend on scheduling.
+// Narrow products (ma * mb <= 16: norms, dots, residual norms) keep every
+// pair's sum in registers and stream the rows with independent loads; wider
+// ones (the Rayleigh matrix) stage 64-row tiles in shared memory with all
+// threads of the block splitting the rows of a tile between them.
 // ---------------------------------------------------------------------------
 constexpr int kGramMax = 16;
-constexpr int kGramRows = 32;
+constexpr int kGramRows = 64;
 constexpr unsigned kGramBlocks = 152 * 2;
+constexpr int kGramRegPairs = 16;
+
+__device__ inline void block_sum_pairs(double* acc, int P, double* __restrict__ out) {
+  __shared__ double red[8][kGramRegPairs];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int p = 0; p < kGramRegPairs; ++p) {
+    if (p >= P) break;
+    double v = acc[p];
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+    if (lane == 0) red[w][p] = v;
+  }
+  __syncthreads();
+  if ((int)threadIdx.x < P) {
+    double v = 0.0;
+    for (int ww = 0; ww < (int)(blockDim.x >> 5); ++ww) v += red[ww][threadIdx.x];
+    out[threadIdx.x] = v;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_gram_reg(const double* __restrict__ A, size_t lda, int ma,
+                                                  const double* __restrict__ B, size_t ldb, int mb, size_t N,
+                                                  double* __restrict__ part) {
+  double acc[kGramRegPairs];
+#pragma unroll
+  for (int p = 0; p < kGramRegPairs; ++p) acc[p] = 0.0;
+  const int P = ma * mb;
+  const size_t per = (N + gridDim.x - 1) / gridDim.x;
+  const size_t r0 = (size_t)blockIdx.x * per;
+  const size_t r1 = r0 + per < N ? r0 + per : N;
+  // repeated loads of one row's entries hit L1; only distinct ones reach L2
+  for (size_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+#pragma unroll
+    for (int p = 0; p < kGramRegPairs; ++p)
+      if (p < P) acc[p] += A[(size_t)(p % ma) * lda + r] * B[(size_t)(p / ma) * ldb + r];
+  }
+  block_sum_pairs(acc, P, part + (size_t)blockIdx.x * P);
+}
 
 __global__ void __launch_bounds__(256) k_gram_part(const double* __restrict__ A, size_t lda, int ma,
                                                    const double* __restrict__ B, size_t ldb, int mb, size_t N,
                                                    double* __restrict__ part) {
   __shared__ double sA[kGramMax][kGramRows + 1];
   __shared__ double sB[kGramMax][kGramRows + 1];
+  __shared__ double red[256];
   const int t = threadIdx.x;
   const int P = ma * mb;
-  const int pi = t % ma, pj = t / ma;
+  const int S = 256 / P;  // threads per pair, splitting the rows of a tile
+  const int pp = t % P, q = t / P;
+  const int pi = pp % ma, pj = pp / ma;
+  const bool active = q < S;
   double acc = 0.0;
   const size_t per = (N + gridDim.x - 1) / gridDim.x;
   const size_t r0 = (size_t)blockIdx.x * per;
   const size_t r1 = r0 + per < N ? r0 + per : N;
   for (size_t base = r0; base < r1; base += kGramRows) {
-    for (int e = t; e < kGramMax * kGramRows; e += blockDim.x) {
-      int c = e / kGramRows, rr = e % kGramRows;
-      size_t row = base + rr;
-      sA[c][rr] = (c < ma && row < r1) ? A[(size_t)c * lda + row] : 0.0;
-      sB[c][rr] = (c < mb && row < r1) ? B[(size_t)c * ldb + row] : 0.0;
+    for (int e = t; e < ma * kGramRows; e += blockDim.x) {
+      const int c = e / kGramRows, rr = e % kGramRows;
+      const size_t row = base + rr;
+      sA[c][rr] = row < r1 ? A[(size_t)c * lda + row] : 0.0;
+    }
+    for (int e = t; e < mb * kGramRows; e += blockDim.x) {
+      const int c = e / kGramRows, rr = e % kGramRows;
+      const size_t row = base + rr;
+      sB[c][rr] = row < r1 ? B[(size_t)c * ldb + row] : 0.0;
     }
     __syncthreads();
-    if (t < P) {
-#pragma unroll 8
-      for (int rr = 0; rr < kGramRows; ++rr) acc += sA[pi][rr] * sB[pj][rr];
-    }
+    if (active)
+      for (int rr = q; rr < kGramRows; rr += S) acc += sA[pi][rr] * sB[pj][rr];
     __syncthreads();
   }
-  if (t < P) part[(size_t)blockIdx.x * P + t] = acc;
+  red[t] = active ? acc : 0.0;
+  __syncthreads();
+  if (t < P) {
+    double v = 0.0;
+    for (int k = 0; k < S; ++k) v += red[t + k * P];
+    part[(size_t)blockIdx.x * P + t] = v;
+  }
 }
 
 __global__ void k_gram_sum(const double* __restrict__ part, int nblocks, int P, double* __restrict__ G) {
@@ -345,12 +400,15 @@ __global__ void k_gram_sum(const double* __restrict__ part, int nblocks, int P, 
 
 void ts_gram(const double* A, size_t lda, int ma, const double* B, size_t ldb, int mb, size_t N, double* G,
              DevBuf<double>& part, cudaStream_t s) {
-  if (ma > kGramMax || mb > kGramMax || ma * mb > 256) throw Error(kErrInvalid, "Gram block too wide");
+  if (ma < 1 || mb < 1 || ma > kGramMax || mb > kGramMax) throw Error(kErrInvalid, "Gram block too wide");
   unsigned nb = kGramBlocks;
   if ((size_t)nb * kGramRows > N) nb = (unsigned)((N + kGramRows - 1) / kGramRows);
   if (nb < 1) nb = 1;
   part.reserve((size_t)nb * ma * mb);
-  k_gram_part<<<nb, 256, 0, s>>>(A, lda, ma, B, ldb, mb, N, part.p);
+  if (ma * mb <= kGramRegPairs)
+    k_gram_reg<<<nb, 256, 0, s>>>(A, lda, ma, B, ldb, mb, N, part.p);
+  else
+    k_gram_part<<<nb, 256, 0, s>>>(A, lda, ma, B, ldb, mb, N, part.p);
   SHCI_LAUNCH_CHECK();
   k_gram_sum<<<1, 256, 0, s>>>(part.p, (int)nb, ma * mb, G);
   SHCI_LAUNCH_CHECK();

@@ -48,6 +48,9 @@ SIGNATURES = [
     ("shci_run_ci", _i32, [_vp, _vp, _i64]),
     ("shci_run_timings", _i32, [_vp, _P(_dbl), _P(_dbl), _P(_dbl), _P(_dbl), _P(_i64), _P(_dbl)]),
     ("shci_set_preconditioner", _i32, [_vp, _i32]),
+    ("shci_set_davidson_basis", _i32, [_vp, _i32, _i32]),
+    ("shci_fcidump_info", _i32, [ctypes.c_char_p, _P(_i32), _P(_i32), _P(_dbl), _P(_i64)]),
+    ("shci_input_info", _i32, [ctypes.c_char_p, _vp, _i32, _P(_i32), _vp, _vp]),
     ("shci_pt2_shift", _i32, [_vp, _dbl, _vp]),
     ("shci_mlp_configure", _i32, [_vp, _i32, _i32, ctypes.c_float, _i64]),
     ("shci_mlp_train", _i32, [_vp, _dbl, _P(ctypes.c_float)]),
@@ -86,6 +89,36 @@ class ShciError(RuntimeError):
 
 def _p(a):
     return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _host_check(rc):
+    if rc:
+        raise ShciError(rc, load_library().shci_last_error(None).decode())
+
+
+def fcidump_info(path):
+    """Parse an FCIDUMP on the host only (no device): (norb, nelec, coreE,
+    number of distinct nonzero two-electron integrals)."""
+    norb, nelec, n2 = _i32(), _i32(), _i64()
+    core = _dbl()
+    _host_check(load_library().shci_fcidump_info(str(path).encode(), ctypes.byref(norb), ctypes.byref(nelec),
+                                                 ctypes.byref(core), ctypes.byref(n2)))
+    return norb.value, nelec.value, core.value, n2.value
+
+
+def input_info(path):
+    """Parse a Dice input file on the host only (no device): the expanded
+    eps1 schedule and the variational settings, as a dict."""
+    n = _i32()
+    tols = np.zeros(3)
+    ints = np.zeros(8, np.int32)
+    _host_check(load_library().shci_input_info(str(path).encode(), None, 0, ctypes.byref(n), _p(tols), _p(ints)))
+    eps = np.zeros(max(n.value, 1))
+    _host_check(load_library().shci_input_info(str(path).encode(), _p(eps), n.value, ctypes.byref(n), None, None))
+    keys = ("nroots", "ndet", "ncore", "nact", "precision", "blockdavidson", "precond", "davidson_basis")
+    out = {k: int(v) for k, v in zip(keys, ints)}
+    out.update(eps1=list(eps[:n.value]), davidsonTol=tols[0], davidsonTolLoose=tols[1], dE=tols[2])
+    return out
 
 
 class Engine:
@@ -280,6 +313,11 @@ class Engine:
 
     def set_preconditioner(self, mode):
         self._check(load_library().shci_set_preconditioner(self.h, self.PRECOND.get(mode, mode)))
+
+    def set_davidson_basis(self, max_basis=0, keep=0):
+        """Subspace of every Davidson solve of run_input: at most max_basis
+        vectors, collapsed to keep; (0, 0) is the reference's rule."""
+        self._check(load_library().shci_set_davidson_basis(self.h, int(max_basis), int(keep)))
 
     def pt2_shift(self, E):
         out = np.zeros(self.ndets())

@@ -60,6 +60,21 @@ int shci_set_alloc_cap(shci_ctx* ctx, uint64_t bytes);
  * twoIntHeatBathSHM::constructClass (SHCI/integral.h:125-153,
  * SHCI/integral.cpp:228-389). Builds the heat-bath tables as well. */
 int shci_read_fcidump(shci_ctx* ctx, const char* path, int* norb, int* nelec, double* coreE);
+
+/* Host-only parsers (no context, no device): the same readers the context
+ * calls, for drivers that validate their inputs before touching a GPU. On
+ * failure the message is in shci_last_error(NULL).
+ * shci_fcidump_info: readIntegrals' header and body checks
+ * (SHCI/integral.cpp:43-225); *nnz_i2 receives the number of distinct
+ * nonzero two-electron integrals (up to the 8-fold permutational symmetry). */
+int shci_fcidump_info(const char* path, int* norb, int* nelec, double* coreE, int64_t* nnz_i2);
+/* shci_input_info: readInput for the variational keys (SHCI/input.cpp:35-404).
+ * eps1[cap_eps] receives the expanded eps1 schedule (one entry per variational
+ * iteration), *n_eps its length; tols[3] = davidsonTol, davidsonTolLoose, dE;
+ * ints[8] = nroots, ndet (nocc lines), ncore, nact, precision (-1 unset,
+ * 0 fp64, 1 mixed), blockdavidson, precond (-1 unset, 0 plain, 1 pt2, 2 mlp),
+ * davidsonBasis max (0 = the reference's subspace). Any pointer may be NULL. */
+int shci_input_info(const char* path, double* eps1, int cap_eps, int* n_eps, double* tols, int* ints);
 /* Heat-bath table sizes and contents (for parity checks). which: 1 = same
  * spin, 0 = opposite spin. Arrays may be NULL. starts has n(n+1)/2+1 entries,
  * pairs 2 per entry, singles (2n)^2. */
@@ -185,6 +200,14 @@ int shci_run_timings(shci_ctx* ctx, double* t_select, double* t_ham, double* t_d
  *     its sign or shrink it below a fifth, and convergence is still judged on
  *     the unpreconditioned residual, so eigenvalues do not change. */
 int shci_set_preconditioner(shci_ctx* ctx, int mode);
+/* Davidson subspace size (no counterpart in the reference, whose subspace is
+ * nroots+4 vectors collapsed to nroots+2 Ritz vectors, SHCI/SHCIbasics.cpp:1171,
+ * SHCI/Davidson.cpp:325-345): at most max_basis (3..16) vectors, collapsed to
+ * the keep lowest Ritz vectors. Used by shci_run_input for every solve;
+ * (0, 0) restores the reference's rule. A larger subspace keeps more of the
+ * Krylov space across restarts and needs fewer iterations to the same
+ * tolerance; it changes no converged eigenvalue. */
+int shci_set_davidson_basis(shci_ctx* ctx, int max_basis, int keep);
 /* Second-order level shifts of the current space at energy E (host out[N]). */
 int shci_pt2_shift(shci_ctx* ctx, double E, double* out);
 /* MLP training settings: Adam steps per training call, minibatch, learning
