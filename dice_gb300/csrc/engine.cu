@@ -6,7 +6,11 @@
 // iteration forms G = V^T W (one fused Gram pass), solves the small symmetric
 // eigenproblem on the host in FP64, forms Ritz vectors X = V Q, HX = W Q and
 // residuals R = HX - lambda X on the device, and appends preconditioned,
-// orthogonalised corrections. The basis is only rotated on collapse; the
+// orthogonalised corrections. An iteration is two CUDA graphs, captured once
+// per basis size and active-root set and replayed after that: (1) Ritz
+// vectors, residuals and their norms; (2) corrections, orthonormalisation,
+// collapse, append, sigma and the next Gram matrix. The host reads back only
+// the small matrices (two synchronisations per iteration). The basis is only rotated on collapse; the
 // subspace sequence is the reference's (same maxCopies, same collapse to the
 // lowest nroots+2 Ritz vectors, corrections orthogonalised against the whole
 // basis before the collapse). Block mode adds one correction per unconverged
@@ -24,6 +28,7 @@
 #include <cstring>
 #include <memory>
 #include <numeric>
+#include <unordered_map>
 
 #include "../../include/shci_gpu.h"
 #include "ham.h"
@@ -208,7 +213,57 @@ struct Context {
   int64_t n_sigma = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
+  // captured Davidson iterations: graph per (phase, basis size, active roots)
+  bool use_graphs = true;
+  bool sigma_deferred = false;  // apply_sigma inside a capture: timing read later
+  std::unordered_map<uint64_t, std::pair<cudaGraphExec_t, int64_t>> gcache;
+  double* pin = nullptr;  // pinned staging for the small matrices (kPin doubles)
+  static constexpr int kPinQ = 0, kPinLam = 256, kPinAct = 272, kPinRR = 288, kPinG = 544, kPinNrm = 800,
+                       kPin = 816;
+  DevBuf<double> dactlam, drr, dnrm, dpar;
+
+  void graphs_clear() {
+    for (auto& kv : gcache) cudaGraphExecDestroy(kv.second.first);
+    gcache.clear();
+  }
+  // Run body() on the stream: captured into a graph the first time `key` is
+  // seen in this solve, replayed from then on. body() must not synchronise,
+  // read device results on the host or allocate.
+  template <class F>
+  void launch_body(uint64_t key, F&& body) {
+    if (!use_graphs) {
+      body();
+      return;
+    }
+    auto it = gcache.find(key);
+    if (it == gcache.end()) {
+      const int64_t l0 = g_launch_count.load();
+      SHCI_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+      try {
+        body();
+      } catch (...) {
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(stream, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+      }
+      cudaGraph_t g = nullptr;
+      SHCI_CUDA(cudaStreamEndCapture(stream, &g));
+      cudaGraphExec_t ex = nullptr;
+      const cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
+      cudaGraphDestroy(g);
+      SHCI_CUDA(e);
+      const int64_t nk = g_launch_count.load() - l0;
+      g_launch_count.fetch_sub(nk);  // counted once per replay below
+      it = gcache.emplace(key, std::make_pair(ex, nk)).first;
+    }
+    SHCI_CUDA(cudaGraphLaunch(it->second.first, stream));
+    g_launch_count.fetch_add(it->second.second);
+  }
+
   ~Context() {
+    graphs_clear();
+    if (pin) cudaFreeHost(pin);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (stream) cudaStreamDestroy(stream);
@@ -395,7 +450,9 @@ struct Context {
     if (mode == SHCI_MODE_MIXED && ham_mode != SHCI_MODE_MIXED)
       throw Error(kErrState, "mixed sigma needs a Hamiltonian built in mixed mode");
     const size_t N = ndet;
-    SHCI_CUDA(cudaEventRecord(ev0, stream));
+    // inside a capture the records must be external to become graph nodes
+    const unsigned evflag = sigma_deferred ? cudaEventRecordExternal : 0u;
+    SHCI_CUDA(cudaEventRecordWithFlags(ev0, stream, evflag));
     for (int done = 0; done < k;) {
       const int kk = std::min(4, k - done);
       const int kp = kk == 3 ? 4 : kk;
@@ -416,7 +473,8 @@ struct Context {
       }
       done += kk;
     }
-    SHCI_CUDA(cudaEventRecord(ev1, stream));
+    SHCI_CUDA(cudaEventRecordWithFlags(ev1, stream, evflag));
+    if (sigma_deferred) return;  // captured: the caller reads the events after the replay
     SHCI_CUDA(cudaEventSynchronize(ev1));
     float ms = 0.f;
     SHCI_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
@@ -477,6 +535,8 @@ struct Context {
                      std::vector<double>& E, int& numIter, bool stall_exit = false, int resume_m = 0,
                      int* basis_m = nullptr) {
     const size_t N = ndet;
+    const double t_enter = now_s();
+    double t_g1 = 0.0, t_g2 = 0.0, t_loop0 = 0.0, sig0 = t_sigma;
     // FP32 stage: hold the iterates in the alpha <-> beta flip sector that exact
     // arithmetic would keep them in (see the note on compensated accumulation
     // in kernels_sigma.cu); FP64 sigma keeps it to rounding by itself.
@@ -536,22 +596,51 @@ struct Context {
     std::vector<double> lam, Q;
     double best_resid = 1e300;
     int stall = 0, stall_root = 0;
+    // everything the captured bodies touch is allocated before the first capture
+    graphs_clear();
+    dG.reserve(256);
+    dQ.reserve(256);
+    dlam.reserve(16);
+    dactlam.reserve(16);
+    drr.reserve(256);
+    dnrm.reserve(16);
+    dpar.reserve(16);
+    dsmall.reserve(16);
+    gpart.reserve(256 * 304 + 2 * 304);
+    if (mode == SHCI_MODE_MIXED) xb32.reserve(N * 4);
+    if (mode == SHCI_MODE_FP64) xb64.reserve(N * 4);
+    if (mode == SHCI_MODE_DIRECT) {
+      xb64.reserve(N * 4);
+      yb64.reserve(N * 4);
+    }
+    if (sym) ftmp.reserve(N);
+    const double* shiftp = (shift_ready && shift.n >= N) ? shift.p : nullptr;
+    std::vector<double> G = gram_host(V.p, N, m, W.p, N, m);
+    t_loop0 = now_s();
     while (true) {
-      // Rayleigh-Ritz (SHCI/Davidson.cpp:250-269)
-      std::vector<double> G = gram_host(V.p, N, m, W.p, N, m);
+      // Rayleigh-Ritz (SHCI/Davidson.cpp:250-269): small eigenproblem on the host
       std::vector<double> hs((size_t)m * m);
       for (int i = 0; i < m; ++i)
         for (int j = i; j < m; ++j) hs[(size_t)i * m + j] = hs[(size_t)j * m + i] = G[(size_t)i + (size_t)j * m];
       sym_eig(m, hs, lam, Q);
-      to_dev(dQ, Q);
-      std::vector<double> lr(lam.begin(), lam.begin() + nroots);
-      to_dev(dlam, lr);
-      ts_gemm(V.p, N, m, dQ.p, nroots, N, 1.0, 0.0, X.p, N, stream);
-      ts_gemm(W.p, N, m, dQ.p, nroots, N, 1.0, 0.0, Y.p, N, stream);
-      residual(X.p, Y.p, dlam.p, nroots, N, N, R.p, stream);
-      std::vector<double> RR = gram_host(R.p, N, nroots, R.p, N, nroots);
+      std::memcpy(pin + kPinQ, Q.data(), (size_t)m * m * sizeof(double));
+      std::memcpy(pin + kPinLam, lam.data(), (size_t)nroots * sizeof(double));
+      // graph 1: Ritz vectors, residuals and the residual Gram matrix
+      launch_body(((uint64_t)1 << 60) | (uint64_t)m, [&]() {
+        SHCI_CUDA(cudaMemcpyAsync(dQ.p, pin + kPinQ, (size_t)m * m * sizeof(double), cudaMemcpyHostToDevice, stream));
+        SHCI_CUDA(cudaMemcpyAsync(dlam.p, pin + kPinLam, (size_t)nroots * sizeof(double), cudaMemcpyHostToDevice,
+                                  stream));
+        ts_gemm(V.p, N, m, dQ.p, nroots, N, 1.0, 0.0, X.p, N, stream);
+        ts_gemm(W.p, N, m, dQ.p, nroots, N, 1.0, 0.0, Y.p, N, stream);
+        residual(X.p, Y.p, dlam.p, nroots, N, N, R.p, stream);
+        ts_gram(R.p, N, nroots, R.p, N, nroots, N, drr.p, gpart, stream);
+        SHCI_CUDA(cudaMemcpyAsync(pin + kPinRR, drr.p, (size_t)nroots * nroots * sizeof(double),
+                                  cudaMemcpyDeviceToHost, stream));
+      });
+      SHCI_CUDA(cudaStreamSynchronize(stream));
+      if (trace_level() > 0) t_g1 += now_s() - t_loop0, t_loop0 = now_s();
       std::vector<double> rn(nroots);
-      for (int c = 0; c < nroots; ++c) rn[c] = std::sqrt(std::max(0.0, RR[(size_t)c * nroots + c]));
+      for (int c = 0; c < nroots; ++c) rn[c] = std::sqrt(std::max(0.0, pin[kPinRR + (size_t)c * nroots + c]));
       numIter++;
       if (trace_level() > 0)
         std::fprintf(stderr, "[davidson mode=%d it=%d m=%d] lam0=%.12f res0=%.3e G00=%.12f\n", mode, numIter, m,
@@ -561,6 +650,13 @@ struct Context {
         E.assign(lam.begin(), lam.begin() + nroots);
         SHCI_CUDA(cudaMemcpyAsync(x, X.p, N * nroots * sizeof(double), cudaMemcpyDeviceToDevice, stream));
         SHCI_CUDA(cudaStreamSynchronize(stream));
+        graphs_clear();
+        if (trace_level() > 0)
+          std::fprintf(stderr,
+                       "[davidson-time mode=%d N=%zu iters=%d mmax=%d] total %.2f ms: setup %.2f, ritz %.2f, "
+                       "correction+sigma %.2f (sigma %.2f)\n",
+                       mode, N, numIter, mmax, 1e3 * (now_s() - t_enter), 1e3 * (t_loop0 - t_enter - t_g1 - t_g2),
+                       1e3 * t_g1, 1e3 * t_g2, 1e3 * (t_sigma - sig0));
       };
       if ((size_t)m == N) {
         finish();
@@ -634,56 +730,108 @@ struct Context {
         }
       }
       const int nact = (int)act.size();
-      for (int a = 0; a < nact; ++a)
-        SHCI_CUDA(cudaMemcpyAsync(D.p + (size_t)a * N, R.p + (size_t)act[a] * N, N * sizeof(double),
-                                  cudaMemcpyDeviceToDevice, stream));
-      to_dev(dlam, act_lam);
-      if (shift_ready && shift.n >= N)
-        precondition_shift(diag.p, shift.p, dlam.p, nact, N, D.p, N, stream);
-      else
-        precondition(diag.p, dlam.p, nact, N, D.p, N, stream);
-      if (sym) {
-        // keep each correction in the flip sector of the root it corrects
+      std::memcpy(pin + kPinAct, act_lam.data(), (size_t)nact * sizeof(double));
+      uint64_t amask = 0;
+      for (int a : act) amask |= 1ull << a;
+      const bool collapse = m + nact > mmax;
+      int keep = m;
+      if (collapse) {
+        keep = basis_keep > 0 ? std::min(basis_keep, mmax - nact)
+                              : (block ? mmax - nact : std::min(nroots + 2, mmax - nact));
+        if (keep < nroots) keep = nroots;
+      }
+      const int m1 = collapse ? keep : m;
+      // graph 2: corrections, orthonormalisation, collapse, append, sigma, Gram
+      sigma_deferred = use_graphs;
+      launch_body(((uint64_t)2 << 60) | ((uint64_t)m << 40) | ((uint64_t)keep << 20) | amask, [&]() {
+        SHCI_CUDA(cudaMemcpyAsync(dactlam.p, pin + kPinAct, (size_t)nact * sizeof(double), cudaMemcpyHostToDevice,
+                                  stream));
         for (int a = 0; a < nact; ++a) {
-          const double p = flip_parity(X.p + (size_t)act[a] * N, N, flipidx.p, flipsgn.p, gpart, stream);
-          if (std::fabs(p) > kParityDefinite) project_parity(D.p + (size_t)a * N, p > 0 ? 1.0 : -1.0);
+          // residual with the eigenvalue the reference uses for this root, preconditioned
+          double* da = D.p + (size_t)a * N;
+          residual(X.p + (size_t)act[a] * N, Y.p + (size_t)act[a] * N, dactlam.p + a, 1, N, N, da, stream);
+          if (shiftp)
+            precondition_shift(diag.p, shiftp, dactlam.p + a, 1, N, da, N, stream);
+          else
+            precondition(diag.p, dactlam.p + a, 1, N, da, N, stream);
+          if (sym) {
+            // keep each correction in the flip sector of the root it corrects
+            flip_parity_dev(X.p + (size_t)act[a] * N, N, flipidx.p, flipsgn.p, gpart, dpar.p + a, stream);
+            flip_project_cond(da, N, flipidx.p, flipsgn.p, dpar.p + a, kParityDefinite, ftmp.p, stream);
+          }
         }
+        // orthogonalise against the whole basis (two classical Gram-Schmidt passes)
+        for (int pass = 0; pass < 2; ++pass) {
+          ts_gram(V.p, N, m, D.p, N, nact, N, dG.p, gpart, stream);
+          ts_gemm(V.p, N, m, dG.p, nact, N, -1.0, 1.0, D.p, N, stream);
+        }
+        for (int a = 0; a < nact; ++a) {
+          double* da = D.p + (size_t)a * N;
+          for (int b2 = 0; b2 < a; ++b2) project_out(D.p + (size_t)b2 * N, da);
+          ts_gram(da, N, 1, da, N, 1, N, dnrm.p + a, gpart, stream);
+          scale_inv_norm(da, N, dnrm.p + a, stream);
+        }
+        SHCI_CUDA(cudaMemcpyAsync(pin + kPinNrm, dnrm.p, (size_t)nact * sizeof(double), cudaMemcpyDeviceToHost,
+                                  stream));
+        if (collapse) {
+          ts_gemm(V.p, N, m, dQ.p, keep, N, 1.0, 0.0, Vt.p, N, stream);
+          ts_gemm(W.p, N, m, dQ.p, keep, N, 1.0, 0.0, Wt.p, N, stream);
+          SHCI_CUDA(cudaMemcpyAsync(V.p, Vt.p, (size_t)keep * N * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+          SHCI_CUDA(cudaMemcpyAsync(W.p, Wt.p, (size_t)keep * N * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+        }
+        SHCI_CUDA(cudaMemcpyAsync(V.p + (size_t)m1 * N, D.p, (size_t)nact * N * sizeof(double),
+                                  cudaMemcpyDeviceToDevice, stream));
+        apply_sigma(mode, V.p, N, m1, nact, W.p, N, m1);
+        ts_gram(V.p, N, m1 + nact, W.p, N, m1 + nact, N, dG.p, gpart, stream);
+        SHCI_CUDA(cudaMemcpyAsync(pin + kPinG, dG.p, (size_t)(m1 + nact) * (m1 + nact) * sizeof(double),
+                                  cudaMemcpyDeviceToHost, stream));
+      });
+      sigma_deferred = false;
+      SHCI_CUDA(cudaStreamSynchronize(stream));
+      if (trace_level() > 0) t_g2 += now_s() - t_loop0, t_loop0 = now_s();
+      if (use_graphs) {
+        float ms = 0.f;
+        SHCI_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+        t_sigma += ms * 1e-3;
+        n_sigma += 1;
       }
-      // orthogonalise against the whole basis (two classical Gram-Schmidt passes)
-      dG.reserve((size_t)m * nact);
-      for (int pass = 0; pass < 2; ++pass) {
-        ts_gram(V.p, N, m, D.p, N, nact, N, dG.p, gpart, stream);
-        ts_gemm(V.p, N, m, dG.p, nact, N, -1.0, 1.0, D.p, N, stream);
+      bool dependent = false;
+      for (int a = 0; a < nact; ++a) dependent |= !(std::sqrt(pin[kPinNrm + a]) > 1e-14);
+      if (!dependent) {
+        m = m1 + nact;
+        G.assign(pin + kPinG, pin + kPinG + (size_t)m * m);
+        continue;
       }
+      // Some correction was linearly dependent on the basis (rare: tiny or
+      // exhausted spaces). Drop it, as the reference does, and redo the
+      // append and sigma for the others on the stream directly; the rotated
+      // basis (if collapsed) is kept.
       int kept = 0;
       for (int a = 0; a < nact; ++a) {
-        double* da = D.p + (size_t)a * N;
-        for (int b = 0; b < kept; ++b) project_out(D.p + (size_t)b * N, da);
-        double nrm = norm_host(da);
-        if (!(nrm > 1e-14)) continue;  // linearly dependent correction
-        scale_col(da, 1.0 / nrm);
+        if (!(std::sqrt(pin[kPinNrm + a]) > 1e-14)) continue;
         if (kept != a)
-          SHCI_CUDA(cudaMemcpyAsync(D.p + (size_t)kept * N, da, N * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+          SHCI_CUDA(cudaMemcpyAsync(D.p + (size_t)kept * N, D.p + (size_t)a * N, N * sizeof(double),
+                                    cudaMemcpyDeviceToDevice, stream));
         ++kept;
       }
+      m = m1;
       if (kept == 0) {  // nothing new to add: the subspace is exhausted
+        G = gram_host(V.p, N, m, W.p, N, m);
+        std::vector<double> hs2((size_t)m * m);
+        for (int i = 0; i < m; ++i)
+          for (int j = i; j < m; ++j) hs2[(size_t)i * m + j] = hs2[(size_t)j * m + i] = G[(size_t)i + (size_t)j * m];
+        sym_eig(m, hs2, lam, Q);
+        to_dev(dQ, Q);
+        to_dev(dlam, std::vector<double>(lam.begin(), lam.begin() + nroots));
+        ts_gemm(V.p, N, m, dQ.p, nroots, N, 1.0, 0.0, X.p, N, stream);
         finish();
         return;
-      }
-      if (m + kept > mmax) {
-        int keep = basis_keep > 0 ? std::min(basis_keep, mmax - kept)
-                   : (block ? mmax - kept : std::min(nroots + 2, mmax - kept));
-        if (keep < nroots) keep = nroots;
-        ts_gemm(V.p, N, m, dQ.p, keep, N, 1.0, 0.0, Vt.p, N, stream);
-        ts_gemm(W.p, N, m, dQ.p, keep, N, 1.0, 0.0, Wt.p, N, stream);
-        V.swap(Vt);
-        W.swap(Wt);
-        m = keep;
       }
       SHCI_CUDA(cudaMemcpyAsync(V.p + (size_t)m * N, D.p, (size_t)kept * N * sizeof(double),
                                 cudaMemcpyDeviceToDevice, stream));
       apply_sigma(mode, V.p, N, m, kept, W.p, N, m);
       m += kept;
+      G = gram_host(V.p, N, m, W.p, N, m);
     }
   }
 
@@ -968,6 +1116,7 @@ int shci_ctx_create(int device, shci_ctx** out) {
     SHCI_CUDA(cudaStreamCreateWithFlags(&ctx->c.stream, cudaStreamNonBlocking));
     SHCI_CUDA(cudaEventCreate(&ctx->c.ev0));
     SHCI_CUDA(cudaEventCreate(&ctx->c.ev1));
+    SHCI_CUDA(cudaMallocHost(&ctx->c.pin, Context::kPin * sizeof(double)));
     *out = ctx.release();
     return SHCI_OK;
   } catch (const Error& e) {
@@ -1333,6 +1482,13 @@ int shci_set_davidson_basis(shci_ctx* ctx, int max_basis, int keep) {
     if (keep < 1 || keep >= max_basis) throw Error(SHCI_ERR_INVALID, "keep must be in 1..max_basis-1");
     c.basis_max = max_basis;
     c.basis_keep = keep;
+  });
+}
+
+int shci_set_davidson_graphs(shci_ctx* ctx, int on) {
+  return guarded(ctx, [&](Context& c) {
+    c.graphs_clear();
+    c.use_graphs = on != 0;
   });
 }
 

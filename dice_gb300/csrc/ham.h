@@ -118,6 +118,12 @@ double flip_parity(const double* x, size_t n, const int32_t* flip, const int8_t*
 // x <- (x + p F x) / 2 in place (p = +1 or -1), using tmp (n doubles)
 void flip_project(double* x, size_t n, const int32_t* flip, const int8_t* sign, double p, double* tmp,
                   cudaStream_t s);
+// Device-resident forms (no host synchronisation): the parity is written to
+// *out; the projection uses the sign of *p and applies only if |*p| > thresh.
+void flip_parity_dev(const double* x, size_t n, const int32_t* flip, const int8_t* sign, DevBuf<double>& part,
+                     double* out, cudaStream_t s);
+void flip_project_cond(double* x, size_t n, const int32_t* flip, const int8_t* sign, const double* p, double thresh,
+                       double* tmp, cudaStream_t s);
 
 // ---- sigma and Davidson vector kernels (kernels_sigma.cu) -------------------
 // Y[:, c] (column-major, leading dimension ldy) = diag .* X[:, c] + Hoff X[:, c]
@@ -145,6 +151,8 @@ void ts_gram(const double* A, size_t lda, int ma, const double* B, size_t ldb, i
 // Y = alpha * A Q + beta * Y, Q (m x k column-major, device).
 void ts_gemm(const double* A, size_t lda, int m, const double* Q, int k, size_t N, double alpha, double beta,
              double* Y, size_t ldy, cudaStream_t s);
+// c <- c / sqrt(g[0]) when sqrt(g[0]) > 1e-14 (g: device squared norm)
+void scale_inv_norm(double* c, size_t N, const double* g, cudaStream_t s);
 // R[:, c] = Y[:, c] - lam[c] X[:, c]
 void residual(const double* X, const double* Y, const double* lam, int k, size_t N, size_t ld, double* R,
               cudaStream_t s);

@@ -493,6 +493,18 @@ void precondition_shift(const double* diag, const double* shift, const double* l
   SHCI_LAUNCH_CHECK();
 }
 
+__global__ void k_scale_inv_norm(double* __restrict__ c, size_t N, const double* __restrict__ g) {
+  const double nrm = sqrt(g[0]);
+  if (!(nrm > 1e-14)) return;  // linearly dependent: left for the host to drop
+  const double sc = 1.0 / nrm;
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < N; r += (size_t)gridDim.x * blockDim.x)
+    c[r] *= sc;
+}
+void scale_inv_norm(double* c, size_t N, const double* g, cudaStream_t s) {
+  k_scale_inv_norm<<<grid_for(N, 256), 256, 0, s>>>(c, N, g);
+  SHCI_LAUNCH_CHECK();
+}
+
 __global__ void k_scale_cols(double* __restrict__ A, size_t ld, const double* __restrict__ sc, int k, size_t N) {
   for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < N; r += (size_t)gridDim.x * blockDim.x)
     for (int c = 0; c < k; ++c) A[(size_t)c * ld + r] *= sc[c];

@@ -49,6 +49,7 @@ SIGNATURES = [
     ("shci_run_timings", _i32, [_vp, _P(_dbl), _P(_dbl), _P(_dbl), _P(_dbl), _P(_i64), _P(_dbl)]),
     ("shci_set_preconditioner", _i32, [_vp, _i32]),
     ("shci_set_davidson_basis", _i32, [_vp, _i32, _i32]),
+    ("shci_set_davidson_graphs", _i32, [_vp, _i32]),
     ("shci_fcidump_info", _i32, [ctypes.c_char_p, _P(_i32), _P(_i32), _P(_dbl), _P(_i64)]),
     ("shci_input_info", _i32, [ctypes.c_char_p, _vp, _i32, _P(_i32), _vp, _vp]),
     ("shci_pt2_shift", _i32, [_vp, _dbl, _vp]),
@@ -318,6 +319,10 @@ class Engine:
         """Subspace of every Davidson solve of run_input: at most max_basis
         vectors, collapsed to keep; (0, 0) is the reference's rule."""
         self._check(load_library().shci_set_davidson_basis(self.h, int(max_basis), int(keep)))
+
+    def set_davidson_graphs(self, on=True):
+        """Davidson iterations as replayed CUDA graphs (default) or eager launches."""
+        self._check(load_library().shci_set_davidson_graphs(self.h, int(bool(on))))
 
     def pt2_shift(self, E):
         out = np.zeros(self.ndets())

@@ -208,6 +208,10 @@ int shci_set_preconditioner(shci_ctx* ctx, int mode);
  * Krylov space across restarts and needs fewer iterations to the same
  * tolerance; it changes no converged eigenvalue. */
 int shci_set_davidson_basis(shci_ctx* ctx, int max_basis, int keep);
+/* Davidson iterations as captured CUDA graphs (1, the default) or as the
+ * same kernels launched one by one (0); results are identical. No
+ * counterpart in the reference. */
+int shci_set_davidson_graphs(shci_ctx* ctx, int on);
 /* Second-order level shifts of the current space at energy E (host out[N]). */
 int shci_pt2_shift(shci_ctx* ctx, double E, double* out);
 /* MLP training settings: Adam steps per training call, minibatch, learning

@@ -289,3 +289,37 @@ def test_larger_davidson_subspace_same_energy_fewer_iterations(tmp_path):
         assert out[(16, 8), mode][1] < 0.8 * out[(0, 0), mode][1]
     with pytest.raises(eng.ShciError):
         eng.Engine(0).set_davidson_basis(32, 8)
+
+
+@pytest.mark.parametrize("mode", ["fp64", "mixed"])
+def test_graph_captured_davidson_identical_to_eager(golden, mode):
+    """The two captured graphs of a Davidson iteration replay exactly the
+    kernels the eager path launches: same eigenvalues, iteration counts and
+    vectors, bit for bit, for one root and for a 4-root block solve."""
+    inp = golden("h8_631g", "dice.dat")
+    dets = np.load(os.path.join(GOLDEN, "h8_631g_dets.npz"))["dets"]
+    o = orc.Oracle(_fcidump(inp))
+    diag = np.array([o.energy(x) for x in dets])
+    order = np.argsort(diag)
+    res = {}
+    for graphs in (True, False):
+        e = eng.Engine(0)
+        e.set_davidson_graphs(graphs)
+        e.read_fcidump(_fcidump(inp))
+        e.set_dets(dets)
+        e.ham_build(mode)
+        x1 = np.zeros((1, len(dets)))
+        x1[0, order[0]] = 1.0
+        x4 = np.zeros((4, len(dets)))
+        for r in range(4):
+            x4[r, order[r]] = 1.0
+        l0 = e.launch_count()
+        r1 = e.davidson(x1, mode=mode, tol=1e-7)
+        r4 = e.davidson(x4, mode=mode, block=True, max_copies=12, tol=1e-7)
+        res[graphs] = (r1, r4, e.launch_count() - l0)
+        e.close()
+    for a, b in zip(res[True][:2], res[False][:2]):
+        assert np.array_equal(a[0], b[0]) and a[2] == b[2]
+        assert np.array_equal(a[1], b[1])
+    # replays count the kernels of every captured graph
+    assert res[True][2] == res[False][2]
