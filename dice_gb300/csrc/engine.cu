@@ -462,8 +462,14 @@ struct Context {
         sigma_csr_mixed(H, diag.p, xb32.p, kp, kk, Yp + (size_t)(yc0 + done) * ldy, ldy, stream);
       } else if (mode == SHCI_MODE_FP64) {
         xb64.reserve(N * kp);
-        pack_f64(A, lda, c0 + done, kk, kp, N, xb64.p, stream);
-        sigma_csr_f64(H, diag.p, xb64.p, kp, kk, Yp + (size_t)(yc0 + done) * ldy, ldy, H.v64.p == nullptr, stream);
+        if (H.v64.p) {
+          pack_f64(A, lda, c0 + done, kk, kp, N, xb64.p, stream);
+          sigma_csr_f64(H, diag.p, xb64.p, kp, kk, Yp + (size_t)(yc0 + done) * ldy, ldy, false, stream);
+        } else {  // mixed-path matrix: float-float refinement sigma on head + tail
+          float* xff = reinterpret_cast<float*>(xb64.p);
+          pack_ff(A, lda, c0 + done, kk, kp, N, xff, stream);
+          sigma_csr_ff(H, diag.p, xff, kp, A, lda, c0 + done, kk, Yp + (size_t)(yc0 + done) * ldy, ldy, stream);
+        }
       } else {
         xb64.reserve(N * kp);
         yb64.reserve(N * kp);
@@ -782,8 +788,9 @@ struct Context {
         SHCI_CUDA(cudaMemcpyAsync(V.p + (size_t)m1 * N, D.p, (size_t)nact * N * sizeof(double),
                                   cudaMemcpyDeviceToDevice, stream));
         apply_sigma(mode, V.p, N, m1, nact, W.p, N, m1);
-        ts_gram(V.p, N, m1 + nact, W.p, N, m1 + nact, N, dG.p, gpart, stream);
-        SHCI_CUDA(cudaMemcpyAsync(pin + kPinG, dG.p, (size_t)(m1 + nact) * (m1 + nact) * sizeof(double),
+        // only the new columns of G = V^T W: (m1 + nact) x nact
+        ts_gram(V.p, N, m1 + nact, W.p + (size_t)m1 * N, N, nact, N, dG.p, gpart, stream);
+        SHCI_CUDA(cudaMemcpyAsync(pin + kPinG, dG.p, (size_t)(m1 + nact) * nact * sizeof(double),
                                   cudaMemcpyDeviceToHost, stream));
       });
       sigma_deferred = false;
@@ -798,8 +805,36 @@ struct Context {
       bool dependent = false;
       for (int a = 0; a < nact; ++a) dependent |= !(std::sqrt(pin[kPinNrm + a]) > 1e-14);
       if (!dependent) {
-        m = m1 + nact;
-        G.assign(pin + kPinG, pin + kPinG + (size_t)m * m);
+        // G of the new basis: the kept block (rotated on the host after a
+        // collapse: Q_k^T G Q_k) plus the new columns from the device
+        const int mm = m1 + nact;
+        std::vector<double> Gn((size_t)mm * mm, 0.0);
+        if (collapse) {
+          std::vector<double> T((size_t)m * keep, 0.0);  // hs Q_k (m x keep, column-major)
+          for (int b2 = 0; b2 < keep; ++b2)
+            for (int i = 0; i < m; ++i) {
+              double t = 0.0;
+              for (int j = 0; j < m; ++j) t += hs[(size_t)i * m + j] * Q[(size_t)j + (size_t)b2 * m];
+              T[(size_t)i + (size_t)b2 * m] = t;
+            }
+          for (int b2 = 0; b2 < keep; ++b2)
+            for (int a2 = 0; a2 < keep; ++a2) {
+              double t = 0.0;
+              for (int i = 0; i < m; ++i) t += Q[(size_t)i + (size_t)a2 * m] * T[(size_t)i + (size_t)b2 * m];
+              Gn[(size_t)a2 + (size_t)b2 * mm] = t;
+            }
+        } else {
+          for (int j = 0; j < m; ++j)
+            for (int i = 0; i < m; ++i) Gn[(size_t)i + (size_t)j * mm] = G[(size_t)i + (size_t)j * m];
+        }
+        for (int j = 0; j < nact; ++j)
+          for (int i = 0; i < mm; ++i) {
+            const double g = pin[kPinG + (size_t)i + (size_t)j * mm];
+            Gn[(size_t)i + (size_t)(m1 + j) * mm] = g;
+            Gn[(size_t)(m1 + j) + (size_t)i * mm] = g;
+          }
+        m = mm;
+        G.swap(Gn);
         continue;
       }
       // Some correction was linearly dependent on the basis (rare: tiny or

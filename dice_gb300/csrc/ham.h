@@ -132,6 +132,11 @@ void sigma_csr_mixed(const Csr& H, const double* diag, const float* x32, int kp,
                      cudaStream_t s);
 void sigma_csr_f64(const Csr& H, const double* diag, const double* x64, int kp, int k, double* y, size_t ldy,
                    bool use_hilo, cudaStream_t s);
+// Refinement sigma on the FP32 head + tail values in float-float arithmetic:
+// xff is x split as (head, tail) float pairs, row-interleaved [N][kp]; the
+// diagonal term is taken in FP64 from column-major xd (columns c0..c0+k-1).
+void sigma_csr_ff(const Csr& H, const double* diag, const float* xff, int kp, const double* xd, size_t ldx, int c0,
+                  int k, double* y, size_t ldy, cudaStream_t s);
 // Sigma that allocates nothing: x (column-major, ldx) is packed into a fixed
 // device array of kNoAllocPackBytes (16 MiB: N x k up to 4,194,304 in the
 // mixed path, 2,097,152 in the FP64 path; k = 3 counts as 4) and the stored
@@ -143,6 +148,8 @@ void sigma_noalloc(const Csr& H, const double* diag, int mode_mixed, const doubl
 // (zero padded) in FP32 or FP64.
 void pack_f32(const double* A, size_t lda, int c0, int k, int kp, size_t N, float* out, cudaStream_t s);
 void pack_f64(const double* A, size_t lda, int c0, int k, int kp, size_t N, double* out, cudaStream_t s);
+// Columns split into (head, tail) float pairs, row-interleaved [N][kp] float2.
+void pack_ff(const double* A, size_t lda, int c0, int k, int kp, size_t N, float* out, cudaStream_t s);
 void unpack_f64(const double* in, int kp, int k, size_t N, double* A, size_t lda, int c0, cudaStream_t s);
 // Tall-skinny products over column-major N x m blocks (deterministic order):
 // G (ma x mb, column-major) = A^T B.

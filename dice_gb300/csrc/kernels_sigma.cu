@@ -191,6 +191,110 @@ __global__ void __launch_bounds__(256) k_sigma_f64(const int64_t* __restrict__ r
   }
 }
 
+// Refinement sigma on the mixed path's head + tail values, in float-float
+// arithmetic: x is split as x = xh + xl (two floats) and every product
+// (hi + lo)(xh + xl) enters the compensated accumulator as its exactly
+// rounded head hi*xh plus the FMA residual and the cross terms hi*xl + lo*xh.
+// The result matches the FP64 product sum to ~1e-13 relative while keeping
+// every operation of the inner loop on the FP32 pipe (the FP64 pipe of this
+// GPU issues about two FMAs per clock per SM, so an FP64 head + tail sum,
+// with its two conversions, one add and one FMA per nonzero, runs 3.5x
+// slower). The diagonal term is added in FP64 from the unsplit x.
+__device__ __forceinline__ void acc_add_ff(Acc& a, float hi, float lo, float xh, float xl) {
+  const float p = __fmul_rn(hi, xh);
+  const float pe = __fmaf_rn(hi, xh, -p);
+  const float small = __fmaf_rn(hi, xl, __fmaf_rn(lo, xh, pe));
+  const float t = __fadd_rn(a.s, p);
+  const float bp = __fsub_rn(t, a.s);
+  const float e = __fadd_rn(__fsub_rn(a.s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+  a.s = t;
+  a.c = __fadd_rn(a.c, __fadd_rn(e, small));
+}
+
+template <int KP>
+struct VecFF;
+template <>
+struct VecFF<1> {
+  __device__ static void fma(Acc* acc, float hi, float lo, const float* x, int j) {
+    const float2 v = __ldg(reinterpret_cast<const float2*>(x) + j);
+    acc_add_ff(acc[0], hi, lo, v.x, v.y);
+  }
+};
+template <>
+struct VecFF<2> {
+  __device__ static void fma(Acc* acc, float hi, float lo, const float* x, int j) {
+    const float4 v = __ldg(reinterpret_cast<const float4*>(x) + j);
+    acc_add_ff(acc[0], hi, lo, v.x, v.y);
+    acc_add_ff(acc[1], hi, lo, v.z, v.w);
+  }
+};
+template <>
+struct VecFF<4> {
+  __device__ static void fma(Acc* acc, float hi, float lo, const float* x, int j) {
+    const float4 v0 = __ldg(reinterpret_cast<const float4*>(x) + 2 * (size_t)j);
+    const float4 v1 = __ldg(reinterpret_cast<const float4*>(x) + 2 * (size_t)j + 1);
+    acc_add_ff(acc[0], hi, lo, v0.x, v0.y);
+    acc_add_ff(acc[1], hi, lo, v0.z, v0.w);
+    acc_add_ff(acc[2], hi, lo, v1.x, v1.y);
+    acc_add_ff(acc[3], hi, lo, v1.z, v1.w);
+  }
+};
+
+template <int VW, int KP>
+__global__ void __launch_bounds__(256) k_sigma_ff(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                                                  const float* __restrict__ vhi, const float* __restrict__ vlo,
+                                                  const double* __restrict__ diag, const float* __restrict__ xff,
+                                                  const double* __restrict__ xd, size_t ldx, int c0, size_t N, int k,
+                                                  double* __restrict__ y, size_t ldy) {
+  // same row mapping as k_sigma_mixed
+  const int sub = threadIdx.x & (VW - 1);
+  const size_t rows_per_warp = 32 / VW;
+  const size_t stride = ((size_t)gridDim.x * blockDim.x / 32) * rows_per_warp;
+  for (size_t wr = (((size_t)blockIdx.x * blockDim.x + threadIdx.x) / 32) * rows_per_warp; wr < N; wr += stride) {
+    const size_t r = wr + (threadIdx.x & 31) / VW;
+    const bool live = r < N;
+    Acc acc[KP];
+#pragma unroll
+    for (int c = 0; c < KP; ++c) acc[c] = Acc{0.f, 0.f};
+    const int64_t p0 = live ? __ldg(rowptr + r) : 0;
+    const int64_t p1 = live ? __ldg(rowptr + r + 1) : 0;
+    int64_t p = p0 + sub;
+    for (; p + 3 * VW < p1; p += 4 * VW) {
+      const int j0 = __ldcs(col + p), j1 = __ldcs(col + p + VW);
+      const int j2 = __ldcs(col + p + 2 * VW), j3 = __ldcs(col + p + 3 * VW);
+      const float h0 = __ldcs(vhi + p), h1 = __ldcs(vhi + p + VW);
+      const float h2 = __ldcs(vhi + p + 2 * VW), h3 = __ldcs(vhi + p + 3 * VW);
+      const float l0 = __ldcs(vlo + p), l1 = __ldcs(vlo + p + VW);
+      const float l2 = __ldcs(vlo + p + 2 * VW), l3 = __ldcs(vlo + p + 3 * VW);
+      VecFF<KP>::fma(acc, h0, l0, xff, j0);
+      VecFF<KP>::fma(acc, h1, l1, xff, j1);
+      VecFF<KP>::fma(acc, h2, l2, xff, j2);
+      VecFF<KP>::fma(acc, h3, l3, xff, j3);
+    }
+    for (; p < p1; p += VW) VecFF<KP>::fma(acc, __ldcs(vhi + p), __ldcs(vlo + p), xff, __ldcs(col + p));
+#pragma unroll
+    for (int c = 0; c < KP; ++c) {
+#pragma unroll
+      for (int o = VW / 2; o; o >>= 1) {
+        Acc other{__shfl_xor_sync(kFull, acc[c].s, o, VW), __shfl_xor_sync(kFull, acc[c].c, o, VW)};
+        if ((threadIdx.x & o) == 0) {
+          acc_merge(acc[c], other);
+        } else {
+          acc_merge(other, acc[c]);
+          acc[c] = other;
+        }
+      }
+    }
+    if (sub == 0 && live) {
+      const double dg = diag[r];
+#pragma unroll
+      for (int c = 0; c < KP; ++c)
+        if (c < k)
+          y[(size_t)c * ldy + r] = dg * xd[(size_t)(c0 + c) * ldx + r] + ((double)acc[c].s + (double)acc[c].c);
+    }
+  }
+}
+
 static int pick_vw(const Csr& H) {
   double avg = H.N ? (double)H.nnz / (double)H.N : 0.0;
   if (avg >= 96) return 32;
@@ -265,6 +369,34 @@ void sigma_csr_f64(const Csr& H, const double* diag, const double* x64, int kp, 
   }
 }
 
+template <int KP>
+static void launch_ff(int vw, const Csr& H, const double* diag, const float* xff, const double* xd, size_t ldx, int c0,
+                      int k, double* y, size_t ldy, cudaStream_t s) {
+  const size_t threads = H.N * (size_t)vw;
+  const unsigned blocks = grid_for(threads, 256, 152 * 16);
+  const float *vhi = H.vhi.p, *vlo = H.vlo.p;
+  switch (vw) {
+    case 32: k_sigma_ff<32, KP><<<blocks, 256, 0, s>>>(H.rowptr.p, H.col.p, vhi, vlo, diag, xff, xd, ldx, c0, H.N, k, y, ldy); break;
+    case 16: k_sigma_ff<16, KP><<<blocks, 256, 0, s>>>(H.rowptr.p, H.col.p, vhi, vlo, diag, xff, xd, ldx, c0, H.N, k, y, ldy); break;
+    case 8: k_sigma_ff<8, KP><<<blocks, 256, 0, s>>>(H.rowptr.p, H.col.p, vhi, vlo, diag, xff, xd, ldx, c0, H.N, k, y, ldy); break;
+    default: k_sigma_ff<4, KP><<<blocks, 256, 0, s>>>(H.rowptr.p, H.col.p, vhi, vlo, diag, xff, xd, ldx, c0, H.N, k, y, ldy); break;
+  }
+  SHCI_LAUNCH_CHECK();
+}
+
+void sigma_csr_ff(const Csr& H, const double* diag, const float* xff, int kp, const double* xd, size_t ldx, int c0,
+                  int k, double* y, size_t ldy, cudaStream_t s) {
+  if (H.N == 0) return;
+  if (!(H.vhi.p && H.vlo.p)) throw Error(kErrState, "Hamiltonian has no FP32 head/tail values");
+  const int vw = pick_vw(H);
+  switch (kp) {
+    case 1: launch_ff<1>(vw, H, diag, xff, xd, ldx, c0, k, y, ldy, s); break;
+    case 2: launch_ff<2>(vw, H, diag, xff, xd, ldx, c0, k, y, ldy, s); break;
+    case 4: launch_ff<4>(vw, H, diag, xff, xd, ldx, c0, k, y, ldy, s); break;
+    default: throw Error(kErrInvalid, "sigma block width must be 1, 2 or 4");
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Packing between column-major FP64 blocks and row-interleaved vectors
 // ---------------------------------------------------------------------------
@@ -282,6 +414,23 @@ __global__ void k_unpack_f64(const double* __restrict__ in, int kp, int k, size_
                              size_t lda, int c0) {
   for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < N; r += (size_t)gridDim.x * blockDim.x)
     for (int c = 0; c < k; ++c) A[(size_t)(c0 + c) * lda + r] = in[r * kp + c];
+}
+__global__ void k_pack_ff(const double* __restrict__ A, size_t lda, int c0, int k, int kp, size_t N,
+                          float2* __restrict__ out) {
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < N; r += (size_t)gridDim.x * blockDim.x)
+    for (int c = 0; c < kp; ++c) {
+      float2 v = make_float2(0.f, 0.f);
+      if (c < k) {
+        const double x = A[(size_t)(c0 + c) * lda + r];
+        v.x = __double2float_rn(x);
+        v.y = __double2float_rn(x - (double)v.x);
+      }
+      out[r * kp + c] = v;
+    }
+}
+void pack_ff(const double* A, size_t lda, int c0, int k, int kp, size_t N, float* out, cudaStream_t s) {
+  k_pack_ff<<<grid_for(N, 256), 256, 0, s>>>(A, lda, c0, k, kp, N, reinterpret_cast<float2*>(out));
+  SHCI_LAUNCH_CHECK();
 }
 void pack_f32(const double* A, size_t lda, int c0, int k, int kp, size_t N, float* out, cudaStream_t s) {
   k_pack_f32<<<grid_for(N, 256), 256, 0, s>>>(A, lda, c0, k, kp, N, out);
@@ -414,18 +563,23 @@ void ts_gram(const double* A, size_t lda, int ma, const double* B, size_t ldb, i
   SHCI_LAUNCH_CHECK();
 }
 
-// Y = alpha * A Q + beta * Y
-__global__ void k_ts_gemm(const double* __restrict__ A, size_t lda, int m, const double* __restrict__ Q, int k,
-                          size_t N, double alpha, double beta, double* __restrict__ Y, size_t ldy) {
+// Y = alpha * A Q + beta * Y. Each thread owns one row; the row's m entries
+// stay in registers (loops unrolled to the 16-column maximum and predicated).
+__global__ void __launch_bounds__(256) k_ts_gemm(const double* __restrict__ A, size_t lda, int m,
+                                                 const double* __restrict__ Q, int k, size_t N, double alpha,
+                                                 double beta, double* __restrict__ Y, size_t ldy) {
   __shared__ double sQ[kGramMax * kGramMax];
   for (int e = threadIdx.x; e < m * k; e += blockDim.x) sQ[e] = Q[e];
   __syncthreads();
   for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < N; r += (size_t)gridDim.x * blockDim.x) {
     double a[kGramMax];
-    for (int i = 0; i < m; ++i) a[i] = A[(size_t)i * lda + r];
+#pragma unroll
+    for (int i = 0; i < kGramMax; ++i) a[i] = i < m ? A[(size_t)i * lda + r] : 0.0;
     for (int c = 0; c < k; ++c) {
       double s = 0.0;
-      for (int i = 0; i < m; ++i) s += a[i] * sQ[c * m + i];
+#pragma unroll
+      for (int i = 0; i < kGramMax; ++i)
+        if (i < m) s += a[i] * sQ[c * m + i];
       double* yp = Y + (size_t)c * ldy + r;
       *yp = (beta == 0.0) ? alpha * s : alpha * s + beta * (*yp);
     }
@@ -564,8 +718,13 @@ void sigma_noalloc(const Csr& H, const double* diag, int mode_mixed, const doubl
     pack_f32(x, ldx, 0, k, kp, N, static_cast<float*>(scratch), s);
     sigma_csr_mixed(H, diag, static_cast<const float*>(scratch), kp, k, y, ldy, s);
   } else {
-    pack_f64(x, ldx, 0, k, kp, N, static_cast<double*>(scratch), s);
-    sigma_csr_f64(H, diag, static_cast<const double*>(scratch), kp, k, y, ldy, H.v64.p == nullptr, s);
+    if (H.v64.p) {
+      pack_f64(x, ldx, 0, k, kp, N, static_cast<double*>(scratch), s);
+      sigma_csr_f64(H, diag, static_cast<const double*>(scratch), kp, k, y, ldy, false, s);
+    } else {  // head + tail values: float-float refinement sigma (same 8 bytes per entry)
+      pack_ff(x, ldx, 0, k, kp, N, static_cast<float*>(scratch), s);
+      sigma_csr_ff(H, diag, static_cast<const float*>(scratch), kp, x, ldx, 0, k, y, ldy, s);
+    }
   }
 }
 
