@@ -13,6 +13,7 @@
 // The Davidson kernels (Gram products, Ritz combinations, residuals and the
 // diagonal preconditioner of SHCI/Davidson.cpp:85-106) reduce in a fixed
 // order, so results do not depend on scheduling.
+#include <cstdlib>
 #include <mutex>
 
 #include "ham.h"
@@ -83,19 +84,89 @@ struct VecF<4> {
   }
 };
 
+// Row walk shared by the stored-matrix sigma kernels; every lane of a warp
+// sees the same sequence of row groups (32 / VW rows, VW lanes each), so the
+// width-VW shuffles always run on full warps.
+//
+// Single vector (kBalanced): block b owns the contiguous rows whose nonzeros
+// fall in the b-th equal share of all nonzeros -- equal work per block
+// whatever the row lengths -- and its warps take the next rows of that range
+// from a shared-memory counter. Consecutive rows of the determinant order are
+// close determinants with largely the same connections, so the rows one block
+// runs together gather the same parts of x and hit in L1 (launched as two
+// 1024-thread blocks per SM, one wave).
+// Several vectors: the grid strides over the rows (x is k times larger and
+// the band of rows the whole GPU works on at once is what stays in cache).
+__device__ __forceinline__ size_t lower_bound_i64(const int64_t* __restrict__ a, size_t n, int64_t v) {
+  size_t lo = 0, hi = n;
+  while (lo < hi) {
+    const size_t mid = (lo + hi) >> 1;
+    if (a[mid] < v)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+template <int VW, bool kBalanced>
+struct RowWalk;
+template <int VW>
+struct RowWalk<VW, true> {
+  unsigned long long* next;
+  unsigned long long end;
+  __device__ RowWalk(const int64_t* __restrict__ rowptr, size_t N, unsigned long long* sh) : next(sh) {
+    if (threadIdx.x == 0) {
+      const int64_t nnz = rowptr[N];
+      const int64_t g = (int64_t)gridDim.x, b = (int64_t)blockIdx.x;
+      const size_t r0 = lower_bound_i64(rowptr, N + 1, nnz / g * b + nnz % g * b / g);
+      size_t r1 = b + 1 == g ? N : lower_bound_i64(rowptr, N + 1, nnz / g * (b + 1) + nnz % g * (b + 1) / g);
+      if (r1 > N) r1 = N;
+      sh[0] = r0 < r1 ? r0 : r1;
+      sh[1] = r1;
+    }
+    __syncthreads();
+    end = sh[1];
+  }
+  __device__ unsigned long long grab() {
+    unsigned long long w = 0;
+    if ((threadIdx.x & 31) == 0) w = atomicAdd(next, (unsigned long long)(32 / VW));
+    return __shfl_sync(kFull, w, 0);
+  }
+};
+template <int VW>
+struct RowWalk<VW, false> {
+  unsigned long long cur, stride, end;
+  __device__ RowWalk(const int64_t* __restrict__, size_t N, unsigned long long*) {
+    cur = (((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * (32 / VW);
+    stride = ((unsigned long long)gridDim.x * blockDim.x >> 5) * (32 / VW);
+    end = N;
+  }
+  __device__ unsigned long long grab() {
+    const unsigned long long w = cur;
+    cur += stride;
+    return w;
+  }
+};
+
+#define ROW_LOOP_BEGIN                                                      \
+  __shared__ unsigned long long s_walk[2];                                  \
+  RowWalk<VW, KP == 1> walk(rowptr, N, s_walk);                             \
+  const int sub = threadIdx.x & (VW - 1);                                   \
+  for (unsigned long long wr = walk.grab(); wr < walk.end; wr = walk.grab()) { \
+    const size_t pos = wr + (threadIdx.x & 31) / VW;                        \
+    const bool live = pos < walk.end;                                       \
+    const size_t r = live ? pos : 0;
+
 template <int VW, int KP>
-__global__ void __launch_bounds__(256) k_sigma_mixed(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+__global__ void __launch_bounds__(KP == 1 ? 1024 : 256) k_sigma_mixed(const int64_t* __restrict__ rowptr,
+                                                     const int32_t* __restrict__ col,
                                                      const float* __restrict__ val, const double* __restrict__ diag,
                                                      const float* __restrict__ x, size_t N, int k,
                                                      double* __restrict__ y, size_t ldy) {
-  // The row loop is uniform per warp (rows past N run empty) so that the
-  // width-VW shuffles below always see all 32 lanes.
-  const int sub = threadIdx.x & (VW - 1);
-  const size_t rows_per_warp = 32 / VW;
-  const size_t stride = ((size_t)gridDim.x * blockDim.x / 32) * rows_per_warp;
-  for (size_t wr = (((size_t)blockIdx.x * blockDim.x + threadIdx.x) / 32) * rows_per_warp; wr < N; wr += stride) {
-    const size_t r = wr + (threadIdx.x & 31) / VW;
-    const bool live = r < N;
+  // The row loop is uniform per warp (rows past the slice run empty) so that
+  // the width-VW shuffles below always see all 32 lanes.
+  ROW_LOOP_BEGIN
     Acc acc[KP];
 #pragma unroll
     for (int c = 0; c < KP; ++c) acc[c] = Acc{0.f, 0.f};
@@ -141,17 +212,13 @@ __global__ void __launch_bounds__(256) k_sigma_mixed(const int64_t* __restrict__
 }
 
 template <int VW, int KP, bool HILO>
-__global__ void __launch_bounds__(256) k_sigma_f64(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+__global__ void __launch_bounds__(KP == 1 ? 1024 : 256) k_sigma_f64(const int64_t* __restrict__ rowptr,
+                                                   const int32_t* __restrict__ col,
                                                    const double* __restrict__ v64, const float* __restrict__ vhi,
                                                    const float* __restrict__ vlo, const double* __restrict__ diag,
                                                    const double* __restrict__ x, size_t N, int k,
                                                    double* __restrict__ y, size_t ldy) {
-  const int sub = threadIdx.x & (VW - 1);
-  const size_t rows_per_warp = 32 / VW;
-  const size_t stride = ((size_t)gridDim.x * blockDim.x / 32) * rows_per_warp;
-  for (size_t wr = (((size_t)blockIdx.x * blockDim.x + threadIdx.x) / 32) * rows_per_warp; wr < N; wr += stride) {
-    const size_t r = wr + (threadIdx.x & 31) / VW;
-    const bool live = r < N;
+  ROW_LOOP_BEGIN
     double acc[KP];
 #pragma unroll
     for (int c = 0; c < KP; ++c) acc[c] = 0.0;
@@ -241,18 +308,14 @@ struct VecFF<4> {
 };
 
 template <int VW, int KP>
-__global__ void __launch_bounds__(256) k_sigma_ff(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+__global__ void __launch_bounds__(KP == 1 ? 1024 : 256) k_sigma_ff(const int64_t* __restrict__ rowptr,
+                                                  const int32_t* __restrict__ col,
                                                   const float* __restrict__ vhi, const float* __restrict__ vlo,
                                                   const double* __restrict__ diag, const float* __restrict__ xff,
                                                   const double* __restrict__ xd, size_t ldx, int c0, size_t N, int k,
                                                   double* __restrict__ y, size_t ldy) {
   // same row mapping as k_sigma_mixed
-  const int sub = threadIdx.x & (VW - 1);
-  const size_t rows_per_warp = 32 / VW;
-  const size_t stride = ((size_t)gridDim.x * blockDim.x / 32) * rows_per_warp;
-  for (size_t wr = (((size_t)blockIdx.x * blockDim.x + threadIdx.x) / 32) * rows_per_warp; wr < N; wr += stride) {
-    const size_t r = wr + (threadIdx.x & 31) / VW;
-    const bool live = r < N;
+  ROW_LOOP_BEGIN
     Acc acc[KP];
 #pragma unroll
     for (int c = 0; c < KP; ++c) acc[c] = Acc{0.f, 0.f};
@@ -295,6 +358,27 @@ __global__ void __launch_bounds__(256) k_sigma_ff(const int64_t* __restrict__ ro
   }
 }
 
+// Launch shape of the stored-matrix sigma kernels (see RowWalk): one vector
+// runs as two 1024-thread blocks per SM over nonzero-balanced row ranges;
+// several vectors as a grid-strided launch of 256-thread blocks.
+struct SigmaLaunch {
+  unsigned blocks;
+  int threads;
+};
+static int sm_count() {
+  static int n = [] {
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      v = 152;
+    return v > 0 ? v : 152;
+  }();
+  return n;
+}
+static SigmaLaunch sigma_launch(size_t N, int vw, int kp) {
+  if (kp == 1) return SigmaLaunch{(unsigned)(2 * sm_count()), 1024};
+  return SigmaLaunch{grid_for(N * (size_t)vw, 256, (size_t)sm_count() * 16), 256};
+}
+
 static int pick_vw(const Csr& H) {
   double avg = H.N ? (double)H.nnz / (double)H.N : 0.0;
   if (avg >= 96) return 32;
@@ -306,13 +390,12 @@ static int pick_vw(const Csr& H) {
 template <int KP>
 static void launch_mixed(int vw, const Csr& H, const double* diag, const float* x, int k, double* y, size_t ldy,
                          cudaStream_t s) {
-  const size_t threads = H.N * (size_t)vw;
-  const unsigned blocks = grid_for(threads, 256, 152 * 16);
+  const SigmaLaunch L = sigma_launch(H.N, vw, KP);
   switch (vw) {
-    case 32: k_sigma_mixed<32, KP><<<blocks, 256, 0, s>>>(H.rowptr.p, H.col.p, H.vhi.p, diag, x, H.N, k, y, ldy); break;
-    case 16: k_sigma_mixed<16, KP><<<blocks, 256, 0, s>>>(H.rowptr.p, H.col.p, H.vhi.p, diag, x, H.N, k, y, ldy); break;
-    case 8: k_sigma_mixed<8, KP><<<blocks, 256, 0, s>>>(H.rowptr.p, H.col.p, H.vhi.p, diag, x, H.N, k, y, ldy); break;
-    default: k_sigma_mixed<4, KP><<<blocks, 256, 0, s>>>(H.rowptr.p, H.col.p, H.vhi.p, diag, x, H.N, k, y, ldy); break;
+    case 32: k_sigma_mixed<32, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, H.vhi.p, diag, x, H.N, k, y, ldy); break;
+    case 16: k_sigma_mixed<16, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, H.vhi.p, diag, x, H.N, k, y, ldy); break;
+    case 8: k_sigma_mixed<8, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, H.vhi.p, diag, x, H.N, k, y, ldy); break;
+    default: k_sigma_mixed<4, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, H.vhi.p, diag, x, H.N, k, y, ldy); break;
   }
   SHCI_LAUNCH_CHECK();
 }
@@ -333,15 +416,14 @@ void sigma_csr_mixed(const Csr& H, const double* diag, const float* x32, int kp,
 template <int KP, bool HILO>
 static void launch_f64(int vw, const Csr& H, const double* diag, const double* x, int k, double* y, size_t ldy,
                        cudaStream_t s) {
-  const size_t threads = H.N * (size_t)vw;
-  const unsigned blocks = grid_for(threads, 256, 152 * 16);
+  const SigmaLaunch L = sigma_launch(H.N, vw, KP);
   const double* v64 = H.v64.p;
   const float *vhi = H.vhi.p, *vlo = H.vlo.p;
   switch (vw) {
-    case 32: k_sigma_f64<32, KP, HILO><<<blocks, 256, 0, s>>>(H.rowptr.p, H.col.p, v64, vhi, vlo, diag, x, H.N, k, y, ldy); break;
-    case 16: k_sigma_f64<16, KP, HILO><<<blocks, 256, 0, s>>>(H.rowptr.p, H.col.p, v64, vhi, vlo, diag, x, H.N, k, y, ldy); break;
-    case 8: k_sigma_f64<8, KP, HILO><<<blocks, 256, 0, s>>>(H.rowptr.p, H.col.p, v64, vhi, vlo, diag, x, H.N, k, y, ldy); break;
-    default: k_sigma_f64<4, KP, HILO><<<blocks, 256, 0, s>>>(H.rowptr.p, H.col.p, v64, vhi, vlo, diag, x, H.N, k, y, ldy); break;
+    case 32: k_sigma_f64<32, KP, HILO><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, v64, vhi, vlo, diag, x, H.N, k, y, ldy); break;
+    case 16: k_sigma_f64<16, KP, HILO><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, v64, vhi, vlo, diag, x, H.N, k, y, ldy); break;
+    case 8: k_sigma_f64<8, KP, HILO><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, v64, vhi, vlo, diag, x, H.N, k, y, ldy); break;
+    default: k_sigma_f64<4, KP, HILO><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, v64, vhi, vlo, diag, x, H.N, k, y, ldy); break;
   }
   SHCI_LAUNCH_CHECK();
 }
@@ -372,14 +454,13 @@ void sigma_csr_f64(const Csr& H, const double* diag, const double* x64, int kp, 
 template <int KP>
 static void launch_ff(int vw, const Csr& H, const double* diag, const float* xff, const double* xd, size_t ldx, int c0,
                       int k, double* y, size_t ldy, cudaStream_t s) {
-  const size_t threads = H.N * (size_t)vw;
-  const unsigned blocks = grid_for(threads, 256, 152 * 16);
+  const SigmaLaunch L = sigma_launch(H.N, vw, KP);
   const float *vhi = H.vhi.p, *vlo = H.vlo.p;
   switch (vw) {
-    case 32: k_sigma_ff<32, KP><<<blocks, 256, 0, s>>>(H.rowptr.p, H.col.p, vhi, vlo, diag, xff, xd, ldx, c0, H.N, k, y, ldy); break;
-    case 16: k_sigma_ff<16, KP><<<blocks, 256, 0, s>>>(H.rowptr.p, H.col.p, vhi, vlo, diag, xff, xd, ldx, c0, H.N, k, y, ldy); break;
-    case 8: k_sigma_ff<8, KP><<<blocks, 256, 0, s>>>(H.rowptr.p, H.col.p, vhi, vlo, diag, xff, xd, ldx, c0, H.N, k, y, ldy); break;
-    default: k_sigma_ff<4, KP><<<blocks, 256, 0, s>>>(H.rowptr.p, H.col.p, vhi, vlo, diag, xff, xd, ldx, c0, H.N, k, y, ldy); break;
+    case 32: k_sigma_ff<32, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, vhi, vlo, diag, xff, xd, ldx, c0, H.N, k, y, ldy); break;
+    case 16: k_sigma_ff<16, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, vhi, vlo, diag, xff, xd, ldx, c0, H.N, k, y, ldy); break;
+    case 8: k_sigma_ff<8, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, vhi, vlo, diag, xff, xd, ldx, c0, H.N, k, y, ldy); break;
+    default: k_sigma_ff<4, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, vhi, vlo, diag, xff, xd, ldx, c0, H.N, k, y, ldy); break;
   }
   SHCI_LAUNCH_CHECK();
 }
