@@ -896,35 +896,16 @@ struct Context {
     teacher.resize(ndet);
     pt2_shift(H, diag.p, E, teacher.p, stream);
     const int64_t ns = std::min<int64_t>(mlp_sample, (int64_t)ndet);
-    std::vector<int32_t> idx(ndet);
-    std::iota(idx.begin(), idx.end(), 0);
-    uint64_t st = 0x2545F4914F6CDD1Dull ^ (uint64_t)ndet;
-    for (int64_t i = (int64_t)ndet - 1; i > 0; --i) {  // Fisher-Yates with xorshift
-      st ^= st << 13;
-      st ^= st >> 7;
-      st ^= st << 17;
-      std::swap(idx[i], idx[st % (uint64_t)(i + 1)]);
-    }
-    idx.resize(ns);
-    std::vector<double> t(ndet);
-    SHCI_CUDA(cudaMemcpyAsync(t.data(), teacher.p, ndet * sizeof(double), cudaMemcpyDeviceToHost, stream));
-    SHCI_CUDA(cudaStreamSynchronize(stream));
-    double rms = 0.0;
-    for (int32_t i : idx) rms += t[i] * t[i];
-    rms = std::sqrt(rms / std::max<int64_t>(1, ns));
-    if (!(rms > 0.0)) rms = 1.0;
-    mlp.sigma = rms;
-    std::vector<float> tg(ns);
-    for (int64_t k = 0; k < ns; ++k) tg[k] = (float)(t[idx[k]] / rms);
+    // rows drawn on the device (hashed, with replacement), targets scaled to unit rms
     tr_idx.resize(ns);
     tr_tgt.resize(ns);
-    SHCI_CUDA(cudaMemcpyAsync(tr_idx.p, idx.data(), ns * sizeof(int32_t), cudaMemcpyHostToDevice, stream));
-    SHCI_CUDA(cudaMemcpyAsync(tr_tgt.p, tg.data(), ns * sizeof(float), cudaMemcpyHostToDevice, stream));
+    mlp.sigma = shci::mlp_sample(teacher.p, ndet, ns, 0x2545F4914F6CDD1Dull ^ (uint64_t)ndet, tr_idx.p, tr_tgt.p,
+                                 gpart, stream);
     const int B = (int)std::min<int64_t>(mlp_batch, ns);
     double loss = 0.0;
     for (int s = 0; s < mlp_steps; ++s) {
       const int64_t off = ((int64_t)s * B) % std::max<int64_t>(1, ns - B + 1);
-      loss = mlp.gradient(dets.p, diag.p, tr_idx.p + off, tr_tgt.p + off, B, E, stream);
+      loss = mlp.gradient(dets.p, diag.p, tr_idx.p + off, tr_tgt.p + off, B, E, stream, s + 1 == mlp_steps);
       mlp.adam(mlp_lr, stream);
     }
     SHCI_CUDA(cudaStreamSynchronize(stream));

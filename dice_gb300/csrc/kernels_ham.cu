@@ -152,11 +152,13 @@ static void build_groups(const uint64_t* str_of_det, const uint64_t* partner_of_
   (void)str_of_det;
 }
 
-// Key of a partial string: alpha group g with the beta string bpart (one
-// electron removed). A splitmix64-style mix; lookups verify every candidate,
-// so a collision costs a wasted probe, never a wrong connection.
-__device__ __forceinline__ uint64_t partial_key(uint32_t g, uint64_t bpart) {
-  uint64_t z = bpart + 0x9E3779B97F4A7C15ull * ((uint64_t)g + 1ull);
+// Hash of a partial string: alpha group g with the beta string bpart (one
+// electron removed), splitmix64-style. Entries are compared on their exact
+// fields; the build checks that no two different keys share a hash (and
+// re-salts if they do), so equal keys are always contiguous.
+constexpr uint32_t kM1GroupBits = 26;
+__device__ __forceinline__ uint64_t partial_key(uint32_t g, uint64_t bpart, uint64_t salt) {
+  uint64_t z = bpart + 0x9E3779B97F4A7C15ull * ((uint64_t)g + 1ull) + salt;
   z ^= z >> 30;
   z *= 0xBF58476D1CE4E5B9ull;
   z ^= z >> 27;
@@ -170,18 +172,36 @@ __global__ void k_m1_count(const uint64_t* __restrict__ bstr, size_t n, int64_t*
     cnt[i] = __popcll(bstr[i]);
 }
 __global__ void k_m1_fill(const uint64_t* __restrict__ bstr, const uint32_t* __restrict__ aidx, size_t n,
-                          const int64_t* __restrict__ off, uint64_t* __restrict__ key, uint32_t* __restrict__ det) {
+                          const int64_t* __restrict__ off, uint64_t salt, uint64_t* __restrict__ key,
+                          uint32_t* __restrict__ perm, uint4* __restrict__ ent) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     const uint64_t B = bstr[i];
     const uint32_t g = aidx[i];
     int64_t q = off[i];
     for (uint64_t r = B; r; r &= r - 1) {
-      const uint64_t bit = r & (~r + 1ull);
-      key[q] = partial_key(g, B ^ bit);
-      det[q] = (uint32_t)i;
+      const int b = __ffsll((long long)r) - 1;
+      const uint64_t bm = B ^ (1ull << b);
+      key[q] = partial_key(g, bm, salt);
+      perm[q] = (uint32_t)q;
+      ent[q] = make_uint4((uint32_t)bm, (uint32_t)(bm >> 32), g | ((uint32_t)b << kM1GroupBits), (uint32_t)i);
       ++q;
     }
   }
+}
+__global__ void k_m1_permute(const uint4* __restrict__ src, const uint32_t* __restrict__ perm, int64_t n,
+                             uint4* __restrict__ dst) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+    dst[k] = src[perm[k]];
+}
+// flag if two adjacent entries share a hash but not their (group, partial string)
+__global__ void k_m1_collisions(const uint64_t* __restrict__ key, const uint4* __restrict__ ent, int64_t n,
+                                int* __restrict__ flag) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x + 1; k < n; k += (int64_t)gridDim.x * blockDim.x)
+    if (key[k] == key[k - 1]) {
+      const uint4 a = ent[k], b = ent[k - 1];
+      const uint32_t mask = (1u << kM1GroupBits) - 1u;
+      if (a.x != b.x || a.y != b.y || (a.z & mask) != (b.z & mask)) atomicOr(flag, 1);
+    }
 }
 // dir[p] = first entry whose key's top `bits` bits are >= p, p in [0, 2^bits]
 __global__ void k_m1_dir(const uint64_t* __restrict__ key, int64_t n, int bits, uint32_t* __restrict__ dir) {
@@ -241,18 +261,40 @@ void Helpers::build(const Det2* dets, size_t n, int norb, Prims& pr, cudaStream_
     int64_t ne = 0;
     scan_exclusive_i64(c1.p, o1.p, n, &ne, pr, s);
     if (ne >= ((int64_t)1 << 32)) throw Error(kErrInvalid, "partial-string index too large");
+    if (NA >= ((int64_t)1 << kM1GroupBits)) throw Error(kErrInvalid, "too many alpha strings for the partial-string index");
     nm1 = ne;
     if (ne > 0) {
-      m1key.resize(ne);
-      m1det.resize(ne);
-      k_m1_fill<<<grid_for(n, 256), 256, 0, s>>>(bstr.p, aidx.p, n, o1.p, m1key.p, m1det.p);
-      SHCI_LAUNCH_CHECK();
-      sort_u64(m1key.p, m1det.p, (size_t)ne, pr, s);
+      DevBuf<uint64_t> key;
+      DevBuf<uint32_t> perm;
+      DevBuf<uint4> raw;
+      DevBuf<int> flag;
+      key.resize(ne);
+      perm.resize(ne);
+      raw.resize(ne);
+      m1ent.resize(ne);
+      flag.resize(1);
+      const unsigned eb = grid_for((size_t)ne, 256);
+      for (int attempt = 0;; ++attempt) {
+        m1salt = (uint64_t)attempt * 0xD1B54A32D192ED03ull;
+        k_m1_fill<<<grid_for(n, 256), 256, 0, s>>>(bstr.p, aidx.p, n, o1.p, m1salt, key.p, perm.p, raw.p);
+        SHCI_LAUNCH_CHECK();
+        sort_u64(key.p, perm.p, (size_t)ne, pr, s);
+        k_m1_permute<<<eb, 256, 0, s>>>(raw.p, perm.p, ne, m1ent.p);
+        SHCI_LAUNCH_CHECK();
+        SHCI_CUDA(cudaMemsetAsync(flag.p, 0, sizeof(int), s));
+        k_m1_collisions<<<eb, 256, 0, s>>>(key.p, m1ent.p, ne, flag.p);
+        SHCI_LAUNCH_CHECK();
+        int h = 0;
+        SHCI_CUDA(cudaMemcpyAsync(&h, flag.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+        SHCI_CUDA(cudaStreamSynchronize(s));
+        if (!h) break;
+        if (attempt == 7) throw Error(kErrInvalid, "partial-string index: hash collisions persist");
+      }
       int bits = 4;
-      while (bits < 28 && ((int64_t)1 << bits) < ne) ++bits;  // about one entry per bucket
+      while (bits < 28 && ((int64_t)2 << bits) < ne) ++bits;  // about two entries per bucket
       m1bits = bits;
       m1dir.resize(((size_t)1 << bits) + 1);
-      k_m1_dir<<<grid_for(((size_t)1 << bits) + 1, 256), 256, 0, s>>>(m1key.p, ne, bits, m1dir.p);
+      k_m1_dir<<<grid_for(((size_t)1 << bits) + 1, 256), 256, 0, s>>>(key.p, ne, bits, m1dir.p);
       SHCI_LAUNCH_CHECK();
     }
   }
@@ -286,7 +328,7 @@ __device__ void visit_row(const HelperView& h, uint32_t I, V& v) {
   }
   // 2. alpha single excitation: beta equal (single alpha) or beta single
   // (alpha-beta double), from the partial-string index
-  if (h.m1key != nullptr && B != 0) {
+  if (h.m1ent != nullptr && B != 0) {
     const int64_t s0 = h.aSingStart[ia], s1 = h.aSingStart[ia + 1];
     const int nb = __popcll(B);
     const int64_t nprobe = (s1 - s0) * nb;
@@ -295,23 +337,29 @@ __device__ void visit_row(const HelperView& h, uint32_t I, V& v) {
       const int64_t t = base + lane;
       // each lane locates the entries of its key (As, B - b)
       int64_t lo = 0, len = 0;
-      uint32_t As = 0;
-      uint64_t Bm = 0;
+      int bq = 0;  // the beta orbital removed by this probe
       bool first_b = false;
       if (t < nprobe) {
-        As = h.aSing[s0 + t / nb];
+        const uint32_t As = h.aSing[s0 + t / nb];
         const int which = (int)(t % nb);
         uint64_t r = B;
         for (int k = 0; k < which; ++k) r &= r - 1;
-        Bm = B ^ (r & (~r + 1ull));
+        bq = __ffsll((long long)r) - 1;
+        const uint64_t Bm = B ^ (1ull << bq);
         first_b = which == 0;
-        const uint64_t key = partial_key(As, Bm);
+        const uint64_t key = partial_key(As, Bm, h.m1salt);
         const uint32_t p = (uint32_t)(key >> shift);
         uint32_t e = h.m1dir[p];
         const uint32_t e1 = h.m1dir[p + 1];
-        while (e < e1 && h.m1key[e] < key) ++e;
+        const uint32_t lo32 = (uint32_t)Bm, hi32 = (uint32_t)(Bm >> 32);
+        const uint32_t gmask = (1u << kM1GroupBits) - 1u;
+        auto match = [&](uint32_t q) {
+          const uint4 en = h.m1ent[q];
+          return en.x == lo32 && en.y == hi32 && (en.z & gmask) == As;
+        };
+        while (e < e1 && !match(e)) ++e;
         uint32_t f = e;
-        while (f < e1 && h.m1key[f] == key) ++f;
+        while (f < e1 && match(f)) ++f;
         lo = e;
         len = f - e;
       }
@@ -335,22 +383,18 @@ __device__ void visit_row(const HelperView& h, uint32_t I, V& v) {
         }
         const int64_t elo = __shfl_sync(kFull, lo, src);
         const int64_t eo = __shfl_sync(kFull, excl, src);
-        const uint32_t as = __shfl_sync(kFull, As, src);
-        const uint64_t bm = __shfl_sync(kFull, Bm, src);
+        const int wb = __shfl_sync(kFull, bq, src);
         const bool fb = __shfl_sync(kFull, first_b, src);
         bool hit = false, single = false;
         uint32_t J = 0;
         if (f < total) {
-          J = h.m1det[elo + (f - eo)];
-          if (h.aidx[J] == as) {
-            const uint64_t BJ = h.bstr[J];
-            if ((BJ & bm) == bm) {
-              const int d = __popcll(BJ ^ B);
-              // beta equal: found once per occupied b, kept for the first
-              single = d == 0;
-              hit = single ? fb : d == 2;
-            }
-          }
+          // the entry holds J and the orbital b' its beta string has beyond
+          // B - b: b' == b means beta equal (found once per occupied b, kept
+          // for the first), otherwise a beta single excitation b -> b'
+          const uint4 en = h.m1ent[elo + (f - eo)];
+          J = en.w;
+          single = (int)(en.z >> kM1GroupBits) == wb;
+          hit = single ? fb : true;
         }
         v.step(hit, J, single);
       }
@@ -466,8 +510,11 @@ struct EmitVisitor {
       if (vlo) vlo[q] = (float)(hv - (double)hi);
     }
   }
-  // evaluate the first `cnt` (<= 32) entries of queue q, then shift the rest down
-  __device__ int drain(uint32_t* q, int n, int cnt) {
+  // evaluate the first `cnt` (<= 32) entries of queue q, then shift the rest
+  // down. Kept out of line: step() is inlined at every scan site and the
+  // Slater-Condon code would otherwise be copied into each (instruction-cache
+  // misses were the main stall of this kernel).
+  __device__ __noinline__ int drain(uint32_t* q, int n, int cnt) {
     const int lane = threadIdx.x & 31;
     if (lane < cnt) store(pos + lane, q[lane]);
     pos += cnt;
@@ -516,65 +563,127 @@ __global__ void __launch_bounds__(256) k_ham_emit(HelperView h, int64_t row0, co
 
 __global__ void k_set_last(int64_t* rowptr, int64_t n, int64_t total) { rowptr[n] = total; }
 
-// Bitonic sort of one row (columns with their values) in shared memory, one
-// block per row. Rows longer than kRowSortCap are left in emission order
-// (still correct, only with less gather locality in sigma).
+// Sort of one row by column, one block per row. The row's columns become
+// 64-bit keys (column << 12 | position in the row) sorted by a bitonic network
+// in which each of the 256 threads keeps E consecutive keys in registers: the
+// compare-exchange steps between keys of one thread run in registers, only
+// the longer-distance steps go through shared memory (36 of the 66 steps for
+// a 2048-key row). The values are then gathered from their old positions
+// (read into registers before any write, the row is sorted in place). Rows
+// longer than kRowSortCap are left in emission order (still correct, only
+// with less gather locality in sigma).
 constexpr int kRowSortCap = 4096;
+constexpr int kSortThreads = 256;
 
-__global__ void __launch_bounds__(256) k_row_sort(const int64_t* __restrict__ rowptr, size_t N, int32_t* __restrict__ col,
-                                                  double* __restrict__ v64, float* __restrict__ vhi,
-                                                  float* __restrict__ vlo) {
-  extern __shared__ unsigned char sm_raw[];
-  uint32_t* key = reinterpret_cast<uint32_t*>(sm_raw);
-  uint64_t* pay = reinterpret_cast<uint64_t*>(sm_raw + (size_t)kRowSortCap * sizeof(uint32_t));
+template <int E>
+__device__ __forceinline__ void sort_exchange_regs(uint64_t (&v)[E], int g0, int k) {
+  // the steps of merge size k with partner distance j < E: partner in the same thread
+#pragma unroll
+  for (int j = E >> 1; j > 0; j >>= 1) {
+    if (j >= k) continue;  // merges smaller than E start at j = k / 2
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const int pe = e ^ j;
+      if (pe > e) {
+        const bool up = ((g0 + e) & k) == 0;
+        const uint64_t x = v[e], y = v[pe];
+        if ((x > y) == up) {
+          v[e] = y;
+          v[pe] = x;
+        }
+      }
+    }
+  }
+}
+
+template <int E>
+__device__ void sort_row_keys(uint64_t* sk, int P) {
+  // threads [0, P/E) own keys [t*E, t*E+E); others only join the barriers
+  const int T = P / E;
+  const int t = threadIdx.x;
+  const bool act = t < T;
+  const int g0 = t * E;
+  uint64_t v[E];
+  for (int k = 2; k <= P; k <<= 1) {
+    // distances j >= E: pairs in shared memory
+    for (int j = k >> 1; j >= E; j >>= 1) {
+      for (int q = t; q < P / 2; q += blockDim.x) {
+        const int lo = ((q / j) * 2 * j) + (q % j);  // lower index of the q-th pair
+        const int hi = lo + j;
+        const bool up = (lo & k) == 0;
+        const uint64_t x = sk[lo], y = sk[hi];
+        if ((x > y) == up) {
+          sk[lo] = y;
+          sk[hi] = x;
+        }
+      }
+      __syncthreads();
+    }
+    // distances j < E: in registers
+    if (E > 1) {
+      if (act) {
+#pragma unroll
+        for (int e = 0; e < E; ++e) v[e] = sk[g0 + e];
+        sort_exchange_regs<E>(v, g0, k);
+#pragma unroll
+        for (int e = 0; e < E; ++e) sk[g0 + e] = v[e];
+      }
+      __syncthreads();
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_row_sort(const int64_t* __restrict__ rowptr, size_t N,
+                                                           int32_t* __restrict__ col, double* __restrict__ v64,
+                                                           float* __restrict__ vhi, float* __restrict__ vlo) {
+  __shared__ uint64_t sk[kRowSortCap];
+  constexpr int kPer = kRowSortCap / kSortThreads;  // values gathered per thread
   for (size_t r = blockIdx.x; r < N; r += gridDim.x) {
     const int64_t p0 = rowptr[r], len = rowptr[r + 1] - p0;
     if (len <= 1 || len > kRowSortCap) continue;  // uniform across the block
     int P = 2;
     while (P < len) P <<= 1;
-    for (int i = threadIdx.x; i < P; i += blockDim.x) {
+    for (int i = threadIdx.x; i < P; i += blockDim.x)
+      sk[i] = i < len ? ((uint64_t)(uint32_t)col[p0 + i] << 12) | (uint64_t)i : ~0ull;
+    __syncthreads();
+    if (P >= 16 * kSortThreads)
+      sort_row_keys<16>(sk, P);
+    else if (P >= 8 * kSortThreads)
+      sort_row_keys<8>(sk, P);
+    else if (P >= 4 * kSortThreads)
+      sort_row_keys<4>(sk, P);
+    else if (P >= 2 * kSortThreads)
+      sort_row_keys<2>(sk, P);
+    else
+      sort_row_keys<1>(sk, P);
+    // gather the values of this thread's output positions, then write
+    uint64_t pay[kPer];
+#pragma unroll
+    for (int m = 0; m < kPer; ++m) {
+      const int i = threadIdx.x + m * kSortThreads;
+      pay[m] = 0;
       if (i < len) {
-        key[i] = (uint32_t)col[p0 + i];
-        uint64_t v;
+        const int src = (int)(sk[i] & 0xFFFull);
         if (v64) {
-          v = (uint64_t)__double_as_longlong(v64[p0 + i]);
+          pay[m] = (uint64_t)__double_as_longlong(v64[p0 + src]);
         } else {
-          v = (uint64_t)__float_as_uint(vhi[p0 + i]);
-          if (vlo) v |= (uint64_t)__float_as_uint(vlo[p0 + i]) << 32;
+          pay[m] = (uint64_t)__float_as_uint(vhi[p0 + src]);
+          if (vlo) pay[m] |= (uint64_t)__float_as_uint(vlo[p0 + src]) << 32;
         }
-        pay[i] = v;
-      } else {
-        key[i] = 0xffffffffu;
-        pay[i] = 0;
       }
     }
     __syncthreads();
-    for (int k = 2; k <= P; k <<= 1)
-      for (int j = k >> 1; j > 0; j >>= 1) {
-        for (int i = threadIdx.x; i < P; i += blockDim.x) {
-          const int ixj = i ^ j;
-          if (ixj > i) {
-            const bool up = (i & k) == 0;
-            const uint32_t a = key[i], b = key[ixj];
-            if ((a > b) == up) {
-              key[i] = b;
-              key[ixj] = a;
-              const uint64_t t = pay[i];
-              pay[i] = pay[ixj];
-              pay[ixj] = t;
-            }
-          }
+#pragma unroll
+    for (int m = 0; m < kPer; ++m) {
+      const int i = threadIdx.x + m * kSortThreads;
+      if (i < len) {
+        col[p0 + i] = (int32_t)(sk[i] >> 12);
+        if (v64) {
+          v64[p0 + i] = __longlong_as_double((long long)pay[m]);
+        } else {
+          vhi[p0 + i] = __uint_as_float((uint32_t)pay[m]);
+          if (vlo) vlo[p0 + i] = __uint_as_float((uint32_t)(pay[m] >> 32));
         }
-        __syncthreads();
-      }
-    for (int i = threadIdx.x; i < len; i += blockDim.x) {
-      col[p0 + i] = (int32_t)key[i];
-      const uint64_t v = pay[i];
-      if (v64) {
-        v64[p0 + i] = __longlong_as_double((long long)v);
-      } else {
-        vhi[p0 + i] = __uint_as_float((uint32_t)v);
-        if (vlo) vlo[p0 + i] = __uint_as_float((uint32_t)(v >> 32));
       }
     }
     __syncthreads();
@@ -591,10 +700,8 @@ struct CsrVals {
 
 static void sort_rows(const int64_t* rowptr, size_t n, const CsrVals& v, cudaStream_t s) {
   if (n == 0) return;
-  const size_t smem = (size_t)kRowSortCap * (sizeof(uint32_t) + sizeof(uint64_t));
-  SHCI_CUDA(cudaFuncSetAttribute(k_row_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  const unsigned sblocks = (unsigned)std::min<size_t>(n, 152 * 8);
-  k_row_sort<<<sblocks, 256, smem, s>>>(rowptr, n, v.col, v.v64, v.vhi, v.vlo);
+  const unsigned sblocks = (unsigned)std::min<size_t>(n, 152 * 6);
+  k_row_sort<<<sblocks, kSortThreads, 0, s>>>(rowptr, n, v.col, v.v64, v.vhi, v.vlo);
   SHCI_LAUNCH_CHECK();
 }
 

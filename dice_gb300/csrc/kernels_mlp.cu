@@ -304,8 +304,57 @@ MlpView Mlp::view() const {
 
 constexpr int kGradBlocks = 152 * 2;
 
+constexpr unsigned kSampleBlocks = 152;
+__global__ void k_mlp_sample(const double* __restrict__ teacher, size_t N, int64_t ns, uint64_t seed,
+                             int32_t* __restrict__ idx, float* __restrict__ tgt, double* __restrict__ part) {
+  __shared__ double red[8];
+  double ss = 0.0;
+  const int64_t per = (ns + gridDim.x - 1) / gridDim.x;
+  const int64_t k0 = (int64_t)blockIdx.x * per, k1 = k0 + per < ns ? k0 + per : ns;
+  for (int64_t k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+    const size_t i = (size_t)(mix64(seed ^ (0x9E3779B97F4A7C15ull * (uint64_t)(k + 1))) % N);
+    const double t = teacher[i];
+    idx[k] = (int32_t)i;
+    tgt[k] = (float)t;
+    ss += t * t;
+  }
+  for (int o = 16; o; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = ss;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double v = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += red[w];
+    part[blockIdx.x] = v;
+  }
+}
+__global__ void k_mlp_scale_targets(float* __restrict__ tgt, int64_t ns, const double* __restrict__ part, int np) {
+  double ss = 0.0;
+  for (int b = 0; b < np; ++b) ss += part[b];
+  double rms = ns > 0 ? sqrt(ss / (double)ns) : 1.0;
+  if (!(rms > 0.0)) rms = 1.0;
+  const float inv = (float)(1.0 / rms);
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < ns; k += (int64_t)gridDim.x * blockDim.x)
+    tgt[k] *= inv;
+}
+double mlp_sample(const double* teacher, size_t N, int64_t ns, uint64_t seed, int32_t* idx, float* tgt,
+                  DevBuf<double>& part, cudaStream_t s) {
+  if (N == 0 || ns <= 0) return 1.0;
+  part.reserve(kSampleBlocks);
+  k_mlp_sample<<<kSampleBlocks, 256, 0, s>>>(teacher, N, ns, seed, idx, tgt, part.p);
+  SHCI_LAUNCH_CHECK();
+  k_mlp_scale_targets<<<kSampleBlocks, 256, 0, s>>>(tgt, ns, part.p, (int)kSampleBlocks);
+  SHCI_LAUNCH_CHECK();
+  std::vector<double> h(kSampleBlocks);
+  SHCI_CUDA(cudaMemcpyAsync(h.data(), part.p, kSampleBlocks * sizeof(double), cudaMemcpyDeviceToHost, s));
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  double ss = 0.0;
+  for (double v : h) ss += v;
+  double rms = std::sqrt(ss / (double)ns);
+  return rms > 0.0 ? rms : 1.0;
+}
+
 float Mlp::gradient(const Det2* dets, const double* diag, const int32_t* idx, const float* target, int B, double E,
-                    cudaStream_t s) {
+                    cudaStream_t s, bool want_loss) {
   const size_t smem = mlp_grad_smem(F);
   SHCI_CUDA(cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int nb = std::min(kGradBlocks, std::max(1, B));
@@ -315,6 +364,7 @@ float Mlp::gradient(const Det2* dets, const double* diag, const int32_t* idx, co
   SHCI_LAUNCH_CHECK();
   k_mlp_grad_sum<<<(nparam + 255) / 256, 256, 0, s>>>(part.p, nb, nparam, grad.p);
   SHCI_LAUNCH_CHECK();
+  if (!want_loss) return std::nanf("");
   std::vector<float> lp(nb);
   SHCI_CUDA(cudaMemcpyAsync(lp.data(), lpart.p, nb * sizeof(float), cudaMemcpyDeviceToHost, s));
   SHCI_CUDA(cudaStreamSynchronize(s));

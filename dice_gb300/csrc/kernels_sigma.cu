@@ -109,54 +109,48 @@ __device__ __forceinline__ size_t lower_bound_i64(const int64_t* __restrict__ a,
   return lo;
 }
 
-template <int VW, bool kBalanced>
-struct RowWalk;
-template <int VW>
-struct RowWalk<VW, true> {
-  unsigned long long* next;
-  unsigned long long end;
-  __device__ RowWalk(const int64_t* __restrict__ rowptr, size_t N, unsigned long long* sh) : next(sh) {
+template <int VW, bool kBalanced, class F>
+__device__ __forceinline__ void run_rows(const int64_t* __restrict__ rowptr, size_t N, F& row) {
+  if constexpr (kBalanced) {
+    __shared__ unsigned long long s_next, s_end;
     if (threadIdx.x == 0) {
       const int64_t nnz = rowptr[N];
       const int64_t g = (int64_t)gridDim.x, b = (int64_t)blockIdx.x;
       const size_t r0 = lower_bound_i64(rowptr, N + 1, nnz / g * b + nnz % g * b / g);
       size_t r1 = b + 1 == g ? N : lower_bound_i64(rowptr, N + 1, nnz / g * (b + 1) + nnz % g * (b + 1) / g);
       if (r1 > N) r1 = N;
-      sh[0] = r0 < r1 ? r0 : r1;
-      sh[1] = r1;
+      s_next = r0 < r1 ? r0 : r1;
+      s_end = r1;
     }
     __syncthreads();
-    end = sh[1];
+    const unsigned long long end = s_end;
+    while (true) {
+      unsigned long long wr = 0;
+      if ((threadIdx.x & 31) == 0) wr = atomicAdd(&s_next, (unsigned long long)(32 / VW));
+      wr = __shfl_sync(kFull, wr, 0);
+      if (wr >= end) break;
+      const size_t pos = wr + (threadIdx.x & 31) / VW;
+      row(pos < end ? pos : 0, pos < end);
+    }
+  } else {
+    const size_t rows_per_warp = 32 / VW;
+    const size_t stride = ((size_t)gridDim.x * blockDim.x / 32) * rows_per_warp;
+    for (size_t wr = (((size_t)blockIdx.x * blockDim.x + threadIdx.x) / 32) * rows_per_warp; wr < N; wr += stride) {
+      const size_t r = wr + (threadIdx.x & 31) / VW;
+      row(r, r < N);
+    }
   }
-  __device__ unsigned long long grab() {
-    unsigned long long w = 0;
-    if ((threadIdx.x & 31) == 0) w = atomicAdd(next, (unsigned long long)(32 / VW));
-    return __shfl_sync(kFull, w, 0);
-  }
-};
-template <int VW>
-struct RowWalk<VW, false> {
-  unsigned long long cur, stride, end;
-  __device__ RowWalk(const int64_t* __restrict__, size_t N, unsigned long long*) {
-    cur = (((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * (32 / VW);
-    stride = ((unsigned long long)gridDim.x * blockDim.x >> 5) * (32 / VW);
-    end = N;
-  }
-  __device__ unsigned long long grab() {
-    const unsigned long long w = cur;
-    cur += stride;
-    return w;
-  }
-};
+}
 
-#define ROW_LOOP_BEGIN                                                      \
-  __shared__ unsigned long long s_walk[2];                                  \
-  RowWalk<VW, KP == 1> walk(rowptr, N, s_walk);                             \
-  const int sub = threadIdx.x & (VW - 1);                                   \
-  for (unsigned long long wr = walk.grab(); wr < walk.end; wr = walk.grab()) { \
-    const size_t pos = wr + (threadIdx.x & 31) / VW;                        \
-    const bool live = pos < walk.end;                                       \
-    const size_t r = live ? pos : 0;
+// Opens the per-row body (a lambda over the row r and whether it is live);
+// ROW_LOOP_END runs it over the rows with the walk above.
+#define ROW_LOOP_BEGIN                         \
+  const int sub = threadIdx.x & (VW - 1);      \
+  auto row = [&](const size_t r, const bool live) {
+#define ROW_LOOP_END \
+  }              \
+  ;              \
+  run_rows<VW, KP == 1>(rowptr, N, row);
 
 template <int VW, int KP>
 __global__ void __launch_bounds__(KP == 1 ? 1024 : 256) k_sigma_mixed(const int64_t* __restrict__ rowptr,
@@ -208,7 +202,7 @@ __global__ void __launch_bounds__(KP == 1 ? 1024 : 256) k_sigma_mixed(const int6
       for (int c = 0; c < KP; ++c)
         if (c < k) y[(size_t)c * ldy + r] = dg * (double)x[r * KP + c] + ((double)acc[c].s + (double)acc[c].c);
     }
-  }
+  ROW_LOOP_END
 }
 
 template <int VW, int KP, bool HILO>
@@ -255,7 +249,7 @@ __global__ void __launch_bounds__(KP == 1 ? 1024 : 256) k_sigma_f64(const int64_
       for (int c = 0; c < KP; ++c)
         if (c < k) y[(size_t)c * ldy + r] = dg * x[r * KP + c] + acc[c];
     }
-  }
+  ROW_LOOP_END
 }
 
 // Refinement sigma on the mixed path's head + tail values, in float-float
@@ -355,10 +349,10 @@ __global__ void __launch_bounds__(KP == 1 ? 1024 : 256) k_sigma_ff(const int64_t
         if (c < k)
           y[(size_t)c * ldy + r] = dg * xd[(size_t)(c0 + c) * ldx + r] + ((double)acc[c].s + (double)acc[c].c);
     }
-  }
+  ROW_LOOP_END
 }
 
-// Launch shape of the stored-matrix sigma kernels (see RowWalk): one vector
+// Launch shape of the stored-matrix sigma kernels (see run_rows): one vector
 // runs as two 1024-thread blocks per SM over nonzero-balanced row ranges;
 // several vectors as a grid-strided launch of 256-thread blocks.
 struct SigmaLaunch {

@@ -20,6 +20,11 @@ struct MlpView {
 // s_i = sum_j H_ij^2 / (E - diag_j).
 void pt2_shift(const Csr& H, const double* diag, double E, double* s, cudaStream_t st);
 
+// Training sample on the device: idx[k] = a hashed row (with replacement),
+// tgt[k] = teacher[idx[k]] / rms; returns the rms (one small read-back).
+double mlp_sample(const double* teacher, size_t N, int64_t ns, uint64_t seed, int32_t* idx, float* tgt,
+                  DevBuf<double>& part, cudaStream_t s);
+
 struct Mlp {
   int nspin = 0, F = 0, nparam = 0;
   int offW1 = 0, offW2 = 0, offb1 = 0, offb2 = 0, offw3 = 0, offb3 = 0;
@@ -35,8 +40,9 @@ struct Mlp {
   MlpView view() const;
   // mean squared error of the batch (rows idx, targets already divided by
   // sigma) and its gradient into `grad`
+  // Loss (read back, one synchronisation) only when want_loss; NaN otherwise.
   float gradient(const Det2* dets, const double* diag, const int32_t* idx, const float* target, int B, double E,
-                 cudaStream_t s);
+                 cudaStream_t s, bool want_loss = true);
   void adam(float lr, cudaStream_t s);
   // out[i] = sigma * net(features of det i)
   void infer(const Det2* dets, const double* diag, size_t N, double E, double* out, cudaStream_t s) const;
