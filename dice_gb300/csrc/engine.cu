@@ -158,6 +158,7 @@ struct Context {
   HostHeatBath hhb;
   bool have_ints = false;
   DevBuf<double> dI1, dI2, dDirect, dExchange, dSingles;
+  DevBuf<float> dI1f, dI2f;  // FP32 copies for the FP32 matrix-free sigma
   DevBuf<float> dSameVal, dOppVal;
   DevBuf<int16_t> dSamePairs, dOppPairs;
   DevBuf<int64_t> dSameStart, dOppStart;
@@ -220,7 +221,7 @@ struct Context {
   double* pin = nullptr;  // pinned staging for the small matrices (kPin doubles)
   static constexpr int kPinQ = 0, kPinLam = 256, kPinAct = 272, kPinRR = 288, kPinG = 544, kPinNrm = 800,
                        kPin = 816;
-  DevBuf<double> dactlam, drr, dnrm, dpar;
+  DevBuf<double> dactlam, drr, dnrm;
 
   void graphs_clear() {
     for (auto& kv : gcache) cudaGraphExecDestroy(kv.second.first);
@@ -269,7 +270,7 @@ struct Context {
     if (stream) cudaStreamDestroy(stream);
   }
 
-  IntsView ints() const { return IntsView{dI1.p, dI2.p, dDirect.p, dExchange.p, hints.norb}; }
+  IntsView ints() const { return IntsView{dI1.p, dI2.p, dDirect.p, dExchange.p, hints.norb, dI1f.p, dI2f.p}; }
   HeatBathView hb() const {
     return HeatBathView{dSameVal.p, dSamePairs.p, dSameStart.p, dOppVal.p, dOppPairs.p, dOppStart.p, dSingles.p};
   }
@@ -296,6 +297,12 @@ struct Context {
     hhb = std::move(hb);
     upload(dI1, hints.I1);
     upload(dI2, hints.I2);
+    {
+      const std::vector<float> f1(hints.I1.begin(), hints.I1.end()), f2(hints.I2.begin(), hints.I2.end());
+      upload(dI1f, f1);
+      upload(dI2f, f2);
+      SHCI_CUDA(cudaStreamSynchronize(stream));  // the host copies go out of scope
+    }
     upload(dDirect, hints.Direct);
     upload(dExchange, hints.Exchange);
     upload(dSingles, hhb.singles);
@@ -410,10 +417,12 @@ struct Context {
     ndiag = ndet;
   }
 
+  static bool is_direct(int m) { return m == SHCI_MODE_DIRECT || m == SHCI_MODE_DIRECT_MIXED; }
+
   void build_ham(int mode) {
     require_ints();
     require_dets();
-    if (mode < 0 || mode > 2) throw Error(kErrInvalid, "unknown Hamiltonian mode");
+    if (mode < 0 || mode > 3) throw Error(kErrInvalid, "unknown Hamiltonian mode");
     PhaseTimer pt(stream);
     if (!helpers_ok) {
       helpers.build(dets.p, ndet, hints.norb, prims, stream);
@@ -421,7 +430,7 @@ struct Context {
     }
     pt.mark("string tables");
     ensure_diag();
-    if (mode == SHCI_MODE_DIRECT) {
+    if (is_direct(mode)) {
       H.col.release();
       H.v64.release();
       H.vhi.release();
@@ -444,8 +453,8 @@ struct Context {
   // Y[:, yc0 + c] = H A[:, c0 + c], c < k, in the given sigma mode.
   void apply_sigma(int mode, const double* A, size_t lda, int c0, int k, double* Yp, size_t ldy, int yc0) {
     if (!ham_ok) throw Error(kErrState, "Hamiltonian not built for the current space (call shci_ham_build)");
-    if (mode == SHCI_MODE_DIRECT && !helpers_ok) throw Error(kErrState, "string tables missing");
-    if (mode != SHCI_MODE_DIRECT && ham_mode == SHCI_MODE_DIRECT)
+    if (is_direct(mode) && !helpers_ok) throw Error(kErrState, "string tables missing");
+    if (!is_direct(mode) && is_direct(ham_mode))
       throw Error(kErrState, "Hamiltonian was built matrix-free; stored sigma unavailable");
     if (mode == SHCI_MODE_MIXED && ham_mode != SHCI_MODE_MIXED)
       throw Error(kErrState, "mixed sigma needs a Hamiltonian built in mixed mode");
@@ -470,6 +479,12 @@ struct Context {
           pack_ff(A, lda, c0 + done, kk, kp, N, xff, stream);
           sigma_csr_ff(H, diag.p, xff, kp, A, lda, c0 + done, kk, Yp + (size_t)(yc0 + done) * ldy, ldy, stream);
         }
+      } else if (mode == SHCI_MODE_DIRECT_MIXED) {  // FP32 matrix-free
+        xb32.reserve(N * kp);
+        yb64.reserve(N * kp);
+        pack_f32(A, lda, c0 + done, kk, kp, N, xb32.p, stream);
+        sigma_direct32(helpers, dets.p, ints(), diag.p, xb32.p, yb64.p, kp, stream);
+        unpack_f64(yb64.p, kp, kk, N, Yp, ldy, yc0 + done, stream);
       } else {
         xb64.reserve(N * kp);
         yb64.reserve(N * kp);
@@ -543,10 +558,14 @@ struct Context {
     const size_t N = ndet;
     const double t_enter = now_s();
     double t_g1 = 0.0, t_g2 = 0.0, t_loop0 = 0.0, sig0 = t_sigma;
-    // FP32 stage: hold the iterates in the alpha <-> beta flip sector that exact
-    // arithmetic would keep them in (see the note on compensated accumulation
-    // in kernels_sigma.cu); FP64 sigma keeps it to rounding by itself.
+    // FP32 stage: when every start vector lies in one alpha <-> beta flip
+    // sector, exact arithmetic keeps the iterates there, and so does FP64
+    // sigma to rounding; FP32 sigma does not (see the note on compensated
+    // accumulation in kernels_sigma.cu), so its corrections are projected
+    // back into that sector. Start vectors spanning both sectors (e.g. the
+    // random guesses of extra roots) already reach every state: no projection.
     const bool sym = stall_exit && ensure_flip();
+    int sector = 0;
     last_stalled = false;
     if (nroots < 1) throw Error(kErrInvalid, "nroots must be >= 1");
     if ((size_t)nroots > N) throw Error(kErrInvalid, "more roots than determinants");
@@ -584,14 +603,18 @@ struct Context {
         scale_col(bi, 1.0 / norm_host(bi));
       }
       if (sym) {
-        for (int i = 0; i < nroots; ++i) {
-          double* bi = V.p + (size_t)i * N;
-          const double p = flip_parity(bi, N, flipidx.p, flipsgn.p, gpart, stream);
-          if (std::fabs(p) > kParityDefinite) {
-            project_parity(bi, p > 0 ? 1.0 : -1.0);
+        std::vector<double> par(nroots);
+        for (int i = 0; i < nroots; ++i)
+          par[i] = flip_parity(V.p + (size_t)i * N, N, flipidx.p, flipsgn.p, gpart, stream);
+        sector = par[0] > kParityDefinite ? 1 : (par[0] < -kParityDefinite ? -1 : 0);
+        for (int i = 1; i < nroots; ++i)
+          if (!(par[i] * sector > kParityDefinite)) sector = 0;
+        if (sector != 0)
+          for (int i = 0; i < nroots; ++i) {
+            double* bi = V.p + (size_t)i * N;
+            project_parity(bi, (double)sector);
             scale_col(bi, 1.0 / norm_host(bi));
           }
-        }
       }
       apply_sigma(mode, V.p, N, 0, nroots, W.p, N, 0);
     }
@@ -610,13 +633,16 @@ struct Context {
     dactlam.reserve(16);
     drr.reserve(256);
     dnrm.reserve(16);
-    dpar.reserve(16);
     dsmall.reserve(16);
     gpart.reserve(256 * 304 + 2 * 304);
     if (mode == SHCI_MODE_MIXED) xb32.reserve(N * 4);
     if (mode == SHCI_MODE_FP64) xb64.reserve(N * 4);
     if (mode == SHCI_MODE_DIRECT) {
       xb64.reserve(N * 4);
+      yb64.reserve(N * 4);
+    }
+    if (mode == SHCI_MODE_DIRECT_MIXED) {
+      xb32.reserve(N * 4);
       yb64.reserve(N * 4);
     }
     if (sym) ftmp.reserve(N);
@@ -681,12 +707,15 @@ struct Context {
             stall = 0;
           }
         }
-        // Only near the FP32 rounding floor (~1e-6): a plateau higher up is
-        // ordinary Davidson behaviour and the FP32 stage keeps going.
+        // One root: only near the FP32 rounding floor (~1e-6); a plateau
+        // higher up is ordinary Davidson behaviour and the FP32 stage keeps
+        // going. Several roots (block): any plateau of the worst root hands
+        // over, with the whole basis, to the refinement stage, which finishes
+        // the roots whose FP32 residuals stall above the floor.
         if (worst < 0.8 * best_resid) {
           best_resid = worst;
           stall = 0;
-        } else if (worst < kStallWindow && ++stall >= 8) {
+        } else if ((block || worst < kStallWindow) && ++stall >= 8) {
           last_stalled = true;
           finish();
           return;
@@ -760,11 +789,7 @@ struct Context {
             precondition_shift(diag.p, shiftp, dactlam.p + a, 1, N, da, N, stream);
           else
             precondition(diag.p, dactlam.p + a, 1, N, da, N, stream);
-          if (sym) {
-            // keep each correction in the flip sector of the root it corrects
-            flip_parity_dev(X.p + (size_t)act[a] * N, N, flipidx.p, flipsgn.p, gpart, dpar.p + a, stream);
-            flip_project_cond(da, N, flipidx.p, flipsgn.p, dpar.p + a, kParityDefinite, ftmp.p, stream);
-          }
+          if (sector != 0) project_parity(da, (double)sector);  // stay in the start sector
         }
         // orthogonalise against the whole basis (two classical Gram-Schmidt passes)
         for (int pass = 0; pass < 2; ++pass) {
@@ -877,7 +902,7 @@ struct Context {
     if (precond == 0 || !(E == E) || ndet == 0) return;
     shift.resize(ndet);
     if (precond == 1) {
-      if (!ham_ok || ham_mode == SHCI_MODE_DIRECT) return;
+      if (!ham_ok || is_direct(ham_mode)) return;
       pt2_shift(H, diag.p, E, shift.p, stream);
       shift_ready = true;
     } else if (precond == 2 && mlp.trained && mlp.nspin == 2 * hints.norb) {
@@ -890,7 +915,7 @@ struct Context {
   // space at energy E, the pairs the Davidson run itself produced. Returns the
   // final minibatch loss.
   double train_mlp(double E) {
-    if (!ham_ok || ham_mode == SHCI_MODE_DIRECT) throw Error(kErrState, "training needs a stored Hamiltonian");
+    if (!ham_ok || is_direct(ham_mode)) throw Error(kErrState, "training needs a stored Hamiltonian");
     ensure_diag();
     if (mlp.nspin != 2 * hints.norb) mlp.init(2 * hints.norb, 7, stream);
     teacher.resize(ndet);
@@ -919,15 +944,16 @@ struct Context {
     if (!ham_ok) throw Error(kErrState, "Hamiltonian not built for the current space (call shci_ham_build)");
     ensure_diag();
     prepare_shift(E_est);
-    if (mode == SHCI_MODE_MIXED) {
-      // FP32 stage, then the FP64 stage continues on the same basis with W
-      // recomputed in FP64 (head + tail values)
+    if (mode == SHCI_MODE_MIXED || mode == SHCI_MODE_DIRECT_MIXED) {
+      // FP32 stage, then the refinement stage continues on the same basis with
+      // W recomputed accurately (stored: head + tail values in float-float;
+      // matrix-free: FP64 elements and accumulation)
+      const int refine = mode == SHCI_MODE_MIXED ? SHCI_MODE_FP64 : SHCI_MODE_DIRECT;
       int it1 = 0, it2 = 0, m = 0;
-      davidson_core(SHCI_MODE_MIXED, block, nroots, x, maxCopies, tol, direct_rules, E, it1, true, 0, &m);
-      // converged in FP32: one FP64 sigma of the Ritz vectors usually confirms
-      // it; stopped at the FP32 floor: keep the whole basis for the FP64 stage
-      davidson_core(SHCI_MODE_FP64, block, nroots, x, maxCopies, tol, direct_rules, E, it2, false,
-                    last_stalled ? m : 0);
+      davidson_core(mode, block, nroots, x, maxCopies, tol, direct_rules, E, it1, true, 0, &m);
+      // converged in FP32: one accurate sigma of the Ritz vectors usually
+      // confirms it; stopped at the FP32 floor: keep the whole basis
+      davidson_core(refine, block, nroots, x, maxCopies, tol, direct_rules, E, it2, false, last_stalled ? m : 0);
       iters = it1 + it2;
     } else {
       davidson_core(mode, block, nroots, x, maxCopies, tol, direct_rules, E, iters);
@@ -944,7 +970,8 @@ struct Context {
     shift_ready = false;
     mlp.trained = false;
     log.clear();
-    if (s.direct) mode = SHCI_MODE_DIRECT;
+    if (s.direct)
+      mode = (mode == SHCI_MODE_MIXED || mode == SHCI_MODE_DIRECT_MIXED) ? SHCI_MODE_DIRECT_MIXED : SHCI_MODE_DIRECT;
     // selection parameters
     sp.ncore = s.ncore;
     sp.nact = s.nact;
@@ -1056,7 +1083,7 @@ struct Context {
       t_dav += td - tc;
       log.push_back({(int64_t)N, E0[0] + hints.coreE, numIter, td - t0});
       total_dav_iters += numIter;
-      if (precond == 2 && mode != SHCI_MODE_DIRECT) {
+      if (precond == 2 && !is_direct(mode)) {
         train_mlp(E0[0]);  // pairs from this solve, used from the next solve on
         t_mlp += now_s() - td;
       }
@@ -1303,7 +1330,7 @@ int shci_ham_build(shci_ctx* ctx, int mode, int64_t* nnz) {
 
 int shci_ham_export(shci_ctx* ctx, int64_t* rowptr, int32_t* col, double* val) {
   return guarded(ctx, [&](Context& c) {
-    if (!c.ham_ok || c.ham_mode == SHCI_MODE_DIRECT) throw Error(SHCI_ERR_STATE, "no stored Hamiltonian");
+    if (!c.ham_ok || Context::is_direct(c.ham_mode)) throw Error(SHCI_ERR_STATE, "no stored Hamiltonian");
     const size_t N = c.H.N, nnz = (size_t)c.H.nnz;
     SHCI_CUDA(cudaMemcpyAsync(rowptr, c.H.rowptr.p, (N + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, c.stream));
     if (nnz) {
@@ -1361,7 +1388,7 @@ int shci_sigma_packed_device(shci_ctx* ctx, int mode, const void* x_packed, int 
                              int64_t ld) {
   return guarded(ctx, [&](Context& c) {
     if (!(kp == 1 || kp == 2 || kp == 4) || k < 1 || k > kp) throw Error(SHCI_ERR_INVALID, "need k <= kp in {1,2,4}");
-    if (!c.ham_ok || c.ham_mode == SHCI_MODE_DIRECT) throw Error(SHCI_ERR_STATE, "no stored Hamiltonian");
+    if (!c.ham_ok || Context::is_direct(c.ham_mode)) throw Error(SHCI_ERR_STATE, "no stored Hamiltonian");
     if (ld < (int64_t)c.ndet) throw Error(SHCI_ERR_INVALID, "leading dimension smaller than N");
     c.ensure_diag();
     if (mode == SHCI_MODE_MIXED)
@@ -1384,7 +1411,7 @@ int shci_sigma_device_noalloc(shci_ctx* ctx, int mode, const double* x_dev, doub
       throw Error(SHCI_ERR_INVALID, "allocation-free sigma: N x k needs " + std::to_string(need) +
                                         " bytes of scratch, more than its fixed " +
                                         std::to_string(shci::kNoAllocPackBytes) + " bytes");
-    if (!c.ham_ok || c.ham_mode == SHCI_MODE_DIRECT) throw Error(SHCI_ERR_STATE, "no stored Hamiltonian");
+    if (!c.ham_ok || Context::is_direct(c.ham_mode)) throw Error(SHCI_ERR_STATE, "no stored Hamiltonian");
     if (mode == SHCI_MODE_MIXED && c.ham_mode != SHCI_MODE_MIXED)
       throw Error(SHCI_ERR_STATE, "mixed sigma needs a Hamiltonian built in mixed mode");
     if (c.ndiag < c.ndet) throw Error(SHCI_ERR_STATE, "diagonal not computed (call shci_ham_build first)");
@@ -1510,7 +1537,7 @@ int shci_set_davidson_graphs(shci_ctx* ctx, int on) {
 
 int shci_pt2_shift(shci_ctx* ctx, double E, double* out) {
   return guarded(ctx, [&](Context& c) {
-    if (!c.ham_ok || c.ham_mode == SHCI_MODE_DIRECT) throw Error(SHCI_ERR_STATE, "no stored Hamiltonian");
+    if (!c.ham_ok || Context::is_direct(c.ham_mode)) throw Error(SHCI_ERR_STATE, "no stored Hamiltonian");
     c.ensure_diag();
     c.teacher.resize(c.ndet);
     shci::pt2_shift(c.H, c.diag.p, E, c.teacher.p, c.stream);

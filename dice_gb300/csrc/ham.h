@@ -78,6 +78,9 @@ void build_ham_csr(const Helpers& hp, const Det2* dets, const IntsView& ints, Cs
 void compute_diag(const Det2* dets, size_t n, const IntsView& ints, double* diag, cudaStream_t s);
 void sigma_direct(const Helpers& hp, const Det2* dets, const IntsView& ints, const double* diag, const double* x,
                   double* y, int k, cudaStream_t s);
+// FP32 matrix-free sigma: x row-interleaved FP32 [N][k], y FP64 [N][k].
+void sigma_direct32(const Helpers& hp, const Det2* dets, const IntsView& ints, const double* diag, const float* x,
+                    double* y, int k, cudaStream_t s);
 
 // ---- selection (kernels_select.cu) -----------------------------------------
 struct HeatBathView {
@@ -121,12 +124,6 @@ double flip_parity(const double* x, size_t n, const int32_t* flip, const int8_t*
 // x <- (x + p F x) / 2 in place (p = +1 or -1), using tmp (n doubles)
 void flip_project(double* x, size_t n, const int32_t* flip, const int8_t* sign, double p, double* tmp,
                   cudaStream_t s);
-// Device-resident forms (no host synchronisation): the parity is written to
-// *out; the projection uses the sign of *p and applies only if |*p| > thresh.
-void flip_parity_dev(const double* x, size_t n, const int32_t* flip, const int8_t* sign, DevBuf<double>& part,
-                     double* out, cudaStream_t s);
-void flip_project_cond(double* x, size_t n, const int32_t* flip, const int8_t* sign, const double* p, double thresh,
-                       double* tmp, cudaStream_t s);
 
 // ---- sigma and Davidson vector kernels (kernels_sigma.cu) -------------------
 // Y[:, c] (column-major, leading dimension ldy) = diag .* X[:, c] + Hoff X[:, c]

@@ -21,6 +21,7 @@
 // This visits the same (I, J) set as the reference's five helper-list classes
 // (single alpha, alpha-beta, single beta, double beta, double alpha).
 #include <algorithm>
+#include <type_traits>
 
 #include "engine.h"
 #include "ham.h"
@@ -907,40 +908,117 @@ void compute_diag(const Det2* dets, size_t n, const IntsView& ints, double* diag
 // Matrix-free sigma: y[I] = diag[I] x[I] + sum_J H_IJ x[J] with H_IJ
 // recomputed for every connection. X and Y are row-interleaved [N][K].
 // ---------------------------------------------------------------------------
-template <int K>
-struct DirectVisitor {
+// Matrix-free sigma (HmultDirect, SHCI/Hmult.h:241-381): row I's connections
+// are found by visit_row and H_IJ is recomputed (ket = max(I, J), so the
+// element is the same in both triangles). Hits are queued per warp, singles
+// and doubles apart, and evaluated 32 at a time on full warps, as in the H
+// build. FP64: the reference's arithmetic. FP32 (the first stage of the
+// mixed matrix-free path): FP32 integrals, FP32 elements, compensated FP32
+// accumulation of h * x.
+template <int K, bool F32>
+struct DirectQVisitor {
+  using T = typename std::conditional<F32, float, double>::type;
   const Det2* dets;
   IntsView ints;
   Det2 dI;
   uint32_t I;
-  const double* x;
-  double acc[K];
-  __device__ void step(bool hit, uint32_t J, bool) {
-    if (hit) {
-      Det2 dJ = dets[J];
-      double hv = (J < I) ? hij_any(ints, dJ, dI) : hij_any(ints, dI, dJ);
+  const T* x;  // [N][K]
+  uint32_t* qs;
+  uint32_t* qd;
+  int ns, nd;
+  Acc a32[K];
+  double a64[K];
+
+  __device__ void add(uint32_t J) {
+    const Det2 dJ = dets[J];
+    if constexpr (F32) {
+      const float hv = (J < I) ? hij_any_f32(ints, dJ, dI) : hij_any_f32(ints, dI, dJ);
 #pragma unroll
-      for (int r = 0; r < K; ++r) acc[r] += hv * x[(size_t)J * K + r];
+      for (int r = 0; r < K; ++r) acc_add(a32[r], hv, x[(size_t)J * K + r]);
+    } else {
+      const double hv = (J < I) ? hij_any(ints, dJ, dI) : hij_any(ints, dI, dJ);
+#pragma unroll
+      for (int r = 0; r < K; ++r) a64[r] += hv * x[(size_t)J * K + r];
     }
+  }
+  // out of line for the same reason as EmitVisitor::drain
+  __device__ __noinline__ int drain(uint32_t* q, int n, int cnt) {
+    const int lane = threadIdx.x & 31;
+    if (lane < cnt) add(q[lane]);
+    __syncwarp();
+    const int rest = n - cnt;
+    const uint32_t v = lane < rest ? q[cnt + lane] : 0u;
+    __syncwarp();
+    if (lane < rest) q[lane] = v;
+    __syncwarp();
+    return rest;
+  }
+  __device__ void step(bool hit, uint32_t J, bool single) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const unsigned ms = __ballot_sync(kFull, hit && single);
+    const unsigned md = __ballot_sync(kFull, hit && !single);
+    if (hit && single) qs[ns + __popc(ms & lt)] = J;
+    if (hit && !single) qd[nd + __popc(md & lt)] = J;
+    ns += __popc(ms);
+    nd += __popc(md);
+    __syncwarp();
+    if (ns >= 32) ns = drain(qs, ns, 32);
+    if (nd >= 32) nd = drain(qd, nd, 32);
+  }
+  __device__ void flush() {
+    if (ns) ns = drain(qs, ns, ns);
+    if (nd) nd = drain(qd, nd, nd);
   }
 };
 
-template <int K>
-__global__ void k_sigma_direct(HelperView h, const Det2* __restrict__ dets, IntsView ints,
-                               const double* __restrict__ diag, const double* __restrict__ x, double* __restrict__ y) {
-  const int lane = threadIdx.x & 31;
+template <int K, bool F32>
+__global__ void __launch_bounds__(256) k_sigma_direct(HelperView h, const Det2* __restrict__ dets, IntsView ints,
+                                                      const double* __restrict__ diag,
+                                                      const typename DirectQVisitor<K, F32>::T* __restrict__ x,
+                                                      double* __restrict__ y) {
+  __shared__ uint32_t s_q[8][2][64];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   for (int64_t I = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; I < (int64_t)h.N; I += warps) {
-    DirectVisitor<K> v{dets, ints, dets[I], (uint32_t)I, x, {}};
-#pragma unroll
-    for (int r = 0; r < K; ++r) v.acc[r] = 0.0;
-    visit_row(h, (uint32_t)I, v);
+    DirectQVisitor<K, F32> v;
+    v.dets = dets;
+    v.ints = ints;
+    v.dI = dets[I];
+    v.I = (uint32_t)I;
+    v.x = x;
+    v.qs = s_q[wib][0];
+    v.qd = s_q[wib][1];
+    v.ns = v.nd = 0;
 #pragma unroll
     for (int r = 0; r < K; ++r) {
-      double a = v.acc[r];
+      v.a32[r] = Acc{0.f, 0.f};
+      v.a64[r] = 0.0;
+    }
+    visit_row(h, (uint32_t)I, v);
+    v.flush();
 #pragma unroll
-      for (int o = 16; o; o >>= 1) a += __shfl_xor_sync(kFull, a, o);
-      if (lane == 0) y[(size_t)I * K + r] = diag[I] * x[(size_t)I * K + r] + a;
+    for (int r = 0; r < K; ++r) {
+      if constexpr (F32) {
+        Acc a = v.a32[r];
+        // merge in lane order (a fixed tree); FP64 diagonal term
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+          Acc other{__shfl_xor_sync(kFull, a.s, o), __shfl_xor_sync(kFull, a.c, o)};
+          if ((lane & o) == 0) {
+            acc_merge(a, other);
+          } else {
+            acc_merge(other, a);
+            a = other;
+          }
+        }
+        if (lane == 0) y[(size_t)I * K + r] = diag[I] * (double)x[(size_t)I * K + r] + ((double)a.s + (double)a.c);
+      } else {
+        double a = v.a64[r];
+#pragma unroll
+        for (int o = 16; o; o >>= 1) a += __shfl_xor_sync(kFull, a, o);
+        if (lane == 0) y[(size_t)I * K + r] = diag[I] * x[(size_t)I * K + r] + a;
+      }
     }
   }
 }
@@ -950,9 +1028,23 @@ void sigma_direct(const Helpers& hp, const Det2* dets, const IntsView& ints, con
   HelperView hv = hp.view();
   const unsigned blocks = grid_for(hp.N * 32, 256, 152 * 16);
   switch (k) {
-    case 1: k_sigma_direct<1><<<blocks, 256, 0, s>>>(hv, dets, ints, diag, x, y); break;
-    case 2: k_sigma_direct<2><<<blocks, 256, 0, s>>>(hv, dets, ints, diag, x, y); break;
-    case 4: k_sigma_direct<4><<<blocks, 256, 0, s>>>(hv, dets, ints, diag, x, y); break;
+    case 1: k_sigma_direct<1, false><<<blocks, 256, 0, s>>>(hv, dets, ints, diag, x, y); break;
+    case 2: k_sigma_direct<2, false><<<blocks, 256, 0, s>>>(hv, dets, ints, diag, x, y); break;
+    case 4: k_sigma_direct<4, false><<<blocks, 256, 0, s>>>(hv, dets, ints, diag, x, y); break;
+    default: throw Error(kErrInvalid, "direct sigma supports k in {1,2,4}");
+  }
+  SHCI_LAUNCH_CHECK();
+}
+
+void sigma_direct32(const Helpers& hp, const Det2* dets, const IntsView& ints, const double* diag, const float* x,
+                    double* y, int k, cudaStream_t s) {
+  if (!ints.I1f || !ints.I2f) throw Error(kErrState, "FP32 integrals missing");
+  HelperView hv = hp.view();
+  const unsigned blocks = grid_for(hp.N * 32, 256, 152 * 16);
+  switch (k) {
+    case 1: k_sigma_direct<1, true><<<blocks, 256, 0, s>>>(hv, dets, ints, diag, x, y); break;
+    case 2: k_sigma_direct<2, true><<<blocks, 256, 0, s>>>(hv, dets, ints, diag, x, y); break;
+    case 4: k_sigma_direct<4, true><<<blocks, 256, 0, s>>>(hv, dets, ints, diag, x, y); break;
     default: throw Error(kErrInvalid, "direct sigma supports k in {1,2,4}");
   }
   SHCI_LAUNCH_CHECK();

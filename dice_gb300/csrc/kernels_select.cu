@@ -307,45 +307,6 @@ double flip_parity(const double* x, size_t n, const int32_t* flip, const int8_t*
   return b > 0.0 ? a / b : 0.0;
 }
 
-// Device-side variants for captured Davidson iterations: the parity stays on
-// the device, and the projection applies only when it is definite.
-__global__ void k_flip_parity_sum(const double* __restrict__ part, double* __restrict__ out) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    double a = 0.0, b = 0.0;
-    for (unsigned k = 0; k < kParBlocks; ++k) {
-      a += part[2 * k];
-      b += part[2 * k + 1];
-    }
-    *out = b > 0.0 ? a / b : 0.0;
-  }
-}
-void flip_parity_dev(const double* x, size_t n, const int32_t* flip, const int8_t* sign, DevBuf<double>& part,
-                     double* out, cudaStream_t s) {
-  part.reserve(2 * kParBlocks);
-  k_flip_parity<<<kParBlocks, 256, 0, s>>>(x, n, flip, sign, part.p);
-  SHCI_LAUNCH_CHECK();
-  k_flip_parity_sum<<<1, 32, 0, s>>>(part.p, out);
-  SHCI_LAUNCH_CHECK();
-}
-__global__ void k_flip_apply_cond(const double* __restrict__ x, size_t n, const int32_t* __restrict__ flip,
-                                  const int8_t* __restrict__ sign, const double* __restrict__ pd, double thresh,
-                                  double* __restrict__ out) {
-  const double pv = *pd;
-  const bool on = fabs(pv) > thresh;
-  const double p = pv > 0 ? 1.0 : -1.0;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    out[i] = on ? 0.5 * (x[i] + p * (double)sign[i] * x[flip[i]]) : x[i];
-}
-void flip_project_cond(double* x, size_t n, const int32_t* flip, const int8_t* sign, const double* p, double thresh,
-                       double* tmp, cudaStream_t s) {
-  size_t blocks = (n + 255) / 256;
-  if (blocks > 152 * 32) blocks = 152 * 32;
-  if (blocks < 1) blocks = 1;
-  k_flip_apply_cond<<<(unsigned)blocks, 256, 0, s>>>(x, n, flip, sign, p, thresh, tmp);
-  SHCI_LAUNCH_CHECK();
-  SHCI_CUDA(cudaMemcpyAsync(x, tmp, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
-}
-
 __global__ void k_flip_apply(const double* __restrict__ x, size_t n, const int32_t* __restrict__ flip,
                              const int8_t* __restrict__ sign, double p, double* __restrict__ out) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)

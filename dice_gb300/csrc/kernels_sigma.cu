@@ -39,25 +39,7 @@ static inline unsigned grid_for(size_t n, int threads, size_t max_blocks = 152 *
 // its flipped partner hold the same products in a different order; plain FP32
 // accumulation rounds them differently, breaking the symmetry at 1e-7, and a
 // lower flip-odd state (present in some spaces) can then take over the solve.
-struct Acc {
-  float s, c;
-};
-__device__ __forceinline__ void acc_add(Acc& a, float h, float x) {
-  const float p = __fmul_rn(h, x);
-  const float pe = __fmaf_rn(h, x, -p);  // exact product residual
-  const float t = __fadd_rn(a.s, p);
-  const float bp = __fsub_rn(t, a.s);
-  const float e = __fadd_rn(__fsub_rn(a.s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
-  a.s = t;
-  a.c = __fadd_rn(a.c, __fadd_rn(e, pe));
-}
-__device__ __forceinline__ void acc_merge(Acc& a, const Acc& b) {
-  const float t = __fadd_rn(a.s, b.s);
-  const float bp = __fsub_rn(t, a.s);
-  const float e = __fadd_rn(__fsub_rn(a.s, __fsub_rn(t, bp)), __fsub_rn(b.s, bp));
-  a.s = t;
-  a.c = __fadd_rn(a.c, __fadd_rn(e, b.c));
-}
+// (Acc, acc_add and acc_merge live in shci_common.cuh.)
 
 template <int KP>
 struct VecF;

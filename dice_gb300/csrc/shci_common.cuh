@@ -87,6 +87,8 @@ struct IntsView {
   const double* Direct;    // n x n, (ii|jj)
   const double* Exchange;  // n x n, (ij|ji)
   int norb;
+  const float* I1f;  // FP32 copies for the FP32 matrix-free sigma
+  const float* I2f;
 };
 
 __device__ __forceinline__ int pair_index(int i, int j) {
@@ -159,6 +161,84 @@ __device__ inline double hij_any(const IntsView& I, const Det2& bra, const Det2&
   if (ncre == 1) return hij_single(I, ket, cre[0], des[0]);
   if (ncre == 2) return hij_double(I, ket, des[0], des[1], cre[0], cre[1]);
   return 0.0;
+}
+
+// FP32 counterparts of hij_single / hij_double / hij_any on the FP32 integral
+// copies, for the FP32 matrix-free sigma: same excitation and sign logic,
+// FP32 arithmetic (about 1e-7 relative error per element: the rounding of
+// the integrals to FP32 plus the FP32 sum of a single excitation's terms).
+__device__ __forceinline__ float i2f_spatial(const float* __restrict__ I2f, int i, int j, int k, int l) {
+  int ij = pair_index(i, j), kl = pair_index(k, l);
+  size_t A = ij > kl ? ij : kl, B = ij > kl ? kl : ij;
+  return __ldg(I2f + A * (A + 1) / 2 + B);
+}
+__device__ inline float hij_single_f32(const IntsView& I, const Det2& ket, int a, int i) {
+  const int n2 = 2 * I.norb;
+  float energy = __ldg(I.I1f + (size_t)a * n2 + i);
+  const int sa = a & 1;
+  const int ai = pair_index(a >> 1, i >> 1);
+#pragma unroll 1
+  for (int w = 0; w < 2; ++w) {
+    uint64_t bits = w ? ket.w1 : ket.w0;
+    while (bits) {
+      const int j = __ffsll((long long)bits) - 1 + 64 * w;
+      bits &= bits - 1;
+      const int jj = pair_index(j >> 1, j >> 1);
+      const size_t A = ai > jj ? ai : jj, B = ai > jj ? jj : ai;
+      float t = __ldg(I.I2f + A * (A + 1) / 2 + B);
+      if ((j & 1) == sa) t -= i2f_spatial(I.I2f, a >> 1, j >> 1, j >> 1, i >> 1);
+      energy += t;
+    }
+  }
+  const int lo = a < i ? a : i, hi = a < i ? i : a;
+  return (occ_between(ket, lo, hi) & 1) ? -energy : energy;
+}
+__device__ inline float hij_double_f32(const IntsView& I, const Det2& ket, int i, int j, int a, int b) {
+  int c = occ_between(ket, i < a ? i : a, i < a ? a : i) + occ_between(ket, j < b ? j : b, j < b ? b : j);
+  bool neg = (c & 1) != 0;
+  if (a > j || b < i) neg = !neg;
+  float v = 0.f;
+  if (!(((a ^ i) & 1) || ((b ^ j) & 1))) v = i2f_spatial(I.I2f, a >> 1, i >> 1, b >> 1, j >> 1);
+  if (!(((a ^ j) & 1) || ((b ^ i) & 1))) v -= i2f_spatial(I.I2f, a >> 1, j >> 1, b >> 1, i >> 1);
+  return neg ? -v : v;
+}
+__device__ inline float hij_any_f32(const IntsView& I, const Det2& bra, const Det2& ket) {
+  uint64_t u0 = bra.w0 ^ ket.w0, u1 = bra.w1 ^ ket.w1;
+  uint64_t c0 = u0 & bra.w0, c1 = u1 & bra.w1;
+  uint64_t d0 = u0 & ket.w0, d1 = u1 & ket.w1;
+  int ncre = __popcll(c0) + __popcll(c1);
+  int cre[2], des[2];
+  int k = 0;
+  while (c0 && k < 2) { cre[k++] = __ffsll((long long)c0) - 1; c0 &= c0 - 1; }
+  while (c1 && k < 2) { cre[k++] = __ffsll((long long)c1) - 1 + 64; c1 &= c1 - 1; }
+  k = 0;
+  while (d0 && k < 2) { des[k++] = __ffsll((long long)d0) - 1; d0 &= d0 - 1; }
+  while (d1 && k < 2) { des[k++] = __ffsll((long long)d1) - 1 + 64; d1 &= d1 - 1; }
+  if (ncre == 1) return hij_single_f32(I, ket, cre[0], des[0]);
+  if (ncre == 2) return hij_double_f32(I, ket, des[0], des[1], cre[0], cre[1]);
+  return 0.f;
+}
+
+// Compensated FP32 accumulator (s + c): TwoSum of every addition and the FMA
+// residual of every product are collected in c.
+struct Acc {
+  float s, c;
+};
+__device__ __forceinline__ void acc_add(Acc& a, float h, float x) {
+  const float p = __fmul_rn(h, x);
+  const float pe = __fmaf_rn(h, x, -p);  // exact product residual
+  const float t = __fadd_rn(a.s, p);
+  const float bp = __fsub_rn(t, a.s);
+  const float e = __fadd_rn(__fsub_rn(a.s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+  a.s = t;
+  a.c = __fadd_rn(a.c, __fadd_rn(e, pe));
+}
+__device__ __forceinline__ void acc_merge(Acc& a, const Acc& b) {
+  const float t = __fadd_rn(a.s, b.s);
+  const float bp = __fsub_rn(t, a.s);
+  const float e = __fadd_rn(__fsub_rn(a.s, __fsub_rn(t, bp)), __fsub_rn(b.s, bp));
+  a.s = t;
+  a.c = __fadd_rn(a.c, __fadd_rn(e, b.c));
 }
 
 // Determinant::Energy without the core energy (SHCI/Determinants.cpp:252-300).

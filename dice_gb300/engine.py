@@ -12,8 +12,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libshci_gpu.so")
 
-MODE_FP64, MODE_MIXED, MODE_DIRECT = 0, 1, 2
-MODES = {"fp64": MODE_FP64, "mixed": MODE_MIXED, "direct": MODE_DIRECT}
+MODE_FP64, MODE_MIXED, MODE_DIRECT, MODE_DIRECT_MIXED = 0, 1, 2, 3
+MODES = {"fp64": MODE_FP64, "mixed": MODE_MIXED, "direct": MODE_DIRECT, "direct_mixed": MODE_DIRECT_MIXED}
 
 _ERR = {1: "invalid argument", 2: "I/O error", 3: "CUDA error", 4: "out of device memory",
         5: "Davidson did not converge", 6: "device wait timed out", 7: "call out of order"}

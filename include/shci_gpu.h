@@ -43,7 +43,8 @@ enum {
 enum {
   SHCI_MODE_FP64 = 0,   /* plain path: FP64 CSR values, FP64 sigma */
   SHCI_MODE_MIXED = 1,  /* FP32 CSR head + FP32 tail, FP32 sigma, FP64 refinement */
-  SHCI_MODE_DIRECT = 2  /* matrix-free: H_ij recomputed in every sigma (HmultDirect) */
+  SHCI_MODE_DIRECT = 2,       /* matrix-free: H_ij recomputed in every sigma (HmultDirect), FP64 */
+  SHCI_MODE_DIRECT_MIXED = 3  /* matrix-free, FP32 elements and accumulation, then FP64 refinement */
 };
 
 /* Context. */
@@ -106,8 +107,8 @@ int shci_select(shci_ctx* ctx, const double* cmax, double eps1, int64_t* n_new);
 /* Hamiltonian. Replaces HamHelpers2::PopulateHelpers/MakeSHMHelpers and
  * SparseHam::makeFromHelper (SHCI/SHCImakeHamiltonian.cpp:290-408, :959-1147,
  * :486-715). mode: SHCI_MODE_*; MIXED also keeps the FP32 tail for FP64
- * refinement, DIRECT builds only the string tables. *nnz = off-diagonal
- * nonzeros, both triangles. */
+ * refinement, DIRECT and DIRECT_MIXED build only the string tables.
+ * *nnz = off-diagonal nonzeros, both triangles. */
 int shci_ham_build(shci_ctx* ctx, int mode, int64_t* nnz);
 /* The stored off-diagonal CSR (full rows) in FP64; rowptr N+1, col/val nnz.
  * For MIXED, val = head + tail. */
@@ -122,7 +123,9 @@ int shci_diag(shci_ctx* ctx, double* out);
  * :241). The reference's Hmult2 writes y (zero-initialised) and HmultDirect
  * accumulates into y; this call always overwrites y.
  * mode SHCI_MODE_MIXED computes in FP32; SHCI_MODE_FP64 in FP64 (FP64 values,
- * or head+tail when the matrix was built MIXED); SHCI_MODE_DIRECT matrix-free. */
+ * or head+tail when the matrix was built MIXED, then in float-float
+ * arithmetic); SHCI_MODE_DIRECT matrix-free in FP64; SHCI_MODE_DIRECT_MIXED
+ * matrix-free with FP32 elements and compensated FP32 accumulation. */
 int shci_sigma(shci_ctx* ctx, int mode, const double* x, double* y, int k);
 /* Same on device buffers of this context's device (column-major, leading
  * dimension ld), enqueued on the context stream without host synchronisation. */
@@ -161,7 +164,8 @@ int shci_ham_bytes(shci_ctx* ctx, int64_t* csr_bytes, int64_t* helper_bytes);
  * :353-590) with the diagonal preconditioner (:85-106).
  * x0: host nroots x N column-major, initial guesses in, eigenvectors out.
  * mode: SHCI_MODE_FP64 (plain), SHCI_MODE_MIXED (FP32 sigma, then FP64
- * refinement of the Ritz pairs), SHCI_MODE_DIRECT.
+ * refinement of the Ritz pairs), SHCI_MODE_DIRECT, SHCI_MODE_DIRECT_MIXED
+ * (FP32 matrix-free sigma, then FP64 matrix-free refinement).
  * block: 0 = one correction vector per iteration for the lowest unconverged
  * root (the reference's scheme), 1 = one per unconverged root in a single
  * k-vector sigma launch. max_copies: subspace size (reference: nroots+4).

@@ -99,6 +99,8 @@ def test_sigma_paths_against_oracle(gpu, golden):
         assert np.allclose(y, ref[:k], rtol=1e-12, atol=1e-12 * np.abs(ref).max())
     y = gpu.sigma(X, "direct")
     assert np.allclose(y, ref, rtol=1e-12, atol=1e-12 * np.abs(ref).max())
+    y32d = gpu.sigma(X, "direct_mixed")  # FP32 elements and accumulation, recomputed
+    assert np.max(np.abs(y32d - ref)) < 2e-5 * np.abs(ref).max()
     gpu.ham_build("mixed")
     y32 = gpu.sigma(X, "mixed")
     scale = np.abs(ref).max()
@@ -146,7 +148,7 @@ def test_selection_with_restriction(gpu, golden):
     assert np.array_equal(gpu.dets()[300:], ref)
 
 
-@pytest.mark.parametrize("mode", ["fp64", "mixed", "direct"])
+@pytest.mark.parametrize("mode", ["fp64", "mixed", "direct", "direct_mixed"])
 def test_davidson_against_oracle(gpu, golden, mode):
     inp = golden("h8_631g", "dice.dat")
     dets = np.load(os.path.join(GOLDEN, "h8_631g_dets.npz"))["dets"]
@@ -158,7 +160,7 @@ def test_davidson_against_oracle(gpu, golden, mode):
     e_ref, v_ref, it_ref = o.davidson(x0, diag, 5, 1e-8)
     gpu.read_fcidump(_fcidump(inp))
     gpu.set_dets(dets)
-    gpu.ham_build("mixed" if mode == "mixed" else ("direct" if mode == "direct" else "fp64"))
+    gpu.ham_build(mode)
     e, v, it = gpu.davidson(x0, mode=mode, tol=1e-8)
     assert abs(e[0] - e_ref[0]) < 1e-9
     if mode == "fp64":
