@@ -918,14 +918,17 @@ struct Context {
     if (!ham_ok || is_direct(ham_mode)) throw Error(kErrState, "training needs a stored Hamiltonian");
     ensure_diag();
     if (mlp.nspin != 2 * hints.norb) mlp.init(2 * hints.norb, 7, stream);
+    PhaseTimer pt(stream);
     teacher.resize(ndet);
     pt2_shift(H, diag.p, E, teacher.p, stream);
+    pt.mark("mlp teacher");
     const int64_t ns = std::min<int64_t>(mlp_sample, (int64_t)ndet);
     // rows drawn on the device (hashed, with replacement), targets scaled to unit rms
     tr_idx.resize(ns);
     tr_tgt.resize(ns);
     mlp.sigma = shci::mlp_sample(teacher.p, ndet, ns, 0x2545F4914F6CDD1Dull ^ (uint64_t)ndet, tr_idx.p, tr_tgt.p,
                                  gpart, stream);
+    pt.mark("mlp sample");
     const int B = (int)std::min<int64_t>(mlp_batch, ns);
     double loss = 0.0;
     for (int s = 0; s < mlp_steps; ++s) {
@@ -934,6 +937,7 @@ struct Context {
       mlp.adam(mlp_lr, stream);
     }
     SHCI_CUDA(cudaStreamSynchronize(stream));
+    pt.mark("mlp steps");
     mlp.trained = true;
     last_loss = loss;
     return loss;
