@@ -197,6 +197,7 @@ struct Context {
   int basis_max = 0, basis_keep = 0;
   Mlp mlp;
   DevBuf<double> shift, teacher;
+  DevBuf<float> pt2inv;  // 1 / (E - H_jj) for the second-order shift
   bool shift_ready = false;
   DevBuf<int32_t> tr_idx;
   DevBuf<float> tr_tgt;
@@ -903,7 +904,7 @@ struct Context {
     shift.resize(ndet);
     if (precond == 1) {
       if (!ham_ok || is_direct(ham_mode)) return;
-      pt2_shift(H, diag.p, E, shift.p, stream);
+      pt2_shift(H, diag.p, E, shift.p, pt2inv, stream);
       shift_ready = true;
     } else if (precond == 2 && mlp.trained && mlp.nspin == 2 * hints.norb) {
       mlp.infer(dets.p, diag.p, ndet, E, shift.p, stream);
@@ -914,13 +915,14 @@ struct Context {
   // Trains the MLP on the second-order shifts of (a sample of) the current
   // space at energy E, the pairs the Davidson run itself produced. Returns the
   // final minibatch loss.
-  double train_mlp(double E) {
+  // steps: Adam steps of this call (0 = mlp_steps)
+  double train_mlp(double E, int steps = 0) {
     if (!ham_ok || is_direct(ham_mode)) throw Error(kErrState, "training needs a stored Hamiltonian");
     ensure_diag();
     if (mlp.nspin != 2 * hints.norb) mlp.init(2 * hints.norb, 7, stream);
     PhaseTimer pt(stream);
     teacher.resize(ndet);
-    pt2_shift(H, diag.p, E, teacher.p, stream);
+    pt2_shift(H, diag.p, E, teacher.p, pt2inv, stream);
     pt.mark("mlp teacher");
     const int64_t ns = std::min<int64_t>(mlp_sample, (int64_t)ndet);
     // rows drawn on the device (hashed, with replacement), targets scaled to unit rms
@@ -931,9 +933,10 @@ struct Context {
     pt.mark("mlp sample");
     const int B = (int)std::min<int64_t>(mlp_batch, ns);
     double loss = 0.0;
-    for (int s = 0; s < mlp_steps; ++s) {
+    const int nsteps = steps > 0 ? steps : mlp_steps;
+    for (int s = 0; s < nsteps; ++s) {
       const int64_t off = ((int64_t)s * B) % std::max<int64_t>(1, ns - B + 1);
-      loss = mlp.gradient(dets.p, diag.p, tr_idx.p + off, tr_tgt.p + off, B, E, stream, s + 1 == mlp_steps);
+      loss = mlp.gradient(dets.p, diag.p, tr_idx.p + off, tr_tgt.p + off, B, E, stream, s + 1 == nsteps);
       mlp.adam(mlp_lr, stream);
     }
     SHCI_CUDA(cudaStreamSynchronize(stream));
@@ -1088,7 +1091,9 @@ struct Context {
       log.push_back({(int64_t)N, E0[0] + hints.coreE, numIter, td - t0});
       total_dav_iters += numIter;
       if (precond == 2 && !is_direct(mode)) {
-        train_mlp(E0[0]);  // pairs from this solve, used from the next solve on
+        // pairs from this solve, used from the next solve on; later calls
+        // refine the network already trained (a third of the steps)
+        train_mlp(E0[0], mlp.trained ? std::max(1, mlp_steps / 3) : 0);
         t_mlp += now_s() - td;
       }
       if (std::fabs(E0[0] - prevE0) < s.dE || iter == s.epsilon1.size() - 1) {
@@ -1544,7 +1549,7 @@ int shci_pt2_shift(shci_ctx* ctx, double E, double* out) {
     if (!c.ham_ok || Context::is_direct(c.ham_mode)) throw Error(SHCI_ERR_STATE, "no stored Hamiltonian");
     c.ensure_diag();
     c.teacher.resize(c.ndet);
-    shci::pt2_shift(c.H, c.diag.p, E, c.teacher.p, c.stream);
+    shci::pt2_shift(c.H, c.diag.p, E, c.teacher.p, c.pt2inv, c.stream);
     SHCI_CUDA(cudaMemcpyAsync(out, c.teacher.p, c.ndet * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     SHCI_CUDA(cudaStreamSynchronize(c.stream));
   });

@@ -547,7 +547,7 @@ struct EmitVisitor {
 };
 
 // Rows [row0, N) into a CSR whose row pointers start at row row0.
-__global__ void __launch_bounds__(256) k_ham_emit(HelperView h, int64_t row0, const Det2* __restrict__ dets,
+__global__ void __launch_bounds__(256, 4) k_ham_emit(HelperView h, int64_t row0, const Det2* __restrict__ dets,
                                                   IntsView ints, const int64_t* __restrict__ rowptr,
                                                   int32_t* __restrict__ col, double* __restrict__ v64,
                                                   float* __restrict__ vhi, float* __restrict__ vlo) {

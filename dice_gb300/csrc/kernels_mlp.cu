@@ -14,6 +14,7 @@
 //   target:   s_i / sigma (sigma = RMS of the teacher shifts).
 // The forward, backward and Adam kernels below are the project's own; the
 // hidden activations are kept in FP32 inside the kernels.
+#include <algorithm>
 #include <cuda_bf16.h>
 
 #include "ham.h"
@@ -22,36 +23,46 @@
 namespace shci {
 
 // ---------------------------------------------------------------------------
-// teacher: s_i = sum_j h_ij^2 / (E - d_j) over stored row i
+// teacher: s_i = sum_j h_ij^2 / (E - d_j) over stored row i. The reciprocals
+// 1 / (E - d_j) are formed once per determinant (a division per nonzero would
+// run on this GPU's slow FP64 divide path); the row sums run in FP32, ample
+// for a level shift that only scales the preconditioner.
 // ---------------------------------------------------------------------------
+__global__ void k_pt2_inverse(const double* __restrict__ diag, size_t N, double E, float* __restrict__ inv) {
+  for (size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < N; j += (size_t)gridDim.x * blockDim.x) {
+    const double den = E - diag[j];
+    inv[j] = fabs(den) > 1e-8 ? (float)(1.0 / den) : 0.f;
+  }
+}
 template <bool F64>
 __global__ void k_pt2_shift(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
                             const double* __restrict__ v64, const float* __restrict__ vhi,
-                            const double* __restrict__ diag, size_t N, double E, double* __restrict__ s) {
+                            const float* __restrict__ inv, size_t N, double* __restrict__ s) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < (int64_t)N; r += warps) {
-    double acc = 0.0;
+    float acc = 0.f;
     for (int64_t p = rowptr[r] + lane; p < rowptr[r + 1]; p += 32) {
-      const int j = col[p];
-      const double h = F64 ? v64[p] : (double)vhi[p];
-      const double den = E - diag[j];
-      if (fabs(den) > 1e-8) acc += h * h / den;
+      const float h = F64 ? (float)v64[p] : vhi[p];
+      acc = fmaf(h * h, __ldg(inv + col[p]), acc);
     }
 #pragma unroll
     for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
-    if (lane == 0) s[r] = acc;
+    if (lane == 0) s[r] = (double)acc;
   }
 }
 
-void pt2_shift(const Csr& H, const double* diag, double E, double* s, cudaStream_t st) {
+void pt2_shift(const Csr& H, const double* diag, double E, double* s, DevBuf<float>& inv, cudaStream_t st) {
   if (H.N == 0) return;
+  inv.reserve(H.N);
+  k_pt2_inverse<<<(unsigned)std::min<size_t>((H.N + 255) / 256, 152 * 32), 256, 0, st>>>(diag, H.N, E, inv.p);
+  SHCI_LAUNCH_CHECK();
   size_t blocks = (H.N * 32 + 255) / 256;
   if (blocks > 152 * 16) blocks = 152 * 16;
   if (H.v64.p)
-    k_pt2_shift<true><<<(unsigned)blocks, 256, 0, st>>>(H.rowptr.p, H.col.p, H.v64.p, nullptr, diag, H.N, E, s);
+    k_pt2_shift<true><<<(unsigned)blocks, 256, 0, st>>>(H.rowptr.p, H.col.p, H.v64.p, nullptr, inv.p, H.N, s);
   else
-    k_pt2_shift<false><<<(unsigned)blocks, 256, 0, st>>>(H.rowptr.p, H.col.p, nullptr, H.vhi.p, diag, H.N, E, s);
+    k_pt2_shift<false><<<(unsigned)blocks, 256, 0, st>>>(H.rowptr.p, H.col.p, nullptr, H.vhi.p, inv.p, H.N, s);
   SHCI_LAUNCH_CHECK();
 }
 

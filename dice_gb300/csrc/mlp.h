@@ -18,7 +18,7 @@ struct MlpView {
 
 // Second-order level shift of every row of the stored Hamiltonian at energy E:
 // s_i = sum_j H_ij^2 / (E - diag_j).
-void pt2_shift(const Csr& H, const double* diag, double E, double* s, cudaStream_t st);
+void pt2_shift(const Csr& H, const double* diag, double E, double* s, DevBuf<float>& inv, cudaStream_t st);
 
 // Training sample on the device: idx[k] = a hashed row (with replacement),
 // tgt[k] = teacher[idx[k]] / rms; returns the rms (one small read-back).

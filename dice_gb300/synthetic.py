@@ -19,8 +19,11 @@ import numpy as np
 WORKLOADS = {
     "hubbard12": dict(kind="hubbard", norb=12, nalpha=6, nbeta=6, U=4.0, t=1.0,
                       schedule=[(0, 1e-3), (3, 1e-4)], maxiter=6, nroots=1),
+    # final Davidson solve to 1e-6 (loose solves keep the reference's 5e-5), so
+    # that E_var comparisons at the 1 uHa level are not dominated by where a
+    # solve happened to stop below the reference's default tolerance
     "mol24": dict(kind="molecular", norb=24, nalpha=12, nbeta=12, rank=72, seed=20260001,
-                  schedule=[(0, 1e-3), (2, 3e-4), (4, 1e-4)], maxiter=7, nroots=1),
+                  schedule=[(0, 1e-3), (2, 3e-4), (4, 1e-4)], maxiter=7, nroots=1, davidson_tol=1e-6),
     "mol36": dict(kind="molecular", norb=36, nalpha=14, nbeta=14, rank=108, seed=20260002,
                   schedule=[(0, 1e-3), (2, 1e-4), (4, 3e-5)], maxiter=7, nroots=4),
     "mol50": dict(kind="molecular", norb=50, nalpha=16, nbeta=16, rank=150, seed=20260003,
@@ -120,5 +123,5 @@ def make_workload(name, directory, **overrides):
     write_fcidump(fcidump, h, eri, w["nalpha"] + w["nbeta"], ms2=w["nalpha"] - w["nbeta"])
     inp = os.path.join(directory, "input.dat")
     write_input(inp, reference_occupation(w), w["schedule"], w["maxiter"], nroots=w["nroots"],
-                extra=w.get("extra", ()))
+                davidson_tol=w.get("davidson_tol", 5e-5), extra=w.get("extra", ()))
     return inp
