@@ -699,11 +699,115 @@ struct CsrVals {
   float* vlo;
 };
 
+// Rows longer than kRowSortCap: one 1024-thread block per row runs the
+// bitonic network on 64-bit keys (column << 32 | position) in a global
+// scratch segment (L2-resident), then the values are permuted through a second
+// scratch segment. Every row then leaves the build sorted, so the order of a
+// row's entries (and of sigma's sums over it) does not depend on the atomic
+// order in which the incremental build placed its new columns.
+__global__ void k_long_rows(const int64_t* __restrict__ rowptr, size_t N, int cap, uint32_t* __restrict__ list,
+                            unsigned long long* __restrict__ count) {
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < N; r += (size_t)gridDim.x * blockDim.x)
+    if (rowptr[r + 1] - rowptr[r] > cap) list[atomicAdd(count, 1ull)] = (uint32_t)r;
+}
+__global__ void __launch_bounds__(1024) k_long_row_sort(const int64_t* __restrict__ rowptr,
+                                                        const uint32_t* __restrict__ rows,
+                                                        const int64_t* __restrict__ soff, uint64_t* __restrict__ key,
+                                                        uint64_t* __restrict__ pay, CsrVals v) {
+  const size_t r = rows[blockIdx.x];
+  const int64_t p0 = rowptr[r], len = rowptr[r + 1] - p0;
+  uint64_t* k = key + soff[blockIdx.x];
+  uint64_t* y = pay + soff[blockIdx.x];
+  int64_t P = 2;
+  while (P < len) P <<= 1;
+  for (int64_t i = threadIdx.x; i < P; i += blockDim.x)
+    k[i] = i < len ? ((uint64_t)(uint32_t)v.col[p0 + i] << 32) | (uint64_t)i : ~0ull;
+  __syncthreads();
+  for (int64_t kk = 2; kk <= P; kk <<= 1)
+    for (int64_t j = kk >> 1; j > 0; j >>= 1) {
+      for (int64_t q = threadIdx.x; q < P / 2; q += blockDim.x) {
+        const int64_t lo = (q / j) * 2 * j + (q % j), hi = lo + j;
+        const bool up = (lo & kk) == 0;
+        const uint64_t a = k[lo], b = k[hi];
+        if ((a > b) == up) {
+          k[lo] = b;
+          k[hi] = a;
+        }
+      }
+      __syncthreads();
+    }
+  // permute the values through y, then write columns and values back
+  for (int64_t i = threadIdx.x; i < len; i += blockDim.x) {
+    const int64_t src = (int64_t)(k[i] & 0xFFFFFFFFull);
+    uint64_t val;
+    if (v.v64) {
+      val = (uint64_t)__double_as_longlong(v.v64[p0 + src]);
+    } else {
+      val = (uint64_t)__float_as_uint(v.vhi[p0 + src]);
+      if (v.vlo) val |= (uint64_t)__float_as_uint(v.vlo[p0 + src]) << 32;
+    }
+    y[i] = val;
+  }
+  __syncthreads();
+  for (int64_t i = threadIdx.x; i < len; i += blockDim.x) {
+    v.col[p0 + i] = (int32_t)(k[i] >> 32);
+    const uint64_t val = y[i];
+    if (v.v64) {
+      v.v64[p0 + i] = __longlong_as_double((long long)val);
+    } else {
+      v.vhi[p0 + i] = __uint_as_float((uint32_t)val);
+      if (v.vlo) v.vlo[p0 + i] = __uint_as_float((uint32_t)(val >> 32));
+    }
+  }
+}
+
+__global__ void k_list_lens(const int64_t* __restrict__ rowptr, const uint32_t* __restrict__ rows, size_t n,
+                            int64_t* __restrict__ len) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    len[i] = rowptr[rows[i] + 1] - rowptr[rows[i]];
+}
+
 static void sort_rows(const int64_t* rowptr, size_t n, const CsrVals& v, cudaStream_t s) {
   if (n == 0) return;
   const unsigned sblocks = (unsigned)std::min<size_t>(n, 152 * 6);
   k_row_sort<<<sblocks, kSortThreads, 0, s>>>(rowptr, n, v.col, v.v64, v.vhi, v.vlo);
   SHCI_LAUNCH_CHECK();
+  // rows past the shared-memory cap
+  DevBuf<unsigned long long> cnt;
+  cnt.resize(1);
+  SHCI_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(unsigned long long), s));
+  DevBuf<uint32_t> list;
+  list.resize(n);
+  k_long_rows<<<grid_for(n, 256), 256, 0, s>>>(rowptr, n, kRowSortCap, list.p, cnt.p);
+  SHCI_LAUNCH_CHECK();
+  unsigned long long nl = 0;
+  SHCI_CUDA(cudaMemcpyAsync(&nl, cnt.p, sizeof(nl), cudaMemcpyDeviceToHost, s));
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  if (nl == 0) return;
+  DevBuf<int64_t> lens;
+  lens.resize(nl);
+  k_list_lens<<<grid_for(nl, 256), 256, 0, s>>>(rowptr, list.p, nl, lens.p);
+  SHCI_LAUNCH_CHECK();
+  std::vector<int64_t> hl(nl);
+  SHCI_CUDA(cudaMemcpyAsync(hl.data(), lens.p, nl * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  std::vector<int64_t> off(nl);
+  int64_t tot = 0;
+  for (unsigned long long i = 0; i < nl; ++i) {
+    int64_t P = 2;
+    while (P < hl[i]) P <<= 1;
+    off[i] = tot;
+    tot += P;
+  }
+  DevBuf<int64_t> doff;
+  doff.resize(nl);
+  SHCI_CUDA(cudaMemcpyAsync(doff.p, off.data(), nl * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+  DevBuf<uint64_t> key, pay;
+  key.resize(tot);
+  pay.resize(tot);
+  k_long_row_sort<<<(unsigned)nl, 1024, 0, s>>>(rowptr, list.p, doff.p, key.p, pay.p, v);
+  SHCI_LAUNCH_CHECK();
+  SHCI_CUDA(cudaStreamSynchronize(s));  // the scratch is freed on return
 }
 
 // Count, emit and sort the full rows [row0, N) into (rowptr, vals); returns nnz.

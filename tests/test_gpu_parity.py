@@ -325,3 +325,27 @@ def test_graph_captured_davidson_identical_to_eager(golden, mode):
         assert np.array_equal(a[1], b[1])
     # replays count the kernels of every captured graph
     assert res[True][2] == res[False][2]
+
+
+def test_mixed_run_is_reproducible(tmp_path):
+    """Two runs of the mixed path give the same determinants and the same
+    E_var bit for bit: every reduction has a fixed order, and every row of the
+    stored Hamiltonian leaves the build sorted by column (including rows past
+    the shared-memory sort and the new columns the incremental build places
+    with atomics). The FP32 stage is sensitive to the last bit of its sums, so
+    any run-dependent order showed up as run-dependent determinant counts."""
+    inp = synthetic.make_workload("mol24", str(tmp_path / "m"), schedule=[(0, 1e-3), (2, 3e-4)], maxiter=3)
+    out = []
+    for _ in range(2):
+        e = eng.Engine(0)
+        e.set_davidson_basis(16, 8)
+        E = e.run_input(inp, mode="mixed")
+        out.append((E[0], list(e.run_log()["ndets"]), e.ham_export(e.ham_build("mixed"))))
+        e.close()
+    assert out[0][0] == out[1][0]
+    assert out[0][1] == out[1][1]
+    for a, b in zip(out[0][2], out[1][2]):
+        assert np.array_equal(a, b)
+    rp, col = out[0][2][0], out[0][2][1]
+    for i in range(len(rp) - 1):  # every row sorted, long ones included
+        assert np.all(np.diff(col[rp[i]:rp[i + 1]]) > 0)
