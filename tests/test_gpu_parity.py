@@ -347,5 +347,8 @@ def test_mixed_run_is_reproducible(tmp_path):
     for a, b in zip(out[0][2], out[1][2]):
         assert np.array_equal(a, b)
     rp, col = out[0][2][0], out[0][2][1]
-    for i in range(len(rp) - 1):  # every row sorted, long ones included
-        assert np.all(np.diff(col[rp[i]:rp[i + 1]]) > 0)
+    d = np.diff(col.astype(np.int64))
+    within = np.ones(len(d), bool)
+    within[rp[1:-1][(rp[1:-1] > 0) & (rp[1:-1] < len(col))] - 1] = False  # pairs across a row boundary
+    assert np.all(d[within] > 0)  # every row sorted, long ones included
+    assert (np.diff(rp) > 4096).any()  # the space has rows past the shared-memory sort
