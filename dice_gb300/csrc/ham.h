@@ -21,13 +21,10 @@ struct HelperView {
   const uint32_t* aSing;
   // partial-string index: one 16-byte entry per (determinant J, occupied
   // beta orbital b of J): {beta string of J without b (low, high word),
-  // alpha group of J | b << 26, J}, sorted by a hash of (alpha group, partial
-  // string) so that equal keys are contiguous; m1dir[p] = first entry whose
-  // hash has top m1bits bits >= p
+  // alpha group of J | b << 26, J}, sorted by (alpha group, partial string);
+  // the entries of alpha group g are [m1g[g], m1g[g+1])
   const uint4* m1ent;
-  const uint32_t* m1dir;
-  int m1bits;
-  uint64_t m1salt;
+  const uint32_t* m1g;
 };
 
 // Alpha/beta string tables of one determinant space
@@ -39,20 +36,18 @@ struct Helpers {
   DevBuf<uint32_t> aidx, bidx, aDets, bDets, aSing;
   DevBuf<int64_t> aStart, bStart, aSingStart;
   DevBuf<uint4> m1ent;
-  DevBuf<uint32_t> m1dir;
-  int m1bits = 0;
+  DevBuf<uint32_t> m1g;
   int64_t nm1 = 0;
-  uint64_t m1salt = 0;
   void build(const Det2* dets, size_t n, int norb, Prims& pr, cudaStream_t s);
   HelperView view() const {
     return HelperView{N,         astr.p,      bstr.p,  aidx.p,  bidx.p,  aStart.p, aDets.p,
                       aGroupB.p, bStart.p,    bDets.p, bGroupA.p, aSingStart.p, aSing.p,
-                      nm1 > 0 ? m1ent.p : nullptr, m1dir.p, m1bits, m1salt};
+                      nm1 > 0 ? m1ent.p : nullptr, m1g.p};
   }
   size_t bytes() const {
     return astr.bytes() + bstr.bytes() + ua.bytes() + ub.bytes() + aGroupB.bytes() + bGroupA.bytes() +
            aidx.bytes() + bidx.bytes() + aDets.bytes() + bDets.bytes() + aSing.bytes() + aStart.bytes() +
-           bStart.bytes() + aSingStart.bytes() + m1ent.bytes() + m1dir.bytes();
+           bStart.bytes() + aSingStart.bytes() + m1ent.bytes() + m1g.bytes();
   }
 };
 

@@ -153,28 +153,19 @@ static void build_groups(const uint64_t* str_of_det, const uint64_t* partner_of_
   (void)str_of_det;
 }
 
-// Hash of a partial string: alpha group g with the beta string bpart (one
-// electron removed), splitmix64-style. Entries are compared on their exact
-// fields; the build checks that no two different keys share a hash (and
-// re-salts if they do), so equal keys are always contiguous.
+// Partial-string index entries, sorted by (alpha group, partial beta string):
+// the entries of one alpha group are contiguous and ordered by partial
+// string, so the probes of one row for one alpha string As search one small
+// section, and rows of the same alpha string search the same sections.
 constexpr uint32_t kM1GroupBits = 26;
-__device__ __forceinline__ uint64_t partial_key(uint32_t g, uint64_t bpart, uint64_t salt) {
-  uint64_t z = bpart + 0x9E3779B97F4A7C15ull * ((uint64_t)g + 1ull) + salt;
-  z ^= z >> 30;
-  z *= 0xBF58476D1CE4E5B9ull;
-  z ^= z >> 27;
-  z *= 0x94D049BB133111EBull;
-  z ^= z >> 31;
-  return z;
-}
 
 __global__ void k_m1_count(const uint64_t* __restrict__ bstr, size_t n, int64_t* __restrict__ cnt) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     cnt[i] = __popcll(bstr[i]);
 }
 __global__ void k_m1_fill(const uint64_t* __restrict__ bstr, const uint32_t* __restrict__ aidx, size_t n,
-                          const int64_t* __restrict__ off, uint64_t salt, uint64_t* __restrict__ key,
-                          uint32_t* __restrict__ perm, uint4* __restrict__ ent) {
+                          const int64_t* __restrict__ off, uint64_t* __restrict__ key, uint32_t* __restrict__ perm,
+                          uint4* __restrict__ ent) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     const uint64_t B = bstr[i];
     const uint32_t g = aidx[i];
@@ -182,45 +173,36 @@ __global__ void k_m1_fill(const uint64_t* __restrict__ bstr, const uint32_t* __r
     for (uint64_t r = B; r; r &= r - 1) {
       const int b = __ffsll((long long)r) - 1;
       const uint64_t bm = B ^ (1ull << b);
-      key[q] = partial_key(g, bm, salt);
+      key[q] = bm;
       perm[q] = (uint32_t)q;
       ent[q] = make_uint4((uint32_t)bm, (uint32_t)(bm >> 32), g | ((uint32_t)b << kM1GroupBits), (uint32_t)i);
       ++q;
     }
   }
 }
+__global__ void k_m1_group_keys(const uint4* __restrict__ ent, const uint32_t* __restrict__ perm, int64_t n,
+                                uint64_t* __restrict__ gk) {
+  const uint32_t mask = (1u << kM1GroupBits) - 1u;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+    gk[k] = ent[perm[k]].z & mask;
+}
 __global__ void k_m1_permute(const uint4* __restrict__ src, const uint32_t* __restrict__ perm, int64_t n,
                              uint4* __restrict__ dst) {
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
     dst[k] = src[perm[k]];
 }
-// flag if two adjacent entries share a hash but not their (group, partial string)
-__global__ void k_m1_collisions(const uint64_t* __restrict__ key, const uint4* __restrict__ ent, int64_t n,
-                                int* __restrict__ flag) {
-  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x + 1; k < n; k += (int64_t)gridDim.x * blockDim.x)
-    if (key[k] == key[k - 1]) {
-      const uint4 a = ent[k], b = ent[k - 1];
-      const uint32_t mask = (1u << kM1GroupBits) - 1u;
-      if (a.x != b.x || a.y != b.y || (a.z & mask) != (b.z & mask)) atomicOr(flag, 1);
-    }
-}
-// dir[p] = first entry whose key's top `bits` bits are >= p, p in [0, 2^bits]
-__global__ void k_m1_dir(const uint64_t* __restrict__ key, int64_t n, int bits, uint32_t* __restrict__ dir) {
-  const int64_t nb = (int64_t)1 << bits;
-  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p <= nb; p += (int64_t)gridDim.x * blockDim.x) {
+// gstart[g] = first entry of alpha group g (g in [0, ng]), from the sorted group keys
+__global__ void k_m1_groups(const uint64_t* __restrict__ gk, int64_t n, int64_t ng, uint32_t* __restrict__ gstart) {
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g <= ng; g += (int64_t)gridDim.x * blockDim.x) {
     int64_t lo = 0, hi = n;
-    if (p == nb) {
-      lo = n;
-    } else {
-      while (lo < hi) {
-        const int64_t mid = (lo + hi) >> 1;
-        if ((int64_t)(key[mid] >> (64 - bits)) < p)
-          lo = mid + 1;
-        else
-          hi = mid;
-      }
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) >> 1;
+      if ((int64_t)gk[mid] < g)
+        lo = mid + 1;
+      else
+        hi = mid;
     }
-    dir[p] = (uint32_t)lo;
+    gstart[g] = (uint32_t)lo;
   }
 }
 
@@ -268,34 +250,21 @@ void Helpers::build(const Det2* dets, size_t n, int norb, Prims& pr, cudaStream_
       DevBuf<uint64_t> key;
       DevBuf<uint32_t> perm;
       DevBuf<uint4> raw;
-      DevBuf<int> flag;
       key.resize(ne);
       perm.resize(ne);
       raw.resize(ne);
       m1ent.resize(ne);
-      flag.resize(1);
       const unsigned eb = grid_for((size_t)ne, 256);
-      for (int attempt = 0;; ++attempt) {
-        m1salt = (uint64_t)attempt * 0xD1B54A32D192ED03ull;
-        k_m1_fill<<<grid_for(n, 256), 256, 0, s>>>(bstr.p, aidx.p, n, o1.p, m1salt, key.p, perm.p, raw.p);
-        SHCI_LAUNCH_CHECK();
-        sort_u64(key.p, perm.p, (size_t)ne, pr, s);
-        k_m1_permute<<<eb, 256, 0, s>>>(raw.p, perm.p, ne, m1ent.p);
-        SHCI_LAUNCH_CHECK();
-        SHCI_CUDA(cudaMemsetAsync(flag.p, 0, sizeof(int), s));
-        k_m1_collisions<<<eb, 256, 0, s>>>(key.p, m1ent.p, ne, flag.p);
-        SHCI_LAUNCH_CHECK();
-        int h = 0;
-        SHCI_CUDA(cudaMemcpyAsync(&h, flag.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-        SHCI_CUDA(cudaStreamSynchronize(s));
-        if (!h) break;
-        if (attempt == 7) throw Error(kErrInvalid, "partial-string index: hash collisions persist");
-      }
-      int bits = 4;
-      while (bits < 28 && ((int64_t)2 << bits) < ne) ++bits;  // about two entries per bucket
-      m1bits = bits;
-      m1dir.resize(((size_t)1 << bits) + 1);
-      k_m1_dir<<<grid_for(((size_t)1 << bits) + 1, 256), 256, 0, s>>>(key.p, ne, bits, m1dir.p);
+      k_m1_fill<<<grid_for(n, 256), 256, 0, s>>>(bstr.p, aidx.p, n, o1.p, key.p, perm.p, raw.p);
+      SHCI_LAUNCH_CHECK();
+      sort_u64(key.p, perm.p, (size_t)ne, pr, s);  // by partial string
+      k_m1_group_keys<<<eb, 256, 0, s>>>(raw.p, perm.p, ne, key.p);
+      SHCI_LAUNCH_CHECK();
+      sort_u64(key.p, perm.p, (size_t)ne, pr, s);  // then by alpha group (stable)
+      k_m1_permute<<<eb, 256, 0, s>>>(raw.p, perm.p, ne, m1ent.p);
+      SHCI_LAUNCH_CHECK();
+      m1g.resize((size_t)NA + 1);
+      k_m1_groups<<<grid_for((size_t)NA + 1, 256), 256, 0, s>>>(key.p, ne, NA, m1g.p);
       SHCI_LAUNCH_CHECK();
     }
   }
@@ -333,7 +302,6 @@ __device__ void visit_row(const HelperView& h, uint32_t I, V& v) {
     const int64_t s0 = h.aSingStart[ia], s1 = h.aSingStart[ia + 1];
     const int nb = __popcll(B);
     const int64_t nprobe = (s1 - s0) * nb;
-    const int shift = 64 - h.m1bits;
     for (int64_t base = 0; base < nprobe; base += 32) {
       const int64_t t = base + lane;
       // each lane locates the entries of its key (As, B - b)
@@ -348,19 +316,26 @@ __device__ void visit_row(const HelperView& h, uint32_t I, V& v) {
         bq = __ffsll((long long)r) - 1;
         const uint64_t Bm = B ^ (1ull << bq);
         first_b = which == 0;
-        const uint64_t key = partial_key(As, Bm, h.m1salt);
-        const uint32_t p = (uint32_t)(key >> shift);
-        uint32_t e = h.m1dir[p];
-        const uint32_t e1 = h.m1dir[p + 1];
-        const uint32_t lo32 = (uint32_t)Bm, hi32 = (uint32_t)(Bm >> 32);
-        const uint32_t gmask = (1u << kM1GroupBits) - 1u;
-        auto match = [&](uint32_t q) {
-          const uint4 en = h.m1ent[q];
-          return en.x == lo32 && en.y == hi32 && (en.z & gmask) == As;
+        // lower bound of Bm in the section of group As, then the run of equal keys
+        uint32_t e = h.m1g[As];
+        uint32_t e1 = h.m1g[As + 1];
+        auto bm_of = [&](uint32_t q) {
+          const uint2 v = *reinterpret_cast<const uint2*>(h.m1ent + q);
+          return ((uint64_t)v.y << 32) | v.x;
         };
-        while (e < e1 && !match(e)) ++e;
+        {
+          uint32_t l = e, u = e1;
+          while (l < u) {
+            const uint32_t mid = (l + u) >> 1;
+            if (bm_of(mid) < Bm)
+              l = mid + 1;
+            else
+              u = mid;
+          }
+          e = l;
+        }
         uint32_t f = e;
-        while (f < e1 && match(f)) ++f;
+        while (f < e1 && bm_of(f) == Bm) ++f;
         lo = e;
         len = f - e;
       }
