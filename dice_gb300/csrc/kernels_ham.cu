@@ -440,10 +440,16 @@ struct CountVisitor {
 };
 
 // Rows [row0, N); counts[I - row0] = number of off-diagonal connections.
-__global__ void k_ham_count(HelperView h, int64_t row0, int64_t* __restrict__ counts) {
+// order[k], k < N - row0: the rows [row0, N) in alpha-major order (rows of one
+// alpha string probe the same index sections; run together, they share them
+// in cache). Output positions stay indexed by the row.
+__global__ void k_ham_count(HelperView h, int64_t row0, const uint32_t* __restrict__ order,
+                            int64_t* __restrict__ counts) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t I = row0 + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); I < (int64_t)h.N; I += warps) {
+  const int64_t nr = (int64_t)h.N - row0;
+  for (int64_t k = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < nr; k += warps) {
+    const int64_t I = order[k];
     CountVisitor v;
     visit_row(h, (uint32_t)I, v);
     int64_t c = v.c;
@@ -522,14 +528,17 @@ struct EmitVisitor {
 };
 
 // Rows [row0, N) into a CSR whose row pointers start at row row0.
-__global__ void __launch_bounds__(256, 4) k_ham_emit(HelperView h, int64_t row0, const Det2* __restrict__ dets,
-                                                  IntsView ints, const int64_t* __restrict__ rowptr,
-                                                  int32_t* __restrict__ col, double* __restrict__ v64,
-                                                  float* __restrict__ vhi, float* __restrict__ vlo) {
+__global__ void __launch_bounds__(256, 4) k_ham_emit(HelperView h, int64_t row0, const uint32_t* __restrict__ order,
+                                                     const Det2* __restrict__ dets, IntsView ints,
+                                                     const int64_t* __restrict__ rowptr, int32_t* __restrict__ col,
+                                                     double* __restrict__ v64, float* __restrict__ vhi,
+                                                     float* __restrict__ vlo) {
   __shared__ uint32_t s_q[8][2][64];
   const int wib = threadIdx.x >> 5;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t I = row0 + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); I < (int64_t)h.N; I += warps) {
+  const int64_t nr = (int64_t)h.N - row0;
+  for (int64_t k = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < nr; k += warps) {
+    const int64_t I = order[k];
     EmitVisitor v{dets, ints, dets[I], (uint32_t)I, rowptr[I - row0], col, v64, vhi, vlo, s_q[wib][0], s_q[wib][1],
                   0, 0};
     visit_row(h, (uint32_t)I, v);
@@ -786,6 +795,14 @@ static void sort_rows(const int64_t* rowptr, size_t n, const CsrVals& v, cudaStr
 }
 
 // Count, emit and sort the full rows [row0, N) into (rowptr, vals); returns nnz.
+__global__ void k_order_keys(const uint32_t* __restrict__ aidx, int64_t row0, int64_t nr, uint64_t* __restrict__ key,
+                             uint32_t* __restrict__ val) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nr; k += (int64_t)gridDim.x * blockDim.x) {
+    key[k] = aidx[row0 + k];
+    val[k] = (uint32_t)(row0 + k);
+  }
+}
+
 static int64_t emit_rows(const Helpers& hp, size_t row0, const Det2* dets, const IntsView& ints, DevBuf<int64_t>& rowptr,
                          DevBuf<int32_t>& col, DevBuf<double>& v64, DevBuf<float>& vhi, DevBuf<float>& vlo,
                          bool want64, bool want32, bool want_lo, Prims& pr, cudaStream_t s, PhaseTimer& pt) {
@@ -793,9 +810,19 @@ static int64_t emit_rows(const Helpers& hp, size_t row0, const Det2* dets, const
   HelperView hv = hp.view();
   DevBuf<int64_t> counts;
   counts.resize(nr > 0 ? nr : 1);
+  // the new rows in alpha-major order (stable: by row within an alpha string)
+  DevBuf<uint32_t> order;
+  order.resize(nr > 0 ? nr : 1);
+  if (nr) {
+    DevBuf<uint64_t> okey;
+    okey.resize(nr);
+    k_order_keys<<<grid_for(nr, 256), 256, 0, s>>>(hp.aidx.p, (int64_t)row0, (int64_t)nr, okey.p, order.p);
+    SHCI_LAUNCH_CHECK();
+    sort_u64(okey.p, order.p, nr, pr, s);
+  }
   const unsigned blocks = grid_for(nr * 32, 256, 152 * 16);
   if (nr) {
-    k_ham_count<<<blocks, 256, 0, s>>>(hv, (int64_t)row0, counts.p);
+    k_ham_count<<<blocks, 256, 0, s>>>(hv, (int64_t)row0, order.p, counts.p);
     SHCI_LAUNCH_CHECK();
   }
   pt.mark("ham count");
@@ -811,7 +838,8 @@ static int64_t emit_rows(const Helpers& hp, size_t row0, const Det2* dets, const
   if (want32 && want_lo) vlo.resize(cap); else vlo.release();
   CsrVals v{col.p, want64 ? v64.p : nullptr, want32 ? vhi.p : nullptr, (want32 && want_lo) ? vlo.p : nullptr};
   if (nr) {
-    k_ham_emit<<<blocks, 256, 0, s>>>(hv, (int64_t)row0, dets, ints, rowptr.p, v.col, v.v64, v.vhi, v.vlo);
+    k_ham_emit<<<blocks, 256, 0, s>>>(hv, (int64_t)row0, order.p, dets, ints, rowptr.p, v.col, v.v64, v.vhi,
+                                      v.vlo);
     SHCI_LAUNCH_CHECK();
   }
   pt.mark("ham emit");
