@@ -432,6 +432,7 @@ struct Context {
     pt.mark("string tables");
     ensure_diag();
     if (is_direct(mode)) {
+      H.drop_compressed();
       H.col.release();
       H.v64.release();
       H.vhi.release();
@@ -443,8 +444,11 @@ struct Context {
       // the stored rows stay valid for the unchanged prefix of the space
       // (selection only appends), so only new rows and columns are built
       const size_t n_old = (ham_mode == mode) ? H.N : 0;
+      H.drop_compressed();  // stale; rebuilt below (frees its memory before the build)
       build_ham_csr(helpers, dets.p, ints(), H, mode == SHCI_MODE_FP64, mode == SHCI_MODE_MIXED,
                     mode == SHCI_MODE_MIXED, n_old, prims, stream);
+      if (mode == SHCI_MODE_MIXED) compress_csr(H, prims, stream);
+      pt.mark("ham compress");
     }
     ham_mode = mode;
     ham_ok = true;

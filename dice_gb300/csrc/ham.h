@@ -62,8 +62,32 @@ struct Csr {
   DevBuf<int32_t> col;
   DevBuf<double> v64;
   DevBuf<float> vhi, vlo;
-  size_t bytes() const { return rowptr.bytes() + col.bytes() + v64.bytes() + vhi.bytes() + vlo.bytes(); }
+  // Copy for the single-vector FP32 sigma with 16-bit column deltas: row r's
+  // entries are [crow[r], crow[r+1]); the column of an entry is cbase[r] plus
+  // the deltas of the row up to and including it (the first delta is 0).
+  // Gaps of 65536 or more are bridged by zero-valued entries of delta 65535.
+  // 6 bytes per entry instead of 8.
+  DevBuf<int64_t> crow;
+  DevBuf<int32_t> cbase;
+  DevBuf<uint16_t> cdel;
+  DevBuf<float> cval;
+  int64_t cnnz = 0;
+  bool cvalid = false;
+  size_t bytes() const {
+    return rowptr.bytes() + col.bytes() + v64.bytes() + vhi.bytes() + vlo.bytes() + crow.bytes() + cbase.bytes() +
+           cdel.bytes() + cval.bytes();
+  }
+  void drop_compressed() {
+    crow.release();
+    cbase.release();
+    cdel.release();
+    cval.release();
+    cnnz = 0;
+    cvalid = false;
+  }
 };
+// Builds the 16-bit-delta copy of a column-sorted FP32 (head) matrix.
+void compress_csr(Csr& H, Prims& pr, cudaStream_t s);
 
 // Builds H for the space described by hp. When H already holds rows for the
 // first n_old determinants (same value arrays), only the rows >= n_old and the

@@ -187,6 +187,151 @@ __global__ void __launch_bounds__(KP == 1 ? 1024 : 256) k_sigma_mixed(const int6
   ROW_LOOP_END
 }
 
+// Single-vector FP32 sigma on the 16-bit-delta copy (Csr::cdel): the same
+// row walk and accumulation as k_sigma_mixed. Rows are padded to multiples of
+// four entries and start at multiples of four, so each lane takes four
+// consecutive entries with one 8-byte load of deltas and one 16-byte load of
+// values; the columns come from the lane's running sum plus one segmented
+// prefix sum of the lanes' totals per 4 x VW entries. 6 bytes per entry
+// streamed instead of 8.
+template <int VW>
+__global__ void __launch_bounds__(1024) k_sigma_mixed16(const int64_t* __restrict__ rowptr,
+                                                        const int32_t* __restrict__ cbase,
+                                                        const uint16_t* __restrict__ cdel,
+                                                        const float* __restrict__ val, const double* __restrict__ diag,
+                                                        const float* __restrict__ x, size_t N, double* __restrict__ y) {
+  constexpr int KP = 1;
+  const unsigned seg = VW == 32 ? kFull : (((1u << VW) - 1u) << (threadIdx.x & 31 & ~(VW - 1)));
+  ROW_LOOP_BEGIN
+    Acc acc{0.f, 0.f};
+    const int64_t p0 = live ? __ldg(rowptr + r) : 0;
+    const int64_t p1 = live ? __ldg(rowptr + r + 1) : 0;
+    int carry = live ? __ldg(cbase + r) : 0;  // column before the chunk's first entry (first delta is 0)
+    for (int64_t q = p0; q < p1; q += 4 * VW) {
+      const int64_t p = q + 4 * sub;
+      const bool ok = p < p1;
+      uint2 dd = make_uint2(0u, 0u);
+      float4 hh = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (ok) {
+        dd = __ldcs(reinterpret_cast<const uint2*>(cdel + p));
+        hh = __ldcs(reinterpret_cast<const float4*>(val + p));
+      }
+      const int d0 = (int)(dd.x & 0xFFFFu), d1 = (int)(dd.x >> 16);
+      const int d2 = (int)(dd.y & 0xFFFFu), d3 = (int)(dd.y >> 16);
+      const int t = d0 + d1 + d2 + d3;
+      int incl = t;
+#pragma unroll
+      for (int o = 1; o < VW; o <<= 1) {
+        const int u = __shfl_up_sync(seg, incl, o, VW);
+        if (sub >= o) incl += u;
+      }
+      const int c0 = carry + incl - t + d0, c1 = c0 + d1, c2 = c1 + d2, c3 = c2 + d3;
+      carry += __shfl_sync(seg, incl, VW - 1, VW);
+      if (ok) {
+        const float x0 = hh.x != 0.f ? __ldg(x + c0) : 0.f;
+        const float x1 = hh.y != 0.f ? __ldg(x + c1) : 0.f;
+        const float x2 = hh.z != 0.f ? __ldg(x + c2) : 0.f;
+        const float x3 = hh.w != 0.f ? __ldg(x + c3) : 0.f;
+        acc_add(acc, hh.x, x0);
+        acc_add(acc, hh.y, x1);
+        acc_add(acc, hh.z, x2);
+        acc_add(acc, hh.w, x3);
+      }
+    }
+#pragma unroll
+    for (int o = VW / 2; o; o >>= 1) {
+      Acc other{__shfl_xor_sync(kFull, acc.s, o, VW), __shfl_xor_sync(kFull, acc.c, o, VW)};
+      if ((threadIdx.x & o) == 0) {
+        acc_merge(acc, other);
+      } else {
+        acc_merge(other, acc);
+        acc = other;
+      }
+    }
+    if (sub == 0 && live) y[r] = diag[r] * (double)x[r] + ((double)acc.s + (double)acc.c);
+  ROW_LOOP_END
+}
+
+// ---- building the 16-bit-delta copy ----------------------------------------
+// bridges needed before entry p of its row: (gap - 1) / 65535 for a gap >= 65536
+__global__ void k_c_count(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col, size_t N,
+                          int64_t* __restrict__ len) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < (int64_t)N; r += warps) {
+    const int64_t p0 = rowptr[r], p1 = rowptr[r + 1];
+    int64_t b = 0;
+    for (int64_t p = p0 + 1 + lane; p < p1; p += 32) b += ((int64_t)col[p] - col[p - 1] - 1) / 65535;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) b += __shfl_xor_sync(kFull, b, o);
+    if (lane == 0) len[r] = ((p1 - p0) + b + 3) & ~(int64_t)3;  // padded to a multiple of four
+  }
+}
+__global__ void k_c_fill(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                         const float* __restrict__ vhi, size_t N, const int64_t* __restrict__ crow,
+                         int32_t* __restrict__ cbase, uint16_t* __restrict__ cdel, float* __restrict__ cval) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < (int64_t)N; r += warps) {
+    const int64_t p0 = rowptr[r], p1 = rowptr[r + 1];
+    if (lane == 0) cbase[r] = p1 > p0 ? col[p0] : 0;
+    int64_t out0 = crow[r];  // output position of this chunk's first item
+    for (int64_t q = p0; q < p1; q += 32) {
+      const int64_t p = q + lane;
+      int64_t gap = 0, nb = 0;
+      if (p < p1) {
+        gap = p > p0 ? (int64_t)col[p] - col[p - 1] : 0;
+        nb = gap > 0 ? (gap - 1) / 65535 : 0;
+      }
+      int64_t incl = (p < p1 ? 1 : 0) + nb;  // items this lane writes (bridges + the entry)
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int64_t t = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += t;
+      }
+      if (p < p1) {
+        int64_t o = out0 + incl - 1 - nb;
+        for (int64_t t = 0; t < nb; ++t, ++o) {
+          cdel[o] = 65535;
+          cval[o] = 0.f;
+        }
+        cdel[o] = (uint16_t)(gap - nb * 65535);
+        cval[o] = vhi[p];
+      }
+      out0 += __shfl_sync(kFull, incl, 31);
+    }
+    // padding to the next multiple of four: delta 0 (same column), value 0
+    const int64_t end = crow[r + 1];
+    if (lane < end - out0) {
+      cdel[out0 + lane] = 0;
+      cval[out0 + lane] = 0.f;
+    }
+  }
+}
+
+void compress_csr(Csr& H, Prims& pr, cudaStream_t s) {
+  H.drop_compressed();
+  if (!H.vhi.p || H.N == 0) return;
+  const size_t N = H.N;
+  DevBuf<int64_t> len;
+  len.resize(N);
+  const unsigned blocks = grid_for(N * 32, 256, 152 * 16);
+  k_c_count<<<blocks, 256, 0, s>>>(H.rowptr.p, H.col.p, N, len.p);
+  SHCI_LAUNCH_CHECK();
+  H.crow.resize(N + 1);
+  int64_t total = 0;
+  scan_exclusive_i64(len.p, H.crow.p, N, &total, pr, s);
+  SHCI_CUDA(cudaMemcpyAsync(H.crow.p + N, &total, sizeof(int64_t), cudaMemcpyHostToDevice, s));
+  H.cbase.resize(N);
+  H.cdel.resize(total > 0 ? total : 1);
+  H.cval.resize(total > 0 ? total : 1);
+  k_c_fill<<<blocks, 256, 0, s>>>(H.rowptr.p, H.col.p, H.vhi.p, N, H.crow.p, H.cbase.p, H.cdel.p, H.cval.p);
+  SHCI_LAUNCH_CHECK();
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  H.cnnz = total;
+  H.cvalid = true;
+}
+
 template <int VW, int KP, bool HILO>
 __global__ void __launch_bounds__(KP == 1 ? 1024 : 256) k_sigma_f64(const int64_t* __restrict__ rowptr,
                                                    const int32_t* __restrict__ col,
@@ -381,6 +526,17 @@ void sigma_csr_mixed(const Csr& H, const double* diag, const float* x32, int kp,
   if (!H.vhi.p) throw Error(kErrState, "Hamiltonian has no FP32 values (built for the FP64 path)");
   if (H.N == 0) return;
   int vw = pick_vw(H);
+  if (kp == 1 && H.cvalid) {
+    const SigmaLaunch L = sigma_launch(H.N, vw, 1);
+    switch (vw) {
+      case 32: k_sigma_mixed16<32><<<L.blocks, L.threads, 0, s>>>(H.crow.p, H.cbase.p, H.cdel.p, H.cval.p, diag, x32, H.N, y); break;
+      case 16: k_sigma_mixed16<16><<<L.blocks, L.threads, 0, s>>>(H.crow.p, H.cbase.p, H.cdel.p, H.cval.p, diag, x32, H.N, y); break;
+      case 8: k_sigma_mixed16<8><<<L.blocks, L.threads, 0, s>>>(H.crow.p, H.cbase.p, H.cdel.p, H.cval.p, diag, x32, H.N, y); break;
+      default: k_sigma_mixed16<4><<<L.blocks, L.threads, 0, s>>>(H.crow.p, H.cbase.p, H.cdel.p, H.cval.p, diag, x32, H.N, y); break;
+    }
+    SHCI_LAUNCH_CHECK();
+    return;
+  }
   switch (kp) {
     case 1: launch_mixed<1>(vw, H, diag, x32, k, y, ldy, s); break;
     case 2: launch_mixed<2>(vw, H, diag, x32, k, y, ldy, s); break;

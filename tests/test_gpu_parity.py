@@ -105,6 +105,8 @@ def test_sigma_paths_against_oracle(gpu, golden):
     y32 = gpu.sigma(X, "mixed")
     scale = np.abs(ref).max()
     assert np.max(np.abs(y32 - ref)) < 2e-5 * scale
+    y1 = gpu.sigma(X[0], "mixed")  # one vector: the 16-bit-delta copy of the matrix
+    assert np.max(np.abs(y1 - ref[0])) < 2e-5 * scale
     y64 = gpu.sigma(X, "fp64")  # head + tail refinement sigma
     assert np.allclose(y64, ref, rtol=1e-11, atol=1e-11 * scale)
 
@@ -352,3 +354,25 @@ def test_mixed_run_is_reproducible(tmp_path):
     within[rp[1:-1][(rp[1:-1] > 0) & (rp[1:-1] < len(col))] - 1] = False  # pairs across a row boundary
     assert np.all(d[within] > 0)  # every row sorted, long ones included
     assert (np.diff(rp) > 4096).any()  # the space has rows past the shared-memory sort
+
+
+def test_mixed_single_vector_sigma_on_large_space(tmp_path):
+    """The single-vector FP32 sigma reads the 16-bit column-delta copy of the
+    matrix; on a space of more than 65,536 determinants some column gaps need
+    bridge entries. Against the refinement sigma of the same matrix (float-
+    float on head + tail, ~1e-13) and the int32-column FP32 kernel (k = 2)."""
+    inp = synthetic.make_workload("mol24", str(tmp_path / "m"), schedule=[(0, 1e-3)], maxiter=2)
+    e = eng.Engine(0)
+    e.run_input(inp, mode="mixed")
+    e.ham_build("mixed")
+    n = e.ndets()
+    assert n > 65536
+    rng = np.random.default_rng(11)
+    X = rng.standard_normal((2, n))
+    ref = e.sigma(X, "fp64")
+    y1 = e.sigma(X[0], "mixed")
+    y2 = e.sigma(X, "mixed")
+    scale = np.abs(ref).max()
+    assert np.max(np.abs(y1 - ref[0])) < 2e-5 * scale
+    assert np.max(np.abs(y1 - y2[0])) < 1e-6 * scale
+    e.close()
