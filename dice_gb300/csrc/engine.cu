@@ -1440,6 +1440,26 @@ int shci_ham_bytes(shci_ctx* ctx, int64_t* csr_bytes, int64_t* helper_bytes) {
   });
 }
 
+int shci_sigma_bytes(shci_ctx* ctx, int mode, int k, int64_t* bytes) {
+  return guarded(ctx, [&](Context& c) {
+    if (!bytes || k < 1 || k > 4) throw Error(SHCI_ERR_INVALID, "need bytes and 1 <= k <= 4");
+    if (!c.ham_ok || Context::is_direct(c.ham_mode)) throw Error(SHCI_ERR_STATE, "no stored Hamiltonian");
+    const int64_t N = (int64_t)c.H.N, nnz = c.H.nnz;
+    int64_t b = 0;
+    if (mode == SHCI_MODE_MIXED && k == 1 && c.H.cvalid)  // 16-bit deltas + FP32 values, row bases
+      b = c.H.cnnz * 6 + 8 * (N + 1) + 4 * N + 8 * N + 4 * N + 8 * N;
+    else if (mode == SHCI_MODE_MIXED)
+      b = nnz * 8 + 8 * (N + 1) + 8 * N + (int64_t)k * N * (4 + 8);
+    else if (mode == SHCI_MODE_FP64 && c.H.v64.p)
+      b = nnz * 12 + 8 * (N + 1) + 8 * N + (int64_t)k * N * (8 + 8);
+    else if (mode == SHCI_MODE_FP64)  // float-float on head + tail: split x, FP64 x for the diagonal
+      b = nnz * 12 + 8 * (N + 1) + 8 * N + (int64_t)k * N * (8 + 8 + 8);
+    else
+      throw Error(SHCI_ERR_INVALID, "stored sigma modes only");
+    *bytes = b;
+  });
+}
+
 int shci_davidson(shci_ctx* ctx, int mode, int block, int nroots, double* x0, int max_copies, double tol, double* E,
                   int* iters) {
   return guarded(ctx, [&](Context& c) {

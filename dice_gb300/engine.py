@@ -42,6 +42,7 @@ SIGNATURES = [
     ("shci_sigma_packed_device", _i32, [_vp, _i32, _vp, _i32, _i32, _vp, _i64]),
     ("shci_sigma_device_noalloc", _i32, [_vp, _i32, _vp, _vp, _i32, _i64]),
     ("shci_ham_bytes", _i32, [_vp, _P(_i64), _P(_i64)]),
+    ("shci_sigma_bytes", _i32, [_vp, _i32, _i32, _P(_i64)]),
     ("shci_davidson", _i32, [_vp, _i32, _i32, _i32, _vp, _i32, _dbl, _vp, _P(_i32)]),
     ("shci_run_input", _i32, [_vp, ctypes.c_char_p, ctypes.c_char_p, _i32, _i32, _vp, _i32, _P(_i32)]),
     ("shci_run_log", _i32, [_vp, _i32, _P(_i32), _vp, _vp, _vp, _vp]),
@@ -256,6 +257,12 @@ class Engine:
         a, b = ctypes.c_int64(), ctypes.c_int64()
         self._check(load_library().shci_ham_bytes(self.h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
+
+    def sigma_bytes(self, mode, k=1):
+        """Algorithmic bytes of one stored-matrix sigma launch (roofline numerator)."""
+        b = ctypes.c_int64()
+        self._check(load_library().shci_sigma_bytes(self.h, MODES.get(mode, mode), int(k), ctypes.byref(b)))
+        return b.value
 
     def davidson(self, x0, mode="fp64", block=False, max_copies=None, tol=5e-5, e_est=float("nan")):
         """e_est: energy estimate for the shifted preconditioners (NaN: none)."""

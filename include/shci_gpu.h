@@ -159,6 +159,11 @@ int shci_sigma_device_noalloc(shci_ctx* ctx, int mode, const double* x_dev, doub
 /* Bytes of the stored Hamiltonian (row pointers, columns, values) and of the
  * string tables, for memory and roofline accounting. */
 int shci_ham_bytes(shci_ctx* ctx, int64_t* csr_bytes, int64_t* helper_bytes);
+/* Algorithmic bytes one stored-matrix sigma launch of k vectors streams in
+ * the given mode for the current layout (matrix entries, row pointers,
+ * diagonal, x read once, y written once): the numerator of its roofline. No
+ * counterpart in the reference. */
+int shci_sigma_bytes(shci_ctx* ctx, int mode, int k, int64_t* bytes);
 
 /* Davidson. Replaces davidson / davidsonDirect (SHCI/Davidson.cpp:111-348,
  * :353-590) with the diagonal preconditioner (:85-106).
