@@ -34,10 +34,10 @@ sys.path.insert(0, ROOT)
 WORKLOAD = "mol24"
 CPU_SAMPLE_DETS = 100000
 # DRAM bytes per mixed-sigma launch divided by its algorithmic bytes, from one
-# ncu capture of the medium case (5.988 GB measured / 5.915 GB algorithmic);
+# ncu capture of the medium case (4.4831 GB measured / 4.4546 GB algorithmic);
 # the full-size launch is too large to capture, and its traffic scales with
 # the nonzeros it streams.
-TRAFFIC_RATIO = 5.988 / 5.915
+TRAFFIC_RATIO = 4.4831 / 4.4546
 
 
 def dist_info():
