@@ -45,6 +45,20 @@ def dist_info():
             int(os.environ.get("LOCAL_RANK", 0)))
 
 
+def replicas_throughput(t_local, units_per_rank, world, device="cpu"):
+    """Whole-job throughput of `world` replicas: every rank processed
+    units_per_rank units; the job took as long as its slowest rank (max over
+    ranks of the local step time). Returns (units per second, max time)."""
+    t = t_local
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        tt = torch.tensor([t_local], dtype=torch.float64, device=device)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+    return world * units_per_rank / t, t
+
+
 class Clocks:
     """nvidia-smi sampling during the timed region."""
 
@@ -244,12 +258,8 @@ def run_ours(args):
     wall = time.perf_counter() - wall0
     clk = clocks.stop()
     torch.cuda.synchronize()
-    t_max = statistics.mean(ts32)
-    if world > 1:
-        tt = torch.tensor([t_max], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_max = tt.item()
-    value = world * k * N / t_max / 1e6
+    rate, t_max = replicas_throughput(statistics.mean(ts32), k * N, world, device="cuda")
+    value = rate / 1e6
     sig_err = float((y32 - y64).abs().max() / y64.abs().max())
     # block sigma: k = 4 vectors per pass (the block-Davidson launch)
     x4 = torch.tensor(rng.standard_normal((N, 4)), device="cuda").float().contiguous()
