@@ -180,6 +180,49 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def other_configs(work, device):
+    """The other synthetic workloads at sizes a bench run affords, each the
+    plain FP64 GPU path against the new form on the same input (final
+    Davidson solve to 1e-6, loose solves at the reference's 5e-5):
+    mol36 with 4 roots in block Davidson, mol64 matrix-free with 4 roots,
+    mol50 with and without the learned preconditioner."""
+    from dice_gb300 import engine as eng, synthetic
+
+    def run(name, sched, maxiter, mode, block, precond="plain", basis=(0, 0), extra=()):
+        inp = synthetic.make_workload(name, os.path.join(work, name), schedule=sched, maxiter=maxiter,
+                                      extra=("davidsonTol 1e-6",) + tuple(extra))
+        g = eng.Engine(device)
+        g.set_preconditioner(precond)
+        g.set_davidson_basis(*basis)
+        E = g.run_input(inp, mode=mode, block=block)
+        t, st, lg = g.timings(), g.run_stats(), g.run_log()
+        g.close()
+        return {"E_var": [float(v) for v in E], "wall_s": t["total"], "ham_s": t["ham"], "davidson_s": t["davidson"],
+                "sigma_s": t["sigma"], "davidson_iters": int(st["davidson_iters"]),
+                "ndets": [int(v) for v in lg["ndets"]]}
+
+    out = {}
+    sched = [(0, 1e-3)]
+    ref = run("mol36", sched, 2, "fp64", True)
+    new = run("mol36", sched, 2, "mixed", True, basis=(16, 12))
+    out["mol36_4roots_block"] = {
+        "what": "n=36, 14a+14b, 4 roots, block Davidson (k=4 per sigma launch), eps1 1e-3 x2",
+        "fp64": ref, "new_form": new, "dE_per_root": [a - b for a, b in zip(new["E_var"], ref["E_var"])],
+        "wall_speedup": ref["wall_s"] / new["wall_s"]}
+    ref = run("mol64", [(0, 2e-3)], 1, "fp64", True, extra=("DirectDavidson",))
+    new = run("mol64", [(0, 2e-3)], 1, "mixed", True, extra=("DirectDavidson",))
+    out["mol64_4roots_matrix_free"] = {
+        "what": "n=64, 20a+20b (two-word determinants), 4 roots, matrix-free sigma, eps1 2e-3",
+        "fp64": ref, "mixed": new, "dE_per_root": [a - b for a, b in zip(new["E_var"], ref["E_var"])]}
+    sched = [(0, 3e-3), (1, 7e-4)]
+    plain = run("mol50", sched, 3, "mixed", False, "plain")
+    mlp = run("mol50", sched, 3, "mixed", False, "mlp")
+    out["mol50_learned_preconditioner"] = {
+        "what": "n=50, 16a+16b, 1 root, mixed precision, reference subspace, eps1 3e-3 -> 7e-4",
+        "plain": plain, "mlp": mlp, "dE": mlp["E_var"][0] - plain["E_var"][0]}
+    return out
+
+
 def run_ours(args):
     import torch
     rank, world, local = dist_info()
@@ -343,9 +386,11 @@ def run_ours(args):
     }
     if cpu:
         line["cpu_baseline"] = cpu
+    e.close()
+    if args.case == "full" and not args.no_configs:
+        line["configs"] = other_configs(work, local)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    e.close()
     if world > 1:
         torch.distributed.destroy_process_group()
 
@@ -357,6 +402,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-configs", action="store_true", help="skip the other workloads (mol36, mol64, mol50)")
     ap.add_argument("--case", default="full", choices=["full", "medium", "small"],
                     help="small: the profiling case (two eps1 = 1e-3 iterations)")
     args = ap.parse_args()
