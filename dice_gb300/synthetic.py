@@ -22,6 +22,10 @@ WORKLOADS = {
     # final Davidson solve to 1e-6 (loose solves keep the reference's 5e-5), so
     # that E_var comparisons at the 1 uHa level are not dominated by where a
     # solve happened to stop below the reference's default tolerance
+    # full CI space of 14,400 determinants: small enough for a brute-force
+    # second-order check against the complete Hamiltonian
+    "mol10": dict(kind="molecular", norb=10, nalpha=3, nbeta=3, rank=30, seed=20260005,
+                  schedule=[(0, 2e-2)], maxiter=3, nroots=1, davidson_tol=1e-8),
     "mol24": dict(kind="molecular", norb=24, nalpha=12, nbeta=12, rank=72, seed=20260001,
                   schedule=[(0, 1e-3), (2, 3e-4), (4, 1e-4)], maxiter=7, nroots=1, davidson_tol=1e-6),
     "mol36": dict(kind="molecular", norb=36, nalpha=14, nbeta=14, rank=108, seed=20260002,

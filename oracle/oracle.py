@@ -73,12 +73,39 @@ def lib():
         L.orc_var_log.argtypes = [vp, vp, vp, vp, vp, vp]
         L.orc_var_dets.argtypes = [vp, vp]
         L.orc_var_ci.argtypes = [vp, i32, vp]
+        L.orc_pt_det.restype = dbl
+        L.orc_pt_det.argtypes = [vp, vp, i64, vp, dbl, dbl, vp, i32]
+        L.orc_var_pt.restype = dbl
+        L.orc_var_pt.argtypes = [vp, i32, dbl]
+        L.orc_input_epsilon2.restype = dbl
+        L.orc_input_epsilon2.argtypes = [vp]
+        L.orc_input_deterministic.restype = i32
+        L.orc_input_deterministic.argtypes = [vp]
+        L.orc_pt_stats.argtypes = [vp, vp, vp, vp]
         _lib = L
     return _lib
 
 
 def _p(a):
     return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _pack_restrictions(restrictions):
+    """(min, max, spatial_orbital_list) triples -> int64[n, 4] rows
+    (min, max, orbital mask, 0)."""
+    r = np.zeros((max(1, len(restrictions)), 4), np.int64)
+    for i, (lo, hi, orbs) in enumerate(restrictions):
+        m = 0
+        for o in orbs:
+            m |= 1 << o
+        r[i] = (lo, hi, np.uint64(m).view(np.int64) if m >= 2**63 else m, 0)
+    return r
+
+
+def _pt_stats(h):
+    c, u, p = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_double()
+    lib().orc_pt_stats(h, ctypes.byref(c), ctypes.byref(u), ctypes.byref(p))
+    return dict(candidates=c.value, unique=u.value, psi1_norm=p.value)
 
 
 class Oracle:
@@ -138,12 +165,7 @@ class Oracle:
         dets = np.ascontiguousarray(dets, dtype=np.uint64)
         cmax = np.ascontiguousarray(cmax, dtype=np.float64)
         ex = np.ascontiguousarray(existing_sorted, dtype=np.uint64)
-        r = np.zeros((max(1, len(restrictions)), 4), np.int64)
-        for i, (lo, hi, orbs) in enumerate(restrictions):
-            m = 0
-            for o in orbs:
-                m |= 1 << o
-            r[i] = (lo, hi, np.int64(np.uint64(m).view(np.int64)) if m >= 2**63 else m, 0)
+        r = _pack_restrictions(restrictions)
         cap = 1 << 16
         while True:
             out = np.zeros((cap, 2), np.uint64)
@@ -152,6 +174,16 @@ class Oracle:
             if n <= cap:
                 return out[:n]
             cap = n
+
+    def pt_det(self, dets, ci, E0, eps2, restrictions=()):
+        """Deterministic PT2 correction E2 for the space `dets` with
+        coefficients `ci` (E0 including coreE). Returns (E2, stats) with
+        stats = dict(candidates, unique, psi1_norm)."""
+        dets = np.ascontiguousarray(dets, dtype=np.uint64)
+        ci = np.ascontiguousarray(ci, dtype=np.float64)
+        r = _pack_restrictions(restrictions)
+        e2 = lib().orc_pt_det(self.h, _p(dets), len(dets), _p(ci), E0, eps2, _p(r), len(restrictions))
+        return e2, _pt_stats(self.h)
 
     def ham(self, dets):
         """Lower-triangle CSR as the reference's SparseHam holds it: row I is
@@ -212,6 +244,14 @@ class VarRun:
         self.seconds = L.orc_var_seconds(h)
         self.nnz_lower = L.orc_var_nnz_lower(h)
         self.oracle = Oracle(_handle=h)
+        self.epsilon2 = L.orc_input_epsilon2(h)
+        self.deterministic = bool(L.orc_input_deterministic(h))
+
+    def pt(self, root=0, eps2=-1.0):
+        """Deterministic PT2 on this run's space and coefficients (eps2 <= 0:
+        the input's epsilon2). Returns (E2, stats)."""
+        e2 = lib().orc_var_pt(self.h, root, eps2)
+        return e2, _pt_stats(self.h)
 
 
 def run_input(input_path, fcidump=None, verbose=False):

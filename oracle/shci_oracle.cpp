@@ -495,6 +495,174 @@ static void select_all(const Ints& I, const HeatBath& hb, const Det* dets, size_
 }
 
 // ---------------------------------------------------------------------------
+// Deterministic second-order (Epstein-Nesbet) perturbation theory
+// ---------------------------------------------------------------------------
+// EnergyAfterExcitation, single i -> A (SHCI/Determinants.cpp:124-172):
+// the excited determinant's energy from the parent's, i the index into closed.
+static double energy_after_single(const Ints& I, const int* closed, int nclosed, int i, int A, double Energyd) {
+  double E = Energyd;
+  E += -I.i1(closed[i], closed[i]) + I.i1(A, A);
+  for (int k = 0; k < nclosed; k++) {
+    if (k == i) continue;
+    E = E - I.direct(closed[k] / 2, closed[i] / 2) + I.direct(closed[k] / 2, A / 2);
+    if ((closed[k] % 2) == (closed[i] % 2))
+      E = E + I.exchange(closed[k] / 2, closed[i] / 2) - I.exchange(closed[k] / 2, A / 2);
+  }
+  return E;
+}
+
+// EnergyAfterExcitation, double i -> A, j -> B (SHCI/Determinants.cpp:178-249).
+static double energy_after_double(const Ints& I, const int* closed, int nclosed, int i, int A, int j, int B,
+                                  double Energyd) {
+  double E = Energyd - I.i1(closed[i], closed[i]) + I.i1(A, A) - I.i1(closed[j], closed[j]) + I.i1(B, B);
+  for (int k = 0; k < nclosed; k++) {
+    if (k == i) continue;
+    E = E - I.direct(closed[k] / 2, closed[i] / 2) + I.direct(closed[k] / 2, A / 2);
+    if ((closed[k] % 2) == (closed[i] % 2))
+      E = E + I.exchange(closed[k] / 2, closed[i] / 2) - I.exchange(closed[k] / 2, A / 2);
+  }
+  for (int k = 0; k < nclosed; k++) {
+    if (k == i || k == j) continue;
+    E = E - I.direct(closed[k] / 2, closed[j] / 2) + I.direct(closed[k] / 2, B / 2);
+    if ((closed[k] % 2) == (closed[j] % 2))
+      E = E + I.exchange(closed[k] / 2, closed[j] / 2) - I.exchange(closed[k] / 2, B / 2);
+  }
+  E = E - I.direct(A / 2, closed[j] / 2) + I.direct(A / 2, B / 2);
+  if ((closed[i] % 2) == (closed[j] % 2)) E = E + I.exchange(A / 2, closed[j] / 2) - I.exchange(A / 2, B / 2);
+  return E;
+}
+
+// Determinant::parity(a, b, i, j, sgn) evaluated on the excited determinant
+// di (SHCI/Determinants.cpp:332-357, called at
+// SHCI/SHCIgetdeterminants.cpp:155-157): the a<->i transposition counted on
+// di, then the b<->j one on di with a emptied and i refilled.
+static double pt_double_sign(Det di, int a, int b, int i, int j) {
+  double sgn = parity_between(di, std::min(a, i), std::max(a, i));
+  setocc(di, a, false);
+  setocc(di, i, true);
+  sgn *= parity_between(di, std::min(b, j), std::max(b, j));
+  return sgn;
+}
+
+struct PtCand {
+  Det d;
+  double num;
+  double E;
+};
+
+// SHCIgetdeterminants::getDeterminantsDeterministicPT
+// (SHCI/SHCIgetdeterminants.cpp:40-171): every single above epsilon by its
+// exact matrix element, every double whose heat-bath |float| is >= epsilon;
+// numerator H_ai c_i (the double's from the FP32 list value), energy by
+// EnergyAfterExcitation. No ncore/nact filter: only the PT restrictions.
+static void pt_from_parent(const Ints& I, const HeatBath& hb, const Det& d, double epsilon, double ci1,
+                           std::vector<Restriction>& rs, std::vector<PtCand>& out) {
+  const int nspin = 2 * I.norb;
+  int closed[128], open[128];
+  int nclosed = 0, nopen = 0;
+  for (int p = 0; p < nspin; ++p) {
+    if (getocc(d, p))
+      closed[nclosed++] = p;
+    else
+      open[nopen++] = p;
+  }
+  const double Energyd = det_energy(I, d) + I.coreE;
+  restrictions_init(rs, closed, nclosed);
+  for (int ia = 0; ia < nopen * nclosed; ia++) {
+    int i = ia / nopen, a = ia % nopen;
+    if (!restr_one(rs, closed[i], open[a])) continue;
+    double integral = hij_1excite(I, open[a], closed[i], closed, nclosed);
+    if (closed[i] % 2 != open[a] % 2) {
+      // spin flip: I1 has no alpha-beta block, so the element is zero
+      double sgn = parity_between(d, std::min(open[a], closed[i]), std::max(open[a], closed[i]));
+      integral = I.i1(open[a], closed[i]) * sgn;
+    }
+    if (fabs(integral) > epsilon) {
+      PtCand c;
+      c.d = d;
+      setocc(c.d, open[a], true);
+      setocc(c.d, closed[i], false);
+      c.num = integral * ci1;
+      c.E = energy_after_single(I, closed, nclosed, i, open[a], Energyd);
+      out.push_back(c);
+    }
+  }
+  if (fabs(I.maxEntry) < epsilon) return;
+  for (int ij = 0; ij < nclosed * nclosed; ij++) {
+    int i = ij / nclosed, j = ij % nclosed;
+    if (i <= j) continue;
+    int Ii = closed[i] / 2, Jj = closed[j] / 2;
+    int X = std::max(Ii, Jj), Y = std::min(Ii, Jj);
+    int pairIndex = X * (X + 1) / 2 + Y;
+    bool same = closed[i] % 2 == closed[j] % 2;
+    size_t start = same ? hb.sameStart[pairIndex] : hb.oppStart[pairIndex];
+    size_t end = same ? hb.sameStart[pairIndex + 1] : hb.oppStart[pairIndex + 1];
+    const float* integrals = same ? hb.sameVal.data() : hb.oppVal.data();
+    const int16_t* orbIndices = same ? hb.samePairs.data() : hb.oppPairs.data();
+    for (size_t index = start; index < end; index++) {
+      if (fabsf(integrals[index]) < epsilon) break;
+      int a = 2 * orbIndices[2 * index] + closed[i] % 2;
+      int b = 2 * orbIndices[2 * index + 1] + closed[j] % 2;
+      if (!restr_two(rs, closed[i], closed[j], a, b)) continue;
+      if (!(getocc(d, a) || getocc(d, b))) {
+        PtCand c;
+        c.d = d;
+        setocc(c.d, a, true);
+        setocc(c.d, b, true);
+        setocc(c.d, closed[i], false);
+        setocc(c.d, closed[j], false);
+        double sgn = pt_double_sign(c.d, a, b, closed[i], closed[j]);
+        c.num = integrals[index] * sgn * ci1;
+        c.E = energy_after_double(I, closed, nclosed, i, a, j, b, Energyd);
+        out.push_back(c);
+      }
+    }
+  }
+}
+
+struct PtStats {
+  int64_t candidates = 0, unique = 0;
+  double psi1_norm = 0.0;
+};
+
+// SHCIbasics::DoPerturbativeDeterministic (SHCI/SHCIbasics.cpp:453-728),
+// serial, without the RDM/response branch: candidates of every parent with
+// epsilon = |eps2 / c_i|, stable sort by determinant, duplicates merged by
+// summing numerators in generation order (StitchDEH::MergeSortAndRemoveDuplicates,
+// SHCI/SHCISortMpiUtils.cpp:541-640), determinants of the variational space
+// removed (StitchDEH::RemoveDetsPresentIn, :750-800), then
+// E2 = sum |N_a|^2 / (E0 - E_a). E0 and the energies include coreE.
+static double pt_deterministic(const Ints& I, const HeatBath& hb, const Det* dets, size_t n, const double* ci,
+                               double E0, double eps2, std::vector<Restriction> rs, PtStats& st) {
+  std::vector<PtCand> all;
+  for (size_t i = 0; i < n; i++) pt_from_parent(I, hb, dets[i], fabs(eps2 / ci[i]), ci[i], rs, all);
+  st.candidates = (int64_t)all.size();
+  std::stable_sort(all.begin(), all.end(), [](const PtCand& x, const PtCand& y) { return det_less(x.d, y.d); });
+  std::vector<Det> sorted(dets, dets + n);
+  std::sort(sorted.begin(), sorted.end(), det_less);
+  double e2 = 0.0, psi = 0.0;
+  int64_t uniq = 0;
+  size_t k = 0, v = 0;
+  while (k < all.size()) {
+    size_t e = k + 1;
+    double num = all[k].num;
+    while (e < all.size() && det_eq(all[e].d, all[k].d)) num += all[e++].num;
+    while (v < sorted.size() && det_less(sorted[v], all[k].d)) ++v;
+    bool present = v < sorted.size() && det_eq(sorted[v], all[k].d);
+    if (!present) {
+      const double de = E0 - all[k].E;
+      psi += pow(fabs(num / de), 2);
+      e2 += pow(fabs(num), 2) / de;
+      ++uniq;
+    }
+    k = e;
+  }
+  st.unique = uniq;
+  st.psi1_norm = psi;
+  return e2;
+}
+
+// ---------------------------------------------------------------------------
 // Sparse Hamiltonian: lower triangle with diagonal first, as SparseHam holds it
 // (SHCI/SHCImakeHamiltonian.cpp:486-715). Connections are every J < I at
 // excitation distance 1 or 2; values Hij(Dets[J], Dets[I]).
@@ -807,6 +975,8 @@ struct Schedule {
   bool direct = false;
   SelParams sel;
   std::string integralFile = "FCIDUMP";
+  double epsilon2 = 1.e-8;  // SHCI/input.cpp:58
+  bool stochastic = true;   // SHCI/input.cpp:67; `deterministic` clears it (:322-323)
 };
 
 static int read_input(const char* path, Schedule& s, std::string& err) {
@@ -851,6 +1021,8 @@ static int read_input(const char* path, Schedule& s, std::string& err) {
     else if (iequals(arg, "davidsonTolLoose")) s.davidsonTolLoose = atof(tok[1].c_str());
     else if (iequals(arg, "dE")) s.dE = atof(tok[1].c_str());
     else if (iequals(arg, "maxiter")) maxiter = atoi(tok[1].c_str());
+    else if (iequals(arg, "epsilon2")) s.epsilon2 = atof(tok[1].c_str());
+    else if (iequals(arg, "deterministic")) s.stochastic = false;
     else if (iequals(arg, "restrict") || iequals(arg, "restrictv")) {
       Restriction r;
       r.minElec = atoi(tok[1].c_str());
@@ -1022,8 +1194,27 @@ struct orc_ctx {
   SparseHam ham;
   size_t ham_n = 0;
   VarResult var;
+  Schedule sched;
+  PtStats pt;
   std::string err;
 };
+
+static std::vector<Restriction> unpack_restrictions(const int64_t* restr, int nrestr) {
+  std::vector<Restriction> rs;
+  for (int r = 0; r < nrestr; ++r) {
+    Restriction R;
+    R.minElec = (int)restr[4 * r];
+    R.maxElec = (int)restr[4 * r + 1];
+    uint64_t m0 = (uint64_t)restr[4 * r + 2];
+    for (int k = 0; k < 64; ++k)
+      if ((m0 >> k) & 1) {
+        R.orbs.push_back(2 * k);
+        R.orbs.push_back(2 * k + 1);
+      }
+    rs.push_back(R);
+  }
+  return rs;
+}
 
 extern "C" {
 
@@ -1088,18 +1279,7 @@ int64_t orc_select(orc_ctx* c, const uint64_t* dets, int64_t n, const double* cm
   SelParams sp;
   sp.ncore = ncore;
   sp.nact = nact;
-  for (int r = 0; r < nrestr; ++r) {
-    Restriction R;
-    R.minElec = (int)restr[4 * r];
-    R.maxElec = (int)restr[4 * r + 1];
-    uint64_t m0 = (uint64_t)restr[4 * r + 2];
-    for (int k = 0; k < 64; ++k)
-      if ((m0 >> k) & 1) {
-        R.orbs.push_back(2 * k);
-        R.orbs.push_back(2 * k + 1);
-      }
-    sp.restrictions.push_back(R);
-  }
+  sp.restrictions = unpack_restrictions(restr, nrestr);
   std::vector<Det> nd;
   select_all(c->ints, c->hb, (const Det*)dets, (size_t)n, cmax, eps1, sp, (const Det*)existing_sorted,
              (size_t)nexisting, nd);
@@ -1155,8 +1335,33 @@ int orc_run_input(orc_ctx** out_ctx, const char* input, const char* fcidump_over
     delete c;
     return 3;
   }
+  c->sched = s;
   *out_ctx = c;
   return 0;
+}
+
+// Deterministic PT2 correction for the given space and coefficients (E0 with
+// coreE). restr as for orc_select (the PT restrictions). Returns E2.
+double orc_pt_det(orc_ctx* c, const uint64_t* dets, int64_t n, const double* ci, double E0, double eps2,
+                  const int64_t* restr, int nrestr) {
+  return pt_deterministic(c->ints, c->hb, (const Det*)dets, (size_t)n, ci, E0, eps2,
+                          unpack_restrictions(restr, nrestr), c->pt);
+}
+
+// PT2 on the result of orc_run_input for one root, eps2 <= 0 taking the
+// input's epsilon2; the restrictions are the input's (`restrict` applies to
+// both stages, SHCI/input.cpp:267-277). Returns E2.
+double orc_var_pt(orc_ctx* c, int root, double eps2) {
+  if (eps2 <= 0) eps2 = c->sched.epsilon2;
+  return pt_deterministic(c->ints, c->hb, c->var.dets.data(), c->var.dets.size(), c->var.ci[root].data(),
+                          c->var.E[root], eps2, c->sched.sel.restrictions, c->pt);
+}
+double orc_input_epsilon2(orc_ctx* c) { return c->sched.epsilon2; }
+int orc_input_deterministic(orc_ctx* c) { return c->sched.stochastic ? 0 : 1; }
+void orc_pt_stats(orc_ctx* c, int64_t* candidates, int64_t* unique, double* psi1_norm) {
+  *candidates = c->pt.candidates;
+  *unique = c->pt.unique;
+  *psi1_norm = c->pt.psi1_norm;
 }
 
 int orc_var_nroots(orc_ctx* c) { return (int)c->var.E.size(); }
@@ -1195,6 +1400,12 @@ int main(int argc, char** argv) {
     return rc;
   }
   for (size_t i = 0; i < c->var.E.size(); ++i) printf("root %zu  E_var %.12f\n", i, c->var.E[i]);
+  if (!c->sched.stochastic)
+    for (size_t i = 0; i < c->var.E.size(); ++i) {
+      double e2 = orc_var_pt(c, (int)i, -1.0);
+      printf("root %zu  E_PT2 %.12f  E_var+PT2 %.12f  candidates %lld unique %lld\n", i, e2, c->var.E[i] + e2,
+             (long long)c->pt.candidates, (long long)c->pt.unique);
+    }
   printf("ndets %zu  seconds %.3f\n", c->var.dets.size(), c->var.seconds);
   orc_free(c);
   return 0;

@@ -11,8 +11,9 @@ What is copied, and what it pins:
     the eps1 schedule 5e-3 -> 1e-3 -> 5e-5.
   * tests/SHCI/n2_RAS: FCIDUMP, input.dat (with an occupation restriction),
     trusted_hci.e (E_var).
-  * tests/SHCI/o2_det: FCIDUMP and input.dat (used as an extra parity case;
-    its trusted energy includes perturbation theory, which is not pinned).
+  * tests/SHCI/o2_det: FCIDUMP and input.dat (`deterministic`, epsilon2
+    1e-7); trusted_hci.e holds E_var + E_PT2 of root 0 (runSmallTests.sh
+    tolerance 1e-6).
 FCIDUMPs are stored gzip-compressed. Energies and tables go to golden.json.
 """
 import gzip
@@ -93,10 +94,12 @@ def main(ref):
     out["n2_RAS"] = {"E_var": read_e(os.path.join(n2, "trusted_hci.e")),
                      "source": "tests/SHCI/n2_RAS/trusted_hci.e"}
 
-    # o2 (variational part only is used)
+    # o2 with deterministic PT
     o2 = os.path.join(ref, "tests", "SHCI", "o2_det")
     gz(os.path.join(o2, "FCIDUMP"), os.path.join(HERE, "o2.FCIDUMP.gz"))
     shutil.copy(os.path.join(o2, "input.dat"), os.path.join(HERE, "o2.input.dat"))
+    out["o2_det"] = {"E_total": read_e(os.path.join(o2, "trusted_hci.e")), "tol": 1e-6,
+                     "source": "tests/SHCI/o2_det/trusted_hci.e (runSmallTests.sh tolerance 1e-6)"}
 
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump(out, f, indent=1)

@@ -131,3 +131,71 @@ def test_slater_condon_matches_second_quantisation(golden):
         got = o.hij(word(bra), word(ket))
         assert abs(ref - got) < 1e-10, (bra, ket, ref, got)
         ntest += 1
+
+
+# ---------------------------------------------------------------------------
+# Deterministic second-order perturbation theory
+# ---------------------------------------------------------------------------
+def test_o2_det_total_energy_matches_trusted(golden):
+    """tests/SHCI/o2_det: E_var + E_PT2 of the `deterministic` run against
+    trusted_hci.e, at the reference's own tolerance (1e-6). The converged
+    112-determinant space is closed under H here, so E_PT2 vanishes."""
+    run = orc.run_input(golden("o2", "input.dat"))
+    assert run.deterministic and run.epsilon2 == 1e-7
+    e2, st = run.pt(0)
+    assert st["candidates"] > 0 and st["unique"] == 0 and e2 == 0.0
+    assert abs(run.E[0] + e2 - G["o2_det"]["E_total"]) < G["o2_det"]["tol"]
+
+
+def _fci_dets(norb, na, nb):
+    import itertools
+    out = []
+    for A in itertools.combinations(range(norb), na):
+        for B in itertools.combinations(range(norb), nb):
+            w = 0
+            for k in A:
+                w |= 1 << (2 * k)
+            for k in B:
+                w |= 1 << (2 * k + 1)
+            out.append((w & (2**64 - 1), w >> 64))
+    return np.array(out, dtype=np.uint64)
+
+
+def test_pt_matches_brute_force_second_order(tmp_path):
+    """Seeded 10-orbital Hamiltonian (6 electrons, full CI space of 14,400
+    determinants): with epsilon2 -> 0 the deterministic PT energy must equal
+    sum_a (H c)_a^2 / (E0 - H_aa) over every determinant outside the
+    variational space, from the complete Hamiltonian. The only difference
+    allowed is the FP32 rounding of the heat-bath double-excitation values
+    the reference uses as numerators (relative 1e-7 per element)."""
+    import scipy.sparse as sp
+    from dice_gb300 import synthetic
+    inp = synthetic.make_workload("mol10", str(tmp_path / "m"))
+    run = orc.run_input(inp)
+    o = run.oracle
+    dets = _fci_dets(o.norb, 3, 3)
+    rp, col, val = o.ham(dets)
+    N = len(dets)
+    rows = np.repeat(np.arange(N), np.diff(rp))
+    L = sp.csr_matrix((val, (rows, col)), shape=(N, N))
+    H = L + sp.triu(L.T, 1)
+    key = {(int(a), int(b)): i for i, (a, b) in enumerate(dets)}
+    idx = np.array([key[(int(a), int(b))] for a, b in run.dets])
+    c = np.zeros(N)
+    c[idx] = run.ci[0]
+    E0 = run.E[0] - o.coreE
+    Hc = H @ c
+    out = np.ones(N, bool)
+    out[idx] = False
+    brute = float(np.sum(Hc[out] ** 2 / (E0 - H.diagonal()[out])))
+    e2, st = run.pt(0, 1e-12)
+    print("brute", brute, "oracle", e2, st)
+    assert brute < -1e-2
+    # heat-bath lists keep |integral| > 1e-10 only: couplings below that are
+    # not generated, those far above it all are
+    assert np.count_nonzero(np.abs(Hc[out]) > 1e-8) <= st["unique"] <= np.count_nonzero(Hc[out])
+    assert abs(e2 - brute) < 1e-8 * abs(brute)
+    # a finite threshold drops only small contributions
+    e2b, stb = run.pt(0, 1e-6)
+    assert stb["candidates"] < st["candidates"]
+    assert abs(e2b - brute) < 1e-4 * abs(brute)
