@@ -17,7 +17,7 @@ OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libshci_gpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["kernels_core.cu", "kernels_ham.cu", "kernels_select.cu", "kernels_sigma.cu", "kernels_mlp.cu",
+CUDA_SOURCES = ["kernels_core.cu", "kernels_ham.cu", "kernels_select.cu", "kernels_sigma.cu", "kernels_mlp.cu", "kernels_pt.cu",
                 "engine.cu"]
 CXX_SOURCES = ["host_io.cpp"]
 

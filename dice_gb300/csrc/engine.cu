@@ -206,9 +206,18 @@ struct Context {
   int64_t mlp_sample = 200000;
   double last_loss = 0.0;
 
+  // deterministic perturbation theory
+  PtWork ptw;
+  PtResult pt_last;
+  int64_t pt_max_cand = 0;  // partition capacity override (0: from free memory)
+  double t_pt = 0;
+  DevBuf<double> ptc;  // coefficients passed from the host
+
   // run state
   DevBuf<double> ci, cmax;
   int nroots_run = 0;
+  std::vector<double> Evar;  // E_var per root of the last run, coreE included
+  double run_eps2 = 1e-8;    // the last input's epsilon2
   std::vector<IterLog> log;
   double t_select = 0, t_ham = 0, t_dav = 0, t_total = 0, t_sigma = 0, t_mlp = 0;
   int64_t total_dav_iters = 0;
@@ -324,6 +333,7 @@ struct Context {
     helpers_ok = false;
     ham_ok = false;
     flip_state = -1;
+    Evar.clear();  // the run's coefficients no longer match the space
   }
 
   // True when the space is closed under the alpha <-> beta flip (equal alpha
@@ -419,6 +429,25 @@ struct Context {
   }
 
   static bool is_direct(int m) { return m == SHCI_MODE_DIRECT || m == SHCI_MODE_DIRECT_MIXED; }
+
+  // Deterministic PT2 of the current space with coefficients c (device, ndet
+  // entries); E0 includes coreE, as in SHCIbasics::DoPerturbativeDeterministic
+  // (SHCI/SHCIbasics.cpp:453-728). The selection restrictions apply (the
+  // reference's `restrict` fills both lists, SHCI/input.cpp:267-277); ncore and
+  // nact do not.
+  double perturb(const double* c, double E0, double eps2) {
+    require_ints();
+    require_dets();
+    const double t0 = now_s();
+    hash.build(dets.p, ndet, stream);
+    SelectParams psp = sp;
+    psp.ncore = 0;
+    psp.nact = 1 << 30;
+    pt_last = pt_deterministic(dets.p, ndet, c, E0 - hints.coreE, eps2, ints(), hb(), hints.maxEntry, psp, hash,
+                               pt_max_cand, ptw, prims, stream);
+    t_pt = now_s() - t0;
+    return pt_last.e2;
+  }
 
   void build_ham(int mode) {
     require_ints();
@@ -1112,6 +1141,8 @@ struct Context {
     }
     Eout.resize(nroots);
     for (int r = 0; r < nroots; ++r) Eout[r] = E0[r] + hints.coreE;
+    Evar = Eout;
+    run_eps2 = s.epsilon2;
     t_total = now_s() - t0;
   }
 };
@@ -1503,6 +1534,47 @@ int shci_run_input(shci_ctx* ctx, const char* input_path, const char* fcidump, i
     c.run(s, mode, block != 0, ev);
     if (nroots) *nroots = (int)ev.size();
     for (int r = 0; r < (int)ev.size() && r < cap_roots; ++r) E[r] = ev[r];
+  });
+}
+
+int shci_pt_deterministic(shci_ctx* ctx, const double* ci, double E0, double eps2, double* e2) {
+  return guarded(ctx, [&](Context& c) {
+    if (!ci || !e2) throw Error(SHCI_ERR_INVALID, "null argument");
+    c.require_dets();
+    c.ptc.resize(c.ndet);
+    SHCI_CUDA(cudaMemcpyAsync(c.ptc.p, ci, c.ndet * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    *e2 = c.perturb(c.ptc.p, E0, eps2);
+  });
+}
+
+int shci_run_pt(shci_ctx* ctx, double eps2, double* E, int cap_roots, int* nroots) {
+  return guarded(ctx, [&](Context& c) {
+    if (c.Evar.empty() || c.nroots_run != (int)c.Evar.size())
+      throw Error(SHCI_ERR_STATE, "no variational run to perturb (call shci_run_input first)");
+    if (!(eps2 > 0.0)) eps2 = c.run_eps2;
+    if (nroots) *nroots = (int)c.Evar.size();
+    for (int r = 0; r < (int)c.Evar.size(); ++r) {
+      const double e2 = c.perturb(c.ci.p + (size_t)r * c.ndet, c.Evar[r], eps2);
+      if (E && r < cap_roots) E[r] = c.Evar[r] + e2;
+    }
+  });
+}
+
+int shci_pt_stats(shci_ctx* ctx, int64_t* candidates, int64_t* unique, int* partitions, double* psi1_norm,
+                  double* seconds) {
+  return guarded(ctx, [&](Context& c) {
+    if (candidates) *candidates = c.pt_last.candidates;
+    if (unique) *unique = c.pt_last.unique;
+    if (partitions) *partitions = c.pt_last.partitions;
+    if (psi1_norm) *psi1_norm = c.pt_last.psi1_norm;
+    if (seconds) *seconds = c.t_pt;
+  });
+}
+
+int shci_set_pt_batch(shci_ctx* ctx, int64_t max_candidates) {
+  return guarded(ctx, [&](Context& c) {
+    if (max_candidates < 0) throw Error(SHCI_ERR_INVALID, "max_candidates must be >= 0");
+    c.pt_max_cand = max_candidates;
   });
 }
 

@@ -123,6 +123,25 @@ struct SelectParams {
   uint64_t rmask1[kMaxRestrict];  // bits 64..127
 };
 
+// Membership test in a DetHash (slots index into `dets`; linear probing).
+__device__ __forceinline__ bool hash_contains(const uint32_t* __restrict__ slots, uint64_t mask,
+                                              const Det2* __restrict__ dets, const Det2& x) {
+  uint64_t h = det_hash(x) & mask;
+  for (uint64_t probe = 0; probe <= mask; ++probe) {
+    uint32_t s = slots[h];
+    if (s == 0xffffffffu) return false;
+    Det2 y = dets[s];
+    if (det_eq(x, y)) return true;
+    h = (h + 1) & mask;
+  }
+  return false;
+}
+
+// Whether spin orbital p belongs to restriction r.
+__device__ __forceinline__ int in_mask(const SelectParams& sp, int r, int p) {
+  return p < 64 ? (int)((sp.rmask0[r] >> p) & 1ull) : (int)((sp.rmask1[r] >> (p - 64)) & 1ull);
+}
+
 // Candidates from every parent, dropping those already present (hash set);
 // returns the number of candidates written (may exceed cap: then nothing past
 // cap is written and the caller retries with a larger buffer).
@@ -143,6 +162,30 @@ double flip_parity(const double* x, size_t n, const int32_t* flip, const int8_t*
 // x <- (x + p F x) / 2 in place (p = +1 or -1), using tmp (n doubles)
 void flip_project(double* x, size_t n, const int32_t* flip, const int8_t* sign, double p, double* tmp,
                   cudaStream_t s);
+
+// ---- deterministic second-order perturbation theory (kernels_pt.cu) --------
+struct PtResult {
+  double e2 = 0.0;         // sum_a N_a^2 / (E0 - E_a)
+  double psi1_norm = 0.0;  // sum_a (N_a / (E0 - E_a))^2
+  int64_t candidates = 0;  // generated outside the variational space (before merging)
+  int64_t unique = 0;      // distinct determinants a
+  int partitions = 0;
+};
+struct PtWork {
+  DevBuf<int64_t> counts, offs;
+  DevBuf<Det2> cand;
+  DevBuf<double> num, part;
+  DevBuf<uint32_t> perm;
+  DevBuf<unsigned long long> next;
+};
+// E2 of the space `dets` (hash set `present` over it) with coefficients c
+// (device, n) for threshold eps2: candidates with |H_ai c_i| criteria of the
+// reference, numerators merged per determinant. E0 without the core energy.
+// sp supplies the occupation restrictions (its ncore/nact are not applied).
+// max_candidates > 0 caps one partition (default: from free device memory).
+PtResult pt_deterministic(const Det2* dets, size_t n, const double* c, double E0, double eps2, const IntsView& ints,
+                          const HeatBathView& hb, double maxEntry, const SelectParams& sp, const DetHash& present,
+                          int64_t max_candidates, PtWork& w, Prims& pr, cudaStream_t s);
 
 // ---- sigma and Davidson vector kernels (kernels_sigma.cu) -------------------
 // Y[:, c] (column-major, leading dimension ldy) = diag .* X[:, c] + Hoff X[:, c]

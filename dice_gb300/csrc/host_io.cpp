@@ -200,7 +200,7 @@ void build_heatbath(const HostInts& H, HostHeatBath& hb) {
 // Keywords accepted and ignored: they configure stages outside the
 // variational loop (perturbation theory, RDMs, I/O, restarts, SOC, cdfci).
 static const char* kIgnored[] = {
-    "epsilon2", "epsilon2Large", "sampleN", "nPTiter", "targetError", "deterministic", "io", "noio", "prefix",
+    "epsilon2Large", "sampleN", "nPTiter", "targetError", "io", "noio", "prefix",
     "printbestdeterminants", "printalldeterminants", "writebestdeterminants", "dordm", "DoOneRDM",
     "DoSpinOneRDM", "dospinrdm", "TransitionRDM", "DoThreeRDM", "DoFourRDM", "seed", "outputlevel",
     "num_thrds", "nblocks", "excitation", "nvirt", "extrapolate", "relaxedRDM", "quasiq", "dosoc",
@@ -300,6 +300,11 @@ void read_input(const std::string& path, Schedule& s) {
         s.mode = 1;
       else
         throw Error(kErrInvalid, "precision must be fp64 or mixed");
+    } else if (iequal(arg, "epsilon2")) {
+      need(1);
+      s.epsilon2 = std::atof(tok[1].c_str());
+    } else if (iequal(arg, "deterministic")) {
+      s.stochastic = false;
     } else if (iequal(arg, "blockdavidson")) {
       s.block = true;
     } else if (iequal(arg, "precond")) {

@@ -29,7 +29,8 @@ struct Restriction {
   uint64_t mask = 0;  // spatial orbitals
 };
 
-// Variational subset of the reference's schedule (SHCI/input.h:35-194).
+// Variational and deterministic-PT subset of the reference's schedule
+// (SHCI/input.h:35-194).
 struct Schedule {
   std::vector<std::vector<int>> occupied;
   std::vector<double> epsilon1;
@@ -43,6 +44,8 @@ struct Schedule {
   bool block = false;  // blockdavidson keyword
   int precond = -1;    // precond keyword: -1 unset, 0 plain, 1 pt2, 2 mlp
   int basis_max = 0, basis_keep = 0;  // davidsonBasis keyword: 0 = the reference's subspace
+  double epsilon2 = 1.e-8;  // PT threshold (SHCI/input.cpp:58)
+  bool stochastic = true;   // `deterministic` clears it (SHCI/input.cpp:322-323)
 };
 
 void split_tokens(const std::string& in, const char* delims, std::vector<std::string>& tok);

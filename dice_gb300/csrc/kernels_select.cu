@@ -35,23 +35,6 @@ struct SelArgs {
 constexpr int kSelThreads = 256;
 constexpr int kSelWarps = kSelThreads / 32;
 
-__device__ __forceinline__ bool hash_contains(const uint32_t* __restrict__ slots, uint64_t mask,
-                                              const Det2* __restrict__ dets, const Det2& x) {
-  uint64_t h = det_hash(x) & mask;
-  for (uint64_t probe = 0; probe <= mask; ++probe) {
-    uint32_t s = slots[h];
-    if (s == 0xffffffffu) return false;
-    Det2 y = dets[s];
-    if (det_eq(x, y)) return true;
-    h = (h + 1) & mask;
-  }
-  return false;
-}
-
-__device__ __forceinline__ int in_mask(const SelectParams& sp, int r, int p) {
-  return p < 64 ? (int)((sp.rmask0[r] >> p) & 1ull) : (int)((sp.rmask1[r] >> (p - 64)) & 1ull);
-}
-
 // Warp-aggregated append of one candidate per lane with `emit` set.
 __device__ __forceinline__ void append(const SelArgs& a, bool emit, const Det2& cand) {
   const int lane = threadIdx.x & 31;

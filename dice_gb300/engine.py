@@ -61,6 +61,10 @@ SIGNATURES = [
     ("shci_mlp_set_params", _i32, [_vp, _vp, _i32, _dbl]),
     ("shci_mlp_gradient", _i32, [_vp, _vp, _vp, _i32, _dbl, _vp, _P(ctypes.c_float)]),
     ("shci_run_stats", _i32, [_vp, _P(_i64), _P(_dbl), _P(ctypes.c_float)]),
+    ("shci_pt_deterministic", _i32, [_vp, _vp, _dbl, _dbl, _P(_dbl)]),
+    ("shci_run_pt", _i32, [_vp, _dbl, _vp, _i32, _P(_i32)]),
+    ("shci_pt_stats", _i32, [_vp, _P(_i64), _P(_i64), _P(_i32), _P(_dbl), _P(_dbl)]),
+    ("shci_set_pt_batch", _i32, [_vp, _i64]),
     ("shci_launch_count", _i32, [_vp, _P(_i64)]),
 ]
 
@@ -375,6 +379,34 @@ class Engine:
         it, tm, loss = ctypes.c_int64(), ctypes.c_double(), ctypes.c_float()
         self._check(load_library().shci_run_stats(self.h, ctypes.byref(it), ctypes.byref(tm), ctypes.byref(loss)))
         return {"davidson_iters": it.value, "t_mlp": tm.value, "mlp_loss": loss.value}
+
+    def pt_deterministic(self, ci, E0, eps2):
+        """Deterministic PT2 correction E2 of the current space for host
+        coefficients ci (one per determinant); E0 includes the core energy."""
+        c = np.ascontiguousarray(ci, dtype=np.float64)
+        if c.shape != (self.ndets(),):
+            raise ValueError("ci must hold one coefficient per determinant")
+        e2 = ctypes.c_double()
+        self._check(load_library().shci_pt_deterministic(self.h, _p(c), float(E0), float(eps2), ctypes.byref(e2)))
+        return e2.value
+
+    def run_pt(self, eps2=-1.0):
+        """After run_input: E_var + E2 per root (eps2 <= 0: the input's epsilon2)."""
+        E = np.zeros(16)
+        nr = ctypes.c_int()
+        self._check(load_library().shci_run_pt(self.h, float(eps2), _p(E), 16, ctypes.byref(nr)))
+        return E[:nr.value].copy()
+
+    def pt_stats(self):
+        c, u, n = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int()
+        psi, t = ctypes.c_double(), ctypes.c_double()
+        self._check(load_library().shci_pt_stats(self.h, ctypes.byref(c), ctypes.byref(u), ctypes.byref(n),
+                                                 ctypes.byref(psi), ctypes.byref(t)))
+        return {"candidates": c.value, "unique": u.value, "partitions": n.value, "psi1_norm": psi.value,
+                "seconds": t.value}
+
+    def set_pt_batch(self, max_candidates):
+        self._check(load_library().shci_set_pt_batch(self.h, int(max_candidates)))
 
     def launch_count(self):
         n = ctypes.c_int64()

@@ -193,6 +193,33 @@ int shci_run_log(shci_ctx* ctx, int cap, int* niter, int64_t* ndets, double* ene
 /* Coefficient vectors of the last run's final space, host out (nroots x N). */
 int shci_run_ci(shci_ctx* ctx, double* out, int64_t cap);
 
+/* Deterministic second-order (Epstein-Nesbet) perturbation theory.
+ * Replaces SHCIbasics::DoPerturbativeDeterministic (SHCI/SHCIbasics.cpp:453-728,
+ * without its RDM branch) and its generator
+ * SHCIgetdeterminants::getDeterminantsDeterministicPT
+ * (SHCI/SHCIgetdeterminants.cpp:40-171), as selected by `deterministic` in
+ * the input (SHCI/SHCI.cpp:707-721).
+ * shci_pt_deterministic: E2 for the context's current space with coefficients
+ *   ci (host, one per determinant, in the order of shci_dets_get), E0 the
+ *   variational energy WITH coreE (as the reference passes it), threshold
+ *   eps2 (>= 0). The caller adds E0 to get the PT energy. The selection
+ *   restrictions of shci_set_selection_params apply; ncore/nact do not.
+ * shci_run_pt: after shci_run_input, E[r] = E_var[r] + E2[r] for every root
+ *   (what the reference writes to shci.e), eps2 <= 0 taking the input's
+ *   epsilon2 (default 1e-8, SHCI/input.cpp:58).
+ * shci_pt_stats: of the last PT call: candidates generated outside the
+ *   variational space before merging, distinct determinants, hash partitions
+ *   used, first-order norm sum_a (N_a / (E0 - E_a))^2, seconds.
+ * shci_set_pt_batch: cap on the candidates held on the device at once
+ *   (0 = from free memory). Larger candidate sets are split into hash
+ *   partitions, as the reference splits them over MPI ranks; E2 agrees to
+ *   rounding across partition counts. */
+int shci_pt_deterministic(shci_ctx* ctx, const double* ci, double E0, double eps2, double* e2);
+int shci_run_pt(shci_ctx* ctx, double eps2, double* E, int cap_roots, int* nroots);
+int shci_pt_stats(shci_ctx* ctx, int64_t* candidates, int64_t* unique, int* partitions, double* psi1_norm,
+                  double* seconds);
+int shci_set_pt_batch(shci_ctx* ctx, int64_t max_candidates);
+
 /* Stage timings of the last run in seconds: selection, Hamiltonian build,
  * Davidson, total; and the sigma calls/time spent inside Davidson. */
 int shci_run_timings(shci_ctx* ctx, double* t_select, double* t_ham, double* t_davidson, double* t_total,

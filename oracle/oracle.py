@@ -81,7 +81,7 @@ def lib():
         L.orc_input_epsilon2.argtypes = [vp]
         L.orc_input_deterministic.restype = i32
         L.orc_input_deterministic.argtypes = [vp]
-        L.orc_pt_stats.argtypes = [vp, vp, vp, vp]
+        L.orc_pt_stats.argtypes = [vp, vp, vp, vp, vp]
         _lib = L
     return _lib
 
@@ -103,9 +103,9 @@ def _pack_restrictions(restrictions):
 
 
 def _pt_stats(h):
-    c, u, p = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_double()
-    lib().orc_pt_stats(h, ctypes.byref(c), ctypes.byref(u), ctypes.byref(p))
-    return dict(candidates=c.value, unique=u.value, psi1_norm=p.value)
+    c, u, p, o = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_double(), ctypes.c_int64()
+    lib().orc_pt_stats(h, ctypes.byref(c), ctypes.byref(u), ctypes.byref(p), ctypes.byref(o))
+    return dict(candidates=c.value, unique=u.value, psi1_norm=p.value, outside=o.value)
 
 
 class Oracle:

@@ -622,6 +622,7 @@ static void pt_from_parent(const Ints& I, const HeatBath& hb, const Det& d, doub
 
 struct PtStats {
   int64_t candidates = 0, unique = 0;
+  int64_t outside = 0;  // candidates not in the variational space, before merging
   double psi1_norm = 0.0;
 };
 
@@ -637,6 +638,7 @@ static double pt_deterministic(const Ints& I, const HeatBath& hb, const Det* det
   std::vector<PtCand> all;
   for (size_t i = 0; i < n; i++) pt_from_parent(I, hb, dets[i], fabs(eps2 / ci[i]), ci[i], rs, all);
   st.candidates = (int64_t)all.size();
+  st.outside = 0;
   std::stable_sort(all.begin(), all.end(), [](const PtCand& x, const PtCand& y) { return det_less(x.d, y.d); });
   std::vector<Det> sorted(dets, dets + n);
   std::sort(sorted.begin(), sorted.end(), det_less);
@@ -650,6 +652,7 @@ static double pt_deterministic(const Ints& I, const HeatBath& hb, const Det* det
     while (v < sorted.size() && det_less(sorted[v], all[k].d)) ++v;
     bool present = v < sorted.size() && det_eq(sorted[v], all[k].d);
     if (!present) {
+      st.outside += (int64_t)(e - k);
       const double de = E0 - all[k].E;
       psi += pow(fabs(num / de), 2);
       e2 += pow(fabs(num), 2) / de;
@@ -1358,7 +1361,8 @@ double orc_var_pt(orc_ctx* c, int root, double eps2) {
 }
 double orc_input_epsilon2(orc_ctx* c) { return c->sched.epsilon2; }
 int orc_input_deterministic(orc_ctx* c) { return c->sched.stochastic ? 0 : 1; }
-void orc_pt_stats(orc_ctx* c, int64_t* candidates, int64_t* unique, double* psi1_norm) {
+void orc_pt_stats(orc_ctx* c, int64_t* candidates, int64_t* unique, double* psi1_norm, int64_t* outside) {
+  *outside = c->pt.outside;
   *candidates = c->pt.candidates;
   *unique = c->pt.unique;
   *psi1_norm = c->pt.psi1_norm;
