@@ -88,16 +88,19 @@ __device__ __forceinline__ double pt_double_sign(Det2 di, int a, int b, int i, i
   return ((n1 + n2) & 1) ? -1.0 : 1.0;
 }
 
-// Warp-uniform count / ordered write of the lanes with `keep`.
+// Warp-uniform count / ordered write of the lanes with `keep`. Writes stay
+// inside the parent's range [base, lim) of the counting pass.
 template <bool EMIT>
 __device__ __forceinline__ void pt_put(const PtArgs& a, bool keep, const Det2& cand, double v, int64_t base,
-                                       int64_t& cnt) {
+                                       int64_t lim, int64_t& cnt) {
   const int lane = threadIdx.x & 31;
   const unsigned m = __ballot_sync(kFull, keep);
   if (EMIT && keep) {
     const int64_t q = base + cnt + __popc(m & ((1u << lane) - 1u));
-    a.out[q] = cand;
-    a.num[q] = v;
+    if (q < lim) {
+      a.out[q] = cand;
+      a.num[q] = v;
+    }
   }
   cnt += __popc(m);
 }
@@ -121,6 +124,7 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
     const double cp = a.c[p];
     const double eps = fabs(a.eps2 / cp);
     const int64_t base = EMIT ? a.offs[p] : 0;
+    const int64_t lim = EMIT ? base + a.counts[p] : 0;
     int64_t cnt = 0;
     if (eps < INFINITY) {  // c_i = 0: nothing passes either threshold
       __syncwarp();
@@ -164,7 +168,7 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
             }
           }
         }
-        pt_put<EMIT>(a, keep, cand, v, base, cnt);
+        pt_put<EMIT>(a, keep, cand, v, base, lim, cnt);
       }
 
       // ---- doubles: heat-bath list prefixes, flattened over the warp
@@ -248,7 +252,7 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
                 if (keep) v = (double)vals[index] * pt_double_sign(cand, av, bv, oci, ocj) * cp;
               }
             }
-            pt_put<EMIT>(a, keep, cand, v, base, cnt);
+            pt_put<EMIT>(a, keep, cand, v, base, lim, cnt);
           }
         }
       }
