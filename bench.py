@@ -33,6 +33,8 @@ sys.path.insert(0, ROOT)
 
 WORKLOAD = "mol24"
 CPU_SAMPLE_DETS = 100000
+# deterministic PT2 on the final mixed-precision space of the workload
+PT_EPS2 = 1e-5
 # DRAM bytes per mixed-sigma launch divided by its algorithmic bytes, from one
 # ncu capture of the medium case (4.4831 GB measured / 4.4546 GB algorithmic);
 # the full-size launch is too large to capture, and its traffic scales with
@@ -178,6 +180,46 @@ def run_reference(args):
             "e2e": {"value": val, "unit": "Mdets/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "Dice cannot be built here (needs Boost and MPI); the CPU oracle restating its serial path is timed"}
     print(json.dumps(line), flush=True)
+
+
+def pt_section(e, E0, steps, cpu_leg, fcidump):
+    """Deterministic PT2 (Epstein-Nesbet) of the final space through the
+    C-ABI (host coefficients in, E2 out): candidates outside the variational
+    space generated, merged and summed per second. CPU leg: the oracle's
+    restatement on a bounded sample of parents (the middle of the space,
+    doubled until it takes 5 s), against the whole space for removal."""
+    ci = e.run_ci(1)[0]
+    e.pt_deterministic(ci, E0, PT_EPS2)  # warm-up: allocations
+    ts = []
+    for _ in range(max(2, steps // 4)):
+        t0 = time.perf_counter()
+        e2 = e.pt_deterministic(ci, E0, PT_EPS2)
+        ts.append(time.perf_counter() - t0)
+    st = e.pt_stats()
+    t = statistics.mean(ts)
+    out = {"eps2": PT_EPS2, "E_var": E0, "E2": e2, "E_total": E0 + e2, "candidates": st["candidates"],
+           "unique": st["unique"], "partitions": st["partitions"], "psi1_norm": st["psi1_norm"],
+           "seconds": t, "reps": len(ts), "Mcand_s": st["candidates"] / t / 1e6,
+           "what": "shci_pt_deterministic on the final mixed-precision space (the reference's "
+                   "DoPerturbativeDeterministic): count, scan, emit, radix sort, per-run reduction"}
+    if cpu_leg:
+        from oracle import oracle as orc
+        dets = e.dets()
+        o = orc.Oracle(fcidump)
+        n = len(dets)
+        p0, k = n // 2, 256
+        while True:
+            t0 = time.perf_counter()
+            _, sto = o.pt_det_range(dets, ci, E0, PT_EPS2, p0, min(n, p0 + k))
+            tc = time.perf_counter() - t0
+            if tc > 5.0 or p0 + k >= n:
+                break
+            k *= 2
+        out["cpu_oracle"] = {"Mcand_s": sto["outside"] / tc / 1e6, "cores": 1, "kind": "port", "seconds": tc,
+                             "sample": "parents [%d, %d) of %d, %d candidates outside the space"
+                                       % (p0, min(n, p0 + k), n, sto["outside"])}
+        out["speedup_vs_cpu_oracle"] = out["Mcand_s"] / out["cpu_oracle"]["Mcand_s"]
+    return out
 
 
 def other_configs(work, device):
@@ -386,6 +428,8 @@ def run_ours(args):
     }
     if cpu:
         line["cpu_baseline"] = cpu
+    line["pt"] = pt_section(e, float(E32[0]), args.steps, rank == 0 and not args.no_cpu,
+                            os.path.join(os.path.dirname(inp), "FCIDUMP"))
     e.close()
     if args.case == "full" and not args.no_configs:
         line["configs"] = other_configs(work, local)

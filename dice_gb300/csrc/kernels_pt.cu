@@ -380,7 +380,9 @@ PtResult pt_deterministic(const Det2* dets, size_t n, const double* c, double E0
   cap = std::min<int64_t>(cap, (int64_t)0xfffffff0u);
   if (cap < 1) throw Error(kErrOOM, "no device memory left for perturbation candidates");
 
+  PhaseTimer pt(s);
   const int64_t total_all = gen(false, 1, 0);
+  pt.mark("pt count");
   uint32_t nparts = total_all <= cap ? 1u : (uint32_t)((total_all + total_all / 8) / cap + 1);
   const size_t smem = 2 * sizeof(double) * ints.norb * ints.norb;
   SHCI_CUDA(cudaFuncSetAttribute(k_pt_reduce, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -401,12 +403,15 @@ PtResult pt_deterministic(const Det2* dets, size_t n, const double* c, double E0
       w.num.reserve((size_t)m);
       w.perm.resize((size_t)m);
       gen(true, nparts, part);
+      pt.mark("pt emit");
       k_pt_iota<<<grid_for((size_t)m, 256), 256, 0, s>>>(w.perm.p, (size_t)m);
       SHCI_LAUNCH_CHECK();
       sort_dets(w.cand.p, w.perm.p, (size_t)m, pr, s);
+      pt.mark("pt sort");
       k_pt_reduce<<<kPtRedBlocks, kPtRedThreads, smem, s>>>(w.cand.p, w.perm.p, w.num.p, (size_t)m, ints, E0,
                                                             w.part.p);
       SHCI_LAUNCH_CHECK();
+      pt.mark("pt reduce");
       SHCI_CUDA(cudaMemcpyAsync(hp.data(), w.part.p, hp.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
       SHCI_CUDA(cudaStreamSynchronize(s));
       for (unsigned b = 0; b < kPtRedBlocks; ++b) {

@@ -75,6 +75,8 @@ def lib():
         L.orc_var_ci.argtypes = [vp, i32, vp]
         L.orc_pt_det.restype = dbl
         L.orc_pt_det.argtypes = [vp, vp, i64, vp, dbl, dbl, vp, i32]
+        L.orc_pt_det_range.restype = dbl
+        L.orc_pt_det_range.argtypes = [vp, vp, i64, vp, dbl, dbl, i64, i64]
         L.orc_var_pt.restype = dbl
         L.orc_var_pt.argtypes = [vp, i32, dbl]
         L.orc_input_epsilon2.restype = dbl
@@ -183,6 +185,14 @@ class Oracle:
         ci = np.ascontiguousarray(ci, dtype=np.float64)
         r = _pack_restrictions(restrictions)
         e2 = lib().orc_pt_det(self.h, _p(dets), len(dets), _p(ci), E0, eps2, _p(r), len(restrictions))
+        return e2, _pt_stats(self.h)
+
+    def pt_det_range(self, dets, ci, E0, eps2, p0, p1):
+        """pt_det with the candidates of parents [p0, p1) only (no
+        restrictions), for timing a bounded sample."""
+        dets = np.ascontiguousarray(dets, dtype=np.uint64)
+        ci = np.ascontiguousarray(ci, dtype=np.float64)
+        e2 = lib().orc_pt_det_range(self.h, _p(dets), len(dets), _p(ci), E0, eps2, p0, p1)
         return e2, _pt_stats(self.h)
 
     def ham(self, dets):

@@ -633,10 +633,17 @@ struct PtStats {
 // SHCI/SHCISortMpiUtils.cpp:541-640), determinants of the variational space
 // removed (StitchDEH::RemoveDetsPresentIn, :750-800), then
 // E2 = sum |N_a|^2 / (E0 - E_a). E0 and the energies include coreE.
+// Parents [p0, p1) only when p1 > p0 (a bounded sample for timing); the
+// whole space is still removed from the candidates.
 static double pt_deterministic(const Ints& I, const HeatBath& hb, const Det* dets, size_t n, const double* ci,
-                               double E0, double eps2, std::vector<Restriction> rs, PtStats& st) {
+                               double E0, double eps2, std::vector<Restriction> rs, PtStats& st, size_t p0 = 0,
+                               size_t p1 = 0) {
   std::vector<PtCand> all;
-  for (size_t i = 0; i < n; i++) pt_from_parent(I, hb, dets[i], fabs(eps2 / ci[i]), ci[i], rs, all);
+  if (p1 <= p0) {
+    p0 = 0;
+    p1 = n;
+  }
+  for (size_t i = p0; i < p1 && i < n; i++) pt_from_parent(I, hb, dets[i], fabs(eps2 / ci[i]), ci[i], rs, all);
   st.candidates = (int64_t)all.size();
   st.outside = 0;
   std::stable_sort(all.begin(), all.end(), [](const PtCand& x, const PtCand& y) { return det_less(x.d, y.d); });
@@ -1349,6 +1356,12 @@ double orc_pt_det(orc_ctx* c, const uint64_t* dets, int64_t n, const double* ci,
                   const int64_t* restr, int nrestr) {
   return pt_deterministic(c->ints, c->hb, (const Det*)dets, (size_t)n, ci, E0, eps2,
                           unpack_restrictions(restr, nrestr), c->pt);
+}
+// The same with the candidates of parents [p0, p1) only.
+double orc_pt_det_range(orc_ctx* c, const uint64_t* dets, int64_t n, const double* ci, double E0, double eps2,
+                        int64_t p0, int64_t p1) {
+  return pt_deterministic(c->ints, c->hb, (const Det*)dets, (size_t)n, ci, E0, eps2, {}, c->pt, (size_t)p0,
+                          (size_t)p1);
 }
 
 // PT2 on the result of orc_run_input for one root, eps2 <= 0 taking the
