@@ -172,11 +172,10 @@ struct PtResult {
   int partitions = 0;
 };
 struct PtWork {
-  DevBuf<int64_t> counts, offs;
   DevBuf<Det2> cand;
-  DevBuf<double> num, part;
+  DevBuf<double> num, en, part;
   DevBuf<uint32_t> perm;
-  DevBuf<unsigned long long> next;
+  DevBuf<unsigned long long> next;  // parent queue, candidate counter
 };
 // E2 of the space `dets` (hash set `present` over it) with coefficients c
 // (device, n) for threshold eps2: candidates with |H_ai c_i| criteria of the

@@ -14,19 +14,25 @@
 // variational space removed, and E2 = sum_a N_a^2 / (E0 - E_a).
 //
 // GPU form (one launch sequence per hash partition):
-//   k_pt_gen<false>  one warp per parent (dynamic queue) counts the candidates
-//                    outside the variational space (hash probe) that fall in
-//                    this partition;
-//   exclusive scan   -> each parent's output offset, so the output is in
-//                    (parent, generation) order whatever the warp schedule;
-//   k_pt_gen<true>   the same walk writes (determinant, numerator);
-//   radix sort       stable, by determinant, with the candidate index as payload;
-//   k_pt_reduce      one thread per run of equal determinants: numerators summed
-//                    in parent order, E_a from the integrals, fixed-grid block
-//                    partials summed on the host in block order.
-// Results are therefore bitwise reproducible for a given partition count.
-// When the candidates do not fit in device memory they are split by a hash of
-// the determinant, as the reference splits them over MPI ranks
+//   k_pt_gen     one warp per parent (dynamic queue); candidates outside the
+//                variational space (hash probe) in this partition are
+//                appended (warp-aggregated atomics) with their numerator and
+//                energy. The energy is updated from the parent's in O(1):
+//                with F_p = sum_{q occupied} V(p, q) and V the same-spin-aware
+//                Coulomb-minus-exchange, a single i -> a changes E by
+//                h_aa - h_ii + F_a - F_i - V(a, i), a double by the analogous
+//                pair terms (the reference's EnergyAfterExcitation,
+//                SHCI/Determinants.cpp:124-249, sums the same terms in a loop);
+//   radix sort   by determinant, candidate index as payload;
+//   k_pt_reduce  one thread per run of equal determinants: the numerators are
+//                summed exactly in 128-bit fixed point (2^-80 units), so the
+//                sum does not depend on the order the atomics left the run in,
+//                E_a is the minimum over the run (the copies differ only by
+//                rounding), and N^2 / (E0 - E_a) goes into fixed-grid block
+//                partials summed on the host in block order.
+// E2 is therefore bitwise reproducible for a given partition count.
+// Candidates that do not fit in device memory are split by a hash of the
+// determinant, as the reference splits them over MPI ranks
 // (SHCI/SHCIbasics.cpp:519-530); each partition is generated, sorted and
 // reduced alone.
 #include <algorithm>
@@ -40,11 +46,13 @@ namespace {
 
 constexpr int kPtThreads = 256;
 constexpr int kPtWarps = kPtThreads / 32;
+constexpr unsigned kPtGenBlocks = 152 * 6;
 constexpr unsigned kPtRedBlocks = 152 * 4;
 constexpr int kPtRedThreads = 256;
 // device bytes per candidate in one partition: determinant (16), numerator (8),
-// sort payload (4), the sort's split words and alternates (16 + 16 + 4)
-constexpr size_t kPtBytesPerCand = 64;
+// energy (8), sort payload (4), the sort's split words and alternates (16 + 16 + 4)
+constexpr size_t kPtBytesPerCand = 72;
+constexpr int kFixBits = 80;  // fixed-point numerator sums in units of 2^-80
 
 inline unsigned grid_for(size_t n, int threads, size_t max_blocks = 152 * 64) {
   size_t b = (n + threads - 1) / threads;
@@ -65,11 +73,12 @@ struct PtArgs {
   const uint32_t* hslots;
   uint64_t hmask;
   uint32_t nparts, part;
-  unsigned long long* next;
-  int64_t* counts;
-  const int64_t* offs;
+  unsigned long long* next;     // parent queue
+  unsigned long long* counter;  // candidates appended (counts past cap too)
+  int64_t cap;
   Det2* out;
   double* num;
+  double* en;
 };
 
 __device__ __forceinline__ bool in_part(const PtArgs& a, const Det2& d) {
@@ -88,31 +97,52 @@ __device__ __forceinline__ double pt_double_sign(Det2 di, int a, int b, int i, i
   return ((n1 + n2) & 1) ? -1.0 : 1.0;
 }
 
-// Warp-uniform count / ordered write of the lanes with `keep`. Writes stay
-// inside the parent's range [base, lim) of the counting pass.
-template <bool EMIT>
-__device__ __forceinline__ void pt_put(const PtArgs& a, bool keep, const Det2& cand, double v, int64_t base,
-                                       int64_t lim, int64_t& cnt) {
+// Warp-aggregated append of the lanes with `keep`; slots past cap are counted
+// but not written.
+__device__ __forceinline__ void pt_put(const PtArgs& a, bool keep, const Det2& cand, double v, double e) {
   const int lane = threadIdx.x & 31;
   const unsigned m = __ballot_sync(kFull, keep);
-  if (EMIT && keep) {
-    const int64_t q = base + cnt + __popc(m & ((1u << lane) - 1u));
-    if (q < lim) {
+  if (!m) return;
+  const int leader = __ffs(m) - 1;
+  unsigned long long base = 0;
+  if (lane == leader) base = atomicAdd(a.counter, (unsigned long long)__popc(m));
+  base = __shfl_sync(kFull, base, leader);
+  if (keep) {
+    const unsigned long long q = base + __popc(m & ((1u << lane) - 1u));
+    if (q < (unsigned long long)a.cap) {
       a.out[q] = cand;
       a.num[q] = v;
+      a.en[q] = e;
     }
   }
-  cnt += __popc(m);
 }
 
-template <bool EMIT>
+// V(p, q): Coulomb minus (same spin only) exchange of spin orbitals p, q,
+// from the n x n Direct/Exchange tables staged in shared memory.
+__device__ __forceinline__ double vpair(const double* sD, const double* sX, int n, int p, int q) {
+  const int o = (p >> 1) * n + (q >> 1);
+  return ((p ^ q) & 1) ? sD[o] : __dsub_rn(sD[o], sX[o]);
+}
+
 __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
+  extern __shared__ double smd[];
   __shared__ unsigned char s_closed[kPtWarps][kMaxSpin];
   __shared__ unsigned char s_open[kPtWarps][kMaxSpin];
+  __shared__ double s_F[kPtWarps][kMaxSpin];
+  const int n = a.ints.norb, nn = n * n;
+  double* sD = smd;
+  double* sX = smd + nn;
+  for (int j = threadIdx.x; j < nn; j += blockDim.x) {
+    sD[j] = a.ints.Direct[j];
+    sX[j] = a.ints.Exchange[j];
+  }
+  __syncthreads();
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   unsigned char* closed = s_closed[wib];
   unsigned char* open = s_open[wib];
-  const int n2 = 2 * a.ints.norb;
+  double* F = s_F[wib];
+  const int n2 = 2 * n;
+  const int ld1 = n2 + 1;  // diagonal stride of the (2n)x(2n) one-electron matrix
   const SelectParams& sp = a.sp;
   while (true) {
     unsigned long long pp = 0;
@@ -123,141 +153,155 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
     const Det2 d = a.dets[p];
     const double cp = a.c[p];
     const double eps = fabs(a.eps2 / cp);
-    const int64_t base = EMIT ? a.offs[p] : 0;
-    const int64_t lim = EMIT ? base + a.counts[p] : 0;
-    int64_t cnt = 0;
-    if (eps < INFINITY) {  // c_i = 0: nothing passes either threshold
-      __syncwarp();
-      if (lane == 0) {
-        int nc = 0, no = 0;
-        for (int q = 0; q < n2; ++q) {
-          if (det_getocc(d, q))
-            closed[nc++] = (unsigned char)q;
-          else
-            open[no++] = (unsigned char)q;
-        }
-      }
-      __syncwarp();
-      const int nclosed = __popcll(d.w0) + __popcll(d.w1);
-      const int nopen = n2 - nclosed;
-      int cur[kMaxRestrict];
-      for (int r = 0; r < sp.nrestrict; ++r) cur[r] = __popcll(d.w0 & sp.rmask0[r]) + __popcll(d.w1 & sp.rmask1[r]);
-
-      // ---- singles: every same-spin (i, a); the exact element decides
-      const int ns = nclosed * nopen;
-      for (int b0 = 0; b0 < ns; b0 += 32) {
-        const int q = b0 + lane;
-        bool keep = false;
-        Det2 cand = d;
-        double v = 0.0;
-        if (q < ns) {
-          const int ci = closed[q / nopen], oa = open[q % nopen];
-          // a spin flip has a zero element (no alpha-beta block in I1)
-          bool ok = (ci & 1) == (oa & 1);
-          for (int r = 0; ok && r < sp.nrestrict; ++r) {
-            int e = cur[r] - in_mask(sp, r, ci) + in_mask(sp, r, oa);
-            ok = e >= sp.rmin[r] && e <= sp.rmax[r];
-          }
-          if (ok) {
-            const double h = hij_single(a.ints, d, oa, ci);
-            if (fabs(h) > eps) {
-              det_flip(cand, oa);
-              det_flip(cand, ci);
-              keep = in_part(a, cand) && !hash_contains(a.hslots, a.hmask, a.dets, cand);
-              v = h * cp;
-            }
-          }
-        }
-        pt_put<EMIT>(a, keep, cand, v, base, lim, cnt);
-      }
-
-      // ---- doubles: heat-bath list prefixes, flattened over the warp
-      if (!(fabs(a.maxEntry) < eps)) {
-        const int npairs = nclosed * (nclosed - 1) / 2;
-        for (int pb = 0; pb < npairs; pb += 32) {
-          const int q = pb + lane;
-          int ci = 0, cj = 0;
-          int64_t lstart = 0, len = 0;
-          bool same = false;
-          if (q < npairs) {
-            // q -> (i, j), i > j, q = i(i-1)/2 + j
-            int i = (int)((1.0 + sqrt(1.0 + 8.0 * (double)q)) * 0.5);
-            while (i * (i - 1) / 2 > q) --i;
-            while ((i + 1) * i / 2 <= q) ++i;
-            const int j = q - i * (i - 1) / 2;
-            ci = closed[i];
-            cj = closed[j];
-            const int I = ci >> 1, J = cj >> 1;
-            const int X = I > J ? I : J, Y = I > J ? J : I;
-            const int pair = X * (X + 1) / 2 + Y;
-            same = (ci & 1) == (cj & 1);
-            const int64_t* st = same ? a.hb.sameStart : a.hb.oppStart;
-            const float* vals = same ? a.hb.sameVal : a.hb.oppVal;
-            const int64_t s0 = st[pair], s1 = st[pair + 1];
-            // first entry with |v| < eps (lists sorted by |v| descending)
-            int64_t lo = s0, hi = s1;
-            while (lo < hi) {
-              const int64_t mid = (lo + hi) >> 1;
-              if ((double)fabsf(vals[mid]) < eps)
-                hi = mid;
-              else
-                lo = mid + 1;
-            }
-            lstart = s0;
-            len = lo - s0;
-          }
-          int64_t incl = len;
-#pragma unroll
-          for (int o = 1; o < 32; o <<= 1) {
-            const int64_t y = __shfl_up_sync(kFull, incl, o);
-            if (lane >= o) incl += y;
-          }
-          const int64_t total = __shfl_sync(kFull, incl, 31);
-          const int64_t excl = incl - len;
-          for (int64_t f0 = 0; f0 < total; f0 += 32) {
-            const int64_t f = f0 + lane;
-            // owner lane of flattened entry f: last lane with excl <= f
-            int lo = 0;
-#pragma unroll
-            for (int st = 16; st >= 1; st >>= 1) {
-              const int c = lo + st;
-              const int64_t e = __shfl_sync(kFull, excl, c < 32 ? c : 31);
-              if (c < 32 && e <= f) lo = c;
-            }
-            const int64_t ls = __shfl_sync(kFull, lstart, lo);
-            const int64_t eo = __shfl_sync(kFull, excl, lo);
-            const int oci = __shfl_sync(kFull, ci, lo);
-            const int ocj = __shfl_sync(kFull, cj, lo);
-            const bool osame = __shfl_sync(kFull, (int)same, lo) != 0;
-            bool keep = false;
-            Det2 cand = d;
-            double v = 0.0;
-            if (f < total) {
-              const int64_t index = ls + (f - eo);
-              const int16_t* pr = osame ? a.hb.samePairs : a.hb.oppPairs;
-              const float* vals = osame ? a.hb.sameVal : a.hb.oppVal;
-              const int av = 2 * pr[2 * index] + (oci & 1);
-              const int bv = 2 * pr[2 * index + 1] + (ocj & 1);
-              bool ok = true;
-              for (int r = 0; ok && r < sp.nrestrict; ++r) {
-                int e = cur[r] - in_mask(sp, r, oci) - in_mask(sp, r, ocj) + in_mask(sp, r, av) + in_mask(sp, r, bv);
-                ok = e >= sp.rmin[r] && e <= sp.rmax[r];
-              }
-              if (ok && !(det_getocc(d, av) || det_getocc(d, bv))) {
-                det_flip(cand, av);
-                det_flip(cand, bv);
-                det_flip(cand, oci);
-                det_flip(cand, ocj);
-                keep = in_part(a, cand) && !hash_contains(a.hslots, a.hmask, a.dets, cand);
-                if (keep) v = (double)vals[index] * pt_double_sign(cand, av, bv, oci, ocj) * cp;
-              }
-            }
-            pt_put<EMIT>(a, keep, cand, v, base, lim, cnt);
-          }
-        }
+    if (!(eps < INFINITY)) continue;  // c_i = 0: nothing passes either threshold
+    __syncwarp();
+    if (lane == 0) {
+      int nc = 0, no = 0;
+      for (int q = 0; q < n2; ++q) {
+        if (det_getocc(d, q))
+          closed[nc++] = (unsigned char)q;
+        else
+          open[no++] = (unsigned char)q;
       }
     }
-    if (!EMIT && lane == 0) a.counts[p] = cnt;
+    __syncwarp();
+    const int nclosed = __popcll(d.w0) + __popcll(d.w1);
+    const int nopen = n2 - nclosed;
+    // F_q = sum over occupied r of V(q, r) (V(q, q) = 0), and the parent's energy
+    double ed = 0.0;
+    for (int q = lane; q < n2; q += 32) {
+      double f = 0.0;
+      for (int k = 0; k < nclosed; ++k) f += vpair(sD, sX, n, q, closed[k]);
+      F[q] = f;
+      if (det_getocc(d, q)) ed += __ldg(a.ints.I1 + (size_t)q * ld1) + 0.5 * f;
+    }
+    for (int o = 16; o; o >>= 1) ed += __shfl_xor_sync(kFull, ed, o);
+    __syncwarp();
+    int cur[kMaxRestrict];
+    for (int r = 0; r < sp.nrestrict; ++r) cur[r] = __popcll(d.w0 & sp.rmask0[r]) + __popcll(d.w1 & sp.rmask1[r]);
+
+    // ---- singles: every same-spin (i, a); the exact element decides
+    const int ns = nclosed * nopen;
+    for (int b0 = 0; b0 < ns; b0 += 32) {
+      const int q = b0 + lane;
+      bool keep = false;
+      Det2 cand = d;
+      double v = 0.0, e = 0.0;
+      if (q < ns) {
+        const int ci = closed[q / nopen], oa = open[q % nopen];
+        // a spin flip has a zero element (no alpha-beta block in I1)
+        bool ok = (ci & 1) == (oa & 1);
+        for (int r = 0; ok && r < sp.nrestrict; ++r) {
+          int c2 = cur[r] - in_mask(sp, r, ci) + in_mask(sp, r, oa);
+          ok = c2 >= sp.rmin[r] && c2 <= sp.rmax[r];
+        }
+        if (ok) {
+          const double h = hij_single(a.ints, d, oa, ci);
+          if (fabs(h) > eps) {
+            det_flip(cand, oa);
+            det_flip(cand, ci);
+            keep = in_part(a, cand) && !hash_contains(a.hslots, a.hmask, a.dets, cand);
+            if (keep) {
+              v = h * cp;
+              e = ed - __ldg(a.ints.I1 + (size_t)ci * ld1) + __ldg(a.ints.I1 + (size_t)oa * ld1) - F[ci] + F[oa] -
+                  vpair(sD, sX, n, oa, ci);
+            }
+          }
+        }
+      }
+      pt_put(a, keep, cand, v, e);
+    }
+
+    // ---- doubles: heat-bath list prefixes, flattened over the warp
+    if (fabs(a.maxEntry) < eps) continue;
+    const int npairs = nclosed * (nclosed - 1) / 2;
+    for (int pb = 0; pb < npairs; pb += 32) {
+      const int q = pb + lane;
+      int ci = 0, cj = 0;
+      int64_t lstart = 0, len = 0;
+      bool same = false;
+      if (q < npairs) {
+        // q -> (i, j), i > j, q = i(i-1)/2 + j
+        int i = (int)((1.0 + sqrt(1.0 + 8.0 * (double)q)) * 0.5);
+        while (i * (i - 1) / 2 > q) --i;
+        while ((i + 1) * i / 2 <= q) ++i;
+        const int j = q - i * (i - 1) / 2;
+        ci = closed[i];
+        cj = closed[j];
+        const int I = ci >> 1, J = cj >> 1;
+        const int X = I > J ? I : J, Y = I > J ? J : I;
+        const int pair = X * (X + 1) / 2 + Y;
+        same = (ci & 1) == (cj & 1);
+        const int64_t* st = same ? a.hb.sameStart : a.hb.oppStart;
+        const float* vals = same ? a.hb.sameVal : a.hb.oppVal;
+        const int64_t s0 = st[pair], s1 = st[pair + 1];
+        // first entry with |v| < eps (lists sorted by |v| descending)
+        int64_t lo = s0, hi = s1;
+        while (lo < hi) {
+          const int64_t mid = (lo + hi) >> 1;
+          if ((double)fabsf(vals[mid]) < eps)
+            hi = mid;
+          else
+            lo = mid + 1;
+        }
+        lstart = s0;
+        len = lo - s0;
+      }
+      int64_t incl = len;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int64_t y = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += y;
+      }
+      const int64_t total = __shfl_sync(kFull, incl, 31);
+      const int64_t excl = incl - len;
+      for (int64_t f0 = 0; f0 < total; f0 += 32) {
+        const int64_t f = f0 + lane;
+        // owner lane of flattened entry f: last lane with excl <= f
+        int lo = 0;
+#pragma unroll
+        for (int st = 16; st >= 1; st >>= 1) {
+          const int c2 = lo + st;
+          const int64_t e2 = __shfl_sync(kFull, excl, c2 < 32 ? c2 : 31);
+          if (c2 < 32 && e2 <= f) lo = c2;
+        }
+        const int64_t ls = __shfl_sync(kFull, lstart, lo);
+        const int64_t eo = __shfl_sync(kFull, excl, lo);
+        const int oci = __shfl_sync(kFull, ci, lo);
+        const int ocj = __shfl_sync(kFull, cj, lo);
+        const bool osame = __shfl_sync(kFull, (int)same, lo) != 0;
+        bool keep = false;
+        Det2 cand = d;
+        double v = 0.0, e = 0.0;
+        if (f < total) {
+          const int64_t index = ls + (f - eo);
+          const int16_t* pr = osame ? a.hb.samePairs : a.hb.oppPairs;
+          const float* vals = osame ? a.hb.sameVal : a.hb.oppVal;
+          const int av = 2 * pr[2 * index] + (oci & 1);
+          const int bv = 2 * pr[2 * index + 1] + (ocj & 1);
+          bool ok = true;
+          for (int r = 0; ok && r < sp.nrestrict; ++r) {
+            int c2 = cur[r] - in_mask(sp, r, oci) - in_mask(sp, r, ocj) + in_mask(sp, r, av) + in_mask(sp, r, bv);
+            ok = c2 >= sp.rmin[r] && c2 <= sp.rmax[r];
+          }
+          if (ok && !(det_getocc(d, av) || det_getocc(d, bv))) {
+            det_flip(cand, av);
+            det_flip(cand, bv);
+            det_flip(cand, oci);
+            det_flip(cand, ocj);
+            keep = in_part(a, cand) && !hash_contains(a.hslots, a.hmask, a.dets, cand);
+            if (keep) {
+              v = (double)vals[index] * pt_double_sign(cand, av, bv, oci, ocj) * cp;
+              e = ed - __ldg(a.ints.I1 + (size_t)oci * ld1) - __ldg(a.ints.I1 + (size_t)ocj * ld1) +
+                  __ldg(a.ints.I1 + (size_t)av * ld1) + __ldg(a.ints.I1 + (size_t)bv * ld1) - F[oci] - F[ocj] +
+                  vpair(sD, sX, n, oci, ocj) + F[av] - vpair(sD, sX, n, av, oci) - vpair(sD, sX, n, av, ocj) +
+                  F[bv] - vpair(sD, sX, n, bv, oci) - vpair(sD, sX, n, bv, ocj) + vpair(sD, sX, n, av, bv);
+            }
+          }
+        }
+        pt_put(a, keep, cand, v, e);
+      }
+    }
   }
 }
 
@@ -266,33 +310,52 @@ __global__ void k_pt_iota(uint32_t* __restrict__ p, size_t n) {
     p[i] = (uint32_t)i;
 }
 
+// x in units of 2^-kFixBits, truncated toward zero (|x| < 2^47).
+__device__ __forceinline__ __int128 to_fix(double x) {
+  const long long b = __double_as_longlong(x);
+  const int ex = (int)((b >> 52) & 0x7ff);
+  if (ex == 0) return 0;  // zero or subnormal: below the unit
+  const unsigned long long m = ((unsigned long long)b & 0xfffffffffffffull) | (1ull << 52);
+  const int sh = ex - 1075 + kFixBits;
+  unsigned __int128 v = 0;
+  if (sh >= 0)
+    v = (unsigned __int128)m << (sh < 74 ? sh : 74);
+  else if (sh > -64)
+    v = m >> (-sh);
+  return b < 0 ? -(__int128)v : (__int128)v;
+}
+
+__device__ __forceinline__ double from_fix(__int128 v) {
+  const bool neg = v < 0;
+  const unsigned __int128 m = neg ? (unsigned __int128)(-v) : (unsigned __int128)v;
+  const double d = (double)(unsigned long long)(m >> 64) * 18446744073709551616.0 + (double)(unsigned long long)m;
+  return (neg ? -d : d) * 8.271806125530276748714086920699e-25;  // 2^-80
+}
+
 // One thread per run of equal determinants in the sorted candidates; block
 // partials {E2, |psi1|^2, count} in part[3 * block].
 __global__ void __launch_bounds__(kPtRedThreads) k_pt_reduce(const Det2* __restrict__ sorted,
                                                              const uint32_t* __restrict__ perm,
-                                                             const double* __restrict__ num, size_t m, IntsView ints,
-                                                             double E0, double* __restrict__ part) {
-  extern __shared__ double sm[];
-  const int nn = ints.norb * ints.norb;
-  double* sD = sm;
-  double* sX = sm + nn;
-  for (int j = threadIdx.x; j < nn; j += blockDim.x) {
-    sD[j] = ints.Direct[j];
-    sX[j] = ints.Exchange[j];
-  }
-  __syncthreads();
+                                                             const double* __restrict__ num,
+                                                             const double* __restrict__ en, size_t m, double E0,
+                                                             double* __restrict__ part) {
   double e2 = 0.0, psi = 0.0, cnt = 0.0;
   for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < m; k += (size_t)gridDim.x * blockDim.x) {
     const Det2 d = sorted[k];
     if (k > 0 && det_eq(d, sorted[k - 1])) continue;
-    double s = num[perm[k]];
+    uint32_t pk = perm[k];
+    __int128 s = to_fix(num[pk]);
+    double ea = en[pk];
     for (size_t j = k + 1; j < m; ++j) {
       if (!det_eq(sorted[j], d)) break;
-      s += num[perm[j]];
+      pk = perm[j];
+      s += to_fix(num[pk]);
+      ea = fmin(ea, en[pk]);
     }
-    const double de = E0 - det_energy(ints, d, sD, sX);
-    e2 += s * s / de;
-    const double t = s / de;
+    const double sn = from_fix(s);
+    const double de = E0 - ea;
+    e2 += sn * sn / de;
+    const double t = sn / de;
     psi += t * t;
     cnt += 1.0;
   }
@@ -329,9 +392,7 @@ PtResult pt_deterministic(const Det2* dets, size_t n, const double* c, double E0
   PtResult res;
   if (n == 0) return res;
   if (!(eps2 >= 0.0)) throw Error(kErrInvalid, "epsilon2 must be >= 0");
-  w.counts.resize(n);
-  w.offs.resize(n);
-  w.next.resize(1);
+  w.next.resize(2);
   w.part.resize(3 * kPtRedBlocks);
   PtArgs a{};
   a.dets = dets;
@@ -345,26 +406,9 @@ PtResult pt_deterministic(const Det2* dets, size_t n, const double* c, double E0
   a.hslots = present.slots.p;
   a.hmask = present.mask;
   a.next = w.next.p;
-  a.counts = w.counts.p;
-  a.offs = w.offs.p;
-  const unsigned gen_blocks = 152 * 8;  // one warp per parent from a shared queue
-  auto gen = [&](bool emit, uint32_t nparts, uint32_t part) -> int64_t {
-    a.nparts = nparts;
-    a.part = part;
-    SHCI_CUDA(cudaMemsetAsync(w.next.p, 0, sizeof(unsigned long long), s));
-    if (emit) {
-      a.out = w.cand.p;
-      a.num = w.num.p;
-      k_pt_gen<true><<<gen_blocks, kPtThreads, 0, s>>>(a);
-      SHCI_LAUNCH_CHECK();
-      return 0;
-    }
-    k_pt_gen<false><<<gen_blocks, kPtThreads, 0, s>>>(a);
-    SHCI_LAUNCH_CHECK();
-    int64_t total = 0;
-    scan_exclusive_i64(w.counts.p, w.offs.p, n, &total, pr, s);
-    return total;
-  };
+  a.counter = w.next.p + 1;
+  const size_t gsmem = 2 * sizeof(double) * ints.norb * ints.norb;
+  SHCI_CUDA(cudaFuncSetAttribute(k_pt_gen, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsmem));
 
   // capacity of one partition
   int64_t cap = max_candidates;
@@ -374,57 +418,85 @@ PtResult pt_deterministic(const Det2* dets, size_t n, const double* c, double E0
     size_t avail = fr;
     if (g_alloc_cap) avail = std::min(avail, g_alloc_cap > g_alloc_live ? g_alloc_cap - g_alloc_live : (size_t)0);
     // what the buffers already hold counts as available to them
-    avail += w.cand.cap * sizeof(Det2) + w.num.cap * sizeof(double) + w.perm.cap * sizeof(uint32_t);
+    avail += w.cand.cap * sizeof(Det2) + (w.num.cap + w.en.cap) * sizeof(double) + w.perm.cap * sizeof(uint32_t);
     cap = (int64_t)(avail / 4 * 3 / kPtBytesPerCand);
   }
   cap = std::min<int64_t>(cap, (int64_t)0xfffffff0u);
   if (cap < 1) throw Error(kErrOOM, "no device memory left for perturbation candidates");
 
+  // one generation pass into buffers of `room` candidates; returns the count
+  auto gen = [&](uint32_t nparts, uint32_t part, int64_t room) -> int64_t {
+    w.cand.reserve((size_t)room);
+    w.num.reserve((size_t)room);
+    w.en.reserve((size_t)room);
+    a.nparts = nparts;
+    a.part = part;
+    a.cap = room;
+    a.out = w.cand.p;
+    a.num = w.num.p;
+    a.en = w.en.p;
+    SHCI_CUDA(cudaMemsetAsync(w.next.p, 0, 2 * sizeof(unsigned long long), s));
+    k_pt_gen<<<kPtGenBlocks, kPtThreads, gsmem, s>>>(a);
+    SHCI_LAUNCH_CHECK();
+    unsigned long long total = 0;
+    SHCI_CUDA(cudaMemcpyAsync(&total, w.next.p + 1, sizeof(total), cudaMemcpyDeviceToHost, s));
+    SHCI_CUDA(cudaStreamSynchronize(s));
+    return (int64_t)total;
+  };
+  auto reduce = [&](int64_t m, PtResult& r) {
+    w.perm.resize((size_t)m);
+    k_pt_iota<<<grid_for((size_t)m, 256), 256, 0, s>>>(w.perm.p, (size_t)m);
+    SHCI_LAUNCH_CHECK();
+    sort_dets(w.cand.p, w.perm.p, (size_t)m, pr, s);
+    k_pt_reduce<<<kPtRedBlocks, kPtRedThreads, 0, s>>>(w.cand.p, w.perm.p, w.num.p, w.en.p, (size_t)m, E0,
+                                                       w.part.p);
+    SHCI_LAUNCH_CHECK();
+    std::vector<double> hp(3 * kPtRedBlocks);
+    SHCI_CUDA(cudaMemcpyAsync(hp.data(), w.part.p, hp.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+    SHCI_CUDA(cudaStreamSynchronize(s));
+    for (unsigned b = 0; b < kPtRedBlocks; ++b) {
+      r.e2 += hp[3 * b];
+      r.psi1_norm += hp[3 * b + 1];
+      r.unique += (int64_t)hp[3 * b + 2];
+    }
+  };
+
   PhaseTimer pt(s);
-  const int64_t total_all = gen(false, 1, 0);
-  pt.mark("pt count");
-  uint32_t nparts = total_all <= cap ? 1u : (uint32_t)((total_all + total_all / 8) / cap + 1);
-  const size_t smem = 2 * sizeof(double) * ints.norb * ints.norb;
-  SHCI_CUDA(cudaFuncSetAttribute(k_pt_reduce, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  std::vector<double> hp(3 * kPtRedBlocks);
+  // first pass into what the buffers hold (at least 64 per parent, at most cap)
+  int64_t room = std::min<int64_t>(cap, std::max<int64_t>((int64_t)w.cand.cap, 64 * (int64_t)n));
+  int64_t total = gen(1, 0, room);
+  pt.mark("pt generate");
+  if (total <= cap) {
+    if (total > room) {  // buffers too small: regenerate into exact room
+      gen(1, 0, total);
+      pt.mark("pt regenerate");
+    }
+    res.partitions = 1;
+    res.candidates = total;
+    if (total > 0) reduce(total, res);
+    pt.mark("pt sort+reduce");
+    return res;
+  }
+  // split by hash; a partition that still overflows doubles the count
+  uint32_t nparts = (uint32_t)((total + total / 8) / cap + 1);
   for (int attempt = 0;; ++attempt) {
     res = PtResult();
     res.partitions = (int)nparts;
     bool overflow = false;
-    for (uint32_t part = 0; part < nparts; ++part) {
-      const int64_t m = nparts == 1 ? total_all : gen(false, nparts, part);
+    for (uint32_t part = 0; part < nparts && !overflow; ++part) {
+      const int64_t m = gen(nparts, part, cap);
       if (m > cap) {
         overflow = true;
         break;
       }
       res.candidates += m;
-      if (m == 0) continue;
-      w.cand.reserve((size_t)m);
-      w.num.reserve((size_t)m);
-      w.perm.resize((size_t)m);
-      gen(true, nparts, part);
-      pt.mark("pt emit");
-      k_pt_iota<<<grid_for((size_t)m, 256), 256, 0, s>>>(w.perm.p, (size_t)m);
-      SHCI_LAUNCH_CHECK();
-      sort_dets(w.cand.p, w.perm.p, (size_t)m, pr, s);
-      pt.mark("pt sort");
-      k_pt_reduce<<<kPtRedBlocks, kPtRedThreads, smem, s>>>(w.cand.p, w.perm.p, w.num.p, (size_t)m, ints, E0,
-                                                            w.part.p);
-      SHCI_LAUNCH_CHECK();
-      pt.mark("pt reduce");
-      SHCI_CUDA(cudaMemcpyAsync(hp.data(), w.part.p, hp.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
-      SHCI_CUDA(cudaStreamSynchronize(s));
-      for (unsigned b = 0; b < kPtRedBlocks; ++b) {
-        res.e2 += hp[3 * b];
-        res.psi1_norm += hp[3 * b + 1];
-        res.unique += (int64_t)hp[3 * b + 2];
-      }
+      if (m > 0) reduce(m, res);
     }
     if (!overflow) break;
     if (attempt >= 8) throw Error(kErrOOM, "perturbation candidates do not fit in device memory");
     nparts *= 2;
   }
-  SHCI_CUDA(cudaStreamSynchronize(s));
+  pt.mark("pt partitions");
   return res;
 }
 
