@@ -182,22 +182,23 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def pt_section(e, E0, steps, cpu_leg, fcidump):
+def pt_section(e, E0, steps, cpu_leg, fcidump, eps2=PT_EPS2, warmup=1):
     """Deterministic PT2 (Epstein-Nesbet) of the final space through the
     C-ABI (host coefficients in, E2 out): candidates outside the variational
     space generated, merged and summed per second. CPU leg: the oracle's
     restatement on a bounded sample of parents (the middle of the space,
     doubled until it takes 5 s), against the whole space for removal."""
     ci = e.run_ci(1)[0]
-    e.pt_deterministic(ci, E0, PT_EPS2)  # warm-up: allocations
+    for _ in range(max(1, warmup)):
+        e.pt_deterministic(ci, E0, eps2)  # warm-up: allocations
     ts = []
     for _ in range(max(2, steps // 4)):
         t0 = time.perf_counter()
-        e2 = e.pt_deterministic(ci, E0, PT_EPS2)
+        e2 = e.pt_deterministic(ci, E0, eps2)
         ts.append(time.perf_counter() - t0)
     st = e.pt_stats()
     t = statistics.mean(ts)
-    out = {"eps2": PT_EPS2, "E_var": E0, "E2": e2, "E_total": E0 + e2, "candidates": st["candidates"],
+    out = {"eps2": eps2, "ndets": len(ci), "E_var": E0, "E2": e2, "E_total": E0 + e2, "candidates": st["candidates"],
            "unique": st["unique"], "partitions": st["partitions"], "psi1_norm": st["psi1_norm"],
            "seconds": t, "reps": len(ts), "Mcand_s": st["candidates"] / t / 1e6,
            "what": "shci_pt_deterministic on the final mixed-precision space (the reference's "
@@ -210,7 +211,7 @@ def pt_section(e, E0, steps, cpu_leg, fcidump):
         p0, k = n // 2, 256
         while True:
             t0 = time.perf_counter()
-            _, sto = o.pt_det_range(dets, ci, E0, PT_EPS2, p0, min(n, p0 + k))
+            _, sto = o.pt_det_range(dets, ci, E0, eps2, p0, min(n, p0 + k))
             tc = time.perf_counter() - t0
             if tc > 5.0 or p0 + k >= n:
                 break
@@ -220,6 +221,31 @@ def pt_section(e, E0, steps, cpu_leg, fcidump):
                                        % (p0, min(n, p0 + k), n, sto["outside"])}
         out["speedup_vs_cpu_oracle"] = out["Mcand_s"] / out["cpu_oracle"]["Mcand_s"]
     return out
+
+
+def run_pt_only(args):
+    """--section pt: the variational stage in the mixed path on the chosen
+    case, then the perturbative stage timed alone (one JSON line)."""
+    import torch
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    from dice_gb300 import engine as eng
+    work = tempfile.mkdtemp()
+    inp = make_inputs(work, args.case)
+    e = eng.Engine(local)
+    E = e.run_input(inp, mode="mixed")
+    l0 = e.launch_count()
+    pt = pt_section(e, float(E[0]), args.steps, rank == 0 and not args.no_cpu, os.path.join(work, "FCIDUMP"),
+                    eps2=args.pt_eps2, warmup=args.warmup)
+    launches = (e.launch_count() - l0) // (pt["reps"] + args.warmup)
+    e.close()
+    line = {"metric": "PT2 candidates/s (deterministic Epstein-Nesbet)", "value": pt["Mcand_s"],
+            "unit": "Mcand/s", "n_gpus": 1, "steps": pt["reps"], "warmup": args.warmup,
+            "ms_per_step": pt["seconds"] * 1e3, "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "mol24 (%s case): %d determinants, eps2 %g" % (args.case, pt["ndets"], pt["eps2"])},
+            "gpu_launches": launches, "pt": pt}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
 
 
 def other_configs(work, device):
@@ -449,11 +475,16 @@ def main():
     ap.add_argument("--no-configs", action="store_true", help="skip the other workloads (mol36, mol64, mol50)")
     ap.add_argument("--case", default="full", choices=["full", "medium", "small"],
                     help="small: the profiling case (two eps1 = 1e-3 iterations)")
+    ap.add_argument("--section", default="all", choices=["all", "pt"],
+                    help="pt: only the variational run and the timed perturbative stage")
+    ap.add_argument("--pt-eps2", type=float, default=PT_EPS2)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.section == "pt":
+        run_pt_only(args)
     else:
         run_ours(args)
 

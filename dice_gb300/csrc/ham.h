@@ -176,6 +176,9 @@ struct PtWork {
   DevBuf<double> num, en, part;
   DevBuf<uint32_t> perm;
   DevBuf<unsigned long long> next;  // parent queue, candidate counter
+  DevBuf<double> coul, exch;        // dense (AI|JJ), (AJ|JI) of the integrals below
+  const double* tables_of = nullptr;
+  int tables_n = 0;
 };
 // E2 of the space `dets` (hash set `present` over it) with coefficients c
 // (device, n) for threshold eps2: candidates with |H_ai c_i| criteria of the

@@ -73,6 +73,8 @@ struct PtArgs {
   const uint32_t* hslots;
   uint64_t hmask;
   uint32_t nparts, part;
+  const double* coul;  // (AI|JJ) at (A n + I) n + J (spatial)
+  const double* exch;  // (AJ|JI) at (A n + I) n + J
   unsigned long long* next;     // parent queue
   unsigned long long* counter;  // candidates appended (counts past cap too)
   int64_t cap;
@@ -117,6 +119,32 @@ __device__ __forceinline__ void pt_put(const PtArgs& a, bool keep, const Det2& c
   }
 }
 
+// Hij_1Excite(a, i) of `ket` (SHCI/Determinants.cpp:437-469) with the two
+// integrals of each term read from the dense rows of (a, i): the same values
+// summed in the same order as hij_single, so bit-identical, but from 2 x n
+// contiguous doubles instead of 2 x n scattered packed-table entries.
+__device__ __forceinline__ double hij_single_rows(const PtArgs& a, const Det2& ket, int ao, int io) {
+  const int n = a.ints.norb, n2 = 2 * n;
+  const size_t row = ((size_t)(ao >> 1) * n + (io >> 1)) * n;
+  const double* __restrict__ cr = a.coul + row;
+  const double* __restrict__ xr = a.exch + row;
+  double energy = __ldg(a.ints.I1 + (size_t)ao * n2 + io);
+  const uint64_t same = (ao & 1) ? 0xaaaaaaaaaaaaaaaaull : 0x5555555555555555ull;
+#pragma unroll 1
+  for (int w = 0; w < 2; ++w) {
+    uint64_t bits = w ? ket.w1 : ket.w0;
+    while (bits) {
+      const int j = __ffsll((long long)bits) - 1;
+      const double dd = __ldg(cr + ((j + 64 * w) >> 1));
+      const double x = ((same >> j) & 1ull) ? __ldg(xr + ((j + 64 * w) >> 1)) : 0.0;
+      bits &= bits - 1;
+      energy = __dadd_rn(energy, __dsub_rn(dd, x));
+    }
+  }
+  const int lo = ao < io ? ao : io, hi = ao < io ? io : ao;
+  return (occ_between(ket, lo, hi) & 1) ? -energy : energy;
+}
+
 // V(p, q): Coulomb minus (same spin only) exchange of spin orbitals p, q,
 // from the n x n Direct/Exchange tables staged in shared memory.
 __device__ __forceinline__ double vpair(const double* sD, const double* sX, int n, int p, int q) {
@@ -127,7 +155,8 @@ __device__ __forceinline__ double vpair(const double* sD, const double* sX, int 
 __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
   extern __shared__ double smd[];
   __shared__ unsigned char s_closed[kPtWarps][kMaxSpin];
-  __shared__ unsigned char s_open[kPtWarps][kMaxSpin];
+  __shared__ unsigned char s_open[kPtWarps][kMaxSpin];   // alpha holes, then beta holes
+  __shared__ unsigned char s_cspin[kPtWarps][kMaxSpin];  // alpha electrons, then beta electrons
   __shared__ double s_F[kPtWarps][kMaxSpin];
   const int n = a.ints.norb, nn = n * n;
   double* sD = smd;
@@ -140,7 +169,9 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   unsigned char* closed = s_closed[wib];
   unsigned char* open = s_open[wib];
+  unsigned char* cspin = s_cspin[wib];
   double* F = s_F[wib];
+  const unsigned lt = (1u << lane) - 1u;
   const int n2 = 2 * n;
   const int ld1 = n2 + 1;  // diagonal stride of the (2n)x(2n) one-electron matrix
   const SelectParams& sp = a.sp;
@@ -154,19 +185,40 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
     const double cp = a.c[p];
     const double eps = fabs(a.eps2 / cp);
     if (!(eps < INFINITY)) continue;  // c_i = 0: nothing passes either threshold
+    // occupied list (ascending) and per-spin electron / hole lists, by ballot
+    const int nclosed = __popcll(d.w0) + __popcll(d.w1);
+    const int ncA = __popcll(d.w0 & 0x5555555555555555ull) + __popcll(d.w1 & 0x5555555555555555ull);
+    const int nhA = n - ncA;
     __syncwarp();
-    if (lane == 0) {
-      int nc = 0, no = 0;
-      for (int q = 0; q < n2; ++q) {
-        if (det_getocc(d, q))
-          closed[nc++] = (unsigned char)q;
-        else
-          open[no++] = (unsigned char)q;
+    {
+      int nc = 0, ea = 0, eb = 0, ha = 0, hb2 = 0;
+      for (int base = 0; base < n2; base += 32) {
+        const int q = base + lane;
+        const bool valid = q < n2;
+        const bool occ = valid && det_getocc(d, q);
+        const unsigned mo = __ballot_sync(kFull, occ), mv = __ballot_sync(kFull, valid);
+        const unsigned mh = mv & ~mo;
+        const unsigned evn = 0x55555555u, odd = 0xaaaaaaaau;  // alpha lanes, beta lanes
+        if (occ) {
+          closed[nc + __popc(mo & lt)] = (unsigned char)q;
+          if (q & 1)
+            cspin[ncA + eb + __popc(mo & odd & lt)] = (unsigned char)q;
+          else
+            cspin[ea + __popc(mo & evn & lt)] = (unsigned char)q;
+        } else if (valid) {
+          if (q & 1)
+            open[nhA + hb2 + __popc(mh & odd & lt)] = (unsigned char)q;
+          else
+            open[ha + __popc(mh & evn & lt)] = (unsigned char)q;
+        }
+        nc += __popc(mo);
+        ea += __popc(mo & evn);
+        eb += __popc(mo & odd);
+        ha += __popc(mh & evn);
+        hb2 += __popc(mh & odd);
       }
     }
     __syncwarp();
-    const int nclosed = __popcll(d.w0) + __popcll(d.w1);
-    const int nopen = n2 - nclosed;
     // F_q = sum over occupied r of V(q, r) (V(q, q) = 0), and the parent's energy
     double ed = 0.0;
     for (int q = lane; q < n2; q += 32) {
@@ -180,23 +232,31 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
     int cur[kMaxRestrict];
     for (int r = 0; r < sp.nrestrict; ++r) cur[r] = __popcll(d.w0 & sp.rmask0[r]) + __popcll(d.w1 & sp.rmask1[r]);
 
-    // ---- singles: every same-spin (i, a); the exact element decides
-    const int ns = nclosed * nopen;
+    // ---- singles: every same-spin (i, a) (a spin flip has a zero element:
+    // I1 has no alpha-beta block); the exact element decides
+    const int ncB = nclosed - ncA, nhB = n - ncB;
+    const int nsA = ncA * nhA, ns = nsA + ncB * nhB;
     for (int b0 = 0; b0 < ns; b0 += 32) {
       const int q = b0 + lane;
       bool keep = false;
       Det2 cand = d;
       double v = 0.0, e = 0.0;
       if (q < ns) {
-        const int ci = closed[q / nopen], oa = open[q % nopen];
-        // a spin flip has a zero element (no alpha-beta block in I1)
-        bool ok = (ci & 1) == (oa & 1);
+        int ci, oa;
+        if (q < nsA) {
+          ci = cspin[q / nhA];
+          oa = open[q % nhA];
+        } else {
+          ci = cspin[ncA + (q - nsA) / nhB];
+          oa = open[nhA + (q - nsA) % nhB];
+        }
+        bool ok = true;
         for (int r = 0; ok && r < sp.nrestrict; ++r) {
           int c2 = cur[r] - in_mask(sp, r, ci) + in_mask(sp, r, oa);
           ok = c2 >= sp.rmin[r] && c2 <= sp.rmax[r];
         }
         if (ok) {
-          const double h = hij_single(a.ints, d, oa, ci);
+          const double h = hij_single_rows(a, d, oa, ci);
           if (fabs(h) > eps) {
             det_flip(cand, oa);
             det_flip(cand, ci);
@@ -305,6 +365,16 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
   }
 }
 
+__global__ void k_pt_tables(const double* __restrict__ I2, int n, double* __restrict__ coul,
+                            double* __restrict__ exch) {
+  const size_t nt = (size_t)n * n * n;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += (size_t)gridDim.x * blockDim.x) {
+    const int J = (int)(t % n), I = (int)((t / n) % n), A = (int)(t / ((size_t)n * n));
+    coul[t] = i2_spatial(I2, A, I, J, J);
+    exch[t] = i2_spatial(I2, A, J, J, I);
+  }
+}
+
 __global__ void k_pt_iota(uint32_t* __restrict__ p, size_t n) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     p[i] = (uint32_t)i;
@@ -407,6 +477,17 @@ PtResult pt_deterministic(const Det2* dets, size_t n, const double* c, double E0
   a.hmask = present.mask;
   a.next = w.next.p;
   a.counter = w.next.p + 1;
+  if (w.tables_of != ints.I2 || w.tables_n != ints.norb) {
+    const size_t nt = (size_t)ints.norb * ints.norb * ints.norb;
+    w.coul.resize(nt);
+    w.exch.resize(nt);
+    k_pt_tables<<<grid_for(nt, 256), 256, 0, s>>>(ints.I2, ints.norb, w.coul.p, w.exch.p);
+    SHCI_LAUNCH_CHECK();
+    w.tables_of = ints.I2;
+    w.tables_n = ints.norb;
+  }
+  a.coul = w.coul.p;
+  a.exch = w.exch.p;
   const size_t gsmem = 2 * sizeof(double) * ints.norb * ints.norb;
   SHCI_CUDA(cudaFuncSetAttribute(k_pt_gen, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsmem));
 
