@@ -201,7 +201,7 @@ def pt_section(e, E0, steps, cpu_leg, fcidump, eps2=PT_EPS2, warmup=1):
     out = {"eps2": eps2, "ndets": len(ci), "E_var": E0, "E2": e2, "E_total": E0 + e2, "candidates": st["candidates"],
            "unique": st["unique"], "partitions": st["partitions"], "psi1_norm": st["psi1_norm"],
            "seconds": t, "reps": len(ts), "Mcand_s": st["candidates"] / t / 1e6,
-           XX
+           "what": "shci_pt_deterministic on the final mixed-precision space (the reference's "
                    "DoPerturbativeDeterministic): generation with atomic append, radix sort by "
                    "determinant, per-run exact numerator sums"}
     if cpu_leg:
