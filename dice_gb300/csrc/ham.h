@@ -177,6 +177,7 @@ struct PtWork {
   DevBuf<uint32_t> perm;
   DevBuf<unsigned long long> next;  // parent queue, candidate counter
   DevBuf<double> coul, exch;        // dense (AI|JJ), (AJ|JI) of the integrals below
+  DevBuf<float> coul32, exch32;     // and their FP32 roundings
   const double* tables_of = nullptr;
   int tables_n = 0;
 };

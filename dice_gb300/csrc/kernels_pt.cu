@@ -18,11 +18,14 @@
 //                variational space (hash probe) in this partition are
 //                appended (warp-aggregated atomics) with their numerator and
 //                energy. The energy is updated from the parent's in O(1):
-//                with F_p = sum_{q occupied} V(p, q) and V the same-spin-aware
-//                Coulomb-minus-exchange, a single i -> a changes E by
-//                h_aa - h_ii + F_a - F_i - V(a, i), a double by the analogous
-//                pair terms (the reference's EnergyAfterExcitation,
-//                SHCI/Determinants.cpp:124-249, sums the same terms in a loop);
+//                with orbital energies F_p = h_pp + sum_{q occupied} V(p, q)
+//                and V the same-spin-aware Coulomb-minus-exchange, a single
+//                i -> a changes E by F_a - F_i - V(a, i), a double by the
+//                analogous pair terms (the reference's EnergyAfterExcitation,
+//                SHCI/Determinants.cpp:124-249, sums the same terms in a loop).
+//                Singles are screened in FP32 with a rigorous error bound and
+//                evaluated exactly (bit-identical to the reference's FP64
+//                element) only where the screen cannot decide or keeps them;
 //   radix sort   by determinant, candidate index as payload;
 //   k_pt_reduce  one thread per run of equal determinants: the numerators are
 //                summed exactly in 128-bit fixed point (2^-80 units), so the
@@ -73,8 +76,12 @@ struct PtArgs {
   const uint32_t* hslots;
   uint64_t hmask;
   uint32_t nparts, part;
-  const double* coul;  // (AI|JJ) at (A n + I) n + J (spatial)
-  const double* exch;  // (AJ|JI) at (A n + I) n + J
+  // dense single-excitation integrals, A fastest so that the lanes of a warp
+  // (same I, neighbouring A, the same J sequence) read contiguous addresses:
+  const double* coul;   // (AI|JJ) at (I n + J) n + A (spatial)
+  const double* exch;   // (AJ|JI) at (I n + J) n + A
+  const float* coul32;  // the same rounded to FP32, for the screen
+  const float* exch32;
   unsigned long long* next;     // parent queue
   unsigned long long* counter;  // candidates appended (counts past cap too)
   int64_t cap;
@@ -120,14 +127,11 @@ __device__ __forceinline__ void pt_put(const PtArgs& a, bool keep, const Det2& c
 }
 
 // Hij_1Excite(a, i) of `ket` (SHCI/Determinants.cpp:437-469) with the two
-// integrals of each term read from the dense rows of (a, i): the same values
-// summed in the same order as hij_single, so bit-identical, but from 2 x n
-// contiguous doubles instead of 2 x n scattered packed-table entries.
+// integrals of each term read from the dense tables: the same values summed
+// in the same order as hij_single, so bit-identical.
 __device__ __forceinline__ double hij_single_rows(const PtArgs& a, const Det2& ket, int ao, int io) {
   const int n = a.ints.norb, n2 = 2 * n;
-  const size_t row = ((size_t)(ao >> 1) * n + (io >> 1)) * n;
-  const double* __restrict__ cr = a.coul + row;
-  const double* __restrict__ xr = a.exch + row;
+  const size_t base = (size_t)(io >> 1) * n * n + (ao >> 1);
   double energy = __ldg(a.ints.I1 + (size_t)ao * n2 + io);
   const uint64_t same = (ao & 1) ? 0xaaaaaaaaaaaaaaaaull : 0x5555555555555555ull;
 #pragma unroll 1
@@ -135,8 +139,9 @@ __device__ __forceinline__ double hij_single_rows(const PtArgs& a, const Det2& k
     uint64_t bits = w ? ket.w1 : ket.w0;
     while (bits) {
       const int j = __ffsll((long long)bits) - 1;
-      const double dd = __ldg(cr + ((j + 64 * w) >> 1));
-      const double x = ((same >> j) & 1ull) ? __ldg(xr + ((j + 64 * w) >> 1)) : 0.0;
+      const size_t t = base + (size_t)((j + 64 * w) >> 1) * n;
+      const double dd = __ldg(a.coul + t);
+      const double x = ((same >> j) & 1ull) ? __ldg(a.exch + t) : 0.0;
       bits &= bits - 1;
       energy = __dadd_rn(energy, __dsub_rn(dd, x));
     }
@@ -145,11 +150,45 @@ __device__ __forceinline__ double hij_single_rows(const PtArgs& a, const Det2& k
   return (occ_between(ket, lo, hi) & 1) ? -energy : energy;
 }
 
-// V(p, q): Coulomb minus (same spin only) exchange of spin orbitals p, q,
-// from the n x n Direct/Exchange tables staged in shared memory.
-__device__ __forceinline__ double vpair(const double* sD, const double* sX, int n, int p, int q) {
+// FP32 screen of |Hij_1Excite(a, i)| against eps: returns +1 when the FP64
+// element certainly exceeds eps, -1 when it certainly does not, 0 when the
+// FP32 sum is too close to tell. Error bound: with u = 2^-24 and S the sum of
+// |I1_ai| and |d|, |x| over the m terms, the rounding of the integrals to
+// FP32 (u per value), of each difference and of the running sum stays below
+// (m + 3) u S; the margin used is (m + 8) 2u S.
+__device__ __forceinline__ int single_screen(const PtArgs& a, const Det2& ket, int ao, int io, double eps) {
+  const int n = a.ints.norb, n2 = 2 * n;
+  const size_t base = (size_t)(io >> 1) * n * n + (ao >> 1);
+  float h = (float)__ldg(a.ints.I1 + (size_t)ao * n2 + io);
+  float S = fabsf(h);
+  int m = 0;
+  const uint64_t same = (ao & 1) ? 0xaaaaaaaaaaaaaaaaull : 0x5555555555555555ull;
+#pragma unroll 1
+  for (int w = 0; w < 2; ++w) {
+    uint64_t bits = w ? ket.w1 : ket.w0;
+    while (bits) {
+      const int j = __ffsll((long long)bits) - 1;
+      const size_t t = base + (size_t)((j + 64 * w) >> 1) * n;
+      const float dd = __ldg(a.coul32 + t);
+      const float x = ((same >> j) & 1ull) ? __ldg(a.exch32 + t) : 0.0f;
+      bits &= bits - 1;
+      h += dd - x;
+      S += fabsf(dd) + fabsf(x);
+      ++m;
+    }
+  }
+  const double margin = (double)(m + 8) * 1.1920928955078125e-07 * (double)S;
+  const double ah = fabs((double)h);
+  if (ah - margin > eps) return 1;
+  if (ah + margin < eps) return -1;
+  return 0;
+}
+
+// V(p, q): Coulomb (opposite spins) or Coulomb minus exchange (same spin) of
+// spin orbitals p, q, from the n x n tables J and J - K staged in shared memory.
+__device__ __forceinline__ double vpair(const double* sJ, const double* sJK, int n, int p, int q) {
   const int o = (p >> 1) * n + (q >> 1);
-  return ((p ^ q) & 1) ? sD[o] : __dsub_rn(sD[o], sX[o]);
+  return ((p ^ q) & 1) ? sJ[o] : sJK[o];
 }
 
 __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
@@ -159,11 +198,11 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
   __shared__ unsigned char s_cspin[kPtWarps][kMaxSpin];  // alpha electrons, then beta electrons
   __shared__ double s_F[kPtWarps][kMaxSpin];
   const int n = a.ints.norb, nn = n * n;
-  double* sD = smd;
-  double* sX = smd + nn;
+  double* sD = smd;       // J
+  double* sX = smd + nn;  // J - K
   for (int j = threadIdx.x; j < nn; j += blockDim.x) {
     sD[j] = a.ints.Direct[j];
-    sX[j] = a.ints.Exchange[j];
+    sX[j] = __dsub_rn(a.ints.Direct[j], a.ints.Exchange[j]);
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -219,13 +258,20 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
       }
     }
     __syncwarp();
-    // F_q = sum over occupied r of V(q, r) (V(q, q) = 0), and the parent's energy
+    // orbital energies F_q = h_qq + sum over occupied r of V(q, r) (V(q, q) = 0)
+    // and the parent's energy sum_occ (h_qq + F_q) / 2
     double ed = 0.0;
     for (int q = lane; q < n2; q += 32) {
-      double f = 0.0;
-      for (int k = 0; k < nclosed; ++k) f += vpair(sD, sX, n, q, closed[k]);
-      F[q] = f;
-      if (det_getocc(d, q)) ed += __ldg(a.ints.I1 + (size_t)q * ld1) + 0.5 * f;
+      double f0 = 0.0, f1 = 0.0;
+      int k = 0;
+      for (; k + 1 < nclosed; k += 2) {
+        f0 += vpair(sD, sX, n, q, closed[k]);
+        f1 += vpair(sD, sX, n, q, closed[k + 1]);
+      }
+      if (k < nclosed) f0 += vpair(sD, sX, n, q, closed[k]);
+      const double hq = __ldg(a.ints.I1 + (size_t)q * ld1);
+      F[q] = hq + (f0 + f1);
+      if (det_getocc(d, q)) ed += hq + 0.5 * (f0 + f1);
     }
     for (int o = 16; o; o >>= 1) ed += __shfl_xor_sync(kFull, ed, o);
     __syncwarp();
@@ -256,15 +302,15 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
           ok = c2 >= sp.rmin[r] && c2 <= sp.rmax[r];
         }
         if (ok) {
-          const double h = hij_single_rows(a, d, oa, ci);
-          if (fabs(h) > eps) {
+          const int scr = single_screen(a, d, oa, ci, eps);
+          const double h = scr >= 0 ? hij_single_rows(a, d, oa, ci) : 0.0;
+          if (scr >= 0 && fabs(h) > eps) {
             det_flip(cand, oa);
             det_flip(cand, ci);
             keep = in_part(a, cand) && !hash_contains(a.hslots, a.hmask, a.dets, cand);
             if (keep) {
               v = h * cp;
-              e = ed - __ldg(a.ints.I1 + (size_t)ci * ld1) + __ldg(a.ints.I1 + (size_t)oa * ld1) - F[ci] + F[oa] -
-                  vpair(sD, sX, n, oa, ci);
+              e = ed + (F[oa] - F[ci]) - vpair(sD, sX, n, oa, ci);
             }
           }
         }
@@ -352,10 +398,10 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
             keep = in_part(a, cand) && !hash_contains(a.hslots, a.hmask, a.dets, cand);
             if (keep) {
               v = (double)vals[index] * pt_double_sign(cand, av, bv, oci, ocj) * cp;
-              e = ed - __ldg(a.ints.I1 + (size_t)oci * ld1) - __ldg(a.ints.I1 + (size_t)ocj * ld1) +
-                  __ldg(a.ints.I1 + (size_t)av * ld1) + __ldg(a.ints.I1 + (size_t)bv * ld1) - F[oci] - F[ocj] +
-                  vpair(sD, sX, n, oci, ocj) + F[av] - vpair(sD, sX, n, av, oci) - vpair(sD, sX, n, av, ocj) +
-                  F[bv] - vpair(sD, sX, n, bv, oci) - vpair(sD, sX, n, bv, ocj) + vpair(sD, sX, n, av, bv);
+              e = ed + ((F[av] + F[bv]) - (F[oci] + F[ocj])) +
+                  ((vpair(sD, sX, n, oci, ocj) + vpair(sD, sX, n, av, bv)) -
+                   ((vpair(sD, sX, n, av, oci) + vpair(sD, sX, n, av, ocj)) +
+                    (vpair(sD, sX, n, bv, oci) + vpair(sD, sX, n, bv, ocj))));
             }
           }
         }
@@ -366,12 +412,15 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
 }
 
 __global__ void k_pt_tables(const double* __restrict__ I2, int n, double* __restrict__ coul,
-                            double* __restrict__ exch) {
+                            double* __restrict__ exch, float* __restrict__ coul32, float* __restrict__ exch32) {
   const size_t nt = (size_t)n * n * n;
   for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += (size_t)gridDim.x * blockDim.x) {
-    const int J = (int)(t % n), I = (int)((t / n) % n), A = (int)(t / ((size_t)n * n));
-    coul[t] = i2_spatial(I2, A, I, J, J);
-    exch[t] = i2_spatial(I2, A, J, J, I);
+    const int A = (int)(t % n), J = (int)((t / n) % n), I = (int)(t / ((size_t)n * n));
+    const double c = i2_spatial(I2, A, I, J, J), x = i2_spatial(I2, A, J, J, I);
+    coul[t] = c;
+    exch[t] = x;
+    coul32[t] = (float)c;
+    exch32[t] = (float)x;
   }
 }
 
@@ -481,13 +530,17 @@ PtResult pt_deterministic(const Det2* dets, size_t n, const double* c, double E0
     const size_t nt = (size_t)ints.norb * ints.norb * ints.norb;
     w.coul.resize(nt);
     w.exch.resize(nt);
-    k_pt_tables<<<grid_for(nt, 256), 256, 0, s>>>(ints.I2, ints.norb, w.coul.p, w.exch.p);
+    w.coul32.resize(nt);
+    w.exch32.resize(nt);
+    k_pt_tables<<<grid_for(nt, 256), 256, 0, s>>>(ints.I2, ints.norb, w.coul.p, w.exch.p, w.coul32.p, w.exch32.p);
     SHCI_LAUNCH_CHECK();
     w.tables_of = ints.I2;
     w.tables_n = ints.norb;
   }
   a.coul = w.coul.p;
   a.exch = w.exch.p;
+  a.coul32 = w.coul32.p;
+  a.exch32 = w.exch32.p;
   const size_t gsmem = 2 * sizeof(double) * ints.norb * ints.norb;
   SHCI_CUDA(cudaFuncSetAttribute(k_pt_gen, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsmem));
 
