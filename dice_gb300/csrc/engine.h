@@ -120,6 +120,10 @@ void scan_exclusive_u32(const uint32_t* in, uint32_t* out, size_t n, Prims& pr, 
 void sort_dets(Det2* keys, uint32_t* vals, size_t n, Prims& pr, cudaStream_t s);
 // Stable sort of uint64 keys (unsigned order) with a uint32 payload, in place.
 void sort_u64(uint64_t* keys, uint32_t* vals, size_t n, Prims& pr, cudaStream_t s);
+// Stable sort of 128-bit keys (k1 high word, k0 low word; unsigned order)
+// with a uint32 payload, in place. A high word that is the same for every key
+// is not moved.
+void sort_u128(uint64_t* k0, uint64_t* k1, uint32_t* vals, size_t n, Prims& pr, cudaStream_t s);
 // Remove adjacent duplicates of sorted determinants; returns the new count.
 size_t unique_dets(Det2* keys, size_t n, Prims& pr, cudaStream_t s);
 

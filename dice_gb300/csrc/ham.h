@@ -172,7 +172,7 @@ struct PtResult {
   int partitions = 0;
 };
 struct PtWork {
-  DevBuf<Det2> cand;
+  DevBuf<uint64_t> key0, key1;  // candidate determinants, word by word
   DevBuf<double> num, en, part;
   DevBuf<uint32_t> perm;
   DevBuf<unsigned long long> next;  // parent queue, candidate counter

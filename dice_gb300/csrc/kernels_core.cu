@@ -267,6 +267,14 @@ static void radix_sort_soa(uint64_t* k0, uint64_t* k1, uint32_t* v, size_t n, Pr
   pr.sort_k0.reserve(n);
   if (k1) pr.sort_k1.reserve(n);
   if (v) pr.sort_v.reserve(n);
+  // a constant high word needs no moving: every permutation leaves it as is
+  bool k1_const = k1 != nullptr;
+  for (int d = 8; k1_const && d < 16; ++d) {
+    int nz = 0;
+    for (int j = 0; j < 256; ++j) nz += glob[d * 256 + j] != 0;
+    k1_const = nz <= 1;
+  }
+  if (k1_const) k1 = nullptr;
   uint64_t *a0 = k0, *a1 = k1, *b0 = pr.sort_k0.p, *b1 = k1 ? pr.sort_k1.p : nullptr;
   uint32_t *av = v, *bv = v ? pr.sort_v.p : nullptr;
   int npass = 0;
@@ -325,6 +333,10 @@ void sort_dets(Det2* keys, uint32_t* vals, size_t n, Prims& pr, cudaStream_t s) 
 
 void sort_u64(uint64_t* keys, uint32_t* vals, size_t n, Prims& pr, cudaStream_t s) {
   radix_sort_soa(keys, nullptr, vals, n, pr, s);
+}
+
+void sort_u128(uint64_t* k0, uint64_t* k1, uint32_t* vals, size_t n, Prims& pr, cudaStream_t s) {
+  radix_sort_soa(k0, k1, vals, n, pr, s);
 }
 
 __global__ void k_unique_flags(const Det2* __restrict__ k, size_t n, int64_t* __restrict__ flag) {

@@ -26,7 +26,8 @@
 //                Singles are screened in FP32 with a rigorous error bound and
 //                evaluated exactly (bit-identical to the reference's FP64
 //                element) only where the screen cannot decide or keeps them;
-//   radix sort   by determinant, candidate index as payload;
+//   radix sort   of the determinants (two key words, written apart by the
+//                generator) with the candidate index as payload;
 //   k_pt_reduce  one thread per run of equal determinants: the numerators are
 //                summed exactly in 128-bit fixed point (2^-80 units), so the
 //                sum does not depend on the order the atomics left the run in,
@@ -53,8 +54,8 @@ constexpr unsigned kPtGenBlocks = 152 * 6;
 constexpr unsigned kPtRedBlocks = 152 * 4;
 constexpr int kPtRedThreads = 256;
 // device bytes per candidate in one partition: determinant (16), numerator (8),
-// energy (8), sort payload (4), the sort's split words and alternates (16 + 16 + 4)
-constexpr size_t kPtBytesPerCand = 72;
+// energy (8), sort payload (4), the sort's alternates (16 + 4)
+constexpr size_t kPtBytesPerCand = 56;
 constexpr int kFixBits = 80;  // fixed-point numerator sums in units of 2^-80
 
 inline unsigned grid_for(size_t n, int threads, size_t max_blocks = 152 * 64) {
@@ -85,7 +86,8 @@ struct PtArgs {
   unsigned long long* next;     // parent queue
   unsigned long long* counter;  // candidates appended (counts past cap too)
   int64_t cap;
-  Det2* out;
+  uint64_t* key0;  // candidate determinant, low word
+  uint64_t* key1;  // high word
   double* num;
   double* en;
 };
@@ -119,7 +121,8 @@ __device__ __forceinline__ void pt_put(const PtArgs& a, bool keep, const Det2& c
   if (keep) {
     const unsigned long long q = base + __popc(m & ((1u << lane) - 1u));
     if (q < (unsigned long long)a.cap) {
-      a.out[q] = cand;
+      a.key0[q] = cand.w0;
+      a.key1[q] = cand.w1;
       a.num[q] = v;
       a.en[q] = e;
     }
@@ -453,20 +456,21 @@ __device__ __forceinline__ double from_fix(__int128 v) {
 
 // One thread per run of equal determinants in the sorted candidates; block
 // partials {E2, |psi1|^2, count} in part[3 * block].
-__global__ void __launch_bounds__(kPtRedThreads) k_pt_reduce(const Det2* __restrict__ sorted,
+__global__ void __launch_bounds__(kPtRedThreads) k_pt_reduce(const uint64_t* __restrict__ k0,
+                                                             const uint64_t* __restrict__ k1,
                                                              const uint32_t* __restrict__ perm,
                                                              const double* __restrict__ num,
                                                              const double* __restrict__ en, size_t m, double E0,
                                                              double* __restrict__ part) {
   double e2 = 0.0, psi = 0.0, cnt = 0.0;
   for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < m; k += (size_t)gridDim.x * blockDim.x) {
-    const Det2 d = sorted[k];
-    if (k > 0 && det_eq(d, sorted[k - 1])) continue;
+    const uint64_t d0 = k0[k], d1 = k1[k];
+    if (k > 0 && d0 == k0[k - 1] && d1 == k1[k - 1]) continue;
     uint32_t pk = perm[k];
     __int128 s = to_fix(num[pk]);
     double ea = en[pk];
     for (size_t j = k + 1; j < m; ++j) {
-      if (!det_eq(sorted[j], d)) break;
+      if (k0[j] != d0 || k1[j] != d1) break;
       pk = perm[j];
       s += to_fix(num[pk]);
       ea = fmin(ea, en[pk]);
@@ -552,7 +556,8 @@ PtResult pt_deterministic(const Det2* dets, size_t n, const double* c, double E0
     size_t avail = fr;
     if (g_alloc_cap) avail = std::min(avail, g_alloc_cap > g_alloc_live ? g_alloc_cap - g_alloc_live : (size_t)0);
     // what the buffers already hold counts as available to them
-    avail += w.cand.cap * sizeof(Det2) + (w.num.cap + w.en.cap) * sizeof(double) + w.perm.cap * sizeof(uint32_t);
+    avail += (w.key0.cap + w.key1.cap) * sizeof(uint64_t) + (w.num.cap + w.en.cap) * sizeof(double) +
+             w.perm.cap * sizeof(uint32_t);
     cap = (int64_t)(avail / 4 * 3 / kPtBytesPerCand);
   }
   cap = std::min<int64_t>(cap, (int64_t)0xfffffff0u);
@@ -560,13 +565,15 @@ PtResult pt_deterministic(const Det2* dets, size_t n, const double* c, double E0
 
   // one generation pass into buffers of `room` candidates; returns the count
   auto gen = [&](uint32_t nparts, uint32_t part, int64_t room) -> int64_t {
-    w.cand.reserve((size_t)room);
+    w.key0.reserve((size_t)room);
+    w.key1.reserve((size_t)room);
     w.num.reserve((size_t)room);
     w.en.reserve((size_t)room);
     a.nparts = nparts;
     a.part = part;
     a.cap = room;
-    a.out = w.cand.p;
+    a.key0 = w.key0.p;
+    a.key1 = w.key1.p;
     a.num = w.num.p;
     a.en = w.en.p;
     SHCI_CUDA(cudaMemsetAsync(w.next.p, 0, 2 * sizeof(unsigned long long), s));
@@ -577,13 +584,15 @@ PtResult pt_deterministic(const Det2* dets, size_t n, const double* c, double E0
     SHCI_CUDA(cudaStreamSynchronize(s));
     return (int64_t)total;
   };
+  PhaseTimer pt(s);
   auto reduce = [&](int64_t m, PtResult& r) {
     w.perm.resize((size_t)m);
     k_pt_iota<<<grid_for((size_t)m, 256), 256, 0, s>>>(w.perm.p, (size_t)m);
     SHCI_LAUNCH_CHECK();
-    sort_dets(w.cand.p, w.perm.p, (size_t)m, pr, s);
-    k_pt_reduce<<<kPtRedBlocks, kPtRedThreads, 0, s>>>(w.cand.p, w.perm.p, w.num.p, w.en.p, (size_t)m, E0,
-                                                       w.part.p);
+    sort_u128(w.key0.p, w.key1.p, w.perm.p, (size_t)m, pr, s);
+    pt.mark("pt sort");
+    k_pt_reduce<<<kPtRedBlocks, kPtRedThreads, 0, s>>>(w.key0.p, w.key1.p, w.perm.p, w.num.p, w.en.p, (size_t)m,
+                                                       E0, w.part.p);
     SHCI_LAUNCH_CHECK();
     std::vector<double> hp(3 * kPtRedBlocks);
     SHCI_CUDA(cudaMemcpyAsync(hp.data(), w.part.p, hp.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -595,9 +604,8 @@ PtResult pt_deterministic(const Det2* dets, size_t n, const double* c, double E0
     }
   };
 
-  PhaseTimer pt(s);
   // first pass into what the buffers hold (at least 64 per parent, at most cap)
-  int64_t room = std::min<int64_t>(cap, std::max<int64_t>((int64_t)w.cand.cap, 64 * (int64_t)n));
+  int64_t room = std::min<int64_t>(cap, std::max<int64_t>((int64_t)w.key0.cap, 64 * (int64_t)n));
   int64_t total = gen(1, 0, room);
   pt.mark("pt generate");
   if (total <= cap) {
@@ -608,7 +616,7 @@ PtResult pt_deterministic(const Det2* dets, size_t n, const double* c, double E0
     res.partitions = 1;
     res.candidates = total;
     if (total > 0) reduce(total, res);
-    pt.mark("pt sort+reduce");
+    pt.mark("pt reduce");
     return res;
   }
   // split by hash; a partition that still overflows doubles the count
