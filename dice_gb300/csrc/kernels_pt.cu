@@ -454,33 +454,117 @@ __device__ __forceinline__ double from_fix(__int128 v) {
   return (neg ? -d : d) * 8.271806125530276748714086920699e-25;  // 2^-80
 }
 
-// One thread per run of equal determinants in the sorted candidates; block
-// partials {E2, |psi1|^2, count} in part[3 * block].
+// Runs of equal determinants in the sorted candidates, reduced by warps: a
+// warp owns the runs whose first element lies in its tile of kPtRedTile
+// positions and walks them 32 positions at a time (following the last owned
+// run past the tile end). All loads of a round are independent (keys and
+// payload in order, numerators and energies gathered), and a segmented
+// inclusive scan over the lanes sums the fixed-point numerators and takes
+// the minimum energy per run; the lane at a run's end adds its term. Block
+// partials {E2, |psi1|^2, count} go to part[3 * block].
+constexpr int kPtRedTile = 256;
+
+__device__ __forceinline__ __int128 shfl_up_i128(__int128 v, int o) {
+  const unsigned long long lo = __shfl_up_sync(kFull, (unsigned long long)v, o);
+  const long long hi = __shfl_up_sync(kFull, (long long)(v >> 64), o);
+  return (__int128)(((unsigned __int128)(unsigned long long)hi << 64) | lo);
+}
+__device__ __forceinline__ __int128 shfl_i128(__int128 v, int src) {
+  const unsigned long long lo = __shfl_sync(kFull, (unsigned long long)v, src);
+  const long long hi = __shfl_sync(kFull, (long long)(v >> 64), src);
+  return (__int128)(((unsigned __int128)(unsigned long long)hi << 64) | lo);
+}
+
 __global__ void __launch_bounds__(kPtRedThreads) k_pt_reduce(const uint64_t* __restrict__ k0,
                                                              const uint64_t* __restrict__ k1,
                                                              const uint32_t* __restrict__ perm,
                                                              const double* __restrict__ num,
                                                              const double* __restrict__ en, size_t m, double E0,
                                                              double* __restrict__ part) {
+  const int lane = threadIdx.x & 31;
+  const size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const size_t nwarps = ((size_t)gridDim.x * blockDim.x) >> 5;
   double e2 = 0.0, psi = 0.0, cnt = 0.0;
-  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < m; k += (size_t)gridDim.x * blockDim.x) {
-    const uint64_t d0 = k0[k], d1 = k1[k];
-    if (k > 0 && d0 == k0[k - 1] && d1 == k1[k - 1]) continue;
-    uint32_t pk = perm[k];
-    __int128 s = to_fix(num[pk]);
-    double ea = en[pk];
-    for (size_t j = k + 1; j < m; ++j) {
-      if (k0[j] != d0 || k1[j] != d1) break;
-      pk = perm[j];
-      s += to_fix(num[pk]);
-      ea = fmin(ea, en[pk]);
+  // head flag of position q (first of its run)
+  auto is_head = [&](size_t q) -> bool {
+    return q == 0 || k0[q] != k0[q - 1] || k1[q] != k1[q - 1];
+  };
+  for (size_t t0 = warp * kPtRedTile; t0 < m; t0 += nwarps * kPtRedTile) {
+    const size_t t1 = t0 + kPtRedTile < m ? t0 + kPtRedTile : m;
+    // first head at or after t0, inside the tile
+    size_t b = t0;
+    bool found = false;
+    for (; b < t1; b += 32) {
+      const size_t q = b + lane;
+      const unsigned hm = __ballot_sync(kFull, q < t1 && is_head(q));
+      if (hm) {
+        b += __ffs(hm) - 1;
+        found = true;
+        break;
+      }
     }
-    const double sn = from_fix(s);
-    const double de = E0 - ea;
-    e2 += sn * sn / de;
-    const double t = sn / de;
-    psi += t * t;
-    cnt += 1.0;
+    if (!found) continue;
+    __int128 cs = 0;     // open run carried from the previous round
+    double ce = INFINITY;
+    size_t chead = b;
+    bool open = false;
+    for (; b < m; b += 32) {
+      if (b >= t1 && !(open && chead < t1)) break;
+      const size_t q = b + lane;
+      const bool valid = q < m;
+      bool head = false;
+      __int128 v = 0;
+      double e = INFINITY;
+      if (valid) {
+        head = (lane == 0) ? !open : is_head(q);
+        const uint32_t pk = perm[q];
+        v = to_fix(num[pk]);
+        e = en[pk];
+      }
+      // the run open at the end of the last round continues in lane 0's segment
+      if (lane == 0 && open && !head) {
+        v += cs;
+        e = fmin(e, ce);
+      }
+      size_t hp = head ? q : 0;
+      bool f = head;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const __int128 nv = shfl_up_i128(v, o);
+        const double ne = __shfl_up_sync(kFull, e, o);
+        const bool nf = __shfl_up_sync(kFull, (int)f, o) != 0;
+        const size_t nh = __shfl_up_sync(kFull, (unsigned long long)hp, o);
+        if (lane >= o) {
+          if (!f) {
+            v += nv;
+            e = fmin(e, ne);
+          }
+          f = f || nf;
+          hp = hp > nh ? hp : nh;
+        }
+      }
+      if (!f) hp = chead;  // lanes before the first head of the round
+      // does the run of this lane end here? (next position is a head or past the end)
+      bool next_head = __shfl_down_sync(kFull, (int)head, 1) != 0;
+      if (lane == 31) next_head = (q + 1 >= m) || is_head(q + 1);
+      if (valid && (q + 1 >= m || next_head)) {
+        if (hp < t1) {
+          const double sn = from_fix(v);
+          const double de = E0 - e;
+          e2 += sn * sn / de;
+          const double t = sn / de;
+          psi += t * t;
+          cnt += 1.0;
+        }
+      }
+      // carry lane 31's run when it continues into the next round
+      const bool cont = __shfl_sync(kFull, (int)(valid && !(q + 1 >= m || next_head)), 31) != 0;
+      cs = shfl_i128(v, 31);
+      ce = __shfl_sync(kFull, e, 31);
+      chead = __shfl_sync(kFull, (unsigned long long)hp, 31);
+      open = cont;
+      if (!open && b + 32 >= t1) break;
+    }
   }
   __shared__ double r0[kPtRedThreads / 32], r1[kPtRedThreads / 32], r2[kPtRedThreads / 32];
   for (int o = 16; o; o >>= 1) {
