@@ -108,6 +108,8 @@ __global__ void __launch_bounds__(kSelThreads) k_select(SelArgs a) {
 
     // ---- doubles
     if (fabs(a.maxEntry) < eps) continue;
+    // for a float v, (double)|v| < eps exactly when |v| < eps rounded up to float
+    const float eps_f = __double2float_ru(eps);
     const int npairs = nclosed * (nclosed - 1) / 2;
     for (int pb = 0; pb < npairs; pb += 32) {
       const int q = pb + lane;
@@ -116,7 +118,7 @@ __global__ void __launch_bounds__(kSelThreads) k_select(SelArgs a) {
       bool same = false;
       if (q < npairs) {
         // q -> (i, j), i > j, q = i(i-1)/2 + j
-        int i = (int)((1.0 + sqrt(1.0 + 8.0 * (double)q)) * 0.5);
+        int i = (int)((1.0f + sqrtf(1.0f + 8.0f * (float)q)) * 0.5f);  // corrected below
         while (i * (i - 1) / 2 > q) --i;
         while ((i + 1) * i / 2 <= q) ++i;
         int j = q - i * (i - 1) / 2;
@@ -134,7 +136,7 @@ __global__ void __launch_bounds__(kSelThreads) k_select(SelArgs a) {
           int64_t lo = s0, hi = s1;
           while (lo < hi) {
             int64_t mid = (lo + hi) >> 1;
-            if ((double)fabsf(vals[mid]) < eps)
+            if (fabsf(vals[mid]) < eps_f)
               hi = mid;
             else
               lo = mid + 1;
