@@ -173,11 +173,13 @@ struct PtResult {
 };
 struct PtWork {
   DevBuf<uint64_t> key0, key1;  // candidate determinants, word by word
-  DevBuf<double> num, en, part;
+  DevBuf<float2> num, en;  // numerators, E_a - E0 (float pairs)
+  DevBuf<double> part;
   DevBuf<uint32_t> perm;
   DevBuf<unsigned long long> next;  // parent queue, candidate counter
   DevBuf<double> coul, exch;        // dense (AI|JJ), (AJ|JI) of the integrals below
   DevBuf<float> coul32, exch32;     // and their FP32 roundings
+  DevBuf<float2> coulff, exchff;    // and as float pairs
   const double* tables_of = nullptr;
   int tables_n = 0;
 };

@@ -83,13 +83,16 @@ struct PtArgs {
   const double* exch;   // (AJ|JI) at (I n + J) n + A
   const float* coul32;  // the same rounded to FP32, for the screen
   const float* exch32;
+  const float2* coulff;  // and as float pairs
+  const float2* exchff;
   unsigned long long* next;     // parent queue
   unsigned long long* counter;  // candidates appended (counts past cap too)
   int64_t cap;
   uint64_t* key0;  // candidate determinant, low word
   uint64_t* key1;  // high word
-  double* num;
-  double* en;
+  float2* num;  // numerator as an unevaluated float pair (hi + lo)
+  float2* en;   // E_a - E0 as a float pair
+  float2 e0;    // E0 (without the core energy) as a float pair
 };
 
 __device__ __forceinline__ bool in_part(const PtArgs& a, const Det2& d) {
@@ -108,9 +111,47 @@ __device__ __forceinline__ double pt_double_sign(Det2 di, int a, int b, int i, i
   return ((n1 + n2) & 1) ? -1.0 : 1.0;
 }
 
+// ---- float pairs (hi + lo, |lo| <= ulp(hi)/2): the per-candidate arithmetic
+// runs on the FP32 pipe (the FP64 pipe of this part issues 2 lanes per clock
+// per SM). u = 2^-24 below.
+__device__ __forceinline__ float2 ff_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float v = __fsub_rn(s, a);
+  return make_float2(s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, v)), __fsub_rn(b, v)));
+}
+__device__ __forceinline__ float2 ff_fast_two_sum(float a, float b) {  // |a| >= |b| or a == 0
+  const float s = __fadd_rn(a, b);
+  return make_float2(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+// error below 3 u^2 (|a| + |b|)
+__device__ __forceinline__ float2 ff_add(float2 a, float2 b) {
+  const float2 t = ff_two_sum(a.x, b.x);
+  return ff_fast_two_sum(t.x, __fadd_rn(t.y, __fadd_rn(a.y, b.y)));
+}
+__device__ __forceinline__ float2 ff_neg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 ff_sub(float2 a, float2 b) { return ff_add(a, ff_neg(b)); }
+__device__ __forceinline__ float2 ff_mul(float2 a, float2 b) {
+  const float p = __fmul_rn(a.x, b.x);
+  const float e = __fmaf_rn(a.x, b.x, -p);
+  return ff_fast_two_sum(p, __fmaf_rn(a.x, b.y, __fmaf_rn(a.y, b.x, e)));
+}
+__device__ __forceinline__ float2 ff_mul_f(float a, float2 b) {
+  const float p = __fmul_rn(a, b.x);
+  const float e = __fmaf_rn(a, b.x, -p);
+  return ff_fast_two_sum(p, __fmaf_rn(a, b.y, e));
+}
+__device__ __forceinline__ float2 ff_of(double x) {
+  const float h = __double2float_rn(x);
+  return make_float2(h, __double2float_rn(x - (double)h));
+}
+__device__ __forceinline__ bool ff_less(float2 a, float2 b) { return a.x < b.x || (a.x == b.x && a.y < b.y); }
+__device__ __forceinline__ float2 shfl_ff(float2 v, int src) {
+  return make_float2(__shfl_sync(kFull, v.x, src), __shfl_sync(kFull, v.y, src));
+}
+
 // Warp-aggregated append of the lanes with `keep`; slots past cap are counted
 // but not written.
-__device__ __forceinline__ void pt_put(const PtArgs& a, bool keep, const Det2& cand, double v, double e) {
+__device__ __forceinline__ void pt_put(const PtArgs& a, bool keep, const Det2& cand, float2 v, float2 e) {
   const int lane = threadIdx.x & 31;
   const unsigned m = __ballot_sync(kFull, keep);
   if (!m) return;
@@ -155,14 +196,16 @@ __device__ __forceinline__ double hij_single_rows(const PtArgs& a, const Det2& k
 
 // FP32 screen of |Hij_1Excite(a, i)| against eps: returns +1 when the FP64
 // element certainly exceeds eps, -1 when it certainly does not, 0 when the
-// FP32 sum is too close to tell. Error bound: with u = 2^-24 and S the sum of
-// |I1_ai| and |d|, |x| over the m terms, the rounding of the integrals to
-// FP32 (u per value), of each difference and of the running sum stays below
-// (m + 3) u S; the margin used is (m + 8) 2u S.
-__device__ __forceinline__ int single_screen(const PtArgs& a, const Det2& ket, int ao, int io, double eps) {
+// FP32 sum is too close to tell. Error bound: with S the sum of |I1_ai| and
+// |d|, |x| over the m terms, the rounding of the integrals to FP32 (u per
+// value), of each difference and of the running sum stays below (m + 3) u S;
+// the margin used is (m + 8) 2u S, and the comparisons round against the
+// decision (eps_lo <= eps <= eps_hi are its FP32 neighbours).
+__device__ __forceinline__ int single_screen(const PtArgs& a, const Det2& ket, int ao, int io, float eps_lo,
+                                             float eps_hi) {
   const int n = a.ints.norb, n2 = 2 * n;
   const size_t base = (size_t)(io >> 1) * n * n + (ao >> 1);
-  float h = (float)__ldg(a.ints.I1 + (size_t)ao * n2 + io);
+  float h = __double2float_rn(__ldg(a.ints.I1 + (size_t)ao * n2 + io));
   float S = fabsf(h);
   int m = 0;
   const uint64_t same = (ao & 1) ? 0xaaaaaaaaaaaaaaaaull : 0x5555555555555555ull;
@@ -175,47 +218,92 @@ __device__ __forceinline__ int single_screen(const PtArgs& a, const Det2& ket, i
       const float dd = __ldg(a.coul32 + t);
       const float x = ((same >> j) & 1ull) ? __ldg(a.exch32 + t) : 0.0f;
       bits &= bits - 1;
-      h += dd - x;
-      S += fabsf(dd) + fabsf(x);
+      h = __fadd_rn(h, __fsub_rn(dd, x));
+      S = __fadd_rn(S, __fadd_rn(fabsf(dd), fabsf(x)));
       ++m;
     }
   }
-  const double margin = (double)(m + 8) * 1.1920928955078125e-07 * (double)S;
-  const double ah = fabs((double)h);
-  if (ah - margin > eps) return 1;
-  if (ah + margin < eps) return -1;
+  const float margin = __fmul_ru((float)(m + 8) * 1.1920928955078125e-07f, S);
+  const float ah = fabsf(h);
+  if (__fsub_rd(ah, margin) > eps_hi) return 1;
+  if (__fadd_ru(ah, margin) < eps_lo) return -1;
+  return 0;
+}
+
+// Hij_1Excite(a, i) in float pairs from the float-pair tables, with the
+// decision against eps: returns +1 / -1 when |H| certainly is above / not
+// above eps, 0 when FP64 must decide. Error bound: every table value carries
+// u^2 relative error, every pair addition 3 u^2 (|a| + |b|), so |H_ff - H|
+// stays below (7m + 8) u^2 S; the margin used is (8m + 24) u^2 (S + eps).
+__device__ __forceinline__ int single_ff(const PtArgs& a, const Det2& ket, int ao, int io, float2 eps_ff,
+                                         float2& H) {
+  const int n = a.ints.norb, n2 = 2 * n;
+  const size_t base = (size_t)(io >> 1) * n * n + (ao >> 1);
+  float2 h = ff_of(__ldg(a.ints.I1 + (size_t)ao * n2 + io));
+  float S = fabsf(h.x);
+  int m = 0;
+  const uint64_t same = (ao & 1) ? 0xaaaaaaaaaaaaaaaaull : 0x5555555555555555ull;
+#pragma unroll 1
+  for (int w = 0; w < 2; ++w) {
+    uint64_t bits = w ? ket.w1 : ket.w0;
+    while (bits) {
+      const int j = __ffsll((long long)bits) - 1;
+      const size_t t = base + (size_t)((j + 64 * w) >> 1) * n;
+      const float2 dd = __ldg(a.coulff + t);
+      bits &= bits - 1;
+      if ((same >> j) & 1ull) {
+        const float2 x = __ldg(a.exchff + t);
+        h = ff_add(h, ff_sub(dd, x));
+        S = __fadd_rn(S, __fadd_rn(fabsf(dd.x), fabsf(x.x)));
+      } else {
+        h = ff_add(h, dd);
+        S = __fadd_rn(S, fabsf(dd.x));
+      }
+      ++m;
+    }
+  }
+  const int lo = ao < io ? ao : io, hi = ao < io ? io : ao;
+  if (occ_between(ket, lo, hi) & 1) h = ff_neg(h);
+  H = h;
+  const float2 ah = h.x < 0.0f ? ff_neg(h) : h;
+  const float2 diff = ff_sub(ah, eps_ff);
+  const float margin = __fmul_ru((float)(8 * m + 24) * 3.5527136788005009e-15f, __fadd_ru(S, eps_ff.x));
+  if (diff.x > margin) return 1;
+  if (diff.x < -margin) return -1;
   return 0;
 }
 
 // V(p, q): Coulomb (opposite spins) or Coulomb minus exchange (same spin) of
-// spin orbitals p, q, from the n x n tables J and J - K staged in shared memory.
-__device__ __forceinline__ double vpair(const double* sJ, const double* sJK, int n, int p, int q) {
+// spin orbitals p, q, from the n x n float-pair tables J and J - K staged in
+// shared memory.
+__device__ __forceinline__ float2 vpair(const float2* sJ, const float2* sJK, int n, int p, int q) {
   const int o = (p >> 1) * n + (q >> 1);
   return ((p ^ q) & 1) ? sJ[o] : sJK[o];
 }
 
 __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
-  extern __shared__ double smd[];
+  extern __shared__ float2 smf[];
   __shared__ unsigned char s_closed[kPtWarps][kMaxSpin];
   __shared__ unsigned char s_open[kPtWarps][kMaxSpin];   // alpha holes, then beta holes
   __shared__ unsigned char s_cspin[kPtWarps][kMaxSpin];  // alpha electrons, then beta electrons
-  __shared__ double s_F[kPtWarps][kMaxSpin];
+  __shared__ float2 s_F[kPtWarps][kMaxSpin];
   const int n = a.ints.norb, nn = n * n;
-  double* sD = smd;       // J
-  double* sX = smd + nn;  // J - K
+  float2* sD = smf;            // J
+  float2* sX = smf + nn;       // J - K
+  float2* sH = smf + 2 * nn;   // h_pp, spin orbitals
   for (int j = threadIdx.x; j < nn; j += blockDim.x) {
-    sD[j] = a.ints.Direct[j];
-    sX[j] = __dsub_rn(a.ints.Direct[j], a.ints.Exchange[j]);
+    sD[j] = ff_of(a.ints.Direct[j]);
+    sX[j] = ff_of(__dsub_rn(a.ints.Direct[j], a.ints.Exchange[j]));
   }
+  for (int j = threadIdx.x; j < 2 * n; j += blockDim.x) sH[j] = ff_of(a.ints.I1[(size_t)j * (2 * n + 1)]);
   __syncthreads();
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   unsigned char* closed = s_closed[wib];
   unsigned char* open = s_open[wib];
   unsigned char* cspin = s_cspin[wib];
-  double* F = s_F[wib];
+  float2* F = s_F[wib];
   const unsigned lt = (1u << lane) - 1u;
   const int n2 = 2 * n;
-  const int ld1 = n2 + 1;  // diagonal stride of the (2n)x(2n) one-electron matrix
   const SelectParams& sp = a.sp;
   while (true) {
     unsigned long long pp = 0;
@@ -227,6 +315,8 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
     const double cp = a.c[p];
     const double eps = fabs(a.eps2 / cp);
     if (!(eps < INFINITY)) continue;  // c_i = 0: nothing passes either threshold
+    const float eps_lo = __double2float_rd(eps), eps_hi = __double2float_ru(eps);
+    const float2 eps_ff = ff_of(eps), cp_ff = ff_of(cp);
     // occupied list (ascending) and per-spin electron / hole lists, by ballot
     const int nclosed = __popcll(d.w0) + __popcll(d.w1);
     const int ncA = __popcll(d.w0 & 0x5555555555555555ull) + __popcll(d.w1 & 0x5555555555555555ull);
@@ -262,21 +352,21 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
     }
     __syncwarp();
     // orbital energies F_q = h_qq + sum over occupied r of V(q, r) (V(q, q) = 0)
-    // and the parent's energy sum_occ (h_qq + F_q) / 2
-    double ed = 0.0;
+    // and the parent's energy relative to E0, sum_occ (h_qq + F_q) / 2 - E0
+    float2 ed = make_float2(0.0f, 0.0f);
     for (int q = lane; q < n2; q += 32) {
-      double f0 = 0.0, f1 = 0.0;
-      int k = 0;
-      for (; k + 1 < nclosed; k += 2) {
-        f0 += vpair(sD, sX, n, q, closed[k]);
-        f1 += vpair(sD, sX, n, q, closed[k + 1]);
+      float2 f = make_float2(0.0f, 0.0f);
+      for (int k = 0; k < nclosed; ++k) f = ff_add(f, vpair(sD, sX, n, q, closed[k]));
+      const float2 hq = sH[q];
+      F[q] = ff_add(hq, f);
+      if (det_getocc(d, q)) {
+        const float2 half = ff_add(hq, make_float2(0.5f * f.x, 0.5f * f.y));
+        ed = ff_add(ed, half);
       }
-      if (k < nclosed) f0 += vpair(sD, sX, n, q, closed[k]);
-      const double hq = __ldg(a.ints.I1 + (size_t)q * ld1);
-      F[q] = hq + (f0 + f1);
-      if (det_getocc(d, q)) ed += hq + 0.5 * (f0 + f1);
     }
-    for (int o = 16; o; o >>= 1) ed += __shfl_xor_sync(kFull, ed, o);
+    for (int o = 16; o; o >>= 1) ed = ff_add(ed, make_float2(__shfl_xor_sync(kFull, ed.x, o),
+                                                         __shfl_xor_sync(kFull, ed.y, o)));
+    ed = ff_sub(shfl_ff(ed, 0), a.e0);  // one value for the whole warp
     __syncwarp();
     int cur[kMaxRestrict];
     for (int r = 0; r < sp.nrestrict; ++r) cur[r] = __popcll(d.w0 & sp.rmask0[r]) + __popcll(d.w1 & sp.rmask1[r]);
@@ -289,7 +379,7 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
       const int q = b0 + lane;
       bool keep = false;
       Det2 cand = d;
-      double v = 0.0, e = 0.0;
+      float2 v = make_float2(0.0f, 0.0f), e = v;
       if (q < ns) {
         int ci, oa;
         if (q < nsA) {
@@ -305,15 +395,22 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
           ok = c2 >= sp.rmin[r] && c2 <= sp.rmax[r];
         }
         if (ok) {
-          const int scr = single_screen(a, d, oa, ci, eps);
-          const double h = scr >= 0 ? hij_single_rows(a, d, oa, ci) : 0.0;
-          if (scr >= 0 && fabs(h) > eps) {
+          // FP32 screen, then float pairs, then (rarely) the FP64 element
+          int dec = single_screen(a, d, oa, ci, eps_lo, eps_hi);
+          float2 H = make_float2(0.0f, 0.0f);
+          if (dec >= 0) dec = single_ff(a, d, oa, ci, eps_ff, H);
+          if (dec == 0) {
+            const double h = hij_single_rows(a, d, oa, ci);
+            dec = fabs(h) > eps ? 1 : -1;
+            H = ff_of(h);
+          }
+          if (dec > 0) {
             det_flip(cand, oa);
             det_flip(cand, ci);
             keep = in_part(a, cand) && !hash_contains(a.hslots, a.hmask, a.dets, cand);
             if (keep) {
-              v = h * cp;
-              e = ed + (F[oa] - F[ci]) - vpair(sD, sX, n, oa, ci);
+              v = ff_mul(H, cp_ff);
+              e = ff_sub(ff_add(ed, ff_sub(F[oa], F[ci])), vpair(sD, sX, n, oa, ci));
             }
           }
         }
@@ -383,7 +480,7 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
         const bool osame = __shfl_sync(kFull, (int)same, lo) != 0;
         bool keep = false;
         Det2 cand = d;
-        double v = 0.0, e = 0.0;
+        float2 v = make_float2(0.0f, 0.0f), e = v;
         if (f < total) {
           const int64_t index = ls + (f - eo);
           const int16_t* pr = osame ? a.hb.samePairs : a.hb.oppPairs;
@@ -402,11 +499,13 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
             det_flip(cand, ocj);
             keep = in_part(a, cand) && !hash_contains(a.hslots, a.hmask, a.dets, cand);
             if (keep) {
-              v = (double)vals[index] * pt_double_sign(cand, av, bv, oci, ocj) * cp;
-              e = ed + ((F[av] + F[bv]) - (F[oci] + F[ocj])) +
-                  ((vpair(sD, sX, n, oci, ocj) + vpair(sD, sX, n, av, bv)) -
-                   ((vpair(sD, sX, n, av, oci) + vpair(sD, sX, n, av, ocj)) +
-                    (vpair(sD, sX, n, bv, oci) + vpair(sD, sX, n, bv, ocj))));
+              const float vf = vals[index];
+              v = ff_mul_f(pt_double_sign(cand, av, bv, oci, ocj) > 0.0 ? vf : -vf, cp_ff);
+              const float2 fa = ff_add(F[av], F[bv]), fi = ff_add(F[oci], F[ocj]);
+              const float2 vin = ff_add(vpair(sD, sX, n, oci, ocj), vpair(sD, sX, n, av, bv));
+              const float2 vx = ff_add(ff_add(vpair(sD, sX, n, av, oci), vpair(sD, sX, n, av, ocj)),
+                                       ff_add(vpair(sD, sX, n, bv, oci), vpair(sD, sX, n, bv, ocj)));
+              e = ff_add(ed, ff_add(ff_sub(fa, fi), ff_sub(vin, vx)));
             }
           }
         }
@@ -417,7 +516,8 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
 }
 
 __global__ void k_pt_tables(const double* __restrict__ I2, int n, double* __restrict__ coul,
-                            double* __restrict__ exch, float* __restrict__ coul32, float* __restrict__ exch32) {
+                            double* __restrict__ exch, float* __restrict__ coul32, float* __restrict__ exch32,
+                            float2* __restrict__ coulff, float2* __restrict__ exchff) {
   const size_t nt = (size_t)n * n * n;
   for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += (size_t)gridDim.x * blockDim.x) {
     const int A = (int)(t % n), J = (int)((t / n) % n), I = (int)(t / ((size_t)n * n));
@@ -426,6 +526,8 @@ __global__ void k_pt_tables(const double* __restrict__ I2, int n, double* __rest
     exch[t] = x;
     coul32[t] = (float)c;
     exch32[t] = (float)x;
+    coulff[t] = ff_of(c);
+    exchff[t] = ff_of(x);
   }
 }
 
@@ -435,19 +537,21 @@ __global__ void k_pt_iota(uint32_t* __restrict__ p, size_t n) {
 }
 
 // x in units of 2^-kFixBits, truncated toward zero (|x| < 2^47).
-__device__ __forceinline__ __int128 to_fix(double x) {
-  const long long b = __double_as_longlong(x);
-  const int ex = (int)((b >> 52) & 0x7ff);
+__device__ __forceinline__ __int128 to_fix(float x) {
+  const unsigned b = __float_as_uint(x);
+  const int ex = (int)((b >> 23) & 0xff);
   if (ex == 0) return 0;  // zero or subnormal: below the unit
-  const unsigned long long m = ((unsigned long long)b & 0xfffffffffffffull) | (1ull << 52);
-  const int sh = ex - 1075 + kFixBits;
+  const unsigned long long m = (b & 0x7fffffu) | 0x800000u;
+  const int sh = ex - 150 + kFixBits;
   unsigned __int128 v = 0;
   if (sh >= 0)
-    v = (unsigned __int128)m << (sh < 74 ? sh : 74);
-  else if (sh > -64)
+    v = (unsigned __int128)m << (sh < 103 ? sh : 103);
+  else if (sh > -32)
     v = m >> (-sh);
-  return b < 0 ? -(__int128)v : (__int128)v;
+  return (b >> 31) ? -(__int128)v : (__int128)v;
 }
+// a float pair exactly (up to the 2^-kFixBits truncation of each part)
+__device__ __forceinline__ __int128 to_fix(float2 x) { return to_fix(x.x) + to_fix(x.y); }
 
 __device__ __forceinline__ double from_fix(__int128 v) {
   const bool neg = v < 0;
@@ -480,8 +584,8 @@ __device__ __forceinline__ __int128 shfl_i128(__int128 v, int src) {
 __global__ void __launch_bounds__(kPtRedThreads) k_pt_reduce(const uint64_t* __restrict__ k0,
                                                              const uint64_t* __restrict__ k1,
                                                              const uint32_t* __restrict__ perm,
-                                                             const double* __restrict__ num,
-                                                             const double* __restrict__ en, size_t m, double E0,
+                                                             const float2* __restrict__ num,
+                                                             const float2* __restrict__ en, size_t m,
                                                              double* __restrict__ part) {
   const int lane = threadIdx.x & 31;
   const size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -507,7 +611,7 @@ __global__ void __launch_bounds__(kPtRedThreads) k_pt_reduce(const uint64_t* __r
     }
     if (!found) continue;
     __int128 cs = 0;     // open run carried from the previous round
-    double ce = INFINITY;
+    float2 ce = make_float2(INFINITY, 0.0f);
     size_t chead = b;
     bool open = false;
     for (; b < m; b += 32) {
@@ -516,7 +620,7 @@ __global__ void __launch_bounds__(kPtRedThreads) k_pt_reduce(const uint64_t* __r
       const bool valid = q < m;
       bool head = false;
       __int128 v = 0;
-      double e = INFINITY;
+      float2 e = make_float2(INFINITY, 0.0f);
       if (valid) {
         head = (lane == 0) ? !open : is_head(q);
         const uint32_t pk = perm[q];
@@ -526,20 +630,20 @@ __global__ void __launch_bounds__(kPtRedThreads) k_pt_reduce(const uint64_t* __r
       // the run open at the end of the last round continues in lane 0's segment
       if (lane == 0 && open && !head) {
         v += cs;
-        e = fmin(e, ce);
+        if (ff_less(ce, e)) e = ce;
       }
       size_t hp = head ? q : 0;
       bool f = head;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
         const __int128 nv = shfl_up_i128(v, o);
-        const double ne = __shfl_up_sync(kFull, e, o);
+        const float2 ne = make_float2(__shfl_up_sync(kFull, e.x, o), __shfl_up_sync(kFull, e.y, o));
         const bool nf = __shfl_up_sync(kFull, (int)f, o) != 0;
         const size_t nh = __shfl_up_sync(kFull, (unsigned long long)hp, o);
         if (lane >= o) {
           if (!f) {
             v += nv;
-            e = fmin(e, ne);
+            if (ff_less(ne, e)) e = ne;
           }
           f = f || nf;
           hp = hp > nh ? hp : nh;
@@ -552,7 +656,7 @@ __global__ void __launch_bounds__(kPtRedThreads) k_pt_reduce(const uint64_t* __r
       if (valid && (q + 1 >= m || next_head)) {
         if (hp < t1) {
           const double sn = from_fix(v);
-          const double de = E0 - e;
+          const double de = -((double)e.x + (double)e.y);  // E0 - E_a
           e2 += sn * sn / de;
           const double t = sn / de;
           psi += t * t;
@@ -562,7 +666,7 @@ __global__ void __launch_bounds__(kPtRedThreads) k_pt_reduce(const uint64_t* __r
       // carry lane 31's run when it continues into the next round
       const bool cont = __shfl_sync(kFull, (int)(valid && !(q + 1 >= m || next_head)), 31) != 0;
       cs = shfl_i128(v, 31);
-      ce = __shfl_sync(kFull, e, 31);
+      ce = shfl_ff(e, 31);
       chead = __shfl_sync(kFull, (unsigned long long)hp, 31);
       open = cont;
       if (!open && b + 32 >= t1) break;
@@ -622,7 +726,10 @@ PtResult pt_deterministic(const Det2* dets, size_t n, const double* c, double E0
     w.exch.resize(nt);
     w.coul32.resize(nt);
     w.exch32.resize(nt);
-    k_pt_tables<<<grid_for(nt, 256), 256, 0, s>>>(ints.I2, ints.norb, w.coul.p, w.exch.p, w.coul32.p, w.exch32.p);
+    w.coulff.resize(nt);
+    w.exchff.resize(nt);
+    k_pt_tables<<<grid_for(nt, 256), 256, 0, s>>>(ints.I2, ints.norb, w.coul.p, w.exch.p, w.coul32.p, w.exch32.p,
+                                                   w.coulff.p, w.exchff.p);
     SHCI_LAUNCH_CHECK();
     w.tables_of = ints.I2;
     w.tables_n = ints.norb;
@@ -630,8 +737,14 @@ PtResult pt_deterministic(const Det2* dets, size_t n, const double* c, double E0
   a.coul = w.coul.p;
   a.exch = w.exch.p;
   a.coul32 = w.coul32.p;
+  a.coulff = w.coulff.p;
+  a.exchff = w.exchff.p;
+  {
+    const float h = (float)E0;
+    a.e0 = make_float2(h, (float)(E0 - (double)h));
+  }
   a.exch32 = w.exch32.p;
-  const size_t gsmem = 2 * sizeof(double) * ints.norb * ints.norb;
+  const size_t gsmem = sizeof(float2) * (2 * ints.norb * ints.norb + 2 * ints.norb);
   SHCI_CUDA(cudaFuncSetAttribute(k_pt_gen, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsmem));
 
   // capacity of one partition
@@ -642,7 +755,7 @@ PtResult pt_deterministic(const Det2* dets, size_t n, const double* c, double E0
     size_t avail = fr;
     if (g_alloc_cap) avail = std::min(avail, g_alloc_cap > g_alloc_live ? g_alloc_cap - g_alloc_live : (size_t)0);
     // what the buffers already hold counts as available to them
-    avail += (w.key0.cap + w.key1.cap) * sizeof(uint64_t) + (w.num.cap + w.en.cap) * sizeof(double) +
+    avail += (w.key0.cap + w.key1.cap) * sizeof(uint64_t) + (w.num.cap + w.en.cap) * sizeof(float2) +
              w.perm.cap * sizeof(uint32_t);
     cap = (int64_t)(avail / 4 * 3 / kPtBytesPerCand);
   }
@@ -678,7 +791,7 @@ PtResult pt_deterministic(const Det2* dets, size_t n, const double* c, double E0
     sort_u128(w.key0.p, w.key1.p, w.perm.p, (size_t)m, pr, s);
     pt.mark("pt sort");
     k_pt_reduce<<<kPtRedBlocks, kPtRedThreads, 0, s>>>(w.key0.p, w.key1.p, w.perm.p, w.num.p, w.en.p, (size_t)m,
-                                                       E0, w.part.p);
+                                                       w.part.p);
     SHCI_LAUNCH_CHECK();
     std::vector<double> hp(3 * kPtRedBlocks);
     SHCI_CUDA(cudaMemcpyAsync(hp.data(), w.part.p, hp.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
