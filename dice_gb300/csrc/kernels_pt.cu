@@ -287,6 +287,8 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
   __shared__ unsigned char s_open[kPtWarps][kMaxSpin];   // alpha holes, then beta holes
   __shared__ unsigned char s_cspin[kPtWarps][kMaxSpin];  // alpha electrons, then beta electrons
   __shared__ float2 s_F[kPtWarps][kMaxSpin];
+  __shared__ uint32_t s_qo[kPtWarps][64];
+  __shared__ float s_qv[kPtWarps][64];
   const int n = a.ints.norb, nn = n * n;
   float2* sD = smf;            // J
   float2* sX = smf + nn;       // J - K
@@ -371,17 +373,83 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
     int cur[kMaxRestrict];
     for (int r = 0; r < sp.nrestrict; ++r) cur[r] = __popcll(d.w0 & sp.rmask0[r]) + __popcll(d.w1 & sp.rmask1[r]);
 
+    // Survivors of the cheap tests wait in a per-warp ring of 64 entries and
+    // are processed 32 at a time, so that the costly part (pair-arithmetic
+    // element or energy, hash probe, stores) runs on full warps. Entry: the
+    // orbitals i | j << 8 | a << 16 | b << 24 (j = b = 0xff for a single) and
+    // the heat-bath value of a double.
+    uint32_t* qo = s_qo[wib];
+    float* qv = s_qv[wib];
+    unsigned qh = 0, qn = 0;  // ring head and length (warp-uniform)
+    auto push = [&](bool surv, uint32_t w, float val) {
+      const unsigned m = __ballot_sync(kFull, surv);
+      if (surv) {
+        const unsigned slot = (qh + qn + __popc(m & lt)) & 63u;
+        qo[slot] = w;
+        qv[slot] = val;
+      }
+      qn += __popc(m);
+      __syncwarp();
+    };
+    auto drain = [&](unsigned cnt) {  // the first cnt (<= 32) entries
+      bool keep = false;
+      Det2 cand = d;
+      float2 v = make_float2(0.0f, 0.0f), e = v;
+      if ((unsigned)lane < cnt) {
+        const unsigned slot = (qh + lane) & 63u;
+        const uint32_t w = qo[slot];
+        const int oi = w & 0xff, oj = (w >> 8) & 0xff, oa = (w >> 16) & 0xff, ob = w >> 24;
+        if (oj == 0xff) {
+          // single i -> a: float pairs, then (rarely) the FP64 element
+          float2 H = make_float2(0.0f, 0.0f);
+          int dec = single_ff(a, d, oa, oi, eps_ff, H);
+          if (dec == 0) {
+            const double h = hij_single_rows(a, d, oa, oi);
+            dec = fabs(h) > eps ? 1 : -1;
+            H = ff_of(h);
+          }
+          if (dec > 0) {
+            det_flip(cand, oa);
+            det_flip(cand, oi);
+            keep = in_part(a, cand) && !hash_contains(a.hslots, a.hmask, a.dets, cand);
+            if (keep) {
+              v = ff_mul(H, cp_ff);
+              e = ff_sub(ff_add(ed, ff_sub(F[oa], F[oi])), vpair(sD, sX, n, oa, oi));
+            }
+          }
+        } else {
+          // double i -> a, j -> b
+          det_flip(cand, oa);
+          det_flip(cand, ob);
+          det_flip(cand, oi);
+          det_flip(cand, oj);
+          keep = in_part(a, cand) && !hash_contains(a.hslots, a.hmask, a.dets, cand);
+          if (keep) {
+            const float vf = qv[slot];
+            v = ff_mul_f(pt_double_sign(cand, oa, ob, oi, oj) > 0.0 ? vf : -vf, cp_ff);
+            const float2 fa = ff_add(F[oa], F[ob]), fi = ff_add(F[oi], F[oj]);
+            const float2 vin = ff_add(vpair(sD, sX, n, oi, oj), vpair(sD, sX, n, oa, ob));
+            const float2 vx = ff_add(ff_add(vpair(sD, sX, n, oa, oi), vpair(sD, sX, n, oa, oj)),
+                                     ff_add(vpair(sD, sX, n, ob, oi), vpair(sD, sX, n, ob, oj)));
+            e = ff_add(ed, ff_add(ff_sub(fa, fi), ff_sub(vin, vx)));
+          }
+        }
+      }
+      pt_put(a, keep, cand, v, e);
+      qh = (qh + cnt) & 63u;
+      qn -= cnt;
+      __syncwarp();
+    };
+
     // ---- singles: every same-spin (i, a) (a spin flip has a zero element:
-    // I1 has no alpha-beta block); the exact element decides
+    // I1 has no alpha-beta block); FP32 screen here, the rest when drained
     const int ncB = nclosed - ncA, nhB = n - ncB;
     const int nsA = ncA * nhA, ns = nsA + ncB * nhB;
     for (int b0 = 0; b0 < ns; b0 += 32) {
       const int q = b0 + lane;
-      bool keep = false;
-      Det2 cand = d;
-      float2 v = make_float2(0.0f, 0.0f), e = v;
+      bool surv = false;
+      int ci = 0, oa = 0;
       if (q < ns) {
-        int ci, oa;
         if (q < nsA) {
           ci = cspin[q / nhA];
           oa = open[q % nhA];
@@ -394,29 +462,12 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
           int c2 = cur[r] - in_mask(sp, r, ci) + in_mask(sp, r, oa);
           ok = c2 >= sp.rmin[r] && c2 <= sp.rmax[r];
         }
-        if (ok) {
-          // FP32 screen, then float pairs, then (rarely) the FP64 element
-          int dec = single_screen(a, d, oa, ci, eps_lo, eps_hi);
-          float2 H = make_float2(0.0f, 0.0f);
-          if (dec >= 0) dec = single_ff(a, d, oa, ci, eps_ff, H);
-          if (dec == 0) {
-            const double h = hij_single_rows(a, d, oa, ci);
-            dec = fabs(h) > eps ? 1 : -1;
-            H = ff_of(h);
-          }
-          if (dec > 0) {
-            det_flip(cand, oa);
-            det_flip(cand, ci);
-            keep = in_part(a, cand) && !hash_contains(a.hslots, a.hmask, a.dets, cand);
-            if (keep) {
-              v = ff_mul(H, cp_ff);
-              e = ff_sub(ff_add(ed, ff_sub(F[oa], F[ci])), vpair(sD, sX, n, oa, ci));
-            }
-          }
-        }
+        surv = ok && single_screen(a, d, oa, ci, eps_lo, eps_hi) >= 0;
       }
-      pt_put(a, keep, cand, v, e);
+      push(surv, (uint32_t)ci | 0xff00u | ((uint32_t)oa << 16) | 0xff000000u, 0.0f);
+      if (qn >= 32) drain(32);
     }
+    while (qn > 0) drain(qn < 32 ? qn : 32);
 
     // ---- doubles: heat-bath list prefixes, flattened over the warp
     if (fabs(a.maxEntry) < eps) continue;
@@ -478,13 +529,12 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
         const int oci = __shfl_sync(kFull, ci, lo);
         const int ocj = __shfl_sync(kFull, cj, lo);
         const bool osame = __shfl_sync(kFull, (int)same, lo) != 0;
-        bool keep = false;
-        Det2 cand = d;
-        float2 v = make_float2(0.0f, 0.0f), e = v;
+        bool surv = false;
+        uint32_t w = 0;
+        float vf = 0.0f;
         if (f < total) {
           const int64_t index = ls + (f - eo);
           const int16_t* pr = osame ? a.hb.samePairs : a.hb.oppPairs;
-          const float* vals = osame ? a.hb.sameVal : a.hb.oppVal;
           const int av = 2 * pr[2 * index] + (oci & 1);
           const int bv = 2 * pr[2 * index + 1] + (ocj & 1);
           bool ok = true;
@@ -492,26 +542,17 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
             int c2 = cur[r] - in_mask(sp, r, oci) - in_mask(sp, r, ocj) + in_mask(sp, r, av) + in_mask(sp, r, bv);
             ok = c2 >= sp.rmin[r] && c2 <= sp.rmax[r];
           }
-          if (ok && !(det_getocc(d, av) || det_getocc(d, bv))) {
-            det_flip(cand, av);
-            det_flip(cand, bv);
-            det_flip(cand, oci);
-            det_flip(cand, ocj);
-            keep = in_part(a, cand) && !hash_contains(a.hslots, a.hmask, a.dets, cand);
-            if (keep) {
-              const float vf = vals[index];
-              v = ff_mul_f(pt_double_sign(cand, av, bv, oci, ocj) > 0.0 ? vf : -vf, cp_ff);
-              const float2 fa = ff_add(F[av], F[bv]), fi = ff_add(F[oci], F[ocj]);
-              const float2 vin = ff_add(vpair(sD, sX, n, oci, ocj), vpair(sD, sX, n, av, bv));
-              const float2 vx = ff_add(ff_add(vpair(sD, sX, n, av, oci), vpair(sD, sX, n, av, ocj)),
-                                       ff_add(vpair(sD, sX, n, bv, oci), vpair(sD, sX, n, bv, ocj)));
-              e = ff_add(ed, ff_add(ff_sub(fa, fi), ff_sub(vin, vx)));
-            }
+          surv = ok && !(det_getocc(d, av) || det_getocc(d, bv));
+          if (surv) {
+            w = (uint32_t)oci | ((uint32_t)ocj << 8) | ((uint32_t)av << 16) | ((uint32_t)bv << 24);
+            vf = (osame ? a.hb.sameVal : a.hb.oppVal)[index];
           }
         }
-        pt_put(a, keep, cand, v, e);
+        push(surv, w, vf);
+        if (qn >= 32) drain(32);
       }
     }
+    while (qn > 0) drain(qn < 32 ? qn : 32);
   }
 }
 
