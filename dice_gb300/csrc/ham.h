@@ -173,7 +173,7 @@ struct PtResult {
 };
 struct PtWork {
   DevBuf<uint64_t> key0, key1;  // candidate determinants, word by word
-  DevBuf<float2> num, en;  // numerators, E_a - E0 (float pairs)
+  DevBuf<float4> ne;  // numerator and E_a - E0 of each candidate (float pairs)
   DevBuf<double> part;
   DevBuf<uint32_t> perm;
   DevBuf<unsigned long long> next;  // parent queue, candidate counter

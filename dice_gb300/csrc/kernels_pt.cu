@@ -90,8 +90,7 @@ struct PtArgs {
   int64_t cap;
   uint64_t* key0;  // candidate determinant, low word
   uint64_t* key1;  // high word
-  float2* num;  // numerator as an unevaluated float pair (hi + lo)
-  float2* en;   // E_a - E0 as a float pair
+  float4* ne;   // numerator (x + y) and E_a - E0 (z + w), both float pairs
   float2 e0;    // E0 (without the core energy) as a float pair
 };
 
@@ -164,8 +163,7 @@ __device__ __forceinline__ void pt_put(const PtArgs& a, bool keep, const Det2& c
     if (q < (unsigned long long)a.cap) {
       a.key0[q] = cand.w0;
       a.key1[q] = cand.w1;
-      a.num[q] = v;
-      a.en[q] = e;
+      a.ne[q] = make_float4(v.x, v.y, e.x, e.y);
     }
   }
 }
@@ -625,13 +623,36 @@ __device__ __forceinline__ __int128 shfl_i128(__int128 v, int src) {
 __global__ void __launch_bounds__(kPtRedThreads) k_pt_reduce(const uint64_t* __restrict__ k0,
                                                              const uint64_t* __restrict__ k1,
                                                              const uint32_t* __restrict__ perm,
-                                                             const float2* __restrict__ num,
-                                                             const float2* __restrict__ en, size_t m,
+                                                             const float4* __restrict__ ne, size_t m,
                                                              double* __restrict__ part) {
   const int lane = threadIdx.x & 31;
   const size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const size_t nwarps = ((size_t)gridDim.x * blockDim.x) >> 5;
   double e2 = 0.0, psi = 0.0, cnt = 0.0;
+  __shared__ unsigned long long s_qlo[kPtRedThreads / 32][64];
+  __shared__ long long s_qhi[kPtRedThreads / 32][64];
+  __shared__ float2 s_qe[kPtRedThreads / 32][64];
+  unsigned long long* qlo = s_qlo[threadIdx.x >> 5];
+  long long* qhi = s_qhi[threadIdx.x >> 5];
+  float2* qe = s_qe[threadIdx.x >> 5];
+  unsigned qh = 0, qn = 0;  // finished runs waiting (warp-uniform)
+  const unsigned lt = (1u << lane) - 1u;
+  auto flush = [&](unsigned c) {
+    if ((unsigned)lane < c) {
+      const unsigned slot = (qh + lane) & 63u;
+      const __int128 v = (__int128)(((unsigned __int128)(unsigned long long)qhi[slot] << 64) | qlo[slot]);
+      const float2 e = qe[slot];
+      const double sn = from_fix(v);
+      const double inv = 1.0 / -((double)e.x + (double)e.y);  // 1 / (E0 - E_a)
+      const double t = sn * inv;
+      e2 += sn * t;
+      psi += t * t;
+      cnt += 1.0;
+    }
+    qh = (qh + c) & 63u;
+    qn -= c;
+    __syncwarp();
+  };
   // head flag of position q (first of its run)
   auto is_head = [&](size_t q) -> bool {
     return q == 0 || k0[q] != k0[q - 1] || k1[q] != k1[q - 1];
@@ -665,8 +686,9 @@ __global__ void __launch_bounds__(kPtRedThreads) k_pt_reduce(const uint64_t* __r
       if (valid) {
         head = (lane == 0) ? !open : is_head(q);
         const uint32_t pk = perm[q];
-        v = to_fix(num[pk]);
-        e = en[pk];
+        const float4 x = ne[pk];
+        v = to_fix(make_float2(x.x, x.y));
+        e = make_float2(x.z, x.w);
       }
       // the run open at the end of the last round continues in lane 0's segment
       if (lane == 0 && open && !head) {
@@ -694,16 +716,19 @@ __global__ void __launch_bounds__(kPtRedThreads) k_pt_reduce(const uint64_t* __r
       // does the run of this lane end here? (next position is a head or past the end)
       bool next_head = __shfl_down_sync(kFull, (int)head, 1) != 0;
       if (lane == 31) next_head = (q + 1 >= m) || is_head(q + 1);
-      if (valid && (q + 1 >= m || next_head)) {
-        if (hp < t1) {
-          const double sn = from_fix(v);
-          const double de = -((double)e.x + (double)e.y);  // E0 - E_a
-          e2 += sn * sn / de;
-          const double t = sn / de;
-          psi += t * t;
-          cnt += 1.0;
-        }
+      // a finished run waits in the warp's queue, evaluated 32 at a time
+      // (the FP64 tail costs a full-warp issue however few lanes take part)
+      const bool fin = valid && (q + 1 >= m || next_head) && hp < t1;
+      const unsigned fm = __ballot_sync(kFull, fin);
+      if (fin) {
+        const unsigned slot = (qh + qn + __popc(fm & lt)) & 63u;
+        qlo[slot] = (unsigned long long)v;
+        qhi[slot] = (long long)(v >> 64);
+        qe[slot] = e;
       }
+      qn += __popc(fm);
+      __syncwarp();
+      if (qn >= 32) flush(32);
       // carry lane 31's run when it continues into the next round
       const bool cont = __shfl_sync(kFull, (int)(valid && !(q + 1 >= m || next_head)), 31) != 0;
       cs = shfl_i128(v, 31);
@@ -713,6 +738,7 @@ __global__ void __launch_bounds__(kPtRedThreads) k_pt_reduce(const uint64_t* __r
       if (!open && b + 32 >= t1) break;
     }
   }
+  while (qn > 0) flush(qn < 32 ? qn : 32);
   __shared__ double r0[kPtRedThreads / 32], r1[kPtRedThreads / 32], r2[kPtRedThreads / 32];
   for (int o = 16; o; o >>= 1) {
     e2 += __shfl_xor_sync(kFull, e2, o);
@@ -796,7 +822,7 @@ PtResult pt_deterministic(const Det2* dets, size_t n, const double* c, double E0
     size_t avail = fr;
     if (g_alloc_cap) avail = std::min(avail, g_alloc_cap > g_alloc_live ? g_alloc_cap - g_alloc_live : (size_t)0);
     // what the buffers already hold counts as available to them
-    avail += (w.key0.cap + w.key1.cap) * sizeof(uint64_t) + (w.num.cap + w.en.cap) * sizeof(float2) +
+    avail += (w.key0.cap + w.key1.cap) * sizeof(uint64_t) + w.ne.cap * sizeof(float4) +
              w.perm.cap * sizeof(uint32_t);
     cap = (int64_t)(avail / 4 * 3 / kPtBytesPerCand);
   }
@@ -807,15 +833,13 @@ PtResult pt_deterministic(const Det2* dets, size_t n, const double* c, double E0
   auto gen = [&](uint32_t nparts, uint32_t part, int64_t room) -> int64_t {
     w.key0.reserve((size_t)room);
     w.key1.reserve((size_t)room);
-    w.num.reserve((size_t)room);
-    w.en.reserve((size_t)room);
+    w.ne.reserve((size_t)room);
     a.nparts = nparts;
     a.part = part;
     a.cap = room;
     a.key0 = w.key0.p;
     a.key1 = w.key1.p;
-    a.num = w.num.p;
-    a.en = w.en.p;
+    a.ne = w.ne.p;
     SHCI_CUDA(cudaMemsetAsync(w.next.p, 0, 2 * sizeof(unsigned long long), s));
     k_pt_gen<<<kPtGenBlocks, kPtThreads, gsmem, s>>>(a);
     SHCI_LAUNCH_CHECK();
@@ -831,7 +855,7 @@ PtResult pt_deterministic(const Det2* dets, size_t n, const double* c, double E0
     SHCI_LAUNCH_CHECK();
     sort_u128(w.key0.p, w.key1.p, w.perm.p, (size_t)m, pr, s);
     pt.mark("pt sort");
-    k_pt_reduce<<<kPtRedBlocks, kPtRedThreads, 0, s>>>(w.key0.p, w.key1.p, w.perm.p, w.num.p, w.en.p, (size_t)m,
+    k_pt_reduce<<<kPtRedBlocks, kPtRedThreads, 0, s>>>(w.key0.p, w.key1.p, w.perm.p, w.ne.p, (size_t)m,
                                                        w.part.p);
     SHCI_LAUNCH_CHECK();
     std::vector<double> hp(3 * kPtRedBlocks);
