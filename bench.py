@@ -191,11 +191,14 @@ def pt_section(e, E0, steps, cpu_leg, fcidump, eps2=PT_EPS2, warmup=1):
     ci = e.run_ci(1)[0]
     for _ in range(max(1, warmup)):
         e.pt_deterministic(ci, E0, eps2)  # warm-up: allocations
+    import torch
     ts = []
+    torch.cuda.nvtx.range_push("bench_pt")  # lets a profiler select exactly these launches
     for _ in range(max(2, steps // 4)):
         t0 = time.perf_counter()
         e2 = e.pt_deterministic(ci, E0, eps2)
         ts.append(time.perf_counter() - t0)
+    torch.cuda.nvtx.range_pop()
     st = e.pt_stats()
     t = statistics.mean(ts)
     out = {"eps2": eps2, "ndets": len(ci), "E_var": E0, "E2": e2, "E_total": E0 + e2, "candidates": st["candidates"],
