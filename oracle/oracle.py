@@ -77,6 +77,9 @@ def lib():
         L.orc_pt_det.argtypes = [vp, vp, i64, vp, dbl, dbl, vp, i32]
         L.orc_pt_det_range.restype = dbl
         L.orc_pt_det_range.argtypes = [vp, vp, i64, vp, dbl, dbl, i64, i64]
+        L.orc_rdm.argtypes = [vp, vp, i64, vp, vp, vp]
+        L.orc_rdm_energy.restype = dbl
+        L.orc_rdm_energy.argtypes = [vp, vp]
         L.orc_var_pt.restype = dbl
         L.orc_var_pt.argtypes = [vp, i32, dbl]
         L.orc_input_epsilon2.restype = dbl
@@ -194,6 +197,22 @@ class Oracle:
         ci = np.ascontiguousarray(ci, dtype=np.float64)
         e2 = lib().orc_pt_det_range(self.h, _p(dets), len(dets), _p(ci), E0, eps2, p0, p1)
         return e2, _pt_stats(self.h)
+
+    def rdm(self, dets, ci):
+        """Spatial 2-RDM as an (n, n, n, n) array with [p, q, r, s] = the
+        reference's s2RDM(p n + q, r n + s), and the spatial 1-RDM (n, n)."""
+        dets = np.ascontiguousarray(dets, dtype=np.uint64)
+        ci = np.ascontiguousarray(ci, dtype=np.float64)
+        n = self.norb
+        s2 = np.zeros((n, n, n, n))
+        s1 = np.zeros((n, n))
+        lib().orc_rdm(self.h, _p(dets), len(dets), _p(ci), _p(s2), _p(s1))
+        return s2, s1
+
+    def rdm_energy(self, s2):
+        """Energy (core energy included) from a spatial 2-RDM."""
+        s2 = np.ascontiguousarray(s2, dtype=np.float64)
+        return lib().orc_rdm_energy(self.h, _p(s2))
 
     def ham(self, dets):
         """Lower-triangle CSR as the reference's SparseHam holds it: row I is

@@ -767,6 +767,115 @@ static void build_ham(const Ints& I, const Det* dets, size_t N, SparseHam& H) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Reduced density matrices of the variational wavefunction
+// ---------------------------------------------------------------------------
+// SHCIrdm::populateSpatialRDM (SHCI/SHCIrdm.cpp:846-861): s2 is the n^2 x n^2
+// spatial 2-RDM, element (I n + J, K n + L) at (I n + J) n^2 + K n + L.
+static void populate_spatial(std::vector<double>& s2, int n, int i, int j, int k, int l, double v) {
+  const size_t n2 = (size_t)n * n;
+  const int I = i / 2, J = j / 2, K = k / 2, L = l / 2;
+  if (i % 2 == l % 2 && j % 2 == k % 2) {
+    s2[(size_t)(I * n + J) * n2 + L * n + K] -= v;
+    s2[(size_t)(J * n + I) * n2 + K * n + L] -= v;
+  }
+  if (i % 2 == k % 2 && l % 2 == j % 2) {
+    s2[(size_t)(I * n + J) * n2 + K * n + L] += v;
+    s2[(size_t)(J * n + I) * n2 + L * n + K] += v;
+  }
+}
+
+// getOrbDiff(bra, ket) (SHCI/Determinants.cpp:508-560): spin orbitals created
+// (occupied in bra only) and destroyed (in ket only), each ascending.
+static int orb_diff(const Det& bra, const Det& ket, int* cre, int* des) {
+  int nc = 0, nd = 0;
+  for (int w = 0; w < W; ++w) {
+    uint64_t u = bra.w[w] ^ ket.w[w];
+    uint64_t b = u & bra.w[w], k = u & ket.w[w];
+    while (b) {
+      if (nc < 2) cre[nc] = __builtin_ctzll(b) + 64 * w;
+      ++nc;
+      b &= b - 1;
+    }
+    while (k) {
+      if (nd < 2) des[nd] = __builtin_ctzll(k) + 64 * w;
+      ++nd;
+      k &= k - 1;
+    }
+  }
+  return nc;
+}
+
+// SHCIrdm::EvaluateRDM (SHCI/SHCIrdm.cpp:863-993) and EvaluateOneRDM
+// (:996-1100) with cibra = ciket = c, over the connection lists of the
+// variational Hamiltonian (row i: the diagonal, then every connected J < i;
+// orbital differences of getOrbDiff(Dets[J], Dets[i]), as the build stores
+// them at SHCI/SHCImakeHamiltonian.cpp:578-588). s1 is the n x n spatial 1-RDM.
+static void evaluate_rdm(const Ints& I, const Det* dets, const SparseHam& H, size_t N, const double* c,
+                         std::vector<double>& s2, std::vector<double>& s1) {
+  const int n = I.norb, nspin = 2 * n;
+  s2.assign((size_t)n * n * n * n, 0.0);
+  s1.assign((size_t)n * n, 0.0);
+  int closed[128];
+  for (size_t i = 0; i < N; i++) {
+    const int nelec = closed_list(dets[i], nspin, closed);
+    const double cii = c[i] * c[i];
+    for (int n1 = 0; n1 < nelec; n1++)
+      for (int n2 = 0; n2 < n1; n2++) populate_spatial(s2, n, closed[n1], closed[n2], closed[n1], closed[n2], cii);
+    for (int n1 = 0; n1 < nelec; n1++) s1[(size_t)(closed[n1] / 2) * n + closed[n1] / 2] += cii;
+    for (int64_t p = H.rowptr[i] + 1; p < H.rowptr[i + 1]; ++p) {
+      const int J = H.col[p];
+      int cre[2], des[2];
+      const int nc = orb_diff(dets[J], dets[i], cre, des);
+      const double w = c[J] * c[i];
+      if (nc == 1) {
+        const int c0 = cre[0], d0 = des[0];
+        const double sgn0 = parity_between(dets[i], std::min(d0, c0), std::max(d0, c0));
+        for (int n1 = 0; n1 < nelec; n1++) {
+          const int k = closed[n1];
+          if (k == d0 || k == c0) continue;
+          const int a = std::max(k, c0), b = std::min(k, c0), II = std::max(k, d0), JJ = std::min(k, d0);
+          double sgn = sgn0;
+          if (!((k > c0 && k > d0) || (k < c0 && k < d0))) sgn *= -1.;
+          populate_spatial(s2, n, a, b, II, JJ, sgn * w);
+          populate_spatial(s2, n, II, JJ, a, b, sgn * w);
+        }
+        s1[(size_t)(c0 / 2) * n + d0 / 2] += sgn0 * w;
+        s1[(size_t)(d0 / 2) * n + c0 / 2] += sgn0 * w;
+      } else if (nc == 2) {
+        const int c0 = cre[0], c1 = cre[1], d0 = des[0], d1 = des[1];
+        // Determinant::parity(d1, d0, c1, c0, sgn) (SHCI/Determinants.cpp:332-357)
+        Det t = dets[i];
+        double sgn = parity_between(t, std::min(d1, c1), std::max(d1, c1));
+        setocc(t, d1, false);
+        setocc(t, c1, true);
+        sgn *= parity_between(t, std::min(d0, c0), std::max(d0, c0));
+        populate_spatial(s2, n, c1, c0, d1, d0, sgn * w);
+        populate_spatial(s2, n, d1, d0, c1, c0, sgn * w);
+      }
+    }
+  }
+}
+
+// SHCIrdm::ComputeEnergyFromSpatialRDM (SHCI/SHCIrdm.cpp:1188-1245).
+static double rdm_energy(const Ints& I, const std::vector<double>& s2, int nelec) {
+  const int n = I.norb;
+  const size_t n2 = (size_t)n * n;
+  std::vector<double> one(n2, 0.0);
+  for (int p = 0; p < n; p++)
+    for (int q = 0; q < n; q++)
+      for (int r = 0; r < n; r++) one[p * n + q] += s2[(size_t)(p * n + r) * n2 + q * n + r] / (1. * nelec - 1.);
+  double onebody = 0.0, twobody = 0.0;
+  for (int p = 0; p < n; p++)
+    for (int q = 0; q < n; q++) onebody += I.i1(2 * p, 2 * q) * one[p * n + q];
+  for (int p = 0; p < n; p++)
+    for (int q = 0; q < n; q++)
+      for (int r = 0; r < n; r++)
+        for (int s_ = 0; s_ < n; s_++)
+          twobody += 0.5 * s2[(size_t)(p * n + q) * n2 + r * n + s_] * I.i2(2 * p, 2 * r, 2 * q, 2 * s_);
+  return I.coreE + onebody + twobody;
+}
+
 // Hmult2::operator() (SHCI/Hmult.h:52-150), serial branch: symmetric
 // scatter from the lower triangle.
 static void sigma(const SparseHam& H, size_t N, const double* x, double* y) {
@@ -1362,6 +1471,22 @@ double orc_pt_det_range(orc_ctx* c, const uint64_t* dets, int64_t n, const doubl
                         int64_t p0, int64_t p1) {
   return pt_deterministic(c->ints, c->hb, (const Det*)dets, (size_t)n, ci, E0, eps2, {}, c->pt, (size_t)p0,
                           (size_t)p1);
+}
+
+// Spatial 2-RDM (n^4, element (p n + q, r n + s) at (p n + q) n^2 + r n + s)
+// and spatial 1-RDM (n^2) of the wavefunction c on the space `dets`.
+void orc_rdm(orc_ctx* c, const uint64_t* dets, int64_t n, const double* ci, double* s2, double* s1) {
+  SparseHam H;
+  build_ham(c->ints, (const Det*)dets, (size_t)n, H);
+  std::vector<double> a, b;
+  evaluate_rdm(c->ints, (const Det*)dets, H, (size_t)n, ci, a, b);
+  std::copy(a.begin(), a.end(), s2);
+  std::copy(b.begin(), b.end(), s1);
+}
+// Energy (coreE included) from a spatial 2-RDM.
+double orc_rdm_energy(orc_ctx* c, const double* s2) {
+  const size_t n4 = (size_t)c->ints.norb * c->ints.norb * c->ints.norb * c->ints.norb;
+  return rdm_energy(c->ints, std::vector<double>(s2, s2 + n4), c->ints.nelec);
 }
 
 // PT2 on the result of orc_run_input for one root, eps2 <= 0 taking the

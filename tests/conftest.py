@@ -1,5 +1,6 @@
 import gzip
 import os
+import re
 import shutil
 import sys
 
@@ -25,8 +26,9 @@ def golden_case(tmp_path, name, input_name):
         shutil.copyfileobj(f, g)
     src = os.path.join(GOLDEN, name + "." + input_name)
     text = open(src).read()
-    # inputs name their integral file relative to their own directory
-    text = text.replace("orbitals ./FCIDUMP", "orbitals FCIDUMP")
+    # inputs name their integral file relative to their own directory; the
+    # fixture's FCIDUMP sits beside the unpacked input
+    text = re.sub(r"(?im)^(\s*orbitals)\s+\S+", r"\1 FCIDUMP", text)
     with open(d / "input.dat", "w") as f:
         f.write(text)
     return str(d / "input.dat")

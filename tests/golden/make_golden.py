@@ -14,6 +14,10 @@ What is copied, and what it pins:
   * tests/SHCI/o2_det: FCIDUMP and input.dat (`deterministic`, epsilon2
     1e-7); trusted_hci.e holds E_var + E_PT2 of root 0 (runSmallTests.sh
     tolerance 1e-6).
+  * Reduced density matrices: tests/SHCI/H2He_rdm and tests/SHCI/h2co_rdm
+    (FCIDUMPs from tests/SHCI/integrals, inputs, PySCF FCI 1- and 2-RDMs,
+    runTests.sh tolerances on the error per element), tests/SHCI/o2_stoc
+    (input and the reference's own spatial 2-RDM, trusted2RDM.txt).
 FCIDUMPs are stored gzip-compressed. Energies and tables go to golden.json.
 """
 import gzip
@@ -100,6 +104,26 @@ def main(ref):
     shutil.copy(os.path.join(o2, "input.dat"), os.path.join(HERE, "o2.input.dat"))
     out["o2_det"] = {"E_total": read_e(os.path.join(o2, "trusted_hci.e")), "tol": 1e-6,
                      "source": "tests/SHCI/o2_det/trusted_hci.e (runSmallTests.sh tolerance 1e-6)"}
+
+    # reduced density matrices: PySCF FCI references (H2He, h2co) and the
+    # reference's own 2-RDM output (o2_stoc)
+    shci = os.path.join(ref, "tests", "SHCI")
+    gz(os.path.join(shci, "integrals", "H2H2_FCIDUMP_nosym"), os.path.join(HERE, "h2he_rdm.FCIDUMP.gz"))
+    shutil.copy(os.path.join(shci, "H2He_rdm", "input.dat"), os.path.join(HERE, "h2he_rdm.input.dat"))
+    gz(os.path.join(shci, "integrals", "h2co_FCIDUMP_nosymm"), os.path.join(HERE, "h2co_rdm.FCIDUMP.gz"))
+    shutil.copy(os.path.join(shci, "h2co_rdm", "test_input.dat"), os.path.join(HERE, "h2co_rdm.input.dat"))
+    rdm = {}
+    for name, sub in (("h2he_rdm", "H2He_rdm"), ("h2co_rdm", "h2co_rdm")):
+        arrays = {k: np.load(os.path.join(shci, sub, "pyscf_%s.npy" % k)) for k in ("1RDM", "2RDM")}
+        np.savez_compressed(os.path.join(HERE, name + "_pyscf.npz"), **arrays)
+        rdm[name] = {"source": "tests/SHCI/%s/pyscf_1RDM.npy, pyscf_2RDM.npy" % sub}
+    rdm["h2he_rdm"]["tol"] = {"1RDM": 1e-9, "2RDM": 1e-9}
+    rdm["h2co_rdm"]["tol"] = {"1RDM": 1e-8, "2RDM": 1e-9}
+    gz(os.path.join(o2, "FCIDUMP"), os.path.join(HERE, "o2_stoc.FCIDUMP.gz"))
+    shutil.copy(os.path.join(shci, "o2_stoc", "input.dat"), os.path.join(HERE, "o2_stoc.input.dat"))
+    shutil.copy(os.path.join(shci, "o2_stoc", "trusted2RDM.txt"), os.path.join(HERE, "o2_stoc.trusted2RDM.txt"))
+    rdm["o2_stoc"] = {"source": "tests/SHCI/o2_stoc/trusted2RDM.txt", "tol": {"2RDM": 1e-8}}
+    out["rdm"] = rdm
 
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump(out, f, indent=1)

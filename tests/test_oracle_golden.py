@@ -199,3 +199,56 @@ def test_pt_matches_brute_force_second_order(tmp_path):
     e2b, stb = run.pt(0, 1e-6)
     assert stb["candidates"] < st["candidates"]
     assert abs(e2b - brute) < 1e-4 * abs(brute)
+
+
+# ---------------------------------------------------------------------------
+# Reduced density matrices of the variational wavefunction
+# ---------------------------------------------------------------------------
+def _read_dice_2rdm(path):
+    """The reference's spatialRDM text format: a line with n, then
+    `p q r s value` for the nonzero elements (tests/SHCI/rdm_utilities.py)."""
+    lines = open(path).read().split("\n")
+    n = int(lines[0].split()[0])
+    out = np.zeros((n,) * 4)
+    for ln in lines[1:]:
+        f = ln.split()
+        if len(f) == 5:
+            out[int(f[0]), int(f[1]), int(f[2]), int(f[3])] = float(f[4])
+    return out
+
+
+def _err_per_element(a, b):
+    # tests/SHCI/test_twopdm.py: L2 norm of the difference over the element count
+    return np.linalg.norm(a - b) / a.size
+
+
+@pytest.mark.parametrize("name", ["h2he_rdm", "h2co_rdm"])
+def test_rdms_match_pyscf_fci(golden, name):
+    """tests/SHCI/H2He_rdm (eps1 1e-10) and tests/SHCI/h2co_rdm (eps1 0, the
+    full CI space): spatial 1- and 2-RDMs of the variational wavefunction
+    against PySCF's FCI ones, at the reference's test tolerances (PySCF's
+    2-RDM is compared through transpose(0, 2, 1, 3), as test_twopdm.py
+    does); the energy from the 2-RDM reproduces E_var."""
+    run = orc.run_input(golden(name, "input.dat"))
+    s2, s1 = run.oracle.rdm(run.dets, run.ci[0])
+    ref = np.load(os.path.join(GOLDEN, name + "_pyscf.npz"))
+    tol = G["rdm"][name]["tol"]
+    e1 = _err_per_element(s1, ref["1RDM"])
+    e2 = _err_per_element(s2, ref["2RDM"].transpose(0, 2, 1, 3))
+    print(name, len(run.dets), "1RDM", e1, "2RDM", e2)
+    assert e1 < tol["1RDM"] and e2 < tol["2RDM"]
+    assert abs(np.trace(s1) - run.oracle.nelec) < 1e-10
+    assert abs(run.oracle.rdm_energy(s2) - run.E[0]) < 1e-9
+
+
+def test_o2_stoc_2rdm_matches_trusted(golden):
+    """tests/SHCI/o2_stoc: the reference's own spatial 2-RDM output of the
+    variational wavefunction (its stochastic PT leaves the RDM variational),
+    at its 1e-8 error-per-element tolerance."""
+    run = orc.run_input(golden("o2_stoc", "input.dat"))
+    s2, _ = run.oracle.rdm(run.dets, run.ci[0])
+    ref = _read_dice_2rdm(os.path.join(GOLDEN, "o2_stoc.trusted2RDM.txt"))
+    err = _err_per_element(s2, ref)
+    print("o2_stoc", len(run.dets), err, np.abs(s2 - ref).max())
+    assert err < G["rdm"]["o2_stoc"]["tol"]["2RDM"]
+    assert abs(run.oracle.rdm_energy(s2) - run.E[0]) < 1e-9
