@@ -17,8 +17,8 @@ OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libshci_gpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["kernels_core.cu", "kernels_ham.cu", "kernels_select.cu", "kernels_sigma.cu", "kernels_mlp.cu", "kernels_pt.cu",
-                "engine.cu"]
+CUDA_SOURCES = ["kernels_core.cu", "kernels_ham.cu", "kernels_select.cu", "kernels_sigma.cu", "kernels_mlp.cu",
+                "kernels_pt.cu", "kernels_rdm.cu", "engine.cu"]
 CXX_SOURCES = ["host_io.cpp"]
 
 

@@ -213,6 +213,11 @@ struct Context {
   double t_pt = 0;
   DevBuf<double> ptc;  // coefficients passed from the host
 
+  // reduced density matrices
+  DevBuf<unsigned long long> rdm_fix;
+  DevBuf<double> rdm_out;
+  double t_rdm = 0;
+
   // run state
   DevBuf<double> ci, cmax;
   int nroots_run = 0;
@@ -429,6 +434,24 @@ struct Context {
   }
 
   static bool is_direct(int m) { return m == SHCI_MODE_DIRECT || m == SHCI_MODE_DIRECT_MIXED; }
+
+  // Spatial 2-RDM (n^4) and 1-RDM (n^2) of the wavefunction c (device, ndet
+  // entries) to the host (either may be null), over the connection lists of
+  // the stored Hamiltonian (built in the mixed form when the current one is
+  // matrix-free or stale, as the reference rebuilds helpers for its RDM after
+  // a matrix-free Davidson, SHCI/SHCIbasics.cpp:1274-1283).
+  void rdm(const double* c, double* s2, double* s1) {
+    require_ints();
+    require_dets();
+    const double t0 = now_s();
+    if (!ham_ok || is_direct(ham_mode)) build_ham(SHCI_MODE_MIXED);
+    const size_t n = (size_t)hints.norb, n2 = n * n, n4 = n2 * n2;
+    rdm_evaluate(dets.p, c, ndet, H, hints.norb, rdm_fix, rdm_out, stream);
+    if (s2) SHCI_CUDA(cudaMemcpyAsync(s2, rdm_out.p, n4 * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    if (s1) SHCI_CUDA(cudaMemcpyAsync(s1, rdm_out.p + n4, n2 * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    SHCI_CUDA(cudaStreamSynchronize(stream));
+    t_rdm = now_s() - t0;
+  }
 
   // Deterministic PT2 of the current space with coefficients c (device, ndet
   // entries); E0 includes coreE, as in SHCIbasics::DoPerturbativeDeterministic
@@ -1557,6 +1580,34 @@ int shci_run_pt(shci_ctx* ctx, double eps2, double* E, int cap_roots, int* nroot
       const double e2 = c.perturb(c.ci.p + (size_t)r * c.ndet, c.Evar[r], eps2);
       if (E && r < cap_roots) E[r] = c.Evar[r] + e2;
     }
+  });
+}
+
+int shci_ints_info(shci_ctx* ctx, int* norb, int* nelec, double* coreE) {
+  return guarded(ctx, [&](Context& c) {
+    c.require_ints();
+    if (norb) *norb = c.hints.norb;
+    if (nelec) *nelec = c.hints.nelec;
+    if (coreE) *coreE = c.hints.coreE;
+  });
+}
+
+int shci_rdm(shci_ctx* ctx, const double* ci, double* s2, double* s1) {
+  return guarded(ctx, [&](Context& c) {
+    if (!ci) throw Error(SHCI_ERR_INVALID, "null coefficients");
+    c.require_dets();
+    c.ptc.resize(c.ndet);
+    SHCI_CUDA(cudaMemcpyAsync(c.ptc.p, ci, c.ndet * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    c.rdm(c.ptc.p, s2, s1);
+  });
+}
+
+int shci_run_rdm(shci_ctx* ctx, int root, double* s2, double* s1) {
+  return guarded(ctx, [&](Context& c) {
+    if (c.Evar.empty() || c.nroots_run != (int)c.Evar.size())
+      throw Error(SHCI_ERR_STATE, "no variational run (call shci_run_input first)");
+    if (root < 0 || root >= c.nroots_run) throw Error(SHCI_ERR_INVALID, "root out of range");
+    c.rdm(c.ci.p + (size_t)root * c.ndet, s2, s1);
   });
 }
 

@@ -192,6 +192,13 @@ PtResult pt_deterministic(const Det2* dets, size_t n, const double* c, double E0
                           const HeatBathView& hb, double maxEntry, const SelectParams& sp, const DetHash& present,
                           int64_t max_candidates, PtWork& w, Prims& pr, cudaStream_t s);
 
+// ---- reduced density matrices (kernels_rdm.cu) ------------------------------
+// Spatial 2-RDM (out[0, n^4): element (p n + q, r n + s) at (p n + q) n^2 + r n + s)
+// and spatial 1-RDM (out[n^4, n^4 + n^2)) of the wavefunction c over the
+// connection lists of the stored Hamiltonian H of the space `dets`.
+void rdm_evaluate(const Det2* dets, const double* c, size_t N, const Csr& H, int n, DevBuf<unsigned long long>& fix,
+                  DevBuf<double>& out, cudaStream_t s);
+
 // ---- sigma and Davidson vector kernels (kernels_sigma.cu) -------------------
 // Y[:, c] (column-major, leading dimension ldy) = diag .* X[:, c] + Hoff X[:, c]
 // for c < k, where X is row-interleaved [N][kp] in the path's precision.

@@ -65,10 +65,32 @@ SIGNATURES = [
     ("shci_run_pt", _i32, [_vp, _dbl, _vp, _i32, _P(_i32)]),
     ("shci_pt_stats", _i32, [_vp, _P(_i64), _P(_i64), _P(_i32), _P(_dbl), _P(_dbl)]),
     ("shci_set_pt_batch", _i32, [_vp, _i64]),
+    ("shci_ints_info", _i32, [_vp, _P(_i32), _P(_i32), _P(_dbl)]),
+    ("shci_rdm", _i32, [_vp, _vp, _vp, _vp]),
+    ("shci_run_rdm", _i32, [_vp, _i32, _vp, _vp]),
     ("shci_launch_count", _i32, [_vp, _P(_i64)]),
 ]
 
 _lib = None
+
+
+def write_spatial_rdm(path, s2):
+    """The reference's spatialRDM text format (SHCI/SHCIrdm.cpp:478-510):
+    n, then `p q r s value` for |value| > 1e-15."""
+    n = s2.shape[0]
+    with open(path, "w") as f:
+        f.write("%d\n" % n)
+        for idx in zip(*np.nonzero(np.abs(s2) > 1e-15)):
+            f.write("%3d   %3d   %3d   %3d   %16.12g\n" % (tuple(int(i) for i in idx) + (s2[idx],)))
+
+
+def write_spatial_1rdm(path, s1):
+    """The reference's spatial1RDM text format (SHCI/SHCIrdm.cpp:356-385)."""
+    n = s1.shape[0]
+    with open(path, "w") as f:
+        f.write("%d\n" % n)
+        for idx in zip(*np.nonzero(np.abs(s1) > 1e-15)):
+            f.write("%3d   %3d   %16.12g\n" % (tuple(int(i) for i in idx) + (s1[idx],)))
 
 
 def load_library(path=LIB_PATH):
@@ -289,6 +311,9 @@ class Engine:
         self._check(load_library().shci_run_input(self.h, os.fspath(path).encode(),
                                                   fcidump.encode() if fcidump else None, m, b, _p(E), 16,
                                                   ctypes.byref(nr)))
+        n, e, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        self._check(load_library().shci_ints_info(self.h, ctypes.byref(n), ctypes.byref(e), ctypes.byref(c)))
+        self.norb, self.nelec, self.coreE = n.value, e.value, c.value
         return E[: nr.value].copy()
 
     def run_log(self):
@@ -407,6 +432,23 @@ class Engine:
 
     def set_pt_batch(self, max_candidates):
         self._check(load_library().shci_set_pt_batch(self.h, int(max_candidates)))
+
+    def rdm(self, ci=None, root=0):
+        """Spatial 2-RDM (norb, norb, norb, norb) with [p, q, r, s] =
+        s2RDM(p n + q, r n + s) and spatial 1-RDM (norb, norb) of host
+        coefficients ci on the current space, or of root `root` of the last
+        run_input when ci is None."""
+        n = self.norb
+        s2 = np.zeros((n, n, n, n))
+        s1 = np.zeros((n, n))
+        if ci is None:
+            self._check(load_library().shci_run_rdm(self.h, int(root), _p(s2), _p(s1)))
+        else:
+            c = np.ascontiguousarray(ci, dtype=np.float64)
+            if c.shape != (self.ndets(),):
+                raise ValueError("ci must hold one coefficient per determinant")
+            self._check(load_library().shci_rdm(self.h, _p(c), _p(s2), _p(s1)))
+        return s2, s1
 
     def launch_count(self):
         n = ctypes.c_int64()

@@ -61,6 +61,9 @@ int shci_set_alloc_cap(shci_ctx* ctx, uint64_t bytes);
  * twoIntHeatBathSHM::constructClass (SHCI/integral.h:125-153,
  * SHCI/integral.cpp:228-389). Builds the heat-bath tables as well. */
 int shci_read_fcidump(shci_ctx* ctx, const char* path, int* norb, int* nelec, double* coreE);
+/* Header values of the integrals the context holds (after shci_read_fcidump
+ * or shci_run_input); any pointer may be NULL. */
+int shci_ints_info(shci_ctx* ctx, int* norb, int* nelec, double* coreE);
 
 /* Host-only parsers (no context, no device): the same readers the context
  * calls, for drivers that validate their inputs before touching a GPU. On
@@ -219,6 +222,22 @@ int shci_run_pt(shci_ctx* ctx, double eps2, double* E, int cap_roots, int* nroot
 int shci_pt_stats(shci_ctx* ctx, int64_t* candidates, int64_t* unique, int* partitions, double* psi1_norm,
                   double* seconds);
 int shci_set_pt_batch(shci_ctx* ctx, int64_t max_candidates);
+
+/* Spatial reduced density matrices of the variational wavefunction.
+ * Replace SHCIrdm::EvaluateRDM (SHCI/SHCIrdm.cpp:863-993) and
+ * SHCIrdm::EvaluateOneRDM (:996-1100) as DoVariational calls them for
+ * DoRDM / DoOneRDM (SHCI/SHCIbasics.cpp:1236-1341), bra = ket.
+ * shci_rdm: ci = host coefficients of the current space (order of
+ *   shci_dets_get); s2 (NORB^4 doubles, may be NULL) receives s2RDM with
+ *   element (p NORB + q, r NORB + s) at (p NORB + q) NORB^2 + r NORB + s, the
+ *   reference's spatialRDM.i.i.txt values; s1 (NORB^2, may be NULL) the
+ *   spatial 1-RDM, row-major (spatial1RDM.i.i.txt). The connection lists of
+ *   the stored Hamiltonian are used (built in the mixed form when the
+ *   current one is matrix-free or missing). Sums are kept in 64-bit fixed
+ *   point (2^-58) with integer atomics: bitwise reproducible.
+ * shci_run_rdm: the same for root `root` of the last shci_run_input. */
+int shci_rdm(shci_ctx* ctx, const double* ci, double* s2, double* s1);
+int shci_run_rdm(shci_ctx* ctx, int root, double* s2, double* s1);
 
 /* Stage timings of the last run in seconds: selection, Hamiltonian build,
  * Davidson, total; and the sigma calls/time spent inside Davidson. */
