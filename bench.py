@@ -13,6 +13,11 @@ vectors. e2e: the same through the C-ABI call with host buffers
 timed region). Extra keys report the variational wall time and E_var of
 both paths.
 
+Further keys: `pt` (deterministic PT2 of the final space, eps2 1e-5, through
+shci_pt_deterministic; `--section pt` times it alone), `rdm` (spatial 1- and
+2-RDMs of the final space through shci_run_rdm), each with the CPU oracle on a
+bounded sample beside it, and `configs` (the other synthetic workloads).
+
 --impl reference: the CPU oracle (a restatement of Dice's serial C++; Dice
 itself needs Boost and MPI, absent here) timed on a bounded sample of the
 same workload.
@@ -227,6 +232,40 @@ def pt_section(e, E0, steps, cpu_leg, fcidump, eps2=PT_EPS2, warmup=1):
     return out
 
 
+def rdm_section(e, nnz_offdiag, cpu):
+    """Spatial 1- and 2-RDMs of root 0 on the final space through the C-ABI
+    (shci_run_rdm, results copied to the host): connected pairs J < I per
+    second. CPU leg: the oracle's restatement of EvaluateRDM + EvaluateOneRDM
+    on its stored connection lists of the sigma sample."""
+    import torch
+    e.rdm()  # warm-up
+    ts = []
+    torch.cuda.nvtx.range_push("bench_rdm")
+    for _ in range(3):
+        t0 = time.perf_counter()
+        s2, s1 = e.rdm()
+        ts.append(time.perf_counter() - t0)
+    torch.cuda.nvtx.range_pop()
+    t = statistics.mean(ts)
+    conn = nnz_offdiag // 2
+    out = {"what": "shci_run_rdm on the final mixed-precision space (the reference's EvaluateRDM + "
+                   "EvaluateOneRDM): fixed-point integer atomics over the stored connection lists",
+           "n_dets": e.ndets(), "connections": conn, "seconds": t, "Gconn_s": conn / t / 1e9,
+           "trace_1rdm": float(np.trace(s1))}
+    if cpu is not None:
+        o, n, nnz_lower = cpu
+        x = np.random.default_rng(3).standard_normal(n)
+        x /= np.linalg.norm(x)
+        t0 = time.perf_counter()
+        o.rdm_on_ham(x)
+        tc = time.perf_counter() - t0
+        out["cpu_oracle"] = {"Gconn_s": (nnz_lower - n) / tc / 1e9, "cores": 1, "kind": "port", "seconds": tc,
+                             "sample": "first %d determinants of the eps1=1e-3 space, %d connected pairs"
+                                       % (n, nnz_lower - n)}
+        out["speedup_vs_cpu_oracle"] = out["Gconn_s"] / out["cpu_oracle"]["Gconn_s"]
+    return out
+
+
 def run_pt_only(args):
     """--section pt: the variational stage in the mixed path on the chosen
     case, then the perturbative stage timed alone (one JSON line)."""
@@ -398,10 +437,12 @@ def run_ours(args):
     ach64 = alg64 / statistics.mean(ts64) / 1e9
 
     cpu = None
+    cpu_rdm = None
     if rank == 0 and not args.no_cpu:
         from oracle import oracle as orc
         orc.build()
         o, dets, nnz_lower, t_build, _ = cpu_sample(work)
+        cpu_rdm = (o, len(dets), nnz_lower)
         tc = time_cpu_sigma(o, len(dets))
         cpu = {"value": len(dets) / statistics.mean(tc) / 1e6, "unit": "Mdets/s", "cores": 1, "kind": "port",
                "sample": "first %d determinants of the eps1=1e-3 space of the workload; serial FP64 symmetric-"
@@ -460,6 +501,7 @@ def run_ours(args):
         line["cpu_baseline"] = cpu
     line["pt"] = pt_section(e, float(E32[0]), args.steps, rank == 0 and not args.no_cpu,
                             os.path.join(os.path.dirname(inp), "FCIDUMP"))
+    line["rdm"] = rdm_section(e, nnz, cpu_rdm)
     e.close()
     if args.case == "full" and not args.no_configs:
         line["configs"] = other_configs(work, local)

@@ -78,6 +78,7 @@ def lib():
         L.orc_pt_det_range.restype = dbl
         L.orc_pt_det_range.argtypes = [vp, vp, i64, vp, dbl, dbl, i64, i64]
         L.orc_rdm.argtypes = [vp, vp, i64, vp, vp, vp]
+        L.orc_rdm_eval.argtypes = [vp, vp, vp, vp]
         L.orc_rdm_energy.restype = dbl
         L.orc_rdm_energy.argtypes = [vp, vp]
         L.orc_var_pt.restype = dbl
@@ -207,6 +208,16 @@ class Oracle:
         s2 = np.zeros((n, n, n, n))
         s1 = np.zeros((n, n))
         lib().orc_rdm(self.h, _p(dets), len(dets), _p(ci), _p(s2), _p(s1))
+        return s2, s1
+
+    def rdm_on_ham(self, ci):
+        """rdm() on the space of the last ham() call, without rebuilding the
+        connection lists."""
+        ci = np.ascontiguousarray(ci, dtype=np.float64)
+        n = self.norb
+        s2 = np.zeros((n, n, n, n))
+        s1 = np.zeros((n, n))
+        lib().orc_rdm_eval(self.h, _p(ci), _p(s2), _p(s1))
         return s2, s1
 
     def rdm_energy(self, s2):

@@ -1312,6 +1312,7 @@ struct orc_ctx {
   HeatBath hb;
   SparseHam ham;
   size_t ham_n = 0;
+  std::vector<Det> ham_dets;  // the space of the last orc_ham_build
   VarResult var;
   Schedule sched;
   PtStats pt;
@@ -1410,6 +1411,7 @@ int64_t orc_select(orc_ctx* c, const uint64_t* dets, int64_t n, const double* cm
 int64_t orc_ham_build(orc_ctx* c, const uint64_t* dets, int64_t n) {
   build_ham(c->ints, (const Det*)dets, (size_t)n, c->ham);
   c->ham_n = (size_t)n;
+  c->ham_dets.assign((const Det*)dets, (const Det*)dets + n);
   return (int64_t)c->ham.col.size();
 }
 void orc_ham_export(orc_ctx* c, int64_t* rowptr, int32_t* col, double* val) {
@@ -1480,6 +1482,14 @@ void orc_rdm(orc_ctx* c, const uint64_t* dets, int64_t n, const double* ci, doub
   build_ham(c->ints, (const Det*)dets, (size_t)n, H);
   std::vector<double> a, b;
   evaluate_rdm(c->ints, (const Det*)dets, H, (size_t)n, ci, a, b);
+  std::copy(a.begin(), a.end(), s2);
+  std::copy(b.begin(), b.end(), s1);
+}
+// The same on the space and connection lists of the last orc_ham_build
+// (the evaluation alone, for timing).
+void orc_rdm_eval(orc_ctx* c, const double* ci, double* s2, double* s1) {
+  std::vector<double> a, b;
+  evaluate_rdm(c->ints, c->ham_dets.data(), c->ham, c->ham_n, ci, a, b);
   std::copy(a.begin(), a.end(), s2);
   std::copy(b.begin(), b.end(), s1);
 }
