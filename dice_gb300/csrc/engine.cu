@@ -223,6 +223,8 @@ struct Context {
   int nroots_run = 0;
   std::vector<double> Evar;  // E_var per root of the last run, coreE included
   double run_eps2 = 1e-8;    // the last input's epsilon2
+  Schedule run_sched;        // the last input's PT settings
+  PtStochResult pts_last;    // last semistochastic PT
   std::vector<IterLog> log;
   double t_select = 0, t_ham = 0, t_dav = 0, t_total = 0, t_sigma = 0, t_mlp = 0;
   int64_t total_dav_iters = 0;
@@ -469,7 +471,30 @@ struct Context {
     pt_last = pt_deterministic(dets.p, ndet, c, E0 - hints.coreE, eps2, ints(), hb(), hints.maxEntry, psp, hash,
                                pt_max_cand, ptw, prims, stream);
     t_pt = now_s() - t0;
+    pts_last = PtStochResult();
     return pt_last.e2;
+  }
+
+  // Semistochastic PT2 (E0 with coreE) of the current space with
+  // coefficients c (device, ndet entries); restrictions as in perturb().
+  double perturb_stoch(const double* c, double E0, double eps2, double eps2L, int nsample, int max_iter,
+                       double target, uint64_t seed) {
+    require_ints();
+    require_dets();
+    const double t0 = now_s();
+    std::vector<double> ch(ndet);
+    SHCI_CUDA(cudaMemcpyAsync(ch.data(), c, ndet * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    SHCI_CUDA(cudaStreamSynchronize(stream));
+    hash.build(dets.p, ndet, stream);
+    SelectParams psp = sp;
+    psp.ncore = 0;
+    psp.nact = 1 << 30;
+    pts_last = pt_semistochastic(dets.p, ndet, c, ch, E0 - hints.coreE, eps2, eps2L, nsample, max_iter, target, seed,
+                                 ints(), hb(), hints.maxEntry, psp, hash, ptw, prims, stream);
+    pt_last = PtResult();
+    pt_last.candidates = pts_last.candidates;
+    t_pt = now_s() - t0;
+    return pts_last.e2;
   }
 
   void build_ham(int mode) {
@@ -1166,6 +1191,7 @@ struct Context {
     for (int r = 0; r < nroots; ++r) Eout[r] = E0[r] + hints.coreE;
     Evar = Eout;
     run_eps2 = s.epsilon2;
+    run_sched = s;
     t_total = now_s() - t0;
   }
 };
@@ -1575,11 +1601,44 @@ int shci_run_pt(shci_ctx* ctx, double eps2, double* E, int cap_roots, int* nroot
     if (c.Evar.empty() || c.nroots_run != (int)c.Evar.size())
       throw Error(SHCI_ERR_STATE, "no variational run to perturb (call shci_run_input first)");
     if (!(eps2 > 0.0)) eps2 = c.run_eps2;
+    const shci::Schedule& s = c.run_sched;
+    // the reference's choice of PT (SHCI/SHCI.cpp:707-760)
+    if (s.stochastic && s.sampleN == -1)
+      throw Error(SHCI_ERR_INVALID, "semistochastic PT needs sampleN (or `deterministic`)");
+    if (s.stochastic && s.sampleN < 2) throw Error(SHCI_ERR_INVALID, "sampleN must be at least 2");
     if (nroots) *nroots = (int)c.Evar.size();
     for (int r = 0; r < (int)c.Evar.size(); ++r) {
-      const double e2 = c.perturb(c.ci.p + (size_t)r * c.ndet, c.Evar[r], eps2);
+      const double* cr = c.ci.p + (size_t)r * c.ndet;
+      double e2 = 0.0;
+      if (!s.stochastic)
+        e2 = c.perturb(cr, c.Evar[r], eps2);
+      else if (s.nPTiter != 0)
+        e2 = c.perturb_stoch(cr, c.Evar[r], eps2, s.epsilon2Large, s.sampleN, s.nPTiter, s.targetError,
+                             s.seed >= 0 ? (uint64_t)s.seed + (uint64_t)r : (uint64_t)0x5eedu + (uint64_t)r);
       if (E && r < cap_roots) E[r] = c.Evar[r] + e2;
     }
+  });
+}
+
+int shci_pt_semistochastic(shci_ctx* ctx, const double* ci, double E0, double eps2, double eps2_large, int sample_n,
+                           int max_iter, double target_error, uint64_t seed, double* e2, double* stddev,
+                           int* iterations) {
+  return guarded(ctx, [&](Context& c) {
+    if (!ci || !e2) throw Error(SHCI_ERR_INVALID, "null argument");
+    c.require_dets();
+    c.ptc.resize(c.ndet);
+    SHCI_CUDA(cudaMemcpyAsync(c.ptc.p, ci, c.ndet * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    *e2 = c.perturb_stoch(c.ptc.p, E0, eps2, eps2_large, sample_n, max_iter, target_error, seed);
+    if (stddev) *stddev = c.pts_last.stddev;
+    if (iterations) *iterations = c.pts_last.iterations;
+  });
+}
+
+int shci_pt_error(shci_ctx* ctx, double* stddev, int* iterations, double* e_large) {
+  return guarded(ctx, [&](Context& c) {
+    if (stddev) *stddev = c.pts_last.stddev;
+    if (iterations) *iterations = c.pts_last.iterations;
+    if (e_large) *e_large = c.pts_last.e_large;
   });
 }
 

@@ -174,6 +174,7 @@ struct PtResult {
 struct PtWork {
   DevBuf<uint64_t> key0, key1;  // candidate determinants, word by word
   DevBuf<float4> ne;  // numerator and E_a - E0 of each candidate (float pairs)
+  DevBuf<float4> n2p;  // semistochastic mode: second numerator and the flag
   DevBuf<double> part;
   DevBuf<uint32_t> perm;
   DevBuf<unsigned long long> next;  // parent queue, candidate counter
@@ -198,6 +199,22 @@ PtResult pt_deterministic(const Det2* dets, size_t n, const double* c, double E0
 // connection lists of the stored Hamiltonian H of the space `dets`.
 void rdm_evaluate(const Det2* dets, const double* c, size_t N, const Csr& H, int n, DevBuf<unsigned long long>& fix,
                   DevBuf<double>& out, cudaStream_t s);
+
+struct PtStochResult {
+  double e2 = 0.0;       // mean of the iteration estimates
+  double stddev = 0.0;   // standard error of the mean (1e4 before the fifth iteration)
+  double e_large = 0.0;  // deterministic part at eps2L (0 when eps2L >= 999)
+  int iterations = 0;
+  int64_t candidates = 0;  // over all iterations
+};
+// Semistochastic PT2 (SHCIbasics::DoPerturbativeStochastic2SingleListDoubleEpsilon2AllTogether,
+// SHCI/SHCIbasics.cpp:55-451): c on the device and on the host (the alias
+// table and the draws are made on the host), E0 without the core energy.
+PtStochResult pt_semistochastic(const Det2* dets, size_t n, const double* c_dev, const std::vector<double>& c_host,
+                                double E0, double eps2, double eps2L, int nsample, int max_iter, double target,
+                                uint64_t seed, const IntsView& ints, const HeatBathView& hb, double maxEntry,
+                                const SelectParams& sp, const DetHash& present, PtWork& w, Prims& pr,
+                                cudaStream_t s);
 
 // ---- sigma and Davidson vector kernels (kernels_sigma.cu) -------------------
 // Y[:, c] (column-major, leading dimension ldy) = diag .* X[:, c] + Hoff X[:, c]

@@ -200,9 +200,9 @@ void build_heatbath(const HostInts& H, HostHeatBath& hb) {
 // Keywords accepted and ignored: they configure stages outside the
 // variational loop (perturbation theory, RDMs, I/O, restarts, SOC, cdfci).
 static const char* kIgnored[] = {
-    "epsilon2Large", "sampleN", "nPTiter", "targetError", "io", "noio", "prefix",
+    "io", "noio", "prefix",
     "printbestdeterminants", "printalldeterminants", "writebestdeterminants", "dordm", "DoOneRDM",
-    "DoSpinOneRDM", "dospinrdm", "TransitionRDM", "DoThreeRDM", "DoFourRDM", "seed", "outputlevel",
+    "DoSpinOneRDM", "dospinrdm", "TransitionRDM", "DoThreeRDM", "DoFourRDM", "outputlevel",
     "num_thrds", "nblocks", "excitation", "nvirt", "extrapolate", "relaxedRDM", "quasiq", "dosoc",
     "dosocqdpt", "dogtensor", "socmultiplier", "doresponse", "onlyperturbative", "algorithm", "dolcc",
     "pointGroup", "spin", "irrep", "searchForLowestEnergyDet", "cdfciTol", "cdfciIter", "cdfciOn",
@@ -305,6 +305,21 @@ void read_input(const std::string& path, Schedule& s) {
       s.epsilon2 = std::atof(tok[1].c_str());
     } else if (iequal(arg, "deterministic")) {
       s.stochastic = false;
+    } else if (iequal(arg, "epsilon2Large")) {
+      need(1);
+      s.epsilon2Large = std::atof(tok[1].c_str());
+    } else if (iequal(arg, "sampleN")) {
+      need(1);
+      s.sampleN = std::atoi(tok[1].c_str());
+    } else if (iequal(arg, "nPTiter")) {
+      need(1);
+      s.nPTiter = std::atoi(tok[1].c_str());
+    } else if (iequal(arg, "targetError")) {
+      need(1);
+      s.targetError = std::atof(tok[1].c_str());
+    } else if (iequal(arg, "seed")) {
+      need(1);
+      s.seed = std::atoll(tok[1].c_str());
     } else if (iequal(arg, "blockdavidson")) {
       s.block = true;
     } else if (iequal(arg, "precond")) {

@@ -46,6 +46,14 @@ struct Schedule {
   int basis_max = 0, basis_keep = 0;  // davidsonBasis keyword: 0 = the reference's subspace
   double epsilon2 = 1.e-8;  // PT threshold (SHCI/input.cpp:58)
   bool stochastic = true;   // `deterministic` clears it (SHCI/input.cpp:322-323)
+  // semistochastic PT (SHCI/input.cpp:59-86): threshold of its deterministic
+  // part, draws per iteration (-1: not set), iteration cap, target error,
+  // seed (-1: not set; the reference then seeds from the clock)
+  double epsilon2Large = 1000.0;
+  int sampleN = -1;
+  int nPTiter = 1000000;
+  double targetError = 1.e-4;
+  long long seed = -1;
 };
 
 void split_tokens(const std::string& in, const char* delims, std::vector<std::string>& tok);

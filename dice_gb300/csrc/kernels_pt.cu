@@ -41,6 +41,7 @@
 // reduced alone.
 #include <algorithm>
 #include <cmath>
+#include <random>
 
 #include "ham.h"
 
@@ -92,6 +93,14 @@ struct PtArgs {
   uint64_t* key1;  // high word
   float4* ne;   // numerator (x + y) and E_a - E0 (z + w), both float pairs
   float2 e0;    // E0 (without the core energy) as a float pair
+  // semistochastic mode (plist != null): the parents are plist[0, n) with
+  // weights pw; numerators use the weight, thresholds the coefficient, and
+  // n2p receives the second numerator (x + y) and the flag |H| > eps2L / |c| (z)
+  const int32_t* plist;
+  const double* pw;
+  double eps2L;
+  double nmcf;  // Nmc / (Nmc - 1)
+  float4* n2p;
 };
 
 __device__ __forceinline__ bool in_part(const PtArgs& a, const Det2& d) {
@@ -150,7 +159,8 @@ __device__ __forceinline__ float2 shfl_ff(float2 v, int src) {
 
 // Warp-aggregated append of the lanes with `keep`; slots past cap are counted
 // but not written.
-__device__ __forceinline__ void pt_put(const PtArgs& a, bool keep, const Det2& cand, float2 v, float2 e) {
+__device__ __forceinline__ void pt_put(const PtArgs& a, bool keep, const Det2& cand, float2 v, float2 e,
+                                       float2 v2 = make_float2(0.0f, 0.0f), bool present = false) {
   const int lane = threadIdx.x & 31;
   const unsigned m = __ballot_sync(kFull, keep);
   if (!m) return;
@@ -164,6 +174,7 @@ __device__ __forceinline__ void pt_put(const PtArgs& a, bool keep, const Det2& c
       a.key0[q] = cand.w0;
       a.key1[q] = cand.w1;
       a.ne[q] = make_float4(v.x, v.y, e.x, e.y);
+      if (a.n2p) a.n2p[q] = make_float4(v2.x, v2.y, present ? 1.0f : 0.0f, 0.0f);
     }
   }
 }
@@ -310,13 +321,19 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
     if (lane == 0) pp = atomicAdd(a.next, 1ull);
     pp = __shfl_sync(kFull, pp, 0);
     if (pp >= (unsigned long long)a.n) break;
-    const size_t p = (size_t)pp;
+    const size_t p = a.plist ? (size_t)a.plist[pp] : (size_t)pp;
     const Det2 d = a.dets[p];
     const double cp = a.c[p];
     const double eps = fabs(a.eps2 / cp);
     if (!(eps < INFINITY)) continue;  // c_i = 0: nothing passes either threshold
     const float eps_lo = __double2float_rd(eps), eps_hi = __double2float_ru(eps);
-    const float2 eps_ff = ff_of(eps), cp_ff = ff_of(cp);
+    // numerator factor: c_i, or the sample weight in the semistochastic mode
+    const double ci1 = a.plist ? a.pw[pp] : cp;
+    const float2 eps_ff = ff_of(eps), cp_ff = ff_of(ci1);
+    const bool stoch = a.plist != nullptr;
+    const double epsL = stoch ? fabs(a.eps2L / cp) : INFINITY;
+    const float epsL_f = __double2float_rd(epsL);
+    const float2 k_ff = ff_of(stoch ? ci1 * (ci1 * a.nmcf - cp) : 0.0);
     // occupied list (ascending) and per-spin electron / hole lists, by ballot
     const int nclosed = __popcll(d.w0) + __popcll(d.w1);
     const int ncA = __popcll(d.w0 & 0x5555555555555555ull) + __popcll(d.w1 & 0x5555555555555555ull);
@@ -390,9 +407,9 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
       __syncwarp();
     };
     auto drain = [&](unsigned cnt) {  // the first cnt (<= 32) entries
-      bool keep = false;
+      bool keep = false, present = false;
       Det2 cand = d;
-      float2 v = make_float2(0.0f, 0.0f), e = v;
+      float2 v = make_float2(0.0f, 0.0f), e = v, v2 = v;
       if ((unsigned)lane < cnt) {
         const unsigned slot = (qh + lane) & 63u;
         const uint32_t w = qo[slot];
@@ -412,6 +429,10 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
             keep = in_part(a, cand) && !hash_contains(a.hslots, a.hmask, a.dets, cand);
             if (keep) {
               v = ff_mul(H, cp_ff);
+              if (stoch) {
+                v2 = ff_mul(ff_mul(H, H), k_ff);
+                present = fabs((double)H.x + (double)H.y) > epsL;
+              }
               e = ff_sub(ff_add(ed, ff_sub(F[oa], F[oi])), vpair(sD, sX, n, oa, oi));
             }
           }
@@ -425,6 +446,11 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
           if (keep) {
             const float vf = qv[slot];
             v = ff_mul_f(pt_double_sign(cand, oa, ob, oi, oj) > 0.0 ? vf : -vf, cp_ff);
+            if (stoch) {
+              const float sq = __fmul_rn(vf, vf);
+              v2 = ff_mul(make_float2(sq, __fmaf_rn(vf, vf, -sq)), k_ff);
+              present = fabsf(vf) > epsL_f;  // (double)|v| > epsL exactly
+            }
             const float2 fa = ff_add(F[oa], F[ob]), fi = ff_add(F[oi], F[oj]);
             const float2 vin = ff_add(vpair(sD, sX, n, oi, oj), vpair(sD, sX, n, oa, ob));
             const float2 vx = ff_add(ff_add(vpair(sD, sX, n, oa, oi), vpair(sD, sX, n, oa, oj)),
@@ -433,7 +459,7 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
           }
         }
       }
-      pt_put(a, keep, cand, v, e);
+      pt_put(a, keep, cand, v, e, v2, present);
       qh = (qh + cnt) & 63u;
       qn -= cnt;
       __syncwarp();
@@ -764,17 +790,81 @@ __global__ void __launch_bounds__(kPtRedThreads) k_pt_reduce(const uint64_t* __r
   }
 }
 
+// Semistochastic estimate over the sorted candidates of one iteration, one
+// thread per run of equal determinants: with S1, S2 the sums of the two
+// numerators (and S1B, S2B over the contributions flagged as already held by
+// the deterministic part), eA = sum (S1^2 f - S2) / (E_a - E0) and eB likewise
+// (SHCI/SHCIbasics.cpp:271-363). Sums in fixed point as in k_pt_reduce; block
+// partials {eA, eB, runs} in part[3 * block].
+__global__ void __launch_bounds__(kPtRedThreads) k_pt_reduce_stoch(const uint64_t* __restrict__ k0,
+                                                                   const uint64_t* __restrict__ k1,
+                                                                   const uint32_t* __restrict__ perm,
+                                                                   const float4* __restrict__ ne,
+                                                                   const float4* __restrict__ n2p, size_t m, double f,
+                                                                   double* __restrict__ part) {
+  double eA = 0.0, eB = 0.0, cnt = 0.0;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < m; k += (size_t)gridDim.x * blockDim.x) {
+    const uint64_t d0 = k0[k], d1 = k1[k];
+    if (k > 0 && d0 == k0[k - 1] && d1 == k1[k - 1]) continue;
+    __int128 s1 = 0, s2 = 0, s1b = 0, s2b = 0;
+    float2 e = make_float2(INFINITY, 0.0f);
+    for (size_t j = k; j < m; ++j) {
+      if (j > k && (k0[j] != d0 || k1[j] != d1)) break;
+      const uint32_t pk = perm[j];
+      const float4 x = ne[pk], y = n2p[pk];
+      const __int128 f1 = to_fix(make_float2(x.x, x.y)), f2 = to_fix(make_float2(y.x, y.y));
+      s1 += f1;
+      s2 += f2;
+      if (y.z != 0.0f) {
+        s1b += f1;
+        s2b += f2;
+      }
+      const float2 ej = make_float2(x.z, x.w);
+      if (ff_less(ej, e)) e = ej;
+    }
+    const double de = (double)e.x + (double)e.y;  // E_a - E0
+    const double n1 = from_fix(s1), n1b = from_fix(s1b);
+    eA += (n1 * n1 * f - from_fix(s2)) / de;
+    eB += (n1b * n1b * f - from_fix(s2b)) / de;
+    cnt += 1.0;
+  }
+  __shared__ double r0[kPtRedThreads / 32], r1[kPtRedThreads / 32], r2[kPtRedThreads / 32];
+  for (int o = 16; o; o >>= 1) {
+    eA += __shfl_xor_sync(kFull, eA, o);
+    eB += __shfl_xor_sync(kFull, eB, o);
+    cnt += __shfl_xor_sync(kFull, cnt, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    r0[threadIdx.x >> 5] = eA;
+    r1[threadIdx.x >> 5] = eB;
+    r2[threadIdx.x >> 5] = cnt;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0, c = 0.0;
+    for (int w = 0; w < kPtRedThreads / 32; ++w) {
+      a += r0[w];
+      b += r1[w];
+      c += r2[w];
+    }
+    part[3 * blockIdx.x] = a;
+    part[3 * blockIdx.x + 1] = b;
+    part[3 * blockIdx.x + 2] = c;
+  }
+}
+
 }  // namespace
 
-PtResult pt_deterministic(const Det2* dets, size_t n, const double* c, double E0, double eps2, const IntsView& ints,
-                          const HeatBathView& hb, double maxEntry, const SelectParams& sp, const DetHash& present,
-                          int64_t max_candidates, PtWork& w, Prims& pr, cudaStream_t s) {
-  PtResult res;
-  if (n == 0) return res;
-  if (!(eps2 >= 0.0)) throw Error(kErrInvalid, "epsilon2 must be >= 0");
+namespace {
+
+// Fields of PtArgs shared by both modes; builds the dense integral tables on
+// first use. Returns the generator's dynamic shared memory size.
+size_t pt_prepare(PtArgs& a, const Det2* dets, size_t n, const double* c, double E0, double eps2,
+                  const IntsView& ints, const HeatBathView& hb, double maxEntry, const SelectParams& sp,
+                  const DetHash& present, PtWork& w, cudaStream_t s) {
   w.next.resize(2);
   w.part.resize(3 * kPtRedBlocks);
-  PtArgs a{};
+  a = PtArgs{};
   a.dets = dets;
   a.c = c;
   a.n = n;
@@ -787,6 +877,7 @@ PtResult pt_deterministic(const Det2* dets, size_t n, const double* c, double E0
   a.hmask = present.mask;
   a.next = w.next.p;
   a.counter = w.next.p + 1;
+  a.nparts = 1;
   if (w.tables_of != ints.I2 || w.tables_n != ints.norb) {
     const size_t nt = (size_t)ints.norb * ints.norb * ints.norb;
     w.coul.resize(nt);
@@ -804,15 +895,28 @@ PtResult pt_deterministic(const Det2* dets, size_t n, const double* c, double E0
   a.coul = w.coul.p;
   a.exch = w.exch.p;
   a.coul32 = w.coul32.p;
+  a.exch32 = w.exch32.p;
   a.coulff = w.coulff.p;
   a.exchff = w.exchff.p;
   {
     const float h = (float)E0;
     a.e0 = make_float2(h, (float)(E0 - (double)h));
   }
-  a.exch32 = w.exch32.p;
   const size_t gsmem = sizeof(float2) * (2 * ints.norb * ints.norb + 2 * ints.norb);
   SHCI_CUDA(cudaFuncSetAttribute(k_pt_gen, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsmem));
+  return gsmem;
+}
+
+}  // namespace
+
+PtResult pt_deterministic(const Det2* dets, size_t n, const double* c, double E0, double eps2, const IntsView& ints,
+                          const HeatBathView& hb, double maxEntry, const SelectParams& sp, const DetHash& present,
+                          int64_t max_candidates, PtWork& w, Prims& pr, cudaStream_t s) {
+  PtResult res;
+  if (n == 0) return res;
+  if (!(eps2 >= 0.0)) throw Error(kErrInvalid, "epsilon2 must be >= 0");
+  PtArgs a;
+  const size_t gsmem = pt_prepare(a, dets, n, c, E0, eps2, ints, hb, maxEntry, sp, present, w, s);
 
   // capacity of one partition
   int64_t cap = max_candidates;
@@ -903,6 +1007,150 @@ PtResult pt_deterministic(const Det2* dets, size_t n, const double* c, double E0
     nparts *= 2;
   }
   pt.mark("pt partitions");
+  return res;
+}
+
+// SHCIsampledeterminants::setUpAliasMethod (SHCI/SHCIsampledeterminants.cpp:64-88).
+static void alias_setup(const std::vector<double>& ci, double cumulative, std::vector<int>& alias,
+                        std::vector<double>& prob) {
+  const size_t N = ci.size();
+  alias.assign(N, 0);
+  prob.assign(N, 0.0);
+  std::vector<int> larger, smaller;
+  for (size_t i = 0; i < N; i++) {
+    prob[i] = fabs(ci[i]) * N / cumulative;
+    if (prob[i] < 1.0)
+      smaller.push_back((int)i);
+    else
+      larger.push_back((int)i);
+  }
+  while (!larger.empty() && !smaller.empty()) {
+    const int l = larger.back();
+    larger.pop_back();
+    const int sm = smaller.back();
+    smaller.pop_back();
+    alias[sm] = l;
+    prob[l] = prob[l] - (1.0 - prob[sm]);
+    if (prob[l] < 1.0)
+      smaller.push_back(l);
+    else
+      larger.push_back(l);
+  }
+}
+
+PtStochResult pt_semistochastic(const Det2* dets, size_t n, const double* c_dev, const std::vector<double>& c_host,
+                                double E0, double eps2, double eps2L, int nsample, int max_iter, double target,
+                                uint64_t seed, const IntsView& ints, const HeatBathView& hb, double maxEntry,
+                                const SelectParams& sp, const DetHash& present, PtWork& w, Prims& pr,
+                                cudaStream_t s) {
+  PtStochResult res;
+  if (n == 0) return res;
+  if (!(eps2 >= 0.0)) throw Error(kErrInvalid, "epsilon2 must be >= 0");
+  if (nsample < 2) throw Error(kErrInvalid, "sampleN must be at least 2");
+  if (max_iter < 1) throw Error(kErrInvalid, "nPTiter must be at least 1");
+  if (eps2L < 999) res.e_large = pt_deterministic(dets, n, c_dev, E0, eps2L, ints, hb, maxEntry, sp, present, 0, w,
+                                                  pr, s).e2;
+  double cumulative = 0.0;
+  for (size_t i = 0; i < n; i++) cumulative += fabs(c_host[i]);
+  std::vector<int> alias;
+  std::vector<double> prob;
+  alias_setup(c_host, cumulative, alias, prob);
+  PtArgs a;
+  const size_t gsmem = pt_prepare(a, dets, n, c_dev, E0, eps2, ints, hb, maxEntry, sp, present, w, s);
+  a.eps2L = eps2L;
+  a.nmcf = (double)nsample / (nsample - 1);
+  DevBuf<int32_t> dlist;
+  DevBuf<double> dw;
+  dlist.resize((size_t)nsample);
+  dw.resize((size_t)nsample);
+  // uniform [0, 1) from a 64-bit Mersenne twister (the reference draws
+  // rand() / RAND_MAX; any uniform stream gives the same estimator)
+  std::mt19937_64 g(seed);
+  auto next = [&]() { return (double)(g() >> 11) * (1.0 / 9007199254740992.0); };
+  std::vector<int32_t> sample((size_t)nsample);
+  std::vector<double> wts((size_t)nsample);
+  std::vector<double> hp(3 * kPtRedBlocks);
+  const double f = (double)nsample / (nsample - 1);
+  double avg = 0.0, avg2 = 0.0;
+  for (int iter = 0; iter < max_iter; ++iter) {
+    // SHCIsampledeterminants::sample_N2_alias (SHCI/SHCIsampledeterminants.cpp:153-190)
+    std::fill(sample.begin(), sample.end(), -1);
+    std::fill(wts.begin(), wts.end(), 0.0);
+    int distinct = 0;
+    for (int k = 0; k < nsample; k++) {
+      int det = (int)floor(next() * n);
+      if (next() >= prob[det]) det = alias[det];
+      int at = -1;
+      for (int q = 0; q < distinct; ++q)
+        if (sample[q] == det) {
+          at = q;
+          break;
+        }
+      const double wgt = cumulative * c_host[det] / fabs(c_host[det]);
+      if (at < 0) {
+        sample[distinct] = det;
+        wts[distinct] = wgt;
+        distinct++;
+      } else {
+        wts[at] += wgt;
+      }
+    }
+    for (int k = 0; k < nsample; k++) wts[k] /= nsample;
+    SHCI_CUDA(cudaMemcpyAsync(dlist.p, sample.data(), distinct * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    SHCI_CUDA(cudaMemcpyAsync(dw.p, wts.data(), distinct * sizeof(double), cudaMemcpyHostToDevice, s));
+    a.plist = dlist.p;
+    a.pw = dw.p;
+    a.n = (size_t)distinct;
+    // generate (twice when the buffers turn out too small)
+    int64_t room = std::max<int64_t>((int64_t)w.key0.cap, (int64_t)1 << 20), m = 0;
+    for (int pass = 0; pass < 2; ++pass) {
+      w.key0.reserve((size_t)room);
+      w.key1.reserve((size_t)room);
+      w.ne.reserve((size_t)room);
+      w.n2p.reserve((size_t)room);
+      a.cap = room;
+      a.key0 = w.key0.p;
+      a.key1 = w.key1.p;
+      a.ne = w.ne.p;
+      a.n2p = w.n2p.p;
+      SHCI_CUDA(cudaMemsetAsync(w.next.p, 0, 2 * sizeof(unsigned long long), s));
+      k_pt_gen<<<kPtGenBlocks, kPtThreads, gsmem, s>>>(a);
+      SHCI_LAUNCH_CHECK();
+      unsigned long long total = 0;
+      SHCI_CUDA(cudaMemcpyAsync(&total, w.next.p + 1, sizeof(total), cudaMemcpyDeviceToHost, s));
+      SHCI_CUDA(cudaStreamSynchronize(s));
+      m = (int64_t)total;
+      if (m <= room) break;
+      if (m >= (int64_t)0xfffffff0u) throw Error(kErrOOM, "semistochastic sample exceeds 2^32 candidates");
+      room = m;
+    }
+    res.candidates += m;
+    double eA = 0.0, eB = 0.0;
+    if (m > 0) {
+      w.perm.resize((size_t)m);
+      k_pt_iota<<<grid_for((size_t)m, 256), 256, 0, s>>>(w.perm.p, (size_t)m);
+      SHCI_LAUNCH_CHECK();
+      sort_u128(w.key0.p, w.key1.p, w.perm.p, (size_t)m, pr, s);
+      k_pt_reduce_stoch<<<kPtRedBlocks, kPtRedThreads, 0, s>>>(w.key0.p, w.key1.p, w.perm.p, w.ne.p, w.n2p.p,
+                                                               (size_t)m, f, w.part.p);
+      SHCI_LAUNCH_CHECK();
+      SHCI_CUDA(cudaMemcpyAsync(hp.data(), w.part.p, hp.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+      SHCI_CUDA(cudaStreamSynchronize(s));
+      for (unsigned b = 0; b < kPtRedBlocks; ++b) {
+        eA += hp[3 * b];
+        eB += hp[3 * b + 1];
+      }
+    }
+    // SHCI/SHCIbasics.cpp:388-449
+    const double est = -eA + eB + res.e_large;
+    avg += est;
+    avg2 += est * est;
+    const int it = iter + 1;
+    res.iterations = it;
+    res.stddev = it < 5 ? 1e4 : pow((it * avg2 - pow(avg, 2)) / it / (it - 1) / it, 0.5);
+    if (res.stddev < target) break;
+  }
+  res.e2 = avg / res.iterations;
   return res;
 }
 

@@ -65,6 +65,9 @@ SIGNATURES = [
     ("shci_run_pt", _i32, [_vp, _dbl, _vp, _i32, _P(_i32)]),
     ("shci_pt_stats", _i32, [_vp, _P(_i64), _P(_i64), _P(_i32), _P(_dbl), _P(_dbl)]),
     ("shci_set_pt_batch", _i32, [_vp, _i64]),
+    ("shci_pt_semistochastic", _i32, [_vp, _vp, _dbl, _dbl, _dbl, _i32, _i32, _dbl, _u64, _P(_dbl), _P(_dbl),
+                                      _P(_i32)]),
+    ("shci_pt_error", _i32, [_vp, _P(_dbl), _P(_i32), _P(_dbl)]),
     ("shci_ints_info", _i32, [_vp, _P(_i32), _P(_i32), _P(_dbl)]),
     ("shci_rdm", _i32, [_vp, _vp, _vp, _vp]),
     ("shci_run_rdm", _i32, [_vp, _i32, _vp, _vp]),
@@ -421,6 +424,27 @@ class Engine:
         nr = ctypes.c_int()
         self._check(load_library().shci_run_pt(self.h, float(eps2), _p(E), 16, ctypes.byref(nr)))
         return E[:nr.value].copy()
+
+    def pt_semistochastic(self, ci, E0, eps2, eps2_large=1000.0, sample_n=200, max_iter=1000000,
+                          target_error=1e-4, seed=1):
+        """Semistochastic PT2 estimate for host coefficients ci (E0 including
+        the core energy). Returns (E2, standard error, iterations)."""
+        c = np.ascontiguousarray(ci, dtype=np.float64)
+        if c.shape != (self.ndets(),):
+            raise ValueError("ci must hold one coefficient per determinant")
+        e2, sd = ctypes.c_double(), ctypes.c_double()
+        it = ctypes.c_int()
+        self._check(load_library().shci_pt_semistochastic(self.h, _p(c), float(E0), float(eps2), float(eps2_large),
+                                                          int(sample_n), int(max_iter), float(target_error),
+                                                          int(seed), ctypes.byref(e2), ctypes.byref(sd),
+                                                          ctypes.byref(it)))
+        return e2.value, sd.value, it.value
+
+    def pt_error(self):
+        sd, el = ctypes.c_double(), ctypes.c_double()
+        it = ctypes.c_int()
+        self._check(load_library().shci_pt_error(self.h, ctypes.byref(sd), ctypes.byref(it), ctypes.byref(el)))
+        return {"stddev": sd.value, "iterations": it.value, "e_large": el.value}
 
     def pt_stats(self):
         c, u, n = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int()

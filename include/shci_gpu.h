@@ -209,7 +209,12 @@ int shci_run_ci(shci_ctx* ctx, double* out, int64_t cap);
  *   restrictions of shci_set_selection_params apply; ncore/nact do not.
  * shci_run_pt: after shci_run_input, E[r] = E_var[r] + E2[r] for every root
  *   (what the reference writes to shci.e), eps2 <= 0 taking the input's
- *   epsilon2 (default 1e-8, SHCI/input.cpp:58).
+ *   epsilon2 (default 1e-8, SHCI/input.cpp:58). As the reference chooses
+ *   (SHCI/SHCI.cpp:707-760): `deterministic` in the input gives the
+ *   deterministic PT; otherwise the semistochastic PT with the input's
+ *   sampleN, nPTiter (0: no PT, E = E_var), targetError, epsilon2Large and
+ *   seed (+ root; without `seed` a fixed default instead of the clock), and an
+ *   input without sampleN is an error, as in the reference.
  * shci_pt_stats: of the last PT call: candidates generated outside the
  *   variational space before merging, distinct determinants, hash partitions
  *   used, first-order norm sum_a (N_a / (E0 - E_a))^2, seconds.
@@ -218,6 +223,26 @@ int shci_run_ci(shci_ctx* ctx, double* out, int64_t cap);
  *   partitions, as the reference splits them over MPI ranks; E2 agrees to
  *   rounding across partition counts. */
 int shci_pt_deterministic(shci_ctx* ctx, const double* ci, double E0, double eps2, double* e2);
+/* Semistochastic PT2. Replaces
+ * SHCIbasics::DoPerturbativeStochastic2SingleListDoubleEpsilon2AllTogether
+ * (SHCI/SHCIbasics.cpp:55-451) with its sampler
+ * SHCIsampledeterminants::setUpAliasMethod / sample_N2_alias
+ * (SHCI/SHCIsampledeterminants.cpp:64-190) and generator
+ * getDeterminantsStochastic2Epsilon (SHCI/SHCIgetdeterminants.cpp:889-1045):
+ * the deterministic part at eps2_large (skipped when >= 999, the reference's
+ * default 1000), then iterations of sample_n alias draws with probability
+ * |c_i| / sum |c| until the standard error of the mean (from the fifth
+ * iteration on) is below target_error or max_iter iterations ran. *e2 = the
+ * mean estimate (the caller adds E0), *stddev its standard error,
+ * *iterations the count. The draws come from a 64-bit Mersenne twister seeded
+ * with `seed` (the reference uses rand() seeded from the clock), so results
+ * are reproducible for a given seed; the estimator is the reference's. */
+int shci_pt_semistochastic(shci_ctx* ctx, const double* ci, double E0, double eps2, double eps2_large, int sample_n,
+                           int max_iter, double target_error, uint64_t seed, double* e2, double* stddev,
+                           int* iterations);
+/* Error of the last semistochastic PT (zeros after a deterministic one):
+ * standard error, iterations, deterministic part at eps2_large. */
+int shci_pt_error(shci_ctx* ctx, double* stddev, int* iterations, double* e_large);
 int shci_run_pt(shci_ctx* ctx, double eps2, double* E, int cap_roots, int* nroots);
 int shci_pt_stats(shci_ctx* ctx, int64_t* candidates, int64_t* unique, int* partitions, double* psi1_norm,
                   double* seconds);

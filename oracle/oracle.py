@@ -81,6 +81,8 @@ def lib():
         L.orc_rdm_eval.argtypes = [vp, vp, vp, vp]
         L.orc_rdm_energy.restype = dbl
         L.orc_rdm_energy.argtypes = [vp, vp]
+        L.orc_pt_stoch.restype = dbl
+        L.orc_pt_stoch.argtypes = [vp, vp, i64, vp, dbl, dbl, dbl, i32, i32, dbl, ctypes.c_uint64, vp, vp, vp]
         L.orc_var_pt.restype = dbl
         L.orc_var_pt.argtypes = [vp, i32, dbl]
         L.orc_input_epsilon2.restype = dbl
@@ -190,6 +192,18 @@ class Oracle:
         r = _pack_restrictions(restrictions)
         e2 = lib().orc_pt_det(self.h, _p(dets), len(dets), _p(ci), E0, eps2, _p(r), len(restrictions))
         return e2, _pt_stats(self.h)
+
+    def pt_stoch(self, dets, ci, E0, eps2, eps2_large=1000.0, sample_n=200, max_iter=1000000,
+                 target_error=1e-4, seed=1):
+        """Semistochastic PT2 estimate E2 (E0 including coreE). Returns
+        (E2, dict(stddev, iterations, e_large))."""
+        dets = np.ascontiguousarray(dets, dtype=np.uint64)
+        ci = np.ascontiguousarray(ci, dtype=np.float64)
+        sd, el = ctypes.c_double(), ctypes.c_double()
+        it = ctypes.c_int()
+        e2 = lib().orc_pt_stoch(self.h, _p(dets), len(dets), _p(ci), E0, eps2, eps2_large, sample_n, max_iter,
+                                target_error, seed, ctypes.byref(sd), ctypes.byref(it), ctypes.byref(el))
+        return e2, dict(stddev=sd.value, iterations=it.value, e_large=el.value)
 
     def pt_det_range(self, dets, ci, E0, eps2, p0, p1):
         """pt_det with the candidates of parents [p0, p1) only (no

@@ -20,6 +20,7 @@
 // SHCI/Determinants.h:247-602.
 
 #include <algorithm>
+#include <random>
 #include <cassert>
 #include <chrono>
 #include <cmath>
@@ -768,6 +769,241 @@ static void build_ham(const Ints& I, const Det* dets, size_t N, SparseHam& H) {
 }
 
 // ---------------------------------------------------------------------------
+// Semistochastic PT2 (SHCIbasics::DoPerturbativeStochastic2SingleListDoubleEpsilon2AllTogether,
+// SHCI/SHCIbasics.cpp:55-451)
+// ---------------------------------------------------------------------------
+struct PtStochCand {
+  Det d;
+  double num1, num2, E;
+  bool present;
+};
+
+// SHCIgetdeterminants::getDeterminantsStochastic2Epsilon
+// (SHCI/SHCIgetdeterminants.cpp:889-1045): the candidates of one sampled
+// parent with threshold epsilon, their numerators H ci1 and
+// H^2 ci1 (ci1 Nmc/(Nmc-1) - ci2), and whether |H| > epsilonLarge (the part
+// the deterministic stage already holds).
+static void pt_stoch_from_parent(const Ints& I, const HeatBath& hb, const Det& d, double epsilon,
+                                 double epsilonLarge, double ci1, double ci2, int Nmc,
+                                 std::vector<Restriction>& rs, std::vector<PtStochCand>& out) {
+  const int nspin = 2 * I.norb;
+  int closed[128], open[128];
+  int nclosed = 0, nopen = 0;
+  for (int p = 0; p < nspin; ++p) {
+    if (getocc(d, p))
+      closed[nclosed++] = p;
+    else
+      open[nopen++] = p;
+  }
+  const double Energyd = det_energy(I, d) + I.coreE;
+  const double Nmcd = 1. * Nmc;
+  restrictions_init(rs, closed, nclosed);
+  for (int ia = 0; ia < nopen * nclosed; ia++) {
+    int i = ia / nopen, a = ia % nopen;
+    if (!restr_one(rs, closed[i], open[a])) continue;
+    double integral = hij_1excite(I, open[a], closed[i], closed, nclosed);
+    if (closed[i] % 2 != open[a] % 2) {
+      double sgn = parity_between(d, std::min(open[a], closed[i]), std::max(open[a], closed[i]));
+      integral = I.i1(open[a], closed[i]) * sgn;
+    }
+    if (fabs(integral) > epsilon) {
+      PtStochCand c;
+      c.d = d;
+      setocc(c.d, open[a], true);
+      setocc(c.d, closed[i], false);
+      c.num1 = integral * ci1;
+      c.num2 = integral * integral * ci1 * (ci1 * Nmcd / (Nmcd - 1) - ci2);
+      c.E = energy_after_single(I, closed, nclosed, i, open[a], Energyd);
+      c.present = fabs(integral) > epsilonLarge;
+      out.push_back(c);
+    }
+  }
+  if (fabs(I.maxEntry) < epsilon) return;
+  for (int ij = 0; ij < nclosed * nclosed; ij++) {
+    int i = ij / nclosed, j = ij % nclosed;
+    if (i <= j) continue;
+    int Ii = closed[i] / 2, Jj = closed[j] / 2;
+    int X = std::max(Ii, Jj), Y = std::min(Ii, Jj);
+    int pairIndex = X * (X + 1) / 2 + Y;
+    bool same = closed[i] % 2 == closed[j] % 2;
+    size_t start = same ? hb.sameStart[pairIndex] : hb.oppStart[pairIndex];
+    size_t end = same ? hb.sameStart[pairIndex + 1] : hb.oppStart[pairIndex + 1];
+    const float* integrals = same ? hb.sameVal.data() : hb.oppVal.data();
+    const int16_t* orbIndices = same ? hb.samePairs.data() : hb.oppPairs.data();
+    for (size_t index = start; index < end; index++) {
+      if (fabsf(integrals[index]) < epsilon) break;
+      int a = 2 * orbIndices[2 * index] + closed[i] % 2;
+      int b = 2 * orbIndices[2 * index + 1] + closed[j] % 2;
+      if (!restr_two(rs, closed[i], closed[j], a, b)) continue;
+      if (!(getocc(d, a) || getocc(d, b))) {
+        PtStochCand c;
+        c.d = d;
+        setocc(c.d, a, true);
+        setocc(c.d, b, true);
+        setocc(c.d, closed[i], false);
+        setocc(c.d, closed[j], false);
+        double sgn = pt_double_sign(c.d, a, b, closed[i], closed[j]);
+        c.num1 = integrals[index] * sgn * ci1;
+        c.num2 = integrals[index] * integrals[index] * ci1 * (ci1 * Nmcd / (Nmcd - 1) - ci2);
+        c.E = energy_after_double(I, closed, nclosed, i, a, j, b, Energyd);
+        c.present = fabs(integrals[index]) > epsilonLarge;
+        out.push_back(c);
+      }
+    }
+  }
+}
+
+// Uniform [0, 1) from a 64-bit Mersenne twister (the reference draws
+// rand() / RAND_MAX from the C library; any uniform stream gives the same
+// estimator, and this one is the same on every platform).
+struct PtRng {
+  std::mt19937_64 g;
+  explicit PtRng(uint64_t seed) : g(seed) {}
+  double next() { return (double)(g() >> 11) * (1.0 / 9007199254740992.0); }
+};
+
+// SHCIsampledeterminants::setUpAliasMethod (SHCI/SHCIsampledeterminants.cpp:64-88).
+static void alias_setup(const double* ci, size_t N, double cumulative, std::vector<int>& alias,
+                        std::vector<double>& prob) {
+  alias.assign(N, 0);
+  prob.assign(N, 0.0);
+  std::vector<int> larger, smaller;
+  for (size_t i = 0; i < N; i++) {
+    prob[i] = fabs(ci[i]) * N / cumulative;
+    if (prob[i] < 1.0)
+      smaller.push_back((int)i);
+    else
+      larger.push_back((int)i);
+  }
+  while (!larger.empty() && !smaller.empty()) {
+    int l = larger.back();
+    larger.pop_back();
+    int s_ = smaller.back();
+    smaller.pop_back();
+    alias[s_] = l;
+    prob[l] = prob[l] - (1.0 - prob[s_]);
+    if (prob[l] < 1.0)
+      smaller.push_back(l);
+    else
+      larger.push_back(l);
+  }
+}
+
+// SHCIsampledeterminants::sample_N2_alias (SHCI/SHCIsampledeterminants.cpp:153-190):
+// Nmc draws, distinct determinants in order of first draw, weights
+// cumulative * sign(c) summed over repeated draws, divided by Nmc.
+static int alias_sample(const double* ci, size_t N, double cumulative, const std::vector<int>& alias,
+                        const std::vector<double>& prob, int Nmc, PtRng& rng, std::vector<int>& sample,
+                        std::vector<double>& wts) {
+  sample.assign(Nmc, -1);
+  wts.assign(Nmc, 0.0);
+  int n = 0;
+  for (int k = 0; k < Nmc; k++) {
+    int det = (int)floor(rng.next() * N);
+    if (rng.next() >= prob[det]) det = alias[det];
+    int at = -1;
+    for (int q = 0; q < n; ++q)
+      if (sample[q] == det) {
+        at = q;
+        break;
+      }
+    const double w = cumulative * ci[det] / fabs(ci[det]);
+    if (at < 0) {
+      sample[n] = det;
+      wts[n] = w;
+      n++;
+    } else {
+      wts[at] += w;
+    }
+  }
+  for (int k = 0; k < Nmc; k++) wts[k] /= Nmc;
+  return n;
+}
+
+struct PtStochStats {
+  int iterations = 0;
+  double stddev = 0.0;
+  double e_large = 0.0;  // the deterministic part at epsilon2Large
+};
+
+// SHCIbasics::DoPerturbativeStochastic2SingleListDoubleEpsilon2AllTogether
+// (SHCI/SHCIbasics.cpp:55-451), one rank: the deterministic part at
+// epsilon2Large (when below 999), then iterations of Nsample alias draws with
+// probability |c_i| / sum |c|; each iteration's estimate is
+// -sum_a (N1a^2 Nmc/(Nmc-1) - N2a) / (E_a - E0) over determinants outside the
+// variational space, plus the same sum restricted to the contributions above
+// epsilon2Large, plus the deterministic part. Stops once the standard error
+// of the mean (from the fifth iteration on) is below targetError, or after
+// nPTiter iterations. Returns the mean (the reference returns the running sum
+// if nPTiter runs out first).
+static double pt_semistochastic(const Ints& I, const HeatBath& hb, const Det* dets, size_t N, const double* ci,
+                                double E0, double eps2, double eps2Large, int Nsample, int nPTiter,
+                                double targetError, uint64_t seed, std::vector<Restriction> rs,
+                                PtStochStats& st) {
+  st = PtStochStats();
+  if (eps2Large < 999) {
+    PtStats dst;
+    st.e_large = pt_deterministic(I, hb, dets, N, ci, E0, eps2Large, rs, dst);
+  }
+  double cumulative = 0.0;
+  for (size_t i = 0; i < N; i++) cumulative += fabs(ci[i]);
+  std::vector<int> alias;
+  std::vector<double> prob;
+  alias_setup(ci, N, cumulative, alias, prob);
+  std::vector<Det> sorted(dets, dets + N);
+  std::sort(sorted.begin(), sorted.end(), det_less);
+  PtRng rng(seed);
+  const int Nmc = Nsample;
+  double avg = 0.0, avg2 = 0.0;
+  std::vector<int> sample;
+  std::vector<double> wts;
+  std::vector<PtStochCand> all;
+  for (int iter = 0; iter < nPTiter; iter++) {
+    const int distinct = alias_sample(ci, N, cumulative, alias, prob, Nmc, rng, sample, wts);
+    all.clear();
+    for (int k = 0; k < distinct; k++) {
+      const int Id = sample[k];
+      pt_stoch_from_parent(I, hb, dets[Id], eps2 / fabs(ci[Id]), eps2Large / fabs(ci[Id]), wts[k], ci[Id], Nmc, rs,
+                           all);
+    }
+    std::stable_sort(all.begin(), all.end(),
+                     [](const PtStochCand& x, const PtStochCand& y) { return det_less(x.d, y.d); });
+    double eA = 0.0, eB = 0.0;
+    size_t k = 0, v = 0;
+    const double f = 1. * Nmc / (Nmc - 1);
+    while (k < all.size()) {
+      size_t e = k;
+      double n1a = 0, n2a = 0, n1b = 0, n2b = 0;
+      while (e < all.size() && det_eq(all[e].d, all[k].d)) {
+        n1a += all[e].num1;
+        n2a += all[e].num2;
+        if (all[e].present) {
+          n1b += all[e].num1;
+          n2b += all[e].num2;
+        }
+        ++e;
+      }
+      while (v < sorted.size() && det_less(sorted[v], all[k].d)) ++v;
+      const bool in_space = v < sorted.size() && det_eq(sorted[v], all[k].d);
+      if (!in_space) {
+        const double de = all[k].E - E0;
+        eA += (pow(fabs(n1a), 2) * f - n2a) / de;
+        eB += (pow(fabs(n1b), 2) * f - n2b) / de;
+      }
+      k = e;
+    }
+    const double est = -eA + eB + st.e_large;
+    avg += est;
+    avg2 += est * est;
+    const int it = iter + 1;
+    st.iterations = it;
+    st.stddev = it < 5 ? 1e4 : pow((it * avg2 - pow(avg, 2)) / it / (it - 1) / it, 0.5);
+    if (st.stddev < targetError) break;
+  }
+  return avg / st.iterations;
+}
+
+// ---------------------------------------------------------------------------
 // Reduced density matrices of the variational wavefunction
 // ---------------------------------------------------------------------------
 // SHCIrdm::populateSpatialRDM (SHCI/SHCIrdm.cpp:846-861): s2 is the n^2 x n^2
@@ -1506,6 +1742,18 @@ double orc_var_pt(orc_ctx* c, int root, double eps2) {
   if (eps2 <= 0) eps2 = c->sched.epsilon2;
   return pt_deterministic(c->ints, c->hb, c->var.dets.data(), c->var.dets.size(), c->var.ci[root].data(),
                           c->var.E[root], eps2, c->sched.sel.restrictions, c->pt);
+}
+// Semistochastic PT2 of dets / ci (E0 with coreE). Returns E2; stats out.
+double orc_pt_stoch(orc_ctx* c, const uint64_t* dets, int64_t n, const double* ci, double E0, double eps2,
+                    double eps2Large, int Nsample, int nPTiter, double targetError, uint64_t seed, double* stddev,
+                    int* iterations, double* e_large) {
+  PtStochStats st;
+  const double e2 = pt_semistochastic(c->ints, c->hb, (const Det*)dets, (size_t)n, ci, E0, eps2, eps2Large, Nsample,
+                                      nPTiter, targetError, seed, c->sched.sel.restrictions, st);
+  *stddev = st.stddev;
+  *iterations = st.iterations;
+  *e_large = st.e_large;
+  return e2;
 }
 double orc_input_epsilon2(orc_ctx* c) { return c->sched.epsilon2; }
 int orc_input_deterministic(orc_ctx* c) { return c->sched.stochastic ? 0 : 1; }

@@ -148,3 +148,48 @@ def test_pt_multiple_roots(tmp_path):
     for r in range(2):
         e2o, _ = o.pt_det(dets, ci[r], E[r], 1e-6)
         assert abs((Ept[r] - E[r]) - e2o) <= REL * abs(e2o)
+
+
+def test_semistochastic_pt_matches_oracle_draw_for_draw(tmp_path):
+    """Semistochastic PT on the GPU and in the oracle with the same seed make
+    the same draws, so a fixed number of iterations (target 0: no early stop)
+    gives the same estimate to 1e-9 relative and the same standard error to
+    1e-6 relative; with and without the deterministic part at epsilon2Large."""
+    inp = synthetic.make_workload("mol24", str(tmp_path / "w"), schedule=[(0, 3e-3)], maxiter=2)
+    e, E = _gpu_run(inp)
+    dets = e.dets()
+    ci = e.run_ci(1)[0]
+    o = orc.Oracle(os.path.join(os.path.dirname(inp), "FCIDUMP"))
+    for eL in (1000.0, 1e-3):
+        g2, gsd, git = e.pt_semistochastic(ci, E[0], 1e-5, eps2_large=eL, sample_n=100, max_iter=12,
+                                           target_error=0.0, seed=11)
+        o2, ost = o.pt_stoch(dets, ci, E[0], 1e-5, eps2_large=eL, sample_n=100, max_iter=12, target_error=0.0,
+                             seed=11)
+        print("eps2Large", eL, "gpu", g2, gsd, git, "oracle", o2, ost)
+        assert git == ost["iterations"] == 12
+        assert abs(g2 - o2) <= 1e-9 * abs(o2)
+        assert abs(gsd - ost["stddev"]) <= 1e-6 * ost["stddev"]
+        assert abs(e.pt_error()["e_large"] - ost["e_large"]) <= 1e-10 * abs(ost["e_large"]) + 1e-15
+    e.close()
+
+
+def test_semistochastic_pt_from_input_estimates_deterministic(tmp_path):
+    """An input without `deterministic` but with sampleN runs the
+    semistochastic PT (the reference's default): its estimate agrees with
+    the deterministic PT2 at the same epsilon2 within 4 standard errors, and
+    nPTiter 0 skips PT (E = E_var)."""
+    extra = ("epsilon2 1e-6", "epsilon2Large 1e-4", "sampleN 50", "targetError 2e-5", "seed 3")
+    inp = synthetic.make_workload("mol10", str(tmp_path / "w"), extra=extra)
+    e, E = _gpu_run(inp)
+    Ept = e.run_pt()
+    err = e.pt_error()
+    ci = e.run_ci(1)[0]
+    ed = e.pt_deterministic(ci, E[0], 1e-6)
+    e.close()
+    print("semistochastic", Ept[0] - E[0], err, "deterministic", ed)
+    assert err["iterations"] >= 5 and err["stddev"] < 2e-5
+    assert abs((Ept[0] - E[0]) - ed) < 4 * err["stddev"]
+    inp2 = synthetic.make_workload("mol10", str(tmp_path / "w2"), extra=extra + ("nPTiter 0",))
+    e, E = _gpu_run(inp2)
+    assert e.run_pt()[0] == E[0]
+    e.close()
