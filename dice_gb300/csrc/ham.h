@@ -174,7 +174,7 @@ struct PtResult {
 struct PtWork {
   DevBuf<uint64_t> key0, key1;  // candidate determinants, word by word
   DevBuf<float4> ne;  // numerator and E_a - E0 of each candidate (float pairs)
-  DevBuf<float4> n2p;  // semistochastic mode: second numerator and the flag
+  DevBuf<double2> n2p;  // semistochastic mode: both numerators in FP64
   DevBuf<double> part;
   DevBuf<uint32_t> perm;
   DevBuf<unsigned long long> next;  // parent queue, candidate counter

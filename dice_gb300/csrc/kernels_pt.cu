@@ -94,13 +94,15 @@ struct PtArgs {
   float4* ne;   // numerator (x + y) and E_a - E0 (z + w), both float pairs
   float2 e0;    // E0 (without the core energy) as a float pair
   // semistochastic mode (plist != null): the parents are plist[0, n) with
-  // weights pw; numerators use the weight, thresholds the coefficient, and
-  // n2p receives the second numerator (x + y) and the flag |H| > eps2L / |c| (z)
+  // weights pw; numerators use the weight, thresholds the coefficient; n2p
+  // receives the two numerators in FP64 (their difference cancels to a few
+  // digits, so they are kept as the reference computes them) and ne.x the
+  // flag |H| > eps2L / |c|
   const int32_t* plist;
   const double* pw;
   double eps2L;
-  double nmcf;  // Nmc / (Nmc - 1)
-  float4* n2p;
+  double nmc;  // number of draws per iteration
+  double2* n2p;
 };
 
 __device__ __forceinline__ bool in_part(const PtArgs& a, const Det2& d) {
@@ -160,7 +162,7 @@ __device__ __forceinline__ float2 shfl_ff(float2 v, int src) {
 // Warp-aggregated append of the lanes with `keep`; slots past cap are counted
 // but not written.
 __device__ __forceinline__ void pt_put(const PtArgs& a, bool keep, const Det2& cand, float2 v, float2 e,
-                                       float2 v2 = make_float2(0.0f, 0.0f), bool present = false) {
+                                       double2 vs = make_double2(0.0, 0.0), bool present = false) {
   const int lane = threadIdx.x & 31;
   const unsigned m = __ballot_sync(kFull, keep);
   if (!m) return;
@@ -173,8 +175,12 @@ __device__ __forceinline__ void pt_put(const PtArgs& a, bool keep, const Det2& c
     if (q < (unsigned long long)a.cap) {
       a.key0[q] = cand.w0;
       a.key1[q] = cand.w1;
-      a.ne[q] = make_float4(v.x, v.y, e.x, e.y);
-      if (a.n2p) a.n2p[q] = make_float4(v2.x, v2.y, present ? 1.0f : 0.0f, 0.0f);
+      if (a.n2p) {
+        a.ne[q] = make_float4(present ? 1.0f : 0.0f, 0.0f, e.x, e.y);
+        a.n2p[q] = vs;
+      } else {
+        a.ne[q] = make_float4(v.x, v.y, e.x, e.y);
+      }
     }
   }
 }
@@ -333,7 +339,8 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
     const bool stoch = a.plist != nullptr;
     const double epsL = stoch ? fabs(a.eps2L / cp) : INFINITY;
     const float epsL_f = __double2float_rd(epsL);
-    const float2 k_ff = ff_of(stoch ? ci1 * (ci1 * a.nmcf - cp) : 0.0);
+    // ci1 * Nmc / (Nmc - 1) - ci2 of getDeterminantsStochastic2Epsilon
+    const double kfac = stoch ? __dsub_rn(__ddiv_rn(__dmul_rn(ci1, a.nmc), __dsub_rn(a.nmc, 1.0)), cp) : 0.0;
     // occupied list (ascending) and per-spin electron / hole lists, by ballot
     const int nclosed = __popcll(d.w0) + __popcll(d.w1);
     const int ncA = __popcll(d.w0 & 0x5555555555555555ull) + __popcll(d.w1 & 0x5555555555555555ull);
@@ -409,7 +416,8 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
     auto drain = [&](unsigned cnt) {  // the first cnt (<= 32) entries
       bool keep = false, present = false;
       Det2 cand = d;
-      float2 v = make_float2(0.0f, 0.0f), e = v, v2 = v;
+      float2 v = make_float2(0.0f, 0.0f), e = v;
+      double2 vs = make_double2(0.0, 0.0);
       if ((unsigned)lane < cnt) {
         const unsigned slot = (qh + lane) & 63u;
         const uint32_t w = qo[slot];
@@ -430,8 +438,10 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
             if (keep) {
               v = ff_mul(H, cp_ff);
               if (stoch) {
-                v2 = ff_mul(ff_mul(H, H), k_ff);
-                present = fabs((double)H.x + (double)H.y) > epsL;
+                // numerators as the reference forms them, from the FP64 element
+                const double hd = hij_single_rows(a, d, oa, oi);
+                vs = make_double2(__dmul_rn(hd, ci1), __dmul_rn(__dmul_rn(__dmul_rn(hd, hd), ci1), kfac));
+                present = fabs(hd) > epsL;
               }
               e = ff_sub(ff_add(ed, ff_sub(F[oa], F[oi])), vpair(sD, sX, n, oa, oi));
             }
@@ -447,8 +457,12 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
             const float vf = qv[slot];
             v = ff_mul_f(pt_double_sign(cand, oa, ob, oi, oj) > 0.0 ? vf : -vf, cp_ff);
             if (stoch) {
+              // integrals[index] * sgn * ci1 and integrals[index]^2 (a float
+              // product) * ci1 * kfac, as the reference forms them
+              const double sg = pt_double_sign(cand, oa, ob, oi, oj);
               const float sq = __fmul_rn(vf, vf);
-              v2 = ff_mul(make_float2(sq, __fmaf_rn(vf, vf, -sq)), k_ff);
+              vs = make_double2(__dmul_rn(__dmul_rn((double)vf, sg), ci1),
+                                __dmul_rn(__dmul_rn((double)sq, ci1), kfac));
               present = fabsf(vf) > epsL_f;  // (double)|v| > epsL exactly
             }
             const float2 fa = ff_add(F[oa], F[ob]), fi = ff_add(F[oi], F[oj]);
@@ -459,7 +473,7 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_gen(PtArgs a) {
           }
         }
       }
-      pt_put(a, keep, cand, v, e, v2, present);
+      pt_put(a, keep, cand, v, e, vs, present);
       qh = (qh + cnt) & 63u;
       qn -= cnt;
       __syncwarp();
@@ -617,6 +631,20 @@ __device__ __forceinline__ __int128 to_fix(float x) {
 }
 // a float pair exactly (up to the 2^-kFixBits truncation of each part)
 __device__ __forceinline__ __int128 to_fix(float2 x) { return to_fix(x.x) + to_fix(x.y); }
+// a double (|x| < 2^47), truncated toward zero to the unit
+__device__ __forceinline__ __int128 to_fix(double x) {
+  const long long b = __double_as_longlong(x);
+  const int ex = (int)((b >> 52) & 0x7ff);
+  if (ex == 0) return 0;
+  const unsigned long long m = ((unsigned long long)b & 0xfffffffffffffull) | (1ull << 52);
+  const int sh = ex - 1075 + kFixBits;
+  unsigned __int128 v = 0;
+  if (sh >= 0)
+    v = (unsigned __int128)m << (sh < 74 ? sh : 74);
+  else if (sh > -64)
+    v = m >> (-sh);
+  return b < 0 ? -(__int128)v : (__int128)v;
+}
 
 __device__ __forceinline__ double from_fix(__int128 v) {
   const bool neg = v < 0;
@@ -800,7 +828,7 @@ __global__ void __launch_bounds__(kPtRedThreads) k_pt_reduce_stoch(const uint64_
                                                                    const uint64_t* __restrict__ k1,
                                                                    const uint32_t* __restrict__ perm,
                                                                    const float4* __restrict__ ne,
-                                                                   const float4* __restrict__ n2p, size_t m, double f,
+                                                                   const double2* __restrict__ n2p, size_t m, double f,
                                                                    double* __restrict__ part) {
   double eA = 0.0, eB = 0.0, cnt = 0.0;
   for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < m; k += (size_t)gridDim.x * blockDim.x) {
@@ -811,11 +839,12 @@ __global__ void __launch_bounds__(kPtRedThreads) k_pt_reduce_stoch(const uint64_
     for (size_t j = k; j < m; ++j) {
       if (j > k && (k0[j] != d0 || k1[j] != d1)) break;
       const uint32_t pk = perm[j];
-      const float4 x = ne[pk], y = n2p[pk];
-      const __int128 f1 = to_fix(make_float2(x.x, x.y)), f2 = to_fix(make_float2(y.x, y.y));
+      const float4 x = ne[pk];
+      const double2 y = n2p[pk];
+      const __int128 f1 = to_fix(y.x), f2 = to_fix(y.y);
       s1 += f1;
       s2 += f2;
-      if (y.z != 0.0f) {
+      if (x.x != 0.0f) {
         s1b += f1;
         s2b += f2;
       }
@@ -1058,7 +1087,7 @@ PtStochResult pt_semistochastic(const Det2* dets, size_t n, const double* c_dev,
   PtArgs a;
   const size_t gsmem = pt_prepare(a, dets, n, c_dev, E0, eps2, ints, hb, maxEntry, sp, present, w, s);
   a.eps2L = eps2L;
-  a.nmcf = (double)nsample / (nsample - 1);
+  a.nmc = (double)nsample;
   DevBuf<int32_t> dlist;
   DevBuf<double> dw;
   dlist.resize((size_t)nsample);
