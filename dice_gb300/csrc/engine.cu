@@ -475,6 +475,59 @@ struct Context {
     return pt_last.e2;
   }
 
+  // getParityForDiceToAlphaBeta (SHCI/Determinants.cpp:691-706): the sign
+  // between Dice's interleaved spin-orbital order and all-alpha-then-beta:
+  // (-1)^(alpha electrons in higher orbitals) for every occupied beta orbital.
+  static double alpha_beta_parity(const uint64_t* w, int norb) {
+    auto occ = [&](int p) { return (w[p >> 6] >> (p & 63)) & 1ull; };
+    int nalpha = 0;
+    for (int k = 0; k < norb; ++k) nalpha += (int)occ(2 * k);
+    double parity = 1.0;
+    int before = 0;  // alpha electrons in orbitals below k
+    for (int k = 0; k < norb; ++k) {
+      if (occ(2 * k + 1)) {
+        const int after = nalpha - before - (int)occ(2 * k);
+        if (after % 2 == 1) parity = -parity;
+      }
+      before += (int)occ(2 * k);
+    }
+    return parity;
+  }
+
+  // writeBestDeterminants (SHCI/SHCI.cpp:465-506): the num largest |c| of a
+  // root as {int num, int norb, then per determinant the coefficient times
+  // the alpha-beta parity (double) and one character per spatial orbital,
+  // '0', 'a', 'b' or '2'}. Ties in |c| keep index order (the reference's
+  // std::sort leaves their order unspecified).
+  void write_best_dets(const double* c, int num, const std::string& path) {
+    require_dets();
+    std::vector<double> ch(ndet);
+    std::vector<uint64_t> dh(2 * ndet);
+    SHCI_CUDA(cudaMemcpyAsync(ch.data(), c, ndet * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    SHCI_CUDA(cudaMemcpyAsync(dh.data(), dets.p, ndet * sizeof(Det2), cudaMemcpyDeviceToHost, stream));
+    SHCI_CUDA(cudaStreamSynchronize(stream));
+    num = (int)std::min<size_t>((size_t)std::max(num, 0), ndet);
+    std::vector<size_t> idx(ndet);
+    std::iota(idx.begin(), idx.end(), 0);
+    std::stable_sort(idx.begin(), idx.end(), [&](size_t a, size_t b) { return std::fabs(ch[a]) > std::fabs(ch[b]); });
+    FILE* f = std::fopen(path.c_str(), "wb");
+    if (!f) throw Error(kErrIO, "cannot write " + path);
+    const int n = hints.norb;
+    bool ok = std::fwrite(&num, sizeof(int), 1, f) == 1 && std::fwrite(&n, sizeof(int), 1, f) == 1;
+    std::vector<char> occ(n);
+    for (int i = 0; ok && i < num; ++i) {
+      const size_t m = idx[i];
+      const uint64_t* w = &dh[2 * m];
+      const double coeff = alpha_beta_parity(w, n) * ch[m];
+      for (int k = 0; k < n; ++k) {
+        const bool a = (w[(2 * k) >> 6] >> ((2 * k) & 63)) & 1ull, b = (w[(2 * k + 1) >> 6] >> ((2 * k + 1) & 63)) & 1ull;
+        occ[k] = a ? (b ? '2' : 'a') : (b ? 'b' : '0');
+      }
+      ok = std::fwrite(&coeff, sizeof(double), 1, f) == 1 && std::fwrite(occ.data(), 1, n, f) == (size_t)n;
+    }
+    if (std::fclose(f) != 0 || !ok) throw Error(kErrIO, "error writing " + path);
+  }
+
   // Semistochastic PT2 (E0 with coreE) of the current space with
   // coefficients c (device, ndet entries); restrictions as in perturb().
   double perturb_stoch(const double* c, double E0, double eps2, double eps2L, int nsample, int max_iter,
@@ -1581,6 +1634,9 @@ int shci_run_input(shci_ctx* ctx, const char* input_path, const char* fcidump, i
     }
     std::vector<double> ev;
     c.run(s, mode, block != 0, ev);
+    for (int r = 0; s.writeBest > 0 && r < (int)ev.size(); ++r)
+      c.write_best_dets(c.ci.p + (size_t)r * c.ndet, s.writeBest,
+                        dir + (r == 0 ? std::string("/dets.bin") : "/dets_" + std::to_string(r) + ".bin"));
     if (nroots) *nroots = (int)ev.size();
     for (int r = 0; r < (int)ev.size() && r < cap_roots; ++r) E[r] = ev[r];
   });
@@ -1639,6 +1695,16 @@ int shci_pt_error(shci_ctx* ctx, double* stddev, int* iterations, double* e_larg
     if (stddev) *stddev = c.pts_last.stddev;
     if (iterations) *iterations = c.pts_last.iterations;
     if (e_large) *e_large = c.pts_last.e_large;
+  });
+}
+
+int shci_write_best_dets(shci_ctx* ctx, int root, int num, const char* path) {
+  return guarded(ctx, [&](Context& c) {
+    if (!path) throw Error(SHCI_ERR_INVALID, "null path");
+    if (c.Evar.empty() || c.nroots_run != (int)c.Evar.size())
+      throw Error(SHCI_ERR_STATE, "no variational run (call shci_run_input first)");
+    if (root < 0 || root >= c.nroots_run) throw Error(SHCI_ERR_INVALID, "root out of range");
+    c.write_best_dets(c.ci.p + (size_t)root * c.ndet, num, path);
   });
 }
 

@@ -201,7 +201,7 @@ void build_heatbath(const HostInts& H, HostHeatBath& hb) {
 // variational loop (perturbation theory, RDMs, I/O, restarts, SOC, cdfci).
 static const char* kIgnored[] = {
     "io", "noio", "prefix",
-    "printbestdeterminants", "printalldeterminants", "writebestdeterminants", "dordm", "DoOneRDM",
+    "printbestdeterminants", "printalldeterminants", "dordm", "DoOneRDM",
     "DoSpinOneRDM", "dospinrdm", "TransitionRDM", "DoThreeRDM", "DoFourRDM", "outputlevel",
     "num_thrds", "nblocks", "excitation", "nvirt", "extrapolate", "relaxedRDM", "quasiq", "dosoc",
     "dosocqdpt", "dogtensor", "socmultiplier", "doresponse", "onlyperturbative", "algorithm", "dolcc",
@@ -317,6 +317,9 @@ void read_input(const std::string& path, Schedule& s) {
     } else if (iequal(arg, "targetError")) {
       need(1);
       s.targetError = std::atof(tok[1].c_str());
+    } else if (iequal(arg, "writebestdeterminants")) {
+      need(1);
+      s.writeBest = std::atoi(tok[1].c_str());
     } else if (iequal(arg, "seed")) {
       need(1);
       s.seed = std::atoll(tok[1].c_str());

@@ -54,6 +54,7 @@ struct Schedule {
   int nPTiter = 1000000;
   double targetError = 1.e-4;
   long long seed = -1;
+  int writeBest = 0;  // writebestdeterminants (SHCI/input.cpp:243-244)
 };
 
 void split_tokens(const std::string& in, const char* delims, std::vector<std::string>& tok);

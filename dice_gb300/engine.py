@@ -70,6 +70,7 @@ SIGNATURES = [
     ("shci_pt_error", _i32, [_vp, _P(_dbl), _P(_i32), _P(_dbl)]),
     ("shci_ints_info", _i32, [_vp, _P(_i32), _P(_i32), _P(_dbl)]),
     ("shci_rdm", _i32, [_vp, _vp, _vp, _vp]),
+    ("shci_write_best_dets", _i32, [_vp, _i32, _i32, ctypes.c_char_p]),
     ("shci_run_rdm", _i32, [_vp, _i32, _vp, _vp]),
     ("shci_launch_count", _i32, [_vp, _P(_i64)]),
 ]
@@ -473,6 +474,10 @@ class Engine:
                 raise ValueError("ci must hold one coefficient per determinant")
             self._check(load_library().shci_rdm(self.h, _p(c), _p(s2), _p(s1)))
         return s2, s1
+
+    def write_best_dets(self, path, num, root=0):
+        """The reference's dets.bin (writeBestDeterminants) for root `root`."""
+        self._check(load_library().shci_write_best_dets(self.h, int(root), int(num), os.fspath(path).encode()))
 
     def launch_count(self):
         n = ctypes.c_int64()

@@ -264,6 +264,15 @@ int shci_set_pt_batch(shci_ctx* ctx, int64_t max_candidates);
 int shci_rdm(shci_ctx* ctx, const double* ci, double* s2, double* s1);
 int shci_run_rdm(shci_ctx* ctx, int root, double* s2, double* s1);
 
+/* writeBestDeterminants (SHCI/SHCI.cpp:465-506) for root `root` of the last
+ * shci_run_input: the file the reference names dets.bin (dets_<root>.bin for
+ * root > 0), for QMC codes: int num, int NORB, then for each of the num
+ * largest |c| the coefficient times getParityForDiceToAlphaBeta
+ * (SHCI/Determinants.cpp:691-706) as a double and NORB characters '0', 'a',
+ * 'b', '2'. Ties in |c| keep index order. shci_run_input writes these files
+ * into the input file's directory when the input sets writebestdeterminants. */
+int shci_write_best_dets(shci_ctx* ctx, int root, int num, const char* path);
+
 /* Stage timings of the last run in seconds: selection, Hamiltonian build,
  * Davidson, total; and the sigma calls/time spent inside Davidson. */
 int shci_run_timings(shci_ctx* ctx, double* t_select, double* t_ham, double* t_davidson, double* t_total,

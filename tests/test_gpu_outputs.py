@@ -1,0 +1,63 @@
+"""Files the reference writes for other programs, produced through the C-ABI.
+
+dets.bin (writebestdeterminants, SHCI/SHCI.cpp:465-506): the coefficients are
+multiplied by the reference's alpha-beta parity, which the h8_631g example's
+own `dets` listing (examples/h8_631g/dets, printed with the same parity) pins:
+every determinant's signed weight must match the listing up to the global
+sign of the eigenvector."""
+import os
+import struct
+
+import numpy as np
+import pytest
+
+from dice_gb300 import engine as eng
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _read_dets_bin(path):
+    raw = open(path, "rb").read()
+    num, norb = struct.unpack_from("ii", raw, 0)
+    off = 8
+    out = []
+    for _ in range(num):
+        (c,) = struct.unpack_from("d", raw, off)
+        s = raw[off + 8: off + 8 + norb].decode()
+        out.append((c, s))
+        off += 8 + norb
+    assert off == len(raw)
+    return num, norb, out
+
+
+def _occ_string(w, norb):
+    out = []
+    for k in range(norb):
+        a = (int(w[(2 * k) // 64]) >> ((2 * k) % 64)) & 1
+        b = (int(w[(2 * k + 1) // 64]) >> ((2 * k + 1) % 64)) & 1
+        out.append("2" if a and b else "a" if a else "b" if b else "0")
+    return "".join(out)
+
+
+def test_dets_bin_matches_reference_listing(golden):
+    inp = golden("h8_631g", "dice.dat")
+    with open(inp, "a") as f:
+        f.write("\nwritebestdeterminants 2470\n")
+    e = eng.Engine(0)
+    e.run_input(inp, mode="fp64")
+    path = os.path.join(os.path.dirname(inp), "dets.bin")
+    num, norb, rows = _read_dets_bin(path)
+    e.close()
+    assert num == 2470 and norb == 16
+    mags = [abs(c) for c, _ in rows]
+    assert all(mags[i] >= mags[i + 1] for i in range(len(mags) - 1))
+    ref = np.load(os.path.join(GOLDEN, "h8_631g_dets.npz"))
+    refw = {_occ_string(w, norb): c for w, c in zip(ref["dets"], ref["weights"])}
+    assert set(refw) == {s for _, s in rows}
+    ours = {s: c for c, s in rows}
+    sign = np.sign(ours[max(refw, key=lambda k: abs(refw[k]))]) * np.sign(refw[max(refw, key=lambda k: abs(refw[k]))])
+    diff = max(abs(sign * ours[s] - refw[s]) for s in refw)
+    print("largest signed-weight difference", diff)
+    assert diff < 1e-7
