@@ -563,6 +563,8 @@ struct Context {
     ensure_diag();
     if (is_direct(mode)) {
       H.drop_compressed();
+      H.perm.release();
+      H.spos.release();
       H.col.release();
       H.v64.release();
       H.vhi.release();
@@ -602,16 +604,16 @@ struct Context {
       const int kp = kk == 3 ? 4 : kk;
       if (mode == SHCI_MODE_MIXED) {
         xb32.reserve(N * kp);
-        pack_f32(A, lda, c0 + done, kk, kp, N, xb32.p, stream);
+        pack_f32(A, lda, c0 + done, kk, kp, N, xb32.p, stream, H.perm.p);
         sigma_csr_mixed(H, diag.p, xb32.p, kp, kk, Yp + (size_t)(yc0 + done) * ldy, ldy, stream);
       } else if (mode == SHCI_MODE_FP64) {
         xb64.reserve(N * kp);
         if (H.v64.p) {
-          pack_f64(A, lda, c0 + done, kk, kp, N, xb64.p, stream);
+          pack_f64(A, lda, c0 + done, kk, kp, N, xb64.p, stream, H.perm.p);
           sigma_csr_f64(H, diag.p, xb64.p, kp, kk, Yp + (size_t)(yc0 + done) * ldy, ldy, false, stream);
         } else {  // mixed-path matrix: float-float refinement sigma on head + tail
           float* xff = reinterpret_cast<float*>(xb64.p);
-          pack_ff(A, lda, c0 + done, kk, kp, N, xff, stream);
+          pack_ff(A, lda, c0 + done, kk, kp, N, xff, stream, H.perm.p);
           sigma_csr_ff(H, diag.p, xff, kp, A, lda, c0 + done, kk, Yp + (size_t)(yc0 + done) * ldy, ldy, stream);
         }
       } else if (mode == SHCI_MODE_DIRECT_MIXED) {  // FP32 matrix-free
@@ -1477,22 +1479,46 @@ int shci_ham_build(shci_ctx* ctx, int mode, int64_t* nnz) {
 int shci_ham_export(shci_ctx* ctx, int64_t* rowptr, int32_t* col, double* val) {
   return guarded(ctx, [&](Context& c) {
     if (!c.ham_ok || Context::is_direct(c.ham_mode)) throw Error(SHCI_ERR_STATE, "no stored Hamiltonian");
+    // the stored matrix is in storage order (sorted by alpha, then beta
+    // string); the export is in the determinant order of shci_dets_get with
+    // every row's columns ascending
     const size_t N = c.H.N, nnz = (size_t)c.H.nnz;
-    SHCI_CUDA(cudaMemcpyAsync(rowptr, c.H.rowptr.p, (N + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, c.stream));
+    std::vector<int64_t> rp(N + 1);
+    std::vector<int32_t> cl(nnz);
+    std::vector<double> v(nnz);
+    std::vector<uint32_t> perm(N), spos(N);
+    SHCI_CUDA(cudaMemcpyAsync(rp.data(), c.H.rowptr.p, (N + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, c.stream));
+    if (N) {
+      SHCI_CUDA(cudaMemcpyAsync(perm.data(), c.H.perm.p, N * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.stream));
+      SHCI_CUDA(cudaMemcpyAsync(spos.data(), c.H.spos.p, N * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.stream));
+    }
     if (nnz) {
-      SHCI_CUDA(cudaMemcpyAsync(col, c.H.col.p, nnz * sizeof(int32_t), cudaMemcpyDeviceToHost, c.stream));
+      SHCI_CUDA(cudaMemcpyAsync(cl.data(), c.H.col.p, nnz * sizeof(int32_t), cudaMemcpyDeviceToHost, c.stream));
       if (c.H.v64.p) {
-        SHCI_CUDA(cudaMemcpyAsync(val, c.H.v64.p, nnz * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        SHCI_CUDA(cudaMemcpyAsync(v.data(), c.H.v64.p, nnz * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
         SHCI_CUDA(cudaStreamSynchronize(c.stream));
       } else {
         std::vector<float> hi(nnz), lo(nnz);
         SHCI_CUDA(cudaMemcpyAsync(hi.data(), c.H.vhi.p, nnz * sizeof(float), cudaMemcpyDeviceToHost, c.stream));
         SHCI_CUDA(cudaMemcpyAsync(lo.data(), c.H.vlo.p, nnz * sizeof(float), cudaMemcpyDeviceToHost, c.stream));
         SHCI_CUDA(cudaStreamSynchronize(c.stream));
-        for (size_t i = 0; i < nnz; ++i) val[i] = (double)hi[i] + (double)lo[i];
+        for (size_t i = 0; i < nnz; ++i) v[i] = (double)hi[i] + (double)lo[i];
       }
     }
     SHCI_CUDA(cudaStreamSynchronize(c.stream));
+    rowptr[0] = 0;
+    for (size_t u = 0; u < N; ++u) rowptr[u + 1] = rowptr[u] + (rp[spos[u] + 1] - rp[spos[u]]);
+    std::vector<std::pair<int32_t, double>> row;
+    for (size_t u = 0; u < N; ++u) {
+      const int64_t p0 = rp[spos[u]], p1 = rp[spos[u] + 1];
+      row.clear();
+      for (int64_t p = p0; p < p1; ++p) row.emplace_back((int32_t)perm[cl[p]], v[p]);
+      std::sort(row.begin(), row.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+      for (size_t t = 0; t < row.size(); ++t) {
+        col[rowptr[u] + t] = row[t].first;
+        val[rowptr[u] + t] = row[t].second;
+      }
+    }
   });
 }
 
@@ -1537,13 +1563,20 @@ int shci_sigma_packed_device(shci_ctx* ctx, int mode, const void* x_packed, int 
     if (!c.ham_ok || Context::is_direct(c.ham_mode)) throw Error(SHCI_ERR_STATE, "no stored Hamiltonian");
     if (ld < (int64_t)c.ndet) throw Error(SHCI_ERR_INVALID, "leading dimension smaller than N");
     c.ensure_diag();
-    if (mode == SHCI_MODE_MIXED)
-      shci::sigma_csr_mixed(c.H, c.diag.p, static_cast<const float*>(x_packed), kp, k, y_dev, (size_t)ld, c.stream);
-    else if (mode == SHCI_MODE_FP64)
-      shci::sigma_csr_f64(c.H, c.diag.p, static_cast<const double*>(x_packed), kp, k, y_dev, (size_t)ld,
-                          c.H.v64.p == nullptr, c.stream);
-    else
+    // x_packed is in the determinant array's order: its rows are gathered
+    // into the stored Hamiltonian's storage order first
+    const size_t N = c.ndet;
+    if (mode == SHCI_MODE_MIXED) {
+      c.xb32.reserve(N * kp);
+      shci::gather_rows(x_packed, sizeof(float) * kp, c.H.perm.p, N, c.xb32.p, c.stream);
+      shci::sigma_csr_mixed(c.H, c.diag.p, c.xb32.p, kp, k, y_dev, (size_t)ld, c.stream);
+    } else if (mode == SHCI_MODE_FP64) {
+      c.xb64.reserve(N * kp);
+      shci::gather_rows(x_packed, sizeof(double) * kp, c.H.perm.p, N, c.xb64.p, c.stream);
+      shci::sigma_csr_f64(c.H, c.diag.p, c.xb64.p, kp, k, y_dev, (size_t)ld, c.H.v64.p == nullptr, c.stream);
+    } else {
       throw Error(SHCI_ERR_INVALID, "packed sigma supports the stored modes only");
+    }
   });
 }
 
@@ -1589,6 +1622,9 @@ int shci_sigma_bytes(shci_ctx* ctx, int mode, int k, int64_t* bytes) {
       b = nnz * 12 + 8 * (N + 1) + 8 * N + (int64_t)k * N * (8 + 8 + 8);
     else
       throw Error(SHCI_ERR_INVALID, "stored sigma modes only");
+    // the storage-order permutation read by the sigma kernel, and the gather
+    // of x into storage order (permutation, x read and written)
+    b += 8 * N + 2 * (int64_t)k * N * (mode == SHCI_MODE_MIXED ? 4 : 8);
     *bytes = b;
   });
 }

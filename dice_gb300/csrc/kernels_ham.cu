@@ -439,12 +439,14 @@ struct CountVisitor {
   __device__ void step(bool hit, uint32_t, bool) { c += hit; }
 };
 
-// Rows [row0, N); counts[I - row0] = number of off-diagonal connections.
+// Rows [row0, N); counts[slot(I)] = number of off-diagonal connections, where
+// slot(I) = slot[I] when a slot map is given (the storage position of a full
+// build), else I - row0.
 // order[k], k < N - row0: the rows [row0, N) in alpha-major order (rows of one
 // alpha string probe the same index sections; run together, they share them
 // in cache). Output positions stay indexed by the row.
 __global__ void k_ham_count(HelperView h, int64_t row0, const uint32_t* __restrict__ order,
-                            int64_t* __restrict__ counts) {
+                            const uint32_t* __restrict__ slot, int64_t* __restrict__ counts) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   const int64_t nr = (int64_t)h.N - row0;
@@ -455,7 +457,7 @@ __global__ void k_ham_count(HelperView h, int64_t row0, const uint32_t* __restri
     int64_t c = v.c;
 #pragma unroll
     for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(kFull, c, o);
-    if (lane == 0) counts[I - row0] = c;
+    if (lane == 0) counts[slot ? (int64_t)slot[I] : I - row0] = c;
   }
 }
 
@@ -469,6 +471,7 @@ __global__ void k_ham_count(HelperView h, int64_t row0, const uint32_t* __restri
 // runs on full warps and singles (an O(n_elec) sum) do not wait on doubles.
 struct EmitVisitor {
   const Det2* dets;
+  const uint32_t* cmap;  // determinant index -> storage column
   IntsView ints;
   Det2 dI;
   uint32_t I;
@@ -484,7 +487,7 @@ struct EmitVisitor {
   __device__ void store(int64_t q, uint32_t J) {
     const Det2 dJ = dets[J];
     const double hv = (J < I) ? hij_any(ints, dJ, dI) : hij_any(ints, dI, dJ);
-    col[q] = (int32_t)J;
+    col[q] = (int32_t)cmap[J];
     if (v64) v64[q] = hv;
     if (vhi) {
       const float hi = (float)hv;
@@ -527,8 +530,11 @@ struct EmitVisitor {
   }
 };
 
-// Rows [row0, N) into a CSR whose row pointers start at row row0.
+// Rows [row0, N) into a CSR whose row pointers are indexed by slot(I) (see
+// k_ham_count); columns are storage positions cmap[J].
 __global__ void __launch_bounds__(256, 4) k_ham_emit(HelperView h, int64_t row0, const uint32_t* __restrict__ order,
+                                                     const uint32_t* __restrict__ slot,
+                                                     const uint32_t* __restrict__ cmap,
                                                      const Det2* __restrict__ dets, IntsView ints,
                                                      const int64_t* __restrict__ rowptr, int32_t* __restrict__ col,
                                                      double* __restrict__ v64, float* __restrict__ vhi,
@@ -539,8 +545,8 @@ __global__ void __launch_bounds__(256, 4) k_ham_emit(HelperView h, int64_t row0,
   const int64_t nr = (int64_t)h.N - row0;
   for (int64_t k = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < nr; k += warps) {
     const int64_t I = order[k];
-    EmitVisitor v{dets, ints, dets[I], (uint32_t)I, rowptr[I - row0], col, v64, vhi, vlo, s_q[wib][0], s_q[wib][1],
-                  0, 0};
+    EmitVisitor v{dets, cmap, ints, dets[I], (uint32_t)I, rowptr[slot ? (int64_t)slot[I] : I - row0], col, v64, vhi,
+                  vlo, s_q[wib][0], s_q[wib][1], 0, 0};
     visit_row(h, (uint32_t)I, v);
     v.flush();
   }
@@ -803,9 +809,12 @@ __global__ void k_order_keys(const uint32_t* __restrict__ aidx, int64_t row0, in
   }
 }
 
-static int64_t emit_rows(const Helpers& hp, size_t row0, const Det2* dets, const IntsView& ints, DevBuf<int64_t>& rowptr,
-                         DevBuf<int32_t>& col, DevBuf<double>& v64, DevBuf<float>& vhi, DevBuf<float>& vlo,
-                         bool want64, bool want32, bool want_lo, Prims& pr, cudaStream_t s, PhaseTimer& pt) {
+// slot: storage position of each row (full build) or null (rows at I - row0);
+// cmap: determinant index -> storage column.
+static int64_t emit_rows(const Helpers& hp, size_t row0, const uint32_t* slot, const uint32_t* cmap,
+                         const Det2* dets, const IntsView& ints, DevBuf<int64_t>& rowptr, DevBuf<int32_t>& col,
+                         DevBuf<double>& v64, DevBuf<float>& vhi, DevBuf<float>& vlo, bool want64, bool want32,
+                         bool want_lo, Prims& pr, cudaStream_t s, PhaseTimer& pt) {
   const size_t N = hp.N, nr = N - row0;
   HelperView hv = hp.view();
   DevBuf<int64_t> counts;
@@ -822,7 +831,7 @@ static int64_t emit_rows(const Helpers& hp, size_t row0, const Det2* dets, const
   }
   const unsigned blocks = grid_for(nr * 32, 256, 152 * 16);
   if (nr) {
-    k_ham_count<<<blocks, 256, 0, s>>>(hv, (int64_t)row0, order.p, counts.p);
+    k_ham_count<<<blocks, 256, 0, s>>>(hv, (int64_t)row0, order.p, slot, counts.p);
     SHCI_LAUNCH_CHECK();
   }
   pt.mark("ham count");
@@ -838,8 +847,8 @@ static int64_t emit_rows(const Helpers& hp, size_t row0, const Det2* dets, const
   if (want32 && want_lo) vlo.resize(cap); else vlo.release();
   CsrVals v{col.p, want64 ? v64.p : nullptr, want32 ? vhi.p : nullptr, (want32 && want_lo) ? vlo.p : nullptr};
   if (nr) {
-    k_ham_emit<<<blocks, 256, 0, s>>>(hv, (int64_t)row0, order.p, dets, ints, rowptr.p, v.col, v.v64, v.vhi,
-                                      v.vlo);
+    k_ham_emit<<<blocks, 256, 0, s>>>(hv, (int64_t)row0, order.p, slot, cmap, dets, ints, rowptr.p, v.col, v.v64,
+                                      v.vhi, v.vlo);
     SHCI_LAUNCH_CHECK();
   }
   pt.mark("ham emit");
@@ -850,63 +859,151 @@ static int64_t emit_rows(const Helpers& hp, size_t row0, const Det2* dets, const
   return total;
 }
 
-// Incremental build helpers. New rows R >= n_old are emitted in full; their
-// entries with column C < n_old are the new columns of old row C (same value:
-// H_CR is evaluated with R, the higher index, as the ket in both places).
+// Storage order: the determinants sorted by (alpha string, beta string);
+// perm[i] = determinant at storage position i, spos = its inverse.
+__global__ void k_storage_keys(const uint64_t* __restrict__ astr, const uint64_t* __restrict__ bstr, size_t n,
+                               uint64_t* __restrict__ k0, uint64_t* __restrict__ k1, uint32_t* __restrict__ v) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    k0[i] = bstr[i];
+    k1[i] = astr[i];
+    v[i] = (uint32_t)i;
+  }
+}
+__global__ void k_invert(const uint32_t* __restrict__ perm, size_t n, uint32_t* __restrict__ inv) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    inv[perm[i]] = (uint32_t)i;
+}
+static void storage_order(const Helpers& hp, DevBuf<uint32_t>& perm, DevBuf<uint32_t>& spos, Prims& pr,
+                          cudaStream_t s) {
+  const size_t n = hp.N;
+  perm.resize(n > 0 ? n : 1);
+  spos.resize(n > 0 ? n : 1);
+  if (n == 0) return;
+  DevBuf<uint64_t> k0, k1;
+  k0.resize(n);
+  k1.resize(n);
+  k_storage_keys<<<grid_for(n, 256), 256, 0, s>>>(hp.astr.p, hp.bstr.p, n, k0.p, k1.p, perm.p);
+  SHCI_LAUNCH_CHECK();
+  sort_u128(k0.p, k1.p, perm.p, n, pr, s);
+  k_invert<<<grid_for(n, 256), 256, 0, s>>>(perm.p, n, spos.p);
+  SHCI_LAUNCH_CHECK();
+  SHCI_CUDA(cudaStreamSynchronize(s));  // k0, k1 are freed on return
+}
+
+// Incremental build helpers. The rows of the new determinants R >= n_old are
+// emitted in full (row R at R - n_old, columns in the new storage order);
+// their entries whose column is an old determinant C < n_old are the new
+// columns of old row C (same value: H_CR is evaluated with R, the higher
+// index, as the ket in both places).
 __global__ void k_delta_count(const int64_t* __restrict__ rp_new, size_t nr, const int32_t* __restrict__ col_new,
-                              int64_t n_old, unsigned long long* __restrict__ dcnt) {
+                              const uint32_t* __restrict__ perm, int64_t n_old, unsigned long long* __restrict__ dcnt) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < (int64_t)nr; r += warps)
     for (int64_t p = rp_new[r] + lane; p < rp_new[r + 1]; p += 32) {
-      const int32_t c = col_new[p];
-      if (c < n_old) atomicAdd(&dcnt[c], 1ull);
+      const uint32_t c = perm[col_new[p]];
+      if ((int64_t)c < n_old) atomicAdd(&dcnt[c], 1ull);
     }
 }
-__global__ void k_delta_fill(const int64_t* __restrict__ rp_new, size_t nr, CsrVals nv, int64_t n_old,
+// Delta row C (indexed by the determinant) receives storage column spos[n_old + r].
+__global__ void k_delta_fill(const int64_t* __restrict__ rp_new, size_t nr, CsrVals nv,
+                             const uint32_t* __restrict__ perm, const uint32_t* __restrict__ spos, int64_t n_old,
                              const int64_t* __restrict__ dptr, unsigned long long* __restrict__ dfill, CsrVals dv) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < (int64_t)nr; r += warps)
+  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < (int64_t)nr; r += warps) {
+    const int32_t me = (int32_t)spos[n_old + r];
     for (int64_t p = rp_new[r] + lane; p < rp_new[r + 1]; p += 32) {
-      const int32_t c = nv.col[p];
-      if (c >= n_old) continue;
+      const uint32_t c = perm[nv.col[p]];
+      if ((int64_t)c >= n_old) continue;
       const int64_t q = dptr[c] + (int64_t)atomicAdd(&dfill[c], 1ull);
-      dv.col[q] = (int32_t)(n_old + r);
+      dv.col[q] = me;
       if (dv.v64) dv.v64[q] = nv.v64[p];
       if (dv.vhi) dv.vhi[q] = nv.vhi[p];
       if (dv.vlo) dv.vlo[q] = nv.vlo[p];
     }
+  }
 }
-__global__ void k_merged_len(const int64_t* __restrict__ rp_old, const int64_t* __restrict__ dptr, int64_t n_old,
-                             const int64_t* __restrict__ rp_new, int64_t nr, int64_t* __restrict__ len) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_old + nr;
-       i += (int64_t)gridDim.x * blockDim.x)
-    len[i] = i < n_old ? (rp_old[i + 1] - rp_old[i]) + (dptr[i + 1] - dptr[i]) : rp_new[i - n_old + 1] - rp_new[i - n_old];
+// rel[o] = new storage position of the determinant at old storage position o.
+// Both orders sort by the same key, so rel is increasing.
+__global__ void k_relabel(const uint32_t* __restrict__ perm_old, const uint32_t* __restrict__ spos, int64_t n_old,
+                          uint32_t* __restrict__ rel) {
+  for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < n_old; o += (int64_t)gridDim.x * blockDim.x)
+    rel[o] = spos[perm_old[o]];
 }
-// Merged row I: old row I followed by its new columns (all larger than the
-// old ones, so the row stays sorted); rows >= n_old are copied from the new rows.
-__global__ void k_merge_rows(const int64_t* __restrict__ rp_old, CsrVals ov, const int64_t* __restrict__ dptr,
-                             CsrVals dv, const int64_t* __restrict__ rp_new, CsrVals nv, int64_t n_old, int64_t nr,
-                             const int64_t* __restrict__ rp, CsrVals out) {
+__global__ void k_merged_len(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ spos_old,
+                             const int64_t* __restrict__ rp_old, const int64_t* __restrict__ dptr, int64_t n_old,
+                             const int64_t* __restrict__ rp_new, int64_t N, int64_t* __restrict__ len) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t u = perm[i];
+    if (u < n_old) {
+      const int64_t o = spos_old[u];
+      len[i] = (rp_old[o + 1] - rp_old[o]) + (dptr[u + 1] - dptr[u]);
+    } else {
+      len[i] = rp_new[u - n_old + 1] - rp_new[u - n_old];
+    }
+  }
+}
+// number of entries of the sorted b[0, n) smaller than key
+__device__ __forceinline__ int64_t count_below(const int32_t* __restrict__ b, int64_t n, int32_t key) {
+  int64_t lo = 0, hi = n;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (b[mid] < key)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+// same over old columns a[0, n) read through the increasing relabelling rel
+__device__ __forceinline__ int64_t count_below_rel(const int32_t* __restrict__ a, int64_t n,
+                                                   const uint32_t* __restrict__ rel, int32_t key) {
+  int64_t lo = 0, hi = n;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if ((int32_t)rel[a[mid]] < key)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+// Merged row at storage position i, warp per row. An old determinant's row is
+// its old row with columns relabelled (still sorted) merged with its new
+// columns (sorted; disjoint from the old ones): every entry's output position
+// is its index in its own list plus the number of entries of the other list
+// below it. A new determinant's row is copied from the new rows.
+__global__ void k_merge_rows(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ spos_old,
+                             const int64_t* __restrict__ rp_old, CsrVals ov, const uint32_t* __restrict__ rel,
+                             const int64_t* __restrict__ dptr, CsrVals dv, const int64_t* __restrict__ rp_new,
+                             CsrVals nv, int64_t n_old, int64_t N, const int64_t* __restrict__ rp, CsrVals out) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  auto copy = [&](const CsrVals& src, int64_t s0, int64_t s1, int64_t d0) {
-    for (int64_t p = s0 + lane; p < s1; p += 32) {
-      const int64_t q = d0 + (p - s0);
-      out.col[q] = src.col[p];
-      if (out.v64) out.v64[q] = src.v64[p];
-      if (out.vhi) out.vhi[q] = src.vhi[p];
-      if (out.vlo) out.vlo[q] = src.vlo[p];
-    }
+  auto put = [&](const CsrVals& src, int64_t p, int64_t q, int32_t c) {
+    out.col[q] = c;
+    if (out.v64) out.v64[q] = src.v64[p];
+    if (out.vhi) out.vhi[q] = src.vhi[p];
+    if (out.vlo) out.vlo[q] = src.vlo[p];
   };
-  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n_old + nr; i += warps) {
+  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < N; i += warps) {
     const int64_t d = rp[i];
-    if (i < n_old) {
-      copy(ov, rp_old[i], rp_old[i + 1], d);
-      copy(dv, dptr[i], dptr[i + 1], d + (rp_old[i + 1] - rp_old[i]));
+    const int64_t u = perm[i];
+    if (u < n_old) {
+      const int64_t o = spos_old[u];
+      const int64_t a0 = rp_old[o], la = rp_old[o + 1] - a0;
+      const int64_t b0 = dptr[u], lb = dptr[u + 1] - b0;
+      for (int64_t t = lane; t < la; t += 32) {
+        const int32_t c = (int32_t)rel[ov.col[a0 + t]];
+        put(ov, a0 + t, d + t + count_below(dv.col + b0, lb, c), c);
+      }
+      for (int64_t t = lane; t < lb; t += 32) {
+        const int32_t c = dv.col[b0 + t];
+        put(dv, b0 + t, d + t + count_below_rel(ov.col + a0, la, rel, c), c);
+      }
     } else {
-      copy(nv, rp_new[i - n_old], rp_new[i - n_old + 1], d);
+      const int64_t s0 = rp_new[u - n_old], s1 = rp_new[u - n_old + 1];
+      for (int64_t p = s0 + lane; p < s1; p += 32) put(nv, p, d + (p - s0), nv.col[p]);
     }
   }
 }
@@ -915,28 +1012,35 @@ void build_ham_csr(const Helpers& hp, const Det2* dets, const IntsView& ints, Cs
                    bool want_lo, size_t n_old, Prims& pr, cudaStream_t s) {
   const size_t N = hp.N;
   PhaseTimer pt(s);
-  const bool incremental = n_old > 0 && n_old < N && H.N == n_old && (H.v64.p != nullptr) == want64 &&
-                           (H.vhi.p != nullptr) == want32 && (H.vlo.p != nullptr) == (want32 && want_lo);
+  const bool incremental = n_old > 0 && n_old < N && H.N == n_old && H.perm.n >= n_old &&
+                           (H.v64.p != nullptr) == want64 && (H.vhi.p != nullptr) == want32 &&
+                           (H.vlo.p != nullptr) == (want32 && want_lo);
   if (!incremental) {
     if (n_old == N && H.N == N) return;  // nothing new
-    H.nnz = emit_rows(hp, 0, dets, ints, H.rowptr, H.col, H.v64, H.vhi, H.vlo, want64, want32, want_lo, pr, s, pt);
+    storage_order(hp, H.perm, H.spos, pr, s);
+    pt.mark("ham storage order");
+    H.nnz = emit_rows(hp, 0, H.spos.p, H.spos.p, dets, ints, H.rowptr, H.col, H.v64, H.vhi, H.vlo, want64, want32,
+                      want_lo, pr, s, pt);
     H.N = N;
     SHCI_CUDA(cudaStreamSynchronize(s));
     return;
   }
   const size_t nr = N - n_old;
-  Csr Hn;  // rows n_old .. N-1
-  Hn.nnz = emit_rows(hp, n_old, dets, ints, Hn.rowptr, Hn.col, Hn.v64, Hn.vhi, Hn.vlo, want64, want32, want_lo, pr, s,
-                     pt);
+  DevBuf<uint32_t> perm, spos;
+  storage_order(hp, perm, spos, pr, s);
+  pt.mark("ham storage order");
+  Csr Hn;  // rows of the determinants n_old .. N-1
+  Hn.nnz = emit_rows(hp, n_old, nullptr, spos.p, dets, ints, Hn.rowptr, Hn.col, Hn.v64, Hn.vhi, Hn.vlo, want64,
+                     want32, want_lo, pr, s, pt);
   CsrVals nv{Hn.col.p, Hn.v64.p, Hn.vhi.p, Hn.vlo.p};
-  // new columns of the old rows
+  // new columns of the old rows, indexed by the old determinant
   DevBuf<unsigned long long> dcnt, dfill;
   dcnt.resize(n_old);
   dfill.resize(n_old);
   SHCI_CUDA(cudaMemsetAsync(dcnt.p, 0, n_old * sizeof(unsigned long long), s));
   SHCI_CUDA(cudaMemsetAsync(dfill.p, 0, n_old * sizeof(unsigned long long), s));
   const unsigned wblocks = grid_for(nr * 32, 256, 152 * 16);
-  k_delta_count<<<wblocks, 256, 0, s>>>(Hn.rowptr.p, nr, Hn.col.p, (int64_t)n_old, dcnt.p);
+  k_delta_count<<<wblocks, 256, 0, s>>>(Hn.rowptr.p, nr, Hn.col.p, perm.p, (int64_t)n_old, dcnt.p);
   SHCI_LAUNCH_CHECK();
   DevBuf<int64_t> dptr;
   dptr.resize(n_old + 1);
@@ -951,15 +1055,20 @@ void build_ham_csr(const Helpers& hp, const Det2* dets, const IntsView& ints, Cs
   if (want32) Hd.vhi.resize(dcap);
   if (want32 && want_lo) Hd.vlo.resize(dcap);
   CsrVals dv{Hd.col.p, Hd.v64.p, Hd.vhi.p, Hd.vlo.p};
-  k_delta_fill<<<wblocks, 256, 0, s>>>(Hn.rowptr.p, nr, nv, (int64_t)n_old, dptr.p, dfill.p, dv);
+  k_delta_fill<<<wblocks, 256, 0, s>>>(Hn.rowptr.p, nr, nv, perm.p, spos.p, (int64_t)n_old, dptr.p, dfill.p, dv);
   SHCI_LAUNCH_CHECK();
   sort_rows(dptr.p, n_old, dv, s);
   pt.mark("ham new columns");
-  // merge
+  // merge in the new storage order
+  DevBuf<uint32_t> rel;
+  rel.resize(n_old);
+  k_relabel<<<grid_for(n_old, 256), 256, 0, s>>>(H.perm.p, spos.p, (int64_t)n_old, rel.p);
+  SHCI_LAUNCH_CHECK();
   DevBuf<int64_t> len, rp;
   len.resize(N);
   rp.resize(N + 1);
-  k_merged_len<<<grid_for(N, 256), 256, 0, s>>>(H.rowptr.p, dptr.p, (int64_t)n_old, Hn.rowptr.p, (int64_t)nr, len.p);
+  k_merged_len<<<grid_for(N, 256), 256, 0, s>>>(perm.p, H.spos.p, H.rowptr.p, dptr.p, (int64_t)n_old, Hn.rowptr.p,
+                                                (int64_t)N, len.p);
   SHCI_LAUNCH_CHECK();
   int64_t total = 0;
   scan_exclusive_i64(len.p, rp.p, N, &total, pr, s);
@@ -972,8 +1081,8 @@ void build_ham_csr(const Helpers& hp, const Det2* dets, const IntsView& ints, Cs
   if (want32) M.vhi.resize(cap);
   if (want32 && want_lo) M.vlo.resize(cap);
   CsrVals ov{H.col.p, H.v64.p, H.vhi.p, H.vlo.p}, mv{M.col.p, M.v64.p, M.vhi.p, M.vlo.p};
-  k_merge_rows<<<grid_for(N * 32, 256, 152 * 16), 256, 0, s>>>(H.rowptr.p, ov, dptr.p, dv, Hn.rowptr.p, nv,
-                                                               (int64_t)n_old, (int64_t)nr, rp.p, mv);
+  k_merge_rows<<<grid_for(N * 32, 256, 152 * 16), 256, 0, s>>>(perm.p, H.spos.p, H.rowptr.p, ov, rel.p, dptr.p, dv,
+                                                               Hn.rowptr.p, nv, (int64_t)n_old, (int64_t)N, rp.p, mv);
   SHCI_LAUNCH_CHECK();
   SHCI_CUDA(cudaStreamSynchronize(s));
   H.rowptr.swap(rp);
@@ -981,6 +1090,8 @@ void build_ham_csr(const Helpers& hp, const Det2* dets, const IntsView& ints, Cs
   H.v64.swap(M.v64);
   H.vhi.swap(M.vhi);
   H.vlo.swap(M.vlo);
+  H.perm.swap(perm);
+  H.spos.swap(spos);
   H.N = N;
   H.nnz = total;
   pt.mark("ham merge");

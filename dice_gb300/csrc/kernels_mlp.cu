@@ -26,18 +26,22 @@ namespace shci {
 // teacher: s_i = sum_j h_ij^2 / (E - d_j) over stored row i. The reciprocals
 // 1 / (E - d_j) are formed once per determinant (a division per nonzero would
 // run on this GPU's slow FP64 divide path); the row sums run in FP32, ample
-// for a level shift that only scales the preconditioner.
+// for a level shift that only scales the preconditioner. The reciprocals are
+// laid out in the matrix's storage order (inv[j] belongs to determinant
+// perm[j]), the shifts in the determinant array's order.
 // ---------------------------------------------------------------------------
-__global__ void k_pt2_inverse(const double* __restrict__ diag, size_t N, double E, float* __restrict__ inv) {
+__global__ void k_pt2_inverse(const double* __restrict__ diag, const uint32_t* __restrict__ perm, size_t N, double E,
+                              float* __restrict__ inv) {
   for (size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < N; j += (size_t)gridDim.x * blockDim.x) {
-    const double den = E - diag[j];
+    const double den = E - diag[perm[j]];
     inv[j] = fabs(den) > 1e-8 ? (float)(1.0 / den) : 0.f;
   }
 }
 template <bool F64>
 __global__ void k_pt2_shift(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
                             const double* __restrict__ v64, const float* __restrict__ vhi,
-                            const float* __restrict__ inv, size_t N, double* __restrict__ s) {
+                            const float* __restrict__ inv, const uint32_t* __restrict__ perm, size_t N,
+                            double* __restrict__ s) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < (int64_t)N; r += warps) {
@@ -48,21 +52,22 @@ __global__ void k_pt2_shift(const int64_t* __restrict__ rowptr, const int32_t* _
     }
 #pragma unroll
     for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
-    if (lane == 0) s[r] = (double)acc;
+    if (lane == 0) s[perm[r]] = (double)acc;
   }
 }
 
 void pt2_shift(const Csr& H, const double* diag, double E, double* s, DevBuf<float>& inv, cudaStream_t st) {
   if (H.N == 0) return;
   inv.reserve(H.N);
-  k_pt2_inverse<<<(unsigned)std::min<size_t>((H.N + 255) / 256, 152 * 32), 256, 0, st>>>(diag, H.N, E, inv.p);
+  k_pt2_inverse<<<(unsigned)std::min<size_t>((H.N + 255) / 256, 152 * 32), 256, 0, st>>>(diag, H.perm.p, H.N, E,
+                                                                                       inv.p);
   SHCI_LAUNCH_CHECK();
   size_t blocks = (H.N * 32 + 255) / 256;
   if (blocks > 152 * 16) blocks = 152 * 16;
   if (H.v64.p)
-    k_pt2_shift<true><<<(unsigned)blocks, 256, 0, st>>>(H.rowptr.p, H.col.p, H.v64.p, nullptr, inv.p, H.N, s);
+    k_pt2_shift<true><<<(unsigned)blocks, 256, 0, st>>>(H.rowptr.p, H.col.p, H.v64.p, nullptr, inv.p, H.perm.p, H.N, s);
   else
-    k_pt2_shift<false><<<(unsigned)blocks, 256, 0, st>>>(H.rowptr.p, H.col.p, nullptr, H.vhi.p, inv.p, H.N, s);
+    k_pt2_shift<false><<<(unsigned)blocks, 256, 0, st>>>(H.rowptr.p, H.col.p, nullptr, H.vhi.p, inv.p, H.perm.p, H.N, s);
   SHCI_LAUNCH_CHECK();
 }
 

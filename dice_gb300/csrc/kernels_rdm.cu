@@ -20,7 +20,11 @@
 //   k_rdm_diag  thread per determinant; the diagonal elements ((IJ, IJ) and
 //               (IJ, JI)) and the 1-RDM diagonal accumulate in shared memory
 //               per block, then once per block into the global sums;
-//   k_rdm_off   warp per row, lanes over the row's connections J < I;
+//   k_rdm_off   warp per row, lanes over the row's connections J < I (rows
+//               and columns in the stored Hamiltonian's storage order: each
+//               connected pair is visited once, and its terms are symmetric
+//               in the two determinants, so the order does not change the
+//               sums);
 //   k_rdm_fin   fixed point -> FP64.
 #include "ham.h"
 
@@ -111,24 +115,27 @@ __global__ void __launch_bounds__(kRdmThreads) k_rdm_diag(const Det2* __restrict
 __global__ void __launch_bounds__(kRdmThreads) k_rdm_off(const Det2* __restrict__ dets,
                                                          const double* __restrict__ c, size_t N,
                                                          const int64_t* __restrict__ rowptr,
-                                                         const int32_t* __restrict__ col, int n,
+                                                         const int32_t* __restrict__ col,
+                                                         const uint32_t* __restrict__ perm, int n,
                                                          unsigned long long* __restrict__ s2,
                                                          unsigned long long* __restrict__ s1) {
   const int lane = threadIdx.x & 31;
   const size_t warps = ((size_t)gridDim.x * blockDim.x) >> 5;
   for (size_t I = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; I < N; I += warps) {
-    const Det2 di = dets[I];
-    const double cI = c[I];
+    const uint32_t dI = perm[I];
+    const Det2 di = dets[dI];
+    const double cI = c[dI];
     const int64_t p0 = rowptr[I], p1 = rowptr[I + 1];
     for (int64_t p = p0 + lane; p < p1; p += 32) {
       const int J = col[p];
       if ((size_t)J >= I) continue;
-      const Det2 dj = dets[J];
+      const uint32_t dJ = perm[J];
+      const Det2 dj = dets[dJ];
       // created: in J only; destroyed: in I only (getOrbDiff(Dets[J], Dets[I]))
       const uint64_t cr0 = dj.w0 & ~di.w0, cr1 = dj.w1 & ~di.w1;
       const uint64_t de0 = di.w0 & ~dj.w0, de1 = di.w1 & ~dj.w1;
       const int ncre = __popcll(cr0) + __popcll(cr1);
-      const long long v = __double2ll_rn(c[J] * cI * kRdmUnit);
+      const long long v = __double2ll_rn(c[dJ] * cI * kRdmUnit);
       int cre[2], des[2];
       {
         int k = 0;
@@ -192,8 +199,8 @@ void rdm_evaluate(const Det2* dets, const double* c, size_t N, const Csr& H, int
     SHCI_CUDA(cudaFuncSetAttribute(k_rdm_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_rdm_diag<<<grid_for(N, kRdmThreads, 152 * 4), kRdmThreads, smem, s>>>(dets, c, N, n, s2, s1);
     SHCI_LAUNCH_CHECK();
-    k_rdm_off<<<grid_for(N * 32, kRdmThreads, 152 * 16), kRdmThreads, 0, s>>>(dets, c, N, H.rowptr.p, H.col.p, n, s2,
-                                                                              s1);
+    k_rdm_off<<<grid_for(N * 32, kRdmThreads, 152 * 16), kRdmThreads, 0, s>>>(dets, c, N, H.rowptr.p, H.col.p, H.perm.p,
+                                                                              n, s2, s1);
     SHCI_LAUNCH_CHECK();
   }
   k_rdm_fin<<<grid_for(n4 + n2, 256), 256, 0, s>>>(fix.p, n4 + n2, out.p);

@@ -139,7 +139,8 @@ __global__ void __launch_bounds__(KP == 1 ? 1024 : 256) k_sigma_mixed(const int6
                                                      const int32_t* __restrict__ col,
                                                      const float* __restrict__ val, const double* __restrict__ diag,
                                                      const float* __restrict__ x, size_t N, int k,
-                                                     double* __restrict__ y, size_t ldy) {
+                                                     double* __restrict__ y, size_t ldy,
+                                                     const uint32_t* __restrict__ perm) {
   // The row loop is uniform per warp (rows past the slice run empty) so that
   // the width-VW shuffles below always see all 32 lanes.
   ROW_LOOP_BEGIN
@@ -179,10 +180,11 @@ __global__ void __launch_bounds__(KP == 1 ? 1024 : 256) k_sigma_mixed(const int6
       }
     }
     if (sub == 0 && live) {
-      const double dg = diag[r];
+      const size_t o = __ldg(perm + r);
+      const double dg = diag[o];
 #pragma unroll
       for (int c = 0; c < KP; ++c)
-        if (c < k) y[(size_t)c * ldy + r] = dg * (double)x[r * KP + c] + ((double)acc[c].s + (double)acc[c].c);
+        if (c < k) y[(size_t)c * ldy + o] = dg * (double)x[r * KP + c] + ((double)acc[c].s + (double)acc[c].c);
     }
   ROW_LOOP_END
 }
@@ -199,7 +201,8 @@ __global__ void __launch_bounds__(1024) k_sigma_mixed16(const int64_t* __restric
                                                         const int32_t* __restrict__ cbase,
                                                         const uint16_t* __restrict__ cdel,
                                                         const float* __restrict__ val, const double* __restrict__ diag,
-                                                        const float* __restrict__ x, size_t N, double* __restrict__ y) {
+                                                        const float* __restrict__ x, size_t N, double* __restrict__ y,
+                                                        const uint32_t* __restrict__ perm) {
   constexpr int KP = 1;
   const unsigned seg = VW == 32 ? kFull : (((1u << VW) - 1u) << (threadIdx.x & 31 & ~(VW - 1)));
   ROW_LOOP_BEGIN
@@ -248,7 +251,10 @@ __global__ void __launch_bounds__(1024) k_sigma_mixed16(const int64_t* __restric
         acc = other;
       }
     }
-    if (sub == 0 && live) y[r] = diag[r] * (double)x[r] + ((double)acc.s + (double)acc.c);
+    if (sub == 0 && live) {
+      const size_t o = __ldg(perm + r);
+      y[o] = diag[o] * (double)x[r] + ((double)acc.s + (double)acc.c);
+    }
   ROW_LOOP_END
 }
 
@@ -338,7 +344,8 @@ __global__ void __launch_bounds__(KP == 1 ? 1024 : 256) k_sigma_f64(const int64_
                                                    const double* __restrict__ v64, const float* __restrict__ vhi,
                                                    const float* __restrict__ vlo, const double* __restrict__ diag,
                                                    const double* __restrict__ x, size_t N, int k,
-                                                   double* __restrict__ y, size_t ldy) {
+                                                   double* __restrict__ y, size_t ldy,
+                                                   const uint32_t* __restrict__ perm) {
   ROW_LOOP_BEGIN
     double acc[KP];
 #pragma unroll
@@ -371,10 +378,11 @@ __global__ void __launch_bounds__(KP == 1 ? 1024 : 256) k_sigma_f64(const int64_
       for (int o = VW / 2; o; o >>= 1) acc[c] += __shfl_xor_sync(kFull, acc[c], o, VW);
     }
     if (sub == 0 && live) {
-      const double dg = diag[r];
+      const size_t o = __ldg(perm + r);
+      const double dg = diag[o];
 #pragma unroll
       for (int c = 0; c < KP; ++c)
-        if (c < k) y[(size_t)c * ldy + r] = dg * x[r * KP + c] + acc[c];
+        if (c < k) y[(size_t)c * ldy + o] = dg * x[r * KP + c] + acc[c];
     }
   ROW_LOOP_END
 }
@@ -434,7 +442,8 @@ __global__ void __launch_bounds__(KP == 1 ? 1024 : 256) k_sigma_ff(const int64_t
                                                   const float* __restrict__ vhi, const float* __restrict__ vlo,
                                                   const double* __restrict__ diag, const float* __restrict__ xff,
                                                   const double* __restrict__ xd, size_t ldx, int c0, size_t N, int k,
-                                                  double* __restrict__ y, size_t ldy) {
+                                                  double* __restrict__ y, size_t ldy,
+                                                  const uint32_t* __restrict__ perm) {
   // same row mapping as k_sigma_mixed
   ROW_LOOP_BEGIN
     Acc acc[KP];
@@ -470,11 +479,12 @@ __global__ void __launch_bounds__(KP == 1 ? 1024 : 256) k_sigma_ff(const int64_t
       }
     }
     if (sub == 0 && live) {
-      const double dg = diag[r];
+      const size_t o = __ldg(perm + r);
+      const double dg = diag[o];
 #pragma unroll
       for (int c = 0; c < KP; ++c)
         if (c < k)
-          y[(size_t)c * ldy + r] = dg * xd[(size_t)(c0 + c) * ldx + r] + ((double)acc[c].s + (double)acc[c].c);
+          y[(size_t)c * ldy + o] = dg * xd[(size_t)(c0 + c) * ldx + o] + ((double)acc[c].s + (double)acc[c].c);
     }
   ROW_LOOP_END
 }
@@ -513,10 +523,10 @@ static void launch_mixed(int vw, const Csr& H, const double* diag, const float* 
                          cudaStream_t s) {
   const SigmaLaunch L = sigma_launch(H.N, vw, KP);
   switch (vw) {
-    case 32: k_sigma_mixed<32, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, H.vhi.p, diag, x, H.N, k, y, ldy); break;
-    case 16: k_sigma_mixed<16, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, H.vhi.p, diag, x, H.N, k, y, ldy); break;
-    case 8: k_sigma_mixed<8, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, H.vhi.p, diag, x, H.N, k, y, ldy); break;
-    default: k_sigma_mixed<4, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, H.vhi.p, diag, x, H.N, k, y, ldy); break;
+    case 32: k_sigma_mixed<32, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, H.vhi.p, diag, x, H.N, k, y, ldy, H.perm.p); break;
+    case 16: k_sigma_mixed<16, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, H.vhi.p, diag, x, H.N, k, y, ldy, H.perm.p); break;
+    case 8: k_sigma_mixed<8, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, H.vhi.p, diag, x, H.N, k, y, ldy, H.perm.p); break;
+    default: k_sigma_mixed<4, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, H.vhi.p, diag, x, H.N, k, y, ldy, H.perm.p); break;
   }
   SHCI_LAUNCH_CHECK();
 }
@@ -529,10 +539,10 @@ void sigma_csr_mixed(const Csr& H, const double* diag, const float* x32, int kp,
   if (kp == 1 && H.cvalid) {
     const SigmaLaunch L = sigma_launch(H.N, vw, 1);
     switch (vw) {
-      case 32: k_sigma_mixed16<32><<<L.blocks, L.threads, 0, s>>>(H.crow.p, H.cbase.p, H.cdel.p, H.cval.p, diag, x32, H.N, y); break;
-      case 16: k_sigma_mixed16<16><<<L.blocks, L.threads, 0, s>>>(H.crow.p, H.cbase.p, H.cdel.p, H.cval.p, diag, x32, H.N, y); break;
-      case 8: k_sigma_mixed16<8><<<L.blocks, L.threads, 0, s>>>(H.crow.p, H.cbase.p, H.cdel.p, H.cval.p, diag, x32, H.N, y); break;
-      default: k_sigma_mixed16<4><<<L.blocks, L.threads, 0, s>>>(H.crow.p, H.cbase.p, H.cdel.p, H.cval.p, diag, x32, H.N, y); break;
+      case 32: k_sigma_mixed16<32><<<L.blocks, L.threads, 0, s>>>(H.crow.p, H.cbase.p, H.cdel.p, H.cval.p, diag, x32, H.N, y, H.perm.p); break;
+      case 16: k_sigma_mixed16<16><<<L.blocks, L.threads, 0, s>>>(H.crow.p, H.cbase.p, H.cdel.p, H.cval.p, diag, x32, H.N, y, H.perm.p); break;
+      case 8: k_sigma_mixed16<8><<<L.blocks, L.threads, 0, s>>>(H.crow.p, H.cbase.p, H.cdel.p, H.cval.p, diag, x32, H.N, y, H.perm.p); break;
+      default: k_sigma_mixed16<4><<<L.blocks, L.threads, 0, s>>>(H.crow.p, H.cbase.p, H.cdel.p, H.cval.p, diag, x32, H.N, y, H.perm.p); break;
     }
     SHCI_LAUNCH_CHECK();
     return;
@@ -552,10 +562,10 @@ static void launch_f64(int vw, const Csr& H, const double* diag, const double* x
   const double* v64 = H.v64.p;
   const float *vhi = H.vhi.p, *vlo = H.vlo.p;
   switch (vw) {
-    case 32: k_sigma_f64<32, KP, HILO><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, v64, vhi, vlo, diag, x, H.N, k, y, ldy); break;
-    case 16: k_sigma_f64<16, KP, HILO><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, v64, vhi, vlo, diag, x, H.N, k, y, ldy); break;
-    case 8: k_sigma_f64<8, KP, HILO><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, v64, vhi, vlo, diag, x, H.N, k, y, ldy); break;
-    default: k_sigma_f64<4, KP, HILO><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, v64, vhi, vlo, diag, x, H.N, k, y, ldy); break;
+    case 32: k_sigma_f64<32, KP, HILO><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, v64, vhi, vlo, diag, x, H.N, k, y, ldy, H.perm.p); break;
+    case 16: k_sigma_f64<16, KP, HILO><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, v64, vhi, vlo, diag, x, H.N, k, y, ldy, H.perm.p); break;
+    case 8: k_sigma_f64<8, KP, HILO><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, v64, vhi, vlo, diag, x, H.N, k, y, ldy, H.perm.p); break;
+    default: k_sigma_f64<4, KP, HILO><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, v64, vhi, vlo, diag, x, H.N, k, y, ldy, H.perm.p); break;
   }
   SHCI_LAUNCH_CHECK();
 }
@@ -589,10 +599,10 @@ static void launch_ff(int vw, const Csr& H, const double* diag, const float* xff
   const SigmaLaunch L = sigma_launch(H.N, vw, KP);
   const float *vhi = H.vhi.p, *vlo = H.vlo.p;
   switch (vw) {
-    case 32: k_sigma_ff<32, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, vhi, vlo, diag, xff, xd, ldx, c0, H.N, k, y, ldy); break;
-    case 16: k_sigma_ff<16, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, vhi, vlo, diag, xff, xd, ldx, c0, H.N, k, y, ldy); break;
-    case 8: k_sigma_ff<8, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, vhi, vlo, diag, xff, xd, ldx, c0, H.N, k, y, ldy); break;
-    default: k_sigma_ff<4, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, vhi, vlo, diag, xff, xd, ldx, c0, H.N, k, y, ldy); break;
+    case 32: k_sigma_ff<32, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, vhi, vlo, diag, xff, xd, ldx, c0, H.N, k, y, ldy, H.perm.p); break;
+    case 16: k_sigma_ff<16, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, vhi, vlo, diag, xff, xd, ldx, c0, H.N, k, y, ldy, H.perm.p); break;
+    case 8: k_sigma_ff<8, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, vhi, vlo, diag, xff, xd, ldx, c0, H.N, k, y, ldy, H.perm.p); break;
+    default: k_sigma_ff<4, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, vhi, vlo, diag, xff, xd, ldx, c0, H.N, k, y, ldy, H.perm.p); break;
   }
   SHCI_LAUNCH_CHECK();
 }
@@ -614,14 +624,18 @@ void sigma_csr_ff(const Csr& H, const double* diag, const float* xff, int kp, co
 // Packing between column-major FP64 blocks and row-interleaved vectors
 // ---------------------------------------------------------------------------
 __global__ void k_pack_f32(const double* __restrict__ A, size_t lda, int c0, int k, int kp, size_t N,
-                           float* __restrict__ out) {
-  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < N; r += (size_t)gridDim.x * blockDim.x)
-    for (int c = 0; c < kp; ++c) out[r * kp + c] = c < k ? (float)A[(size_t)(c0 + c) * lda + r] : 0.f;
+                           float* __restrict__ out, const uint32_t* __restrict__ perm) {
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < N; r += (size_t)gridDim.x * blockDim.x) {
+    const size_t src = perm ? (size_t)perm[r] : r;
+    for (int c = 0; c < kp; ++c) out[r * kp + c] = c < k ? (float)A[(size_t)(c0 + c) * lda + src] : 0.f;
+  }
 }
 __global__ void k_pack_f64(const double* __restrict__ A, size_t lda, int c0, int k, int kp, size_t N,
-                           double* __restrict__ out) {
-  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < N; r += (size_t)gridDim.x * blockDim.x)
-    for (int c = 0; c < kp; ++c) out[r * kp + c] = c < k ? A[(size_t)(c0 + c) * lda + r] : 0.0;
+                           double* __restrict__ out, const uint32_t* __restrict__ perm) {
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < N; r += (size_t)gridDim.x * blockDim.x) {
+    const size_t src = perm ? (size_t)perm[r] : r;
+    for (int c = 0; c < kp; ++c) out[r * kp + c] = c < k ? A[(size_t)(c0 + c) * lda + src] : 0.0;
+  }
 }
 __global__ void k_unpack_f64(const double* __restrict__ in, int kp, int k, size_t N, double* __restrict__ A,
                              size_t lda, int c0) {
@@ -629,28 +643,52 @@ __global__ void k_unpack_f64(const double* __restrict__ in, int kp, int k, size_
     for (int c = 0; c < k; ++c) A[(size_t)(c0 + c) * lda + r] = in[r * kp + c];
 }
 __global__ void k_pack_ff(const double* __restrict__ A, size_t lda, int c0, int k, int kp, size_t N,
-                          float2* __restrict__ out) {
+                          float2* __restrict__ out, const uint32_t* __restrict__ perm) {
   for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < N; r += (size_t)gridDim.x * blockDim.x)
     for (int c = 0; c < kp; ++c) {
       float2 v = make_float2(0.f, 0.f);
       if (c < k) {
-        const double x = A[(size_t)(c0 + c) * lda + r];
+        const double x = A[(size_t)(c0 + c) * lda + (perm ? (size_t)perm[r] : r)];
         v.x = __double2float_rn(x);
         v.y = __double2float_rn(x - (double)v.x);
       }
       out[r * kp + c] = v;
     }
 }
-void pack_ff(const double* A, size_t lda, int c0, int k, int kp, size_t N, float* out, cudaStream_t s) {
-  k_pack_ff<<<grid_for(N, 256), 256, 0, s>>>(A, lda, c0, k, kp, N, reinterpret_cast<float2*>(out));
+void pack_ff(const double* A, size_t lda, int c0, int k, int kp, size_t N, float* out, cudaStream_t s,
+             const uint32_t* perm) {
+  k_pack_ff<<<grid_for(N, 256), 256, 0, s>>>(A, lda, c0, k, kp, N, reinterpret_cast<float2*>(out), perm);
   SHCI_LAUNCH_CHECK();
 }
-void pack_f32(const double* A, size_t lda, int c0, int k, int kp, size_t N, float* out, cudaStream_t s) {
-  k_pack_f32<<<grid_for(N, 256), 256, 0, s>>>(A, lda, c0, k, kp, N, out);
+void pack_f32(const double* A, size_t lda, int c0, int k, int kp, size_t N, float* out, cudaStream_t s,
+              const uint32_t* perm) {
+  k_pack_f32<<<grid_for(N, 256), 256, 0, s>>>(A, lda, c0, k, kp, N, out, perm);
   SHCI_LAUNCH_CHECK();
 }
-void pack_f64(const double* A, size_t lda, int c0, int k, int kp, size_t N, double* out, cudaStream_t s) {
-  k_pack_f64<<<grid_for(N, 256), 256, 0, s>>>(A, lda, c0, k, kp, N, out);
+void pack_f64(const double* A, size_t lda, int c0, int k, int kp, size_t N, double* out, cudaStream_t s,
+              const uint32_t* perm) {
+  k_pack_f64<<<grid_for(N, 256), 256, 0, s>>>(A, lda, c0, k, kp, N, out, perm);
+  SHCI_LAUNCH_CHECK();
+}
+struct Row32 {
+  double2 a, b;
+};
+template <class T>
+__global__ void k_gather_rows(const T* __restrict__ in, const uint32_t* __restrict__ perm, size_t N,
+                              T* __restrict__ out) {
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < N; r += (size_t)gridDim.x * blockDim.x)
+    out[r] = in[perm[r]];
+}
+void gather_rows(const void* in, size_t bytes_per_row, const uint32_t* perm, size_t N, void* out, cudaStream_t s) {
+  if (N == 0) return;
+  const unsigned g = grid_for(N, 256);
+  switch (bytes_per_row) {
+    case 4: k_gather_rows<float><<<g, 256, 0, s>>>(static_cast<const float*>(in), perm, N, static_cast<float*>(out)); break;
+    case 8: k_gather_rows<double><<<g, 256, 0, s>>>(static_cast<const double*>(in), perm, N, static_cast<double*>(out)); break;
+    case 16: k_gather_rows<double2><<<g, 256, 0, s>>>(static_cast<const double2*>(in), perm, N, static_cast<double2*>(out)); break;
+    case 32: k_gather_rows<Row32><<<g, 256, 0, s>>>(static_cast<const Row32*>(in), perm, N, static_cast<Row32*>(out)); break;
+    default: throw Error(kErrInvalid, "gather_rows: row size must be 4, 8, 16 or 32 bytes");
+  }
   SHCI_LAUNCH_CHECK();
 }
 void unpack_f64(const double* in, int kp, int k, size_t N, double* A, size_t lda, int c0, cudaStream_t s) {
@@ -928,14 +966,14 @@ void sigma_noalloc(const Csr& H, const double* diag, int mode_mixed, const doubl
                                  std::to_string(kNoAllocPackBytes));
   void* scratch = noalloc_scratch();
   if (mode_mixed) {
-    pack_f32(x, ldx, 0, k, kp, N, static_cast<float*>(scratch), s);
+    pack_f32(x, ldx, 0, k, kp, N, static_cast<float*>(scratch), s, H.perm.p);
     sigma_csr_mixed(H, diag, static_cast<const float*>(scratch), kp, k, y, ldy, s);
   } else {
     if (H.v64.p) {
-      pack_f64(x, ldx, 0, k, kp, N, static_cast<double*>(scratch), s);
+      pack_f64(x, ldx, 0, k, kp, N, static_cast<double*>(scratch), s, H.perm.p);
       sigma_csr_f64(H, diag, static_cast<const double*>(scratch), kp, k, y, ldy, false, s);
     } else {  // head + tail values: float-float refinement sigma (same 8 bytes per entry)
-      pack_ff(x, ldx, 0, k, kp, N, static_cast<float*>(scratch), s);
+      pack_ff(x, ldx, 0, k, kp, N, static_cast<float*>(scratch), s, H.perm.p);
       sigma_csr_ff(H, diag, static_cast<const float*>(scratch), kp, x, ldx, 0, k, y, ldy, s);
     }
   }

@@ -136,8 +136,11 @@ int shci_sigma_device(shci_ctx* ctx, int mode, const double* x_dev, double* y_de
 
 /* Sigma on vectors already in the engine's gather layout: x_packed is
  * row-interleaved N x kp (kp = 1, 2 or 4; k <= kp columns used), FP32 for
- * SHCI_MODE_MIXED and FP64 for SHCI_MODE_FP64; y_dev column-major (ld).
- * Exactly one kernel launch on the context stream, no synchronisation.
+ * SHCI_MODE_MIXED and FP64 for SHCI_MODE_FP64, rows in the determinant order
+ * of shci_dets_get; y_dev column-major (ld), same order. Two kernel launches
+ * on the context stream, no synchronisation: the rows of x_packed gathered
+ * into the stored matrix's storage order (sorted by alpha, then beta string;
+ * a context buffer, allocated on first use), then the sigma kernel.
  * Replaces the inner product loop of Hmult2::operator() (SHCI/Hmult.h:108-123). */
 int shci_sigma_packed_device(shci_ctx* ctx, int mode, const void* x_packed, int kp, int k, double* y_dev,
                              int64_t ld);
@@ -162,10 +165,11 @@ int shci_sigma_device_noalloc(shci_ctx* ctx, int mode, const double* x_dev, doub
 /* Bytes of the stored Hamiltonian (row pointers, columns, values) and of the
  * string tables, for memory and roofline accounting. */
 int shci_ham_bytes(shci_ctx* ctx, int64_t* csr_bytes, int64_t* helper_bytes);
-/* Algorithmic bytes one stored-matrix sigma launch of k vectors streams in
- * the given mode for the current layout (matrix entries, row pointers,
- * diagonal, x read once, y written once): the numerator of its roofline. No
- * counterpart in the reference. */
+/* Algorithmic bytes one stored-matrix sigma call of k vectors
+ * (shci_sigma_packed_device) streams in the given mode for the current layout
+ * (matrix entries, row pointers, diagonal, x read once, y written once, the
+ * storage-order permutation, and the gather of x into storage order): the
+ * numerator of its roofline. No counterpart in the reference. */
 int shci_sigma_bytes(shci_ctx* ctx, int mode, int k, int64_t* bytes);
 
 /* Davidson. Replaces davidson / davidsonDirect (SHCI/Davidson.cpp:111-348,
