@@ -1272,6 +1272,7 @@ int guarded(shci_ctx* ctx, F&& f) {
   try {
     ctx->c.err.clear();
     cudaSetDevice(ctx->c.device);
+    shci::AllocStream scope(ctx->c.stream);  // this call's buffers: the device pool, in this stream's order
     f(ctx->c);
     return SHCI_OK;
   } catch (const Error& e) {
@@ -1321,6 +1322,10 @@ int shci_ctx_destroy(shci_ctx* ctx) {
   cudaSetDevice(ctx->c.device);
   cudaStreamSynchronize(ctx->c.stream);
   delete ctx;
+  try {
+    shci::release_pool_memory(nullptr);  // the context's memory back to the device
+  } catch (const std::exception&) {
+  }
   return SHCI_OK;
 }
 

@@ -45,8 +45,23 @@ struct PhaseTimer {
 // Device allocation cap (bytes) for out-of-memory emulation in tests; 0 = off.
 extern size_t g_alloc_cap;
 extern size_t g_alloc_live;
-void* dev_alloc(size_t bytes);
-void dev_free(void* p, size_t bytes);
+// Device memory. While a context's call runs on this thread (AllocStream
+// scope), buffers come from the device's stream-ordered memory pool on that
+// context's stream (cudaMallocAsync / cudaFreeAsync): a freed buffer goes back
+// to the pool in stream order and the next allocation reuses its pages, so the
+// multi-GB temporaries of each Hamiltonian build are not unmapped and mapped
+// again (cudaFree of tens of GB costs ~0.4 ms per GB and synchronises the
+// device). Outside such a scope, cudaMalloc / cudaFree. `pooled` records which.
+void* dev_alloc(size_t bytes, bool* pooled);
+void dev_free(void* p, size_t bytes, bool pooled);
+struct AllocStream {
+  cudaStream_t prev;
+  explicit AllocStream(cudaStream_t s);
+  ~AllocStream();
+};
+// Returns the pool's unused memory to the device (after the stream's pending
+// frees have completed), e.g. before sizing buffers from cudaMemGetInfo.
+void release_pool_memory(cudaStream_t s);
 
 // Owning device buffer.
 template <class T>
@@ -54,21 +69,23 @@ struct DevBuf {
   T* p = nullptr;
   size_t n = 0;    // elements in use
   size_t cap = 0;  // elements allocated
+  bool pooled = false;
   DevBuf() = default;
   DevBuf(const DevBuf&) = delete;
   DevBuf& operator=(const DevBuf&) = delete;
   ~DevBuf() { release(); }
   void release() {
-    if (p) dev_free(p, cap * sizeof(T));
+    if (p) dev_free(p, cap * sizeof(T), pooled);
     p = nullptr;
     n = cap = 0;
+    pooled = false;
   }
   // Ensure room for `count` elements; contents are not preserved.
   void reserve(size_t count) {
     if (count <= cap) return;
     release();
     size_t c = count < 16 ? 16 : count;
-    p = static_cast<T*>(dev_alloc(c * sizeof(T)));
+    p = static_cast<T*>(dev_alloc(c * sizeof(T), &pooled));
     cap = c;
   }
   void resize(size_t count) {
@@ -82,11 +99,13 @@ struct DevBuf {
       return;
     }
     size_t c = count + count / 2;
-    T* q = static_cast<T*>(dev_alloc(c * sizeof(T)));
+    bool qpooled = false;
+    T* q = static_cast<T*>(dev_alloc(c * sizeof(T), &qpooled));
     if (p && n) SHCI_CUDA(cudaMemcpyAsync(q, p, n * sizeof(T), cudaMemcpyDeviceToDevice, s));
     SHCI_CUDA(cudaStreamSynchronize(s));
-    if (p) dev_free(p, cap * sizeof(T));
+    if (p) dev_free(p, cap * sizeof(T), pooled);
     p = q;
+    pooled = qpooled;
     cap = c;
     n = count;
   }
@@ -95,6 +114,7 @@ struct DevBuf {
     std::swap(p, o.p);
     std::swap(n, o.n);
     std::swap(cap, o.cap);
+    std::swap(pooled, o.pooled);
   }
 };
 

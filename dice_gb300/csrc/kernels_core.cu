@@ -8,6 +8,7 @@
 // SortedDets in SHCI/SHCIgetdeterminants.cpp:676,727.
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 
 #include "engine.h"
 
@@ -16,21 +17,79 @@ namespace shci {
 size_t g_alloc_cap = 0;
 size_t g_alloc_live = 0;
 
-void* dev_alloc(size_t bytes) {
+namespace {
+thread_local cudaStream_t g_alloc_stream = nullptr;
+
+// The device's default pool keeps freed memory for reuse (no release at
+// stream synchronisation); set once per device.
+cudaMemPool_t device_pool() {
+  static std::mutex mu;
+  static cudaMemPool_t pools[64] = {nullptr};
+  int dev = 0;
+  SHCI_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) throw Error(kErrInvalid, "device index beyond 63");
+  std::lock_guard<std::mutex> lock(mu);
+  if (!pools[dev]) {
+    cudaMemPool_t pool = nullptr;
+    SHCI_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
+    uint64_t keep = ~0ull;
+    SHCI_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    pools[dev] = pool;
+  }
+  return pools[dev];
+}
+}  // namespace
+
+AllocStream::AllocStream(cudaStream_t s) : prev(g_alloc_stream) { g_alloc_stream = s; }
+AllocStream::~AllocStream() { g_alloc_stream = prev; }
+
+void release_pool_memory(cudaStream_t s) {
+  if (s) SHCI_CUDA(cudaStreamSynchronize(s));
+  SHCI_CUDA(cudaMemPoolTrimTo(device_pool(), 0));
+}
+
+void* dev_alloc(size_t bytes, bool* pooled) {
   if (g_alloc_cap && g_alloc_live + bytes > g_alloc_cap)
     throw Error(kErrOOM, "device allocation of " + std::to_string(bytes) + " bytes exceeds the configured cap");
   void* p = nullptr;
-  cudaError_t e = cudaMalloc(&p, bytes);
+  const cudaStream_t s = g_alloc_stream;
+  cudaError_t e;
+  if (s) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    SHCI_CUDA(cudaStreamIsCapturing(s, &cs));
+    if (cs != cudaStreamCaptureStatusNone) throw Error(kErrState, "device allocation inside a captured region");
+    device_pool();
+    e = cudaMallocAsync(&p, bytes, s);
+    if (e == cudaErrorMemoryAllocation) {  // give the pool's unused pages back, then once more
+      cudaGetLastError();
+      release_pool_memory(s);
+      e = cudaMallocAsync(&p, bytes, s);
+    }
+  } else {
+    e = cudaMalloc(&p, bytes);
+  }
   if (e != cudaSuccess) {
     cudaGetLastError();
     throw Error(e == cudaErrorMemoryAllocation ? kErrOOM : kErrCuda,
-                "cudaMalloc(" + std::to_string(bytes) + "): " + cudaGetErrorString(e));
+                std::string(s ? "cudaMallocAsync(" : "cudaMalloc(") + std::to_string(bytes) +
+                    "): " + cudaGetErrorString(e));
+  }
+  *pooled = s != nullptr;
+  if (reinterpret_cast<uintptr_t>(p) & 255u) {  // the vector loads of the kernels assume cudaMalloc's alignment
+    if (s)
+      cudaFreeAsync(p, s);
+    else
+      cudaFree(p);
+    throw Error(kErrCuda, "device allocation not 256-byte aligned");
   }
   g_alloc_live += bytes;
   return p;
 }
-void dev_free(void* p, size_t bytes) {
-  cudaFree(p);
+void dev_free(void* p, size_t bytes, bool pooled) {
+  if (pooled && g_alloc_stream)
+    cudaFreeAsync(p, g_alloc_stream);
+  else
+    cudaFree(p);
   g_alloc_live -= std::min(bytes, g_alloc_live);
 }
 

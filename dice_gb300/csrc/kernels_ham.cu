@@ -956,54 +956,106 @@ __device__ __forceinline__ int64_t count_below(const int32_t* __restrict__ b, in
   }
   return lo;
 }
-// same over old columns a[0, n) read through the increasing relabelling rel
-__device__ __forceinline__ int64_t count_below_rel(const int32_t* __restrict__ a, int64_t n,
-                                                   const uint32_t* __restrict__ rel, int32_t key) {
+// old_below[x] = number of old determinants (index < n_old) at storage
+// positions below x, from the exclusive scan of these flags.
+__global__ void k_old_flags(const uint32_t* __restrict__ perm, int64_t N, int64_t n_old, int64_t* __restrict__ f) {
+  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < N; x += (int64_t)gridDim.x * blockDim.x)
+    f[x] = (int64_t)perm[x] < n_old ? 1 : 0;
+}
+// number of entries of the sorted a[0, n) smaller than key (64-bit keys)
+__device__ __forceinline__ int64_t count_below_old(const int32_t* __restrict__ a, int64_t n, int64_t key) {
   int64_t lo = 0, hi = n;
   while (lo < hi) {
     const int64_t mid = (lo + hi) >> 1;
-    if ((int32_t)rel[a[mid]] < key)
+    if ((int64_t)a[mid] < key)
       lo = mid + 1;
     else
       hi = mid;
   }
   return lo;
 }
+
 // Merged row at storage position i, warp per row. An old determinant's row is
-// its old row with columns relabelled (still sorted) merged with its new
-// columns (sorted; disjoint from the old ones): every entry's output position
-// is its index in its own list plus the number of entries of the other list
-// below it. A new determinant's row is copied from the new rows.
-__global__ void k_merge_rows(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ spos_old,
-                             const int64_t* __restrict__ rp_old, CsrVals ov, const uint32_t* __restrict__ rel,
-                             const int64_t* __restrict__ dptr, CsrVals dv, const int64_t* __restrict__ rp_new,
-                             CsrVals nv, int64_t n_old, int64_t N, const int64_t* __restrict__ rp, CsrVals out) {
+// its old row A with columns relabelled (still sorted) merged with its new
+// columns B (sorted; disjoint from A): each entry goes to its index in its own
+// list plus the number of entries of the other list below it. For A[t] that is
+// a search of its new label in B (short, contiguous); for B[j] (a new
+// determinant at storage position x) the A entries below it are the old
+// determinants below x, old_below[x] of them in the old order, so it is a
+// search of old_below[x] in A's old labels -- no relabelling inside the
+// search. A new determinant's row is copied from the new rows.
+// VK: 0 = FP64 values, 1 = FP32 head + tail.
+template <int VK>
+struct MergeVal;
+template <>
+struct MergeVal<0> {
+  double v;
+  __device__ void load(const double* v64, const float*, const float*, int64_t p) { v = v64[p]; }
+  __device__ void store(double* v64, float*, float*, int64_t q) const { v64[q] = v; }
+};
+template <>
+struct MergeVal<1> {
+  float h, l;
+  __device__ void load(const double*, const float* hi, const float* lo, int64_t p) {
+    h = hi[p];
+    l = lo[p];
+  }
+  __device__ void store(double*, float* hi, float* lo, int64_t q) const {
+    hi[q] = h;
+    lo[q] = l;
+  }
+};
+template <int VK>
+__global__ void __launch_bounds__(256) k_merge_rows(const uint32_t* __restrict__ perm,
+                                                    const uint32_t* __restrict__ spos_old,
+                                                    const int64_t* __restrict__ rp_old, CsrVals ov,
+                                                    const uint32_t* __restrict__ rel,
+                                                    const int64_t* __restrict__ old_below,
+                                                    const int64_t* __restrict__ dptr, CsrVals dv,
+                                                    const int64_t* __restrict__ rp_new, CsrVals nv, int64_t n_old,
+                                                    int64_t N, const int64_t* __restrict__ rp, CsrVals out) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  auto put = [&](const CsrVals& src, int64_t p, int64_t q, int32_t c) {
-    out.col[q] = c;
-    if (out.v64) out.v64[q] = src.v64[p];
-    if (out.vhi) out.vhi[q] = src.vhi[p];
-    if (out.vlo) out.vlo[q] = src.vlo[p];
-  };
+  int32_t* __restrict__ ocol = out.col;
+  double* __restrict__ o64 = out.v64;
+  float* __restrict__ ohi = out.vhi;
+  float* __restrict__ olo = out.vlo;
   for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < N; i += warps) {
     const int64_t d = rp[i];
     const int64_t u = perm[i];
-    if (u < n_old) {
+    const bool old = u < n_old;
+    int64_t a0, la, b0 = 0, lb = 0;
+    if (old) {
       const int64_t o = spos_old[u];
-      const int64_t a0 = rp_old[o], la = rp_old[o + 1] - a0;
-      const int64_t b0 = dptr[u], lb = dptr[u + 1] - b0;
-      for (int64_t t = lane; t < la; t += 32) {
-        const int32_t c = (int32_t)rel[ov.col[a0 + t]];
-        put(ov, a0 + t, d + t + count_below(dv.col + b0, lb, c), c);
-      }
-      for (int64_t t = lane; t < lb; t += 32) {
-        const int32_t c = dv.col[b0 + t];
-        put(dv, b0 + t, d + t + count_below_rel(ov.col + a0, la, rel, c), c);
-      }
+      a0 = rp_old[o];
+      la = rp_old[o + 1] - a0;
+      b0 = dptr[u];
+      lb = dptr[u + 1] - b0;
     } else {
-      const int64_t s0 = rp_new[u - n_old], s1 = rp_new[u - n_old + 1];
-      for (int64_t p = s0 + lane; p < s1; p += 32) put(nv, p, d + (p - s0), nv.col[p]);
+      a0 = rp_new[u - n_old];
+      la = rp_new[u - n_old + 1] - a0;
+    }
+    const int32_t* __restrict__ acol = old ? ov.col : nv.col;
+    const double* __restrict__ a64 = old ? ov.v64 : nv.v64;
+    const float* __restrict__ ahi = old ? ov.vhi : nv.vhi;
+    const float* __restrict__ alo = old ? ov.vlo : nv.vlo;
+    const int32_t* __restrict__ bcol = dv.col + b0;
+    for (int64_t t = lane; t < la; t += 32) {
+      int32_t c = acol[a0 + t];
+      MergeVal<VK> v;
+      v.load(a64, ahi, alo, a0 + t);
+      if (old) c = (int32_t)rel[c];
+      const int64_t q = d + t + (lb ? count_below(bcol, lb, c) : 0);
+      ocol[q] = c;
+      v.store(o64, ohi, olo, q);
+    }
+    for (int64_t j = lane; j < lb; j += 32) {
+      const int32_t c = bcol[j];
+      const int64_t q = d + j + count_below_old(acol + a0, la, old_below[c]);
+      ocol[q] = c;
+      MergeVal<VK> w;
+      w.load(dv.v64, dv.vhi, dv.vlo, b0 + j);
+      w.store(o64, ohi, olo, q);
     }
   }
 }
@@ -1013,6 +1065,7 @@ void build_ham_csr(const Helpers& hp, const Det2* dets, const IntsView& ints, Cs
   const size_t N = hp.N;
   PhaseTimer pt(s);
   const bool incremental = n_old > 0 && n_old < N && H.N == n_old && H.perm.n >= n_old &&
+                           (want64 ? !want32 : (want32 && want_lo)) &&
                            (H.v64.p != nullptr) == want64 && (H.vhi.p != nullptr) == want32 &&
                            (H.vlo.p != nullptr) == (want32 && want_lo);
   if (!incremental) {
@@ -1064,6 +1117,15 @@ void build_ham_csr(const Helpers& hp, const Det2* dets, const IntsView& ints, Cs
   rel.resize(n_old);
   k_relabel<<<grid_for(n_old, 256), 256, 0, s>>>(H.perm.p, spos.p, (int64_t)n_old, rel.p);
   SHCI_LAUNCH_CHECK();
+  DevBuf<int64_t> oflag, old_below;
+  oflag.resize(N);
+  old_below.resize(N);
+  k_old_flags<<<grid_for(N, 256), 256, 0, s>>>(perm.p, (int64_t)N, (int64_t)n_old, oflag.p);
+  SHCI_LAUNCH_CHECK();
+  {
+    int64_t n_old_check = 0;
+    scan_exclusive_i64(oflag.p, old_below.p, N, &n_old_check, pr, s);
+  }
   DevBuf<int64_t> len, rp;
   len.resize(N);
   rp.resize(N + 1);
@@ -1081,8 +1143,14 @@ void build_ham_csr(const Helpers& hp, const Det2* dets, const IntsView& ints, Cs
   if (want32) M.vhi.resize(cap);
   if (want32 && want_lo) M.vlo.resize(cap);
   CsrVals ov{H.col.p, H.v64.p, H.vhi.p, H.vlo.p}, mv{M.col.p, M.v64.p, M.vhi.p, M.vlo.p};
-  k_merge_rows<<<grid_for(N * 32, 256, 152 * 16), 256, 0, s>>>(perm.p, H.spos.p, H.rowptr.p, ov, rel.p, dptr.p, dv,
-                                                               Hn.rowptr.p, nv, (int64_t)n_old, (int64_t)N, rp.p, mv);
+  if (want64)
+    k_merge_rows<0><<<grid_for(N * 32, 256, 152 * 16), 256, 0, s>>>(perm.p, H.spos.p, H.rowptr.p, ov, rel.p,
+                                                                    old_below.p, dptr.p, dv, Hn.rowptr.p, nv,
+                                                                    (int64_t)n_old, (int64_t)N, rp.p, mv);
+  else
+    k_merge_rows<1><<<grid_for(N * 32, 256, 152 * 16), 256, 0, s>>>(perm.p, H.spos.p, H.rowptr.p, ov, rel.p,
+                                                                    old_below.p, dptr.p, dv, Hn.rowptr.p, nv,
+                                                                    (int64_t)n_old, (int64_t)N, rp.p, mv);
   SHCI_LAUNCH_CHECK();
   SHCI_CUDA(cudaStreamSynchronize(s));
   H.rowptr.swap(rp);

@@ -951,6 +951,7 @@ PtResult pt_deterministic(const Det2* dets, size_t n, const double* c, double E0
   int64_t cap = max_candidates;
   if (cap <= 0) {
     size_t fr = 0, tot = 0;
+    release_pool_memory(s);  // freed buffers held for reuse count as free
     SHCI_CUDA(cudaMemGetInfo(&fr, &tot));
     size_t avail = fr;
     if (g_alloc_cap) avail = std::min(avail, g_alloc_cap > g_alloc_live ? g_alloc_cap - g_alloc_live : (size_t)0);
