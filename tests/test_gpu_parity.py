@@ -269,6 +269,52 @@ def test_errors_are_status_codes(gpu, tmp_path):
     e2.close()
 
 
+def test_allocation_failure_is_a_status_and_the_context_recovers(golden):
+    """A device allocation that fails (emulated by the allocation cap, which
+    the library checks before every device allocation) ends the call with
+    SHCI_ERR_OOM; once memory is available again the same context builds the
+    Hamiltonian and its sigma equals a fresh context's bit for bit."""
+    inp = golden("h8_631g", "dice.dat")
+    dets = np.load(os.path.join(GOLDEN, "h8_631g_dets.npz"))["dets"]
+    x = np.random.default_rng(3).standard_normal(len(dets))
+    e = eng.Engine(0)
+    e.read_fcidump(_fcidump(inp))
+    e.set_dets(dets)
+    e.set_alloc_cap(1)
+    try:
+        with pytest.raises(eng.ShciError) as ei:
+            e.ham_build("mixed")
+        assert ei.value.code == 4
+    finally:
+        e.set_alloc_cap(0)
+    nnz = e.ham_build("mixed")
+    y = e.sigma(x, "mixed")
+    f = eng.Engine(0)
+    f.read_fcidump(_fcidump(inp))
+    f.set_dets(dets)
+    assert f.ham_build("mixed") == nnz
+    assert np.array_equal(f.sigma(x, "mixed"), y)
+    e.close()
+    f.close()
+
+
+def test_closed_context_returns_its_memory(tmp_path):
+    """Buffers come from the device's stream-ordered pool, which keeps freed
+    memory for reuse while a context lives; closing the context hands it back
+    to the device (a multi-GB build leaves no footprint behind)."""
+    import torch
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    inp = synthetic.make_workload("mol24", str(tmp_path / "w"), schedule=[(0, 3e-3)], maxiter=2)
+    e = eng.Engine(0)
+    e.run_input(inp, mode="mixed")
+    csr, _ = e.ham_bytes()
+    assert csr > 100 * 2 ** 20
+    e.close()
+    free1 = torch.cuda.mem_get_info()[0]
+    assert free1 > free0 - 64 * 2 ** 20, (free0, free1, csr)
+
+
 def test_larger_davidson_subspace_same_energy_fewer_iterations(tmp_path):
     """shci_set_davidson_basis: a 16-vector subspace collapsed to 8 Ritz
     vectors converges every solve to the same tolerance in fewer iterations;
