@@ -54,6 +54,7 @@ def lib():
         L.orc_ham_build.argtypes = [vp, vp, i64]
         L.orc_ham_export.argtypes = [vp, vp, vp, vp]
         L.orc_sigma.argtypes = [vp, vp, vp]
+        L.orc_sigma_mt.argtypes = [vp, vp, vp, ctypes.c_int]
         L.orc_davidson.restype = i32
         L.orc_davidson.argtypes = [vp, vp, i32, vp, i32, dbl, i32, vp, ctypes.POINTER(i32)]
         L.orc_run_input.restype = i32
@@ -255,6 +256,13 @@ class Oracle:
         x = np.ascontiguousarray(x, dtype=np.float64)
         y = np.zeros_like(x)
         lib().orc_sigma(self.h, _p(x), _p(y))
+        return y
+
+    def sigma_mt(self, x, threads):
+        """The reference's rank-parallel Hmult2 with `threads` workers."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.zeros_like(x)
+        lib().orc_sigma_mt(self.h, _p(x), _p(y), int(threads))
         return y
 
     def davidson(self, x0, diag, max_copies, tol, direct=False):

@@ -32,6 +32,7 @@
 #include <numeric>
 #include <sstream>
 #include <string>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -1127,6 +1128,44 @@ static void sigma(const SparseHam& H, size_t N, const double* x, double* y) {
   for (size_t j = 0; j < N; j++) y[j] = yt[j];
 }
 
+// Hmult2::operator() (SHCI/Hmult.h:52-150), parallel branch for fewer than
+// 1e8 determinants: worker w of T owns the rows i with i % T == w (the
+// reference's MPI ranks own every size-th row), scatters symmetrically into a
+// private full-length ytemp, and the T vectors are summed in worker order (the
+// reference's MPI_Reduce into local rank 0). Threads stand in for the ranks of
+// one node.
+static void sigma_mt(const SparseHam& H, size_t N, const double* x, double* y, int T) {
+  if (T < 1) T = 1;
+  std::vector<std::vector<double>> yt(T);
+  std::vector<std::thread> pool;
+  for (int w = 0; w < T; ++w)
+    pool.emplace_back([&, w] {
+      std::vector<double>& t = yt[w];
+      t.assign(N, 0.0);
+      for (size_t i = (size_t)w; i < N; i += (size_t)T)
+        for (int64_t p = H.rowptr[i]; p < H.rowptr[i + 1]; ++p) {
+          const double h = H.val[p];
+          const int J = H.col[p];
+          t[i] += h * x[J];
+          if ((size_t)J != i) t[J] += h * x[i];
+        }
+    });
+  for (auto& th : pool) th.join();
+  // reduction, also split over the workers by ranges of the vector
+  pool.clear();
+  const size_t chunk = (N + T - 1) / T;
+  for (int w = 0; w < T; ++w)
+    pool.emplace_back([&, w] {
+      const size_t a = std::min(N, (size_t)w * chunk), b = std::min(N, a + chunk);
+      for (size_t j = a; j < b; ++j) {
+        double v = 0.0;
+        for (int r = 0; r < T; ++r) v += yt[r][j];
+        y[j] = v;
+      }
+    });
+  for (auto& th : pool) th.join();
+}
+
 // ---------------------------------------------------------------------------
 // Dense symmetric eigensolver (cyclic Jacobi) for the Davidson subspace. The
 // reference uses Eigen::SelfAdjointEigenSolver (SHCI/Davidson.cpp:262); both
@@ -1656,6 +1695,9 @@ void orc_ham_export(orc_ctx* c, int64_t* rowptr, int32_t* col, double* val) {
   std::copy(c->ham.val.begin(), c->ham.val.end(), val);
 }
 void orc_sigma(orc_ctx* c, const double* x, double* y) { sigma(c->ham, c->ham_n, x, y); }
+void orc_sigma_mt(orc_ctx* c, const double* x, double* y, int threads) {
+  sigma_mt(c->ham, c->ham_n, x, y, threads);
+}
 
 // Dice's Davidson on the last built Hamiltonian. x0: nroots x n (row major);
 // overwritten by the eigenvectors. Returns 0 or 1 (no convergence).

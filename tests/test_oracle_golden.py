@@ -276,3 +276,26 @@ def test_semistochastic_pt_is_unbiased():
         z.append((es - ed) / st["stddev"])
     print("z", np.round(z, 2))
     assert max(abs(v) for v in z) < 4 and abs(np.mean(z)) < 2.5
+
+
+def test_rank_parallel_sigma_equals_serial_sigma(golden):
+    """The reference's rank-parallel Hmult2 (every T-th row per worker, private
+    full-length accumulators, summed in worker order), which the reference arm
+    of the benchmark times on all host cores, gives the serial sigma up to the
+    order of the additions."""
+    inp = golden("h8_631g", "dice.dat")
+    dets = np.load(os.path.join(GOLDEN, "h8_631g_dets.npz"))["dets"]
+    o = orc.Oracle(os.path.join(os.path.dirname(inp), "FCIDUMP"))
+    rowptr, col, val = o.ham(dets)
+    x = np.random.default_rng(7).standard_normal(len(dets))
+    ref = o.sigma(x)
+    # the lower triangle as a dense check of the serial branch itself
+    dense = np.zeros((len(dets), len(dets)))
+    for i in range(len(dets)):
+        for p in range(rowptr[i], rowptr[i + 1]):
+            dense[i, col[p]] = dense[col[p], i] = val[p]
+    assert np.allclose(ref, dense @ x, rtol=1e-12, atol=1e-12 * np.abs(ref).max())
+    for threads in (1, 3, 8):
+        y = o.sigma_mt(x, threads)
+        assert np.allclose(y, ref, rtol=1e-12, atol=1e-13 * np.abs(ref).max()), threads
+    assert np.array_equal(o.sigma_mt(x, 1), ref)
