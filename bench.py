@@ -198,7 +198,8 @@ def run_reference(args):
                        "sample": sample},
             "cpu_baseline": {"value": val, "unit": "Mdets/s", "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": val, "unit": "Mdets/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "note": "Dice cannot be built here (needs Boost and MPI); the CPU oracle restating its serial path is timed"}
+            "note": "Dice cannot be built here (needs Boost and MPI); the CPU oracle restating its rank-parallel "
+                    "sigma is timed"}
     print(json.dumps(line), flush=True)
 
 
