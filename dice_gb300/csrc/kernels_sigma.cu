@@ -132,10 +132,14 @@ __device__ __forceinline__ void run_rows(const int64_t* __restrict__ rowptr, siz
 #define ROW_LOOP_END \
   }              \
   ;              \
-  run_rows<VW, KP == 1>(rowptr, N, row);
+  run_rows<VW, kBalWalk>(rowptr, N, row);
 
-template <int VW, int KP>
-__global__ void __launch_bounds__(KP == 1 ? 1024 : 256) k_sigma_mixed(const int64_t* __restrict__ rowptr,
+// FP32 sigma on int32 columns. One and two vectors walk balanced row ranges
+// (two 1024-thread blocks per SM); four vectors the grid-strided rows, which is
+// faster there (mol24, 2.91 M determinants: k = 2 10.8 ms balanced against
+// 12.6 ms strided; k = 4 20.6 ms against 16.9 ms).
+template <int VW, int KP, bool kBalWalk = (KP <= 2)>
+__global__ void __launch_bounds__(kBalWalk ? 1024 : 256) k_sigma_mixed(const int64_t* __restrict__ rowptr,
                                                      const int32_t* __restrict__ col,
                                                      const float* __restrict__ val, const double* __restrict__ diag,
                                                      const float* __restrict__ x, size_t N, int k,
@@ -204,6 +208,7 @@ __global__ void __launch_bounds__(1024) k_sigma_mixed16(const int64_t* __restric
                                                         const float* __restrict__ x, size_t N, double* __restrict__ y,
                                                         const uint32_t* __restrict__ perm) {
   constexpr int KP = 1;
+  constexpr bool kBalWalk = true;
   const unsigned seg = VW == 32 ? kFull : (((1u << VW) - 1u) << (threadIdx.x & 31 & ~(VW - 1)));
   ROW_LOOP_BEGIN
     Acc acc{0.f, 0.f};
@@ -346,6 +351,7 @@ __global__ void __launch_bounds__(KP == 1 ? 1024 : 256) k_sigma_f64(const int64_
                                                    const double* __restrict__ x, size_t N, int k,
                                                    double* __restrict__ y, size_t ldy,
                                                    const uint32_t* __restrict__ perm) {
+  constexpr bool kBalWalk = KP == 1;
   ROW_LOOP_BEGIN
     double acc[KP];
 #pragma unroll
@@ -444,7 +450,8 @@ __global__ void __launch_bounds__(KP == 1 ? 1024 : 256) k_sigma_ff(const int64_t
                                                   const double* __restrict__ xd, size_t ldx, int c0, size_t N, int k,
                                                   double* __restrict__ y, size_t ldy,
                                                   const uint32_t* __restrict__ perm) {
-  // same row mapping as k_sigma_mixed
+  // same row mapping as the FP64 kernel
+  constexpr bool kBalWalk = KP == 1;
   ROW_LOOP_BEGIN
     Acc acc[KP];
 #pragma unroll
@@ -521,7 +528,7 @@ static int pick_vw(const Csr& H) {
 template <int KP>
 static void launch_mixed(int vw, const Csr& H, const double* diag, const float* x, int k, double* y, size_t ldy,
                          cudaStream_t s) {
-  const SigmaLaunch L = sigma_launch(H.N, vw, KP);
+  const SigmaLaunch L = KP <= 2 ? sigma_launch(H.N, vw, 1) : sigma_launch(H.N, vw, KP);
   switch (vw) {
     case 32: k_sigma_mixed<32, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, H.vhi.p, diag, x, H.N, k, y, ldy, H.perm.p); break;
     case 16: k_sigma_mixed<16, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, H.vhi.p, diag, x, H.N, k, y, ldy, H.perm.p); break;
