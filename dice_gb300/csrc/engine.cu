@@ -25,6 +25,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdlib>
+#include <cstdio>
 #include <cstring>
 #include <memory>
 #include <numeric>
@@ -1104,6 +1105,70 @@ struct Context {
   }
 
   // ---- variational driver (SHCIbasics::DoVariational) -----------------------
+  // ---- checkpoints (writeVariationalResult / readVariationalResult,
+  // SHCI/SHCIbasics.cpp:1481-1590): the iteration, the determinants, the
+  // coefficients of every root and E0 (core energy excluded), in this
+  // library's own binary layout (the reference writes Boost archives).
+  static constexpr char kChkMagic[8] = {'S', 'H', 'C', 'I', 'G', 'P', 'U', '1'};
+  static std::string checkpoint_path(const Schedule& s) {
+    std::string dir = s.prefix.empty() ? std::string(".") : s.prefix;
+    if (dir[0] != '/') dir = s.baseDir + "/" + dir;
+    return dir + "/shci_gpu-variational.chk";
+  }
+  void write_checkpoint(const std::string& path, int iter, int nroots, const std::vector<double>& E0) {
+    std::vector<uint64_t> hd(2 * ndet);
+    std::vector<double> hc((size_t)nroots * ndet);
+    SHCI_CUDA(cudaMemcpyAsync(hd.data(), dets.p, ndet * sizeof(Det2), cudaMemcpyDeviceToHost, stream));
+    SHCI_CUDA(cudaMemcpyAsync(hc.data(), ci.p, hc.size() * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    SHCI_CUDA(cudaStreamSynchronize(stream));
+    std::FILE* f = std::fopen(path.c_str(), "wb");
+    if (!f) throw Error(kErrIO, "cannot write checkpoint " + path);
+    const int32_t head[4] = {1, iter, 1, nroots};  // version, iteration, converged (as the reference saves it), roots
+    const int64_t n = (int64_t)ndet;
+    const int32_t norb = hints.norb;
+    bool ok = std::fwrite(kChkMagic, 1, 8, f) == 8 && std::fwrite(head, sizeof(head), 1, f) == 1 &&
+              std::fwrite(&n, sizeof(n), 1, f) == 1 && std::fwrite(&norb, sizeof(norb), 1, f) == 1 &&
+              std::fwrite(hd.data(), sizeof(uint64_t), hd.size(), f) == hd.size() &&
+              std::fwrite(hc.data(), sizeof(double), hc.size(), f) == hc.size() &&
+              std::fwrite(E0.data(), sizeof(double), (size_t)nroots, f) == (size_t)nroots;
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok) throw Error(kErrIO, "failed writing checkpoint " + path);
+  }
+  // Loads the space and coefficients; returns the saved iteration.
+  int read_checkpoint(const std::string& path, int nroots, bool& converged, std::vector<double>& E0) {
+    std::FILE* f = std::fopen(path.c_str(), "rb");
+    if (!f) throw Error(kErrIO, "cannot open checkpoint " + path + " (restart needs the files of an earlier run)");
+    char magic[8];
+    int32_t head[4];
+    int64_t n = 0;
+    int32_t norb = 0;
+    bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, kChkMagic, 8) == 0 &&
+              std::fread(head, sizeof(head), 1, f) == 1 && std::fread(&n, sizeof(n), 1, f) == 1 &&
+              std::fread(&norb, sizeof(norb), 1, f) == 1 && head[0] == 1 && n > 0 && n < ((int64_t)1 << 31);
+    if (ok && (norb != hints.norb || head[3] != nroots)) {
+      std::fclose(f);
+      throw Error(kErrInvalid, "checkpoint " + path + " was written for another system or number of roots");
+    }
+    std::vector<uint64_t> hd;
+    std::vector<double> hc;
+    if (ok) {
+      hd.resize(2 * (size_t)n);
+      hc.resize((size_t)nroots * (size_t)n);
+      E0.assign(nroots, 0.0);
+      ok = std::fread(hd.data(), sizeof(uint64_t), hd.size(), f) == hd.size() &&
+           std::fread(hc.data(), sizeof(double), hc.size(), f) == hc.size() &&
+           std::fread(E0.data(), sizeof(double), (size_t)nroots, f) == (size_t)nroots;
+    }
+    std::fclose(f);
+    if (!ok) throw Error(kErrIO, "checkpoint " + path + " is not a complete checkpoint of this library");
+    set_dets(hd.data(), n);
+    ci.resize(hc.size());
+    SHCI_CUDA(cudaMemcpyAsync(ci.p, hc.data(), hc.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
+    SHCI_CUDA(cudaStreamSynchronize(stream));
+    converged = head[2] != 0;
+    return head[1];
+  }
+
   void run(const Schedule& s, int mode, bool block, std::vector<double>& Eout) {
     require_ints();
     const double t0 = now_s();
@@ -1193,8 +1258,18 @@ struct Context {
       SHCI_CUDA(cudaMemcpyAsync(ci.p, c0.data(), c0.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
     }
     std::vector<double> E0(nroots, 0.0);
+    const std::string chk = checkpoint_path(s);
+    size_t iterstart = 0;
+    if (s.restart) {  // SHCI/SHCIbasics.cpp:871-943
+      bool converged = false;
+      const int saved = read_checkpoint(chk, nroots, converged, E0);
+      iterstart = s.restart == 2 ? 0 : (size_t)saved + 1;
+      if (s.restart == 1 && converged && saved >= 0 && (size_t)saved < s.epsilon1.size() &&
+          s.epsilon1[saved] <= s.epsilon1.back())
+        iterstart = s.epsilon1.size();  // converged at the final threshold: nothing left to iterate
+    }
     DevBuf<double> X0;
-    for (size_t iter = 0; iter < s.epsilon1.size(); ++iter) {
+    for (size_t iter = iterstart; iter < s.epsilon1.size(); ++iter) {
       const double eps1 = s.epsilon1[iter];
       const size_t N0 = ndet;
       double ta = now_s();
@@ -1239,8 +1314,10 @@ struct Context {
                  s.direct, E0, numIter, E0[0]);
         total_dav_iters += numIter;
         t_dav += now_s() - t1;
+        if (s.io) write_checkpoint(chk, (int)iter, nroots, E0);
         break;
       }
+      if (s.io) write_checkpoint(chk, (int)iter, nroots, E0);
     }
     Eout.resize(nroots);
     for (int r = 0; r < nroots; ++r) Eout[r] = E0[r] + hints.coreE;
@@ -1662,6 +1739,7 @@ int shci_run_input(shci_ctx* ctx, const char* input_path, const char* fcidump, i
     std::string dir = input_path;
     size_t slash = dir.find_last_of('/');
     dir = slash == std::string::npos ? std::string(".") : dir.substr(0, slash);
+    s.baseDir = dir;
     std::string fd = fcidump ? std::string(fcidump)
                              : (s.integralFile.size() && s.integralFile[0] == '/' ? s.integralFile
                                                                                    : dir + "/" + s.integralFile);

@@ -198,19 +198,15 @@ void build_heatbath(const HostInts& H, HostHeatBath& hb) {
 }
 
 // Keywords accepted and ignored: they configure stages outside the
-// variational loop (perturbation theory, RDMs, I/O, restarts, SOC, cdfci).
+// variational loop (RDM variants, printing, SOC, cdfci, time reversal).
 static const char* kIgnored[] = {
-    "io", "noio", "prefix",
     "printbestdeterminants", "printalldeterminants", "dordm", "DoOneRDM",
     "DoSpinOneRDM", "dospinrdm", "TransitionRDM", "DoThreeRDM", "DoFourRDM", "outputlevel",
     "num_thrds", "nblocks", "excitation", "nvirt", "extrapolate", "relaxedRDM", "quasiq", "dosoc",
     "dosocqdpt", "dogtensor", "socmultiplier", "doresponse", "onlyperturbative", "algorithm", "dolcc",
     "pointGroup", "spin", "irrep", "searchForLowestEnergyDet", "cdfciTol", "cdfciIter", "cdfciOn",
     "reportInterval", "z_threshold", "cdfciSample", "eps", "maxseniority", "maxexcitation", "SenioAndExc",
-    "diskdavidson", "Treversal",
-    // no checkpoint files are kept: a restart runs the whole schedule, which
-    // reaches the same variational space as the reference's resumed run
-    "restart", "fullrestart"};
+    "diskdavidson", "Treversal"};
 
 void read_input(const std::string& path, Schedule& s) {
   std::ifstream ifs(path.c_str());
@@ -317,6 +313,17 @@ void read_input(const std::string& path, Schedule& s) {
     } else if (iequal(arg, "targetError")) {
       need(1);
       s.targetError = std::atof(tok[1].c_str());
+    } else if (iequal(arg, "io")) {
+      s.io = true;
+    } else if (iequal(arg, "noio")) {
+      s.io = false;
+    } else if (iequal(arg, "restart")) {
+      s.restart = 1;
+    } else if (iequal(arg, "fullrestart")) {
+      s.restart = 2;
+    } else if (iequal(arg, "prefix")) {
+      need(1);
+      s.prefix = tok[1];
     } else if (iequal(arg, "writebestdeterminants")) {
       need(1);
       s.writeBest = std::atoi(tok[1].c_str());

@@ -55,6 +55,15 @@ struct Schedule {
   double targetError = 1.e-4;
   long long seed = -1;
   int writeBest = 0;  // writebestdeterminants (SHCI/input.cpp:243-244)
+  // checkpoints (SHCI/input.cpp:72, 176-183, 330-331, 400): io writes the
+  // variational result after every iteration (default), noio does not;
+  // restart = 1 resumes after the saved iteration, 2 (fullrestart) reruns the
+  // schedule from the saved space; prefix is the checkpoint directory (a
+  // relative prefix is taken relative to baseDir, the input file's directory)
+  bool io = true;
+  int restart = 0;
+  std::string prefix = ".";
+  std::string baseDir = ".";
 };
 
 void split_tokens(const std::string& in, const char* delims, std::vector<std::string>& tok);

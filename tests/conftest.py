@@ -29,9 +29,9 @@ def golden_case(tmp_path, name, input_name):
     # inputs name their integral file relative to their own directory; the
     # fixture's FCIDUMP sits beside the unpacked input
     text = re.sub(r"(?im)^(\s*orbitals)\s+\S+", r"\1 FCIDUMP", text)
-    with open(d / "input.dat", "w") as f:
+    with open(d / input_name, "w") as f:
         f.write(text)
-    return str(d / "input.dat")
+    return str(d / input_name)
 
 
 @pytest.fixture

@@ -7,7 +7,8 @@ What is copied, and what it pins:
   * examples/h8_631g: FCIDUMP, dice.dat, the per-iteration table of dice.out
     (determinant counts, energies, Davidson iterations) and the final
     determinant set from the `dets` listing (2470 determinants with weights).
-  * tests/SHCI/restart: FCIDUMP and input3.dat; trusted_hci.e holds E_var of
+  * tests/SHCI/restart: FCIDUMP, input2.dat (io run) and input3.dat (restart);
+    trusted_hci.e holds E_var of
     the eps1 schedule 5e-3 -> 1e-3 -> 5e-5.
   * tests/SHCI/n2_RAS: FCIDUMP, input.dat (with an occupation restriction),
     trusted_hci.e (E_var).
@@ -88,6 +89,7 @@ def main(ref):
     rs = os.path.join(ref, "tests", "SHCI", "restart")
     gz(os.path.join(rs, "FCIDUMP"), os.path.join(HERE, "restart.FCIDUMP.gz"))
     shutil.copy(os.path.join(rs, "input3.dat"), os.path.join(HERE, "restart.input3.dat"))
+    shutil.copy(os.path.join(rs, "input2.dat"), os.path.join(HERE, "restart.input2.dat"))
     out["restart"] = {"E_var": read_e(os.path.join(rs, "trusted_hci.e")), "tol": 5e-5,
                       "source": "tests/SHCI/restart/trusted_hci.e (runTests.sh tolerance 5e-5)"}
 

@@ -63,3 +63,60 @@ def test_dets_bin_matches_reference_listing(golden):
     bad = [s for s in refw if abs(sign * ours[s] - refw[s]) > 1e-6 * abs(refw[s]) + 2e-9]
     print("signed weights off the listing:", len(bad))
     assert not bad
+
+
+def _h8_input(golden, name, schedule, maxiter, extra):
+    """The h8 example's input with another schedule, io on and extra keywords."""
+    src = golden("h8_631g", "dice.dat")
+    text = open(src).read()
+    text = text.replace("schedule\n0 1e-6\nend", "schedule\n%s\nend" % schedule)
+    text = text.replace("noio", "io").replace("maxiter 12", "maxiter %d" % maxiter)
+    assert "io\n" in text and ("maxiter %d" % maxiter) in text
+    path = os.path.join(os.path.dirname(src), name)
+    with open(path, "w") as f:
+        f.write(text + "".join(k + "\n" for k in extra))
+    return path
+
+
+def test_checkpoint_restart_and_fullrestart(golden):
+    """io writes the variational result after every iteration
+    (writeVariationalResult); restart resumes after the saved iteration, or
+    ends at once when the saved iteration already used the final threshold;
+    fullrestart reruns the schedule from the saved space
+    (SHCI/SHCIbasics.cpp:871-943)."""
+    sched = "0 1e-4\n2 1e-6"
+    full = _h8_input(golden, "full.dat", sched, 12, ())
+    e = eng.Engine(0)
+    E_full = e.run_input(full, mode="fp64")[0]
+    dets_full = e.dets()
+    e.close()
+    chk = os.path.join(os.path.dirname(full), "shci_gpu-variational.chk")
+    assert os.path.exists(chk)
+
+    # the saved iteration is the converged last one: restart does no iteration
+    r = eng.Engine(0)
+    E_r = r.run_input(_h8_input(golden, "restart.dat", sched, 12, ("restart",)), mode="fp64")[0]
+    assert E_r == E_full
+    assert np.array_equal(r.dets(), dets_full)
+    assert len(r.run_log()["ndets"]) == 0
+    r.close()
+
+    # fullrestart from the converged space: the schedule again from there
+    f = eng.Engine(0)
+    E_f = f.run_input(_h8_input(golden, "fullrestart.dat", sched, 12, ("fullrestart",)), mode="fp64")[0]
+    assert abs(E_f - E_full) < 1e-8
+    assert set(map(tuple, f.dets().tolist())) == set(map(tuple, dets_full.tolist()))
+    f.close()
+
+    # stop after the two eps1 = 1e-4 iterations, then resume at iteration 2
+    t = eng.Engine(0)
+    E_t = t.run_input(_h8_input(golden, "truncated.dat", sched, 2, ()), mode="fp64")[0]
+    n_t = t.ndets()
+    t.close()
+    assert E_t > E_full + 1e-6
+    g = eng.Engine(0)
+    E_g = g.run_input(_h8_input(golden, "resume.dat", sched, 12, ("restart",)), mode="fp64")[0]
+    log = g.run_log()
+    assert len(log["ndets"]) >= 1 and log["ndets"][0] > n_t
+    assert abs(E_g - E_full) < 1e-6
+    g.close()

