@@ -191,7 +191,16 @@ int shci_davidson(shci_ctx* ctx, int mode, int block, int nroots, double* x0, in
  * SHCIbasics::DoVariational, SHCI/SHCIbasics.cpp:783-1378, driven as in
  * SHCI/SHCI.cpp:157-446). Reads input.dat and its FCIDUMP (relative paths
  * resolve against the input file's directory unless fcidump is given).
- * E[cap_roots] receives E_var per root with coreE added; *nroots the count. */
+ * E[cap_roots] receives E_var per root with coreE added; *nroots the count.
+ * Checkpoints as the reference keeps them (writeVariationalResult /
+ * readVariationalResult, SHCI/SHCIbasics.cpp:871-943, 1224-1226, 1346-1352,
+ * 1481-1590): with `io` (the default) the iteration, determinants,
+ * coefficients and E0 are written after every iteration to
+ * <prefix>/shci_gpu-variational.chk (this library's own binary layout; a
+ * relative prefix resolves against the input file's directory); `restart`
+ * resumes after the saved iteration, or returns the saved result when that
+ * iteration already used the final eps1; `fullrestart` reruns the schedule
+ * from the saved space. A missing or foreign checkpoint is SHCI_ERR_IO. */
 int shci_run_input(shci_ctx* ctx, const char* input_path, const char* fcidump, int mode, int block, double* E,
                    int cap_roots, int* nroots);
 /* Per-iteration log of the last run: ndets, E (root 0, coreE added),
