@@ -206,7 +206,7 @@ static const char* kIgnored[] = {
     "dosocqdpt", "dogtensor", "socmultiplier", "doresponse", "onlyperturbative", "algorithm", "dolcc",
     "pointGroup", "spin", "irrep", "searchForLowestEnergyDet", "cdfciTol", "cdfciIter", "cdfciOn",
     "reportInterval", "z_threshold", "cdfciSample", "eps", "maxseniority", "maxexcitation", "SenioAndExc",
-    "diskdavidson", "Treversal"};
+    "diskdavidson"};
 
 void read_input(const std::string& path, Schedule& s) {
   std::ifstream ifs(path.c_str());
@@ -313,6 +313,12 @@ void read_input(const std::string& path, Schedule& s) {
     } else if (iequal(arg, "targetError")) {
       need(1);
       s.targetError = std::atof(tok[1].c_str());
+    } else if (iequal(arg, "Treversal")) {
+      // the time-reversal basis (SHCI/SHCImakeHamiltonian.cpp:411-483) is not
+      // restated here; running the plain path instead would give another energy
+      need(1);
+      if (std::atoi(tok[1].c_str()) != 0)
+        throw Error(kErrInvalid, "Treversal (time-reversal symmetry) is not supported; remove it or set it to 0");
     } else if (iequal(arg, "io")) {
       s.io = true;
     } else if (iequal(arg, "noio")) {
