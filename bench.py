@@ -8,7 +8,8 @@ timed "step" is then one sigma (y = H x) over the final variational space
 with the Hamiltonian resident in HBM.
 
 value: sigma Mdets/s (N / t_sigma / 1e6), kernel-only, device-resident
-vectors. e2e: the same through the C-ABI call with host buffers
+vectors: two launches per step (shci_sigma_packed_device gathers x into the
+stored matrix's storage order, then runs the sigma). e2e: the same through the C-ABI call with host buffers
 (shci_sigma: host->device copy of x and device->host copy of y inside the
 timed region). Extra keys report the variational wall time and E_var of
 both paths.
