@@ -171,6 +171,9 @@ struct Context {
   Helpers helpers;
   bool helpers_ok = false;
   Csr H;
+  // device address of the allocation-free sigma's fixed array on this
+  // context's device, looked up by every stored build
+  void* noalloc_ptr = nullptr;
   int ham_mode = -1;
   bool ham_ok = false;
   DevBuf<double> diag;
@@ -582,6 +585,7 @@ struct Context {
                     mode == SHCI_MODE_MIXED, n_old, prims, stream);
       if (mode == SHCI_MODE_MIXED) compress_csr(H, prims, stream);
       pt.mark("ham compress");
+      noalloc_ptr = noalloc_scratch_address();
     }
     ham_mode = mode;
     ham_ok = true;
@@ -611,7 +615,7 @@ struct Context {
         xb64.reserve(N * kp);
         if (H.v64.p) {
           pack_f64(A, lda, c0 + done, kk, kp, N, xb64.p, stream, H.perm.p);
-          sigma_csr_f64(H, diag.p, xb64.p, kp, kk, Yp + (size_t)(yc0 + done) * ldy, ldy, false, stream);
+          sigma_csr_f64(H, diag.p, xb64.p, kp, kk, Yp + (size_t)(yc0 + done) * ldy, ldy, stream);
         } else {  // mixed-path matrix: float-float refinement sigma on head + tail
           float* xff = reinterpret_cast<float*>(xb64.p);
           pack_ff(A, lda, c0 + done, kk, kp, N, xff, stream, H.perm.p);
@@ -813,8 +817,8 @@ struct Context {
       for (int c = 0; c < nroots; ++c) rn[c] = std::sqrt(std::max(0.0, pin[kPinRR + (size_t)c * nroots + c]));
       numIter++;
       if (trace_level() > 0)
-        std::fprintf(stderr, "[davidson mode=%d it=%d m=%d] lam0=%.12f res0=%.3e G00=%.12f\n", mode, numIter, m,
-                     lam[0], rn[0], G[0]);
+        std::fprintf(stderr, "[davidson mode=%d it=%d m=%d] lam0=%.12f res0=%.3e G00=%.12f t=%.3f\n", mode, numIter,
+                     m, lam[0], rn[0], G[0], now_s() - t_enter);
       auto finish = [&]() {
         if (basis_m) *basis_m = m;
         E.assign(lam.begin(), lam.begin() + nroots);
@@ -1278,6 +1282,8 @@ struct Context {
       SHCI_LAUNCH_CHECK();
       select(cmax.p, eps1);
       const size_t N = ndet;
+      if (trace_level() > 0)
+        std::fprintf(stderr, "[select] %zu eps1=%.3e ndets %zu -> %zu in %.3f s\n", iter, eps1, N0, N, now_s() - ta);
       // X0 = [ci; 0]
       X0.resize(N * nroots);
       SHCI_CUDA(cudaMemsetAsync(X0.p, 0, N * nroots * sizeof(double), stream));
@@ -1301,6 +1307,10 @@ struct Context {
       t_dav += td - tc;
       log.push_back({(int64_t)N, E0[0] + hints.coreE, numIter, td - t0});
       total_dav_iters += numIter;
+      if (trace_level() > 0)  // the reference's per-iteration table line, plus the matrix size
+        std::fprintf(stderr, "[iter] %zu eps1=%.3e ndets=%zu nnz=%lld csr_bytes=%zu helper_bytes=%zu E=%.12f "
+                             "davidson=%d t=%.3f\n", iter, eps1, N, (long long)H.nnz, H.bytes(), helpers.bytes(),
+                     E0[0] + hints.coreE, numIter, td - t0);
       if (precond == 2 && !is_direct(mode)) {
         // pairs from this solve, used from the next solve on; later calls
         // refine the network already trained (a third of the steps)
@@ -1633,6 +1643,7 @@ int shci_sigma_device(shci_ctx* ctx, int mode, const double* x_dev, double* y_de
   return guarded(ctx, [&](Context& c) {
     if (k < 1 || k > 4) throw Error(SHCI_ERR_INVALID, "k must be in 1..4");
     if (ld < (int64_t)c.ndet) throw Error(SHCI_ERR_INVALID, "leading dimension smaller than N");
+    if (!x_dev || !y_dev) throw Error(SHCI_ERR_INVALID, "null vector");
     c.ensure_diag();
     c.apply_sigma(mode, x_dev, (size_t)ld, 0, k, y_dev, (size_t)ld, 0);
   });
@@ -1642,6 +1653,7 @@ int shci_sigma_packed_device(shci_ctx* ctx, int mode, const void* x_packed, int 
                              int64_t ld) {
   return guarded(ctx, [&](Context& c) {
     if (!(kp == 1 || kp == 2 || kp == 4) || k < 1 || k > kp) throw Error(SHCI_ERR_INVALID, "need k <= kp in {1,2,4}");
+    if (!x_packed || !y_dev) throw Error(SHCI_ERR_INVALID, "null vector");
     if (!c.ham_ok || Context::is_direct(c.ham_mode)) throw Error(SHCI_ERR_STATE, "no stored Hamiltonian");
     if (ld < (int64_t)c.ndet) throw Error(SHCI_ERR_INVALID, "leading dimension smaller than N");
     c.ensure_diag();
@@ -1653,9 +1665,14 @@ int shci_sigma_packed_device(shci_ctx* ctx, int mode, const void* x_packed, int 
       shci::gather_rows(x_packed, sizeof(float) * kp, c.H.perm.p, N, c.xb32.p, c.stream);
       shci::sigma_csr_mixed(c.H, c.diag.p, c.xb32.p, kp, k, y_dev, (size_t)ld, c.stream);
     } else if (mode == SHCI_MODE_FP64) {
+      // the FP64 values of a plain build; a mixed build's refinement sigma
+      // (float-float, shci_sigma_device) needs the column-major FP64 x
+      if (!c.H.v64.p)
+        throw Error(SHCI_ERR_STATE, "packed FP64 sigma needs a Hamiltonian built in FP64 mode (a mixed build's "
+                                    "FP64 refinement sigma is shci_sigma_device)");
       c.xb64.reserve(N * kp);
       shci::gather_rows(x_packed, sizeof(double) * kp, c.H.perm.p, N, c.xb64.p, c.stream);
-      shci::sigma_csr_f64(c.H, c.diag.p, c.xb64.p, kp, k, y_dev, (size_t)ld, c.H.v64.p == nullptr, c.stream);
+      shci::sigma_csr_f64(c.H, c.diag.p, c.xb64.p, kp, k, y_dev, (size_t)ld, c.stream);
     } else {
       throw Error(SHCI_ERR_INVALID, "packed sigma supports the stored modes only");
     }
@@ -1677,7 +1694,9 @@ int shci_sigma_device_noalloc(shci_ctx* ctx, int mode, const double* x_dev, doub
       throw Error(SHCI_ERR_STATE, "mixed sigma needs a Hamiltonian built in mixed mode");
     if (c.ndiag < c.ndet) throw Error(SHCI_ERR_STATE, "diagonal not computed (call shci_ham_build first)");
     if (ld < (int64_t)c.ndet) throw Error(SHCI_ERR_INVALID, "leading dimension smaller than N");
-    shci::sigma_noalloc(c.H, c.diag.p, mode == SHCI_MODE_MIXED, x_dev, (size_t)ld, k, y_dev, (size_t)ld, c.stream);
+    if (!x_dev || !y_dev) throw Error(SHCI_ERR_INVALID, "null vector");
+    shci::sigma_noalloc(c.H, c.diag.p, mode == SHCI_MODE_MIXED, x_dev, (size_t)ld, k, y_dev, (size_t)ld,
+                        c.noalloc_ptr, c.stream);
   });
 }
 

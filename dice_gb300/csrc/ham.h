@@ -237,7 +237,7 @@ PtStochResult pt_semistochastic(const Det2* dets, size_t n, const double* c_dev,
 void sigma_csr_mixed(const Csr& H, const double* diag, const float* x32, int kp, int k, double* y, size_t ldy,
                      cudaStream_t s);
 void sigma_csr_f64(const Csr& H, const double* diag, const double* x64, int kp, int k, double* y, size_t ldy,
-                   bool use_hilo, cudaStream_t s);
+                   cudaStream_t s);
 // Refinement sigma on the FP32 head + tail values in float-float arithmetic:
 // xff is x split as (head, tail) float pairs, row-interleaved [N][kp]; the
 // diagonal term is taken in FP64 from column-major xd (columns c0..c0+k-1).
@@ -248,8 +248,11 @@ void sigma_csr_ff(const Csr& H, const double* diag, const float* xff, int kp, co
 // mixed path, 2,097,152 in the FP64 path; k = 3 counts as 4) and the stored
 // Hamiltonian's sigma kernel runs on it. Larger sizes are rejected.
 constexpr size_t kNoAllocPackBytes = (size_t)16 << 20;
+// scratch: the array's device address on the context's device, from
+// noalloc_scratch_address() (looked up while the Hamiltonian is built).
 void sigma_noalloc(const Csr& H, const double* diag, int mode_mixed, const double* x, size_t ldx, int k, double* y,
-                   size_t ldy, cudaStream_t s);
+                   size_t ldy, void* scratch, cudaStream_t s);
+void* noalloc_scratch_address();
 // Pack columns [c0, c0+k) of column-major A (lda) into row-interleaved [N][kp]
 // (zero padded) in FP32 or FP64; with perm (storage order of the stored
 // Hamiltonian), packed row i holds row perm[i] of A.

@@ -14,7 +14,6 @@
 // diagonal preconditioner of SHCI/Davidson.cpp:85-106) reduce in a fixed
 // order, so results do not depend on scheduling.
 #include <cstdlib>
-#include <mutex>
 
 #include "ham.h"
 
@@ -343,11 +342,10 @@ void compress_csr(Csr& H, Prims& pr, cudaStream_t s) {
   H.cvalid = true;
 }
 
-template <int VW, int KP, bool HILO>
+template <int VW, int KP>
 __global__ void __launch_bounds__(KP == 1 ? 1024 : 256) k_sigma_f64(const int64_t* __restrict__ rowptr,
                                                    const int32_t* __restrict__ col,
-                                                   const double* __restrict__ v64, const float* __restrict__ vhi,
-                                                   const float* __restrict__ vlo, const double* __restrict__ diag,
+                                                   const double* __restrict__ v64, const double* __restrict__ diag,
                                                    const double* __restrict__ x, size_t N, int k,
                                                    double* __restrict__ y, size_t ldy,
                                                    const uint32_t* __restrict__ perm) {
@@ -359,11 +357,7 @@ __global__ void __launch_bounds__(KP == 1 ? 1024 : 256) k_sigma_f64(const int64_
     const int64_t p0 = live ? __ldg(rowptr + r) : 0;
     const int64_t p1 = live ? __ldg(rowptr + r + 1) : 0;
     auto elem = [&](int64_t p, int j) {
-      double h;
-      if (HILO)
-        h = (double)__ldcs(vhi + p) + (double)__ldcs(vlo + p);
-      else
-        h = __ldcs(v64 + p);
+      const double h = __ldcs(v64 + p);
 #pragma unroll
       for (int c = 0; c < KP; ++c) acc[c] += h * __ldg(x + (size_t)j * KP + c);
     };
@@ -562,41 +556,30 @@ void sigma_csr_mixed(const Csr& H, const double* diag, const float* x32, int kp,
   }
 }
 
-template <int KP, bool HILO>
+template <int KP>
 static void launch_f64(int vw, const Csr& H, const double* diag, const double* x, int k, double* y, size_t ldy,
                        cudaStream_t s) {
   const SigmaLaunch L = sigma_launch(H.N, vw, KP);
   const double* v64 = H.v64.p;
-  const float *vhi = H.vhi.p, *vlo = H.vlo.p;
   switch (vw) {
-    case 32: k_sigma_f64<32, KP, HILO><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, v64, vhi, vlo, diag, x, H.N, k, y, ldy, H.perm.p); break;
-    case 16: k_sigma_f64<16, KP, HILO><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, v64, vhi, vlo, diag, x, H.N, k, y, ldy, H.perm.p); break;
-    case 8: k_sigma_f64<8, KP, HILO><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, v64, vhi, vlo, diag, x, H.N, k, y, ldy, H.perm.p); break;
-    default: k_sigma_f64<4, KP, HILO><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, v64, vhi, vlo, diag, x, H.N, k, y, ldy, H.perm.p); break;
+    case 32: k_sigma_f64<32, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, v64, diag, x, H.N, k, y, ldy, H.perm.p); break;
+    case 16: k_sigma_f64<16, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, v64, diag, x, H.N, k, y, ldy, H.perm.p); break;
+    case 8: k_sigma_f64<8, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, v64, diag, x, H.N, k, y, ldy, H.perm.p); break;
+    default: k_sigma_f64<4, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, v64, diag, x, H.N, k, y, ldy, H.perm.p); break;
   }
   SHCI_LAUNCH_CHECK();
 }
 
 void sigma_csr_f64(const Csr& H, const double* diag, const double* x64, int kp, int k, double* y, size_t ldy,
-                   bool use_hilo, cudaStream_t s) {
+                   cudaStream_t s) {
   if (H.N == 0) return;
-  if (use_hilo && !(H.vhi.p && H.vlo.p)) throw Error(kErrState, "Hamiltonian has no FP32 head/tail values");
-  if (!use_hilo && !H.v64.p) throw Error(kErrState, "Hamiltonian has no FP64 values");
-  int vw = pick_vw(H);
-  if (use_hilo) {
-    switch (kp) {
-      case 1: launch_f64<1, true>(vw, H, diag, x64, k, y, ldy, s); break;
-      case 2: launch_f64<2, true>(vw, H, diag, x64, k, y, ldy, s); break;
-      case 4: launch_f64<4, true>(vw, H, diag, x64, k, y, ldy, s); break;
-      default: throw Error(kErrInvalid, "sigma block width must be 1, 2 or 4");
-    }
-  } else {
-    switch (kp) {
-      case 1: launch_f64<1, false>(vw, H, diag, x64, k, y, ldy, s); break;
-      case 2: launch_f64<2, false>(vw, H, diag, x64, k, y, ldy, s); break;
-      case 4: launch_f64<4, false>(vw, H, diag, x64, k, y, ldy, s); break;
-      default: throw Error(kErrInvalid, "sigma block width must be 1, 2 or 4");
-    }
+  if (!H.v64.p) throw Error(kErrState, "Hamiltonian has no FP64 values");
+  const int vw = pick_vw(H);
+  switch (kp) {
+    case 1: launch_f64<1>(vw, H, diag, x64, k, y, ldy, s); break;
+    case 2: launch_f64<2>(vw, H, diag, x64, k, y, ldy, s); break;
+    case 4: launch_f64<4>(vw, H, diag, x64, k, y, ldy, s); break;
+    default: throw Error(kErrInvalid, "sigma block width must be 1, 2 or 4");
   }
 }
 
@@ -937,33 +920,23 @@ void scale_cols(double* A, size_t ld, const double* scale, int k, size_t N, cuda
 // ---------------------------------------------------------------------------
 static __device__ __align__(256) unsigned char g_sigma_pack_scratch[kNoAllocPackBytes];
 
-namespace {
-std::mutex g_scratch_mu;
-void* g_scratch_addr[64] = {nullptr};
-}  // namespace
-
-// Device address of the array on the current device, looked up once per
-// device (host code cannot use the symbol itself: on the host it names a
-// stand-in, not device memory).
-static void* noalloc_scratch() {
-  int dev = 0;
-  SHCI_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= 64) throw Error(kErrInvalid, "device index beyond 63");
-  std::lock_guard<std::mutex> lock(g_scratch_mu);
-  if (!g_scratch_addr[dev]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_sigma_pack_scratch);
-    if (e != cudaSuccess) {
-      cudaGetLastError();
-      throw Error(kErrCuda, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
-    }
-    g_scratch_addr[dev] = p;
+// Device address of the array on the current device. Host code cannot use
+// the symbol itself: on the host it names a stand-in, not device memory. The
+// context calls this while it builds a stored Hamiltonian (a call that may
+// allocate and load this file's kernels), so the allocation-free sigma itself
+// only reads the address the context kept.
+void* noalloc_scratch_address() {
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_sigma_pack_scratch);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    throw Error(kErrCuda, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
   }
-  return g_scratch_addr[dev];
+  return p;
 }
 
 void sigma_noalloc(const Csr& H, const double* diag, int mode_mixed, const double* x, size_t ldx, int k, double* y,
-                   size_t ldy, cudaStream_t s) {
+                   size_t ldy, void* scratch, cudaStream_t s) {
   const size_t N = H.N;
   const int kp = k == 3 ? 4 : k;
   const size_t need = N * (size_t)kp * (mode_mixed ? sizeof(float) : sizeof(double));
@@ -971,14 +944,14 @@ void sigma_noalloc(const Csr& H, const double* diag, int mode_mixed, const doubl
     throw Error(kErrInvalid, "allocation-free sigma: N x k = " + std::to_string(N) + " x " + std::to_string(kp) +
                                  " needs " + std::to_string(need) + " bytes of scratch, the fixed maximum is " +
                                  std::to_string(kNoAllocPackBytes));
-  void* scratch = noalloc_scratch();
+  if (!scratch) throw Error(kErrState, "allocation-free sigma: scratch address not set up (build the Hamiltonian)");
   if (mode_mixed) {
     pack_f32(x, ldx, 0, k, kp, N, static_cast<float*>(scratch), s, H.perm.p);
     sigma_csr_mixed(H, diag, static_cast<const float*>(scratch), kp, k, y, ldy, s);
   } else {
     if (H.v64.p) {
       pack_f64(x, ldx, 0, k, kp, N, static_cast<double*>(scratch), s, H.perm.p);
-      sigma_csr_f64(H, diag, static_cast<const double*>(scratch), kp, k, y, ldy, false, s);
+      sigma_csr_f64(H, diag, static_cast<const double*>(scratch), kp, k, y, ldy, s);
     } else {  // head + tail values: float-float refinement sigma (same 8 bytes per entry)
       pack_ff(x, ldx, 0, k, kp, N, static_cast<float*>(scratch), s, H.perm.p);
       sigma_csr_ff(H, diag, static_cast<const float*>(scratch), kp, x, ldx, 0, k, y, ldy, s);

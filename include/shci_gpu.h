@@ -141,6 +141,8 @@ int shci_sigma_device(shci_ctx* ctx, int mode, const double* x_dev, double* y_de
  * on the context stream, no synchronisation: the rows of x_packed gathered
  * into the stored matrix's storage order (sorted by alpha, then beta string;
  * a context buffer, allocated on first use), then the sigma kernel.
+ * SHCI_MODE_FP64 needs a Hamiltonian built in FP64 mode (SHCI_ERR_STATE
+ * otherwise: a mixed build's FP64 refinement sigma is shci_sigma_device).
  * Replaces the inner product loop of Hmult2::operator() (SHCI/Hmult.h:108-123). */
 int shci_sigma_packed_device(shci_ctx* ctx, int mode, const void* x_packed, int kp, int k, double* y_dev,
                              int64_t ld);
@@ -155,12 +157,14 @@ int shci_sigma_packed_device(shci_ctx* ctx, int mode, const void* x_packed, int 
  * compiled into the library instead of a context buffer, which limits N x k
  * (k = 3 counts as 4) to 4,194,304 for SHCI_MODE_MIXED and 2,097,152 for
  * SHCI_MODE_FP64; larger sizes return SHCI_ERR_INVALID. The array is held by
- * every GPU that loads the library until the process exits. The first call on
- * each device looks up the array's device address (cudaGetSymbolAddress), so
- * make that first call before any stream capture on that device. All calls
- * share the array: calls that overlap on the GPU (other streams or contexts
- * at the same time) race on it. Enqueued on the context stream, no host
- * synchronisation. SHCI_MODE_DIRECT is not supported. */
+ * every GPU that loads the library until the process exits. Its device
+ * address is looked up (cudaGetSymbolAddress) by shci_ham_build on the
+ * context's device, so this call does no set-up of its own; after a
+ * cudaDeviceReset every context is gone and a new one must be built. All
+ * calls share the array: calls that overlap on the GPU (other streams or
+ * contexts at the same time) race on it. Null vectors return
+ * SHCI_ERR_INVALID. Enqueued on the context stream, no host synchronisation.
+ * SHCI_MODE_DIRECT is not supported. */
 int shci_sigma_device_noalloc(shci_ctx* ctx, int mode, const double* x_dev, double* y_dev, int k, int64_t ld);
 /* Bytes of the stored Hamiltonian (row pointers, columns, values) and of the
  * string tables, for memory and roofline accounting. */

@@ -57,6 +57,7 @@ def lib():
         L.orc_sigma_mt.argtypes = [vp, vp, vp, ctypes.c_int]
         L.orc_davidson.restype = i32
         L.orc_davidson.argtypes = [vp, vp, i32, vp, i32, dbl, i32, vp, ctypes.POINTER(i32)]
+        L.orc_set_threads.argtypes = [i32]
         L.orc_run_input.restype = i32
         L.orc_run_input.argtypes = [ctypes.POINTER(vp), ctypes.c_char_p, ctypes.c_char_p, i32,
                                     ctypes.c_char_p, i32]
@@ -314,6 +315,12 @@ class VarRun:
         the input's epsilon2). Returns (E2, stats)."""
         e2 = lib().orc_var_pt(self.h, root, eps2)
         return e2, _pt_stats(self.h)
+
+
+def set_threads(threads):
+    """Worker threads of the oracle's selection, Hamiltonian rows and sigma
+    (1, the default, is the serial restatement the parity tests use)."""
+    lib().orc_set_threads(int(threads))
 
 
 def run_input(input_path, fcidump=None, verbose=False):

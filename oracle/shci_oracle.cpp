@@ -20,6 +20,7 @@
 // SHCI/Determinants.h:247-602.
 
 #include <algorithm>
+#include <atomic>
 #include <random>
 #include <cassert>
 #include <chrono>
@@ -414,6 +415,30 @@ static bool restr_two(const std::vector<Restriction>& rs, int i, int j, int a, i
   return true;
 }
 
+// Worker threads of the oracle's timed reference run (orc_set_threads); 1 for
+// the serial restatement every parity test uses. Threads stand in for the
+// MPI ranks of one node: selection deals parents, the build deals rows and
+// sigma is the reference's rank-parallel Hmult2 (sigma_mt below).
+static int g_threads = 1;
+
+// Runs f(b) for b in [0, nblocks) on g_threads workers (blocks handed out in
+// order from a shared counter); serial when g_threads == 1.
+template <class F>
+static void parallel_blocks(size_t nblocks, F&& f) {
+  const int T = std::max(1, std::min<int>(g_threads, (int)std::max<size_t>(1, nblocks)));
+  if (T == 1) {
+    for (size_t b = 0; b < nblocks; ++b) f(b);
+    return;
+  }
+  std::atomic<size_t> next{0};
+  std::vector<std::thread> pool;
+  for (int w = 0; w < T; ++w)
+    pool.emplace_back([&] {
+      for (size_t b; (b = next.fetch_add(1)) < nblocks;) f(b);
+    });
+  for (auto& th : pool) th.join();
+}
+
 struct SelParams {
   int ncore = 0;
   int nact = 1000000;
@@ -490,8 +515,24 @@ static void select_all(const Ints& I, const HeatBath& hb, const Det* dets, size_
                        double eps1, SelParams& sp, const Det* sorted, size_t nsorted,
                        std::vector<Det>& newdets) {
   newdets.clear();
-  for (size_t i = 0; i < n; i++)
-    select_from_parent(I, hb, dets[i], eps1 / fabs(cmax[i]), sp, sorted, nsorted, newdets);
+  if (g_threads <= 1) {
+    for (size_t i = 0; i < n; i++)
+      select_from_parent(I, hb, dets[i], eps1 / fabs(cmax[i]), sp, sorted, nsorted, newdets);
+  } else {  // parents dealt in blocks; the candidates are sorted and uniqued below either way
+    const size_t kPar = 256, nblk = (n + kPar - 1) / kPar;
+    std::vector<std::vector<Det>> part(nblk);
+    parallel_blocks(nblk, [&](size_t b) {
+      SelParams spl = sp;  // restrictions_init rewrites it per parent
+      for (size_t i = b * kPar; i < std::min(n, (b + 1) * kPar); i++)
+        select_from_parent(I, hb, dets[i], eps1 / fabs(cmax[i]), spl, sorted, nsorted, part[b]);
+      std::sort(part[b].begin(), part[b].end(), det_less);
+      part[b].erase(std::unique(part[b].begin(), part[b].end(), det_eq), part[b].end());
+    });
+    for (auto& v : part) {
+      newdets.insert(newdets.end(), v.begin(), v.end());
+      std::vector<Det>().swap(v);
+    }
+  }
   std::sort(newdets.begin(), newdets.end(), det_less);
   newdets.erase(std::unique(newdets.begin(), newdets.end(), det_eq), newdets.end());
 }
@@ -699,7 +740,11 @@ static inline uint64_t spin_string(const Det& d, int s) {
   return out;
 }
 
-static void build_ham(const Ints& I, const Det* dets, size_t N, SparseHam& H) {
+// Rows [n_old, N) of the lower triangle (the rows of the first n_old
+// determinants are kept: selection only appends, and row I holds J <= I), as
+// SparseHam::makeFromHelper builds the rows from StartIndex on
+// (SHCI/SHCImakeHamiltonian.cpp:486-715). n_old = 0 builds every row.
+static void build_ham(const Ints& I, const Det* dets, size_t N, SparseHam& H, size_t n_old = 0) {
   std::unordered_map<uint64_t, int> amap, bmap;
   std::vector<uint64_t> astr, bstr;
   std::vector<int> aidx(N), bidx(N);
@@ -720,52 +765,81 @@ static void build_ham(const Ints& I, const Det* dets, size_t N, SparseHam& H) {
   // single-excitation neighbours among the present alpha strings
   const int n = I.norb;
   std::vector<std::vector<int>> singA(astr.size());
-  for (size_t s = 0; s < astr.size(); ++s) {
-    uint64_t x = astr[s];
-    for (int i = 0; i < n; ++i) {
-      if (!((x >> i) & 1)) continue;
-      for (int a = 0; a < n; ++a) {
-        if ((x >> a) & 1) continue;
-        uint64_t y = (x & ~(1ull << i)) | (1ull << a);
-        auto it = amap.find(y);
-        if (it != amap.end()) singA[s].push_back(it->second);
+  parallel_blocks((astr.size() + 1023) / 1024, [&](size_t blk) {
+    for (size_t s = blk * 1024; s < std::min(astr.size(), (blk + 1) * 1024); ++s) {
+      uint64_t x = astr[s];
+      for (int i = 0; i < n; ++i) {
+        if (!((x >> i) & 1)) continue;
+        for (int a = 0; a < n; ++a) {
+          if ((x >> a) & 1) continue;
+          uint64_t y = (x & ~(1ull << i)) | (1ull << a);
+          auto it = amap.find(y);
+          if (it != amap.end()) singA[s].push_back(it->second);
+        }
       }
     }
-  }
-  H.rowptr.assign(N + 1, 0);
-  H.col.clear();
-  H.val.clear();
-  std::vector<int> row;
-  for (size_t I_ = 0; I_ < N; ++I_) {
-    row.clear();
-    const uint64_t A = astr[aidx[I_]], B = bstr[bidx[I_]];
-    // same alpha string: beta single or double
-    for (int J : byA[aidx[I_]]) {
-      if ((size_t)J >= I_) continue;
-      int d = popc(bstr[bidx[J]] ^ B);
-      if (d == 2 || d == 4) row.push_back(J);
-    }
-    // alpha single: beta equal (single alpha) or beta single (alpha-beta double)
-    for (int As : singA[aidx[I_]])
-      for (int J : byA[As]) {
+  });
+  if (n_old > N || H.rowptr.size() != n_old + 1) n_old = 0;
+  H.rowptr.resize(N + 1);
+  H.rowptr[0] = 0;
+  H.col.resize((size_t)H.rowptr[n_old]);
+  H.val.resize((size_t)H.rowptr[n_old]);
+  // rows in blocks: each block's entries are collected privately, then the
+  // blocks are appended in row order
+  const size_t kRows = 2048;
+  const size_t nblk = (N - n_old + kRows - 1) / kRows;
+  struct Block {
+    std::vector<int64_t> len;
+    std::vector<int32_t> col;
+    std::vector<double> val;
+  };
+  std::vector<Block> blocks(nblk);
+  parallel_blocks(nblk, [&](size_t blk) {
+    Block& B_ = blocks[blk];
+    std::vector<int> row;
+    const size_t r0 = n_old + blk * kRows, r1 = std::min(N, r0 + kRows);
+    for (size_t I_ = r0; I_ < r1; ++I_) {
+      row.clear();
+      const uint64_t A = astr[aidx[I_]], B = bstr[bidx[I_]];
+      // same alpha string: beta single or double
+      for (int J : byA[aidx[I_]]) {
         if ((size_t)J >= I_) continue;
         int d = popc(bstr[bidx[J]] ^ B);
-        if (d == 0 || d == 2) row.push_back(J);
+        if (d == 2 || d == 4) row.push_back(J);
       }
-    // same beta string: alpha double
-    for (int J : byB[bidx[I_]]) {
-      if ((size_t)J >= I_) continue;
-      int d = popc(astr[aidx[J]] ^ A);
-      if (d == 4) row.push_back(J);
+      // alpha single: beta equal (single alpha) or beta single (alpha-beta double)
+      for (int As : singA[aidx[I_]])
+        for (int J : byA[As]) {
+          if ((size_t)J >= I_) continue;
+          int d = popc(bstr[bidx[J]] ^ B);
+          if (d == 0 || d == 2) row.push_back(J);
+        }
+      // same beta string: alpha double
+      for (int J : byB[bidx[I_]]) {
+        if ((size_t)J >= I_) continue;
+        int d = popc(astr[aidx[J]] ^ A);
+        if (d == 4) row.push_back(J);
+      }
+      std::sort(row.begin(), row.end());
+      B_.len.push_back((int64_t)row.size() + 1);
+      B_.col.push_back((int32_t)I_);
+      B_.val.push_back(det_energy(I, dets[I_]));
+      for (int J : row) {
+        B_.col.push_back(J);
+        B_.val.push_back(hij(I, dets[J], dets[I_]));
+      }
     }
-    std::sort(row.begin(), row.end());
-    H.col.push_back((int32_t)I_);
-    H.val.push_back(det_energy(I, dets[I_]));
-    for (int J : row) {
-      H.col.push_back(J);
-      H.val.push_back(hij(I, dets[J], dets[I_]));
+  });
+  size_t r = n_old;
+  for (auto& B_ : blocks) {
+    for (int64_t L : B_.len) {
+      H.rowptr[r + 1] = H.rowptr[r] + L;
+      ++r;
     }
-    H.rowptr[I_ + 1] = H.col.size();
+    H.col.insert(H.col.end(), B_.col.begin(), B_.col.end());
+    H.val.insert(H.val.end(), B_.val.begin(), B_.val.end());
+    Block().col.swap(B_.col);  // release as we go
+    Block().val.swap(B_.val);
   }
 }
 
@@ -1272,7 +1346,10 @@ static int davidson(const SparseHam& H, size_t N, std::vector<std::vector<double
   std::vector<double> tmp;
   while (true) {
     for (int i = sigmaSize; i < bsize; i++) {
-      sigma(H, N, b[i].data(), sig[i].data());
+      if (g_threads > 1)
+        sigma_mt(H, N, b[i].data(), sig[i].data(), g_threads);
+      else
+        sigma(H, N, b[i].data(), sig[i].data());
       sigmaSize++;
     }
     std::vector<double> hs((size_t)bsize * bsize);
@@ -1530,12 +1607,15 @@ static int do_variational(const Ints& I, const HeatBath& hb, Schedule& s, VarRes
       cMax[j] = pow(cMax[j], 0.5);
     }
     std::vector<Det> newDets;
+    const double ts0 = now_s();
     select_all(I, hb, Dets.data(), N0, cMax.data(), eps1, s.sel, sorted.data(), sorted.size(), newDets);
+    const double ts1 = now_s();
     std::vector<std::vector<double>> X0(nroots, std::vector<double>(N0 + newDets.size(), 0.0));
     for (int i = 0; i < nroots; i++) std::copy(ci[i].begin(), ci[i].end(), X0[i].begin());
     Dets.insert(Dets.end(), newDets.begin(), newDets.end());
     size_t N = Dets.size();
-    build_ham(I, Dets.data(), N, H);
+    build_ham(I, Dets.data(), N, H, N0);  // the rows of the first N0 determinants are kept
+    const double ts2 = now_s();
     sorted = Dets;
     std::sort(sorted.begin(), sorted.end(), det_less);
     size_t old = diag.size();
@@ -1553,6 +1633,9 @@ static int do_variational(const Ints& I, const HeatBath& hb, Schedule& s, VarRes
     E0 = ev;
     ci = X0;
     res.log.push_back({(int)iter, eps1, (int64_t)N, E0[0] + I.coreE, numIter, now_s() - t0});
+    if (verbose > 1)
+      fprintf(stderr, "[oracle] iter %d: select %.2f s, build %.2f s (%zu lower-triangle entries), davidson %.2f s\n",
+              (int)iter, ts1 - ts0, ts2 - ts1, H.col.size(), now_s() - ts2);
     if (verbose)
       printf("%4d %4d  %10.2e  %10zu   %18.10f  %9d  %10.2f\n", (int)iter, 0, eps1, N, E0[0] + I.coreE, numIter,
              now_s() - t0);
@@ -1718,6 +1801,10 @@ int orc_davidson(orc_ctx* c, double* x0, int nroots, const double* diag, int max
 
 // Whole variational stage from a Dice input file. The FCIDUMP named in the
 // input (or `fcidump_override`) is read relative to the current directory.
+// Worker threads for selection, Hamiltonian rows and sigma (default 1: the
+// serial restatement).
+void orc_set_threads(int threads) { g_threads = threads < 1 ? 1 : threads; }
+
 int orc_run_input(orc_ctx** out_ctx, const char* input, const char* fcidump_override, int verbose, char* errbuf,
                   int errlen) {
   Schedule s;

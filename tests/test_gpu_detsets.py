@@ -1,0 +1,107 @@
+"""Determinant-set parity of whole variational runs: the GPU's FP64 path
+against the CPU oracle on the synthetic workloads, and the mixed-precision
+path against the FP64 path in parity mode.
+
+The reference's loop (SHCI/SHCIbasics.cpp:954-1077) selects from cMax_i =
+max over roots |c_i| of the previous loose Davidson solve. The FP64 GPU path
+runs the reference's algorithm (one correction vector per iteration for the
+lowest unconverged root, nroots+4 vectors, the same start vectors), so its
+coefficients agree with the oracle's to rounding, and every determinant of
+every iteration must come out identical and in the same index order.
+
+The mixed path computes sigma in FP32 and its loose solves stop elsewhere
+below the tolerance, so at the reference's loose tolerance (5e-5) a few
+borderline candidates can fall on the other side of eps1 / cMax. In parity
+mode (`davidsonTolLoose` set to the final tolerance, 1e-8 here, for both
+paths) every solve pins c to ~1e-8 and the two paths must select identical
+sets; E_var agrees within 1 uHa.
+
+Tolerances: determinant sets and their order exact; E_var 1e-9 Ha between
+the GPU FP64 path and the oracle, 1e-6 Ha between the mixed and FP64 paths.
+"""
+import numpy as np
+import pytest
+
+from dice_gb300 import engine as eng
+from dice_gb300 import synthetic
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+PARITY = ("davidsonTol 1e-8", "davidsonTolLoose 1e-8")
+
+
+def sym_diff(a, b):
+    """Number of determinants in exactly one of the two (N, 2) uint64 lists."""
+    va = np.ascontiguousarray(a, dtype=np.uint64).view(np.dtype((np.void, 16))).ravel()
+    vb = np.ascontiguousarray(b, dtype=np.uint64).view(np.dtype((np.void, 16))).ravel()
+    return len(np.setxor1d(va, vb))
+
+
+def _gpu(inp, mode, block=False):
+    e = eng.Engine(0)
+    E = e.run_input(inp, mode=mode, block=block)
+    out = dict(E=np.asarray(E), dets=e.dets(), ndets=[int(v) for v in e.run_log()["ndets"]])
+    e.close()
+    return out
+
+
+CASES = [
+    # name, schedule, maxiter: the Hubbard ring at its stated schedule, and the
+    # molecular workloads stopped where the oracle finishes in seconds
+    ("hubbard12", [(0, 1e-3), (3, 1e-4)], 6),
+    ("mol24", [(0, 1e-3)], 2),
+    ("mol36", [(0, 3e-3)], 2),
+    ("mol50", [(0, 3e-3)], 2),
+    ("mol64", [(0, 2e-3)], 1),
+]
+
+
+@pytest.mark.parametrize("name,sched,maxiter", CASES, ids=[c[0] for c in CASES])
+def test_fp64_gpu_determinant_sets_equal_the_oracle(tmp_path, name, sched, maxiter):
+    inp = synthetic.make_workload(name, str(tmp_path / name), schedule=sched, maxiter=maxiter)
+    ref = orc.run_input(inp)
+    got = _gpu(inp, "fp64")
+    assert got["ndets"] == [int(v) for v in ref.ndets_log]
+    assert np.array_equal(got["dets"], ref.dets)  # same set, same (reference) index order
+    assert np.max(np.abs(got["E"] - ref.E)) < 1e-9, (got["E"], ref.E)
+
+
+def test_config1_hubbard_ring_stated_schedule_all_paths(tmp_path):
+    """The 12-site Hubbard ring (t = 1, U = 4, 6a + 6b) at its stated
+    schedule (1e-3 for three iterations, then 1e-4, maxiter 6) on the GPU's
+    FP64, mixed and matrix-free paths against the oracle: identical
+    determinants on the FP64 and matrix-free FP64 paths, E_var within 1e-9
+    there and within 1 uHa on the mixed path."""
+    w = synthetic.WORKLOADS["hubbard12"]
+    inp = synthetic.make_workload("hubbard12", str(tmp_path / "h"))
+    ref = orc.run_input(inp)
+    assert [int(v) for v in ref.ndets_log][-1] == len(ref.dets) and len(ref.ndets_log) == w["maxiter"]
+    fp64 = _gpu(inp, "fp64")
+    assert np.array_equal(fp64["dets"], ref.dets)
+    assert abs(fp64["E"][0] - ref.E[0]) < 1e-9
+    direct = synthetic.make_workload("hubbard12", str(tmp_path / "hd"), extra=("DirectDavidson",))
+    dref = orc.run_input(direct)
+    d64 = _gpu(direct, "fp64")
+    assert np.array_equal(d64["dets"], dref.dets)
+    assert abs(d64["E"][0] - dref.E[0]) < 1e-9
+    mixed = _gpu(inp, "mixed")
+    assert abs(mixed["E"][0] - ref.E[0]) < 1e-6
+    print("hubbard12: %d dets, E %.10f; mixed |dS| %d, dE %.2e" % (len(ref.dets), ref.E[0],
+                                                                 sym_diff(mixed["dets"], ref.dets),
+                                                                 mixed["E"][0] - ref.E[0]))
+
+
+@pytest.mark.parametrize("name,sched,maxiter,block", [
+    ("mol24", [(0, 1e-3), (2, 3e-4)], 3, False),
+    ("mol36", [(0, 3e-3)], 2, True),
+], ids=["mol24", "mol36_4roots_block"])
+def test_mixed_path_selects_the_fp64_set_in_parity_mode(tmp_path, name, sched, maxiter, block):
+    inp = synthetic.make_workload(name, str(tmp_path / name), schedule=sched, maxiter=maxiter, extra=PARITY)
+    ref = _gpu(inp, "fp64", block)
+    mix = _gpu(inp, "mixed", block)
+    print(name, "parity mode: ndets", ref["ndets"], mix["ndets"], "dE", mix["E"] - ref["E"])
+    assert mix["ndets"] == ref["ndets"]
+    assert sym_diff(mix["dets"], ref["dets"]) == 0
+    assert np.array_equal(mix["dets"], ref["dets"])
+    assert np.max(np.abs(mix["E"] - ref["E"])) < 1e-6

@@ -464,3 +464,22 @@ def test_packed_sigma_equals_device_sigma(tmp_path, mode, kps):
         torch.cuda.synchronize()
         assert torch.equal(y, y_ref), kp
     e.close()
+
+
+def test_packed_fp64_sigma_on_mixed_build_is_a_state_error(tmp_path):
+    """A mixed build keeps FP32 head + tail values, whose FP64 refinement
+    sigma (float-float, shci_sigma_device) needs the column-major FP64 x; the
+    packed FP64 entry point refuses that matrix instead of computing in
+    another arithmetic than shci_sigma_device."""
+    import torch
+    inp = synthetic.make_workload("mol24", str(tmp_path / "w"), schedule=[(0, 3e-3)], maxiter=1)
+    e = eng.Engine(0)
+    e.run_input(inp, mode="mixed")
+    n = e.ndets()
+    e.ham_build("mixed")
+    x = torch.zeros((n, 1), dtype=torch.float64, device="cuda")
+    y = torch.zeros(n, dtype=torch.float64, device="cuda")
+    with pytest.raises(eng.ShciError) as ei:
+        e.sigma_packed_device(x.data_ptr(), 1, 1, y.data_ptr(), n, mode="fp64")
+    assert ei.value.code == 7
+    e.close()

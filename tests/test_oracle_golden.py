@@ -299,3 +299,24 @@ def test_rank_parallel_sigma_equals_serial_sigma(golden):
         y = o.sigma_mt(x, threads)
         assert np.allclose(y, ref, rtol=1e-12, atol=1e-13 * np.abs(ref).max()), threads
     assert np.array_equal(o.sigma_mt(x, 1), ref)
+
+
+def test_threaded_oracle_run_equals_serial_run(tmp_path):
+    """The oracle's threaded variational run (parents dealt to workers for
+    selection, new Hamiltonian rows built in parallel blocks, the
+    rank-parallel sigma in Davidson), which the reference arm of the benchmark
+    runs on all host cores, selects the serial run's determinants in the same
+    order and lands on the same E_var (the sigma's additions are ordered
+    differently, so the coefficients agree to rounding)."""
+    from dice_gb300 import synthetic
+    inp = synthetic.make_workload("mol24", str(tmp_path / "m"), schedule=[(0, 3e-3)], maxiter=3)
+    serial = orc.run_input(inp)
+    try:
+        orc.set_threads(4)
+        threaded = orc.run_input(inp)
+    finally:
+        orc.set_threads(1)
+    assert len(serial.dets) > 10000
+    assert list(threaded.ndets_log) == list(serial.ndets_log)
+    assert np.array_equal(threaded.dets, serial.dets)
+    assert abs(threaded.E[0] - serial.E[0]) < 1e-10

@@ -26,18 +26,21 @@ def _fcidump(inp):
     return os.path.join(os.path.dirname(inp), "FCIDUMP")
 
 
-@pytest.mark.parametrize("mode", ["mixed", "fp64"])
-def test_noalloc_sigma_matches_regular_sigma(golden, mode):
+# (Hamiltonian build mode, sigma mode): each stored layout the entry point
+# serves, including the FP64 refinement sigma on a mixed build
+@pytest.mark.parametrize("build,mode", [("mixed", "mixed"), ("fp64", "fp64"), ("mixed", "fp64")])
+@pytest.mark.parametrize("k", [1, 2, 3, 4])
+def test_noalloc_sigma_matches_regular_sigma(golden, build, mode, k):
     import torch
     inp = golden("h8_631g", "dice.dat")
     dets = np.load(os.path.join(GOLDEN, "h8_631g_dets.npz"))["dets"]
     e = eng.Engine(0)
     e.read_fcidump(_fcidump(inp))
     e.set_dets(dets)
-    e.ham_build(mode)
+    e.ham_build(build)
     n = len(dets)
-    rng = np.random.default_rng(11)
-    for call, k in ((0, 3), (1, 4)):  # two calls in a row, different vectors
+    rng = np.random.default_rng(11 + k)
+    for call in range(2):  # two calls in a row, different vectors
         x = torch.tensor(rng.standard_normal((k, n)), device="cuda")
         y_ref = torch.zeros_like(x)
         y_new = torch.full_like(x, float("nan"))
@@ -47,6 +50,19 @@ def test_noalloc_sigma_matches_regular_sigma(golden, mode):
         ref, new = y_ref.cpu().numpy(), y_new.cpu().numpy()
         assert np.all(np.isfinite(new)), call
         assert np.allclose(new, ref, rtol=1e-12, atol=1e-12 * np.abs(ref).max()), call
+    e.close()
+
+
+def test_noalloc_sigma_rejects_null_vectors(golden):
+    inp = golden("h8_631g", "dice.dat")
+    dets = np.load(os.path.join(GOLDEN, "h8_631g_dets.npz"))["dets"]
+    e = eng.Engine(0)
+    e.read_fcidump(_fcidump(inp))
+    e.set_dets(dets)
+    e.ham_build("mixed")
+    with pytest.raises(eng.ShciError) as ei:
+        e.sigma_device_noalloc(0, 0, 1, len(dets), mode="mixed")
+    assert ei.value.code == 1 and "null" in str(ei.value)
     e.close()
 
 
