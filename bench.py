@@ -1,28 +1,43 @@
 """Benchmark of the SHCI variational engine on one GB300 (or N replicas).
 
-Workload: the synthetic molecular Hamiltonian with 24 spatial orbitals,
-12 alpha + 12 beta electrons, 72 Cholesky vectors (seeded), eps1 schedule
-1e-3 -> 3e-4 -> 1e-4, one root. The whole variational stage is run in the
-mixed path (FP32 sigma + FP64 refinement) and in the plain FP64 path; the
-timed "step" is then one sigma (y = H x) over the final variational space
-with the Hamiltonian resident in HBM.
+Workload (config 2 of the task's list, the largest whose stated size fits one
+GPU in the stored form): the synthetic molecular Hamiltonian with 24 spatial
+orbitals, 12 alpha + 12 beta electrons, 72 Cholesky vectors (seeded), eps1
+schedule 1e-3 -> 3e-4 -> 1e-4, one root. The whole variational stage runs in
+the plain FP64 path (the reference's algorithm on the GPU), in the mixed
+path with the reference's subspace, in the new form (mixed precision,
+16-vector subspace, graph-captured iterations) with and without the learned
+preconditioner, and in parity mode (loose and final Davidson tolerances both
+1e-8, FP64 and new form). Each run's final determinant set is compared with
+the FP64 run's (|dS| = size of the symmetric difference).
 
-value: sigma Mdets/s (N / t_sigma / 1e6), kernel-only, device-resident
-vectors: two launches per step (shci_sigma_packed_device gathers x into the
-stored matrix's storage order, then runs the sigma). e2e: the same through the C-ABI call with host buffers
-(shci_sigma: host->device copy of x and device->host copy of y inside the
-timed region). Extra keys report the variational wall time and E_var of
-both paths.
+The timed "step" is one sigma (y = H x) over the final space of the FP64 run,
+with the Hamiltonian resident in HBM. That space is the one the reference
+algorithm selects (the oracle's FP64 run reproduces it determinant for
+determinant), so the reference arm times its sigma on the same space.
 
-Further keys: `pt` (deterministic PT2 of the final space, eps2 1e-5, through
+value: sigma Mdets/s (N / t_sigma / 1e6), FP32 (mixed path), kernel-only,
+device-resident vectors: two launches per step (shci_sigma_packed_device
+gathers x into the stored matrix's storage order, then runs the sigma). e2e:
+the same through the C-ABI call with host buffers (shci_sigma: host->device
+copy of x and device->host copy of y inside the timed region).
+
+Further keys: `plain_fp64_sigma`, `block_k4_sigma`, `var` (the runs above),
+`pt` (deterministic PT2 of the final space, eps2 1e-5, through
 shci_pt_deterministic; `--section pt` times it alone), `rdm` (spatial 1- and
-2-RDMs of the final space through shci_run_rdm), each with the CPU oracle on a
-bounded sample beside it, and `configs` (the other synthetic workloads).
+2-RDMs through shci_run_rdm), each with the CPU oracle on a bounded sample
+beside it, and `configs` (the other synthetic workloads, including config 1,
+the 12-site Hubbard ring at its stated schedule, against the CPU oracle).
 
---impl reference: the CPU oracle's restatement of Dice's sigma (Dice itself
-needs Boost and MPI, absent here) timed on a bounded sample of the same
-workload, in the reference's rank-parallel form (rows dealt round-robin to
-one worker per host thread, as Dice's MPI ranks on one node share them).
+cpu_baseline: the oracle's restatement of the reference's rank-parallel
+Hmult2 (rows dealt round-robin to one worker per host thread, private
+accumulators summed) on every CPU_STRIDE-th row of the same final space.
+
+--impl reference: Dice itself needs Boost and MPI, absent here, so the CPU
+oracle (the reference's algorithm restated, threaded as the reference's MPI
+ranks of one node would share the work) runs the same variational schedule
+on the host cores, reproducing the FP64 final space, and its rank-parallel
+sigma over that whole space is timed.
 """
 import argparse
 import json
@@ -39,6 +54,13 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOAD = "mol24"
+WORKLOAD_DESC = ("mol24 (config 2): synthetic molecular FCIDUMP n=24, 12a+12b, rank-72 Cholesky ERIs, seed "
+                 "20260001, eps1 1e-3 -> 3e-4 -> 1e-4, 1 root; sigma over the final space of the FP64 "
+                 "variational run")
+# Davidson tolerance of parity mode (loose and final solves alike)
+PARITY_TOL = 1e-8
+# the CPU baseline of our arm times every CPU_STRIDE-th row of the final space
+CPU_STRIDE = 8
 CPU_SAMPLE_DETS = 100000
 # deterministic PT2 on the final mixed-precision space of the workload
 PT_EPS2 = 1e-5
@@ -116,33 +138,24 @@ def measured_peak_gbs():
     return 6800.0, "fallback"
 
 
-def make_inputs(d, case="full"):
+def make_inputs(d, case="full", extra=()):
     """case "small": the same Hamiltonian stopped after two eps1 = 1e-3
     iterations (about 8e4 determinants, a ~0.8 GB Hamiltonian: larger than L2,
     small enough for a full ncu capture)."""
     from dice_gb300 import synthetic
+    extra = tuple(synthetic.WORKLOADS[WORKLOAD].get("extra", ())) + tuple(extra)
     if case == "small":
-        return synthetic.make_workload(WORKLOAD, d, schedule=[(0, 1e-3)], maxiter=2)
+        return synthetic.make_workload(WORKLOAD, d, schedule=[(0, 1e-3)], maxiter=2, extra=extra)
     if case == "medium":  # ~5.7e5 determinants: x no longer fits L1, a few GB on the device
-        return synthetic.make_workload(WORKLOAD, d, schedule=[(0, 1e-3), (2, 3e-4)], maxiter=3)
-    return synthetic.make_workload(WORKLOAD, d)
+        return synthetic.make_workload(WORKLOAD, d, schedule=[(0, 1e-3), (2, 3e-4)], maxiter=3, extra=extra)
+    return synthetic.make_workload(WORKLOAD, d, extra=extra)
 
 
-def cpu_sample(work_dir, max_dets=CPU_SAMPLE_DETS):
-    """Determinants for the CPU baseline: the first `max_dets` of the space the
-    oracle selects with the first two eps1 = 1e-3 iterations of the workload."""
-    from dice_gb300 import synthetic
-    from oracle import oracle as orc
-    d = os.path.join(work_dir, "cpu_sample")
-    w = dict(synthetic.WORKLOADS[WORKLOAD])
-    inp = synthetic.make_workload(WORKLOAD, d, schedule=[(0, 1e-3)], maxiter=2)
-    run = orc.run_input(inp)
-    dets = run.dets[:max_dets]
-    o = orc.Oracle(os.path.join(d, "FCIDUMP"))
-    t0 = time.perf_counter()
-    rowptr, col, val = o.ham(dets)
-    t_build = time.perf_counter() - t0
-    return o, dets, len(col), t_build, w
+def sym_diff(a, b):
+    """Size of the symmetric difference of two (N, 2) uint64 determinant lists."""
+    va = np.ascontiguousarray(a, dtype=np.uint64).view(np.dtype((np.void, 16))).ravel()
+    vb = np.ascontiguousarray(b, dtype=np.uint64).view(np.dtype((np.void, 16))).ravel()
+    return int(len(np.setxor1d(va, vb)))
 
 
 def host_threads():
@@ -152,10 +165,24 @@ def host_threads():
         return os.cpu_count() or 1
 
 
-def time_cpu_sigma(o, n, threads, seconds=10.0, max_reps=200):
-    """The oracle's restatement of the reference's rank-parallel Hmult2
-    (rows dealt round-robin to `threads` workers, private accumulators,
-    summed), timed on the host cores."""
+def bench_config(world):
+    """The `config` object both arms print (the same workload and space)."""
+    return {"workload": WORKLOAD_DESC, "k_vectors": 1,
+            "l2": "inputs larger than L2: the final-space Hamiltonian is tens of GB (5.4e9 nonzeros); no flush",
+            "parallelism": "replicas" if world > 1 else "single GPU"}
+
+
+def cpu_rows_sample(fcidump, dets, threads, stride=CPU_STRIDE, seconds=10.0, max_reps=50):
+    """The oracle's restatement of the reference's rank-parallel Hmult2 on
+    every stride-th row of the space `dets` (rows dealt round-robin to
+    `threads` workers, private full-length accumulators, summed), timed on
+    the host cores. Returns (oracle, rows in the sample, lower-triangle
+    entries, seconds per pass, passes)."""
+    from oracle import oracle as orc
+    orc.set_threads(threads)
+    o = orc.Oracle(fcidump)
+    nnz = o.ham_rows(dets, stride)
+    n = len(dets)
     x = np.random.default_rng(1).standard_normal(n)
     o.sigma_mt(x, threads)  # warm-up
     times = []
@@ -164,43 +191,56 @@ def time_cpu_sigma(o, n, threads, seconds=10.0, max_reps=200):
         t0 = time.perf_counter()
         o.sigma_mt(x, threads)
         times.append(time.perf_counter() - t0)
-    return times
+    return o, (n + stride - 1) // stride, nnz, statistics.mean(times), len(times)
 
 
 def run_reference(args):
+    """The reference arm: the oracle (the reference's variational algorithm
+    restated, with worker threads standing in for the MPI ranks of one node)
+    runs the workload's whole FP64 variational schedule on the host cores,
+    which reproduces the final space the GPU arm times, then times the
+    reference's rank-parallel Hmult2 over that whole space."""
     rank, world, _ = dist_info()
     if rank != 0:
         return
     from oracle import oracle as orc
     orc.build()
+    threads = host_threads()
+    orc.set_threads(threads)
     with tempfile.TemporaryDirectory() as d:
-        o, dets, nnz_lower, t_build, w = cpu_sample(d)
-        n = len(dets)
-        threads = host_threads()
+        inp = make_inputs(d, args.case)
+        t0 = time.perf_counter()
+        run = orc.run_input(inp)
+        t_var = time.perf_counter() - t0
+        o = run.oracle
+        n = len(run.dets)
         x = np.random.default_rng(1).standard_normal(n)
         for _ in range(args.warmup):
             o.sigma_mt(x, threads)
         times = []
         for _ in range(args.steps):
-            t0 = time.perf_counter()
+            t1 = time.perf_counter()
             o.sigma_mt(x, threads)
-            times.append(time.perf_counter() - t0)
+            times.append(time.perf_counter() - t1)
     t = statistics.mean(times)
     val = n / t / 1e6
-    sample = ("first %d determinants of the eps1=1e-3 space of the workload (oracle selection), "
-              "lower-triangle nnz %d; the reference's rank-parallel Hmult2 (symmetric scatter in FP64, rows "
-              "dealt round-robin to %d host threads standing in for its MPI ranks, private accumulators "
-              "summed)" % (n, nnz_lower, threads))
+    nnz_full = 2 * int(run.nnz_lower) - n
+    sample = ("the whole final space (%d determinants, %d lower-triangle entries) of the oracle's FP64 run of the "
+              "workload's schedule; the reference's rank-parallel Hmult2 (symmetric scatter in FP64, rows dealt "
+              "round-robin to %d host threads standing in for its MPI ranks, private accumulators summed)"
+              % (n, run.nnz_lower, threads))
     line = {"metric": "sigma Mdets/s (SHCI variational, stored H)", "value": val, "unit": "Mdets/s",
             "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "mol24: synthetic molecular FCIDUMP n=24, 12a+12b, rank-72 Cholesky ERIs, seed 20260001",
-                       "sample": sample},
+            "dtype": "f64", "data": "synthetic", "config": bench_config(world),
+            "space": {"n_dets": n, "nnz_offdiag": nnz_full - n, "nnz_lower": int(run.nnz_lower),
+                      "ndets_per_iteration": [int(v) for v in run.ndets_log], "E_var": float(run.E[0])},
+            "gnnz_s": nnz_full / t / 1e9,
+            "var_wall_s": t_var,
             "cpu_baseline": {"value": val, "unit": "Mdets/s", "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": val, "unit": "Mdets/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "note": "Dice cannot be built here (needs Boost and MPI); the CPU oracle restating its rank-parallel "
-                    "sigma is timed"}
+            "note": "Dice cannot be built here (needs Boost and MPI); the CPU oracle restating its variational "
+                    "loop and rank-parallel sigma is run and timed"}
     print(json.dumps(line), flush=True)
 
 
@@ -270,15 +310,15 @@ def rdm_section(e, nnz_offdiag, cpu):
            "n_dets": e.ndets(), "connections": conn, "seconds": t, "Gconn_s": conn / t / 1e9,
            "trace_1rdm": float(np.trace(s1))}
     if cpu is not None:
-        o, n, nnz_lower = cpu
+        o, n, rows, nnz_lower = cpu
         x = np.random.default_rng(3).standard_normal(n)
         x /= np.linalg.norm(x)
         t0 = time.perf_counter()
         o.rdm_on_ham(x)
         tc = time.perf_counter() - t0
-        out["cpu_oracle"] = {"Gconn_s": (nnz_lower - n) / tc / 1e9, "cores": 1, "kind": "port", "seconds": tc,
-                             "sample": "first %d determinants of the eps1=1e-3 space, %d connected pairs"
-                                       % (n, nnz_lower - n)}
+        out["cpu_oracle"] = {"Gconn_s": (nnz_lower - rows) / tc / 1e9, "cores": 1, "kind": "port", "seconds": tc,
+                             "sample": "every %d-th row of the same final space (%d rows), %d connected pairs"
+                                       % (CPU_STRIDE, rows, nnz_lower - rows)}
         out["speedup_vs_cpu_oracle"] = out["Gconn_s"] / out["cpu_oracle"]["Gconn_s"]
     return out
 
@@ -330,6 +370,29 @@ def other_configs(work, device):
                 "ndets": [int(v) for v in lg["ndets"]]}
 
     out = {}
+    # config 1: the 12-site Hubbard ring at its stated schedule, GPU paths
+    # against the oracle's serial run on one host core
+    from oracle import oracle as orc
+    hub = synthetic.make_workload("hubbard12", os.path.join(work, "hubbard12"))
+    orc.set_threads(1)
+    t0 = time.perf_counter()
+    oref = orc.run_input(hub)
+    t_orc = time.perf_counter() - t0
+    res = {}
+    for key, mode, basis in (("fp64", "fp64", (0, 0)), ("new_form", "mixed", (16, 8))):
+        g = eng.Engine(device)
+        g.set_davidson_basis(*basis)
+        E = g.run_input(hub, mode=mode)
+        t = g.timings()
+        res[key] = {"E_var": float(E[0]), "wall_s": t["total"], "ndets": [int(v) for v in g.run_log()["ndets"]],
+                    "dS_vs_oracle": sym_diff(g.dets(), oref.dets), "dE_vs_oracle": float(E[0] - oref.E[0])}
+        g.close()
+    out["hubbard12_config1"] = {
+        "what": "1-D Hubbard ring, 12 sites, t=1, U=4, 6a+6b, eps1 1e-3 (x3) then 1e-4, maxiter 6, 1 root, "
+                "stated schedule; GPU FP64 and new form against the oracle's FP64 run",
+        "oracle": {"E_var": float(oref.E[0]), "wall_s": t_orc, "ndets": [int(v) for v in oref.ndets_log],
+                   "cores": 1, "kind": "port"},
+        **res, "fp64_speedup_vs_oracle": t_orc / res["fp64"]["wall_s"]}
     sched = [(0, 1e-3)]
     ref = run("mol36", sched, 2, "fp64", True)
     new = run("mol36", sched, 2, "mixed", True, basis=(16, 12))
@@ -362,25 +425,52 @@ def run_ours(args):
 
     work = tempfile.mkdtemp()
     inp = make_inputs(work, args.case)
+    inp_parity = make_inputs(os.path.join(work, "parity"), args.case,
+                             extra=("davidsonTol %g" % PARITY_TOL, "davidsonTolLoose %g" % PARITY_TOL))
     e = eng.Engine(local)
 
-    # whole variational stage, four ways: the new form (mixed precision with
-    # a 16-vector Davidson subspace), the same with the learned
-    # preconditioner, the plain FP64 path (the reference's algorithm), then
-    # the mixed path with the reference's subspace, whose final space the
-    # sigma steps below run on
-    def var_run(mode, precond, basis):
+    # the whole variational stage, six ways; the plain FP64 run (the
+    # reference's algorithm) comes last, so that its final space, the one the
+    # reference arm reproduces, stays resident for the sigma steps below
+    def var_run(what, path, mode, precond, basis):
         e.set_preconditioner(precond)
         e.set_davidson_basis(*basis)
-        E = e.run_input(inp, mode=mode)
-        return E, e.timings(), e.run_stats(), e.run_log()
+        E = e.run_input(path, mode=mode)
+        t, st, lg = e.timings(), e.run_stats(), e.run_log()
+        return {"E_var": float(E[0]), "wall_s": t["total"], "stages_s": t, "what": what,
+                "davidson_iters_total": int(st["davidson_iters"]), "mlp_train_s": st["t_mlp"],
+                "ndets": [int(v) for v in lg["ndets"]], "davidson_iters": [int(v) for v in lg["davidson"]],
+                "_dets": e.dets()}
 
-    Enf, tnf, snf, lognf = var_run("mixed", "plain", (16, 8))
-    Eml, tml, sml, logml = var_run("mixed", "mlp", (16, 8))
-    E64, t64, s64, log64 = var_run("fp64", "plain", (0, 0))
-    E32, t32, s32, log32 = var_run("mixed", "plain", (0, 0))
+    NF = "mixed precision (FP32 sigma, float-float refinement) + 16-vector Davidson subspace collapsed to 8, " \
+         "graph-captured iterations"
+    runs = {
+        "new_form": var_run(NF, inp, "mixed", "plain", (16, 8)),
+        "new_form_mlp": var_run("new form + learned (BF16 MLP) preconditioner trained during the run", inp, "mixed",
+                                "mlp", (16, 8)),
+        "mixed": var_run("mixed precision with the reference's Davidson subspace", inp, "mixed", "plain", (0, 0)),
+        "parity_fp64": var_run("parity mode, plain FP64 path: loose and final Davidson tolerance %g" % PARITY_TOL,
+                               inp_parity, "fp64", "plain", (0, 0)),
+        "parity_new_form": var_run("parity mode, new form: loose and final Davidson tolerance %g" % PARITY_TOL,
+                                   inp_parity, "mixed", "plain", (16, 8)),
+        "fp64": var_run("plain FP64 GPU path: the reference's algorithm", inp, "fp64", "plain", (0, 0)),
+    }
     N = e.ndets()
-    dets_mixed = e.dets()
+    dets_fp64 = runs["fp64"]["_dets"]
+    ref64 = runs["fp64"]
+    for key, r in runs.items():
+        if key.startswith("parity"):
+            continue
+        r["dS_vs_fp64"] = sym_diff(r["_dets"], dets_fp64)
+        r["dE_vs_fp64"] = r["E_var"] - ref64["E_var"]
+        r["wall_speedup_vs_fp64"] = ref64["wall_s"] / r["wall_s"]
+    var = {k: {kk: vv for kk, vv in r.items() if not kk.startswith("_")} for k, r in runs.items()}
+    var["parity_mode"] = {
+        "dS_new_form_vs_fp64": sym_diff(runs["parity_new_form"]["_dets"], runs["parity_fp64"]["_dets"]),
+        "dE_new_form_minus_fp64": runs["parity_new_form"]["E_var"] - runs["parity_fp64"]["E_var"],
+        "dS_parity_fp64_vs_default_fp64": sym_diff(runs["parity_fp64"]["_dets"], dets_fp64),
+        "wall_speedup_new_form_vs_fp64": runs["parity_fp64"]["wall_s"] / runs["parity_new_form"]["wall_s"]}
+    del runs
 
     stream = torch.cuda.ExternalStream(e.stream, device=torch.device("cuda", local))
     k = 1
@@ -417,9 +507,9 @@ def run_ours(args):
         return nnz, ts, launches, flush is not None, y, e.sigma_bytes(mode, kp)
 
     x_dev = torch.tensor(x_host, device="cuda")
-    # plain FP64 sigma on the final space of the mixed run
+    # plain FP64 sigma on the FP64 run's matrix
     nnz64, ts64, _, _, y64, alg64 = timed_sigma("fp64", x_dev, max(3, args.steps // 2), args.warmup)
-    # mixed FP32 sigma (the timed region of `value`)
+    # mixed FP32 sigma (the timed region of `value`) on the same space
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -455,29 +545,28 @@ def run_ours(args):
 
     cpu = None
     cpu_rdm = None
+    fcidump = os.path.join(os.path.dirname(inp), "FCIDUMP")
     if rank == 0 and not args.no_cpu:
         from oracle import oracle as orc
         orc.build()
-        o, dets, nnz_lower, t_build, _ = cpu_sample(work)
-        cpu_rdm = (o, len(dets), nnz_lower)
         threads = host_threads()
-        tc = time_cpu_sigma(o, len(dets), threads)
-        cpu = {"value": len(dets) / statistics.mean(tc) / 1e6, "unit": "Mdets/s", "cores": threads, "kind": "port",
-               "sample": "first %d determinants of the eps1=1e-3 space of the workload; the oracle's restatement "
-                         "of the reference's rank-parallel Hmult2 (FP64 symmetric scatter, %d host threads as "
-                         "its MPI ranks), %d reps" % (len(dets), threads, len(tc))}
+        o, rows, nnz_rows, tc, reps = cpu_rows_sample(fcidump, dets_fp64, threads)
+        cpu_rdm = (o, N, rows, nnz_rows)
+        cpu = {"value": rows / tc / 1e6, "unit": "Mdets/s", "cores": threads, "kind": "port",
+               "sample": "every %d-th row of the same final space (%d of %d rows, %d lower-triangle entries); the "
+                         "oracle's restatement of the reference's rank-parallel Hmult2 (FP64 symmetric scatter, %d "
+                         "host threads as its MPI ranks, private full-length accumulators summed), %d passes"
+                         % (CPU_STRIDE, rows, N, nnz_rows, threads, reps)}
 
     line = {
         "metric": "sigma Mdets/s (SHCI variational, stored H)", "value": value, "unit": "Mdets/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 diagonal, FP64 refinement)",
         "data": "synthetic",
-        "config": {"workload": "mol24: synthetic molecular FCIDUMP n=24, 12a+12b, rank-72 Cholesky ERIs, "
-                               "seed 20260001, eps1 1e-3 -> 3e-4 -> 1e-4, 1 root",
-                   "n_dets": N, "nnz_offdiag": nnz, "k_vectors": k,
-                   "l2": "L2 flushed between steps (256 MiB write)" if flushed else
-                         "Hamiltonian (%.1f GB) larger than L2; no flush" % (nnz * 8 / 1e9),
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": bench_config(world),
+        "space": {"n_dets": N, "nnz_offdiag": nnz, "ndets_per_iteration": var["fp64"]["ndets"],
+                  "E_var": var["fp64"]["E_var"]},
+        "gnnz_s": (nnz + N) / t_max / 1e9,
         "e2e": {"value": e2e, "unit": "Mdets/s", "h2d_bytes_per_step": N * k * 8, "d2h_bytes_per_step": N * k * 8},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -489,37 +578,12 @@ def run_ours(args):
         "block_k4_sigma": {"mdets_s": 4 * N / t4 / 1e6, "ms": t4 * 1e3, "achieved_gbs": alg4 / t4 / 1e9,
                            "frac": alg4 / t4 / 1e9 / peak},
         "sigma_rel_err_fp32_vs_fp64": sig_err,
-        "var": {"new_form": {"wall_s": tnf["total"], "E_var": float(Enf[0]), "stages_s": tnf,
-                             "what": "mixed precision (FP32 sigma, float-float refinement) + 16-vector Davidson "
-                                     "subspace collapsed to 8, graph-captured iterations",
-                             "davidson_iters_total": snf["davidson_iters"],
-                             "ndets": [int(v) for v in lognf["ndets"]],
-                             "davidson_iters": [int(v) for v in lognf["davidson"]]},
-                "new_form_mlp": {"wall_s": tml["total"], "E_var": float(Eml[0]), "stages_s": tml,
-                                 "what": "new form + learned (BF16 MLP) preconditioner trained during the run",
-                                 "davidson_iters_total": sml["davidson_iters"], "mlp_train_s": sml["t_mlp"],
-                                 "davidson_iters": [int(v) for v in logml["davidson"]]},
-                "mixed": {"wall_s": t32["total"], "E_var": float(E32[0]), "stages_s": t32,
-                          "what": "mixed precision with the reference's Davidson subspace",
-                          "davidson_iters_total": s32["davidson_iters"],
-                          "ndets": [int(v) for v in log32["ndets"]], "davidson_iters": [int(v) for v in log32["davidson"]]},
-                "fp64": {"wall_s": t64["total"], "E_var": float(E64[0]), "stages_s": t64,
-                         "what": "plain FP64 GPU path: the reference's algorithm",
-                         "davidson_iters_total": s64["davidson_iters"],
-                         "ndets": [int(v) for v in log64["ndets"]], "davidson_iters": [int(v) for v in log64["davidson"]]},
-                "dE_mixed_minus_fp64": float(E32[0] - E64[0]),
-                "wall_speedup_mixed_vs_fp64": t64["total"] / t32["total"],
-                "dE_new_form_minus_fp64": float(Enf[0] - E64[0]),
-                "wall_speedup_new_form_vs_fp64": t64["total"] / tnf["total"],
-                "davidson_speedup_new_form_vs_fp64": t64["davidson"] / tnf["davidson"],
-                "dE_new_form_mlp_minus_fp64": float(Eml[0] - E64[0]),
-                "wall_speedup_new_form_mlp_vs_fp64": t64["total"] / tml["total"]},
+        "var": var,
         "clocks": clk, "timed_wall_s": wall,
     }
     if cpu:
         line["cpu_baseline"] = cpu
-    line["pt"] = pt_section(e, float(E32[0]), args.steps, rank == 0 and not args.no_cpu,
-                            os.path.join(os.path.dirname(inp), "FCIDUMP"))
+    line["pt"] = pt_section(e, var["fp64"]["E_var"], args.steps, rank == 0 and not args.no_cpu, fcidump)
     line["rdm"] = rdm_section(e, nnz, cpu_rdm)
     e.close()
     if args.case == "full" and not args.no_configs:

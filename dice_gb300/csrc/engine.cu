@@ -181,6 +181,7 @@ struct Context {
   Prims prims;
   DevBuf<int64_t> counter;
   DevBuf<Det2> cand;
+  size_t ncand = 0;  // candidates of the last shci_select_candidates left in cand
 
   // Davidson workspace
   DevBuf<double> V, W, Vt, Wt, X, Y, R, D, xb64, yb64, gpart, dG, dQ, dlam, dsmall, ftmp;
@@ -397,6 +398,14 @@ struct Context {
 
   // Heat-bath selection from every current determinant; appends new ones.
   int64_t select(const double* cmax_dev, double eps1) {
+    const size_t nnew = candidates(cmax_dev, eps1);
+    append_candidates(nnew);
+    return (int64_t)nnew;
+  }
+
+  // The new determinants of a selection (parents with cMax 0 contribute
+  // none), sorted in the reference's order and unique, left in cand[0, n).
+  size_t candidates(const double* cmax_dev, double eps1) {
     require_ints();
     require_dets();
     hash.build(dets.p, ndet, stream);
@@ -419,6 +428,14 @@ struct Context {
       sort_dets(cand.p, nullptr, (size_t)total, prims, stream);
       nnew = unique_dets(cand.p, (size_t)total, prims, stream);
     }
+    SHCI_CUDA(cudaStreamSynchronize(stream));
+    ncand = nnew;
+    return nnew;
+  }
+
+  // Appends cand[0, nnew) to the space (new determinants in sorted order, as
+  // the reference appends them, SHCI/SHCIbasics.cpp:1059-1077).
+  void append_candidates(size_t nnew) {
     if (nnew) {
       if (ndet + nnew >= (size_t)0x7fffffff) throw Error(kErrInvalid, "determinant space exceeds 2^31 entries");
       dets.grow_keep(ndet + nnew, stream);
@@ -427,8 +444,36 @@ struct Context {
       ndet += nnew;
       invalidate_space();
     }
+    ncand = 0;
     SHCI_CUDA(cudaStreamSynchronize(stream));
-    return (int64_t)nnew;
+  }
+
+  // Appends host determinants (the merged new determinants of a sharded
+  // selection): they must follow the reference's order strictly, carry the
+  // right electron count and be absent from the space.
+  void append_dets(const uint64_t* h, int64_t n) {
+    require_ints();
+    require_dets();
+    if (n < 0) throw Error(kErrInvalid, "negative determinant count");
+    if (n == 0) return;
+    for (int64_t i = 0; i < n; ++i) {
+      const uint64_t w0 = h[2 * i], w1 = h[2 * i + 1];
+      if (__builtin_popcountll(w0) + __builtin_popcountll(w1) != hints.nelec)
+        throw Error(kErrInvalid, "appended determinant " + std::to_string(i) + " has the wrong electron count");
+      if (i > 0) {  // Determinant::operator<: signed words from the top (SHCI/Determinants.h:490-498)
+        const int64_t a1 = (int64_t)h[2 * i - 1], b1 = (int64_t)w1;
+        const int64_t a0 = (int64_t)h[2 * i - 2], b0 = (int64_t)w0;
+        if (!(a1 < b1 || (a1 == b1 && a0 < b0)))
+          throw Error(kErrInvalid, "appended determinants must be sorted and unique");
+      }
+    }
+    hash.build(dets.p, ndet, stream);
+    cand.reserve((size_t)n);
+    SHCI_CUDA(cudaMemcpyAsync(cand.p, h, (size_t)n * sizeof(Det2), cudaMemcpyHostToDevice, stream));
+    counter.resize(1);
+    if (count_present(cand.p, (size_t)n, hash, dets.p, counter.p, stream) != 0)
+      throw Error(kErrInvalid, "appended determinants must be absent from the space");
+    append_candidates((size_t)n);
   }
 
   void ensure_diag() {
@@ -440,6 +485,8 @@ struct Context {
   }
 
   static bool is_direct(int m) { return m == SHCI_MODE_DIRECT || m == SHCI_MODE_DIRECT_MIXED; }
+  // a stored Hamiltonian of the whole space (not matrix-free, not a row block)
+  bool whole_ham() const { return ham_ok && !is_direct(ham_mode) && !H.block; }
 
   // Spatial 2-RDM (n^4) and 1-RDM (n^2) of the wavefunction c (device, ndet
   // entries) to the host (either may be null), over the connection lists of
@@ -450,7 +497,7 @@ struct Context {
     require_ints();
     require_dets();
     const double t0 = now_s();
-    if (!ham_ok || is_direct(ham_mode)) build_ham(SHCI_MODE_MIXED);
+    if (!whole_ham()) build_ham(SHCI_MODE_MIXED);
     const size_t n = (size_t)hints.norb, n2 = n * n, n4 = n2 * n2;
     rdm_evaluate(dets.p, c, ndet, H, hints.norb, rdm_fix, rdm_out, stream);
     if (s2) SHCI_CUDA(cudaMemcpyAsync(s2, rdm_out.p, n4 * sizeof(double), cudaMemcpyDeviceToHost, stream));
@@ -579,7 +626,7 @@ struct Context {
     } else {
       // the stored rows stay valid for the unchanged prefix of the space
       // (selection only appends), so only new rows and columns are built
-      const size_t n_old = (ham_mode == mode) ? H.N : 0;
+      const size_t n_old = (ham_mode == mode && !H.block) ? H.N : 0;
       H.drop_compressed();  // stale; rebuilt below (frees its memory before the build)
       build_ham_csr(helpers, dets.p, ints(), H, mode == SHCI_MODE_FP64, mode == SHCI_MODE_MIXED,
                     mode == SHCI_MODE_MIXED, n_old, prims, stream);
@@ -587,6 +634,29 @@ struct Context {
       pt.mark("ham compress");
       noalloc_ptr = noalloc_scratch_address();
     }
+    ham_mode = mode;
+    ham_ok = true;
+    SHCI_CUDA(cudaStreamSynchronize(stream));
+  }
+
+  // One rank's share of the stored Hamiltonian in the sharded path: the full
+  // rows of the determinants [r0, r1) (shci_ham_build_rows).
+  void build_ham_rows(int mode, size_t r0, size_t r1) {
+    require_ints();
+    require_dets();
+    if (mode != SHCI_MODE_FP64 && mode != SHCI_MODE_MIXED)
+      throw Error(kErrInvalid, "a row block is stored: mode must be SHCI_MODE_FP64 or SHCI_MODE_MIXED");
+    if (!(r0 < r1 && r1 <= ndet)) throw Error(kErrInvalid, "row block [r0, r1) must be a non-empty range of the space");
+    if (!helpers_ok) {
+      helpers.build(dets.p, ndet, hints.norb, prims, stream);
+      helpers_ok = true;
+    }
+    ensure_diag();
+    ham_ok = false;
+    build_ham_block(helpers, dets.p, ints(), H, mode == SHCI_MODE_FP64, mode == SHCI_MODE_MIXED,
+                    mode == SHCI_MODE_MIXED, r0, r1, prims, stream);
+    if (mode == SHCI_MODE_MIXED) compress_csr(H, prims, stream);
+    noalloc_ptr = noalloc_scratch_address();
     ham_mode = mode;
     ham_ok = true;
     SHCI_CUDA(cudaStreamSynchronize(stream));
@@ -609,16 +679,16 @@ struct Context {
       const int kp = kk == 3 ? 4 : kk;
       if (mode == SHCI_MODE_MIXED) {
         xb32.reserve(N * kp);
-        pack_f32(A, lda, c0 + done, kk, kp, N, xb32.p, stream, H.perm.p);
+        pack_f32(A, lda, c0 + done, kk, kp, N, xb32.p, stream, H.pack_perm());
         sigma_csr_mixed(H, diag.p, xb32.p, kp, kk, Yp + (size_t)(yc0 + done) * ldy, ldy, stream);
       } else if (mode == SHCI_MODE_FP64) {
         xb64.reserve(N * kp);
         if (H.v64.p) {
-          pack_f64(A, lda, c0 + done, kk, kp, N, xb64.p, stream, H.perm.p);
+          pack_f64(A, lda, c0 + done, kk, kp, N, xb64.p, stream, H.pack_perm());
           sigma_csr_f64(H, diag.p, xb64.p, kp, kk, Yp + (size_t)(yc0 + done) * ldy, ldy, stream);
         } else {  // mixed-path matrix: float-float refinement sigma on head + tail
           float* xff = reinterpret_cast<float*>(xb64.p);
-          pack_ff(A, lda, c0 + done, kk, kp, N, xff, stream, H.perm.p);
+          pack_ff(A, lda, c0 + done, kk, kp, N, xff, stream, H.pack_perm());
           sigma_csr_ff(H, diag.p, xff, kp, A, lda, c0 + done, kk, Yp + (size_t)(yc0 + done) * ldy, ldy, stream);
         }
       } else if (mode == SHCI_MODE_DIRECT_MIXED) {  // FP32 matrix-free
@@ -1044,7 +1114,7 @@ struct Context {
     if (precond == 0 || !(E == E) || ndet == 0) return;
     shift.resize(ndet);
     if (precond == 1) {
-      if (!ham_ok || is_direct(ham_mode)) return;
+      if (!whole_ham()) return;
       pt2_shift(H, diag.p, E, shift.p, pt2inv, stream);
       shift_ready = true;
     } else if (precond == 2 && mlp.trained && mlp.nspin == 2 * hints.norb) {
@@ -1058,7 +1128,7 @@ struct Context {
   // final minibatch loss.
   // steps: Adam steps of this call (0 = mlp_steps)
   double train_mlp(double E, int steps = 0) {
-    if (!ham_ok || is_direct(ham_mode)) throw Error(kErrState, "training needs a stored Hamiltonian");
+    if (!whole_ham()) throw Error(kErrState, "training needs the stored Hamiltonian of the whole space");
     ensure_diag();
     if (mlp.nspin != 2 * hints.norb) mlp.init(2 * hints.norb, 7, stream);
     PhaseTimer pt(stream);
@@ -1090,6 +1160,9 @@ struct Context {
   void davidson(int mode, bool block, int nroots, double* x, int maxCopies, double tol, bool direct_rules,
                 std::vector<double>& E, int& iters, double E_est = std::nan("")) {
     if (!ham_ok) throw Error(kErrState, "Hamiltonian not built for the current space (call shci_ham_build)");
+    if (H.block)
+      throw Error(kErrState, "the stored Hamiltonian is a row block (shci_ham_build_rows); Davidson needs the whole "
+                             "matrix on this context (shci_ham_build)");
     ensure_diag();
     prepare_shift(E_est);
     if (mode == SHCI_MODE_MIXED || mode == SHCI_MODE_DIRECT_MIXED) {
@@ -1561,6 +1634,41 @@ int shci_select(shci_ctx* ctx, const double* cmax, double eps1, int64_t* n_new) 
   });
 }
 
+int shci_select_candidates(shci_ctx* ctx, const double* cmax, double eps1, int rank, int world, int64_t* n_new) {
+  return guarded(ctx, [&](Context& c) {
+    c.require_dets();
+    if (!cmax) throw Error(SHCI_ERR_INVALID, "null cmax");
+    if (world < 1 || rank < 0 || rank >= world) throw Error(SHCI_ERR_INVALID, "need 0 <= rank < world");
+    // this rank's parents are the determinants i with i % world == rank
+    // (SHCI/SHCIbasics.cpp:969-970); the others get cMax 0, which the
+    // selection skips
+    std::vector<double> own(c.ndet, 0.0);
+    for (size_t i = (size_t)rank; i < c.ndet; i += (size_t)world) own[i] = cmax[i];
+    c.cmax.resize(c.ndet);
+    SHCI_CUDA(cudaMemcpyAsync(c.cmax.p, own.data(), c.ndet * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    const size_t k = c.candidates(c.cmax.p, eps1);
+    if (n_new) *n_new = (int64_t)k;
+  });
+}
+
+int shci_candidates_get(shci_ctx* ctx, uint64_t* out, int64_t cap) {
+  return guarded(ctx, [&](Context& c) {
+    if (cap < (int64_t)c.ncand) throw Error(SHCI_ERR_INVALID, "output too small for the candidates");
+    if (c.ncand) {
+      if (!out) throw Error(SHCI_ERR_INVALID, "null output");
+      SHCI_CUDA(cudaMemcpyAsync(out, c.cand.p, c.ncand * sizeof(shci::Det2), cudaMemcpyDeviceToHost, c.stream));
+      SHCI_CUDA(cudaStreamSynchronize(c.stream));
+    }
+  });
+}
+
+int shci_dets_append(shci_ctx* ctx, const uint64_t* dets, int64_t n) {
+  return guarded(ctx, [&](Context& c) {
+    if (n > 0 && !dets) throw Error(SHCI_ERR_INVALID, "null determinants");
+    c.append_dets(dets, n);
+  });
+}
+
 int shci_ham_build(shci_ctx* ctx, int mode, int64_t* nnz) {
   return guarded(ctx, [&](Context& c) {
     c.build_ham(mode);
@@ -1568,9 +1676,17 @@ int shci_ham_build(shci_ctx* ctx, int mode, int64_t* nnz) {
   });
 }
 
+int shci_ham_build_rows(shci_ctx* ctx, int mode, int64_t r0, int64_t r1, int64_t* nnz) {
+  return guarded(ctx, [&](Context& c) {
+    if (r0 < 0 || r1 < 0) throw Error(SHCI_ERR_INVALID, "negative row index");
+    c.build_ham_rows(mode, (size_t)r0, (size_t)r1);
+    if (nnz) *nnz = c.H.nnz;
+  });
+}
+
 int shci_ham_export(shci_ctx* ctx, int64_t* rowptr, int32_t* col, double* val) {
   return guarded(ctx, [&](Context& c) {
-    if (!c.ham_ok || Context::is_direct(c.ham_mode)) throw Error(SHCI_ERR_STATE, "no stored Hamiltonian");
+    if (!c.whole_ham()) throw Error(SHCI_ERR_STATE, "no stored Hamiltonian of the whole space");
     // the stored matrix is in storage order (sorted by alpha, then beta
     // string); the export is in the determinant order of shci_dets_get with
     // every row's columns ascending
@@ -1654,7 +1770,7 @@ int shci_sigma_packed_device(shci_ctx* ctx, int mode, const void* x_packed, int 
   return guarded(ctx, [&](Context& c) {
     if (!(kp == 1 || kp == 2 || kp == 4) || k < 1 || k > kp) throw Error(SHCI_ERR_INVALID, "need k <= kp in {1,2,4}");
     if (!x_packed || !y_dev) throw Error(SHCI_ERR_INVALID, "null vector");
-    if (!c.ham_ok || Context::is_direct(c.ham_mode)) throw Error(SHCI_ERR_STATE, "no stored Hamiltonian");
+    if (!c.whole_ham()) throw Error(SHCI_ERR_STATE, "no stored Hamiltonian of the whole space");
     if (ld < (int64_t)c.ndet) throw Error(SHCI_ERR_INVALID, "leading dimension smaller than N");
     c.ensure_diag();
     // x_packed is in the determinant array's order: its rows are gathered
@@ -1689,7 +1805,7 @@ int shci_sigma_device_noalloc(shci_ctx* ctx, int mode, const double* x_dev, doub
       throw Error(SHCI_ERR_INVALID, "allocation-free sigma: N x k needs " + std::to_string(need) +
                                         " bytes of scratch, more than its fixed " +
                                         std::to_string(shci::kNoAllocPackBytes) + " bytes");
-    if (!c.ham_ok || Context::is_direct(c.ham_mode)) throw Error(SHCI_ERR_STATE, "no stored Hamiltonian");
+    if (!c.whole_ham()) throw Error(SHCI_ERR_STATE, "no stored Hamiltonian of the whole space");
     if (mode == SHCI_MODE_MIXED && c.ham_mode != SHCI_MODE_MIXED)
       throw Error(SHCI_ERR_STATE, "mixed sigma needs a Hamiltonian built in mixed mode");
     if (c.ndiag < c.ndet) throw Error(SHCI_ERR_STATE, "diagonal not computed (call shci_ham_build first)");
@@ -1710,7 +1826,7 @@ int shci_ham_bytes(shci_ctx* ctx, int64_t* csr_bytes, int64_t* helper_bytes) {
 int shci_sigma_bytes(shci_ctx* ctx, int mode, int k, int64_t* bytes) {
   return guarded(ctx, [&](Context& c) {
     if (!bytes || k < 1 || k > 4) throw Error(SHCI_ERR_INVALID, "need bytes and 1 <= k <= 4");
-    if (!c.ham_ok || Context::is_direct(c.ham_mode)) throw Error(SHCI_ERR_STATE, "no stored Hamiltonian");
+    if (!c.whole_ham()) throw Error(SHCI_ERR_STATE, "no stored Hamiltonian of the whole space");
     const int64_t N = (int64_t)c.H.N, nnz = c.H.nnz;
     int64_t b = 0;
     if (mode == SHCI_MODE_MIXED && k == 1 && c.H.cvalid)  // 16-bit deltas + FP32 values, row bases
@@ -1956,7 +2072,7 @@ int shci_set_davidson_graphs(shci_ctx* ctx, int on) {
 
 int shci_pt2_shift(shci_ctx* ctx, double E, double* out) {
   return guarded(ctx, [&](Context& c) {
-    if (!c.ham_ok || Context::is_direct(c.ham_mode)) throw Error(SHCI_ERR_STATE, "no stored Hamiltonian");
+    if (!c.whole_ham()) throw Error(SHCI_ERR_STATE, "no stored Hamiltonian of the whole space");
     c.ensure_diag();
     c.teacher.resize(c.ndet);
     shci::pt2_shift(c.H, c.diag.p, E, c.teacher.p, c.pt2inv, c.stream);

@@ -84,9 +84,27 @@ struct Csr {
   DevBuf<float> cval;
   int64_t cnnz = 0;
   bool cvalid = false;
+  // Row block (build_ham_block): N local rows, the full rows of the
+  // determinants [row0, row0 + N) of a space of nfull; perm[r] = determinant
+  // of local row r, xpos[r] = its storage position, xperm = the whole storage
+  // order through which x is packed. Columns are storage positions of the
+  // whole space.
+  bool block = false;
+  size_t nfull = 0, row0 = 0;
+  DevBuf<uint32_t> xpos, xperm;
+  // storage position -> determinant over the whole space (what x is packed by)
+  const uint32_t* pack_perm() const { return block ? xperm.p : perm.p; }
+  // number of determinants x and y span
+  size_t ncols() const { return block ? nfull : N; }
+  void clear_block() {
+    block = false;
+    nfull = row0 = 0;
+    xpos.release();
+    xperm.release();
+  }
   size_t bytes() const {
     return rowptr.bytes() + col.bytes() + v64.bytes() + vhi.bytes() + vlo.bytes() + perm.bytes() + spos.bytes() +
-           crow.bytes() + cbase.bytes() + cdel.bytes() + cval.bytes();
+           crow.bytes() + cbase.bytes() + cdel.bytes() + cval.bytes() + xpos.bytes() + xperm.bytes();
   }
   void drop_compressed() {
     crow.release();
@@ -107,6 +125,9 @@ void compress_csr(Csr& H, Prims& pr, cudaStream_t s);
 // stay sorted) and merged with their new columns. Otherwise all rows.
 void build_ham_csr(const Helpers& hp, const Det2* dets, const IntsView& ints, Csr& H, bool want64, bool want32,
                    bool want_lo, size_t n_old, Prims& pr, cudaStream_t s);
+// Builds only the full rows of the determinants [r0, r1) (see Csr::block).
+void build_ham_block(const Helpers& hp, const Det2* dets, const IntsView& ints, Csr& H, bool want64, bool want32,
+                     bool want_lo, size_t r0, size_t r1, Prims& pr, cudaStream_t s);
 void compute_diag(const Det2* dets, size_t n, const IntsView& ints, double* diag, cudaStream_t s);
 void sigma_direct(const Helpers& hp, const Det2* dets, const IntsView& ints, const double* diag, const double* x,
                   double* y, int k, cudaStream_t s);
@@ -161,6 +182,9 @@ __device__ __forceinline__ int in_mask(const SelectParams& sp, int r, int p) {
 int64_t select_candidates(const Det2* dets, const double* cmax, size_t n, double eps1, const IntsView& ints,
                           const HeatBathView& hb, double maxEntry, const SelectParams& sp, const DetHash& present,
                           Det2* out, int64_t cap, int64_t* d_counter, cudaStream_t s);
+// Number of the n determinants q that the hash set `present` (over dets) holds.
+int64_t count_present(const Det2* q, size_t n, const DetHash& present, const Det2* dets, int64_t* d_counter,
+                      cudaStream_t s);
 
 // ---- alpha <-> beta flip of the space (kernels_select.cu) -------------------
 // flip[i] = index of the determinant with alpha and beta strings exchanged,

@@ -439,17 +439,16 @@ struct CountVisitor {
   __device__ void step(bool hit, uint32_t, bool) { c += hit; }
 };
 
-// Rows [row0, N); counts[slot(I)] = number of off-diagonal connections, where
-// slot(I) = slot[I] when a slot map is given (the storage position of a full
-// build), else I - row0.
-// order[k], k < N - row0: the rows [row0, N) in alpha-major order (rows of one
+// Rows [row0, row0 + nr); counts[slot(I)] = number of off-diagonal
+// connections, where slot(I) = slot[I] when a slot map is given (the storage
+// position of a full build, the local row of a row block), else I - row0.
+// order[k], k < nr: those rows in alpha-major order (rows of one
 // alpha string probe the same index sections; run together, they share them
 // in cache). Output positions stay indexed by the row.
-__global__ void k_ham_count(HelperView h, int64_t row0, const uint32_t* __restrict__ order,
+__global__ void k_ham_count(HelperView h, int64_t row0, int64_t nr, const uint32_t* __restrict__ order,
                             const uint32_t* __restrict__ slot, int64_t* __restrict__ counts) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  const int64_t nr = (int64_t)h.N - row0;
   for (int64_t k = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < nr; k += warps) {
     const int64_t I = order[k];
     CountVisitor v;
@@ -530,9 +529,10 @@ struct EmitVisitor {
   }
 };
 
-// Rows [row0, N) into a CSR whose row pointers are indexed by slot(I) (see
-// k_ham_count); columns are storage positions cmap[J].
-__global__ void __launch_bounds__(256, 4) k_ham_emit(HelperView h, int64_t row0, const uint32_t* __restrict__ order,
+// Rows [row0, row0 + nr) into a CSR whose row pointers are indexed by slot(I)
+// (see k_ham_count); columns are storage positions cmap[J].
+__global__ void __launch_bounds__(256, 4) k_ham_emit(HelperView h, int64_t row0, int64_t nr,
+                                                     const uint32_t* __restrict__ order,
                                                      const uint32_t* __restrict__ slot,
                                                      const uint32_t* __restrict__ cmap,
                                                      const Det2* __restrict__ dets, IntsView ints,
@@ -542,7 +542,6 @@ __global__ void __launch_bounds__(256, 4) k_ham_emit(HelperView h, int64_t row0,
   __shared__ uint32_t s_q[8][2][64];
   const int wib = threadIdx.x >> 5;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  const int64_t nr = (int64_t)h.N - row0;
   for (int64_t k = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < nr; k += warps) {
     const int64_t I = order[k];
     EmitVisitor v{dets, cmap, ints, dets[I], (uint32_t)I, rowptr[slot ? (int64_t)slot[I] : I - row0], col, v64, vhi,
@@ -809,13 +808,14 @@ __global__ void k_order_keys(const uint32_t* __restrict__ aidx, int64_t row0, in
   }
 }
 
-// slot: storage position of each row (full build) or null (rows at I - row0);
+// Rows [row0, row1) of the determinant array. slot: storage position of each
+// row (full build), local row of a row block, or null (rows at I - row0);
 // cmap: determinant index -> storage column.
-static int64_t emit_rows(const Helpers& hp, size_t row0, const uint32_t* slot, const uint32_t* cmap,
+static int64_t emit_rows(const Helpers& hp, size_t row0, size_t row1, const uint32_t* slot, const uint32_t* cmap,
                          const Det2* dets, const IntsView& ints, DevBuf<int64_t>& rowptr, DevBuf<int32_t>& col,
                          DevBuf<double>& v64, DevBuf<float>& vhi, DevBuf<float>& vlo, bool want64, bool want32,
                          bool want_lo, Prims& pr, cudaStream_t s, PhaseTimer& pt) {
-  const size_t N = hp.N, nr = N - row0;
+  const size_t nr = row1 - row0;
   HelperView hv = hp.view();
   DevBuf<int64_t> counts;
   counts.resize(nr > 0 ? nr : 1);
@@ -831,7 +831,7 @@ static int64_t emit_rows(const Helpers& hp, size_t row0, const uint32_t* slot, c
   }
   const unsigned blocks = grid_for(nr * 32, 256, 152 * 16);
   if (nr) {
-    k_ham_count<<<blocks, 256, 0, s>>>(hv, (int64_t)row0, order.p, slot, counts.p);
+    k_ham_count<<<blocks, 256, 0, s>>>(hv, (int64_t)row0, (int64_t)nr, order.p, slot, counts.p);
     SHCI_LAUNCH_CHECK();
   }
   pt.mark("ham count");
@@ -847,7 +847,8 @@ static int64_t emit_rows(const Helpers& hp, size_t row0, const uint32_t* slot, c
   if (want32 && want_lo) vlo.resize(cap); else vlo.release();
   CsrVals v{col.p, want64 ? v64.p : nullptr, want32 ? vhi.p : nullptr, (want32 && want_lo) ? vlo.p : nullptr};
   if (nr) {
-    k_ham_emit<<<blocks, 256, 0, s>>>(hv, (int64_t)row0, order.p, slot, cmap, dets, ints, rowptr.p, v.col, v.v64,
+    k_ham_emit<<<blocks, 256, 0, s>>>(hv, (int64_t)row0, (int64_t)nr, order.p, slot, cmap, dets, ints, rowptr.p,
+                                      v.col, v.v64,
                                       v.vhi, v.vlo);
     SHCI_LAUNCH_CHECK();
   }
@@ -1064,15 +1065,16 @@ void build_ham_csr(const Helpers& hp, const Det2* dets, const IntsView& ints, Cs
                    bool want_lo, size_t n_old, Prims& pr, cudaStream_t s) {
   const size_t N = hp.N;
   PhaseTimer pt(s);
-  const bool incremental = n_old > 0 && n_old < N && H.N == n_old && H.perm.n >= n_old &&
+  const bool incremental = !H.block && n_old > 0 && n_old < N && H.N == n_old && H.perm.n >= n_old &&
                            (want64 ? !want32 : (want32 && want_lo)) &&
                            (H.v64.p != nullptr) == want64 && (H.vhi.p != nullptr) == want32 &&
                            (H.vlo.p != nullptr) == (want32 && want_lo);
   if (!incremental) {
-    if (n_old == N && H.N == N) return;  // nothing new
+    if (n_old == N && H.N == N && !H.block) return;  // nothing new
+    H.clear_block();
     storage_order(hp, H.perm, H.spos, pr, s);
     pt.mark("ham storage order");
-    H.nnz = emit_rows(hp, 0, H.spos.p, H.spos.p, dets, ints, H.rowptr, H.col, H.v64, H.vhi, H.vlo, want64, want32,
+    H.nnz = emit_rows(hp, 0, N, H.spos.p, H.spos.p, dets, ints, H.rowptr, H.col, H.v64, H.vhi, H.vlo, want64, want32,
                       want_lo, pr, s, pt);
     H.N = N;
     SHCI_CUDA(cudaStreamSynchronize(s));
@@ -1083,7 +1085,7 @@ void build_ham_csr(const Helpers& hp, const Det2* dets, const IntsView& ints, Cs
   storage_order(hp, perm, spos, pr, s);
   pt.mark("ham storage order");
   Csr Hn;  // rows of the determinants n_old .. N-1
-  Hn.nnz = emit_rows(hp, n_old, nullptr, spos.p, dets, ints, Hn.rowptr, Hn.col, Hn.v64, Hn.vhi, Hn.vlo, want64,
+  Hn.nnz = emit_rows(hp, n_old, N, nullptr, spos.p, dets, ints, Hn.rowptr, Hn.col, Hn.v64, Hn.vhi, Hn.vlo, want64,
                      want32, want_lo, pr, s, pt);
   CsrVals nv{Hn.col.p, Hn.v64.p, Hn.vhi.p, Hn.vlo.p};
   // new columns of the old rows, indexed by the old determinant
@@ -1163,6 +1165,75 @@ void build_ham_csr(const Helpers& hp, const Det2* dets, const IntsView& ints, Cs
   H.N = N;
   H.nnz = total;
   pt.mark("ham merge");
+}
+
+// ---------------------------------------------------------------------------
+// Row block: one rank's share of the Hamiltonian in the sharded path, the full
+// rows of the determinants [r0, r1) with every column. Local rows are those
+// determinants in storage order (alpha-major, as in the whole matrix);
+// H.perm[r] is the determinant of local row r, H.xpos[r] its storage position
+// (where its own x sits for the diagonal term) and H.xperm the whole storage
+// order (storage position -> determinant), through which x is packed. Columns
+// are storage positions of the whole space. A row's entries and their order
+// are those of the same row in the whole matrix.
+// ---------------------------------------------------------------------------
+__global__ void k_block_flags(const uint32_t* __restrict__ perm, size_t n, uint32_t r0, uint32_t r1,
+                              int64_t* __restrict__ flag) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t d = perm[i];
+    flag[i] = (d >= r0 && d < r1) ? 1 : 0;
+  }
+}
+__global__ void k_block_fill(const uint32_t* __restrict__ perm, size_t n, uint32_t r0, uint32_t r1,
+                             const int64_t* __restrict__ pos, uint32_t* __restrict__ rows, uint32_t* __restrict__ xpos,
+                             uint32_t* __restrict__ slot) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t d = perm[i];
+    if (d >= r0 && d < r1) {
+      const int64_t q = pos[i];
+      rows[q] = d;
+      xpos[q] = (uint32_t)i;
+      slot[d] = (uint32_t)q;
+    }
+  }
+}
+
+void build_ham_block(const Helpers& hp, const Det2* dets, const IntsView& ints, Csr& H, bool want64, bool want32,
+                     bool want_lo, size_t r0, size_t r1, Prims& pr, cudaStream_t s) {
+  const size_t N = hp.N;
+  if (!(r0 < r1 && r1 <= N)) throw Error(kErrInvalid, "row block [r0, r1) must be a non-empty range of the space");
+  const size_t nb = r1 - r0;
+  PhaseTimer pt(s);
+  DevBuf<uint32_t> perm, spos;
+  storage_order(hp, perm, spos, pr, s);
+  DevBuf<int64_t> flag, pos;
+  flag.resize(N);
+  pos.resize(N);
+  k_block_flags<<<grid_for(N, 256), 256, 0, s>>>(perm.p, N, (uint32_t)r0, (uint32_t)r1, flag.p);
+  SHCI_LAUNCH_CHECK();
+  int64_t nflag = 0;
+  scan_exclusive_i64(flag.p, pos.p, N, &nflag, pr, s);
+  if ((size_t)nflag != nb) throw Error(kErrState, "row block: storage order lost determinants");
+  DevBuf<uint32_t> rows, xpos, slot;
+  rows.resize(nb);
+  xpos.resize(nb);
+  slot.resize(N);
+  k_block_fill<<<grid_for(N, 256), 256, 0, s>>>(perm.p, N, (uint32_t)r0, (uint32_t)r1, pos.p, rows.p, xpos.p,
+                                                slot.p);
+  SHCI_LAUNCH_CHECK();
+  pt.mark("ham block order");
+  H.drop_compressed();
+  H.nnz = emit_rows(hp, r0, r1, slot.p, spos.p, dets, ints, H.rowptr, H.col, H.v64, H.vhi, H.vlo, want64, want32,
+                    want_lo, pr, s, pt);
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  H.perm.swap(rows);
+  H.xpos.swap(xpos);
+  H.xperm.swap(perm);
+  H.spos.release();
+  H.N = nb;
+  H.nfull = N;
+  H.row0 = r0;
+  H.block = true;
 }
 
 // ---------------------------------------------------------------------------
@@ -1266,7 +1337,11 @@ __global__ void __launch_bounds__(256) k_sigma_direct(HelperView h, const Det2* 
   __shared__ uint32_t s_q[8][2][64];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t I = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; I < (int64_t)h.N; I += warps) {
+  // rows in alpha-major order (the alpha groups' determinant lists): rows of
+  // one alpha string run side by side and probe the same sections of the
+  // partial-string index, and largely the same connections, from cache
+  for (int64_t k = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < (int64_t)h.N; k += warps) {
+    const int64_t I = h.aDets[k];
     DirectQVisitor<K, F32> v;
     v.dets = dets;
     v.ints = ints;

@@ -308,6 +308,28 @@ void flip_project(double* x, size_t n, const int32_t* flip, const int8_t* sign, 
   SHCI_CUDA(cudaMemcpyAsync(x, tmp, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
 }
 
+// How many of q[0, n) the hash set holds.
+__global__ void k_count_present(const Det2* __restrict__ q, size_t n, const uint32_t* __restrict__ slots,
+                                uint64_t mask, const Det2* __restrict__ dets, unsigned long long* __restrict__ cnt) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    if (hash_contains(slots, mask, dets, q[i])) atomicAdd(cnt, 1ull);
+}
+
+int64_t count_present(const Det2* q, size_t n, const DetHash& present, const Det2* dets, int64_t* d_counter,
+                      cudaStream_t s) {
+  SHCI_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(int64_t), s));
+  size_t blocks = (n + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  if (blocks < 1) blocks = 1;
+  k_count_present<<<(unsigned)blocks, 256, 0, s>>>(q, n, present.slots.p, present.mask, dets,
+                                                   reinterpret_cast<unsigned long long*>(d_counter));
+  SHCI_LAUNCH_CHECK();
+  int64_t total = 0;
+  SHCI_CUDA(cudaMemcpyAsync(&total, d_counter, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  return total;
+}
+
 int64_t select_candidates(const Det2* dets, const double* cmax, size_t n, double eps1, const IntsView& ints,
                           const HeatBathView& hb, double maxEntry, const SelectParams& sp, const DetHash& present,
                           Det2* out, int64_t cap, int64_t* d_counter, cudaStream_t s) {

@@ -143,7 +143,8 @@ __global__ void __launch_bounds__(kBalWalk ? 1024 : 256) k_sigma_mixed(const int
                                                      const float* __restrict__ val, const double* __restrict__ diag,
                                                      const float* __restrict__ x, size_t N, int k,
                                                      double* __restrict__ y, size_t ldy,
-                                                     const uint32_t* __restrict__ perm) {
+                                                     const uint32_t* __restrict__ perm,
+    const uint32_t* __restrict__ xpos) {
   // The row loop is uniform per warp (rows past the slice run empty) so that
   // the width-VW shuffles below always see all 32 lanes.
   ROW_LOOP_BEGIN
@@ -184,10 +185,11 @@ __global__ void __launch_bounds__(kBalWalk ? 1024 : 256) k_sigma_mixed(const int
     }
     if (sub == 0 && live) {
       const size_t o = __ldg(perm + r);
+      const size_t xr = xpos ? (size_t)__ldg(xpos + r) : r;  // the row's own x (row blocks: its storage position)
       const double dg = diag[o];
 #pragma unroll
       for (int c = 0; c < KP; ++c)
-        if (c < k) y[(size_t)c * ldy + o] = dg * (double)x[r * KP + c] + ((double)acc[c].s + (double)acc[c].c);
+        if (c < k) y[(size_t)c * ldy + o] = dg * (double)x[xr * KP + c] + ((double)acc[c].s + (double)acc[c].c);
     }
   ROW_LOOP_END
 }
@@ -205,7 +207,8 @@ __global__ void __launch_bounds__(1024) k_sigma_mixed16(const int64_t* __restric
                                                         const uint16_t* __restrict__ cdel,
                                                         const float* __restrict__ val, const double* __restrict__ diag,
                                                         const float* __restrict__ x, size_t N, double* __restrict__ y,
-                                                        const uint32_t* __restrict__ perm) {
+                                                        const uint32_t* __restrict__ perm,
+    const uint32_t* __restrict__ xpos) {
   constexpr int KP = 1;
   constexpr bool kBalWalk = true;
   const unsigned seg = VW == 32 ? kFull : (((1u << VW) - 1u) << (threadIdx.x & 31 & ~(VW - 1)));
@@ -257,7 +260,8 @@ __global__ void __launch_bounds__(1024) k_sigma_mixed16(const int64_t* __restric
     }
     if (sub == 0 && live) {
       const size_t o = __ldg(perm + r);
-      y[o] = diag[o] * (double)x[r] + ((double)acc.s + (double)acc.c);
+      const size_t xr = xpos ? (size_t)__ldg(xpos + r) : r;
+      y[o] = diag[o] * (double)x[xr] + ((double)acc.s + (double)acc.c);
     }
   ROW_LOOP_END
 }
@@ -348,7 +352,8 @@ __global__ void __launch_bounds__(KP == 1 ? 1024 : 256) k_sigma_f64(const int64_
                                                    const double* __restrict__ v64, const double* __restrict__ diag,
                                                    const double* __restrict__ x, size_t N, int k,
                                                    double* __restrict__ y, size_t ldy,
-                                                   const uint32_t* __restrict__ perm) {
+                                                   const uint32_t* __restrict__ perm,
+    const uint32_t* __restrict__ xpos) {
   constexpr bool kBalWalk = KP == 1;
   ROW_LOOP_BEGIN
     double acc[KP];
@@ -379,10 +384,11 @@ __global__ void __launch_bounds__(KP == 1 ? 1024 : 256) k_sigma_f64(const int64_
     }
     if (sub == 0 && live) {
       const size_t o = __ldg(perm + r);
+      const size_t xr = xpos ? (size_t)__ldg(xpos + r) : r;
       const double dg = diag[o];
 #pragma unroll
       for (int c = 0; c < KP; ++c)
-        if (c < k) y[(size_t)c * ldy + o] = dg * x[r * KP + c] + acc[c];
+        if (c < k) y[(size_t)c * ldy + o] = dg * x[xr * KP + c] + acc[c];
     }
   ROW_LOOP_END
 }
@@ -524,10 +530,10 @@ static void launch_mixed(int vw, const Csr& H, const double* diag, const float* 
                          cudaStream_t s) {
   const SigmaLaunch L = KP <= 2 ? sigma_launch(H.N, vw, 1) : sigma_launch(H.N, vw, KP);
   switch (vw) {
-    case 32: k_sigma_mixed<32, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, H.vhi.p, diag, x, H.N, k, y, ldy, H.perm.p); break;
-    case 16: k_sigma_mixed<16, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, H.vhi.p, diag, x, H.N, k, y, ldy, H.perm.p); break;
-    case 8: k_sigma_mixed<8, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, H.vhi.p, diag, x, H.N, k, y, ldy, H.perm.p); break;
-    default: k_sigma_mixed<4, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, H.vhi.p, diag, x, H.N, k, y, ldy, H.perm.p); break;
+    case 32: k_sigma_mixed<32, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, H.vhi.p, diag, x, H.N, k, y, ldy, H.perm.p, H.block ? H.xpos.p : nullptr); break;
+    case 16: k_sigma_mixed<16, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, H.vhi.p, diag, x, H.N, k, y, ldy, H.perm.p, H.block ? H.xpos.p : nullptr); break;
+    case 8: k_sigma_mixed<8, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, H.vhi.p, diag, x, H.N, k, y, ldy, H.perm.p, H.block ? H.xpos.p : nullptr); break;
+    default: k_sigma_mixed<4, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, H.vhi.p, diag, x, H.N, k, y, ldy, H.perm.p, H.block ? H.xpos.p : nullptr); break;
   }
   SHCI_LAUNCH_CHECK();
 }
@@ -540,10 +546,10 @@ void sigma_csr_mixed(const Csr& H, const double* diag, const float* x32, int kp,
   if (kp == 1 && H.cvalid) {
     const SigmaLaunch L = sigma_launch(H.N, vw, 1);
     switch (vw) {
-      case 32: k_sigma_mixed16<32><<<L.blocks, L.threads, 0, s>>>(H.crow.p, H.cbase.p, H.cdel.p, H.cval.p, diag, x32, H.N, y, H.perm.p); break;
-      case 16: k_sigma_mixed16<16><<<L.blocks, L.threads, 0, s>>>(H.crow.p, H.cbase.p, H.cdel.p, H.cval.p, diag, x32, H.N, y, H.perm.p); break;
-      case 8: k_sigma_mixed16<8><<<L.blocks, L.threads, 0, s>>>(H.crow.p, H.cbase.p, H.cdel.p, H.cval.p, diag, x32, H.N, y, H.perm.p); break;
-      default: k_sigma_mixed16<4><<<L.blocks, L.threads, 0, s>>>(H.crow.p, H.cbase.p, H.cdel.p, H.cval.p, diag, x32, H.N, y, H.perm.p); break;
+      case 32: k_sigma_mixed16<32><<<L.blocks, L.threads, 0, s>>>(H.crow.p, H.cbase.p, H.cdel.p, H.cval.p, diag, x32, H.N, y, H.perm.p, H.block ? H.xpos.p : nullptr); break;
+      case 16: k_sigma_mixed16<16><<<L.blocks, L.threads, 0, s>>>(H.crow.p, H.cbase.p, H.cdel.p, H.cval.p, diag, x32, H.N, y, H.perm.p, H.block ? H.xpos.p : nullptr); break;
+      case 8: k_sigma_mixed16<8><<<L.blocks, L.threads, 0, s>>>(H.crow.p, H.cbase.p, H.cdel.p, H.cval.p, diag, x32, H.N, y, H.perm.p, H.block ? H.xpos.p : nullptr); break;
+      default: k_sigma_mixed16<4><<<L.blocks, L.threads, 0, s>>>(H.crow.p, H.cbase.p, H.cdel.p, H.cval.p, diag, x32, H.N, y, H.perm.p, H.block ? H.xpos.p : nullptr); break;
     }
     SHCI_LAUNCH_CHECK();
     return;
@@ -562,10 +568,10 @@ static void launch_f64(int vw, const Csr& H, const double* diag, const double* x
   const SigmaLaunch L = sigma_launch(H.N, vw, KP);
   const double* v64 = H.v64.p;
   switch (vw) {
-    case 32: k_sigma_f64<32, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, v64, diag, x, H.N, k, y, ldy, H.perm.p); break;
-    case 16: k_sigma_f64<16, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, v64, diag, x, H.N, k, y, ldy, H.perm.p); break;
-    case 8: k_sigma_f64<8, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, v64, diag, x, H.N, k, y, ldy, H.perm.p); break;
-    default: k_sigma_f64<4, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, v64, diag, x, H.N, k, y, ldy, H.perm.p); break;
+    case 32: k_sigma_f64<32, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, v64, diag, x, H.N, k, y, ldy, H.perm.p, H.block ? H.xpos.p : nullptr); break;
+    case 16: k_sigma_f64<16, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, v64, diag, x, H.N, k, y, ldy, H.perm.p, H.block ? H.xpos.p : nullptr); break;
+    case 8: k_sigma_f64<8, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, v64, diag, x, H.N, k, y, ldy, H.perm.p, H.block ? H.xpos.p : nullptr); break;
+    default: k_sigma_f64<4, KP><<<L.blocks, L.threads, 0, s>>>(H.rowptr.p, H.col.p, v64, diag, x, H.N, k, y, ldy, H.perm.p, H.block ? H.xpos.p : nullptr); break;
   }
   SHCI_LAUNCH_CHECK();
 }

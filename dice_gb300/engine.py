@@ -35,6 +35,10 @@ SIGNATURES = [
     ("shci_dets_get", _i32, [_vp, _vp, _i64]),
     ("shci_select", _i32, [_vp, _vp, _dbl, _P(_i64)]),
     ("shci_ham_build", _i32, [_vp, _i32, _P(_i64)]),
+    ("shci_ham_build_rows", _i32, [_vp, _i32, _i64, _i64, _P(_i64)]),
+    ("shci_select_candidates", _i32, [_vp, _vp, _dbl, _i32, _i32, _P(_i64)]),
+    ("shci_candidates_get", _i32, [_vp, _vp, _i64]),
+    ("shci_dets_append", _i32, [_vp, _vp, _i64]),
     ("shci_ham_export", _i32, [_vp, _vp, _vp, _vp]),
     ("shci_diag", _i32, [_vp, _vp]),
     ("shci_sigma", _i32, [_vp, _i32, _vp, _vp, _i32]),
@@ -241,6 +245,28 @@ class Engine:
         k = ctypes.c_int64()
         self._check(load_library().shci_select(self.h, _p(c), float(eps1), ctypes.byref(k)))
         return k.value
+
+    def select_candidates(self, cmax, eps1, rank=0, world=1):
+        """New determinants generated by this rank's parents (i % world ==
+        rank), sorted and unique, not appended: (n, 2) uint64."""
+        c = np.ascontiguousarray(cmax, dtype=np.float64)
+        k = ctypes.c_int64()
+        L = load_library()
+        self._check(L.shci_select_candidates(self.h, _p(c), float(eps1), int(rank), int(world), ctypes.byref(k)))
+        out = np.zeros((k.value, 2), np.uint64)
+        self._check(L.shci_candidates_get(self.h, _p(out), k.value))
+        return out
+
+    def append_dets(self, dets):
+        d = np.ascontiguousarray(dets, dtype=np.uint64).reshape(-1, 2)
+        self._check(load_library().shci_dets_append(self.h, _p(d), len(d)))
+
+    def ham_build_rows(self, r0, r1, mode="fp64"):
+        """Full rows of the determinants [r0, r1) only (one rank's share)."""
+        nnz = ctypes.c_int64()
+        self._check(load_library().shci_ham_build_rows(self.h, MODES.get(mode, mode), int(r0), int(r1),
+                                                       ctypes.byref(nnz)))
+        return nnz.value
 
     def ham_build(self, mode="fp64"):
         nnz = ctypes.c_int64()

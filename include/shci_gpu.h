@@ -107,12 +107,42 @@ int shci_dets_get(shci_ctx* ctx, uint64_t* out, int64_t cap);
  * space; *n_new returns how many. */
 int shci_select(shci_ctx* ctx, const double* cmax, double eps1, int64_t* n_new);
 
+/* Sharded selection, one rank's part. Replaces the rank's share of the parent
+ * loop at SHCI/SHCIbasics.cpp:969-982 (parents i with i % world == rank)
+ * followed by the rank-local sort/unique at :992-994; the reference then
+ * merges the ranks' lists up a binary tree (:1002-1050), which the host
+ * driver (dice_gb300/shard.py) replaces by a hash-partitioned exchange.
+ * shci_select_candidates: the new determinants this rank's parents generate
+ *   (absent from the space, sorted in the reference's order, unique), kept in
+ *   the context; the space is not changed. *n_new = their count.
+ * shci_candidates_get: copies them out (cap >= *n_new, 2 words each).
+ * shci_dets_append: appends determinants to the space in the given order; they
+ *   must be strictly increasing in the reference's order (Determinant::operator<,
+ *   SHCI/Determinants.h:490-498), carry NELEC electrons and be absent from the
+ *   space (SHCI_ERR_INVALID otherwise), as the reference appends the merged
+ *   new determinants at SHCI/SHCIbasics.cpp:1059-1077. */
+int shci_select_candidates(shci_ctx* ctx, const double* cmax, double eps1, int rank, int world, int64_t* n_new);
+int shci_candidates_get(shci_ctx* ctx, uint64_t* out, int64_t cap);
+int shci_dets_append(shci_ctx* ctx, const uint64_t* dets, int64_t n);
+
 /* Hamiltonian. Replaces HamHelpers2::PopulateHelpers/MakeSHMHelpers and
  * SparseHam::makeFromHelper (SHCI/SHCImakeHamiltonian.cpp:290-408, :959-1147,
  * :486-715). mode: SHCI_MODE_*; MIXED also keeps the FP32 tail for FP64
  * refinement, DIRECT and DIRECT_MIXED build only the string tables.
  * *nnz = off-diagonal nonzeros, both triangles. */
 int shci_ham_build(shci_ctx* ctx, int mode, int64_t* nnz);
+/* One rank's row block of the stored Hamiltonian in the sharded path: the full
+ * rows (every column) of the determinants [r0, r1), mode SHCI_MODE_FP64 or
+ * SHCI_MODE_MIXED; *nnz = their off-diagonal entries. Replaces the rank's
+ * share of SparseHam::makeFromHelper (SHCI/SHCImakeHamiltonian.cpp:486-715,
+ * rows I % nprocs == rank there, a contiguous block here). A row's entries
+ * and their order are those of the same row in the whole matrix.
+ * shci_sigma / shci_sigma_device then write only the rows [r0, r1) of y and
+ * leave the others untouched; x spans the whole space. shci_davidson,
+ * shci_ham_export, the packed and allocation-free sigmas and the shifted
+ * preconditioners need the whole matrix and return SHCI_ERR_STATE until
+ * shci_ham_build is called again. */
+int shci_ham_build_rows(shci_ctx* ctx, int mode, int64_t r0, int64_t r1, int64_t* nnz);
 /* The stored off-diagonal CSR (full rows) in FP64; rowptr N+1, col/val nnz.
  * For MIXED, val = head + tail. */
 int shci_ham_export(shci_ctx* ctx, int64_t* rowptr, int32_t* col, double* val);

@@ -53,6 +53,8 @@ def lib():
         L.orc_ham_build.restype = i64
         L.orc_ham_build.argtypes = [vp, vp, i64]
         L.orc_ham_export.argtypes = [vp, vp, vp, vp]
+        L.orc_ham_build_strided.restype = i64
+        L.orc_ham_build_strided.argtypes = [vp, vp, i64, i64]
         L.orc_sigma.argtypes = [vp, vp, vp]
         L.orc_sigma_mt.argtypes = [vp, vp, vp, ctypes.c_int]
         L.orc_davidson.restype = i32
@@ -252,6 +254,16 @@ class Oracle:
         lib().orc_ham_export(self.h, _p(rowptr), _p(col), _p(val))
         self._n = len(dets)
         return rowptr, col, val
+
+    def ham_rows(self, dets, stride):
+        """The lower triangle of the space `dets` for every stride-th row only
+        (the other rows empty): a bounded sample of the rows whose
+        rank-parallel sigma (sigma_mt) can be timed. Returns the entries kept;
+        the CSR stays inside the oracle."""
+        dets = np.ascontiguousarray(dets, dtype=np.uint64)
+        nnz = lib().orc_ham_build_strided(self.h, _p(dets), len(dets), int(stride))
+        self._n = len(dets)
+        return nnz
 
     def sigma(self, x):
         x = np.ascontiguousarray(x, dtype=np.float64)

@@ -744,7 +744,10 @@ static inline uint64_t spin_string(const Det& d, int s) {
 // determinants are kept: selection only appends, and row I holds J <= I), as
 // SparseHam::makeFromHelper builds the rows from StartIndex on
 // (SHCI/SHCImakeHamiltonian.cpp:486-715). n_old = 0 builds every row.
-static void build_ham(const Ints& I, const Det* dets, size_t N, SparseHam& H, size_t n_old = 0) {
+// stride > 1 keeps only the rows I with I % stride == 0 (the others are left
+// empty): a bounded sample of the space's rows for timing the sigma.
+static void build_ham(const Ints& I, const Det* dets, size_t N, SparseHam& H, size_t n_old = 0,
+                      size_t stride = 1) {
   std::unordered_map<uint64_t, int> amap, bmap;
   std::vector<uint64_t> astr, bstr;
   std::vector<int> aidx(N), bidx(N);
@@ -799,6 +802,10 @@ static void build_ham(const Ints& I, const Det* dets, size_t N, SparseHam& H, si
     std::vector<int> row;
     const size_t r0 = n_old + blk * kRows, r1 = std::min(N, r0 + kRows);
     for (size_t I_ = r0; I_ < r1; ++I_) {
+      if (stride > 1 && I_ % stride != 0) {
+        B_.len.push_back(0);
+        continue;
+      }
       row.clear();
       const uint64_t A = astr[aidx[I_]], B = bstr[bidx[I_]];
       // same alpha string: beta single or double
@@ -1554,6 +1561,7 @@ struct VarResult {
   std::vector<IterLog> log;
   int64_t nnz_lower = 0;
   double seconds = 0.0;
+  SparseHam H;  // the final space's lower triangle (kept for timing its sigma)
 };
 
 static double now_s() {
@@ -1654,6 +1662,7 @@ static int do_variational(const Ints& I, const HeatBath& hb, Schedule& s, VarRes
   res.dets = Dets;
   res.ci = ci;
   res.nnz_lower = H.col.size();
+  res.H = std::move(H);
   res.seconds = now_s() - t0;
   return 0;
 }
@@ -1766,6 +1775,14 @@ int64_t orc_select(orc_ctx* c, const uint64_t* dets, int64_t n, const double* cm
 }
 
 // Lower-triangle Hamiltonian with the diagonal first in every row (SparseHam).
+// Builds the lower triangle of the space (every stride-th row when stride > 1,
+// with orc_set_threads workers); returns the entries kept.
+int64_t orc_ham_build_strided(orc_ctx* c, const uint64_t* dets, int64_t n, int64_t stride) {
+  build_ham(c->ints, (const Det*)dets, (size_t)n, c->ham, 0, (size_t)std::max<int64_t>(1, stride));
+  c->ham_n = (size_t)n;
+  c->ham_dets.assign((const Det*)dets, (const Det*)dets + n);
+  return (int64_t)c->ham.col.size();
+}
 int64_t orc_ham_build(orc_ctx* c, const uint64_t* dets, int64_t n) {
   build_ham(c->ints, (const Det*)dets, (size_t)n, c->ham);
   c->ham_n = (size_t)n;
@@ -1822,6 +1839,9 @@ int orc_run_input(orc_ctx** out_ctx, const char* input, const char* fcidump_over
     return 3;
   }
   c->sched = s;
+  // the run's Hamiltonian becomes the context's (orc_sigma / orc_sigma_mt)
+  c->ham = std::move(c->var.H);
+  c->ham_n = c->var.dets.size();
   *out_ctx = c;
   return 0;
 }

@@ -3,11 +3,12 @@ against the CPU oracle on the synthetic workloads, and the mixed-precision
 path against the FP64 path in parity mode.
 
 The reference's loop (SHCI/SHCIbasics.cpp:954-1077) selects from cMax_i =
-max over roots |c_i| of the previous loose Davidson solve. The FP64 GPU path
-runs the reference's algorithm (one correction vector per iteration for the
-lowest unconverged root, nroots+4 vectors, the same start vectors), so its
-coefficients agree with the oracle's to rounding, and every determinant of
-every iteration must come out identical and in the same index order.
+sqrt(sum over roots c_i^2) of the previous loose Davidson solve. The FP64 GPU
+path runs the reference's algorithm (one correction vector per iteration for
+the lowest unconverged root, nroots+4 vectors, the same start vector for the
+first root), so for one root its coefficients agree with the oracle's to
+rounding, and every determinant of every iteration must come out identical
+and in the same index order.
 
 The mixed path computes sigma in FP32 and its loose solves stop elsewhere
 below the tolerance, so at the reference's loose tolerance (5e-5) a few
@@ -47,19 +48,24 @@ def _gpu(inp, mode, block=False):
 
 
 CASES = [
-    # name, schedule, maxiter: the Hubbard ring at its stated schedule, and the
-    # molecular workloads stopped where the oracle finishes in seconds
-    ("hubbard12", [(0, 1e-3), (3, 1e-4)], 6),
-    ("mol24", [(0, 1e-3)], 2),
-    ("mol36", [(0, 3e-3)], 2),
-    ("mol50", [(0, 3e-3)], 2),
-    ("mol64", [(0, 2e-3)], 1),
+    # name, schedule, maxiter, extra input lines: the Hubbard ring at its stated
+    # schedule, and the molecular workloads stopped where the oracle finishes
+    # in seconds. The reference seeds the start vectors of roots beyond the
+    # first at random (Eigen's setRandom, SHCI/Davidson.cpp:155-160), so two
+    # implementations' loose multi-root solves stop at different points below
+    # the tolerance; mol36's four roots are therefore compared in parity mode,
+    # where cMax = sqrt(sum over roots c^2) no longer depends on the start.
+    ("hubbard12", [(0, 1e-3), (3, 1e-4)], 6, ()),
+    ("mol24", [(0, 1e-3)], 2, ()),
+    ("mol36", [(0, 5e-3)], 2, PARITY),
+    ("mol50", [(0, 3e-3)], 2, ()),
+    ("mol64", [(0, 2e-3)], 1, ()),
 ]
 
 
-@pytest.mark.parametrize("name,sched,maxiter", CASES, ids=[c[0] for c in CASES])
-def test_fp64_gpu_determinant_sets_equal_the_oracle(tmp_path, name, sched, maxiter):
-    inp = synthetic.make_workload(name, str(tmp_path / name), schedule=sched, maxiter=maxiter)
+@pytest.mark.parametrize("name,sched,maxiter,extra", CASES, ids=[c[0] for c in CASES])
+def test_fp64_gpu_determinant_sets_equal_the_oracle(tmp_path, name, sched, maxiter, extra):
+    inp = synthetic.make_workload(name, str(tmp_path / name), schedule=sched, maxiter=maxiter, extra=extra)
     ref = orc.run_input(inp)
     got = _gpu(inp, "fp64")
     assert got["ndets"] == [int(v) for v in ref.ndets_log]
