@@ -207,6 +207,17 @@ struct Context {
   DevBuf<int32_t> tr_idx;
   DevBuf<float> tr_tgt;
   int mlp_steps = 60, mlp_batch = 4096;
+  // Davidson (residual, correction) pairs for the learned preconditioner: the
+  // Ritz vector, residual and Ritz value of root 0 at iterations 2, 4, 8 and
+  // 16 of a loose solve, kept until the solve has converged
+  static constexpr int kSnaps = 4;
+  bool record_pairs = false;
+  int n_snap = 0;
+  double snap_theta[kSnaps] = {0, 0, 0, 0};
+  DevBuf<double> snapX, snapR, pair_tgt, pair_tmp;
+  DevBuf<int32_t> pair_idx;
+  DevBuf<int64_t> pair_flag, pair_pos;
+  int64_t last_pairs = 0;
   float mlp_lr = 2e-3f;
   int64_t mlp_sample = 200000;
   double last_loss = 0.0;
@@ -889,6 +900,17 @@ struct Context {
       if (trace_level() > 0)
         std::fprintf(stderr, "[davidson mode=%d it=%d m=%d] lam0=%.12f res0=%.3e G00=%.12f t=%.3f\n", mode, numIter,
                      m, lam[0], rn[0], G[0], now_s() - t_enter);
+      if (record_pairs && n_snap < kSnaps && (numIter == 2 || numIter == 4 || numIter == 8 || numIter == 16)) {
+        if (n_snap == 0) {
+          snapX.reserve(N * kSnaps);
+          snapR.reserve(N * kSnaps);
+        }
+        SHCI_CUDA(cudaMemcpyAsync(snapX.p + (size_t)n_snap * N, X.p, N * sizeof(double), cudaMemcpyDeviceToDevice,
+                                  stream));
+        SHCI_CUDA(cudaMemcpyAsync(snapR.p + (size_t)n_snap * N, R.p, N * sizeof(double), cudaMemcpyDeviceToDevice,
+                                  stream));
+        snap_theta[n_snap++] = lam[0];
+      }
       auto finish = [&]() {
         if (basis_m) *basis_m = m;
         E.assign(lam.begin(), lam.begin() + nroots);
@@ -1157,6 +1179,57 @@ struct Context {
     return loss;
   }
 
+  // Trains the MLP on the (residual, correction) pairs recorded during the
+  // last solve, whose converged root-0 vector is c (device, ndet entries), at
+  // energy E (pair_targets in kernels_mlp.cu gives the target of a pair).
+  // No stored Hamiltonian is needed, so the matrix-free path uses it too.
+  // Returns the final minibatch loss (the previous one when the solve left
+  // too few informative pairs).
+  double train_mlp_pairs(const double* c, double E, int steps = 0) {
+    ensure_diag();
+    const size_t N = ndet;
+    const int nsnap = n_snap;
+    n_snap = 0;
+    if (nsnap == 0 || N < 64) return last_loss;
+    PhaseTimer pt(stream);
+    if (mlp.nspin != 2 * hints.norb) mlp.init(2 * hints.norb, 7, stream);
+    int64_t m = 0;
+    for (int k = 0; k < nsnap; ++k) {
+      const double* xk = snapX.p + (size_t)k * N;
+      const double* rk = snapR.p + (size_t)k * N;
+      const double ck = gram_host(c, N, 1, xk, N, 1)[0];
+      if (!(std::fabs(ck) > 0.5)) continue;  // too far from x* for the first-order relation
+      // entries far below the rms of r_k or of e = x*/ck - x_k (|e|^2 = 1/ck^2 - 1)
+      // are at the rounding level
+      const double rrms = norm_host(rk) / std::sqrt((double)N);
+      const double erms = std::sqrt(std::max(0.0, 1.0 / (ck * ck) - 1.0)) / std::sqrt((double)N);
+      if (!(erms > 0.0)) continue;
+      m += pair_targets(xk, rk, c, ck, diag.p, snap_theta[k], N, 1e-3 * rrms, 1e-3 * erms, m, pair_idx, pair_tgt,
+                        pair_tmp, pair_flag, pair_pos, prims, stream);
+    }
+    last_pairs = m;
+    pt.mark("mlp pairs");
+    if (m < 256) return last_loss;
+    const int64_t ns = std::min<int64_t>(mlp_sample, m);
+    tr_idx.resize(ns);
+    tr_tgt.resize(ns);
+    mlp.sigma = mlp_sample_pairs(pair_idx.p, pair_tgt.p, m, ns, 0x2545F4914F6CDD1Dull ^ (uint64_t)N, tr_idx.p,
+                                 tr_tgt.p, gpart, stream);
+    const int B = (int)std::min<int64_t>(mlp_batch, ns);
+    double loss = 0.0;
+    const int nsteps = steps > 0 ? steps : mlp_steps;
+    for (int st = 0; st < nsteps; ++st) {
+      const int64_t off = ((int64_t)st * B) % std::max<int64_t>(1, ns - B + 1);
+      loss = mlp.gradient(dets.p, diag.p, tr_idx.p + off, tr_tgt.p + off, B, E, stream, st + 1 == nsteps);
+      mlp.adam(mlp_lr, stream);
+    }
+    SHCI_CUDA(cudaStreamSynchronize(stream));
+    pt.mark("mlp steps");
+    mlp.trained = true;
+    last_loss = loss;
+    return loss;
+  }
+
   void davidson(int mode, bool block, int nroots, double* x, int maxCopies, double tol, bool direct_rules,
                 std::vector<double>& E, int& iters, double E_est = std::nan("")) {
     if (!ham_ok) throw Error(kErrState, "Hamiltonian not built for the current space (call shci_ham_build)");
@@ -1374,7 +1447,10 @@ struct Context {
                             : (block ? std::max(nroots + 4, 3 * nroots) : (s.direct ? nroots + 2 : nroots + 4));
       // the shifted preconditioners need an energy: the previous iteration's
       const double E_est = iter == 0 ? std::nan("") : E0[0];
+      n_snap = 0;
+      record_pairs = precond == 2;
       davidson(mode, block, nroots, X0.p, maxCopies, s.davidsonTolLoose, s.direct, E0, numIter, E_est);
+      record_pairs = false;
       ci.swap(X0);
       double td = now_s();
       t_dav += td - tc;
@@ -1384,10 +1460,11 @@ struct Context {
         std::fprintf(stderr, "[iter] %zu eps1=%.3e ndets=%zu nnz=%lld csr_bytes=%zu helper_bytes=%zu E=%.12f "
                              "davidson=%d t=%.3f\n", iter, eps1, N, (long long)H.nnz, H.bytes(), helpers.bytes(),
                      E0[0] + hints.coreE, numIter, td - t0);
-      if (precond == 2 && !is_direct(mode)) {
-        // pairs from this solve, used from the next solve on; later calls
-        // refine the network already trained (a third of the steps)
-        train_mlp(E0[0], mlp.trained ? std::max(1, mlp_steps / 3) : 0);
+      if (precond == 2) {
+        // (residual, correction) pairs of this solve, used from the next solve
+        // on; later calls refine the network already trained (a third of the
+        // steps)
+        train_mlp_pairs(ci.p, E0[0], mlp.trained ? std::max(1, mlp_steps / 3) : 0);
         t_mlp += now_s() - td;
       }
       if (std::fabs(E0[0] - prevE0) < s.dE || iter == s.epsilon1.size() - 1) {

@@ -2,11 +2,15 @@
 // reference, whose preconditioner is r_i / (theta - H_ii), SHCI/Davidson.cpp:85-106).
 //
 // The correction is a per-determinant shift s_i of the denominator,
-//   t_i = r_i / (theta - H_ii - s_i),
-// whose teacher is the second-order level shift of determinant i inside the
-// variational space, s_i = sum_j H_ij^2 / (E - H_jj) (computed from the stored
-// Hamiltonian at the Davidson energy E). A small MLP learns s_i from the
-// determinant itself:
+//   t_i = r_i / (theta - H_ii - s_i).
+// During a variational run the network learns s_i from the (residual,
+// correction) pairs Davidson itself generates (pair_targets below): the shift
+// that would have turned each recorded residual entry into the correction the
+// solve turned out to need. A second target, the second-order level shift of
+// determinant i inside the variational space, s_i = sum_j H_ij^2 / (E - H_jj)
+// (computed from the stored Hamiltonian at the Davidson energy E), serves the
+// explicit training entry point. A small MLP learns s_i from the determinant
+// itself:
 //   features: per spatial orbital "doubly occupied" and "singly occupied"
 //             (2n values, spin-free), (H_ii - E) / 10, and 1;
 //   net:      F -> 128 -> 128 -> 1, ReLU, weights stored in BF16,
@@ -366,6 +370,109 @@ double mlp_sample(const double* teacher, size_t N, int64_t ns, uint64_t seed, in
   double ss = 0.0;
   for (double v : h) ss += v;
   double rms = std::sqrt(ss / (double)ns);
+  return rms > 0.0 ? rms : 1.0;
+}
+
+// ---------------------------------------------------------------------------
+// Targets from Davidson's own (residual, correction) pairs. At iteration k of
+// a solve the Ritz vector x_k has residual r_k = H x_k - theta_k x_k; once the
+// solve has converged to x*, the correction that iteration needed is
+// e = x* / (x* . x_k) - x_k, and to first order (H - theta_k) e = -r_k. The
+// diagonal preconditioner approximates (H - theta)^-1 by 1 / (H_ii - theta);
+// the denominator that would have produced e_i from r_i exactly is
+// -r_i / e_i = H_ii - theta + s_i, so the per-determinant shift the network
+// learns is s_i = -r_i / e_i - (H_ii - theta). Entries where r_i or e_i is
+// at the rounding level carry no information and are dropped, as are shifts
+// that would flip the sign of the plain denominator or exceed twice its size
+// (the preconditioner refuses such shifts anyway).
+// ---------------------------------------------------------------------------
+__global__ void k_pair_targets(const double* __restrict__ xk, const double* __restrict__ rk,
+                               const double* __restrict__ xstar, double inv_ck, const double* __restrict__ diag,
+                               double theta, size_t N, double r_floor, double e_floor, double* __restrict__ tgt,
+                               int64_t* __restrict__ flag) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
+    const double e = xstar[i] * inv_ck - xk[i];
+    const double r = rk[i];
+    const double d = diag[i] - theta;
+    double sh = 0.0;
+    bool ok = fabs(e) > e_floor && fabs(r) > r_floor && fabs(d) > 1e-8;
+    if (ok) {
+      const double den = -r / e;
+      sh = den - d;
+      ok = (den > 0.0) == (d > 0.0) && fabs(sh) <= 2.0 * fabs(d) && isfinite(sh);
+    }
+    tgt[i] = ok ? sh : 0.0;
+    flag[i] = ok ? 1 : 0;
+  }
+}
+__global__ void k_pair_compact(const double* __restrict__ tgt, const int64_t* __restrict__ flag,
+                               const int64_t* __restrict__ pos, size_t N, int64_t base, int32_t* __restrict__ cidx,
+                               double* __restrict__ ctgt) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x)
+    if (flag[i]) {
+      cidx[base + pos[i]] = (int32_t)i;
+      ctgt[base + pos[i]] = tgt[i];
+    }
+}
+// Sample of ns pairs drawn (hashed, with replacement) from the m valid ones.
+__global__ void k_mlp_sample_pairs(const int32_t* __restrict__ cidx, const double* __restrict__ ctgt, int64_t m,
+                                   int64_t ns, uint64_t seed, int32_t* __restrict__ idx, float* __restrict__ tgt,
+                                   double* __restrict__ part) {
+  __shared__ double red[8];
+  double ss = 0.0;
+  const int64_t per = (ns + gridDim.x - 1) / gridDim.x;
+  const int64_t k0 = (int64_t)blockIdx.x * per, k1 = k0 + per < ns ? k0 + per : ns;
+  for (int64_t k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+    const int64_t j = (int64_t)(mix64(seed ^ (0x9E3779B97F4A7C15ull * (uint64_t)(k + 1))) % (uint64_t)m);
+    const double t = ctgt[j];
+    idx[k] = cidx[j];
+    tgt[k] = (float)t;
+    ss += t * t;
+  }
+  for (int o = 16; o; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = ss;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double v = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += red[w];
+    part[blockIdx.x] = v;
+  }
+}
+
+int64_t pair_targets(const double* xk, const double* rk, const double* xstar, double ck, const double* diag,
+                     double theta, size_t N, double r_floor, double e_floor, int64_t base, DevBuf<int32_t>& cidx,
+                     DevBuf<double>& ctgt, DevBuf<double>& tmp, DevBuf<int64_t>& flag, DevBuf<int64_t>& pos, Prims& pr,
+                     cudaStream_t s) {
+  tmp.reserve(N);
+  flag.reserve(N);
+  pos.reserve(N);
+  const unsigned blocks = (unsigned)std::min<size_t>((N + 255) / 256, 152 * 16);
+  k_pair_targets<<<blocks, 256, 0, s>>>(xk, rk, xstar, 1.0 / ck, diag, theta, N, r_floor, e_floor, tmp.p, flag.p);
+  SHCI_LAUNCH_CHECK();
+  int64_t m = 0;
+  scan_exclusive_i64(flag.p, pos.p, N, &m, pr, s);
+  cidx.grow_keep((size_t)(base + m), s);
+  ctgt.grow_keep((size_t)(base + m), s);
+  k_pair_compact<<<blocks, 256, 0, s>>>(tmp.p, flag.p, pos.p, N, base, cidx.p, ctgt.p);
+  SHCI_LAUNCH_CHECK();
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  return m;
+}
+
+double mlp_sample_pairs(const int32_t* cidx, const double* ctgt, int64_t m, int64_t ns, uint64_t seed, int32_t* idx,
+                        float* tgt, DevBuf<double>& part, cudaStream_t s) {
+  if (m <= 0 || ns <= 0) return 1.0;
+  part.reserve(kSampleBlocks);
+  k_mlp_sample_pairs<<<kSampleBlocks, 256, 0, s>>>(cidx, ctgt, m, ns, seed, idx, tgt, part.p);
+  SHCI_LAUNCH_CHECK();
+  k_mlp_scale_targets<<<kSampleBlocks, 256, 0, s>>>(tgt, ns, part.p, (int)kSampleBlocks);
+  SHCI_LAUNCH_CHECK();
+  std::vector<double> h(kSampleBlocks);
+  SHCI_CUDA(cudaMemcpyAsync(h.data(), part.p, kSampleBlocks * sizeof(double), cudaMemcpyDeviceToHost, s));
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  double ss = 0.0;
+  for (double v : h) ss += v;
+  const double rms = std::sqrt(ss / (double)ns);
   return rms > 0.0 ? rms : 1.0;
 }
 

@@ -25,6 +25,19 @@ void pt2_shift(const Csr& H, const double* diag, double E, double* s, DevBuf<flo
 double mlp_sample(const double* teacher, size_t N, int64_t ns, uint64_t seed, int32_t* idx, float* tgt,
                   DevBuf<double>& part, cudaStream_t s);
 
+// Davidson (residual, correction) pairs of one recorded iteration (x_k, r_k,
+// theta_k) against the converged vector x* (ck = x* . x_k): the shifts
+// s_i = -r_i / e_i - (H_ii - theta_k), e = x*/ck - x_k, of the informative
+// entries are appended to (cidx, ctgt) at `base`; returns how many.
+int64_t pair_targets(const double* xk, const double* rk, const double* xstar, double ck, const double* diag,
+                     double theta, size_t N, double r_floor, double e_floor, int64_t base, DevBuf<int32_t>& cidx,
+                     DevBuf<double>& ctgt, DevBuf<double>& tmp, DevBuf<int64_t>& flag, DevBuf<int64_t>& pos, Prims& pr,
+                     cudaStream_t s);
+// Training sample of ns pairs from the m collected ones, targets scaled to
+// unit rms; returns the rms.
+double mlp_sample_pairs(const int32_t* cidx, const double* ctgt, int64_t m, int64_t ns, uint64_t seed, int32_t* idx,
+                        float* tgt, DevBuf<double>& part, cudaStream_t s);
+
 struct Mlp {
   int nspin = 0, F = 0, nparam = 0;
   int offW1 = 0, offW2 = 0, offb1 = 0, offb2 = 0, offw3 = 0, offb3 = 0;

@@ -331,10 +331,15 @@ int shci_run_timings(shci_ctx* ctx, double* t_select, double* t_ham, double* t_d
  *     s_i = sum_j H_ij^2 / (E - H_jj) of the stored Hamiltonian;
  * 2 = shift predicted by the learned MLP (no counterpart in the reference):
  *     in shci_run_input the network is trained after every loose Davidson
- *     solve on the (determinant, s_i) pairs of that solve and used from the
- *     next solve on. The plain denominator is kept wherever a shift would flip
- *     its sign or shrink it below a fifth, and convergence is still judged on
- *     the unpreconditioned residual, so eigenvalues do not change. */
+ *     solve on the (residual, correction) pairs that solve generated -- at
+ *     iterations 2, 4, 8 and 16 the Ritz vector x_k and residual r_k of the
+ *     lowest root; once converged to x*, e = x*/(x*.x_k) - x_k is the
+ *     correction that iteration needed, and s_i = -r_i/e_i - (H_ii - theta_k)
+ *     the shift that would have produced it from r_i -- and used from the next
+ *     solve on, in the stored and the matrix-free paths alike. The plain
+ *     denominator is kept wherever a shift would flip its sign or shrink it
+ *     below a fifth, and convergence is still judged on the unpreconditioned
+ *     residual, so eigenvalues do not change. */
 int shci_set_preconditioner(shci_ctx* ctx, int mode);
 /* Davidson subspace size (no counterpart in the reference, whose subspace is
  * nroots+4 vectors collapsed to nroots+2 Ritz vectors, SHCI/SHCIbasics.cpp:1171,
@@ -353,7 +358,9 @@ int shci_pt2_shift(shci_ctx* ctx, double E, double* out);
 /* MLP training settings: Adam steps per training call, minibatch, learning
  * rate, rows sampled from the space. */
 int shci_mlp_configure(shci_ctx* ctx, int steps, int batch, float lr, int64_t sample_rows);
-/* Train on the current space's level shifts at energy E; final minibatch loss. */
+/* Train on the current space's second-order level shifts at energy E (a
+ * regression target for tests and experiments; shci_run_input trains on
+ * Davidson's own pairs instead); final minibatch loss. */
 int shci_mlp_train(shci_ctx* ctx, double E, float* loss);
 /* Predicted shifts for every determinant of the current space (host out[N]). */
 int shci_mlp_predict(shci_ctx* ctx, double E, double* out);
