@@ -498,7 +498,7 @@ def run_ours(args):
         ts = []
         l0 = e.launch_count()
         # NVTX range so that a profiler can select exactly these launches
-        torch.cuda.nvtx.range_push("bench_sigma_" + mode)
+        torch.cuda.nvtx.range_push("bench_sigma_%s_k%d" % (mode, kp))
         for _ in range(nsteps):
             if flush is not None:
                 with torch.cuda.stream(stream):
@@ -603,6 +603,54 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def run_sigma_only(args):
+    """--section sigma: the plain FP64 variational run of the chosen case, then
+    the stored sigmas timed alone on its final space (FP64 k = 1, mixed k = 4,
+    mixed k = 1), one JSON line. Each kind of launch runs inside its own NVTX
+    range (bench_sigma_<mode>_k<k>), so a profiler can select exactly it."""
+    import torch
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    from dice_gb300 import engine as eng
+    work = tempfile.mkdtemp()
+    inp = make_inputs(work, args.case)
+    e = eng.Engine(local)
+    e.run_input(inp, mode="fp64")
+    N = e.ndets()
+    stream = torch.cuda.ExternalStream(e.stream, device=torch.device("cuda", local))
+    rng = np.random.default_rng(5)
+    out = {"case": args.case, "n_dets": N}
+    peak, _ = measured_peak_gbs()
+    for mode, kp in (("fp64", 1), ("mixed", 4), ("mixed", 1)):
+        nnz = e.ham_build(mode)
+        x = torch.tensor(rng.standard_normal((N, kp)), device="cuda")
+        if mode == "mixed":
+            x = x.float()
+        x = x.contiguous()
+        y = torch.zeros(kp * N, dtype=torch.float64, device="cuda")
+        for _ in range(args.warmup):
+            e.sigma_packed_device(x.data_ptr(), kp, kp, y.data_ptr(), N, mode=mode)
+        torch.cuda.synchronize()
+        ts = []
+        torch.cuda.nvtx.range_push("bench_sigma_%s_k%d" % (mode, kp))
+        for _ in range(args.steps):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            e.sigma_packed_device(x.data_ptr(), kp, kp, y.data_ptr(), N, mode=mode)
+            b.record(stream)
+            b.synchronize()
+            ts.append(a.elapsed_time(b) * 1e-3)
+        torch.cuda.nvtx.range_pop()
+        t = statistics.median(ts)
+        alg = e.sigma_bytes(mode, kp)
+        out["%s_k%d" % (mode, kp)] = {"ms": t * 1e3, "mdets_s": kp * N / t / 1e6, "nnz": nnz, "alg_bytes": alg,
+                                      "achieved_gbs": alg / t / 1e9, "frac": alg / t / 1e9 / peak}
+    e.close()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -613,8 +661,9 @@ def main():
     ap.add_argument("--no-configs", action="store_true", help="skip the other workloads (mol36, mol64, mol50)")
     ap.add_argument("--case", default="full", choices=["full", "medium", "small"],
                     help="small: the profiling case (two eps1 = 1e-3 iterations)")
-    ap.add_argument("--section", default="all", choices=["all", "pt"],
-                    help="pt: only the variational run and the timed perturbative stage")
+    ap.add_argument("--section", default="all", choices=["all", "pt", "sigma"],
+                    help="pt: only the variational run and the timed perturbative stage; sigma: only the FP64 run "
+                         "and the stored sigmas (FP64 k=1, mixed k=4, mixed k=1) timed on its space")
     ap.add_argument("--pt-eps2", type=float, default=PT_EPS2)
     args = ap.parse_args()
     if args.warmup < 3:
@@ -623,6 +672,8 @@ def main():
         run_reference(args)
     elif args.section == "pt":
         run_pt_only(args)
+    elif args.section == "sigma":
+        run_sigma_only(args)
     else:
         run_ours(args)
 

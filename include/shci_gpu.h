@@ -333,7 +333,7 @@ int shci_run_timings(shci_ctx* ctx, double* t_select, double* t_ham, double* t_d
  *     in shci_run_input the network is trained after every loose Davidson
  *     solve on the (residual, correction) pairs that solve generated -- at
  *     iterations 2, 4, 8 and 16 the Ritz vector x_k and residual r_k of the
- *     lowest root; once converged to x*, e = x*/(x*.x_k) - x_k is the
+ *     lowest root; once converged to x_s, e = x_s / (x_s . x_k) - x_k is the
  *     correction that iteration needed, and s_i = -r_i/e_i - (H_ii - theta_k)
  *     the shift that would have produced it from r_i -- and used from the next
  *     solve on, in the stored and the matrix-free paths alike. The plain
