@@ -651,6 +651,43 @@ def run_sigma_only(args):
         print(json.dumps(out), flush=True)
 
 
+def run_direct_only(args):
+    """--section direct: the matrix-free sigma timed alone. The space is config
+    3's generator (mol36: n=36, 14a+14b, rank-108 ERIs, seed 20260002) after
+    two eps1 = 1e-3 iterations of a stored FP64 run with four roots (about
+    5e5 determinants); then four-vector FP32 and FP64 matrix-free sigmas, each
+    inside its own NVTX range (bench_direct_<mode>), with the stored matrix's
+    nonzero count as the element count."""
+    import torch
+    from dice_gb300 import engine as eng, synthetic
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    work = tempfile.mkdtemp()
+    inp = synthetic.make_workload("mol36", work, schedule=[(0, 1e-3)], maxiter=2)
+    e = eng.Engine(local)
+    e.run_input(inp, mode="fp64", block=True)
+    N = e.ndets()
+    nnz = e.ham_build("fp64")
+    x = np.random.default_rng(1).standard_normal((4, N))
+    out = {"workload": "mol36, eps1 1e-3 x2 (config 3's generator)", "n_dets": N, "nnz_offdiag": nnz, "k": 4}
+    for mode in ("direct_mixed", "direct"):
+        e.ham_build(mode)
+        for _ in range(args.warmup):
+            e.sigma(x, mode)
+        ts = []
+        torch.cuda.nvtx.range_push("bench_direct_" + mode)
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            e.sigma(x, mode)
+            ts.append(time.perf_counter() - t0)
+        torch.cuda.nvtx.range_pop()
+        t = statistics.median(ts)
+        out[mode] = {"s": t, "gelem_s": nnz / t / 1e9, "mdets_s": 4 * N / t / 1e6}
+    e.close()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -661,9 +698,10 @@ def main():
     ap.add_argument("--no-configs", action="store_true", help="skip the other workloads (mol36, mol64, mol50)")
     ap.add_argument("--case", default="full", choices=["full", "medium", "small"],
                     help="small: the profiling case (two eps1 = 1e-3 iterations)")
-    ap.add_argument("--section", default="all", choices=["all", "pt", "sigma"],
+    ap.add_argument("--section", default="all", choices=["all", "pt", "sigma", "direct"],
                     help="pt: only the variational run and the timed perturbative stage; sigma: only the FP64 run "
-                         "and the stored sigmas (FP64 k=1, mixed k=4, mixed k=1) timed on its space")
+                         "and the stored sigmas (FP64 k=1, mixed k=4, mixed k=1) timed on its space; direct: the "
+                         "matrix-free sigma (k=4, FP32 and FP64) on config 3's generator")
     ap.add_argument("--pt-eps2", type=float, default=PT_EPS2)
     args = ap.parse_args()
     if args.warmup < 3:
@@ -674,6 +712,8 @@ def main():
         run_pt_only(args)
     elif args.section == "sigma":
         run_sigma_only(args)
+    elif args.section == "direct":
+        run_direct_only(args)
     else:
         run_ours(args)
 

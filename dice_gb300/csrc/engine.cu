@@ -218,6 +218,10 @@ struct Context {
   DevBuf<int32_t> pair_idx;
   DevBuf<int64_t> pair_flag, pair_pos;
   int64_t last_pairs = 0;
+  // the judge's verdict on the network trained last: its corrections point at
+  // the needed one better than the plain preconditioner's on held-out pairs
+  bool mlp_ok = false;
+  double judge_cos_plain = 0.0, judge_cos_learned = 0.0;
   float mlp_lr = 2e-3f;
   int64_t mlp_sample = 200000;
   double last_loss = 0.0;
@@ -1139,7 +1143,7 @@ struct Context {
       if (!whole_ham()) return;
       pt2_shift(H, diag.p, E, shift.p, pt2inv, stream);
       shift_ready = true;
-    } else if (precond == 2 && mlp.trained && mlp.nspin == 2 * hints.norb) {
+    } else if (precond == 2 && mlp.trained && mlp_ok && mlp.nspin == 2 * hints.norb) {
       mlp.infer(dets.p, diag.p, ndet, E, shift.p, stream);
       shift_ready = true;
     }
@@ -1175,6 +1179,7 @@ struct Context {
     SHCI_CUDA(cudaStreamSynchronize(stream));
     pt.mark("mlp steps");
     mlp.trained = true;
+    mlp_ok = true;  // trained explicitly on the level-shift target: used as asked
     last_loss = loss;
     return loss;
   }
@@ -1190,21 +1195,25 @@ struct Context {
     const size_t N = ndet;
     const int nsnap = n_snap;
     n_snap = 0;
-    if (nsnap == 0 || N < 64) return last_loss;
+    if (nsnap < 2 || N < 64) return last_loss;  // nothing to hold out for the judge
     PhaseTimer pt(stream);
     if (mlp.nspin != 2 * hints.norb) mlp.init(2 * hints.norb, 7, stream);
+    // training pairs from every recorded iteration but the last, which the
+    // judge holds out
     int64_t m = 0;
+    double cks[kSnaps];
     for (int k = 0; k < nsnap; ++k) {
       const double* xk = snapX.p + (size_t)k * N;
+      cks[k] = gram_host(c, N, 1, xk, N, 1)[0];
+      if (k == nsnap - 1) break;
+      if (!(std::fabs(cks[k]) > 0.5)) continue;  // too far from x* for the first-order relation
       const double* rk = snapR.p + (size_t)k * N;
-      const double ck = gram_host(c, N, 1, xk, N, 1)[0];
-      if (!(std::fabs(ck) > 0.5)) continue;  // too far from x* for the first-order relation
       // entries far below the rms of r_k or of e = x*/ck - x_k (|e|^2 = 1/ck^2 - 1)
       // are at the rounding level
       const double rrms = norm_host(rk) / std::sqrt((double)N);
-      const double erms = std::sqrt(std::max(0.0, 1.0 / (ck * ck) - 1.0)) / std::sqrt((double)N);
+      const double erms = std::sqrt(std::max(0.0, 1.0 / (cks[k] * cks[k]) - 1.0)) / std::sqrt((double)N);
       if (!(erms > 0.0)) continue;
-      m += pair_targets(xk, rk, c, ck, diag.p, snap_theta[k], N, 1e-3 * rrms, 1e-3 * erms, m, pair_idx, pair_tgt,
+      m += pair_targets(xk, rk, c, cks[k], diag.p, snap_theta[k], N, 1e-3 * rrms, 1e-3 * erms, m, pair_idx, pair_tgt,
                         pair_tmp, pair_flag, pair_pos, prims, stream);
     }
     last_pairs = m;
@@ -1223,10 +1232,26 @@ struct Context {
       loss = mlp.gradient(dets.p, diag.p, tr_idx.p + off, tr_tgt.p + off, B, E, stream, st + 1 == nsteps);
       mlp.adam(mlp_lr, stream);
     }
-    SHCI_CUDA(cudaStreamSynchronize(stream));
-    pt.mark("mlp steps");
     mlp.trained = true;
     last_loss = loss;
+    pt.mark("mlp steps");
+    // the judge: the network is used from the next solve on only if, on the
+    // held-out iteration, its corrections point at the needed correction
+    // better than the plain preconditioner's
+    const int kv = nsnap - 1;
+    mlp_ok = false;
+    // a held-out iteration already at the solution (|e|^2 = 1/ck^2 - 1 at the
+    // rounding level) judges nothing
+    if (std::fabs(cks[kv]) > 0.5 && 1.0 / (cks[kv] * cks[kv]) - 1.0 > 1e-10) {
+      teacher.resize(N);
+      mlp.infer(dets.p, diag.p, N, snap_theta[kv], teacher.p, stream);
+      judge_preconditioners(snapX.p + (size_t)kv * N, snapR.p + (size_t)kv * N, c, cks[kv], diag.p, teacher.p,
+                            snap_theta[kv], N, gpart, stream, &judge_cos_plain, &judge_cos_learned);
+      mlp_ok = judge_cos_learned > 1.05 * judge_cos_plain;  // a clear margin, not noise
+    }
+    if (trace_level() > 0)
+      std::fprintf(stderr, "[mlp] %lld pairs, loss %.4f, judge cos plain %.6f learned %.6f -> %s\n", (long long)m,
+                   loss, judge_cos_plain, judge_cos_learned, mlp_ok ? "learned" : "plain");
     return loss;
   }
 
@@ -1327,6 +1352,7 @@ struct Context {
     total_dav_iters = 0;
     shift_ready = false;
     mlp.trained = false;
+    mlp_ok = false;
     log.clear();
     if (s.direct)
       mode = (mode == SHCI_MODE_MIXED || mode == SHCI_MODE_DIRECT_MIXED) ? SHCI_MODE_DIRECT_MIXED : SHCI_MODE_DIRECT;

@@ -531,7 +531,15 @@ struct EmitVisitor {
 
 // Rows [row0, row0 + nr) into a CSR whose row pointers are indexed by slot(I)
 // (see k_ham_count); columns are storage positions cmap[J].
-__global__ void __launch_bounds__(256, 4) k_ham_emit(HelperView h, int64_t row0, int64_t nr,
+// Resident blocks per SM the emit and the matrix-free sigma are compiled for
+// (the register budget follows: 4 -> 64 registers a thread).
+#ifndef SHCI_EMIT_MIN_BLOCKS
+#define SHCI_EMIT_MIN_BLOCKS 4
+#endif
+#ifndef SHCI_DIRECT_MIN_BLOCKS
+#define SHCI_DIRECT_MIN_BLOCKS 1
+#endif
+__global__ void __launch_bounds__(256, SHCI_EMIT_MIN_BLOCKS) k_ham_emit(HelperView h, int64_t row0, int64_t nr,
                                                      const uint32_t* __restrict__ order,
                                                      const uint32_t* __restrict__ slot,
                                                      const uint32_t* __restrict__ cmap,
@@ -1330,7 +1338,7 @@ struct DirectQVisitor {
 };
 
 template <int K, bool F32>
-__global__ void __launch_bounds__(256) k_sigma_direct(HelperView h, const Det2* __restrict__ dets, IntsView ints,
+__global__ void __launch_bounds__(256, SHCI_DIRECT_MIN_BLOCKS) k_sigma_direct(HelperView h, const Det2* __restrict__ dets, IntsView ints,
                                                       const double* __restrict__ diag,
                                                       const typename DirectQVisitor<K, F32>::T* __restrict__ x,
                                                       double* __restrict__ y) {

@@ -476,6 +476,66 @@ double mlp_sample_pairs(const int32_t* cidx, const double* ctgt, int64_t m, int6
   return rms > 0.0 ? rms : 1.0;
 }
 
+// The judge: on a recorded iteration (x_k, r_k, theta_k) of a converged solve
+// (x*, ck = x* . x_k), how well the plain and the shifted preconditioners
+// would have pointed at the correction that iteration needed,
+// e = x*/ck - x_k. Sums over the determinants of <t, e>, <t, t> for the plain
+// t_i = r_i / (theta - H_ii) and for the shifted one (the shift kept only
+// where the preconditioner keeps it, as k_precondition_shift does), and
+// <e, e>, per block into part[6 * block].
+__global__ void k_judge(const double* __restrict__ xk, const double* __restrict__ rk,
+                        const double* __restrict__ xstar, double inv_ck, const double* __restrict__ diag,
+                        const double* __restrict__ shift, double theta, size_t N, double* __restrict__ part) {
+  __shared__ double red[5][8];
+  double a[5] = {0, 0, 0, 0, 0};
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
+    const double e = xstar[i] * inv_ck - xk[i];
+    double den = theta - diag[i];
+    if (!(fabs(den) > 1e-12)) den -= 1e-12;
+    const double tp = rk[i] / den;
+    double dl = den;
+    const double d2 = den - shift[i];
+    if ((d2 > 0) == (den > 0) && fabs(d2) > 0.2 * fabs(den)) dl = d2;
+    const double tl = rk[i] / dl;
+    a[0] += tp * e;
+    a[1] += tp * tp;
+    a[2] += tl * e;
+    a[3] += tl * tl;
+    a[4] += e * e;
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < 5; ++q) {
+    double v = a[q];
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[q][w] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 5) {
+    double v = 0.0;
+    for (int u = 0; u < (int)(blockDim.x >> 5); ++u) v += red[threadIdx.x][u];
+    part[(size_t)blockIdx.x * 6 + threadIdx.x] = v;
+  }
+}
+
+void judge_preconditioners(const double* xk, const double* rk, const double* xstar, double ck, const double* diag,
+                           const double* shift, double theta, size_t N, DevBuf<double>& part, cudaStream_t s,
+                           double* cos_plain, double* cos_learned) {
+  const unsigned blocks = (unsigned)std::max<size_t>(1, std::min<size_t>((N + 255) / 256, 152 * 4));
+  part.reserve((size_t)blocks * 6);
+  k_judge<<<blocks, 256, 0, s>>>(xk, rk, xstar, 1.0 / ck, diag, shift, theta, N, part.p);
+  SHCI_LAUNCH_CHECK();
+  std::vector<double> h((size_t)blocks * 6);
+  SHCI_CUDA(cudaMemcpyAsync(h.data(), part.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  double a[5] = {0, 0, 0, 0, 0};
+  for (unsigned b = 0; b < blocks; ++b)
+    for (int q = 0; q < 5; ++q) a[q] += h[(size_t)b * 6 + q];
+  const double ne = std::sqrt(a[4]);
+  *cos_plain = (a[1] > 0 && ne > 0) ? std::fabs(a[0]) / (std::sqrt(a[1]) * ne) : 0.0;
+  *cos_learned = (a[3] > 0 && ne > 0) ? std::fabs(a[2]) / (std::sqrt(a[3]) * ne) : 0.0;
+}
+
 float Mlp::gradient(const Det2* dets, const double* diag, const int32_t* idx, const float* target, int B, double E,
                     cudaStream_t s, bool want_loss) {
   const size_t smem = mlp_grad_smem(F);

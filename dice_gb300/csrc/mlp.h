@@ -38,6 +38,15 @@ int64_t pair_targets(const double* xk, const double* rk, const double* xstar, do
 double mlp_sample_pairs(const int32_t* cidx, const double* ctgt, int64_t m, int64_t ns, uint64_t seed, int32_t* idx,
                         float* tgt, DevBuf<double>& part, cudaStream_t s);
 
+// The plain preconditioner as judge of the learned one: on a held-out
+// recorded iteration, |cos| of the angle between the correction each would
+// have produced (plain r_i / (theta - H_ii), shifted by `shift` where the
+// preconditioner keeps the shift) and the correction e = x*/ck - x_k the
+// iteration needed.
+void judge_preconditioners(const double* xk, const double* rk, const double* xstar, double ck, const double* diag,
+                           const double* shift, double theta, size_t N, DevBuf<double>& part, cudaStream_t s,
+                           double* cos_plain, double* cos_learned);
+
 struct Mlp {
   int nspin = 0, F = 0, nparam = 0;
   int offW1 = 0, offW2 = 0, offb1 = 0, offb2 = 0, offw3 = 0, offb3 = 0;

@@ -100,3 +100,32 @@ def test_learned_preconditioner_gains_over_diagonal(tmp_path):
     assert abs(fixed["pt2"][0] - fixed["plain"][0]) < 1e-9
     assert fixed["mlp"][1] < fixed["plain"][1]
     gpu.close()
+
+
+@pytest.mark.parametrize("direct", [False, True], ids=["stored", "matrix_free"])
+def test_pair_trained_preconditioner_keeps_the_eigenvalue(tmp_path, direct):
+    """Preconditioner 2 in a whole run: the network is trained on the
+    (residual, correction) pairs each loose Davidson solve records, the plain
+    preconditioner judges it on a held-out iteration, and the run -- stored or
+    matrix-free, where no level shift is available -- converges to the same
+    determinants and the same E_var as with the plain preconditioner."""
+    # every solve converged tightly, so that both runs select the same
+    # determinants; the matrix-free path (whose loose solves the reference
+    # stops at 3e-2) selects once and then runs its final solve with the
+    # network trained on the first
+    if direct:
+        inp = synthetic.make_workload("mol24", str(tmp_path / "m"), schedule=[(0, 2e-3)], maxiter=1,
+                                      extra=("davidsonTol 1e-7", "DirectDavidson"))
+    else:
+        inp = synthetic.make_workload("mol24", str(tmp_path / "m"), schedule=[(0, 3e-3), (1, 1e-3)], maxiter=3,
+                                      extra=("davidsonTol 1e-7", "davidsonTolLoose 1e-7"))
+    out = {}
+    for precond in ("plain", "mlp"):
+        e = eng.Engine(0)
+        e.set_preconditioner(precond)
+        E = e.run_input(inp, mode="mixed")
+        out[precond] = (E, e.dets(), e.run_stats())
+        e.close()
+    assert out["mlp"][2]["t_mlp"] > 0.0  # the network was trained during the run
+    assert np.array_equal(out["mlp"][1], out["plain"][1])
+    assert abs(out["mlp"][0][0] - out["plain"][0][0]) < 1e-6
