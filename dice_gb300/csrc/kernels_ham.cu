@@ -532,12 +532,15 @@ struct EmitVisitor {
 // Rows [row0, row0 + nr) into a CSR whose row pointers are indexed by slot(I)
 // (see k_ham_count); columns are storage positions cmap[J].
 // Resident blocks per SM the emit and the matrix-free sigma are compiled for
-// (the register budget follows: 4 -> 64 registers a thread).
+// (6 -> at most 40 registers a thread, a few hundred bytes of stack): both
+// wait on the latency of index probes and gathers, and the extra warps hide
+// more of it than the spills cost (mol36, 4-vector matrix-free sigma: 79 ms
+// with 64 registers and 4 blocks, 76 ms with 6; mol24 H build 1.47 -> 1.41 s).
 #ifndef SHCI_EMIT_MIN_BLOCKS
-#define SHCI_EMIT_MIN_BLOCKS 4
+#define SHCI_EMIT_MIN_BLOCKS 6
 #endif
 #ifndef SHCI_DIRECT_MIN_BLOCKS
-#define SHCI_DIRECT_MIN_BLOCKS 1
+#define SHCI_DIRECT_MIN_BLOCKS 6
 #endif
 __global__ void __launch_bounds__(256, SHCI_EMIT_MIN_BLOCKS) k_ham_emit(HelperView h, int64_t row0, int64_t nr,
                                                      const uint32_t* __restrict__ order,
