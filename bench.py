@@ -63,10 +63,11 @@ PARITY_TOL = 1e-8
 # deterministic PT2 on the final mixed-precision space of the workload
 PT_EPS2 = 1e-5
 # DRAM bytes per mixed-sigma launch divided by its algorithmic bytes, from one
-# ncu capture of the medium case (4.4965 GB measured / 4.4565 GB algorithmic);
-# the full-size launch is too large to capture, and its traffic scales with
-# the nonzeros it streams.
-TRAFFIC_RATIO = 4.4965 / 4.4565
+# ncu capture of the medium case (4.4983 GB measured read + write / 4.4633 GB
+# algorithmic, profiles/sigma_mol24_medium.md); the full-size launch is too
+# large to capture with all sections, and its traffic scales with the
+# nonzeros it streams.
+TRAFFIC_RATIO = 4.4983 / 4.4633
 
 
 def dist_info():
@@ -374,10 +375,11 @@ def other_configs(work, device):
         g.set_davidson_basis(*basis)
         E = g.run_input(inp, mode=mode, block=block)
         t, st, lg = g.timings(), g.run_stats(), g.run_log()
+        dets = g.dets()
         g.close()
         return {"E_var": [float(v) for v in E], "wall_s": t["total"], "ham_s": t["ham"], "davidson_s": t["davidson"],
                 "sigma_s": t["sigma"], "davidson_iters": int(st["davidson_iters"]),
-                "ndets": [int(v) for v in lg["ndets"]]}
+                "ndets": [int(v) for v in lg["ndets"]], "_dets": dets}
 
     out = {}
     # config 1: the 12-site Hubbard ring at its stated schedule, GPU paths
@@ -406,33 +408,43 @@ def other_configs(work, device):
     # config 3's generator (n=36, 14a+14b, 4 roots, block Davidson): eps1
     # 1e-3 twice then 6e-4 (eps1 3e-4 already selects 5.8 M determinants,
     # whose stored matrix does not fit beside the FP64 run's)
+    # in parity mode (loose solves as tight as the final one), so that both
+    # paths select the same determinants and the roots compare one to one
     sched = [(0, 1e-3), (2, 6e-4)]
-    ref = run("mol36", sched, 3, "fp64", True)
-    new = run("mol36", sched, 3, "mixed", True, basis=(16, 12))
+    par = ("davidsonTolLoose 1e-6",)
+    ref = run("mol36", sched, 3, "fp64", True, extra=par)
+    new = run("mol36", sched, 3, "mixed", True, basis=(16, 12), extra=par)
     out["mol36_4roots_block"] = {
         "what": "config 3's generator: n=36, 14a+14b, 4 roots, block Davidson (k=4 per sigma launch), eps1 "
-                "1e-3 x2 -> 6e-4 (the stated eps1 3e-5 selects far more than one GPU holds; see DESIGN)",
+                "1e-3 x2 -> 6e-4, parity mode (every solve to 1e-6) (the stated eps1 3e-5 selects far more than one "
+                "GPU holds; see DESIGN)",
         "fp64": ref, "new_form": new, "dE_per_root": [a - b for a, b in zip(new["E_var"], ref["E_var"])],
-        "wall_speedup": ref["wall_s"] / new["wall_s"]}
+        "dS": sym_diff(new.pop("_dets"), ref.pop("_dets")), "wall_speedup": ref["wall_s"] / new["wall_s"]}
     # config 5's generator (n=64, 20a+20b, two-word determinants), 4 roots,
     # matrix-free: eps1 2e-3 twice
-    ref = run("mol64", [(0, 2e-3)], 2, "fp64", True, extra=("DirectDavidson",))
-    new = run("mol64", [(0, 2e-3)], 2, "mixed", True, extra=("DirectDavidson",))
-    out["mol64_4roots_matrix_free"] = {
-        "what": "config 5's generator: n=64, 20a+20b (two-word determinants), 4 roots, matrix-free sigma, "
-                "eps1 2e-3 x2",
-        "fp64": ref, "mixed": new, "dE_per_root": [a - b for a, b in zip(new["E_var"], ref["E_var"])],
-        "wall_speedup": ref["wall_s"] / new["wall_s"]}
+    # one selection (the same space for both paths: the reference forces the
+    # loose tolerance of matrix-free runs to 3e-2, SHCI/input.cpp, so later
+    # selections differ), then two for scale
+    for key, sched, it in (("mol64_4roots_matrix_free", [(0, 1e-3)], 1),
+                           ("mol64_4roots_matrix_free_2iter", [(0, 2e-3)], 2)):
+        ref = run("mol64", sched, it, "fp64", True, extra=("DirectDavidson",))
+        new = run("mol64", sched, it, "mixed", True, extra=("DirectDavidson",))
+        out[key] = {
+            "what": "config 5's generator: n=64, 20a+20b (two-word determinants), 4 roots, matrix-free sigma, "
+                    "schedule %s" % sched,
+            "fp64": ref, "mixed": new, "dE_per_root": [a - b for a, b in zip(new["E_var"], ref["E_var"])],
+            "dS": sym_diff(new.pop("_dets"), ref.pop("_dets")), "wall_speedup": ref["wall_s"] / new["wall_s"]}
     # config 4's generator (n=50, 16a+16b): eps1 1e-3 twice then 3e-4 (2.3 M
     # determinants), learned preconditioner against the plain one
     sched = [(0, 1e-3), (2, 3e-4)]
     plain = run("mol50", sched, 3, "mixed", False, "plain")
     mlp = run("mol50", sched, 3, "mixed", False, "mlp")
+    dS50 = sym_diff(plain.pop("_dets"), mlp.pop("_dets"))
     out["mol50_learned_preconditioner"] = {
         "what": "config 4's generator: n=50, 16a+16b, 1 root, mixed precision, reference subspace, eps1 1e-3 x2 "
                 "-> 3e-4; learned preconditioner (trained on Davidson's residual/correction pairs, judged by the "
                 "plain one) against the plain diagonal preconditioner",
-        "plain": plain, "mlp": mlp, "dE": mlp["E_var"][0] - plain["E_var"][0],
+        "plain": plain, "mlp": mlp, "dE": mlp["E_var"][0] - plain["E_var"][0], "dS": dS50,
         "wall_speedup_mlp_vs_plain": plain["wall_s"] / mlp["wall_s"]}
     return out
 

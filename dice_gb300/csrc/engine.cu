@@ -192,6 +192,12 @@ struct Context {
   DevBuf<int8_t> flipsgn;
   int flip_state = -1;
   bool last_stalled = false;  // the last FP32 Davidson stage stopped at its rounding floor
+  // time reversal: the flip sector every Davidson vector is kept in (0: none;
+  // otherwise +-1, the input's Treversal times (-1)^(beta electrons), in the
+  // sign convention of build_flip_map)
+  int trev_sector = 0;
+  DevBuf<Det2> trev_buf;
+  DevBuf<int64_t> trev_flag, trev_pos;
 
   // preconditioner: 0 the reference's diagonal, 1 diagonal + second-order
   // level shift from the stored H, 2 diagonal + shift predicted by the MLP
@@ -415,6 +421,30 @@ struct Context {
   int64_t select(const double* cmax_dev, double eps1) {
     const size_t nnew = candidates(cmax_dev, eps1);
     append_candidates(nnew);
+    return (int64_t)nnew;
+  }
+
+  // Selection with time reversal: candidates from the standard member of each
+  // pair (the others have cMax 0), made standard, sorted, unique and absent
+  // from the space, then appended followed by their flipped partners, so the
+  // space stays closed under the flip (SHCI/SHCIbasics.cpp:969-997).
+  int64_t select_trev(const double* cmax_dev, double eps1) {
+    const size_t n = candidates(cmax_dev, eps1);
+    size_t nnew = 0;
+    if (n) {
+      trev_buf.reserve(2 * n);
+      nnew = trev_new_dets(cand.p, n, hash, dets.p, trev_buf.p, trev_flag, trev_pos, prims, stream);
+    }
+    ncand = 0;
+    if (nnew) {
+      if (ndet + nnew >= (size_t)0x7fffffff) throw Error(kErrInvalid, "determinant space exceeds 2^31 entries");
+      dets.grow_keep(ndet + nnew, stream);
+      k_append<<<grid_for(nnew, 256), 256, 0, stream>>>(trev_buf.p, nnew, dets.p + ndet);
+      SHCI_LAUNCH_CHECK();
+      ndet += nnew;
+      invalidate_space();
+    }
+    SHCI_CUDA(cudaStreamSynchronize(stream));
     return (int64_t)nnew;
   }
 
@@ -791,8 +821,10 @@ struct Context {
     // accumulation in kernels_sigma.cu), so its corrections are projected
     // back into that sector. Start vectors spanning both sectors (e.g. the
     // random guesses of extra roots) already reach every state: no projection.
-    const bool sym = stall_exit && ensure_flip();
-    int sector = 0;
+    const bool sym = (stall_exit || trev_sector != 0) && ensure_flip();
+    if (trev_sector != 0 && !sym)
+      throw Error(kErrState, "time reversal needs the flipped partner of every determinant in the space");
+    int sector = trev_sector;
     last_stalled = false;
     if (nroots < 1) throw Error(kErrInvalid, "nroots must be >= 1");
     if ((size_t)nroots > N) throw Error(kErrInvalid, "more roots than determinants");
@@ -830,17 +862,30 @@ struct Context {
         scale_col(bi, 1.0 / norm_host(bi));
       }
       if (sym) {
-        std::vector<double> par(nroots);
-        for (int i = 0; i < nroots; ++i)
-          par[i] = flip_parity(V.p + (size_t)i * N, N, flipidx.p, flipsgn.p, gpart, stream);
-        sector = par[0] > kParityDefinite ? 1 : (par[0] < -kParityDefinite ? -1 : 0);
-        for (int i = 1; i < nroots; ++i)
-          if (!(par[i] * sector > kParityDefinite)) sector = 0;
+        if (trev_sector == 0) {
+          std::vector<double> par(nroots);
+          for (int i = 0; i < nroots; ++i)
+            par[i] = flip_parity(V.p + (size_t)i * N, N, flipidx.p, flipsgn.p, gpart, stream);
+          sector = par[0] > kParityDefinite ? 1 : (par[0] < -kParityDefinite ? -1 : 0);
+          for (int i = 1; i < nroots; ++i)
+            if (!(par[i] * sector > kParityDefinite)) sector = 0;
+        }
         if (sector != 0)
           for (int i = 0; i < nroots; ++i) {
             double* bi = V.p + (size_t)i * N;
+            for (int j = 0; j < i; ++j) project_out(V.p + (size_t)j * N, bi);
             project_parity(bi, (double)sector);
-            scale_col(bi, 1.0 / norm_host(bi));
+            double nb = norm_host(bi);
+            if (nb < 1e-8) {  // no component in the sector: a random start there
+              fill_random(bi, 3000 + i);
+              for (int j = 0; j < i; ++j) project_out(V.p + (size_t)j * N, bi);
+              project_parity(bi, (double)sector);
+              nb = norm_host(bi);
+            }
+            if (nb < 1e-8)
+              throw Error(kErrInvalid, "the determinant space has no room for root " + std::to_string(i + 1) +
+                                           " in the time-reversal (alpha <-> beta flip) sector");
+            scale_col(bi, 1.0 / nb);
           }
       }
       apply_sigma(mode, V.p, N, 0, nroots, W.p, N, 0);
@@ -1377,6 +1422,14 @@ struct Context {
       sp.rmask0[r] = m0;
       sp.rmask1[r] = m1;
     }
+    // time reversal: off for an odd number of electrons (SHCI/SHCI.cpp:188-195);
+    // the sector applies to this run's solves only
+    const int trev = (hints.nelec % 2 == 0) ? s.trev : 0;
+    trev_sector = 0;
+    struct SectorReset {
+      int& v;
+      ~SectorReset() { v = 0; }
+    } sector_reset{trev_sector};
     // reference determinants and initial ci (SHCI/SHCI.cpp:289-399)
     std::vector<uint64_t> hd;
     int lowest = 0;
@@ -1391,6 +1444,14 @@ struct Context {
           throw Error(kErrInvalid, "orbital " + std::to_string(p) + " appears twice in input determinant number " +
                                        std::to_string(d));
         w[p >> 6] |= 1ull << (p & 63);
+      }
+      if (trev != 0) {  // makeStandard (SHCI/SHCI.cpp:302)
+        Det2 dd{w[0], w[1]};
+        if (__builtin_popcountll(det_alpha(dd)) != __builtin_popcountll(det_beta(dd)))
+          throw Error(kErrInvalid, "time reversal (Treversal) needs as many alpha as beta electrons");
+        if (!det_is_standard(dd)) dd = det_flip_pair(dd);
+        w[0] = dd.w0;
+        w[1] = dd.w1;
       }
       for (size_t e = 0; e < d; ++e)
         if (hd[2 * e] == w[0] && hd[2 * e + 1] == w[1])
@@ -1417,19 +1478,45 @@ struct Context {
       }
     }
     if (s.occupied.empty()) throw Error(kErrInvalid, "nocc keyword has to be included.");
-    set_dets(hd.data(), (int64_t)s.occupied.size());
+    const size_t nin = s.occupied.size();
+    // with time reversal the flipped partners of the open-shell input
+    // determinants follow them (the pair's basis function is spread over both)
+    std::vector<size_t> partner(nin, (size_t)-1);
+    if (trev != 0) {
+      const int nbeta = __builtin_popcountll(det_beta(Det2{hd[0], hd[1]}));
+      trev_sector = trev * ((nbeta % 2) ? -1 : 1);
+      for (size_t d = 0; d < nin; ++d) {
+        const Det2 dd{hd[2 * d], hd[2 * d + 1]};
+        const Det2 f = det_flip_pair(dd);
+        if (f.w0 == dd.w0 && f.w1 == dd.w1) continue;
+        partner[d] = hd.size() / 2;
+        hd.push_back(f.w0);
+        hd.push_back(f.w1);
+      }
+    }
+    set_dets(hd.data(), (int64_t)(hd.size() / 2));
     const int nroots = s.nroots;
     if (nroots < 1 || nroots > 16) throw Error(kErrInvalid, "nroots must be in 1..16");
     nroots_run = nroots;
     {
+      // the reference's guess over its (symmetrized) basis functions: 1 each,
+      // plus the count on the lowest, normalised; a pair's coefficient c goes
+      // to its two determinants as c/sqrt(2) and sector * sign * c/sqrt(2)
       const size_t n0 = ndet;
       std::vector<double> c0(n0 * nroots, 0.0);
-      for (size_t j = 0; j < n0; ++j) c0[j] = 1.0;
-      c0[lowest] += (double)n0;
+      for (size_t j = 0; j < nin; ++j) c0[j] = 1.0;
+      c0[lowest] += (double)nin;
       double nn = 0.0;
-      for (size_t j = 0; j < n0; ++j) nn += c0[j] * c0[j];
+      for (size_t j = 0; j < nin; ++j) nn += c0[j] * c0[j];
       nn = std::sqrt(nn);
-      for (size_t j = 0; j < n0; ++j) c0[j] /= nn;
+      for (size_t j = 0; j < nin; ++j) c0[j] /= nn;
+      for (size_t j = 0; j < nin; ++j)
+        if (partner[j] != (size_t)-1) {
+          const uint64_t a = det_alpha(Det2{hd[2 * j], hd[2 * j + 1]}), b = det_beta(Det2{hd[2 * j], hd[2 * j + 1]});
+          const double sgn = (__builtin_popcountll(a & b) & 1) ? -1.0 : 1.0;
+          c0[j] /= std::sqrt(2.0);
+          c0[partner[j]] = trev_sector * sgn * c0[j];
+        }
       ci.resize(n0 * nroots);
       SHCI_CUDA(cudaMemcpyAsync(ci.p, c0.data(), c0.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
     }
@@ -1450,9 +1537,16 @@ struct Context {
       const size_t N0 = ndet;
       double ta = now_s();
       cmax.resize(N0);
-      k_cmax<<<grid_for(N0, 256), 256, 0, stream>>>(ci.p, N0, nroots, N0, cmax.p);
-      SHCI_LAUNCH_CHECK();
-      select(cmax.p, eps1);
+      if (trev_sector != 0) {
+        if (!ensure_flip())
+          throw Error(kErrState, "time reversal needs the flipped partner of every determinant in the space");
+        trev_cmax(dets.p, ci.p, N0, nroots, N0, flipidx.p, cmax.p, stream);
+        select_trev(cmax.p, eps1);
+      } else {
+        k_cmax<<<grid_for(N0, 256), 256, 0, stream>>>(ci.p, N0, nroots, N0, cmax.p);
+        SHCI_LAUNCH_CHECK();
+        select(cmax.p, eps1);
+      }
       const size_t N = ndet;
       if (trace_level() > 0)
         std::fprintf(stderr, "[select] %zu eps1=%.3e ndets %zu -> %zu in %.3f s\n", iter, eps1, N0, N, now_s() - ta);

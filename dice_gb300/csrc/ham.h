@@ -182,6 +182,16 @@ __device__ __forceinline__ int in_mask(const SelectParams& sp, int r, int p) {
 int64_t select_candidates(const Det2* dets, const double* cmax, size_t n, double eps1, const IntsView& ints,
                           const HeatBathView& hb, double maxEntry, const SelectParams& sp, const DetHash& present,
                           Det2* out, int64_t cap, int64_t* d_counter, cudaStream_t s);
+// Time reversal (kernels_select.cu): cMax of the reference's symmetrized
+// basis for every determinant (0 for the non-standard member of a pair), and
+// the new determinants of a selection: the standard members of the
+// candidates' pairs, sorted, unique and absent from the space, followed by
+// the flipped partners of the open-shell ones, written to out (room for 2n);
+// returns how many.
+void trev_cmax(const Det2* dets, const double* ci, size_t ld, int nroots, size_t n, const int32_t* flip, double* out,
+               cudaStream_t s);
+size_t trev_new_dets(Det2* cand, size_t n, const DetHash& present, const Det2* dets, Det2* out, DevBuf<int64_t>& flag,
+                     DevBuf<int64_t>& pos, Prims& pr, cudaStream_t s);
 // Number of the n determinants q that the hash set `present` (over dets) holds.
 int64_t count_present(const Det2* q, size_t n, const DetHash& present, const Det2* dets, int64_t* d_counter,
                       cudaStream_t s);

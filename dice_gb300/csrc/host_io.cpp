@@ -313,12 +313,11 @@ void read_input(const std::string& path, Schedule& s) {
     } else if (iequal(arg, "targetError")) {
       need(1);
       s.targetError = std::atof(tok[1].c_str());
-    } else if (iequal(arg, "Treversal")) {
-      // the time-reversal basis (SHCI/SHCImakeHamiltonian.cpp:411-483) is not
-      // restated here; running the plain path instead would give another energy
+    } else if (iequal(arg, "Treversal")) {  // SHCI/input.cpp:253-258
       need(1);
-      if (std::atoi(tok[1].c_str()) != 0)
-        throw Error(kErrInvalid, "Treversal (time-reversal symmetry) is not supported; remove it or set it to 0");
+      s.trev = std::atoi(tok[1].c_str());
+      if (!(s.trev == 0 || s.trev == 1 || s.trev == -1))
+        throw Error(kErrInvalid, "Treversal should be either 0, 1, or -1.");
     } else if (iequal(arg, "io")) {
       s.io = true;
     } else if (iequal(arg, "noio")) {

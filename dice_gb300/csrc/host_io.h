@@ -55,6 +55,10 @@ struct Schedule {
   double targetError = 1.e-4;
   long long seed = -1;
   int writeBest = 0;  // writebestdeterminants (SHCI/input.cpp:243-244)
+  // time-reversal symmetry (Treversal, SHCI/input.cpp:253-258): 0 off, +1 or
+  // -1 the sign that relates a determinant's coefficient to its alpha <-> beta
+  // flipped partner's
+  int trev = 0;
   // checkpoints (SHCI/input.cpp:72, 176-183, 330-331, 400): io writes the
   // variational result after every iteration (default), noio does not;
   // restart = 1 resumes after the saved iteration, 2 (fullrestart) reruns the

@@ -308,6 +308,109 @@ void flip_project(double* x, size_t n, const int32_t* flip, const int8_t* sign, 
   SHCI_CUDA(cudaMemcpyAsync(x, tmp, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
 }
 
+// ---------------------------------------------------------------------------
+// Time-reversal symmetry (Treversal). The reference keeps one determinant of
+// each alpha <-> beta flipped pair, the "standard" one
+// (Determinant::isStandard, SHCI/Determinants.h:241-258: the larger of D and
+// its flip, words compared as unsigned integers from the top word down), and
+// works in the basis (D + t p(D) D~)/sqrt(2). That basis spans the flip sector
+// of the determinant space that holds both members of every pair, so the
+// engine keeps both, selects from the standard one as the reference does, and
+// projects Davidson into the sector.
+// ---------------------------------------------------------------------------
+// cMax of the reference's time-reversal run (SHCI/SHCIbasics.cpp:954-965 on
+// the coefficients of the symmetrized basis): for a standard determinant
+// sqrt(sum over roots of c_i^2 + c_flip(i)^2) (its pair's coefficient is
+// sqrt(2) times each member's), c_i alone for a closed shell; 0 for the
+// flipped member, which the reference does not hold as a parent.
+__global__ void k_trev_cmax(const Det2* __restrict__ dets, const double* __restrict__ ci, size_t ld, int nroots,
+                            size_t n, const int32_t* __restrict__ flip, double* __restrict__ out) {
+  for (size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x) {
+    const Det2 d = dets[j];
+    if (!det_is_standard(d)) {
+      out[j] = 0.0;
+      continue;
+    }
+    const size_t f = (size_t)flip[j];
+    double s = 0.0;
+    for (int r = 0; r < nroots; ++r) {
+      const double c = ci[(size_t)r * ld + j];
+      s = __dadd_rn(s, __dmul_rn(c, c));
+      if (f != j) {
+        const double cf = ci[(size_t)r * ld + f];
+        s = __dadd_rn(s, __dmul_rn(cf, cf));
+      }
+    }
+    out[j] = sqrt(s);
+  }
+}
+void trev_cmax(const Det2* dets, const double* ci, size_t ld, int nroots, size_t n, const int32_t* flip, double* out,
+               cudaStream_t s) {
+  size_t blocks = std::min<size_t>((n + 255) / 256, 152 * 32);
+  if (blocks < 1) blocks = 1;
+  k_trev_cmax<<<(unsigned)blocks, 256, 0, s>>>(dets, ci, ld, nroots, n, flip, out);
+  SHCI_LAUNCH_CHECK();
+}
+
+__global__ void k_make_standard(Det2* __restrict__ q, size_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    if (!det_is_standard(q[i])) q[i] = det_flip_pair(q[i]);
+}
+// flag[i] = q[i] is absent from the hash set (which == 0), or q[i] has unpaired
+// electrons (which == 1)
+__global__ void k_trev_flags(const Det2* __restrict__ q, size_t n, const uint32_t* __restrict__ slots,
+                             uint64_t mask, const Det2* __restrict__ dets, int which, int64_t* __restrict__ flag) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const Det2 d = q[i];
+    if (which == 0) {
+      flag[i] = hash_contains(slots, mask, dets, d) ? 0 : 1;
+    } else {
+      const Det2 f = det_flip_pair(d);
+      flag[i] = (f.w0 != d.w0 || f.w1 != d.w1) ? 1 : 0;
+    }
+  }
+}
+// out[pos[i]] = q[i] (or its flip) for flagged i
+__global__ void k_trev_compact(const Det2* __restrict__ q, size_t n, const int64_t* __restrict__ flag,
+                               const int64_t* __restrict__ pos, int flip_it, Det2* __restrict__ out) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    if (flag[i]) out[pos[i]] = flip_it ? det_flip_pair(q[i]) : q[i];
+}
+
+size_t trev_new_dets(Det2* cand, size_t n, const DetHash& present, const Det2* dets, Det2* out, DevBuf<int64_t>& flag,
+                     DevBuf<int64_t>& pos, Prims& pr, cudaStream_t s) {
+  if (n == 0) return 0;
+  size_t blocks = std::min<size_t>((n + 255) / 256, 152 * 32);
+  // the standard member of each candidate's pair (SHCI/SHCIbasics.cpp:984-987),
+  // sorted and unique (:992-994), without those already present (:996-997)
+  k_make_standard<<<(unsigned)blocks, 256, 0, s>>>(cand, n);
+  SHCI_LAUNCH_CHECK();
+  sort_dets(cand, nullptr, n, pr, s);
+  n = unique_dets(cand, n, pr, s);
+  blocks = std::min<size_t>((n + 255) / 256, 152 * 32);
+  flag.reserve(n);
+  pos.reserve(n);
+  k_trev_flags<<<(unsigned)blocks, 256, 0, s>>>(cand, n, present.slots.p, present.mask, dets, 0, flag.p);
+  SHCI_LAUNCH_CHECK();
+  int64_t m = 0;
+  scan_exclusive_i64(flag.p, pos.p, n, &m, pr, s);
+  k_trev_compact<<<(unsigned)blocks, 256, 0, s>>>(cand, n, flag.p, pos.p, 0, out);
+  SHCI_LAUNCH_CHECK();
+  // then the flipped partners of the open-shell ones, in the same order (the
+  // order in which SHCI/SHCIbasics.cpp:730-781 unpacks them)
+  const size_t bm = std::max<size_t>(1, std::min<size_t>(((size_t)m + 255) / 256, 152 * 32));
+  int64_t f = 0;
+  if (m > 0) {
+    k_trev_flags<<<(unsigned)bm, 256, 0, s>>>(out, (size_t)m, present.slots.p, present.mask, dets, 1, flag.p);
+    SHCI_LAUNCH_CHECK();
+    scan_exclusive_i64(flag.p, pos.p, (size_t)m, &f, pr, s);
+    k_trev_compact<<<(unsigned)bm, 256, 0, s>>>(out, (size_t)m, flag.p, pos.p, 1, out + m);
+    SHCI_LAUNCH_CHECK();
+  }
+  SHCI_CUDA(cudaStreamSynchronize(s));
+  return (size_t)(m + f);
+}
+
 // How many of q[0, n) the hash set holds.
 __global__ void k_count_present(const Det2* __restrict__ q, size_t n, const uint32_t* __restrict__ slots,
                                 uint64_t mask, const Det2* __restrict__ dets, unsigned long long* __restrict__ cnt) {

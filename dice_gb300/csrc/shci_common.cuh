@@ -69,6 +69,24 @@ __host__ __device__ inline Det2 det_from_strings(uint64_t a, uint64_t b) {
   return d;
 }
 
+// The alpha <-> beta flip of a determinant (Determinant::flipAlphaBeta,
+// SHCI/Determinants.h:278-282) and whether it is the standard member of its
+// pair (Determinant::isStandard, :241-258: not smaller than its flip, words
+// compared as unsigned integers from the top word down; a closed shell is its
+// own flip and standard).
+__host__ __device__ inline Det2 det_flip_pair(const Det2& d) {
+  const uint64_t ev = 0x5555555555555555ull, od = 0xAAAAAAAAAAAAAAAAull;
+  Det2 f;
+  f.w0 = ((d.w0 & ev) << 1) | ((d.w0 & od) >> 1);
+  f.w1 = ((d.w1 & ev) << 1) | ((d.w1 & od) >> 1);
+  return f;
+}
+__host__ __device__ inline bool det_is_standard(const Det2& d) {
+  const Det2 f = det_flip_pair(d);
+  if (d.w1 != f.w1) return d.w1 > f.w1;
+  return d.w0 >= f.w0;
+}
+
 // Number of occupied spin orbitals strictly between lo and hi (lo < hi).
 __device__ inline int occ_between(const Det2& d, int lo, int hi) {
   // bits (lo, hi): mask of bits < hi minus bits <= lo

@@ -234,7 +234,19 @@ int shci_davidson(shci_ctx* ctx, int mode, int block, int nroots, double* x0, in
  * relative prefix resolves against the input file's directory); `restart`
  * resumes after the saved iteration, or returns the saved result when that
  * iteration already used the final eps1; `fullrestart` reruns the schedule
- * from the saved space. A missing or foreign checkpoint is SHCI_ERR_IO. */
+ * from the saved space. A missing or foreign checkpoint is SHCI_ERR_IO.
+ * Treversal t = +-1 (time-reversal symmetry, SHCI/input.cpp:253-258;
+ * ignored for an odd electron count as SHCI/SHCI.cpp:188-195 does; needs as
+ * many alpha as beta electrons): the reference keeps the standard member of
+ * every alpha <-> beta flipped pair and works in the basis
+ * (D + t p(D) flip(D))/sqrt(2) (SHCI/Determinants.cpp:32-121,
+ * SHCI/SHCImakeHamiltonian.cpp:411-483); here the space holds both members of
+ * every pair (the form the reference unpacks to, SHCI/SHCIbasics.cpp:730-781),
+ * selection runs from the standard member with the pair's coefficient
+ * (SHCI/SHCIbasics.cpp:984-997) and every Davidson vector is kept in the
+ * sector c(flip(D)) = t p(D) c(D): the same eigenvalues. The space, the
+ * coefficients and the per-iteration determinant counts then count both
+ * members of every pair. */
 int shci_run_input(shci_ctx* ctx, const char* input_path, const char* fcidump, int mode, int block, double* E,
                    int cap_roots, int* nroots);
 /* Per-iteration log of the last run: ndets, E (root 0, coreE added),

@@ -17,12 +17,14 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "slow: long CPU oracle run")
 
 
-def golden_case(tmp_path, name, input_name):
+def golden_case(tmp_path, name, input_name, fcidump=None):
     """Unpack a golden fixture (FCIDUMP + input file) into tmp_path; returns
-    the input path."""
+    the input path. fcidump: the name of another fixture whose FCIDUMP the
+    case shares."""
     d = tmp_path / name
     d.mkdir(parents=True, exist_ok=True)
-    with gzip.open(os.path.join(GOLDEN, name + ".FCIDUMP.gz"), "rb") as f, open(d / "FCIDUMP", "wb") as g:
+    with gzip.open(os.path.join(GOLDEN, (fcidump or name) + ".FCIDUMP.gz"), "rb") as f, \
+            open(d / "FCIDUMP", "wb") as g:
         shutil.copyfileobj(f, g)
     src = os.path.join(GOLDEN, name + "." + input_name)
     text = open(src).read()
@@ -36,7 +38,7 @@ def golden_case(tmp_path, name, input_name):
 
 @pytest.fixture
 def golden(tmp_path):
-    return lambda name, inp: golden_case(tmp_path, name, inp)
+    return lambda name, inp, fcidump=None: golden_case(tmp_path, name, inp, fcidump)
 
 
 def gpu_available():

@@ -7,6 +7,8 @@ What is copied, and what it pins:
   * examples/h8_631g: FCIDUMP, dice.dat, the per-iteration table of dice.out
     (determinant counts, energies, Davidson iterations) and the final
     determinant set from the `dets` listing (2470 determinants with weights).
+  * tests/SHCI/restart_trev: input2.dat and input3.dat with Treversal 1 on the
+    restart FCIDUMP; trusted_hci.e holds E_var of 5e-3 -> 1e-3 -> 1e-4.
   * tests/SHCI/restart: FCIDUMP, input2.dat (io run) and input3.dat (restart);
     trusted_hci.e holds E_var of
     the eps1 schedule 5e-3 -> 1e-3 -> 5e-5.
@@ -92,6 +94,13 @@ def main(ref):
     shutil.copy(os.path.join(rs, "input2.dat"), os.path.join(HERE, "restart.input2.dat"))
     out["restart"] = {"E_var": read_e(os.path.join(rs, "trusted_hci.e")), "tol": 5e-5,
                       "source": "tests/SHCI/restart/trusted_hci.e (runTests.sh tolerance 5e-5)"}
+    # time-reversal restart fixture (the same FCIDUMP as restart, Treversal 1)
+    rt = os.path.join(ref, "tests", "SHCI", "restart_trev")
+    shutil.copy(os.path.join(rt, "input2.dat"), os.path.join(HERE, "restart_trev.input2.dat"))
+    shutil.copy(os.path.join(rt, "input3.dat"), os.path.join(HERE, "restart_trev.input3.dat"))
+    out["restart_trev"] = {"E_var": read_e(os.path.join(rt, "trusted_hci.e")), "tol": 5e-5,
+                           "fcidump": "restart.FCIDUMP.gz",
+                           "source": "tests/SHCI/restart_trev/trusted_hci.e (runTests.sh tolerance 5e-5)"}
 
     # n2 with RAS restriction
     n2 = os.path.join(ref, "tests", "SHCI", "n2_RAS")

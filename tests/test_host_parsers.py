@@ -87,11 +87,12 @@ def test_input_engine_keywords(tmp_path):
     ("schedule\n0 1e-3\nend\nmaxiter 4\n", "nocc"),
     ("nocc 2\n0 1\nend\nschedule\n0 1e-3\nend\nmaxiter 4\nprecision half\n", "precision"),
     ("nocc 2\n0 1\nend\nschedule\n0 1e-3\nend\nmaxiter 4\ndavidsonBasis 32 8\n", "davidsonBasis"),
-    ("nocc 2\n0 1\nend\nschedule\n0 1e-3\nend\nmaxiter 4\nTreversal 1\n", "Treversal"),
+    ("nocc 2\n0 1\nend\nschedule\n0 1e-3\nend\nmaxiter 4\nTreversal 2\n", "Treversal"),
 ])
 def test_input_errors(tmp_path, text, msg):
-    """Malformed inputs and keywords whose stage is not restated here (a
-    nonzero Treversal) are rejected with SHCI_ERR_INVALID and the reason."""
+    """Malformed inputs and invalid values (a Treversal other than 0, 1 or -1,
+    as SHCI/input.cpp:253-258 rejects) are rejected with SHCI_ERR_INVALID and
+    the reason."""
     with pytest.raises(eng.ShciError) as e:
         eng.input_info(_write(tmp_path, text))
     assert e.value.code == 1
