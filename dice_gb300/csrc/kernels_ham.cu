@@ -302,20 +302,41 @@ __device__ void visit_row(const HelperView& h, uint32_t I, V& v) {
     const int64_t s0 = h.aSingStart[ia], s1 = h.aSingStart[ia + 1];
     const int nb = __popcll(B);
     const int64_t nprobe = (s1 - s0) * nb;
+    // Probe t = (excitation sidx, occupied beta orbital `which`): each lane
+    // keeps its pair and steps it by 32 probes a round (no division per
+    // probe), and lane k holds the k-th occupied beta orbital of B for the
+    // others to read (B's orbitals beyond the 32nd, possible only past 32 beta
+    // electrons, are found bit by bit)
+    int occ_k = 0;
+    {
+      uint64_t r = B;
+      for (int k = 0; k < lane && r; ++k) r &= r - 1;
+      occ_k = r ? __ffsll((long long)r) - 1 : 0;
+    }
+    const int step_q = 32 / nb, step_r = 32 % nb;
+    int64_t sidx = lane / nb;
+    int which = lane % nb;
     for (int64_t base = 0; base < nprobe; base += 32) {
       const int64_t t = base + lane;
       // each lane locates the entries of its key (As, B - b)
       int64_t lo = 0, len = 0;
-      int bq = 0;  // the beta orbital removed by this probe
-      bool first_b = false;
-      if (t < nprobe) {
-        const uint32_t As = h.aSing[s0 + t / nb];
-        const int which = (int)(t % nb);
+      int bq = __shfl_sync(kFull, occ_k, which & 31);  // the beta orbital removed by this probe
+      if (which >= 32) {
         uint64_t r = B;
         for (int k = 0; k < which; ++k) r &= r - 1;
         bq = __ffsll((long long)r) - 1;
+      }
+      const int64_t my_s = sidx;
+      const bool first_b = which == 0;
+      which += step_r;
+      sidx += step_q;
+      if (which >= nb) {
+        which -= nb;
+        ++sidx;
+      }
+      if (t < nprobe) {
+        const uint32_t As = h.aSing[s0 + my_s];
         const uint64_t Bm = B ^ (1ull << bq);
-        first_b = which == 0;
         // lower bound of Bm in the section of group As, then the run of equal keys
         uint32_t e = h.m1g[As];
         uint32_t e1 = h.m1g[As + 1];

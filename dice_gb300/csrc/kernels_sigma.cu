@@ -50,18 +50,18 @@ template <>
 struct VecF<2> {
   __device__ static void fma(Acc* acc, float h, const float* x, int j) {
     float2 v = __ldg(reinterpret_cast<const float2*>(x) + j);
-    acc_add(acc[0], h, v.x);
-    acc_add(acc[1], h, v.y);
+    acc_add_rounded(acc[0], h, v.x);
+    acc_add_rounded(acc[1], h, v.y);
   }
 };
 template <>
 struct VecF<4> {
   __device__ static void fma(Acc* acc, float h, const float* x, int j) {
     float4 v = __ldg(reinterpret_cast<const float4*>(x) + j);
-    acc_add(acc[0], h, v.x);
-    acc_add(acc[1], h, v.y);
-    acc_add(acc[2], h, v.z);
-    acc_add(acc[3], h, v.w);
+    acc_add_rounded(acc[0], h, v.x);
+    acc_add_rounded(acc[1], h, v.y);
+    acc_add_rounded(acc[2], h, v.z);
+    acc_add_rounded(acc[3], h, v.w);
   }
 };
 

@@ -251,6 +251,19 @@ __device__ __forceinline__ void acc_add(Acc& a, float h, float x) {
   a.s = t;
   a.c = __fadd_rn(a.c, __fadd_rn(e, pe));
 }
+// The same without the product's rounding residual: the rounded product h*x
+// does not depend on the order of the sum (so a row and its alpha <-> beta
+// flipped row still sum the same products, compensated for order), and its
+// rounding, 2^-24 of the product, is the size of the FP32 rounding of h and x
+// themselves. Used where several vectors share each loaded element.
+__device__ __forceinline__ void acc_add_rounded(Acc& a, float h, float x) {
+  const float p = __fmul_rn(h, x);
+  const float t = __fadd_rn(a.s, p);
+  const float bp = __fsub_rn(t, a.s);
+  const float e = __fadd_rn(__fsub_rn(a.s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+  a.s = t;
+  a.c = __fadd_rn(a.c, e);
+}
 __device__ __forceinline__ void acc_merge(Acc& a, const Acc& b) {
   const float t = __fadd_rn(a.s, b.s);
   const float bp = __fsub_rn(t, a.s);

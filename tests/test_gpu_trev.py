@@ -56,17 +56,23 @@ def test_restart_trev_fixture_end_to_end(golden, mode):
     assert np.allclose(c[idx], parity * c, atol=1e-9)
 
 
-def test_trev_minus_one_from_a_closed_shell_is_an_error(tmp_path, golden):
-    """Treversal -1 keeps the sector in which a closed-shell determinant has
-    no component: started from the closed-shell reference determinant alone
-    the space has no room for a root there, which is a status, not NaNs."""
+def test_trev_minus_one_is_the_other_sector(tmp_path, golden):
+    """Treversal -1 keeps the flip sector in which a closed-shell determinant
+    has no component, so it cannot hold this closed-shell system's ground
+    state: the run (whose first solve starts at random inside the sector,
+    the reference determinant having no component there) converges to a
+    state above the plain run's."""
     first = golden("restart_trev", "input2.dat", fcidump="restart")
     text = open(first).read().replace("Treversal 1", "Treversal -1").replace("\nio", "\nnoio")
     minus = os.path.join(os.path.dirname(first), "minus.dat")
     with open(minus, "w") as f:
         f.write(text)
+    plain = os.path.join(os.path.dirname(first), "plain.dat")
+    with open(plain, "w") as f:
+        f.write(text.replace("Treversal -1", ""))
     e = eng.Engine(0)
-    with pytest.raises(eng.ShciError) as ei:
-        e.run_input(minus, mode="fp64")
-    assert ei.value.code == 1 and "sector" in str(ei.value)
+    Em = e.run_input(minus, mode="fp64")
+    Ep = e.run_input(plain, mode="fp64")
     e.close()
+    assert np.isfinite(Em[0])
+    assert Em[0] > Ep[0] + 1e-3
