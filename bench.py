@@ -1,6 +1,6 @@
 """Benchmark of the SHCI variational engine on one GB300 (or N replicas).
 
-Workload (config 2 of the task's list, the largest whose stated size fits one
+Workload (the largest of the synthetic workloads whose stated size fits one
 GPU in the stored form): the synthetic molecular Hamiltonian with 24 spatial
 orbitals, 12 alpha + 12 beta electrons, 72 Cholesky vectors (seeded), eps1
 schedule 1e-3 -> 3e-4 -> 1e-4, one root. The whole variational stage runs in
@@ -26,8 +26,10 @@ Further keys: `plain_fp64_sigma`, `block_k4_sigma`, `var` (the runs above),
 `pt` (deterministic PT2 of the final space, eps2 1e-5, through
 shci_pt_deterministic; `--section pt` times it alone), `rdm` (spatial 1- and
 2-RDMs through shci_run_rdm), each with the CPU oracle on a bounded sample
-beside it, and `configs` (the other synthetic workloads, including config 1,
-the 12-site Hubbard ring at its stated schedule, against the CPU oracle).
+beside it, and `configs` (the other synthetic workloads, including the
+12-site Hubbard ring at its stated schedule, against the CPU oracle).
+`--section sigma | direct | ham` times the stored sigmas, the matrix-free
+sigma or the Hamiltonian build alone.
 
 cpu_baseline: the oracle's restatement of the reference's rank-parallel
 Hmult2 (rows dealt round-robin to one worker per host thread, private
@@ -55,7 +57,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOAD = "mol24"
-WORKLOAD_DESC = ("mol24 (config 2): synthetic molecular FCIDUMP n=24, 12a+12b, rank-72 Cholesky ERIs, seed "
+WORKLOAD_DESC = ("mol24: synthetic molecular FCIDUMP n=24, 12a+12b, rank-72 Cholesky ERIs, seed "
                  "20260001, eps1 1e-3 -> 3e-4 -> 1e-4, 1 root; sigma over the final space of the FP64 "
                  "variational run")
 # Davidson tolerance of parity mode (loose and final solves alike)
@@ -358,8 +360,8 @@ def run_pt_only(args):
 
 
 def other_configs(work, device):
-    """The other configurations: config 1 (the 12-site Hubbard ring) at its
-    stated schedule against the oracle, and configs 3-5's generators at the
+    """The other workloads: the 12-site Hubbard ring at its stated schedule
+    against the oracle, and the mol36, mol64 and mol50 generators at the
     sizes a bench run affords, each the plain FP64 GPU path against the new
     form on the same input (final Davidson solve to 1e-6, loose solves at the
     reference's 5e-5): mol36 with 4 roots in block Davidson, mol64
@@ -382,7 +384,7 @@ def other_configs(work, device):
                 "ndets": [int(v) for v in lg["ndets"]], "_dets": dets}
 
     out = {}
-    # config 1: the 12-site Hubbard ring at its stated schedule, GPU paths
+    # the 12-site Hubbard ring at its stated schedule, GPU paths
     # against the oracle's serial run on one host core
     from oracle import oracle as orc
     hub = synthetic.make_workload("hubbard12", os.path.join(work, "hubbard12"))
@@ -399,13 +401,13 @@ def other_configs(work, device):
         res[key] = {"E_var": float(E[0]), "wall_s": t["total"], "ndets": [int(v) for v in g.run_log()["ndets"]],
                     "dS_vs_oracle": sym_diff(g.dets(), oref.dets), "dE_vs_oracle": float(E[0] - oref.E[0])}
         g.close()
-    out["hubbard12_config1"] = {
+    out["hubbard12_stated_schedule"] = {
         "what": "1-D Hubbard ring, 12 sites, t=1, U=4, 6a+6b, eps1 1e-3 (x3) then 1e-4, maxiter 6, 1 root, "
                 "stated schedule; GPU FP64 and new form against the oracle's FP64 run",
         "oracle": {"E_var": float(oref.E[0]), "wall_s": t_orc, "ndets": [int(v) for v in oref.ndets_log],
                    "cores": 1, "kind": "port"},
         **res, "fp64_speedup_vs_oracle": t_orc / res["fp64"]["wall_s"]}
-    # config 3's generator (n=36, 14a+14b, 4 roots, block Davidson): eps1
+    # mol36 (n=36, 14a+14b, 4 roots, block Davidson): eps1
     # 1e-3 twice then 6e-4 (eps1 3e-4 already selects 5.8 M determinants,
     # whose stored matrix does not fit beside the FP64 run's)
     # in parity mode (loose solves as tight as the final one), so that both
@@ -415,12 +417,12 @@ def other_configs(work, device):
     ref = run("mol36", sched, 3, "fp64", True, extra=par)
     new = run("mol36", sched, 3, "mixed", True, basis=(16, 12), extra=par)
     out["mol36_4roots_block"] = {
-        "what": "config 3's generator: n=36, 14a+14b, 4 roots, block Davidson (k=4 per sigma launch), eps1 "
-                "1e-3 x2 -> 6e-4, parity mode (every solve to 1e-6) (the stated eps1 3e-5 selects far more than one "
-                "GPU holds; see DESIGN)",
+        "what": "mol36: n=36, 14a+14b, 4 roots, block Davidson (k=4 per sigma launch), eps1 "
+                "1e-3 x2 -> 6e-4, parity mode (every solve to 1e-6) (eps1 3e-5 selects far more determinants than "
+                "one GPU holds in the stored form)",
         "fp64": ref, "new_form": new, "dE_per_root": [a - b for a, b in zip(new["E_var"], ref["E_var"])],
         "dS": sym_diff(new.pop("_dets"), ref.pop("_dets")), "wall_speedup": ref["wall_s"] / new["wall_s"]}
-    # config 5's generator (n=64, 20a+20b, two-word determinants), 4 roots,
+    # mol64 (n=64, 20a+20b, two-word determinants), 4 roots,
     # matrix-free: eps1 2e-3 twice
     # one selection (the same space for both paths: the reference forces the
     # loose tolerance of matrix-free runs to 3e-2, SHCI/input.cpp, so later
@@ -430,18 +432,18 @@ def other_configs(work, device):
         ref = run("mol64", sched, it, "fp64", True, extra=("DirectDavidson",))
         new = run("mol64", sched, it, "mixed", True, extra=("DirectDavidson",))
         out[key] = {
-            "what": "config 5's generator: n=64, 20a+20b (two-word determinants), 4 roots, matrix-free sigma, "
+            "what": "mol64: n=64, 20a+20b (two-word determinants), 4 roots, matrix-free sigma, "
                     "schedule %s" % sched,
             "fp64": ref, "mixed": new, "dE_per_root": [a - b for a, b in zip(new["E_var"], ref["E_var"])],
             "dS": sym_diff(new.pop("_dets"), ref.pop("_dets")), "wall_speedup": ref["wall_s"] / new["wall_s"]}
-    # config 4's generator (n=50, 16a+16b): eps1 1e-3 twice then 3e-4 (2.3 M
+    # mol50 (n=50, 16a+16b): eps1 1e-3 twice then 3e-4 (2.3 M
     # determinants), learned preconditioner against the plain one
     sched = [(0, 1e-3), (2, 3e-4)]
     plain = run("mol50", sched, 3, "mixed", False, "plain")
     mlp = run("mol50", sched, 3, "mixed", False, "mlp")
     dS50 = sym_diff(plain.pop("_dets"), mlp.pop("_dets"))
     out["mol50_learned_preconditioner"] = {
-        "what": "config 4's generator: n=50, 16a+16b, 1 root, mixed precision, reference subspace, eps1 1e-3 x2 "
+        "what": "mol50: n=50, 16a+16b, 1 root, mixed precision, reference subspace, eps1 1e-3 x2 "
                 "-> 3e-4; learned preconditioner (trained on Davidson's residual/correction pairs, judged by the "
                 "plain one) against the plain diagonal preconditioner",
         "plain": plain, "mlp": mlp, "dE": mlp["E_var"][0] - plain["E_var"][0], "dS": dS50,
@@ -678,9 +680,48 @@ def run_sigma_only(args):
         print(json.dumps(out), flush=True)
 
 
+def run_ham_only(args):
+    """--section ham: the plain FP64 variational run of the chosen case, then
+    the Hamiltonian of its final space built from scratch (string tables,
+    partial-string index, diagonal, count, emit, row sort; for the mixed form
+    also the 16-bit-delta copy), FP64 and mixed, each timed build inside its
+    own NVTX range (bench_ham_<mode>). Reloading the determinants before each
+    build drops every table and the stored matrix."""
+    import torch
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    from dice_gb300 import engine as eng
+    work = tempfile.mkdtemp()
+    inp = make_inputs(work, args.case)
+    e = eng.Engine(local)
+    e.run_input(inp, mode="fp64")
+    dets = e.dets()
+    out = {"case": args.case, "n_dets": len(dets)}
+    for mode in ("fp64", "mixed"):
+        ts = []
+        nnz = 0
+        for it in range(args.warmup + args.steps):
+            e.set_dets(dets)
+            torch.cuda.synchronize()
+            timed = it >= args.warmup
+            if timed:
+                torch.cuda.nvtx.range_push("bench_ham_" + mode)
+            t0 = time.perf_counter()
+            nnz = e.ham_build(mode)
+            torch.cuda.synchronize()
+            if timed:
+                ts.append(time.perf_counter() - t0)
+                torch.cuda.nvtx.range_pop()
+        t = statistics.median(ts)
+        out[mode] = {"s": t, "nnz": nnz, "gnnz_s": nnz / t / 1e9}
+    e.close()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
 def run_direct_only(args):
-    """--section direct: the matrix-free sigma timed alone. The space is config
-    3's generator (mol36: n=36, 14a+14b, rank-108 ERIs, seed 20260002) after
+    """--section direct: the matrix-free sigma timed alone. The space is the
+    mol36 workload's (n=36, 14a+14b, rank-108 ERIs, seed 20260002) after
     two eps1 = 1e-3 iterations of a stored FP64 run with four roots (about
     5e5 determinants); then four-vector FP32 and FP64 matrix-free sigmas, each
     inside its own NVTX range (bench_direct_<mode>), with the stored matrix's
@@ -696,7 +737,7 @@ def run_direct_only(args):
     N = e.ndets()
     nnz = e.ham_build("fp64")
     x = np.random.default_rng(1).standard_normal((4, N))
-    out = {"workload": "mol36, eps1 1e-3 x2 (config 3's generator)", "n_dets": N, "nnz_offdiag": nnz, "k": 4}
+    out = {"workload": "mol36 (n=36, 14a+14b, rank-108 ERIs), eps1 1e-3 x2", "n_dets": N, "nnz_offdiag": nnz, "k": 4}
     for mode in ("direct_mixed", "direct"):
         e.ham_build(mode)
         for _ in range(args.warmup):
@@ -725,10 +766,11 @@ def main():
     ap.add_argument("--no-configs", action="store_true", help="skip the other workloads (mol36, mol64, mol50)")
     ap.add_argument("--case", default="full", choices=["full", "medium", "small"],
                     help="small: the profiling case (two eps1 = 1e-3 iterations)")
-    ap.add_argument("--section", default="all", choices=["all", "pt", "sigma", "direct"],
+    ap.add_argument("--section", default="all", choices=["all", "pt", "sigma", "direct", "ham"],
                     help="pt: only the variational run and the timed perturbative stage; sigma: only the FP64 run "
                          "and the stored sigmas (FP64 k=1, mixed k=4, mixed k=1) timed on its space; direct: the "
-                         "matrix-free sigma (k=4, FP32 and FP64) on config 3's generator")
+                         "matrix-free sigma (k=4, FP32 and FP64) on mol36 (n=36, 14a+14b); ham: the FP64 run, "
+                         "then its Hamiltonian built from scratch (FP64 and mixed)")
     ap.add_argument("--pt-eps2", type=float, default=PT_EPS2)
     args = ap.parse_args()
     if args.warmup < 3:
@@ -739,6 +781,8 @@ def main():
         run_pt_only(args)
     elif args.section == "sigma":
         run_sigma_only(args)
+    elif args.section == "ham":
+        run_ham_only(args)
     elif args.section == "direct":
         run_direct_only(args)
     else:

@@ -21,10 +21,16 @@ struct HelperView {
   const uint32_t* aSing;
   // partial-string index: one 16-byte entry per (determinant J, occupied
   // beta orbital b of J): {beta string of J without b (low, high word),
-  // alpha group of J | b << 26, J}, sorted by (alpha group, partial string);
-  // the entries of alpha group g are [m1g[g], m1g[g+1])
+  // alpha group of J | b << 26, J}, sorted by (alpha group, partial string),
+  // so that the entries of one key (alpha group, partial string) are a run
   const uint4* m1ent;
-  const uint32_t* m1g;
+  // per alpha group g, an open-addressing table over the group's distinct
+  // partial strings: m1dir[g] = first slot << 6 | log2(slots); a slot is
+  // {first entry of the key's run, (run length - 1) << 26 | 26-bit
+  // fingerprint of the partial string}, all bits set in an empty slot's first
+  // word; every table is at most half full
+  const uint2* m1tab;
+  const uint64_t* m1dir;
 };
 
 // Alpha/beta string tables of one determinant space
@@ -36,18 +42,19 @@ struct Helpers {
   DevBuf<uint32_t> aidx, bidx, aDets, bDets, aSing;
   DevBuf<int64_t> aStart, bStart, aSingStart;
   DevBuf<uint4> m1ent;
-  DevBuf<uint32_t> m1g;
+  DevBuf<uint2> m1tab;
+  DevBuf<uint64_t> m1dir;
   int64_t nm1 = 0;
   void build(const Det2* dets, size_t n, int norb, Prims& pr, cudaStream_t s);
   HelperView view() const {
     return HelperView{N,         astr.p,      bstr.p,  aidx.p,  bidx.p,  aStart.p, aDets.p,
                       aGroupB.p, bStart.p,    bDets.p, bGroupA.p, aSingStart.p, aSing.p,
-                      nm1 > 0 ? m1ent.p : nullptr, m1g.p};
+                      nm1 > 0 ? m1ent.p : nullptr, m1tab.p, m1dir.p};
   }
   size_t bytes() const {
     return astr.bytes() + bstr.bytes() + ua.bytes() + ub.bytes() + aGroupB.bytes() + bGroupA.bytes() +
            aidx.bytes() + bidx.bytes() + aDets.bytes() + bDets.bytes() + aSing.bytes() + aStart.bytes() +
-           bStart.bytes() + aSingStart.bytes() + m1ent.bytes() + m1g.bytes();
+           bStart.bytes() + aSingStart.bytes() + m1ent.bytes() + m1tab.bytes() + m1dir.bytes();
   }
 };
 

@@ -13,7 +13,8 @@
 //   2. determinants whose alpha string As is a single excitation of A and
 //      whose beta string equals B or is one excitation away. Every such J
 //      contains the partial string B - b for some occupied b of B, so it is
-//      found by looking up the keys (As, B - b) in the partial-string index:
+//      found by looking up the keys (As, B - b) in the partial-string index
+//      (a hash table per alpha group As gives each key's run of entries):
 //      |singles(A)| x |B| probes that return (nearly) only connections,
 //      instead of a scan over every determinant of every group As;
 //   3. determinants sharing I's beta string: alpha distance 2 (scan of the
@@ -154,9 +155,9 @@ static void build_groups(const uint64_t* str_of_det, const uint64_t* partner_of_
 }
 
 // Partial-string index entries, sorted by (alpha group, partial beta string):
-// the entries of one alpha group are contiguous and ordered by partial
-// string, so the probes of one row for one alpha string As search one small
-// section, and rows of the same alpha string search the same sections.
+// the entries of one key are one run and the runs of one alpha group are
+// contiguous, and so are the slots of the group's hash table, so the probes
+// of rows of the same alpha string touch the same small regions.
 constexpr uint32_t kM1GroupBits = 26;
 
 __global__ void k_m1_count(const uint64_t* __restrict__ bstr, size_t n, int64_t* __restrict__ cnt) {
@@ -191,18 +192,65 @@ __global__ void k_m1_permute(const uint4* __restrict__ src, const uint32_t* __re
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
     dst[k] = src[perm[k]];
 }
-// gstart[g] = first entry of alpha group g (g in [0, ng]), from the sorted group keys
-__global__ void k_m1_groups(const uint64_t* __restrict__ gk, int64_t n, int64_t ng, uint32_t* __restrict__ gstart) {
-  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g <= ng; g += (int64_t)gridDim.x * blockDim.x) {
-    int64_t lo = 0, hi = n;
-    while (lo < hi) {
-      const int64_t mid = (lo + hi) >> 1;
-      if ((int64_t)gk[mid] < g)
-        lo = mid + 1;
-      else
-        hi = mid;
+// Per-group hash tables over the index's distinct keys. Entry k starts a run
+// when its key (alpha group, partial string) differs from entry k-1's.
+__device__ __forceinline__ bool m1_same_key(const uint4& a, const uint4& b) {
+  constexpr uint32_t gmask = (1u << kM1GroupBits) - 1u;
+  return a.x == b.x && a.y == b.y && ((a.z ^ b.z) & gmask) == 0;
+}
+// Fibonacci hashing: the top lg bits of the partial string times 2^64 / phi
+// pick the slot; 26 bits of a second product are the slot's fingerprint
+__device__ __forceinline__ uint64_t m1_slot(uint64_t bm, unsigned lg) {
+  return (bm * 0x9e3779b97f4a7c15ull) >> (64u - lg);
+}
+__device__ __forceinline__ uint32_t m1_fingerprint(uint64_t bm) {
+  return (uint32_t)((bm * 0xc2b2ae3d27d4eb4full) >> 38);
+}
+constexpr uint32_t kM1Empty = 0xffffffffu;
+__global__ void k_m1_heads(const uint4* __restrict__ ent, int64_t n, uint32_t* __restrict__ keys_of_group) {
+  constexpr uint32_t gmask = (1u << kM1GroupBits) - 1u;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    const uint4 e = ent[k];
+    if (k == 0 || !m1_same_key(e, ent[k - 1])) atomicAdd(keys_of_group + (e.z & gmask), 1u);
+  }
+}
+// slots of group g: the power of two >= 2 x its distinct keys, at least 2
+__global__ void k_m1_slots(const uint32_t* __restrict__ keys_of_group, int64_t ng, int64_t* __restrict__ slots) {
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += (int64_t)gridDim.x * blockDim.x) {
+    int64_t t = 2;
+    while (t < 2 * (int64_t)keys_of_group[g]) t <<= 1;
+    slots[g] = t;
+  }
+}
+__global__ void k_m1_dir(const int64_t* __restrict__ slots, const int64_t* __restrict__ first, int64_t ng,
+                         uint64_t* __restrict__ dir) {
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += (int64_t)gridDim.x * blockDim.x)
+    dir[g] = ((uint64_t)first[g] << 6) | (uint64_t)(63 - __clzll((long long)slots[g]));
+}
+// One thread per run: measure the run (at most 64 entries: one per beta
+// orbital outside the partial string) and claim a slot of its group's table
+// by linear probing; a table more than half empty always has a free slot.
+__global__ void k_m1_insert(const uint4* __restrict__ ent, int64_t n, const uint64_t* __restrict__ dir,
+                            uint2* __restrict__ tab) {
+  constexpr uint32_t gmask = (1u << kM1GroupBits) - 1u;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    const uint4 e = ent[k];
+    if (k > 0 && m1_same_key(e, ent[k - 1])) continue;
+    int64_t f = k + 1;
+    while (f < n && m1_same_key(ent[f], e)) ++f;
+    const uint64_t d = dir[e.z & gmask];
+    const unsigned lg = (unsigned)(d & 63);
+    const uint64_t mask = (1ull << lg) - 1;
+    uint2* t = tab + (d >> 6);
+    const uint64_t bm = ((uint64_t)e.y << 32) | e.x;
+    uint64_t q = m1_slot(bm, lg);
+    for (uint64_t step = 0; step <= mask; ++step) {
+      if (atomicCAS(&t[q].x, kM1Empty, (uint32_t)k) == kM1Empty) {
+        t[q].y = ((uint32_t)(f - k - 1) << kM1GroupBits) | m1_fingerprint(bm);
+        break;
+      }
+      q = (q + 1) & mask;
     }
-    gstart[g] = (uint32_t)lo;
   }
 }
 
@@ -263,8 +311,25 @@ void Helpers::build(const Det2* dets, size_t n, int norb, Prims& pr, cudaStream_
       sort_u64(key.p, perm.p, (size_t)ne, pr, s);  // then by alpha group (stable)
       k_m1_permute<<<eb, 256, 0, s>>>(raw.p, perm.p, ne, m1ent.p);
       SHCI_LAUNCH_CHECK();
-      m1g.resize((size_t)NA + 1);
-      k_m1_groups<<<grid_for((size_t)NA + 1, 256), 256, 0, s>>>(key.p, ne, NA, m1g.p);
+      // the groups' hash tables
+      DevBuf<uint32_t> nkey;
+      DevBuf<int64_t> slots, first;
+      nkey.resize((size_t)NA);
+      slots.resize((size_t)NA);
+      first.resize((size_t)NA + 1);
+      SHCI_CUDA(cudaMemsetAsync(nkey.p, 0, (size_t)NA * sizeof(uint32_t), s));
+      k_m1_heads<<<eb, 256, 0, s>>>(m1ent.p, ne, nkey.p);
+      SHCI_LAUNCH_CHECK();
+      k_m1_slots<<<grid_for((size_t)NA, 256), 256, 0, s>>>(nkey.p, NA, slots.p);
+      SHCI_LAUNCH_CHECK();
+      int64_t nslot = 0;
+      scan_exclusive_i64(slots.p, first.p, NA, &nslot, pr, s);
+      m1dir.resize((size_t)NA);
+      k_m1_dir<<<grid_for((size_t)NA, 256), 256, 0, s>>>(slots.p, first.p, NA, m1dir.p);
+      SHCI_LAUNCH_CHECK();
+      m1tab.resize((size_t)nslot);
+      SHCI_CUDA(cudaMemsetAsync(m1tab.p, 0xff, (size_t)nslot * sizeof(uint2), s));
+      k_m1_insert<<<eb, 256, 0, s>>>(m1ent.p, ne, m1dir.p, m1tab.p);
       SHCI_LAUNCH_CHECK();
     }
   }
@@ -319,7 +384,8 @@ __device__ void visit_row(const HelperView& h, uint32_t I, V& v) {
     for (int64_t base = 0; base < nprobe; base += 32) {
       const int64_t t = base + lane;
       // each lane locates the entries of its key (As, B - b)
-      int64_t lo = 0, len = 0;
+      uint32_t lo = 0;
+      int len = 0;  // at most 64: one entry per beta orbital outside the key
       int bq = __shfl_sync(kFull, occ_k, which & 31);  // the beta orbital removed by this probe
       if (which >= 32) {
         uint64_t r = B;
@@ -337,49 +403,50 @@ __device__ void visit_row(const HelperView& h, uint32_t I, V& v) {
       if (t < nprobe) {
         const uint32_t As = h.aSing[s0 + my_s];
         const uint64_t Bm = B ^ (1ull << bq);
-        // lower bound of Bm in the section of group As, then the run of equal keys
-        uint32_t e = h.m1g[As];
-        uint32_t e1 = h.m1g[As + 1];
-        auto bm_of = [&](uint32_t q) {
-          const uint2 v = *reinterpret_cast<const uint2*>(h.m1ent + q);
-          return ((uint64_t)v.y << 32) | v.x;
-        };
-        {
-          uint32_t l = e, u = e1;
-          while (l < u) {
-            const uint32_t mid = (l + u) >> 1;
-            if (bm_of(mid) < Bm)
-              l = mid + 1;
-            else
-              u = mid;
+        // the slot of Bm in group As's table gives the key's run of entries
+        // (a fingerprint match is confirmed on the run's first entry, the
+        // entry the flattening below reads first); an empty slot means no
+        // determinant of the space has the key
+        const uint64_t d = h.m1dir[As];
+        const unsigned lg = (unsigned)(d & 63);
+        const uint64_t mask = (1ull << lg) - 1;
+        const uint2* tab = h.m1tab + (d >> 6);
+        const uint32_t fp = m1_fingerprint(Bm);
+        uint64_t q = m1_slot(Bm, lg);
+        for (uint64_t step = 0; step <= mask; ++step) {
+          const uint2 sl = tab[q];
+          if (sl.x == kM1Empty) break;
+          if ((sl.y & ((1u << kM1GroupBits) - 1u)) == fp) {
+            const uint2 k0 = *reinterpret_cast<const uint2*>(h.m1ent + sl.x);
+            if (k0.x == (uint32_t)Bm && k0.y == (uint32_t)(Bm >> 32)) {
+              lo = sl.x;
+              len = (sl.y >> kM1GroupBits) + 1;
+              break;
+            }
           }
-          e = l;
+          q = (q + 1) & mask;
         }
-        uint32_t f = e;
-        while (f < e1 && bm_of(f) == Bm) ++f;
-        lo = e;
-        len = f - e;
       }
       // flatten the lanes' matches and verify them 32 at a time
-      int64_t incl = len;
+      int incl = len;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
-        int64_t y = __shfl_up_sync(kFull, incl, o);
+        const int y = __shfl_up_sync(kFull, incl, o);
         if (lane >= o) incl += y;
       }
-      const int64_t total = __shfl_sync(kFull, incl, 31);
-      const int64_t excl = incl - len;
-      for (int64_t f0 = 0; f0 < total; f0 += 32) {
-        const int64_t f = f0 + lane;
+      const int total = __shfl_sync(kFull, incl, 31);
+      const int excl = incl - len;
+      for (int f0 = 0; f0 < total; f0 += 32) {
+        const int f = f0 + lane;
         int src = 0;
 #pragma unroll
         for (int st = 16; st >= 1; st >>= 1) {
           const int c = src + st;
-          const int64_t e = __shfl_sync(kFull, excl, c < 32 ? c : 31);
+          const int e = __shfl_sync(kFull, excl, c < 32 ? c : 31);
           if (c < 32 && e <= f) src = c;
         }
-        const int64_t elo = __shfl_sync(kFull, lo, src);
-        const int64_t eo = __shfl_sync(kFull, excl, src);
+        const uint32_t elo = __shfl_sync(kFull, lo, src);
+        const int eo = __shfl_sync(kFull, excl, src);
         const int wb = __shfl_sync(kFull, bq, src);
         const bool fb = __shfl_sync(kFull, first_b, src);
         bool hit = false, single = false;
@@ -388,7 +455,7 @@ __device__ void visit_row(const HelperView& h, uint32_t I, V& v) {
           // the entry holds J and the orbital b' its beta string has beyond
           // B - b: b' == b means beta equal (found once per occupied b, kept
           // for the first), otherwise a beta single excitation b -> b'
-          const uint4 en = h.m1ent[elo + (f - eo)];
+          const uint4 en = h.m1ent[(size_t)elo + (uint32_t)(f - eo)];
           J = en.w;
           single = (int)(en.z >> kM1GroupBits) == wb;
           hit = single ? fb : true;
@@ -481,9 +548,25 @@ __global__ void k_ham_count(HelperView h, int64_t row0, int64_t nr, const uint32
   }
 }
 
-// Emits (col, value) for one row; H_IJ is evaluated with the higher-index
-// determinant as the ket, the element the reference stores in row max(I,J)
-// (SHCI/SHCImakeHamiltonian.cpp:565-580).
+// H_IJ with the higher-index determinant as the ket, the element the
+// reference stores in row max(I,J) (SHCI/SHCImakeHamiltonian.cpp:565-580).
+// Kept out of line, taking and returning plain values: the visitors' step()
+// is inlined at every scan site of visit_row, and the Slater-Condon code
+// copied into each caused instruction-cache misses, while an out-of-line
+// member taking the visitor by address kept the visitor's state (queue
+// counts, accumulators, output position) in local memory.
+__device__ __noinline__ double ham_element(const double* I1, const double* I2, int norb, Det2 dI, Det2 dJ,
+                                           bool j_below) {
+  const IntsView iv{I1, I2, nullptr, nullptr, norb, nullptr, nullptr};
+  return j_below ? hij_any(iv, dJ, dI) : hij_any(iv, dI, dJ);
+}
+__device__ __noinline__ float ham_element_f32(const float* I1f, const float* I2f, int norb, Det2 dI, Det2 dJ,
+                                              bool j_below) {
+  const IntsView iv{nullptr, nullptr, nullptr, nullptr, norb, I1f, I2f};
+  return j_below ? hij_any_f32(iv, dJ, dI) : hij_any_f32(iv, dI, dJ);
+}
+
+// Emits (col, value) for one row (elements from ham_element).
 //
 // Connections found by the scans are queued per warp in shared memory, one
 // queue for single and one for double excitations; whenever a queue holds 32
@@ -505,8 +588,7 @@ struct EmitVisitor {
   int ns, nd;
 
   __device__ void store(int64_t q, uint32_t J) {
-    const Det2 dJ = dets[J];
-    const double hv = (J < I) ? hij_any(ints, dJ, dI) : hij_any(ints, dI, dJ);
+    const double hv = ham_element(ints.I1, ints.I2, ints.norb, dI, dets[J], J < I);
     col[q] = (int32_t)cmap[J];
     if (v64) v64[q] = hv;
     if (vhi) {
@@ -516,10 +598,8 @@ struct EmitVisitor {
     }
   }
   // evaluate the first `cnt` (<= 32) entries of queue q, then shift the rest
-  // down. Kept out of line: step() is inlined at every scan site and the
-  // Slater-Condon code would otherwise be copied into each (instruction-cache
-  // misses were the main stall of this kernel).
-  __device__ __noinline__ int drain(uint32_t* q, int n, int cnt) {
+  // down
+  __device__ int drain(uint32_t* q, int n, int cnt) {
     const int lane = threadIdx.x & 31;
     if (lane < cnt) store(pos + lane, q[lane]);
     pos += cnt;
@@ -552,16 +632,17 @@ struct EmitVisitor {
 
 // Rows [row0, row0 + nr) into a CSR whose row pointers are indexed by slot(I)
 // (see k_ham_count); columns are storage positions cmap[J].
-// Resident blocks per SM the emit and the matrix-free sigma are compiled for
-// (6 -> at most 40 registers a thread, a few hundred bytes of stack): both
-// wait on the latency of index probes and gathers, and the extra warps hide
-// more of it than the spills cost (mol36, 4-vector matrix-free sigma: 79 ms
-// with 64 registers and 4 blocks, 76 ms with 6; mol24 H build 1.47 -> 1.41 s).
+// Resident blocks per SM the emit and the matrix-free sigma are compiled for.
+// Both wait on the latency of index probes and gathers. The emit runs best
+// with 6 (at most 40 registers a thread, a few hundred bytes of spills: mol24
+// H build 0.98 s, 1.02 s with 4 blocks); the matrix-free sigma, whose
+// accumulators stay in registers, with 4 (64 registers, almost no spills:
+// mol36, 4 vectors, FP32 64 ms against 70 ms with 6).
 #ifndef SHCI_EMIT_MIN_BLOCKS
 #define SHCI_EMIT_MIN_BLOCKS 6
 #endif
 #ifndef SHCI_DIRECT_MIN_BLOCKS
-#define SHCI_DIRECT_MIN_BLOCKS 6
+#define SHCI_DIRECT_MIN_BLOCKS 4
 #endif
 __global__ void __launch_bounds__(256, SHCI_EMIT_MIN_BLOCKS) k_ham_emit(HelperView h, int64_t row0, int64_t nr,
                                                      const uint32_t* __restrict__ order,
@@ -1321,17 +1402,16 @@ struct DirectQVisitor {
   __device__ void add(uint32_t J) {
     const Det2 dJ = dets[J];
     if constexpr (F32) {
-      const float hv = (J < I) ? hij_any_f32(ints, dJ, dI) : hij_any_f32(ints, dI, dJ);
+      const float hv = ham_element_f32(ints.I1f, ints.I2f, ints.norb, dI, dJ, J < I);
 #pragma unroll
       for (int r = 0; r < K; ++r) acc_add(a32[r], hv, x[(size_t)J * K + r]);
     } else {
-      const double hv = (J < I) ? hij_any(ints, dJ, dI) : hij_any(ints, dI, dJ);
+      const double hv = ham_element(ints.I1, ints.I2, ints.norb, dI, dJ, J < I);
 #pragma unroll
       for (int r = 0; r < K; ++r) a64[r] += hv * x[(size_t)J * K + r];
     }
   }
-  // out of line for the same reason as EmitVisitor::drain
-  __device__ __noinline__ int drain(uint32_t* q, int n, int cnt) {
+  __device__ int drain(uint32_t* q, int n, int cnt) {
     const int lane = threadIdx.x & 31;
     if (lane < cnt) add(q[lane]);
     __syncwarp();

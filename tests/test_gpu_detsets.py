@@ -73,7 +73,7 @@ def test_fp64_gpu_determinant_sets_equal_the_oracle(tmp_path, name, sched, maxit
     assert np.max(np.abs(got["E"] - ref.E)) < 1e-9, (got["E"], ref.E)
 
 
-def test_config1_hubbard_ring_stated_schedule_all_paths(tmp_path):
+def test_hubbard_ring_stated_schedule_all_paths(tmp_path):
     """The 12-site Hubbard ring (t = 1, U = 4, 6a + 6b) at its stated
     schedule (1e-3 for three iterations, then 1e-4, maxiter 6) on the GPU's
     FP64, mixed and matrix-free paths against the oracle: identical

@@ -201,6 +201,36 @@ def test_incremental_hamiltonian_equals_full_build(gpu, golden, mode):
     assert np.array_equal(rp, rp2) and np.array_equal(col, col2) and np.array_equal(val, val2)
 
 
+@pytest.mark.parametrize("mode", ["fp64", "mixed"])
+def test_small_and_large_increments_equal_full_build(gpu, golden, mode):
+    """Appending determinants to a space with a stored H extends it in place
+    (new rows, new columns of the old rows, merge in the new storage order),
+    whether the increment is small or many times the old space; either result
+    equals a from-scratch build of the whole space, element by element."""
+    from dice_gb300.shard import ref_order
+    inp = golden("h8_631g", "dice.dat")
+    gpu.run_input(inp, mode=mode)
+    dets = gpu.dets()
+    N = len(dets)
+    bounds = [int(b) for b in gpu.run_log()["ndets"] if 1 < b < N]
+    small = max(b for b in bounds if N - b <= b)
+    large = min(bounds)
+    assert N - large > large
+    for b in (small, large):
+        tail = dets[b:][ref_order(dets[b:])]  # an appended batch is sorted
+        gpu.set_dets(np.concatenate([dets[:b], tail]))
+        nnz_full = gpu.ham_build(mode)
+        full = gpu.ham_export(nnz_full)
+        gpu.set_dets(dets[:b])
+        gpu.ham_build(mode)
+        gpu.append_dets(tail)
+        nnz = gpu.ham_build(mode)
+        got = gpu.ham_export(nnz)
+        assert nnz == nnz_full, b
+        for a, c in zip(got, full):
+            assert np.array_equal(a, c), b
+
+
 def test_h8_end_to_end_mixed_within_1uha(gpu, golden):
     inp = golden("h8_631g", "dice.dat")
     E = gpu.run_input(inp, mode="mixed")
