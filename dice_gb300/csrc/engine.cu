@@ -150,6 +150,35 @@ struct IterLog {
   double seconds;
 };
 
+// The terms of Hij_1Excite (SHCI/Determinants.cpp:437-469) for every
+// spin-orbital pair (a, i) of one spin s and spin orbital j, laid out as
+// IntsView::V1 reads them: (ai|jj) - (aj|ji) when j has spin s, (ai|jj)
+// otherwise; FP64 (the difference hij_single adds) and FP32 (the FP32 copies'
+// difference hij_single_f32 adds), so the table sums are bit-identical.
+static void single_terms(const HostInts& h, std::vector<double>& v1, std::vector<float>& v1f) {
+  const int n = h.norb, n2 = 2 * n;
+  auto pair = [](size_t p, size_t q) { return p > q ? p * (p + 1) / 2 + q : q * (q + 1) / 2 + p; };
+  auto i2 = [&](int i, int j, int k, int l) { return h.I2[pair(pair(i, j), pair(k, l))]; };
+  v1.assign((size_t)2 * n * n * n2, 0.0);
+  v1f.assign(v1.size(), 0.f);
+  for (int sp = 0; sp < 2; ++sp)
+    for (int a = 0; a < n; ++a)
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n2; ++j) {
+          const size_t t = (((size_t)sp * n + a) * n + i) * n2 + j;
+          const int jp = j >> 1;
+          const double d = i2(a, i, jp, jp);
+          if ((j & 1) == sp) {
+            const double x = i2(a, jp, jp, i);
+            v1[t] = d - x;
+            v1f[t] = (float)d - (float)x;
+          } else {
+            v1[t] = d;
+            v1f[t] = (float)d;
+          }
+        }
+}
+
 struct Context {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -160,6 +189,8 @@ struct Context {
   bool have_ints = false;
   DevBuf<double> dI1, dI2, dDirect, dExchange, dSingles;
   DevBuf<float> dI1f, dI2f;  // FP32 copies for the FP32 matrix-free sigma
+  DevBuf<double> dV1;        // terms of Hij_1Excite per (a, i, j) (IntsView::V1)
+  DevBuf<float> dV1f;
   DevBuf<float> dSameVal, dOppVal;
   DevBuf<int16_t> dSamePairs, dOppPairs;
   DevBuf<int64_t> dSameStart, dOppStart;
@@ -313,7 +344,9 @@ struct Context {
     if (stream) cudaStreamDestroy(stream);
   }
 
-  IntsView ints() const { return IntsView{dI1.p, dI2.p, dDirect.p, dExchange.p, hints.norb, dI1f.p, dI2f.p}; }
+  IntsView ints() const {
+    return IntsView{dI1.p, dI2.p, dDirect.p, dExchange.p, hints.norb, dI1f.p, dI2f.p, dV1.p, dV1f.p};
+  }
   HeatBathView hb() const {
     return HeatBathView{dSameVal.p, dSamePairs.p, dSameStart.p, dOppVal.p, dOppPairs.p, dOppStart.p, dSingles.p};
   }
@@ -344,6 +377,11 @@ struct Context {
       const std::vector<float> f1(hints.I1.begin(), hints.I1.end()), f2(hints.I2.begin(), hints.I2.end());
       upload(dI1f, f1);
       upload(dI2f, f2);
+      std::vector<double> v1;
+      std::vector<float> v1f;
+      single_terms(hints, v1, v1f);
+      upload(dV1, v1);
+      upload(dV1f, v1f);
       SHCI_CUDA(cudaStreamSynchronize(stream));  // the host copies go out of scope
     }
     upload(dDirect, hints.Direct);

@@ -555,14 +555,14 @@ __global__ void k_ham_count(HelperView h, int64_t row0, int64_t nr, const uint32
 // copied into each caused instruction-cache misses, while an out-of-line
 // member taking the visitor by address kept the visitor's state (queue
 // counts, accumulators, output position) in local memory.
-__device__ __noinline__ double ham_element(const double* I1, const double* I2, int norb, Det2 dI, Det2 dJ,
-                                           bool j_below) {
-  const IntsView iv{I1, I2, nullptr, nullptr, norb, nullptr, nullptr};
+__device__ __noinline__ double ham_element(const double* I1, const double* I2, const double* V1, int norb, Det2 dI,
+                                           Det2 dJ, bool j_below) {
+  const IntsView iv{I1, I2, nullptr, nullptr, norb, nullptr, nullptr, V1, nullptr};
   return j_below ? hij_any(iv, dJ, dI) : hij_any(iv, dI, dJ);
 }
-__device__ __noinline__ float ham_element_f32(const float* I1f, const float* I2f, int norb, Det2 dI, Det2 dJ,
-                                              bool j_below) {
-  const IntsView iv{nullptr, nullptr, nullptr, nullptr, norb, I1f, I2f};
+__device__ __noinline__ float ham_element_f32(const float* I1f, const float* I2f, const float* V1f, int norb,
+                                              Det2 dI, Det2 dJ, bool j_below) {
+  const IntsView iv{nullptr, nullptr, nullptr, nullptr, norb, I1f, I2f, nullptr, V1f};
   return j_below ? hij_any_f32(iv, dJ, dI) : hij_any_f32(iv, dI, dJ);
 }
 
@@ -588,7 +588,7 @@ struct EmitVisitor {
   int ns, nd;
 
   __device__ void store(int64_t q, uint32_t J) {
-    const double hv = ham_element(ints.I1, ints.I2, ints.norb, dI, dets[J], J < I);
+    const double hv = ham_element(ints.I1, ints.I2, ints.V1, ints.norb, dI, dets[J], J < I);
     col[q] = (int32_t)cmap[J];
     if (v64) v64[q] = hv;
     if (vhi) {
@@ -1402,11 +1402,11 @@ struct DirectQVisitor {
   __device__ void add(uint32_t J) {
     const Det2 dJ = dets[J];
     if constexpr (F32) {
-      const float hv = ham_element_f32(ints.I1f, ints.I2f, ints.norb, dI, dJ, J < I);
+      const float hv = ham_element_f32(ints.I1f, ints.I2f, ints.V1f, ints.norb, dI, dJ, J < I);
 #pragma unroll
       for (int r = 0; r < K; ++r) acc_add(a32[r], hv, x[(size_t)J * K + r]);
     } else {
-      const double hv = ham_element(ints.I1, ints.I2, ints.norb, dI, dJ, J < I);
+      const double hv = ham_element(ints.I1, ints.I2, ints.V1, ints.norb, dI, dJ, J < I);
 #pragma unroll
       for (int r = 0; r < K; ++r) a64[r] += hv * x[(size_t)J * K + r];
     }

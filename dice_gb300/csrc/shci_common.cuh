@@ -107,6 +107,12 @@ struct IntsView {
   int norb;
   const float* I1f;  // FP32 copies for the FP32 matrix-free sigma
   const float* I2f;
+  // Terms of Hij_1Excite per spin-orbital pair (a, i) of one spin s and
+  // occupied spin orbital j, at [((s n + a/2) n + i/2) 2n + j]:
+  // (ai|jj) - (aj|ji) for j of spin s, (ai|jj) otherwise, each the FP64
+  // difference the sum adds (V1) and its FP32 counterpart (V1f). Optional.
+  const double* V1;
+  const float* V1f;
 };
 
 __device__ __forceinline__ int pair_index(int i, int j) {
@@ -132,6 +138,20 @@ __device__ __forceinline__ double i2_spin(const double* __restrict__ I2, int i, 
 __device__ inline double hij_single(const IntsView& I, const Det2& ket, int a, int i) {
   const int n2 = 2 * I.norb;
   double energy = __ldg(I.I1 + (size_t)a * n2 + i);
+  if (I.V1) {  // the same terms, read from the table, summed in the same order
+    const double* v = I.V1 + ((size_t)((a & 1) * I.norb + (a >> 1)) * I.norb + (i >> 1)) * n2;
+#pragma unroll 1
+    for (int w = 0; w < 2; ++w) {
+      uint64_t bits = w ? ket.w1 : ket.w0;
+      while (bits) {
+        const int j = __ffsll((long long)bits) - 1 + 64 * w;
+        bits &= bits - 1;
+        energy = __dadd_rn(energy, __ldg(v + j));
+      }
+    }
+    const int lo = a < i ? a : i, hi = a < i ? i : a;
+    return (occ_between(ket, lo, hi) & 1) ? -energy : energy;
+  }
   const int sa = a & 1;
   const int ai = pair_index(a >> 1, i >> 1);
 #pragma unroll 1
@@ -193,6 +213,20 @@ __device__ __forceinline__ float i2f_spatial(const float* __restrict__ I2f, int 
 __device__ inline float hij_single_f32(const IntsView& I, const Det2& ket, int a, int i) {
   const int n2 = 2 * I.norb;
   float energy = __ldg(I.I1f + (size_t)a * n2 + i);
+  if (I.V1f) {
+    const float* v = I.V1f + ((size_t)((a & 1) * I.norb + (a >> 1)) * I.norb + (i >> 1)) * n2;
+#pragma unroll 1
+    for (int w = 0; w < 2; ++w) {
+      uint64_t bits = w ? ket.w1 : ket.w0;
+      while (bits) {
+        const int j = __ffsll((long long)bits) - 1 + 64 * w;
+        bits &= bits - 1;
+        energy += __ldg(v + j);
+      }
+    }
+    const int lo = a < i ? a : i, hi = a < i ? i : a;
+    return (occ_between(ket, lo, hi) & 1) ? -energy : energy;
+  }
   const int sa = a & 1;
   const int ai = pair_index(a >> 1, i >> 1);
 #pragma unroll 1
