@@ -19,6 +19,9 @@ struct HelperView {
   const uint64_t* bGroupA;  // BetaMajorToAlpha
   const int64_t* aSingStart;  // SinglesFromAlpha as CSR over alpha groups
   const uint32_t* aSing;
+  // the list of alpha group g holds its small groups (a few times n_beta
+  // determinants at most) in [aSingStart[g], aSingMid[g]), then the large ones
+  const int64_t* aSingMid;
   // partial-string index: one 16-byte entry per (determinant J, occupied
   // beta orbital b of J): {beta string of J without b (low, high word),
   // alpha group of J | b << 26, J}, sorted by (alpha group, partial string),
@@ -40,7 +43,7 @@ struct Helpers {
   int64_t NA = 0, NB = 0, nsing = 0;
   DevBuf<uint64_t> astr, bstr, ua, ub, aGroupB, bGroupA;
   DevBuf<uint32_t> aidx, bidx, aDets, bDets, aSing;
-  DevBuf<int64_t> aStart, bStart, aSingStart;
+  DevBuf<int64_t> aStart, bStart, aSingStart, aSingMid;
   DevBuf<uint4> m1ent;
   DevBuf<uint2> m1tab;
   DevBuf<uint64_t> m1dir;
@@ -48,13 +51,13 @@ struct Helpers {
   void build(const Det2* dets, size_t n, int norb, Prims& pr, cudaStream_t s);
   HelperView view() const {
     return HelperView{N,         astr.p,      bstr.p,  aidx.p,  bidx.p,  aStart.p, aDets.p,
-                      aGroupB.p, bStart.p,    bDets.p, bGroupA.p, aSingStart.p, aSing.p,
+                      aGroupB.p, bStart.p,    bDets.p, bGroupA.p, aSingStart.p, aSing.p, aSingMid.p,
                       nm1 > 0 ? m1ent.p : nullptr, m1tab.p, m1dir.p};
   }
   size_t bytes() const {
     return astr.bytes() + bstr.bytes() + ua.bytes() + ub.bytes() + aGroupB.bytes() + bGroupA.bytes() +
            aidx.bytes() + bidx.bytes() + aDets.bytes() + bDets.bytes() + aSing.bytes() + aStart.bytes() +
-           bStart.bytes() + aSingStart.bytes() + m1ent.bytes() + m1tab.bytes() + m1dir.bytes();
+           bStart.bytes() + aSingStart.bytes() + aSingMid.bytes() + m1ent.bytes() + m1tab.bytes() + m1dir.bytes();
   }
 };
 

@@ -268,6 +268,7 @@ __global__ void __launch_bounds__(1024) k_sigma_mixed16(const int64_t* __restric
 
 // ---- building the 16-bit-delta copy ----------------------------------------
 // bridges needed before entry p of its row: (gap - 1) / 65535 for a gap >= 65536
+// (columns fit 31 bits, so gaps are 32-bit; the division runs only for those)
 __global__ void k_c_count(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col, size_t N,
                           int64_t* __restrict__ len) {
   const int lane = threadIdx.x & 31;
@@ -275,7 +276,10 @@ __global__ void k_c_count(const int64_t* __restrict__ rowptr, const int32_t* __r
   for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < (int64_t)N; r += warps) {
     const int64_t p0 = rowptr[r], p1 = rowptr[r + 1];
     int64_t b = 0;
-    for (int64_t p = p0 + 1 + lane; p < p1; p += 32) b += ((int64_t)col[p] - col[p - 1] - 1) / 65535;
+    for (int64_t p = p0 + 1 + lane; p < p1; p += 32) {
+      const uint32_t gap = (uint32_t)(col[p] - col[p - 1]);  // >= 1: columns ascend
+      if (gap > 65535u) b += (gap - 1u) / 65535u;             // rare: divide only there
+    }
 #pragma unroll
     for (int o = 16; o; o >>= 1) b += __shfl_xor_sync(kFull, b, o);
     if (lane == 0) len[r] = ((p1 - p0) + b + 3) & ~(int64_t)3;  // padded to a multiple of four
@@ -292,24 +296,24 @@ __global__ void k_c_fill(const int64_t* __restrict__ rowptr, const int32_t* __re
     int64_t out0 = crow[r];  // output position of this chunk's first item
     for (int64_t q = p0; q < p1; q += 32) {
       const int64_t p = q + lane;
-      int64_t gap = 0, nb = 0;
+      uint32_t gap = 0, nb = 0;  // a gap needs (gap - 1) / 65535 bridges, none below 65536
       if (p < p1) {
-        gap = p > p0 ? (int64_t)col[p] - col[p - 1] : 0;
-        nb = gap > 0 ? (gap - 1) / 65535 : 0;
+        gap = p > p0 ? (uint32_t)(col[p] - col[p - 1]) : 0u;
+        nb = gap > 65535u ? (gap - 1u) / 65535u : 0u;
       }
-      int64_t incl = (p < p1 ? 1 : 0) + nb;  // items this lane writes (bridges + the entry)
+      int incl = (p < p1 ? 1 : 0) + (int)nb;  // items this lane writes (bridges + the entry)
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
-        const int64_t t = __shfl_up_sync(kFull, incl, o);
+        const int t = __shfl_up_sync(kFull, incl, o);
         if (lane >= o) incl += t;
       }
       if (p < p1) {
-        int64_t o = out0 + incl - 1 - nb;
-        for (int64_t t = 0; t < nb; ++t, ++o) {
+        int64_t o = out0 + incl - 1 - (int64_t)nb;
+        for (uint32_t t = 0; t < nb; ++t, ++o) {
           cdel[o] = 65535;
           cval[o] = 0.f;
         }
-        cdel[o] = (uint16_t)(gap - nb * 65535);
+        cdel[o] = (uint16_t)(gap - nb * 65535u);
         cval[o] = vhi[p];
       }
       out0 += __shfl_sync(kFull, incl, 31);
