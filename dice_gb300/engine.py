@@ -295,6 +295,12 @@ class Engine:
         self._check(load_library().shci_sigma(self.h, MODES.get(mode, mode), _p(xx), _p(y), xx.shape[0]))
         return y[0] if one else y
 
+    def sigma_host(self, x_ptr, y_ptr, k, mode="fp64"):
+        """shci_sigma on caller-owned host buffers (ints: addresses of k x N
+        FP64 arrays, row-major by vector), e.g. pinned memory."""
+        self._check(load_library().shci_sigma(self.h, MODES.get(mode, mode), ctypes.c_void_p(x_ptr),
+                                              ctypes.c_void_p(y_ptr), k))
+
     def sigma_device(self, x_ptr, y_ptr, k, ld, mode="fp64"):
         """Device pointers (ints): column-major x, y with leading dimension ld."""
         self._check(load_library().shci_sigma_device(self.h, MODES.get(mode, mode), ctypes.c_void_p(x_ptr),
