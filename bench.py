@@ -723,6 +723,43 @@ def run_ham_only(args):
         print(json.dumps(out), flush=True)
 
 
+def run_large(args):
+    """--section large: the mol36 workload (n=36, 14a+14b, 4 roots, block
+    Davidson) at millions of determinants (5.8 M at eps1 3e-4; 2e-4 selects
+    24.6 M), run with the matrix-free sigma in FP64 (the reference's
+    DirectDavidson path): eps1 1e-3 twice, then 3e-4, final solve to 1e-6.
+    Prints the determinant counts, per-root energies, stage times and the
+    sigma throughput. Takes minutes."""
+    import torch
+    from dice_gb300 import engine as eng, synthetic
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    work = tempfile.mkdtemp()
+    inp = synthetic.make_workload("mol36", work, schedule=[(0, 1e-3), (2, 3e-4)], maxiter=3,
+                                  extra=("davidsonTol 1e-6", "DirectDavidson"))
+    e = eng.Engine(local)
+    t0 = time.perf_counter()
+    E = e.run_input(inp, mode="fp64", block=True)
+    wall = time.perf_counter() - t0
+    t, st, lg = e.timings(), e.run_stats(), e.run_log()
+    N = e.ndets()
+    x = np.random.default_rng(2).standard_normal((4, N))
+    e.sigma(x, "direct")
+    ts = []
+    for _ in range(2):
+        a = time.perf_counter()
+        e.sigma(x, "direct")
+        ts.append(time.perf_counter() - a)
+    e.close()
+    out = {"workload": "mol36 (n=36, 14a+14b, rank-108 ERIs), 4 roots, block Davidson, matrix-free FP64 sigma, "
+                       "eps1 1e-3 x2 -> 3e-4, final solve 1e-6",
+           "n_dets": N, "ndets": [int(v) for v in lg["ndets"]], "E_var": [float(v) for v in E], "wall_s": wall,
+           "stages_s": t, "davidson_iters": int(st["davidson_iters"]), "sigma_k4_s": statistics.median(ts),
+           "mdets_s": 4 * N / statistics.median(ts) / 1e6}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
 def run_direct_only(args):
     """--section direct: the matrix-free sigma timed alone. The space is the
     mol36 workload's (n=36, 14a+14b, rank-108 ERIs, seed 20260002) after
@@ -770,11 +807,12 @@ def main():
     ap.add_argument("--no-configs", action="store_true", help="skip the other workloads (mol36, mol64, mol50)")
     ap.add_argument("--case", default="full", choices=["full", "medium", "small"],
                     help="small: the profiling case (two eps1 = 1e-3 iterations)")
-    ap.add_argument("--section", default="all", choices=["all", "pt", "sigma", "direct", "ham"],
+    ap.add_argument("--section", default="all", choices=["all", "pt", "sigma", "direct", "ham", "large"],
                     help="pt: only the variational run and the timed perturbative stage; sigma: only the FP64 run "
                          "and the stored sigmas (FP64 k=1, mixed k=4, mixed k=1) timed on its space; direct: the "
                          "matrix-free sigma (k=4, FP32 and FP64) on mol36 (n=36, 14a+14b); ham: the FP64 run, "
-                         "then its Hamiltonian built from scratch (FP64 and mixed)")
+                         "then its Hamiltonian built from scratch (FP64 and mixed); large: mol36 with 4 roots at 5.8 M "
+                         "determinants, matrix-free (minutes)")
     ap.add_argument("--pt-eps2", type=float, default=PT_EPS2)
     args = ap.parse_args()
     if args.warmup < 3:
@@ -787,6 +825,8 @@ def main():
         run_sigma_only(args)
     elif args.section == "ham":
         run_ham_only(args)
+    elif args.section == "large":
+        run_large(args)
     elif args.section == "direct":
         run_direct_only(args)
     else:
