@@ -469,6 +469,25 @@ def test_mixed_single_vector_sigma_on_large_space(tmp_path):
     e.close()
 
 
+def test_sigma_on_pinned_host_buffers_equals_sigma(tmp_path):
+    """shci_sigma on caller-owned page-locked host buffers (the bench's e2e
+    call) returns what it returns on pageable arrays, bit for bit."""
+    import torch
+    inp = synthetic.make_workload("mol24", str(tmp_path / "w"), schedule=[(0, 3e-3)], maxiter=2)
+    e = eng.Engine(0)
+    e.run_input(inp, mode="mixed")
+    n = e.ndets()
+    e.ham_build("mixed")
+    x = np.random.default_rng(9).standard_normal((2, n))
+    for k in (1, 2):
+        xp = torch.tensor(x[:k]).pin_memory()
+        yp = torch.full((k, n), float("nan"), dtype=torch.float64).pin_memory()
+        for mode in ("mixed", "fp64"):
+            e.sigma_host(xp.data_ptr(), yp.data_ptr(), k, mode)
+            assert np.array_equal(yp.numpy(), e.sigma(x[:k], mode)), (k, mode)
+    e.close()
+
+
 @pytest.mark.parametrize("mode,kps", [("mixed", (1, 2, 4)), ("fp64", (1, 2, 4))])
 def test_packed_sigma_equals_device_sigma(tmp_path, mode, kps):
     """shci_sigma_packed_device (the bench's timed call: x already packed
