@@ -15,8 +15,9 @@
 //      contains the partial string B - b for some occupied b of B, so it is
 //      found by looking up the keys (As, B - b) in the partial-string index
 //      (a hash table per alpha group As gives each key's run of entries):
-//      |singles(A)| x |B| probes that return (nearly) only connections,
-//      instead of a scan over every determinant of every group As;
+//      |B| probes per group As that return (nearly) only connections,
+//      instead of a scan over every determinant of the group -- except for
+//      groups of at most a few times |B| determinants, which are scanned;
 //   3. determinants sharing I's beta string: alpha distance 2 (scan of the
 //      beta group).
 // This visits the same (I, J) set as the reference's five helper-list classes
