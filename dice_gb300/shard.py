@@ -23,16 +23,23 @@ rank computes its rows of y from the whole x and the rows are all-gathered,
 so every rank ends with the whole y -- bit for bit what one process computes,
 because each row is summed over the same entries in the same order.
 
+Davidson (SHCI/Davidson.cpp:111-348): the small Rayleigh matrices, the
+basis rotations and the corrections are replicated on every rank (the same
+numpy operations on the same data, so every rank holds the same basis); only
+sigma is sharded. variational() runs the eps1 schedule of DoVariational with
+these three steps.
+
 The per-rank work goes through a backend with the engine's methods
 (dice_gb300.engine.Engine on a GPU):
     select_candidates(cmax, eps1, rank, world) -> (n, 2) uint64
     append_dets(dets)
     ham_build_rows(r0, r1, mode) -> nnz
     sigma(x, mode) -> y   (only the rows [r0, r1) of y are meaningful)
+    diag() -> (n,) diagonal energies
 """
 import numpy as np
 
-__all__ = ["row_block", "owner_of", "ref_order", "select", "sigma", "Comm"]
+__all__ = ["row_block", "owner_of", "ref_order", "select", "sigma", "davidson", "variational", "Comm"]
 
 
 def row_block(n, rank, world):
@@ -146,3 +153,87 @@ def sigma(backend, comm, x, n, mode="fp64"):
     # rank-order concatenation equal to the row order)
     out = np.stack([comm.all_gather_var(rows[c], np.float64) for c in range(rows.shape[0])])
     return out.reshape(y.shape)
+
+
+def davidson(backend, comm, n, diag, x0, tol, max_copies=None, mode="fp64", max_iter=None):
+    """Lowest eigenpairs of the whole Hamiltonian, the rows of which are
+    spread over the ranks (built with backend.ham_build_rows), by the
+    reference's Davidson scheme (SHCI/Davidson.cpp:111-348): the basis is
+    rotated to the Ritz vectors every iteration, the roots converge in order
+    (residual norm below tol), the correction is the residual divided by
+    (theta - H_ii) (1e-12 guard, :85-106), projected out of the basis and
+    normalised, and a full basis of max_copies vectors collapses to nroots + 2
+    Ritz vectors plus the new correction. x0: (nroots, n) start vectors, each
+    with a nonzero norm. Returns (energies, vectors, iterations); raises
+    RuntimeError past the reference's iteration cap (2000 per root)."""
+    x0 = np.atleast_2d(np.asarray(x0, dtype=np.float64))
+    nroots = x0.shape[0]
+    max_copies = max_copies or nroots + 4
+    max_iter = max_iter or 2000 * nroots
+    diag = np.asarray(diag, dtype=np.float64)
+    b = np.zeros((max_copies, n))
+    sig = np.zeros((max_copies, n))
+    for i in range(nroots):  # Gram-Schmidt of the start vectors
+        v = x0[i] - b[:i].T @ (b[:i] @ x0[i]) if i else x0[i].copy()
+        b[i] = v / np.linalg.norm(v)
+    done, bsize, conv, it = 0, nroots, 0, 0
+    while True:
+        if done < bsize:
+            sig[done:bsize] = sigma(backend, comm, b[done:bsize], n, mode)
+            done = bsize
+        hs = b[:bsize] @ sig[:bsize].T
+        hs = 0.5 * (hs + hs.T)
+        ev, vec = np.linalg.eigh(hs)
+        b[:bsize] = vec.T @ b[:bsize]
+        sig[:bsize] = vec.T @ sig[:bsize]
+        for i in range(conv):  # an earlier root that drifted out of tolerance is taken up again
+            if np.linalg.norm(sig[i] - ev[i] * b[i]) > tol:
+                conv = i
+                break
+        r = sig[conv] - ev[conv] * b[conv]
+        it += 1
+        if bsize == n:
+            return ev[:nroots].copy(), b[:nroots].copy(), it
+        if np.linalg.norm(r) < tol:
+            conv += 1
+            if conv == nroots:
+                return ev[:nroots].copy(), b[:nroots].copy(), it
+            continue
+        if it > max_iter:
+            raise RuntimeError("Davidson did not converge in %d iterations" % max_iter)
+        den = ev[conv] - diag
+        den = np.where(np.abs(den) > 1e-12, den, den - 1e-12)
+        r = r / den
+        for i in range(bsize):
+            r -= (b[i] @ r) / (b[i] @ b[i]) * b[i]
+        r /= np.linalg.norm(r)
+        if bsize < max_copies:
+            b[bsize] = r
+            bsize += 1
+        else:  # keep nroots + 2 Ritz vectors (their sigmas too), add the correction
+            bsize, done = nroots + 3, nroots + 2
+            b[bsize - 1] = r
+
+
+def variational(backend, comm, schedule, x0, tol_loose=5e-5, tol=1e-8, mode="fp64"):
+    """The eps1 schedule of DoVariational (SHCI/SHCIbasics.cpp:783-1378) on
+    the ranks: for each eps1, the Hamiltonian rows of the rank's block, a
+    Davidson solve to tol_loose, and a sharded selection with cMax = max over
+    roots |c_i|; after the last selection a solve to tol. x0: (nroots, n) start
+    vectors on the backend's initial space. Returns (energies, vectors,
+    determinant counts after each selection)."""
+    x = np.atleast_2d(np.asarray(x0, dtype=np.float64))
+    counts = []
+    for eps1 in schedule:
+        n = len(x[0])
+        r0, r1 = row_block(n, comm.rank, comm.world)
+        backend.ham_build_rows(r0, r1, mode)
+        _, x, _ = davidson(backend, comm, n, backend.diag(), x, tol_loose, mode=mode)
+        added = select(backend, comm, np.max(np.abs(x), axis=0), eps1)
+        x = np.concatenate([x, np.zeros((x.shape[0], added))], axis=1)
+        counts.append(n + added)
+    n = len(x[0])
+    r0, r1 = row_block(n, comm.rank, comm.world)
+    backend.ham_build_rows(r0, r1, mode)
+    e, x, _ = davidson(backend, comm, n, backend.diag(), x, tol, mode=mode)
+    return e, x, counts

@@ -47,7 +47,11 @@ class OracleBackend:
         full.sort_indices()
         self.r0, self.r1 = r0, r1
         self.rows = full[r0:r1]
+        self.full_diag = full.diagonal()
         return self.rows.nnz
+
+    def diag(self):
+        return self.full_diag.copy()
 
     def sigma(self, x, mode="fp64"):
         x = np.atleast_2d(x)
@@ -84,6 +88,28 @@ def _run(backend, comm, steps):
     backend.ham_build_rows(r0, r1)
     x = np.random.default_rng(7).standard_normal((2, n))
     return backend.dets.copy(), shard.sigma(backend, comm, x, n)
+
+
+def _run_variational(backend, comm, steps):
+    """The whole sharded loop: Davidson on the ranks' row blocks, sharded
+    selection, and a final tight solve."""
+    _, w = _h8_start()
+    e, x, counts = shard.variational(backend, comm, steps, w.reshape(1, -1), tol_loose=1e-6, tol=1e-9)
+    return backend.dets.copy(), e, x, np.array(counts)
+
+
+def _worker_var(rank, world, port, tmp, steps):
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        dets, _ = _h8_start()
+        backend = OracleBackend(_fcidump(os.path.join(tmp, "v%d" % rank)), dets)
+        d, e, x, counts = _run_variational(backend, shard.Comm("cpu"), steps)
+        np.savez(os.path.join(tmp, "var%d.npz" % rank), dets=d, e=e, x=x, counts=counts)
+    finally:
+        dist.destroy_process_group()
 
 
 def _worker(rank, world, port, tmp, steps):
@@ -141,3 +167,33 @@ def test_owner_partition_and_reference_order():
     hi, lo = o[:, 1].view(np.int64), o[:, 0].view(np.int64)
     assert np.all((hi[1:] > hi[:-1]) | ((hi[1:] == hi[:-1]) & (lo[1:] >= lo[:-1])))
     assert [shard.row_block(10, r, 3) for r in range(3)] == [(0, 3), (3, 6), (6, 10)]
+
+
+def test_two_rank_variational_loop_equals_one_process(tmp_path):
+    """shard.variational on two gloo ranks (Davidson replicated, sigma and
+    selection sharded) selects the one-process run's determinants in the same
+    order and converges to the same energy, which is the lowest eigenvalue of
+    the final space's Hamiltonian."""
+    import scipy.sparse.linalg as sla
+    import torch.multiprocessing as mp
+    steps = (1e-4, 1e-6)
+    for r in range(2):
+        os.makedirs(tmp_path / ("v%d" % r))
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    mp.start_processes(_worker_var, args=(2, port, str(tmp_path), steps), nprocs=2, join=True, start_method="spawn")
+    os.makedirs(tmp_path / "one")
+    dets, _ = _h8_start()
+    one = OracleBackend(_fcidump(str(tmp_path / "one")), dets)
+    ref_dets, ref_e, ref_x, ref_counts = _run_variational(one, _OneRank(), steps)
+    assert len(ref_dets) > 1500
+    one.ham_build_rows(0, len(ref_dets))
+    lowest = sla.eigsh(one.rows, k=1, which="SA", tol=1e-12)[0][0]
+    assert abs(ref_e[0] - lowest) < 1e-8
+    for r in range(2):
+        got = np.load(tmp_path / ("var%d.npz" % r))
+        assert np.array_equal(got["dets"], ref_dets), r
+        assert np.array_equal(got["counts"], ref_counts), r
+        assert abs(got["e"][0] - ref_e[0]) < 1e-10, r
