@@ -95,3 +95,24 @@ def test_row_block_sigma_equals_whole_matrix(tmp_path, mode):
         e.close()
     assert np.array_equal(got1, want1)
     assert np.array_equal(got2, want2)
+
+
+def test_sharded_loop_on_the_engine_matches_the_oracle_backend(tmp_path):
+    """shard.variational with an Engine as the rank's backend (one rank, the
+    whole space as its row block) selects the determinants the same loop
+    selects with the CPU oracle as the backend, in the same order, and
+    reaches the same energy."""
+    from test_shard_gloo import OracleBackend, _OneRank, _fcidump, _h8_start
+    dets, w = _h8_start()
+    steps = (1e-4, 1e-6)
+    ob = OracleBackend(_fcidump(str(tmp_path)), dets)
+    e_ref, _, counts_ref = shard.variational(ob, _OneRank(), steps, w.reshape(1, -1), tol_loose=1e-6, tol=1e-9)
+    e = eng.Engine(0)
+    e.read_fcidump(str(tmp_path / "FCIDUMP"))
+    e.set_selection_params(ncore=0, nact=8)  # the h8 example's active space, as the oracle backend selects
+    e.set_dets(dets)
+    en, _, counts = shard.variational(e, _OneRank(), steps, w.reshape(1, -1), tol_loose=1e-6, tol=1e-9)
+    assert counts == counts_ref
+    assert np.array_equal(e.dets(), ob.dets)
+    assert abs(en[0] - e_ref[0]) < 1e-10
+    e.close()
