@@ -169,21 +169,24 @@ def test_owner_partition_and_reference_order():
     assert [shard.row_block(10, r, 3) for r in range(3)] == [(0, 3), (3, 6), (6, 10)]
 
 
-def test_two_rank_variational_loop_equals_one_process(tmp_path):
-    """shard.variational on two gloo ranks (Davidson replicated, sigma and
-    selection sharded) selects the one-process run's determinants in the same
-    order and converges to the same energy, which is the lowest eigenvalue of
-    the final space's Hamiltonian."""
+@pytest.mark.parametrize("world", [2, 3])
+def test_sharded_variational_loop_equals_one_process(tmp_path, world):
+    """shard.variational on gloo ranks (Davidson replicated, sigma and
+    selection sharded; three ranks split rows and parents unevenly) selects
+    the one-process run's determinants in the same order and converges to the
+    same energy, which is the lowest eigenvalue of the final space's
+    Hamiltonian."""
     import scipy.sparse.linalg as sla
     import torch.multiprocessing as mp
     steps = (1e-4, 1e-6)
-    for r in range(2):
+    for r in range(world):
         os.makedirs(tmp_path / ("v%d" % r))
     s = socket.socket()
     s.bind(("127.0.0.1", 0))
     port = s.getsockname()[1]
     s.close()
-    mp.start_processes(_worker_var, args=(2, port, str(tmp_path), steps), nprocs=2, join=True, start_method="spawn")
+    mp.start_processes(_worker_var, args=(world, port, str(tmp_path), steps), nprocs=world, join=True,
+                       start_method="spawn")
     os.makedirs(tmp_path / "one")
     dets, _ = _h8_start()
     one = OracleBackend(_fcidump(str(tmp_path / "one")), dets)
@@ -192,7 +195,7 @@ def test_two_rank_variational_loop_equals_one_process(tmp_path):
     one.ham_build_rows(0, len(ref_dets))
     lowest = sla.eigsh(one.rows, k=1, which="SA", tol=1e-12)[0][0]
     assert abs(ref_e[0] - lowest) < 1e-8
-    for r in range(2):
+    for r in range(world):
         got = np.load(tmp_path / ("var%d.npz" % r))
         assert np.array_equal(got["dets"], ref_dets), r
         assert np.array_equal(got["counts"], ref_counts), r
